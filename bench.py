@@ -1,0 +1,291 @@
+"""Benchmark of the covariation path on one synthetic rRNA-scale alignment.
+
+Workload (one step): an N=2,000 x L=3,000 synthetic RNA alignment (coalescent
+tree of leaf-to-root length 2.0, 900 planted base pairs in 40 helices of 8-35
+pairs, 15% gaps, position-based weights, R-scape's 0.75 gap-column filter),
+its 20 null alignments (Fitch ancestors + shuffled substitutions on the same
+tree), GTp, MIp, CHIp and RAFp scores with APC for all 21 alignments, the
+null histogram and tail fit of each statistic, and the E-values and
+E < 0.05 pair list of the input alignment.
+
+  value  column pairs scored per second (21 alignments x L(L-1)/2 pairs per
+         step, every pair scored with the four statistics), alignment and
+         weights resident on the device, timed with CUDA events on the
+         library's stream;
+  e2e    the same through the public call with host buffers: the alignment
+         and weights copied in and the hit lists copied out in every step.
+
+--impl reference times the reference algorithm on the host cores instead:
+R-scape's per-pair counting loop (corr_NaivePP -> mutual_naive_ppij, then
+the statistic) and its O(N^2) RAF loop, FP64, on a bounded sample of the
+same pairs, one run per statistic as R-scape scores one statistic per run.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "column-pairs/s (GTp+APC) & E-valued MSAs/s; tensor vs plain GPU at same E<0.05 set"
+TYPES = ["GTp", "MIp", "CHIp", "RAFp"]
+CFG = dict(N=2000, L=3000, tree_len=2.0, nbp=900, nhelix=40, hmin=8, hmax=35, gap_rate=0.15, gap_mean=3.0,
+           seed=42, nshuffle=20)
+
+
+def load_covgpu():
+    import __graft_entry__ as g
+    return g._load("covgpu", os.path.join(ROOT, "r-scape_gb300", "covgpu.py"))
+
+
+def workload(cg):
+    c = CFG
+    s = cg.Synth(c["N"], c["L"], c["tree_len"], c["nbp"], c["nhelix"], c["hmin"], c["hmax"], c["gap_rate"],
+                 c["gap_mean"], seed=c["seed"])
+    keep = cg.gapfilter(s.ax, None, 0.75)
+    ax = np.ascontiguousarray(s.ax[:, keep])
+    w = cg.weights_pb(ax)
+    return s, ax, w
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per launch of a kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_reference(ax, w, budget_s, threads):
+    """pairs/s of the reference loops on the host: counting + statistic per
+    pair (x3: GTp, MIp, CHIp are three runs) and RAF's O(N^2) loop."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    N, L = ax.shape
+    # counting + GT sample: rows from the top of the pair triangle
+    t0 = time.time()
+    rows, npairs = 1, 0
+    while True:
+        n, _ = O.faithful_rows(ax, w, 0, rows, threads)
+        dt = time.time() - t0
+        npairs = n
+        if dt > budget_s * 0.3 or rows >= L - 1:
+            break
+        rows = min(L - 1, rows * 2)
+        t0 = time.time()
+    t_count = dt / npairs
+    t0 = time.time()
+    nr = max(threads, 8)
+    while True:
+        n, _ = O.faithful_raf(ax, nr, threads)
+        dt = time.time() - t0
+        if dt > budget_s * 0.3 or nr >= 4096:
+            break
+        nr *= 2
+        t0 = time.time()
+    t_raf = dt / n
+    per_pair = 3 * t_count + t_raf
+    sample = ("%d pairs of count+GT (rows 0-%d) and %d pairs of RAF of the %dx%d alignment, %d threads; "
+              "per pair = 3 x count+statistic + RAF" % (npairs, rows - 1, n, N, L, threads))
+    return 1.0 / per_pair, sample, {"count_stat_s_per_pair": t_count, "raf_s_per_pair": t_raf}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--counter", default="auto", choices=["auto", "simt", "tensor"])
+    ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline sampling")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    cg = load_covgpu()
+    s, ax, w = workload(cg)
+    N, L = ax.shape
+    P = L * (L - 1) // 2
+    ns = CFG["nshuffle"]
+    pairs_step = (ns + 1) * P
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals = []
+        for k in range(args.warmup + args.steps):
+            v, sample, parts = cpu_reference(ax, w, args.cpu_budget / max(1, args.warmup + args.steps) * 2, threads)
+            if k >= args.warmup:
+                vals.append(v)
+        value = statistics.median(vals)
+        out = {"metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": args.gpus,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * pairs_step / value,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+               "data": "synthetic", "impl": "reference",
+               "config": {"workload": "rRNA-scale alignment N=%d x L=%d, %d nulls, %s" % (N, L, ns, ",".join(TYPES)),
+                          "N": N, "L": L, "nshuffle": ns, "statistics": TYPES},
+               "cpu_baseline": {"value": value, "unit": "column-pairs/s", "cores": threads, "kind": "port",
+                                "sample": sample},
+               "e2e": {"value": value, "unit": "column-pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+               "msas_per_s": value / pairs_step}
+        print(json.dumps(out))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    counter = {"auto": 0, "simt": 0, "tensor": 1}[args.counter]
+    if args.counter == "auto":
+        counter = 1 if os.environ.get("COVGPU_COUNTER", "tensor") == "tensor" else 0
+    e = cg.Engine(N, L, maxslots=ns + 1, maxnull=ns, device=local)
+    e.set_tree(s.parent, s.left, s.right)
+    e.set_weights(w)
+    e.set_alignment(0, ax)
+    try:
+        e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)
+    except RuntimeError:
+        counter = 0      # the tensor counter refuses this shape: plain path
+    kind = "tensor" if counter == 1 else "simt"
+    for _ in range(args.warmup):
+        e.flush_l2()
+        e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)
+
+    dev_ms, cnt_ms, nl = [], [], 0
+    with ClockSampler(local) as clk:
+        if world > 1:
+            dist.barrier()
+        for _ in range(args.steps):
+            e.flush_l2()
+            res = e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)
+            ms, n = e.last_timing()
+            dev_ms.append(ms[4])
+            cnt_ms.append(ms[1])
+            nl += n
+        # end to end: host buffers in, hit lists out
+        pinned_ax, pinned_w = np.ascontiguousarray(ax), np.ascontiguousarray(w)
+        t0 = time.perf_counter()
+        e2e_hits = 0
+        for _ in range(args.steps):
+            r = e.rscape(pinned_ax, pinned_w, TYPES, nshuffle=ns, counter=counter)
+            e2e_hits = sum(len(x["hits"]) for x in r)
+        e2e_s = (time.perf_counter() - t0) / args.steps
+    step_s = sum(dev_ms) / len(dev_ms) / 1000.0
+    if world > 1:
+        import torch
+        t = torch.tensor([step_s, e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_s, e2e_s = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    value = world * pairs_step / step_s
+    e2e_value = world * pairs_step / e2e_s
+    peaks = measured_peaks()
+    peak = peaks.get("bf16_tflops") if peaks else 1900.0
+    flop_launch = 32.0 * N * P * (ns + 1)      # algorithmic: 16 cells x one multiply-add per sequence
+    cnt_s = sum(cnt_ms) / len(cnt_ms) / 1000.0
+    achieved = flop_launch / cnt_s / 1e12
+    kname = "k_count_umma" if kind == "tensor" else "k_count_simt"
+    traffic = profile_traffic(kname)
+    cpu_v, cpu_sample, _ = cpu_reference(ax, w, args.cpu_budget, threads)
+    out = {
+        "metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * step_s, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if kind == "simt" else "bf16-limbs+f64", "data": "synthetic",
+        "config": {"workload": "rRNA-scale alignment N=%d x L=%d, %d nulls, %s" % (N, L, ns, ",".join(TYPES)),
+                   "N": N, "L": L, "nshuffle": ns, "statistics": TYPES, "counter": kind,
+                   "l2": "flushed (256 MB write) before every step; count tensors 6 GB per statistic pass"},
+        "msas_per_s": world / step_s,
+        "e2e": {"value": e2e_value, "unit": "column-pairs/s", "h2d_bytes_per_step": int(ax.nbytes + w.nbytes),
+                "d2h_bytes_per_step": int(e2e_hits * 36 + 4 * 200), "msas_per_s": world / e2e_s},
+        "gpu_launches": nl,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic, "kernel": kname,
+                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback 1.9 PFLOP/s"},
+        "cpu_baseline": {"value": cpu_v, "unit": "column-pairs/s", "cores": threads, "kind": "port",
+                         "sample": cpu_sample},
+        "hits": [len(x["hits"]) for x in res],
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

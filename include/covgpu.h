@@ -1,0 +1,151 @@
+/* covgpu.h -- batched C-ABI of the GB300 covariation engine (libcovgpu.so).
+ *
+ * One context owns the device buffers for alignments of N sequences x L
+ * columns (after R-scape's gap-column filter) and up to `maxslots` of them at
+ * once: slot 0 is normally the input alignment, slots 1..nshuffle its null
+ * alignments.  All arguments are plain pointers and sizes; host buffers are
+ * ordinary (or pinned) host memory.  Every call returns 0 on success or a
+ * nonzero status with a message in the context's error buffer
+ * (covgpu_errmsg).
+ *
+ * This is the fast path behind the reference-named entry points of
+ * rscape_cov.h: one call of covgpu_rscape() does what R-scape's
+ * rscape_for_msa() does for the covariation part (src/R-scape.c:2335-2544):
+ * null alignments (null_rscape, :1614-1724), histogram width
+ * (calculate_width_histo, :1281-1371), scoring of every alignment
+ * (cov_Calculate, src/covariation.c:63-306), the null histogram, the tail fit
+ * and the E-values of the input alignment (cov_SignificantPairs_Ranking and
+ * cov_CreateHitList, :325-530, :778-1006).
+ */
+#ifndef COVGPU_H
+#define COVGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct covgpu_ctx covgpu_ctx;
+
+/* counting kernels */
+enum { COVGPU_COUNT_SIMT = 0, COVGPU_COUNT_TENSOR = 1 };
+
+typedef struct {
+  int      covclass;     /* COVCLASS: 0 C16, 1 C2, 2 CWC, 3 CSELECT (default 3) */
+  int      nseqthresh;   /* 8 */
+  int      alenthresh;   /* 50 */
+  int      nshuffle;     /* < 0: R-scape's rule (src/R-scape.c:2449-2456) */
+  double   thresh;       /* E-value threshold (0.05) */
+  double   bmin;         /* -10 */
+  double   w0;           /* 0.05 */
+  int      hpts;         /* 400 */
+  double   pmass;        /* 0.0005 */
+  double   fracfit;      /* 1.0 */
+  int      doexpfit;     /* 0 = gamma tail, 1 = exponential tail */
+  double   tol;          /* 1e-6 */
+  uint64_t seed;         /* 42 */
+  double   allow[16];    /* allowed pairs (AU UA CG GC GU UG) */
+  int      counter;      /* COVGPU_COUNT_SIMT or COVGPU_COUNT_TENSOR */
+} covgpu_params;
+
+typedef struct {
+  int      covtype;       /* COVTYPE code, e.g. 4 = GTp */
+  int      status;        /* 0 ok; 1 scores constant (w == 0); 2 one sequence */
+  int      nshuffle;
+  double   w;             /* histogram width fixed by the first null */
+  double   minCOV, maxCOV;          /* input alignment, after correction */
+  double   null_minCOV, null_maxCOV; /* first null */
+  double   pmass, newmass, mu, lambda, tau;
+  double   sc_thresh;     /* score at the E-value threshold */
+  uint64_t Nt;            /* number of tests */
+  int      nhit;          /* pairs with E < thresh (may exceed hitcap) */
+  /* cumulative null histogram */
+  double   h_bmin, h_w, h_xmin, h_xmax, h_phi;
+  int      h_nb, h_imin, h_imax, h_cmin;
+  uint64_t h_n, h_Nc, h_No;
+} covgpu_result;
+
+typedef struct {
+  int    i, j;            /* 0-based columns of the filtered alignment, i < j */
+  double sc, E, pval;
+} covgpu_hit;
+
+void        covgpu_params_default(covgpu_params *p);
+const char *covgpu_errmsg(const covgpu_ctx *ctx);
+
+int  covgpu_create(covgpu_ctx **ret, int device, int N, int L, int maxslots, int maxnull);
+void covgpu_destroy(covgpu_ctx *ctx);
+
+/* inputs: codes are Easel RNA digital codes, row-major [N][L] */
+int  covgpu_set_weights(covgpu_ctx *ctx, const double *wgt);
+int  covgpu_set_alignment(covgpu_ctx *ctx, int slot, const uint8_t *ax);
+int  covgpu_get_alignment(covgpu_ctx *ctx, int slot, uint8_t *ax);
+/* Easel ESL_TREE convention: node 0 root, parent[v] < v, children > 0 are
+ * internal nodes, <= 0 are leaves -value; arrays of N-1 entries */
+int  covgpu_set_tree(covgpu_ctx *ctx, const int *parent, const int *left, const int *right);
+/* null alignments null_id = first_null .. first_null+nnull-1 of the
+ * alignment in slot 0, written to slots first_slot .. */
+int  covgpu_make_nulls(covgpu_ctx *ctx, uint64_t seed, int first_null, int nnull, int first_slot);
+
+/* scores: covtypes are COVTYPE codes (CHI=0, CHIp=1, CHIa=2, GT=3, GTp=4,
+ * ... CCFa=26), at most 4 per call; minmax[slot][type][2] on return */
+int  covgpu_score(covgpu_ctx *ctx, int first_slot, int nslots, int ntypes, const int *covtypes, int covclass,
+                  int nseqthresh, int alenthresh, const double *allow, int counter, double *minmax);
+/* full L x L score matrix of one (slot, type index of the last covgpu_score),
+ * diagonal -inf, both triangles (the layout of mi->COV) */
+int  covgpu_get_cov(covgpu_ctx *ctx, int slot, int which, double *COV);
+/* probabilities of one slot after covgpu_score: any pointer may be NULL.
+ * nseff, ngap [L*L]; pm [L*4]; ps [L*5]; pp [L*L*16] */
+int  covgpu_get_probs(covgpu_ctx *ctx, int slot, const double *wgt, double *pp, double *nseff, double *ngap,
+                      double *pm, double *ps);
+
+/* the whole per-alignment path for up to 4 covariation types sharing the
+ * same null alignments.  results[ntypes]; hits[ntypes * hitcap].  ax == NULL
+ * or wgt == NULL reuse the alignment in slot 0 / the weights already set;
+ * the tree must have been set with covgpu_set_tree. */
+int  covgpu_rscape(covgpu_ctx *ctx, const covgpu_params *p, const uint8_t *ax, const double *wgt,
+                   int ntypes, const int *covtypes, covgpu_result *results, covgpu_hit *hits, int hitcap);
+
+/* device timing of the last covgpu_rscape phases, milliseconds:
+ * [0] nulls [1] counts [2] statistics+correction [3] histograms+fit+E-values
+ * [4] total; also the number of kernel launches */
+int  covgpu_last_timing(const covgpu_ctx *ctx, double *ms5, int *nlaunch);
+
+/* ---- single-matrix steps behind the reference-named entry points ----
+ * COV is a full L x L host matrix (both triangles); NULL uses the device's
+ * latest score matrix of slot 0. */
+/* APC (actype 0) or ASC (1) of COV into out (may alias COV or be NULL);
+ * minmax[2] of the corrected off-diagonal scores */
+int  covgpu_correct(covgpu_ctx *ctx, const double *COV, int actype, double *out, double *minmax);
+/* counts of max(COV_ij, bmin + w), i < j, in nb bins of width w from bmin */
+int  covgpu_hist_full(covgpu_ctx *ctx, const double *COV, double bmin, double w, int nb, uint64_t *obs);
+/* E-values of every pair against a null histogram h (+ survfit, may be NULL),
+ * times Nt tests; Eval full L x L (may be NULL); pairs with E < thresh */
+int  covgpu_evalue_full(covgpu_ctx *ctx, const double *COV, const void *h, const double *survfit, double Nt,
+                        double thresh, double *Eval, covgpu_hit *hits, int hitcap, int *nhit);
+
+/* writes a 256 MB device buffer (larger than L2) on the context's stream */
+int  covgpu_flush_l2(covgpu_ctx *ctx);
+
+/* ---- host utilities for preparing alignments ---- */
+/* synthetic RNA alignment: coalescent tree of leaf-to-root length tree_len
+ * (Easel convention, arrays of N-1),
+ * nbp base pairs in nhelix hairpins of hmin..hmax pairs, gap runs; ct[L] =
+ * partner column or -1.  Returns 0 or 11 (bad sizes). */
+int  covgpu_synth(int N, int L, double tree_len, int nbp, int nhelix, int hmin, int hmax, double gap_rate,
+                  double gap_mean, uint64_t seed, uint8_t *ax, int *parent, int *left, int *right, double *ld,
+                  double *rd, int *ct);
+/* the same with a choice of tree: 0 = Kingman coalescent (covgpu_synth),
+ * 1 = equal waiting times between merges */
+int  covgpu_synth2(int N, int L, int tree_kind, double tree_len, int nbp, int nhelix, int hmin, int hmax,
+                   double gap_rate, double gap_mean, uint64_t seed, uint8_t *ax, int *parent, int *left, int *right,
+                   double *ld, double *rd, int *ct);
+/* position-based weights (Henikoff & Henikoff 1994), summing to N */
+int  covgpu_weights_pb(const uint8_t *ax, int N, int L, double *wgt);
+/* R-scape's gap-column filter: useme[c] = 1 to keep column c */
+int  covgpu_gapfilter(const uint8_t *ax, const double *wgt, int N, int L, double gapthresh, int *useme);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

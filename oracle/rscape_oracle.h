@@ -1,0 +1,155 @@
+/* rscape_oracle.h -- CPU FP64 oracle for the R-scape covariation path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library restates, in plain C and double
+ * precision, the reference algorithms of R-scape 2.6.11's covariation path
+ * (src/correlators.c, src/covariation.c, src/R-scape.c null loop,
+ * src/msatree.c Fitch, src/msamanip.c substitution shuffle).  It is the
+ * checker for the GPU library: only the tests, the smoke check and the
+ * CPU-baseline leg of the benchmark may load it.  Nothing in the shipped
+ * GPU library links, calls or falls back to it.
+ *
+ * Parity status: counting, marginals, statistics and APC/ASC are pinned by
+ * the golden GTp scores and nseff values published for
+ * tutorial/updated_Arisong.sto (documentation/tutorial.tex:186-212).  The
+ * Easel pieces (sequence weights, histogram binning, binned tail fits, RNG)
+ * are absent from the reference tree and are restated from their published
+ * mathematics; E-values are therefore pinned only against this oracle's own
+ * restatement, not against a stock R-scape build.
+ *
+ * Data conventions (shared with the GPU library):
+ *   ax    uint8 row-major [N][L], Easel RNA digital codes: 0..3 = ACGU,
+ *         4 = gap, 5..14 degenerate, 15 = N, 16 = '*', 17 = '~'.
+ *   wgt   double [N] sequence weights.
+ *   trees follow Easel's ESL_TREE convention: N leaves, N-1 internal nodes,
+ *         node 0 is the root, parent[v] < v, left/right > 0 = internal node,
+ *         <= 0 = leaf -value.
+ */
+#ifndef RSCAPE_ORACLE_H
+#define RSCAPE_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* covariation types: same numbering as COVTYPE (src/correlators.h:45-79) */
+enum { ORC_CHI = 0, ORC_GT = 3, ORC_MI = 6, ORC_MIr = 9, ORC_MIg = 12, ORC_OMES = 15,
+       ORC_RAF = 18, ORC_RAFS = 21, ORC_CCF = 24 };
+/* classes: COVCLASS (src/correlators.h:38-43) */
+enum { ORC_C16 = 0, ORC_C2 = 1, ORC_CWC = 2, ORC_CSELECT = 3 };
+/* corrections: ACTYPE (src/correlators.h:81-84) */
+enum { ORC_APC = 0, ORC_ASC = 1 };
+
+typedef struct {
+  int           N;           /* leaves */
+  const int    *parent;      /* [N-1] */
+  const int    *left;        /* [N-1] */
+  const int    *right;       /* [N-1] */
+  const double *ld;          /* [N-1] */
+  const double *rd;          /* [N-1] */
+} orc_tree_t;
+
+typedef struct {
+  double    bmin, bmax, w;
+  int       nb;
+  uint64_t *obs;
+  uint64_t  n, Nc, No;
+  double    xmin, xmax;
+  int       imin, imax, cmin;
+  double    phi;
+} orc_hist_t;
+
+/* parameters of one R-scape run (defaults of src/R-scape.c:254-433, 883-892) */
+typedef struct {
+  int    covtype;        /* e.g. ORC_GT+1 = GTp */
+  int    covclass;       /* ORC_CSELECT by default */
+  int    nseqthresh;     /* 8 */
+  int    alenthresh;     /* 50 */
+  int    nshuffle;       /* <0: R-scape's rule (src/R-scape.c:2449-2456) */
+  double thresh;         /* E-value threshold, 0.05 */
+  double bmin;           /* -10 */
+  double w0;             /* 0.05 */
+  int    hpts;           /* 400 */
+  double pmass;          /* 0.0005 */
+  double fracfit;        /* 1.0 */
+  int    doexpfit;       /* 0 = gamma */
+  double tol;            /* 1e-6 */
+  uint64_t seed;         /* 42 */
+  double allow[16];      /* allowed pairs, row-major 4x4 */
+} orc_params_t;
+
+typedef struct {
+  int      nshuffle;
+  double   w;             /* histogram width from the first null */
+  double   null_minCOV, null_maxCOV;
+  double   minCOV, maxCOV; /* of the real alignment after correction */
+  double   pmass_used, newmass, mu, lambda, tau;
+  int      fit_ok;
+  double   sc_thresh;     /* evalue2cov threshold (one-set test) */
+  uint64_t Nt;            /* number of tests */
+  int      nhit;
+  /* null histogram metadata */
+  double   h_bmin, h_w;
+  int      h_nb, h_imin, h_imax, h_cmin;
+  uint64_t h_n, h_Nc, h_No;
+  double   h_xmin, h_xmax, h_phi;
+} orc_result_t;
+
+/* ---- RNG: Philox4x32-10 (Salmon et al., SC'11) ---- */
+void orc_philox4x32(const uint32_t key[2], const uint32_t ctr[4], uint32_t out[4]);
+
+/* ---- weights and MSA preparation ---- */
+int  orc_weights_pb (const uint8_t *ax, int N, int L, double *wgt);
+int  orc_weights_gsc(const uint8_t *ax, int N, int L, double *wgt);
+int  orc_gapfilter  (const uint8_t *ax, const double *wgt, int N, int L, double gapthresh, int *useme);
+void orc_degen2n    (uint8_t *ax, int64_t n);
+
+/* ---- probabilities (src/correlators.c:1300-1375, 1423-1545, 1695-1817) ---- */
+int  orc_probs(const uint8_t *ax, const double *wgt, int N, int L, double tol,
+               double *pp, double *nseff, double *ngap, double *pm, double *ps);
+
+/* ---- statistics (src/correlators.c:49-1157) ---- */
+int  orc_stat(int stat, int covclass, int N, int L, int nseqthresh, int alenthresh,
+              const double *pp, const double *pm, const double *nseff, const double *ngap,
+              const double *allow, double *COV, double *minmax);
+int  orc_raf (const uint8_t *ax, int N, int L, const double *allow, double *COV, double *minmax);
+int  orc_rafs(const uint8_t *ax, int N, int L, const double *allow, double *COV, double *minmax);
+int  orc_ccf (int L, const double *pm, const double *nseff, double *COV, double *minmax);
+int  orc_cov_corrected(int actype, int L, double *COV, double *minmax);
+int  orc_cov_calculate(int covtype, int covclass, const uint8_t *ax, const double *wgt, int N, int L,
+                       int nseqthresh, int alenthresh, const double *allow, double tol,
+                       double *COV, double *minmax);
+
+/* ---- histograms (Easel histogram semantics restated) ---- */
+orc_hist_t *orc_hist_create(double bmin, double bmax, double w);
+void        orc_hist_free(orc_hist_t *h);
+int         orc_hist_score2bin(const orc_hist_t *h, double x);
+double      orc_hist_lbound(const orc_hist_t *h, int b);
+double      orc_hist_ubound(const orc_hist_t *h, int b);
+int         orc_hist_add(orc_hist_t *h, double x);
+
+/* ---- null alignments (src/msatree.c:173-227,1700-1931; src/msamanip.c:1164-1233,1449-1780) ---- */
+uint32_t orc_feistel_perm(uint32_t t, uint32_t L, const uint32_t rk[6]);
+int  orc_fitch(const uint8_t *ax, int N, int L, const orc_tree_t *T, uint64_t seed, uint32_t null_id,
+               uint8_t *allmsa);
+int  orc_null_msa(const uint8_t *ax, int N, int L, const orc_tree_t *T, uint64_t seed, uint32_t null_id,
+                  uint8_t *out_ax);
+
+/* ---- the whole per-alignment path (src/R-scape.c:1281-1371, 1564-1724, 2335-2724) ---- */
+void orc_params_default(orc_params_t *p);
+int  orc_rscape(const orc_params_t *p, const uint8_t *ax, const double *wgt, int N, int L,
+                const orc_tree_t *T,
+                double *COV, double *Eval,                 /* [L*L] or NULL */
+                uint64_t *null_obs, int null_obs_cap,      /* cumulative null histogram */
+                int *hit_i, int *hit_j, double *hit_sc, double *hit_E, double *hit_p, int hit_cap,
+                orc_result_t *res);
+
+/* ---- reference-faithful timing mode (per-pair column gathers, FP64) ---- */
+double orc_faithful_rows(const uint8_t *ax, const double *wgt, int N, int L, int i0, int i1,
+                         int nthreads, double *checksum);
+double orc_faithful_raf(const uint8_t *ax, int N, int L, int npairs, int nthreads, double *checksum);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

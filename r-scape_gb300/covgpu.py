@@ -1,0 +1,248 @@
+"""Python binding of libcovgpu.so (the GB300 covariation engine).
+
+Thin ctypes layer over the C-ABI in include/covgpu.h.  There is no CPU path:
+if the shared library cannot be loaded, or no CUDA device is present, the
+calls raise.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(_HERE, "libcovgpu.so")
+_LIB = None
+
+u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+COVTYPES = {"CHI": 0, "GT": 3, "MI": 6, "MIr": 9, "MIg": 12, "OMES": 15, "RAF": 18, "RAFS": 21, "CCF": 24}
+C16, C2, CWC, CSELECT = 0, 1, 2, 3
+SIMT, TENSOR = 0, 1
+
+
+def covtype_code(name):
+    """'GTp' -> 4, 'MIa' -> 8, 'RAF' -> 18 (R-scape's COVTYPE numbering)."""
+    if isinstance(name, int):
+        return name
+    if name.endswith("p") and name[:-1] in COVTYPES:
+        return COVTYPES[name[:-1]] + 1
+    if name.endswith("a") and name[:-1] in COVTYPES:
+        return COVTYPES[name[:-1]] + 2
+    return COVTYPES[name]
+
+
+class Params(C.Structure):
+    _fields_ = [("covclass", C.c_int), ("nseqthresh", C.c_int), ("alenthresh", C.c_int), ("nshuffle", C.c_int),
+                ("thresh", C.c_double), ("bmin", C.c_double), ("w0", C.c_double), ("hpts", C.c_int),
+                ("pmass", C.c_double), ("fracfit", C.c_double), ("doexpfit", C.c_int), ("tol", C.c_double),
+                ("seed", C.c_uint64), ("allow", C.c_double * 16), ("counter", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("covtype", C.c_int), ("status", C.c_int), ("nshuffle", C.c_int), ("w", C.c_double),
+                ("minCOV", C.c_double), ("maxCOV", C.c_double), ("null_minCOV", C.c_double),
+                ("null_maxCOV", C.c_double), ("pmass", C.c_double), ("newmass", C.c_double), ("mu", C.c_double),
+                ("lambda_", C.c_double), ("tau", C.c_double), ("sc_thresh", C.c_double), ("Nt", C.c_uint64),
+                ("nhit", C.c_int), ("h_bmin", C.c_double), ("h_w", C.c_double), ("h_xmin", C.c_double),
+                ("h_xmax", C.c_double), ("h_phi", C.c_double), ("h_nb", C.c_int), ("h_imin", C.c_int),
+                ("h_imax", C.c_int), ("h_cmin", C.c_int), ("h_n", C.c_uint64), ("h_Nc", C.c_uint64),
+                ("h_No", C.c_uint64)]
+
+
+class Hit(C.Structure):
+    _fields_ = [("i", C.c_int), ("j", C.c_int), ("sc", C.c_double), ("E", C.c_double), ("pval", C.c_double)]
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIBPATH):
+            raise RuntimeError("libcovgpu.so is not built (run __graft_entry__.build())")
+        L = C.CDLL(LIBPATH)
+        vp = C.c_void_p
+        L.covgpu_params_default.argtypes = [C.POINTER(Params)]
+        L.covgpu_errmsg.argtypes = [vp]
+        L.covgpu_errmsg.restype = C.c_char_p
+        L.covgpu_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.covgpu_destroy.argtypes = [vp]
+        L.covgpu_set_weights.argtypes = [vp, f64p]
+        L.covgpu_set_alignment.argtypes = [vp, C.c_int, u8p]
+        L.covgpu_get_alignment.argtypes = [vp, C.c_int, u8p]
+        L.covgpu_set_tree.argtypes = [vp, i32p, i32p, i32p]
+        L.covgpu_make_nulls.argtypes = [vp, C.c_uint64, C.c_int, C.c_int, C.c_int]
+        L.covgpu_score.argtypes = [vp, C.c_int, C.c_int, C.c_int, i32p, C.c_int, C.c_int, C.c_int, f64p, C.c_int,
+                                   f64p]
+        L.covgpu_get_cov.argtypes = [vp, C.c_int, C.c_int, f64p]
+        L.covgpu_get_probs.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp]
+        L.covgpu_rscape.argtypes = [vp, C.POINTER(Params), u8p, f64p, C.c_int, i32p, C.POINTER(Result),
+                                    C.POINTER(Hit), C.c_int]
+        L.covgpu_last_timing.argtypes = [vp, f64p, C.POINTER(C.c_int)]
+        L.covgpu_flush_l2.argtypes = [vp]
+        L.covgpu_rscape.argtypes = [vp, C.POINTER(Params), vp, vp, C.c_int, i32p, C.POINTER(Result),
+                                    C.POINTER(Hit), C.c_int]
+        L.covgpu_synth.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                   C.c_double, C.c_uint64, u8p, i32p, i32p, i32p, f64p, f64p, i32p]
+        L.covgpu_synth2.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.c_double, C.c_double, C.c_uint64, u8p, i32p, i32p, i32p, f64p, f64p, i32p]
+        L.covgpu_weights_pb.argtypes = [u8p, C.c_int, C.c_int, f64p]
+        L.covgpu_gapfilter.argtypes = [u8p, f64p, C.c_int, C.c_int, C.c_double, i32p]
+        _LIB = L
+    return _LIB
+
+
+def default_allow():
+    a = np.zeros(16)
+    for x, y in ((0, 3), (3, 0), (1, 2), (2, 1), (2, 3), (3, 2)):
+        a[x * 4 + y] = 1.0
+    return a
+
+
+def params(**kw):
+    p = Params()
+    lib().covgpu_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k == "allow":
+            for i in range(16):
+                p.allow[i] = float(v[i])
+            continue
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+class Synth:
+    """A synthetic alignment with its generating tree and planted structure."""
+
+    def __init__(self, N, L, tree_len, nbp, nhelix, hmin, hmax, gap_rate, gap_mean=3.0, seed=42, tree_kind=0):
+        self.ax = np.zeros((N, L), dtype=np.uint8)
+        self.parent = np.zeros(N - 1, dtype=np.int32)
+        self.left = np.zeros(N - 1, dtype=np.int32)
+        self.right = np.zeros(N - 1, dtype=np.int32)
+        self.ld = np.zeros(N - 1)
+        self.rd = np.zeros(N - 1)
+        self.ct = np.zeros(L, dtype=np.int32)
+        st = lib().covgpu_synth2(N, L, tree_kind, tree_len, nbp, nhelix, hmin, hmax, gap_rate, gap_mean, seed,
+                                 self.ax, self.parent, self.left, self.right, self.ld, self.rd, self.ct)
+        if st:
+            raise ValueError("covgpu_synth: bad sizes (status %d)" % st)
+
+
+def weights_pb(ax):
+    ax = np.ascontiguousarray(ax, dtype=np.uint8)
+    w = np.zeros(ax.shape[0])
+    lib().covgpu_weights_pb(ax, ax.shape[0], ax.shape[1], w)
+    return w
+
+
+def gapfilter(ax, wgt=None, gapthresh=0.75):
+    ax = np.ascontiguousarray(ax, dtype=np.uint8)
+    N, L = ax.shape
+    w = np.ones(N) if wgt is None else np.ascontiguousarray(wgt, dtype=np.float64)
+    use = np.zeros(L, dtype=np.int32)
+    lib().covgpu_gapfilter(ax, w, N, L, gapthresh, use)
+    return use.astype(bool)
+
+
+class Engine:
+    """One device context for alignments of N x L."""
+
+    def __init__(self, N, L, maxslots=1, maxnull=0, device=0):
+        self.N, self.L = N, L
+        self.h = C.c_void_p()
+        st = lib().covgpu_create(C.byref(self.h), device, N, L, maxslots, maxnull)
+        if st:
+            msg = lib().covgpu_errmsg(self.h).decode() if self.h else ""
+            self.close()
+            raise RuntimeError("covgpu_create failed (%d): %s" % (st, msg))
+
+    def close(self):
+        if self.h:
+            lib().covgpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st):
+        if st:
+            raise RuntimeError("covgpu error %d: %s" % (st, lib().covgpu_errmsg(self.h).decode()))
+
+    def set_weights(self, wgt):
+        self._ck(lib().covgpu_set_weights(self.h, np.ascontiguousarray(wgt, dtype=np.float64)))
+
+    def set_alignment(self, slot, ax):
+        self._ck(lib().covgpu_set_alignment(self.h, slot, np.ascontiguousarray(ax, dtype=np.uint8)))
+
+    def get_alignment(self, slot):
+        out = np.zeros((self.N, self.L), dtype=np.uint8)
+        self._ck(lib().covgpu_get_alignment(self.h, slot, out))
+        return out
+
+    def set_tree(self, parent, left, right):
+        self._ck(lib().covgpu_set_tree(self.h, np.ascontiguousarray(parent, dtype=np.int32),
+                                       np.ascontiguousarray(left, dtype=np.int32),
+                                       np.ascontiguousarray(right, dtype=np.int32)))
+
+    def make_nulls(self, seed, first_null, nnull, first_slot):
+        self._ck(lib().covgpu_make_nulls(self.h, seed, first_null, nnull, first_slot))
+
+    def score(self, types, first_slot=0, nslots=1, covclass=CSELECT, nseqthresh=8, alenthresh=50, allow=None,
+              counter=SIMT):
+        codes = np.array([covtype_code(t) for t in types], dtype=np.int32)
+        allow = default_allow() if allow is None else np.ascontiguousarray(allow, dtype=np.float64)
+        mm = np.zeros(nslots * len(codes) * 2)
+        self._ck(lib().covgpu_score(self.h, first_slot, nslots, len(codes), codes, covclass, nseqthresh, alenthresh,
+                                    allow, counter, mm))
+        return mm.reshape(nslots, len(codes), 2)
+
+    def get_cov(self, slot, which=0):
+        out = np.zeros(self.L * self.L)
+        self._ck(lib().covgpu_get_cov(self.h, slot, which, out))
+        return out.reshape(self.L, self.L)
+
+    def get_probs(self, slot, wgt=None):
+        L = self.L
+        pp = np.zeros(L * L * 16)
+        ne = np.zeros(L * L)
+        ng = np.zeros(L * L)
+        pm = np.zeros(L * 4)
+        ps = np.zeros(L * 5)
+        wp = None if wgt is None else np.ascontiguousarray(wgt, dtype=np.float64)
+        self._ck(lib().covgpu_get_probs(self.h, slot, wp.ctypes.data if wp is not None else None, pp.ctypes.data,
+                                        ne.ctypes.data, ng.ctypes.data, pm.ctypes.data, ps.ctypes.data))
+        return pp.reshape(L, L, 16), ne.reshape(L, L), ng.reshape(L, L), pm.reshape(L, 4), ps.reshape(L, 5)
+
+    def rscape(self, ax, wgt, types, hitcap=1 << 16, **kw):
+        """ax / wgt = None reuse what is already on the device."""
+        p = params(**kw)
+        codes = np.array([covtype_code(t) for t in types], dtype=np.int32)
+        res = (Result * len(codes))()
+        hits = (Hit * (len(codes) * hitcap))()
+        axc = None if ax is None else np.ascontiguousarray(ax, dtype=np.uint8)
+        wc = None if wgt is None else np.ascontiguousarray(wgt, dtype=np.float64)
+        self._ck(lib().covgpu_rscape(self.h, C.byref(p), axc.ctypes.data if axc is not None else None,
+                                     wc.ctypes.data if wc is not None else None, len(codes), codes, res, hits,
+                                     hitcap))
+        out = []
+        for q in range(len(codes)):
+            r = {f[0]: getattr(res[q], f[0]) for f in Result._fields_}
+            n = min(r["nhit"], hitcap)
+            r["hits"] = [(hits[q * hitcap + k].i, hits[q * hitcap + k].j, hits[q * hitcap + k].sc,
+                          hits[q * hitcap + k].E, hits[q * hitcap + k].pval) for k in range(n)]
+            out.append(r)
+        return out
+
+    def flush_l2(self):
+        self._ck(lib().covgpu_flush_l2(self.h))
+
+    def last_timing(self):
+        ms = np.zeros(5)
+        n = C.c_int()
+        lib().covgpu_last_timing(self.h, ms, C.byref(n))
+        return ms, n.value

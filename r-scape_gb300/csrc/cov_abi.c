@@ -1,0 +1,671 @@
+/* cov_abi.c -- the reference-named entry points of R-scape's covariation
+ * path (src/correlators.h:445-482, src/covariation.h:27-60) on top of the
+ * GB300 engine.
+ *
+ * State: every struct mutual_s owns one engine context for its nseq x alen
+ * shape (created on first use).  corr_NaivePP / corr_Probs upload the
+ * alignment and count on the device; the corr_Calculate* functions score
+ * the alignment last uploaded for that object and fill mi->COV (both
+ * triangles, diagonal -inf, as corr_ReuseCOV leaves it); the corrections,
+ * histograms and E-values run on the device from mi->COV.  The host keeps the
+ * reference's arrays (pp, nseff, ngap, pm, ps, COV, Eval) so that callers
+ * reading them (power_SPAIR_AddMI, CaCoFold, dot plots) see the same layout.
+ *
+ * Scope: the one-set test (SAMPLE_ALL; every pair tested alike).  Files the
+ * reference writes from cov_CreateHitList (.cov, .sorted.cov, .power) and
+ * helix aggregation belong to its output layer and are not produced here.
+ */
+#include "covgpu.h"
+#include "rscape_cov.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define XFAIL(code, errbuf, ...)                                \
+  do {                                                          \
+    if (errbuf) snprintf((errbuf), 256, __VA_ARGS__);           \
+    return (code);                                              \
+  } while (0)
+
+typedef struct {
+  covgpu_ctx *ctx;
+  int         have_msa;
+  int         have_counts;
+  double     *wgt;        /* weights of the uploaded alignment */
+} gpu_state;
+
+static gpu_state *
+gpu(struct mutual_s *mi, char *errbuf)
+{
+  gpu_state *g = (gpu_state *)mi->gpu;
+  if (!g) {
+    g = (gpu_state *)calloc(1, sizeof(gpu_state));
+    if (!g) return NULL;
+    mi->gpu = g;
+  }
+  if (!g->ctx) {
+    int st = covgpu_create(&g->ctx, 0, (int)mi->nseq, (int)mi->alen, 1, 0);
+    if (st) {
+      if (errbuf) snprintf(errbuf, 256, "GPU context: %s", g->ctx ? covgpu_errmsg(g->ctx) : "cannot create");
+      covgpu_destroy(g->ctx);
+      g->ctx = NULL;
+      return NULL;
+    }
+  }
+  return g;
+}
+
+static ESL_DMATRIX *
+dmx_create(int n, int m)
+{
+  ESL_DMATRIX *D = (ESL_DMATRIX *)calloc(1, sizeof(ESL_DMATRIX));
+  int i;
+  if (!D) return NULL;
+  D->n = n; D->m = m;
+  D->mx = (double **)malloc(sizeof(double *) * (n > 0 ? n : 1));
+  D->mx[0] = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * (m > 0 ? m : 1));
+  for (i = 1; i < n; i++) D->mx[i] = D->mx[0] + (size_t)i * m;
+  return D;
+}
+
+static void
+dmx_destroy(ESL_DMATRIX *D)
+{
+  if (D) { free(D->mx[0]); free(D->mx); free(D); }
+}
+
+static void
+dmx_set(ESL_DMATRIX *D, double v)
+{
+  size_t k, n = (size_t)D->n * D->m;
+  for (k = 0; k < n; k++) D->mx[0][k] = v;
+}
+
+/* ---------------------------------------------------------------------- */
+/* corr_Create / Reuse / ReuseCOV / Destroy  (src/correlators.c:1160-1297) */
+/* ---------------------------------------------------------------------- */
+struct mutual_s *
+corr_Create(int64_t alen, int64_t nseq, int ishuffled, int nseqthresh, int alenthresh, const ESL_ALPHABET *abc,
+            COVCLASS covclass)
+{
+  struct mutual_s *mi;
+  int64_t i, j, L = alen;
+  if (alen < 1 || nseq < 1) return NULL;
+  mi = (struct mutual_s *)calloc(1, sizeof(struct mutual_s));
+  if (!mi) return NULL;
+  mi->alen = alen; mi->nseq = nseq; mi->nseqthresh = nseqthresh; mi->alenthresh = alenthresh;
+  mi->ishuffled = ishuffled; mi->abc = abc;
+  mi->pp    = (double ***)malloc(sizeof(double **) * L);
+  mi->nseff = (double **)malloc(sizeof(double *) * L);
+  mi->ngap  = (double **)malloc(sizeof(double *) * L);
+  mi->pm    = (double **)malloc(sizeof(double *) * L);
+  mi->ps    = (double **)malloc(sizeof(double *) * L);
+  if (!mi->pp || !mi->nseff || !mi->ngap || !mi->pm || !mi->ps) { corr_Destroy(mi); return NULL; }
+  mi->pp[0]    = (double **)malloc(sizeof(double *) * L * L);
+  mi->nseff[0] = (double *)calloc((size_t)L * L, sizeof(double));
+  mi->ngap[0]  = (double *)calloc((size_t)L * L, sizeof(double));
+  mi->pm[0]    = (double *)calloc((size_t)L * 4, sizeof(double));
+  mi->ps[0]    = (double *)calloc((size_t)L * 5, sizeof(double));
+  if (!mi->pp[0] || !mi->nseff[0] || !mi->ngap[0] || !mi->pm[0] || !mi->ps[0]) { corr_Destroy(mi); return NULL; }
+  mi->pp[0][0] = (double *)calloc((size_t)L * L * 16, sizeof(double));
+  if (!mi->pp[0][0]) { corr_Destroy(mi); return NULL; }
+  for (i = 0; i < L; i++) {
+    mi->pp[i]    = mi->pp[0] + i * L;
+    mi->nseff[i] = mi->nseff[0] + i * L;
+    mi->ngap[i]  = mi->ngap[0] + i * L;
+    mi->pm[i]    = mi->pm[0] + i * 4;
+    mi->ps[i]    = mi->ps[0] + i * 5;
+    for (j = 0; j < L; j++) mi->pp[i][j] = mi->pp[0][0] + (i * L + j) * 16;
+  }
+  mi->COV  = dmx_create((int)L, (int)L);
+  mi->Eval = dmx_create((int)L, (int)L);
+  corr_ReuseCOV(mi, COVNONE, covclass);
+  return mi;
+}
+
+int
+corr_ReuseCOV(struct mutual_s *mi, COVTYPE mitype, COVCLASS miclass)
+{
+  mi->type = mitype;
+  mi->class_ = miclass;
+  if (mi->COV)  dmx_set(mi->COV, -INFINITY);
+  if (mi->Eval) dmx_set(mi->Eval, INFINITY);
+  mi->besthreshCOV = -INFINITY;
+  mi->minCOV = INFINITY;
+  mi->maxCOV = -INFINITY;
+  return eslOK;
+}
+
+int
+corr_Reuse(struct mutual_s *mi, int ishuffled, COVTYPE mitype, COVCLASS miclass)
+{
+  const size_t L = (size_t)mi->alen;
+  mi->ishuffled = ishuffled;
+  memset(mi->pp[0][0], 0, sizeof(double) * L * L * 16);
+  memset(mi->nseff[0], 0, sizeof(double) * L * L);
+  memset(mi->ngap[0], 0, sizeof(double) * L * L);
+  memset(mi->pm[0], 0, sizeof(double) * L * 4);
+  memset(mi->ps[0], 0, sizeof(double) * L * 5);
+  return corr_ReuseCOV(mi, mitype, miclass);
+}
+
+void
+corr_Destroy(struct mutual_s *mi)
+{
+  gpu_state *g;
+  if (!mi) return;
+  g = (gpu_state *)mi->gpu;
+  if (g) { covgpu_destroy(g->ctx); free(g->wgt); free(g); }
+  if (mi->pp)    { if (mi->pp[0]) free(mi->pp[0][0]); free(mi->pp[0]); free(mi->pp); }
+  if (mi->nseff) { free(mi->nseff[0]); free(mi->nseff); }
+  if (mi->ngap)  { free(mi->ngap[0]); free(mi->ngap); }
+  if (mi->pm)    { free(mi->pm[0]); free(mi->pm); }
+  if (mi->ps)    { free(mi->ps[0]); free(mi->ps); }
+  dmx_destroy(mi->COV);
+  dmx_destroy(mi->Eval);
+  free(mi);
+}
+
+/* ---------------------------------------------------------------------- */
+/* probabilities                                                            */
+/* ---------------------------------------------------------------------- */
+static int
+upload_msa(struct mutual_s *mi, ESL_MSA *msa, char *errbuf)
+{
+  gpu_state *g;
+  uint8_t   *ax;
+  int64_t    s, L = msa->alen;
+  int        st;
+  if (msa->nseq != mi->nseq || msa->alen != mi->alen)
+    XFAIL(eslEINVAL, errbuf, "alignment %d x %lld does not match mutual_s %lld x %lld", msa->nseq,
+          (long long)msa->alen, (long long)mi->nseq, (long long)mi->alen);
+  if (!(g = gpu(mi, errbuf))) return eslFAIL;
+  ax = (uint8_t *)malloc((size_t)msa->nseq * L);
+  if (!ax) XFAIL(eslEMEM, errbuf, "out of memory");
+  for (s = 0; s < msa->nseq; s++) memcpy(ax + s * L, msa->ax[s] + 1, (size_t)L);
+  st = covgpu_set_alignment(g->ctx, 0, ax);
+  free(ax);
+  if (st) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  free(g->wgt);
+  g->wgt = (double *)malloc(sizeof(double) * msa->nseq);
+  for (s = 0; s < msa->nseq; s++) g->wgt[s] = msa->wgt ? msa->wgt[s] : 1.0;
+  if ((st = covgpu_set_weights(g->ctx, g->wgt))) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  g->have_msa = 1;
+  g->have_counts = 0;
+  return eslOK;
+}
+
+static const double ALLOW_DEFAULT[16] = {0, 0, 0, 1, 0, 0, 1, 0, 0, 1, 0, 1, 1, 0, 1, 0};
+
+static void
+allow16(const ESL_DMATRIX *allowpair, double *a)
+{
+  int x, y;
+  for (x = 0; x < 4; x++)
+    for (y = 0; y < 4; y++) a[x * 4 + y] = allowpair ? allowpair->mx[x][y] : ALLOW_DEFAULT[x * 4 + y];
+}
+
+static int
+count_on_device(struct mutual_s *mi, char *errbuf)
+{
+  gpu_state *g = (gpu_state *)mi->gpu;
+  int type = GT, st;
+  if (!g || !g->have_msa) XFAIL(eslFAIL, errbuf, "no alignment uploaded (call corr_Probs first)");
+  st = covgpu_score(g->ctx, 0, 1, 1, &type, C16, mi->nseqthresh, mi->alenthresh, ALLOW_DEFAULT, COVGPU_COUNT_SIMT,
+                    NULL);
+  if (st) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  g->have_counts = 1;
+  return eslOK;
+}
+
+/* corr_NaivePP, src/correlators.c:1300-1317 */
+int
+corr_NaivePP(ESL_RANDOMNESS *r, ESL_MSA *msa, struct mutual_s *mi, double tol, int verbose, char *errbuf)
+{
+  gpu_state *g;
+  int st;
+  (void)r; (void)tol; (void)verbose;
+  if ((st = upload_msa(mi, msa, errbuf))) return st;
+  if ((st = count_on_device(mi, errbuf))) return st;
+  g = (gpu_state *)mi->gpu;
+  if (covgpu_get_probs(g->ctx, 0, g->wgt, mi->pp[0][0], mi->nseff[0], mi->ngap[0], NULL, NULL))
+    XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  return eslOK;
+}
+
+/* corr_NaivePS, src/correlators.c:1319-1335 */
+int
+corr_NaivePS(ESL_RANDOMNESS *r, ESL_MSA *msa, struct mutual_s *mi, double tol, int verbose, char *errbuf)
+{
+  gpu_state *g = (gpu_state *)mi->gpu;
+  int st;
+  (void)r; (void)tol; (void)verbose;
+  if (!g || !g->have_counts) {
+    if ((st = upload_msa(mi, msa, errbuf))) return st;
+    if ((st = count_on_device(mi, errbuf))) return st;
+    g = (gpu_state *)mi->gpu;
+  }
+  if (covgpu_get_probs(g->ctx, 0, g->wgt, NULL, NULL, NULL, NULL, mi->ps[0]))
+    XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  return eslOK;
+}
+
+/* corr_Marginals, src/correlators.c:1337-1375: the marginals of the counts
+ * of the last corr_NaivePP on the device */
+int
+corr_Marginals(struct mutual_s *mi, double tol, int verbose, char *errbuf)
+{
+  gpu_state *g = (gpu_state *)mi->gpu;
+  int64_t i;
+  (void)verbose;
+  if (!g || !g->have_counts) XFAIL(eslFAIL, errbuf, "corr_Marginals: no counts on the device (call corr_NaivePP)");
+  if (covgpu_get_probs(g->ctx, 0, g->wgt, NULL, NULL, NULL, mi->pm[0], NULL))
+    XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  for (i = 0; i < mi->alen; i++) {
+    double s = mi->pm[i][0] + mi->pm[i][1] + mi->pm[i][2] + mi->pm[i][3];
+    if (fabs(s - 1.0) > tol) XFAIL(eslFAIL, errbuf, "pm[%lld] does not sum to one", (long long)i);
+  }
+  return eslOK;
+}
+
+static int
+validate_vec(const double *v, int n, double tol)
+{
+  double s = 0.0;
+  int k;
+  for (k = 0; k < n; k++) { if (!(v[k] >= 0.0 && v[k] <= 1.0 + tol)) return 1; s += v[k]; }
+  return fabs(s - 1.0) > tol;
+}
+
+/* corr_ValidateProbs, src/correlators.c:1499-1545 */
+int
+corr_ValidateProbs(struct mutual_s *mi, double tol, int verbose, char *errbuf)
+{
+  int64_t i, j;
+  (void)verbose;
+  for (i = 0; i < mi->alen - 1; i++)
+    for (j = i + 1; j < mi->alen; j++)
+      if (validate_vec(mi->pp[i][j], 16, tol)) XFAIL(eslFAIL, errbuf, "pp validation failed");
+  for (i = 0; i < mi->alen; i++) {
+    if (validate_vec(mi->pm[i], 4, tol)) XFAIL(eslFAIL, errbuf, "pm validation failed");
+    if (validate_vec(mi->ps[i], 5, tol)) XFAIL(eslFAIL, errbuf, "ps validation failed");
+  }
+  return eslOK;
+}
+
+/* corr_Probs, src/correlators.c:1423-1496 (NONPARAM / POTTS counting) */
+int
+corr_Probs(ESL_RANDOMNESS *r, ESL_MSA *msa, ESL_TREE *T, void *ribosum, struct mutual_s *mi, METHOD method,
+           double tol, int verbose, char *errbuf)
+{
+  int st;
+  (void)T; (void)ribosum;
+  if (method == AKMAEV) XFAIL(eslFAIL, errbuf, "the AKMAEV pair probabilities are not provided by this library");
+  if ((st = corr_NaivePP(r, msa, mi, tol, verbose, errbuf))) return st;
+  if ((st = corr_NaivePS(r, msa, mi, tol, verbose, errbuf))) return st;
+  if ((st = corr_Marginals(mi, tol, verbose, errbuf))) return st;
+  return corr_ValidateProbs(mi, tol, verbose, errbuf);
+}
+
+/* ---------------------------------------------------------------------- */
+/* statistics                                                               */
+/* ---------------------------------------------------------------------- */
+static int
+score_into_cov(struct mutual_s *mi, int covtype, int cls, const ESL_DMATRIX *allowpair, char *errbuf)
+{
+  gpu_state *g = (gpu_state *)mi->gpu;
+  double a[16], mm[2];
+  int st;
+  if (!g || !g->have_msa) XFAIL(eslFAIL, errbuf, "no alignment on the device (call corr_Probs first)");
+  allow16(allowpair, a);
+  st = covgpu_score(g->ctx, 0, 1, 1, &covtype, cls, mi->nseqthresh, mi->alenthresh, a, COVGPU_COUNT_SIMT, mm);
+  if (st) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  if (covgpu_get_cov(g->ctx, 0, 0, mi->COV->mx[0])) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  g->have_counts = 1;
+  mi->type = (COVTYPE)covtype;
+  mi->minCOV = mm[0];
+  mi->maxCOV = mm[1];
+  return eslOK;
+}
+
+static int
+resolve_class(struct mutual_s *mi, COVCLASS c)
+{
+  if (c == CSELECT) return (mi->nseq <= mi->nseqthresh || mi->alen <= mi->alenthresh) ? C2 : C16;
+  return (int)c;
+}
+
+#define STAT_FAMILY(NAME, BASE)                                                                             \
+  int corr_Calculate##NAME##_C16(struct mutual_s *mi, int verbose, char *errbuf) {                         \
+    (void)verbose;                                                                                         \
+    mi->class_ = C16;                                                                                      \
+    return score_into_cov(mi, BASE, C16, NULL, errbuf);                                                    \
+  }                                                                                                        \
+  int corr_Calculate##NAME##_C2(struct mutual_s *mi, ESL_DMATRIX *allowpair, int verbose, char *errbuf) {  \
+    (void)verbose;                                                                                         \
+    mi->class_ = C2;                                                                                       \
+    return score_into_cov(mi, BASE, C2, allowpair, errbuf);                                                \
+  }                                                                                                        \
+  int corr_Calculate##NAME(COVCLASS covclass, struct data_s *data) {                                       \
+    struct mutual_s *mi = data->mi;                                                                        \
+    int cls = resolve_class(mi, covclass);                                                                 \
+    if (cls == CWC) XFAIL(eslFAIL, data->errbuf, "corr_Calculate" #NAME "() CWC not implemented\n");       \
+    mi->class_ = covclass;                                                                                 \
+    return score_into_cov(mi, BASE, cls, data->allowpair, data->errbuf);                                   \
+  }
+
+/* CHI :49-181, OMES :184-314, MI :493-614, MIr :617-745, MIg :748-874 */
+STAT_FAMILY(CHI, CHI)
+STAT_FAMILY(OMES, OMES)
+STAT_FAMILY(MI, MI)
+STAT_FAMILY(MIr, MIr)
+STAT_FAMILY(MIg, MIg)
+
+/* GT :316-490, with the CWC form */
+int
+corr_CalculateGT_C16(struct mutual_s *mi, int verbose, char *errbuf)
+{
+  (void)verbose;
+  mi->class_ = C16;
+  return score_into_cov(mi, GT, C16, NULL, errbuf);
+}
+
+int
+corr_CalculateGT_C2(struct mutual_s *mi, ESL_DMATRIX *allowpair, int verbose, char *errbuf)
+{
+  (void)verbose;
+  mi->class_ = C2;
+  return score_into_cov(mi, GT, C2, allowpair, errbuf);
+}
+
+int
+corr_CalculateGT_CWC(struct mutual_s *mi, ESL_DMATRIX *allowpair, int verbose, char *errbuf)
+{
+  (void)verbose;
+  mi->class_ = C16;
+  return score_into_cov(mi, GT, CWC, allowpair, errbuf);
+}
+
+int
+corr_CalculateGT(COVCLASS covclass, struct data_s *data)
+{
+  struct mutual_s *mi = data->mi;
+  int cls = resolve_class(mi, covclass);
+  mi->class_ = covclass;
+  return score_into_cov(mi, GT, cls, data->allowpair, data->errbuf);
+}
+
+/* RAF :876-933, RAFS :935-982: unweighted, from the given alignment */
+int
+corr_CalculateRAF(COVCLASS covclass, struct data_s *data, ESL_MSA *msa)
+{
+  int st;
+  (void)covclass;
+  if ((st = upload_msa(data->mi, msa, data->errbuf))) return st;
+  data->mi->class_ = C2;
+  return score_into_cov(data->mi, RAF, C2, data->allowpair, data->errbuf);
+}
+
+int
+corr_CalculateRAFS(COVCLASS covclass, struct data_s *data, ESL_MSA *msa)
+{
+  int st;
+  (void)covclass;
+  if ((st = upload_msa(data->mi, msa, data->errbuf))) return st;
+  data->mi->class_ = C2;
+  return score_into_cov(data->mi, RAFS, C2, data->allowpair, data->errbuf);
+}
+
+/* CCF :984-1061 */
+int
+corr_CalculateCCF_C16(struct mutual_s *mi, int verbose, char *errbuf)
+{
+  (void)verbose;
+  mi->class_ = C16;
+  return score_into_cov(mi, CCF, C16, NULL, errbuf);
+}
+
+int
+corr_CalculateCCF(COVCLASS covclass, struct data_s *data)
+{
+  (void)covclass;
+  return corr_CalculateCCF_C16(data->mi, data->verbose, data->errbuf);
+}
+
+/* corr_CalculateCOVCorrected, src/correlators.c:1063-1157 */
+int
+corr_CalculateCOVCorrected(ACTYPE actype, struct data_s *data, int shiftnonneg)
+{
+  struct mutual_s *mi = data->mi;
+  gpu_state *g = gpu(mi, data->errbuf);
+  double mm[2];
+  int64_t i, j, L = mi->alen;
+  int base;
+  if (!g) return eslFAIL;
+  if (actype != APC && actype != ASC) XFAIL(eslFAIL, data->errbuf, "wrong correction type\n");
+  if (mi->type >= PTFp) XFAIL(eslFAIL, data->errbuf, "wrong COVTYPE");
+  base = ((int)mi->type / 3) * 3;
+  if (covgpu_correct(g->ctx, mi->COV->mx[0], (int)actype, mi->COV->mx[0], mm))
+    XFAIL(eslFAIL, data->errbuf, "bad covariation: %s", covgpu_errmsg(g->ctx));
+  mi->type = (COVTYPE)(base + (actype == APC ? 1 : 2));
+  mi->minCOV = mm[0];
+  mi->maxCOV = mm[1];
+  if (shiftnonneg)
+    for (i = 0; i < L; i++)
+      for (j = 0; j < L; j++)
+        if (i != j) mi->COV->mx[i][j] -= mi->minCOV;
+  return eslOK;
+}
+
+/* corr_COVTYPEString / corr_String2COVTYPE, src/correlators.c:1562-1662 */
+static const char *COVNAMES[] = {"CHI", "CHIp", "CHIa", "GT", "GTp", "GTa", "MI", "MIp", "MIa", "MIr",
+                                 "MIrp", "MIra", "MIg", "MIgp", "MIga", "OMES", "OMESp", "OMESa", "RAF", "RAFp",
+                                 "RAFa", "RAFS", "RAFSp", "RAFSa", "CCF", "CCFp", "CCFa", "PTFp", "PTAp", "PTDp"};
+
+int
+corr_COVTYPEString(char **ret_covtype, COVTYPE type, char *errbuf)
+{
+  size_t n;
+  if ((int)type < 0 || (int)type >= COVNONE) XFAIL(eslFAIL, errbuf, "wrong COVTYPE");
+  n = strlen(COVNAMES[type]) + 1;
+  *ret_covtype = (char *)malloc(n);
+  if (!*ret_covtype) XFAIL(eslEMEM, errbuf, "out of memory");
+  memcpy(*ret_covtype, COVNAMES[type], n);
+  return eslOK;
+}
+
+int
+corr_String2COVTYPE(char *covtype, COVTYPE *ret_type, char *errbuf)
+{
+  int k;
+  for (k = 0; k < COVNONE; k++)
+    if (covtype && strcmp(covtype, COVNAMES[k]) == 0) { *ret_type = (COVTYPE)k; return eslOK; }
+  XFAIL(eslFAIL, errbuf, "wrong COVTYPE %s", covtype ? covtype : "(null)");
+}
+
+/* ---------------------------------------------------------------------- */
+/* cov_Calculate and the ranking                                            */
+/* ---------------------------------------------------------------------- */
+
+/* cov_Calculate, src/covariation.c:63-306 */
+int
+cov_Calculate(struct data_s *data, ESL_MSA *msa, RANKLIST **ret_ranklist, HITLIST **ret_hitlist,
+              RMLIST **ret_rmlist, int analyze)
+{
+  struct mutual_s *mi = data->mi;
+  COVCLASS covclass = mi->class_;
+  int base, corr, st;
+  if ((int)data->covtype >= PTFp) XFAIL(eslFAIL, data->errbuf, "wrong covariation type\n");
+  base = ((int)data->covtype / 3) * 3;
+  corr = (int)data->covtype % 3;
+  if (base != RAF && base != RAFS) {
+    if ((st = corr_Probs(data->r, msa, NULL, NULL, mi, data->covmethod, data->tol, data->verbose, data->errbuf)))
+      return st;
+  }
+  switch (base) {
+    case CHI:  st = corr_CalculateCHI(covclass, data); break;
+    case GT:   st = corr_CalculateGT(covclass, data); break;
+    case MI:   st = corr_CalculateMI(covclass, data); break;
+    case MIr:  st = corr_CalculateMIr(covclass, data); break;
+    case MIg:  st = corr_CalculateMIg(covclass, data); break;
+    case OMES: st = corr_CalculateOMES(covclass, data); break;
+    case RAF:  st = corr_CalculateRAF(covclass, data, msa); break;
+    case RAFS: st = corr_CalculateRAFS(covclass, data, msa); break;
+    case CCF:  st = corr_CalculateCCF(covclass, data); break;
+    default:   XFAIL(eslFAIL, data->errbuf, "wrong covariation type\n");
+  }
+  if (st) return st;
+  if (corr == 1 && (st = corr_CalculateCOVCorrected(APC, data, 0))) return st;
+  if (corr == 2 && (st = corr_CalculateCOVCorrected(ASC, data, 0))) return st;
+  if (ret_rmlist) *ret_rmlist = NULL;
+  if (analyze) return cov_SignificantPairs_Ranking(data, ret_ranklist, ret_hitlist, ret_rmlist);
+  if (ret_ranklist) *ret_ranklist = NULL;
+  if (ret_hitlist) *ret_hitlist = NULL;
+  return eslOK;
+}
+
+/* histogram of the pair scores of mi->COV on the device, into h (nb bins) */
+static int
+rank_into(struct mutual_s *mi, ESL_HISTOGRAM *h, char *errbuf)
+{
+  gpu_state *g = (gpu_state *)mi->gpu;
+  int64_t i, j, L = mi->alen;
+  int b;
+  double lo = h->bmin + h->w, xmin = INFINITY, xmax = -INFINITY;
+  if (!g) XFAIL(eslFAIL, errbuf, "no device context");
+  if (covgpu_hist_full(g->ctx, mi->COV->mx[0], h->bmin, h->w, h->nb, h->obs))
+    XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  for (i = 0; i < L - 1; i++)
+    for (j = i + 1; j < L; j++) {
+      double v = mi->COV->mx[i][j];
+      double add = (v > lo) ? v : lo;
+      if (add < xmin) xmin = add;
+      if (add > xmax) xmax = add;
+    }
+  h->n = h->Nc = h->No = (uint64_t)(L * (L - 1) / 2);
+  h->xmin = xmin; h->xmax = xmax;
+  h->imin = h->nb; h->imax = -1;
+  for (b = 0; b < h->nb; b++)
+    if (h->obs[b]) { if (b < h->imin) h->imin = b; if (b > h->imax) h->imax = b; }
+  h->cmin = h->imin;
+  return eslOK;
+}
+
+/* cov_SignificantPairs_Ranking, src/covariation.c:325-530 (one-set test) */
+int
+cov_SignificantPairs_Ranking(struct data_s *data, RANKLIST **ret_ranklist, HITLIST **ret_hitlist,
+                             RMLIST **ret_rmlist)
+{
+  struct mutual_s *mi = data->mi;
+  RANKLIST *ranklist;
+  HITLIST  *hitlist = NULL;
+  double    bmax, pmass, newmass;
+  int       st;
+  if (ret_rmlist) *ret_rmlist = NULL;
+  if (ret_ranklist) *ret_ranklist = NULL;
+  if (ret_hitlist) *ret_hitlist = NULL;
+  if ((data->nseq > 1 && data->w < 1e-20) || data->nseq == 1) {   /* :348-412 */
+    if (data->thresh) { data->thresh->sc_bp = INFINITY; data->thresh->sc_nbp = INFINITY; }
+    return eslOK;
+  }
+  bmax = mi->maxCOV + 5 * data->w;
+  while (fabs(bmax - data->bmin) < data->tol) bmax += data->w;
+  ranklist = cov_CreateRankList(bmax, data->bmin, data->w);
+  if (!ranklist) XFAIL(eslEMEM, data->errbuf, "out of memory");
+  if ((st = rank_into(mi, ranklist->ha, data->errbuf))) { cov_FreeRankList(ranklist); return st; }
+  if (data->mode == GIVSS || data->mode == FOLDSS) {   /* SAMPLE_ALL: every pair goes to ht */
+    ESL_HISTOGRAM *ht = ranklist->ht, *ha = ranklist->ha;
+    memcpy(ht->obs, ha->obs, sizeof(uint64_t) * ha->nb);
+    ht->n = ha->n; ht->Nc = ha->Nc; ht->No = ha->No; ht->xmin = ha->xmin; ht->xmax = ha->xmax;
+    ht->imin = ha->imin; ht->imax = ha->imax; ht->cmin = ha->cmin;
+  }
+  if (data->ranklist_null && data->mode == GIVSS) {
+    ESL_HISTOGRAM *hn = data->ranklist_null->ha;
+    if (hn->nb < ranklist->ha->nb) {   /* :462-466 */
+      int b;
+      hn->obs = (uint64_t *)realloc(hn->obs, sizeof(uint64_t) * ranklist->ha->nb);
+      for (b = hn->nb; b < ranklist->ha->nb; b++) hn->obs[b] = 0;
+      hn->nb = ranklist->ha->nb;
+    }
+    pmass = covh_pmass(hn, data->pmass, data->fracfit);
+    if (isnan(pmass)) { cov_FreeRankList(ranklist); XFAIL(eslFAIL, data->errbuf, "bad Null histogram fit, pmass is nan."); }
+    free(data->ranklist_null->survfit);
+    data->ranklist_null->survfit = NULL;
+    if (data->doexpfit)
+      st = cov_NullFitExponential(hn, &data->ranklist_null->survfit, pmass, &newmass, &data->mu, &data->lambda,
+                                  data->verbose, data->errbuf);
+    else
+      st = cov_NullFitGamma(hn, &data->ranklist_null->survfit, pmass, &newmass, &data->mu, &data->lambda, &data->tau,
+                            data->verbose, data->errbuf);
+    if (st) { cov_FreeRankList(ranklist); return st; }
+  }
+  if (data->mode == GIVSS && data->thresh) {   /* :490-500 */
+    double Nc = (double)((ranklist->hb->Nc > 0) ? ranklist->hb->Nc : ranklist->ha->Nc);
+    data->thresh->sc_bp = data->ranklist_null
+                              ? covh_evalue2cov(data->thresh->val, Nc, data->ranklist_null->ha, data->ranklist_null->survfit)
+                              : INFINITY;
+    data->thresh->sc_nbp = data->thresh->sc_bp;
+  }
+  if (data->mode == GIVSS) {
+    if ((st = cov_CreateHitList(data, mi, ranklist, &hitlist, NULL, NULL, NULL))) {
+      cov_FreeRankList(ranklist);
+      return st;
+    }
+  }
+  if (ret_ranklist) *ret_ranklist = ranklist; else cov_FreeRankList(ranklist);
+  if (ret_hitlist) *ret_hitlist = hitlist; else cov_FreeHitList(hitlist);
+  return eslOK;
+}
+
+/* cov_CreateHitList, src/covariation.c:778-1006 (one-set test: E = p * Nt) */
+int
+cov_CreateHitList(struct data_s *data, struct mutual_s *mi, RANKLIST *ranklist, HITLIST **ret_hitlist,
+                  RMLIST **ret_rmlist, char *covtype, char *threshtype)
+{
+  gpu_state  *g = (gpu_state *)mi->gpu;
+  HITLIST    *hl;
+  covgpu_hit *hits = NULL;
+  int64_t     P = mi->alen * (mi->alen - 1) / 2;
+  int         nhit = 0, cap, k, st;
+  double      thresh = data->thresh ? data->thresh->val : 0.05;
+  (void)covtype; (void)threshtype;
+  if (ret_rmlist) *ret_rmlist = NULL;
+  hl = (HITLIST *)calloc(1, sizeof(HITLIST));
+  if (!hl) XFAIL(eslEMEM, data->errbuf, "out of memory");
+  hl->Nt = (int64_t)ranklist->ht->Nc;
+  hl->Nb = (int64_t)ranklist->hb->Nc;
+  if (!data->ranklist_null) {   /* naive: every pair with E = 0 */
+    dmx_set(mi->Eval, INFINITY);
+    cap = (thresh > 0.0) ? (int)P : 0;
+    hl->hit = (HIT *)calloc(cap > 0 ? cap : 1, sizeof(HIT));
+    for (k = 0; k < cap; k++) {
+      int64_t i = 0, rem = k;
+      while (rem >= mi->alen - 1 - i) { rem -= mi->alen - 1 - i; i++; }
+      hl->hit[k].i = i; hl->hit[k].j = i + 1 + rem;
+      hl->hit[k].sc = mi->COV->mx[i][i + 1 + rem];
+    }
+    hl->nhit = cap;
+  } else {
+    if (!g) { free(hl); XFAIL(eslFAIL, data->errbuf, "no device context"); }
+    cap = (int)((P < (1 << 22)) ? P : (1 << 22));
+    hits = (covgpu_hit *)malloc(sizeof(covgpu_hit) * (cap > 0 ? cap : 1));
+    st = covgpu_evalue_full(g->ctx, mi->COV->mx[0], data->ranklist_null->ha, data->ranklist_null->survfit,
+                            (double)ranklist->ht->Nc, (thresh > MAX_EVAL) ? 2.0 * MAX_EVAL : thresh, mi->Eval->mx[0],
+                            hits, cap, &nhit);
+    if (st) { free(hits); free(hl); XFAIL(eslFAIL, data->errbuf, "%s", covgpu_errmsg(g->ctx)); }
+    if (nhit > cap) nhit = cap;
+    hl->hit = (HIT *)calloc(nhit > 0 ? nhit : 1, sizeof(HIT));
+    for (k = 0; k < nhit; k++) {
+      hl->hit[k].i = hits[k].i; hl->hit[k].j = hits[k].j;
+      hl->hit[k].sc = hits[k].sc; hl->hit[k].Eval = hits[k].E; hl->hit[k].pval = hits[k].pval;
+    }
+    hl->nhit = nhit;
+    free(hits);
+  }
+  hl->srthit = (HIT **)malloc(sizeof(HIT *) * (hl->nhit > 0 ? hl->nhit : 1));
+  for (k = 0; k < hl->nhit; k++) hl->srthit[k] = &hl->hit[k];
+  *ret_hitlist = hl;
+  return eslOK;
+}

@@ -1,0 +1,812 @@
+// cov_engine.cu -- host orchestration of the GB300 covariation engine and
+// its C-ABI (include/covgpu.h).  One context = one device stream and the
+// device buffers for up to `maxslots` alignments of N x L.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "cov_dev.cuh"
+#include "cov_kernels.h"
+#include "cov_umma.h"
+#include "covgpu.h"
+#include "rscape_cov.h"
+
+using namespace covgpu;
+
+struct covgpu_ctx {
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  int N = 0, L = 0, Lp = 0, nT = 0, ntiles = 0, maxslots = 0, maxnull = 0;
+  char err[512] = {0};
+  TileRC* d_tiles = nullptr;
+  int* d_tile_index = nullptr;
+  uint8_t* d_ax = nullptr;
+  float* d_wf = nullptr;
+  double* d_wd = nullptr;
+  std::vector<double> h_w;
+  double wtot = 0.0;
+  bool have_w = false;
+  float* d_cnt = nullptr;
+  float* d_ucnt = nullptr;
+  double *d_part4 = nullptr, *d_partR = nullptr, *d_pm = nullptr, *d_meanp = nullptr, *d_ps = nullptr;
+  double *d_cov = nullptr, *d_cov2 = nullptr, *d_part1 = nullptr, *d_colx = nullptr, *d_avg = nullptr;
+  double *d_tmin = nullptr, *d_tmax = nullptr, *d_mm = nullptr;
+  int* d_status = nullptr;
+  int last_nout = 0, last_first = 0, last_nslots = 0;
+  int* d_left = nullptr;
+  int* d_right = nullptr;
+  int* d_lnodes = nullptr;
+  std::vector<int> loff;
+  bool have_tree = false;
+  uint8_t *d_fitch = nullptr, *d_scratch = nullptr;
+  unsigned long long* d_obs = nullptr;
+  int nbcap = 0;
+  double *d_sf = nullptr, *d_tail = nullptr;
+  int sfcap = 0;
+  int* d_nhits = nullptr;
+  int *d_hi = nullptr, *d_hj = nullptr;
+  double *d_hsc = nullptr, *d_hE = nullptr, *d_hp = nullptr;
+  int hitcap = 0;
+  double* d_full = nullptr;
+  UmmaPlan* umma = nullptr;
+  unsigned char* d_flush = nullptr;
+  bool counted = false;
+  cudaEvent_t ev[6] = {};
+  double tms[5] = {0, 0, 0, 0, 0};
+  double fit_ms = 0.0;
+  int nlaunch = 0;
+};
+
+static int fail(covgpu_ctx* c, int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(c->err, sizeof(c->err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) return fail(ctx, 90, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+static cudaError_t dalloc(T** p, size_t n) {
+  return cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
+}
+
+extern "C" void covgpu_params_default(covgpu_params* p) {
+  memset(p, 0, sizeof(*p));
+  p->covclass = 3; p->nseqthresh = 8; p->alenthresh = 50; p->nshuffle = -1;
+  p->thresh = 0.05; p->bmin = -10.0; p->w0 = 0.05; p->hpts = 400; p->pmass = 0.0005; p->fracfit = 1.0;
+  p->doexpfit = 0; p->tol = 1e-6; p->seed = 42; p->counter = COVGPU_COUNT_SIMT;
+  p->allow[0 * 4 + 3] = p->allow[3 * 4 + 0] = 1.0;   // src/R-scape.c:883-887
+  p->allow[1 * 4 + 2] = p->allow[2 * 4 + 1] = 1.0;
+  p->allow[2 * 4 + 3] = p->allow[3 * 4 + 2] = 1.0;
+}
+
+extern "C" const char* covgpu_errmsg(const covgpu_ctx* ctx) { return ctx ? ctx->err : "no context"; }
+
+extern "C" int covgpu_create(covgpu_ctx** ret, int device, int N, int L, int maxslots, int maxnull) {
+  *ret = nullptr;
+  if (N < 1 || L < 1 || maxslots < 1 || maxnull < 0) return 11;
+  covgpu_ctx* ctx = new covgpu_ctx();
+  ctx->dev = device; ctx->N = N; ctx->L = L; ctx->maxslots = maxslots; ctx->maxnull = maxnull;
+  ctx->nT = (L + TP - 1) / TP;
+  ctx->Lp = ctx->nT * TP;
+  ctx->ntiles = ctx->nT * (ctx->nT + 1) / 2;
+  *ret = ctx;
+  CK(cudaSetDevice(device));
+  CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+  for (auto& e : ctx->ev) CK(cudaEventCreate(&e));
+  std::vector<TileRC> tiles;
+  std::vector<int> tindex((size_t)ctx->nT * ctx->nT, -1);
+  for (int I = 0; I < ctx->nT; I++)
+    for (int J = I; J < ctx->nT; J++) { tindex[(size_t)I * ctx->nT + J] = (int)tiles.size(); tiles.push_back({I, J}); }
+  const size_t nT2 = (size_t)ctx->nT * ctx->nT, ntl = ctx->ntiles, S = maxslots;
+  CK(dalloc(&ctx->d_tiles, ntl));
+  CK(dalloc(&ctx->d_tile_index, nT2));
+  CK(cudaMemcpy(ctx->d_tiles, tiles.data(), ntl * sizeof(TileRC), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_tile_index, tindex.data(), nT2 * sizeof(int), cudaMemcpyHostToDevice));
+  CK(dalloc(&ctx->d_ax, S * N * ctx->Lp));
+  CK(cudaMemset(ctx->d_ax, 4, S * N * ctx->Lp));
+  CK(dalloc(&ctx->d_wf, N));
+  CK(dalloc(&ctx->d_wd, N));
+  CK(dalloc(&ctx->d_cnt, S * ntl * 16 * TPP));
+  CK(dalloc(&ctx->d_part4, S * nT2 * TP * 4));
+  CK(dalloc(&ctx->d_partR, S * nT2 * TP));
+  CK(dalloc(&ctx->d_pm, S * ctx->Lp * 4));
+  CK(dalloc(&ctx->d_meanp, S * 4));
+  CK(dalloc(&ctx->d_ps, S * ctx->Lp * 5));
+  CK(dalloc(&ctx->d_cov, S * MAXOUT * ntl * TPP));
+  CK(dalloc(&ctx->d_part1, S * MAXOUT * nT2 * TP));
+  CK(dalloc(&ctx->d_colx, S * MAXOUT * ctx->Lp));
+  CK(dalloc(&ctx->d_avg, S * MAXOUT));
+  CK(dalloc(&ctx->d_tmin, S * MAXOUT * ntl));
+  CK(dalloc(&ctx->d_tmax, S * MAXOUT * ntl));
+  CK(dalloc(&ctx->d_mm, S * MAXOUT * 2));
+  CK(dalloc(&ctx->d_status, 1));
+  CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
+  CK(dalloc(&ctx->d_nhits, 1));
+  if (maxnull > 0 && N > 1) {
+    CK(dalloc(&ctx->d_fitch, (size_t)maxnull * (N - 1) * ctx->Lp));
+    CK(dalloc(&ctx->d_scratch, (size_t)maxnull * (N - 1) * ctx->Lp));
+  }
+  ctx->err[0] = 0;
+  return 0;
+}
+
+extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->dev);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  void* ptrs[] = {ctx->d_tiles, ctx->d_tile_index, ctx->d_ax, ctx->d_wf, ctx->d_wd, ctx->d_cnt, ctx->d_ucnt,
+                  ctx->d_part4, ctx->d_partR, ctx->d_pm, ctx->d_meanp, ctx->d_ps, ctx->d_cov, ctx->d_cov2,
+                  ctx->d_part1, ctx->d_colx, ctx->d_avg, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status,
+                  ctx->d_left, ctx->d_right, ctx->d_lnodes, ctx->d_fitch, ctx->d_scratch, ctx->d_obs, ctx->d_sf,
+                  ctx->d_tail, ctx->d_nhits, ctx->d_hi, ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->d_full,
+                  ctx->d_flush};
+  for (void* p : ptrs) if (p) cudaFree(p);
+  if (ctx->umma) umma_plan_destroy(ctx->umma);
+  for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+  delete ctx;
+}
+
+extern "C" int covgpu_set_weights(covgpu_ctx* ctx, const double* wgt) {
+  CK(cudaSetDevice(ctx->dev));
+  ctx->h_w.assign(wgt, wgt + ctx->N);
+  std::vector<float> wf(ctx->N);
+  double s = 0.0;
+  for (int i = 0; i < ctx->N; i++) {
+    if (!(wgt[i] >= 0.0) || !std::isfinite(wgt[i])) return fail(ctx, 11, "weight %d is negative or not finite", i);
+    wf[i] = (float)wgt[i];
+    s += wgt[i];
+  }
+  ctx->wtot = s;
+  CK(cudaMemcpyAsync(ctx->d_wd, wgt, ctx->N * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_wf, wf.data(), ctx->N * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (ctx->umma) umma_set_weights(ctx->umma, wgt, ctx->N, ctx->st);
+  ctx->have_w = true;
+  return 0;
+}
+
+extern "C" int covgpu_set_alignment(covgpu_ctx* ctx, int slot, const uint8_t* ax) {
+  if (slot < 0 || slot >= ctx->maxslots) return fail(ctx, 11, "slot %d out of range", slot);
+  CK(cudaSetDevice(ctx->dev));
+  for (int64_t k = 0; k < (int64_t)ctx->N * ctx->L; k++)
+    if (ax[k] > 17) return fail(ctx, 11, "code %d at %lld is not an RNA digital code", ax[k], (long long)k);
+  uint8_t* dst = ctx->d_ax + (size_t)slot * ctx->N * ctx->Lp;
+  CK(cudaMemcpy2DAsync(dst, ctx->Lp, ax, ctx->L, ctx->L, ctx->N, cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return 0;
+}
+
+extern "C" int covgpu_get_alignment(covgpu_ctx* ctx, int slot, uint8_t* ax) {
+  if (slot < 0 || slot >= ctx->maxslots) return fail(ctx, 11, "slot %d out of range", slot);
+  CK(cudaSetDevice(ctx->dev));
+  const uint8_t* src = ctx->d_ax + (size_t)slot * ctx->N * ctx->Lp;
+  CK(cudaMemcpy2DAsync(ax, ctx->L, src, ctx->Lp, ctx->L, ctx->N, cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return 0;
+}
+
+extern "C" int covgpu_set_tree(covgpu_ctx* ctx, const int* parent, const int* left, const int* right) {
+  const int N = ctx->N;
+  CK(cudaSetDevice(ctx->dev));
+  if (N < 2) { ctx->have_tree = false; return 0; }
+  // validate: Easel convention, parent[v] < v, every leaf and node reached once
+  std::vector<int> seen_leaf(N, 0), seen_node(N - 1, 0), depth(N - 1, 0);
+  for (int v = 0; v < N - 1; v++) {
+    const int ch[2] = {left[v], right[v]};
+    for (int k = 0; k < 2; k++) {
+      const int c = ch[k];
+      if (c <= 0) {
+        if (-c >= N || seen_leaf[-c]++) return fail(ctx, 11, "tree: leaf %d repeated or out of range", -c);
+      } else {
+        if (c >= N - 1 || c <= v || seen_node[c]++) return fail(ctx, 11, "tree: node %d has bad child %d", v, c);
+        if (parent && parent[c] != v) return fail(ctx, 11, "tree: parent[%d] != %d", c, v);
+        depth[c] = depth[v] + 1;
+      }
+    }
+  }
+  int maxd = 0;
+  for (int v = 0; v < N - 1; v++) maxd = std::max(maxd, depth[v]);
+  std::vector<int> order;
+  ctx->loff.assign(maxd + 2, 0);
+  for (int d = 0; d <= maxd; d++) {
+    ctx->loff[d] = (int)order.size();
+    for (int v = 0; v < N - 1; v++) if (depth[v] == d) order.push_back(v);
+  }
+  ctx->loff[maxd + 1] = (int)order.size();
+  if (!ctx->d_left) {
+    CK(dalloc(&ctx->d_left, N - 1));
+    CK(dalloc(&ctx->d_right, N - 1));
+    CK(dalloc(&ctx->d_lnodes, N - 1));
+  }
+  CK(cudaMemcpy(ctx->d_left, left, (N - 1) * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_right, right, (N - 1) * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_lnodes, order.data(), (N - 1) * sizeof(int), cudaMemcpyHostToDevice));
+  ctx->have_tree = true;
+  return 0;
+}
+
+static int make_nulls_async(covgpu_ctx* ctx, uint64_t seed, int first_null, int nnull, int first_slot) {
+  if (nnull <= 0) return 0;
+  if (!ctx->have_tree) return fail(ctx, 11, "no tree set");
+  if (nnull > ctx->maxnull) return fail(ctx, 11, "%d nulls > capacity %d", nnull, ctx->maxnull);
+  if (first_slot < 1 || first_slot + nnull > ctx->maxslots) return fail(ctx, 11, "null slots out of range");
+  if (ctx->L > 48 * 1024) return fail(ctx, 11, "alignment longer than 49152 columns");
+  NullTree T{ctx->N, ctx->d_left, ctx->d_right};
+  const int64_t sstride = (int64_t)ctx->N * ctx->Lp;
+  CK(launch_nullgen(ctx->d_ax, ctx->N, ctx->L, ctx->Lp, T, ctx->d_lnodes, ctx->loff.data(),
+                    (int)ctx->loff.size() - 1, seed, (uint32_t)first_null, nnull, ctx->d_fitch, ctx->d_scratch,
+                    ctx->d_ax + first_slot * sstride, sstride, ctx->st));
+  ctx->nlaunch += 2 + (int)ctx->loff.size() - 1;
+  return 0;
+}
+
+extern "C" int covgpu_make_nulls(covgpu_ctx* ctx, uint64_t seed, int first_null, int nnull, int first_slot) {
+  CK(cudaSetDevice(ctx->dev));
+  int s = make_nulls_async(ctx, seed, first_null, nnull, first_slot);
+  if (s) return s;
+  CK(cudaStreamSynchronize(ctx->st));
+  return 0;
+}
+
+// ------------------------------------------------------------------------
+// scoring
+// ------------------------------------------------------------------------
+static int stat_index(int base) {
+  switch (base) {
+    case 0: return 0;    // CHI
+    case 3: return 1;    // GT
+    case 6: return 2;    // MI
+    case 9: return 3;    // MIr
+    case 12: return 4;   // MIg
+    case 15: return 5;   // OMES
+    case 18: return 6;   // RAF
+    case 21: return 6;   // RAFS (RAF, then the stencil)
+    case 24: return 8;   // CCF
+  }
+  return -1;
+}
+
+static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const int* types, int covclass,
+                       int nseqthresh, int alenthresh, const double* allow, int counter) {
+  if (ntypes < 1 || ntypes > MAXOUT) return fail(ctx, 11, "1..%d covariation types per call", MAXOUT);
+  if (first < 0 || nslots < 1 || first + nslots > ctx->maxslots) return fail(ctx, 11, "slots out of range");
+  if (!ctx->have_w) return fail(ctx, 11, "weights not set");
+  const int N = ctx->N, L = ctx->L, Lp = ctx->Lp, nT = ctx->nT, ntiles = ctx->ntiles;
+  bool need_w = false, need_u = false;
+  unsigned mask = 0;
+  StatsArgs A;
+  memset(&A, 0, sizeof(A));
+  CorrTypes ct;
+  ct.nout = ntypes;
+  int rafs_q[MAXOUT], nrafs = 0;
+  int cls = covclass;
+  if (cls == 3) cls = (N <= nseqthresh || L <= alenthresh) ? 1 : 0;
+  for (int q = 0; q < ntypes; q++) {
+    if (types[q] < 0 || types[q] >= 27) return fail(ctx, 11, "covariation type %d not supported", types[q]);
+    const int base = (types[q] / 3) * 3, corr = types[q] % 3;
+    const int si = stat_index(base);
+    A.outstat[q] = si;
+    ct.act[q] = (corr == 0) ? -1 : corr - 1;
+    if (base == 18 || base == 21) { need_u = true; mask |= S_RAF; }
+    else { need_w = true; mask |= (1u << si); }
+    if (base == 24) mask |= S_CCF;
+    if (base == 21) rafs_q[nrafs++] = q;
+    if (cls == 2 && base != 3 && base != 18 && base != 21 && base != 24)
+      return fail(ctx, 11, "class CWC is only defined for GT");
+  }
+  for (int q = ntypes; q < MAXOUT; q++) { A.outstat[q] = 0; ct.act[q] = -1; }
+  const int64_t sstride = (int64_t)N * Lp;
+  const uint8_t* ax = ctx->d_ax + first * sstride;
+  const int64_t cstride = (int64_t)ntiles * 16 * TPP;
+  if (need_w) {
+    cudaEventRecord(ctx->ev[4], ctx->st);
+    if (counter == COVGPU_COUNT_TENSOR) {
+      if (!ctx->umma) {
+        ctx->umma = umma_plan_create(N, L, Lp, ctx->nT, ctx->d_tiles, ntiles, ctx->maxslots);
+        if (!ctx->umma) return fail(ctx, 12, "tensor counting not available for this shape");
+        umma_set_weights(ctx->umma, ctx->h_w.data(), N, ctx->st);
+      }
+      CK(umma_count(ctx->umma, ax, sstride, nslots, false, ctx->d_cnt, ctx->st));
+    } else {
+      CK(launch_count_simt(ax, sstride, ctx->d_wf, false, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_cnt, ctx->st));
+    }
+    cudaEventRecord(ctx->ev[5], ctx->st);
+    ctx->counted = true;
+    CK(launch_pair_marg(ctx->d_cnt, L, ctx->d_tiles, ntiles, nT, nslots, ctx->d_part4, ctx->d_partR, ctx->st));
+    CK(launch_pm_final(ctx->d_part4, ctx->d_partR, L, Lp, nT, nslots, ctx->d_pm, ctx->d_ps, ctx->d_meanp,
+                       ctx->d_status, ctx->st));
+    ctx->nlaunch += 4;
+  }
+  if (need_u) {
+    if (!ctx->d_ucnt) CK(dalloc(&ctx->d_ucnt, (size_t)ctx->maxslots * cstride));
+    if (counter == COVGPU_COUNT_TENSOR && ctx->umma) {
+      CK(umma_count(ctx->umma, ax, sstride, nslots, true, ctx->d_ucnt, ctx->st));
+    } else {
+      CK(launch_count_simt(ax, sstride, ctx->d_wf, true, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_ucnt, ctx->st));
+    }
+    ctx->nlaunch += 1;
+  }
+  A.cnt = need_w ? ctx->d_cnt : nullptr;
+  A.ucnt = need_u ? ctx->d_ucnt : nullptr;
+  A.pm = ctx->d_pm;
+  A.meanp = ctx->d_meanp;
+  A.cov = ctx->d_cov;
+  A.part1 = ctx->d_part1;
+  A.tiles = ctx->d_tiles;
+  A.ntiles = ntiles; A.nT = nT; A.L = L; A.Lp = Lp; A.N = N;
+  A.wtot = ctx->wtot;
+  A.stats = mask;
+  A.cls = cls;
+  A.nout = ntypes;
+  for (int k = 0; k < 16; k++) A.allow[k] = (float)allow[k];
+  if (!need_w) {
+    // RAF only: pm is never read, but keep the pointers valid
+    CK(cudaMemsetAsync(ctx->d_pm, 0, (size_t)nslots * Lp * 4 * sizeof(double), ctx->st));
+  }
+  CK(launch_stats(A, nslots, ctx->st));
+  ctx->nlaunch += 1;
+  const int64_t plane = (int64_t)ntiles * TPP;
+  const int64_t pplane = (int64_t)nT * nT * TP;
+  for (int r = 0; r < nrafs; r++) {
+    const int q = rafs_q[r];
+    if (!ctx->d_cov2) CK(dalloc(&ctx->d_cov2, (size_t)ctx->maxslots * plane));
+    CK(cudaMemcpy2DAsync(ctx->d_cov2, plane * sizeof(double), ctx->d_cov + q * plane, ntypes * plane * sizeof(double),
+                         plane * sizeof(double), nslots, cudaMemcpyDeviceToDevice, ctx->st));
+    CK(launch_rafs(ctx->d_cov2, ctx->d_cov + q * plane, plane, ntypes * plane, ctx->d_tiles, ctx->d_tile_index, ntiles,
+                   nT, L, nslots, ctx->d_part1 + q * pplane, ntypes * pplane, ctx->st));
+    ctx->nlaunch += 1;
+  }
+  CK(launch_apc(ctx->d_cov, ctx->d_part1, ctx->d_colx, ctx->d_avg, ct, ctx->d_tiles, ntiles, nT, L, Lp,
+                nslots * ntypes, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status, ctx->st));
+  ctx->nlaunch += 4;
+  ctx->last_nout = ntypes; ctx->last_first = first; ctx->last_nslots = nslots;
+  return 0;
+}
+
+static int check_status(covgpu_ctx* ctx) {
+  int s = 0;
+  CK(cudaMemcpyAsync(&s, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (s) {
+    cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->st);
+    if (s == 2) return fail(ctx, 20, "marginal probabilities failed validation");
+    if (s == 3) return fail(ctx, 21, "bad covariation: NaN after correction");
+    if (s == 4) return fail(ctx, 22, "histogram bin out of range");
+    return fail(ctx, 23, "device status %d", s);
+  }
+  return 0;
+}
+
+extern "C" int covgpu_score(covgpu_ctx* ctx, int first_slot, int nslots, int ntypes, const int* covtypes,
+                            int covclass, int nseqthresh, int alenthresh, const double* allow, int counter,
+                            double* minmax) {
+  CK(cudaSetDevice(ctx->dev));
+  int s = score_async(ctx, first_slot, nslots, ntypes, covtypes, covclass, nseqthresh, alenthresh, allow, counter);
+  if (s) return s;
+  if (minmax)
+    CK(cudaMemcpyAsync(minmax, ctx->d_mm, (size_t)nslots * ntypes * 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return check_status(ctx);
+}
+
+extern "C" int covgpu_get_cov(covgpu_ctx* ctx, int slot, int which, double* COV) {
+  CK(cudaSetDevice(ctx->dev));
+  const int rel = slot - ctx->last_first;
+  if (rel < 0 || rel >= ctx->last_nslots || which < 0 || which >= ctx->last_nout)
+    return fail(ctx, 11, "no scores for slot %d / type %d", slot, which);
+  if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->L * ctx->L));
+  const int64_t plane = (int64_t)ctx->ntiles * TPP;
+  CK(launch_untile(ctx->d_cov + ((int64_t)rel * ctx->last_nout + which) * plane, ctx->d_tiles, ctx->ntiles, ctx->L,
+                   -INFINITY, ctx->d_full, ctx->st));
+  CK(cudaMemcpyAsync(COV, ctx->d_full, (size_t)ctx->L * ctx->L * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return 0;
+}
+
+extern "C" int covgpu_get_probs(covgpu_ctx* ctx, int slot, const double* wgt, double* pp, double* nseff,
+                                double* ngap, double* pm, double* ps) {
+  CK(cudaSetDevice(ctx->dev));
+  const int rel = slot - ctx->last_first;
+  if (rel < 0 || rel >= ctx->last_nslots) return fail(ctx, 11, "slot %d was not scored", slot);
+  const int L = ctx->L, Lp = ctx->Lp, N = ctx->N;
+  if (pm) {
+    std::vector<double> t((size_t)Lp * 4);
+    CK(cudaMemcpyAsync(t.data(), ctx->d_pm + (size_t)rel * Lp * 4, t.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    memcpy(pm, t.data(), (size_t)L * 4 * sizeof(double));
+  }
+  if (ps) {
+    CK(launch_ps(ctx->d_ax + (size_t)slot * N * Lp, (int64_t)N * Lp, ctx->d_wd, N, L, Lp, 1, ctx->d_ps, ctx->st));
+    std::vector<double> t((size_t)Lp * 5);
+    CK(cudaMemcpyAsync(t.data(), ctx->d_ps, t.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    memcpy(ps, t.data(), (size_t)L * 5 * sizeof(double));
+  }
+  if (pp || nseff || ngap) {
+    const size_t ntl = ctx->ntiles;
+    std::vector<float> c(ntl * 16 * TPP);
+    CK(cudaMemcpyAsync(c.data(), ctx->d_cnt + (size_t)rel * ntl * 16 * TPP, c.size() * sizeof(float),
+                       cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    double wt = 0.0;
+    for (int s = 0; s < N; s++) wt += wgt ? wgt[s] : ctx->h_w[s];
+    std::vector<TileRC> tiles(ntl);
+    CK(cudaMemcpy(tiles.data(), ctx->d_tiles, ntl * sizeof(TileRC), cudaMemcpyDeviceToHost));
+    if (nseff) for (int64_t k = 0; k < (int64_t)L * L; k++) nseff[k] = 0.0;
+    if (ngap) for (int64_t k = 0; k < (int64_t)L * L; k++) ngap[k] = 0.0;
+    if (pp) for (int64_t k = 0; k < (int64_t)L * L * 16; k++) pp[k] = 0.0;
+    for (size_t t = 0; t < ntl; t++)
+      for (int p = 0; p < TPP; p++) {
+        const int i = tiles[t].I * TP + p / TP, j = tiles[t].J * TP + p % TP;
+        if (!(i < j && j < L)) continue;
+        double C[16], ne = 0.0, sum = 0.0;
+        for (int q = 0; q < 16; q++) { C[q] = c[(t * 16 + q) * TPP + p]; ne += C[q]; }
+        if (nseff) nseff[(int64_t)i * L + j] = nseff[(int64_t)j * L + i] = ne;
+        if (ngap) ngap[(int64_t)i * L + j] = wt - ne;
+        if (pp) {
+          for (int q = 0; q < 16; q++) sum += 1e-10 + C[q];
+          for (int x = 0; x < 4; x++)
+            for (int y = 0; y < 4; y++) {
+              const double v = (1e-10 + C[x * 4 + y]) / sum;
+              pp[((int64_t)i * L + j) * 16 + x * 4 + y] = v;
+              pp[((int64_t)j * L + i) * 16 + y * 4 + x] = v;
+            }
+        }
+      }
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------------------
+// the whole per-alignment path
+// ------------------------------------------------------------------------
+static double elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return (double)ms;
+}
+
+static int bins_for(double bmin, double bmax, double w) {
+  int nb = (int)((bmax - bmin) / w);
+  return nb < 1 ? 1 : nb;
+}
+
+extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint8_t* ax, const double* wgt,
+                             int ntypes, const int* covtypes, covgpu_result* results, covgpu_hit* hits, int hitcap) {
+  CK(cudaSetDevice(ctx->dev));
+  const int N = ctx->N, L = ctx->L;
+  const int64_t P = (int64_t)L * (L - 1) / 2;
+  if (ntypes < 1 || ntypes > MAXOUT) return fail(ctx, 11, "1..%d covariation types per call", MAXOUT);
+  for (int q = 0; q < ntypes; q++) {
+    memset(&results[q], 0, sizeof(covgpu_result));
+    results[q].covtype = covtypes[q];
+  }
+  ctx->nlaunch = 0;
+  ctx->counted = false;
+  ctx->fit_ms = 0.0;
+  int s;
+  // ax / wgt == NULL: use the alignment and weights already on the device
+  if (wgt && (s = covgpu_set_weights(ctx, wgt))) return s;
+  if (ax && (s = covgpu_set_alignment(ctx, 0, ax))) return s;
+  if (!ctx->have_w) return fail(ctx, 11, "weights not set");
+  int ns = p->nshuffle;
+  double fracfit = p->fracfit;
+  if (ns < 0) {   // src/R-scape.c:2449-2456
+    ns = 20;
+    if ((double)N * L < 1e3) ns = 200;
+    if (L < 50) ns = 200;
+    if (L < 40) ns = 300;
+    if (N < 4) ns = 300;
+  }
+  if ((double)N * L < 1e3) fracfit = 0.3;   // :2458-2459
+  if (N == 1) ns = 0;
+  if (ns > ctx->maxnull || ns + 1 > ctx->maxslots)
+    return fail(ctx, 11, "%d null alignments need maxnull >= %d and maxslots >= %d", ns, ns, ns + 1);
+  CK(cudaEventRecord(ctx->ev[0], ctx->st));
+  if ((s = make_nulls_async(ctx, p->seed, 0, ns, 1))) return s;
+  CK(cudaEventRecord(ctx->ev[1], ctx->st));
+  if ((s = score_async(ctx, 0, ns + 1, ntypes, covtypes, p->covclass, p->nseqthresh, p->alenthresh, p->allow,
+                       p->counter)))
+    return s;
+  CK(cudaEventRecord(ctx->ev[2], ctx->st));
+  std::vector<double> mm((size_t)(ns + 1) * ntypes * 2);
+  CK(cudaMemcpyAsync(mm.data(), ctx->d_mm, mm.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if ((s = check_status(ctx))) return s;
+  auto MMn = [&](int slot, int q, int k) { return mm[((size_t)slot * ntypes + q) * 2 + k]; };
+
+  const int64_t plane = (int64_t)ctx->ntiles * TPP;
+  if (hitcap > 0 && ctx->hitcap < hitcap) {
+    cudaFree(ctx->d_hi); cudaFree(ctx->d_hj); cudaFree(ctx->d_hsc); cudaFree(ctx->d_hE); cudaFree(ctx->d_hp);
+    CK(dalloc(&ctx->d_hi, hitcap)); CK(dalloc(&ctx->d_hj, hitcap));
+    CK(dalloc(&ctx->d_hsc, hitcap)); CK(dalloc(&ctx->d_hE, hitcap)); CK(dalloc(&ctx->d_hp, hitcap));
+    ctx->hitcap = hitcap;
+  }
+  for (int q = 0; q < ntypes; q++) {
+    covgpu_result& R = results[q];
+    R.nshuffle = ns;
+    R.minCOV = MMn(0, q, 0); R.maxCOV = MMn(0, q, 1);
+    if (N == 1) { R.status = 2; continue; }
+    // calculate_width_histo (src/R-scape.c:1353-1360) on the first null
+    double w = p->w0;
+    const double nmin = MMn(1, q, 0), nmax = MMn(1, q, 1);
+    R.null_minCOV = nmin; R.null_maxCOV = nmax;
+    if (nmax <= p->bmin) return fail(ctx, 30, "bmin %f should be larger than maxCOV %f", p->bmin, nmax);
+    const double wn = (nmax - std::max(p->bmin, nmin)) / (double)p->hpts;
+    w = std::min(w, wn);
+    if (w < p->tol) w = 0.0;
+    R.w = w;
+    if (w < 1e-20) { R.status = 1; continue; }   // src/covariation.c:348-374
+    // null histograms share bmin and w: their sum is the cumulative null
+    int nbcum = 0;
+    double xmin = INFINITY, xmax = -INFINITY;
+    for (int k = 1; k <= ns; k++) {
+      double bmax = MMn(k, q, 1) + 5 * w;
+      while (fabs(bmax - p->bmin) < p->tol) bmax += w;
+      nbcum = std::max(nbcum, bins_for(p->bmin, bmax, w));
+      xmin = std::min(xmin, std::max(MMn(k, q, 0), p->bmin + w));
+      xmax = std::max(xmax, std::max(MMn(k, q, 1), p->bmin + w));
+    }
+    double bmax_r = R.maxCOV + 5 * w;
+    while (fabs(bmax_r - p->bmin) < p->tol) bmax_r += w;
+    const int nb_real = bins_for(p->bmin, bmax_r, w);
+    if (ctx->nbcap < nbcum) {
+      if (ctx->d_obs) cudaFree(ctx->d_obs);
+      CK(dalloc(&ctx->d_obs, nbcum));
+      ctx->nbcap = nbcum;
+    }
+    CK(cudaMemsetAsync(ctx->d_obs, 0, (size_t)nbcum * sizeof(unsigned long long), ctx->st));
+    CK(launch_hist(ctx->d_cov + ((int64_t)1 * ntypes + q) * plane, ntypes * plane, ctx->d_tiles, ctx->ntiles, L, ns,
+                   p->bmin, w, nbcum, ctx->d_obs, ctx->d_status, ctx->st));
+    ctx->nlaunch += 1;
+    std::vector<uint64_t> obs(nbcum);
+    CK(cudaMemcpyAsync(obs.data(), ctx->d_obs, nbcum * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if ((s = check_status(ctx))) return s;
+    double bmax_c = p->bmin + nbcum * w;
+    ESL_HISTOGRAM* h = covh_Create(p->bmin, bmax_c, w);
+    if (!h) return fail(ctx, 5, "out of host memory");
+    if (h->nb != nbcum) {   // guard the rounding of (bmax - bmin)/w
+      free(h->obs); h->nb = nbcum; h->obs = (uint64_t*)calloc(nbcum, sizeof(uint64_t));
+    }
+    uint64_t tot = 0;
+    int imin = nbcum, imax = -1;
+    for (int b = 0; b < nbcum; b++) {
+      h->obs[b] = obs[b]; tot += obs[b];
+      if (obs[b]) { imin = std::min(imin, b); imax = std::max(imax, b); }
+    }
+    h->n = (uint64_t)ns * (uint64_t)P; h->Nc = tot; h->No = tot;
+    h->xmin = xmin; h->xmax = xmax; h->imin = imin; h->imax = imax; h->cmin = imin;
+    if (h->nb < nb_real) {   // src/covariation.c:462-466
+      h->obs = (uint64_t*)realloc(h->obs, sizeof(uint64_t) * nb_real);
+      for (int b = h->nb; b < nb_real; b++) h->obs[b] = 0;
+      h->nb = nb_real;
+    }
+    const double pmass = covh_pmass(h, p->pmass, fracfit);
+    if (std::isnan(pmass)) { covh_Destroy(h); return fail(ctx, 31, "bad null histogram fit, pmass is nan"); }
+    double* sf = nullptr;
+    double newmass = 0, mu = 0, lambda = 0, tau = 0;
+    char eb[256];
+    auto tf0 = std::chrono::steady_clock::now();
+    int fs = p->doexpfit ? cov_NullFitExponential(h, &sf, pmass, &newmass, &mu, &lambda, 0, eb)
+                         : cov_NullFitGamma(h, &sf, pmass, &newmass, &mu, &lambda, &tau, 0, eb);
+    ctx->fit_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tf0).count();
+    if (getenv("COVGPU_DEBUG"))
+      fprintf(stderr, "covgpu: type %d nb %d tail bins %d fit %.2f ms mu %g lambda %g tau %g\n", covtypes[q], h->nb,
+              h->imax - h->cmin + 1, ctx->fit_ms, mu, lambda, tau);
+    if (fs) { covh_Destroy(h); free(sf); return fail(ctx, 32, "%s", eb); }
+    R.pmass = pmass; R.newmass = newmass; R.mu = mu; R.lambda = lambda; R.tau = tau;
+    R.Nt = (uint64_t)P;
+    R.sc_thresh = covh_evalue2cov(p->thresh, (double)P, h, sf);
+    R.h_bmin = h->bmin; R.h_w = h->w; R.h_nb = h->nb; R.h_imin = h->imin; R.h_imax = h->imax; R.h_cmin = h->cmin;
+    R.h_n = h->n; R.h_Nc = h->Nc; R.h_No = h->No; R.h_xmin = h->xmin; R.h_xmax = h->xmax; R.h_phi = h->phi;
+    // cov2evalue tables
+    std::vector<double> tail(h->nb, 0.0);
+    {
+      double c = 0.0;
+      for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tail[b] = c; }
+    }
+    if (ctx->sfcap < 2 * h->nb) {
+      if (ctx->d_sf) cudaFree(ctx->d_sf);
+      if (ctx->d_tail) cudaFree(ctx->d_tail);
+      CK(dalloc(&ctx->d_sf, 2 * h->nb));
+      CK(dalloc(&ctx->d_tail, 2 * h->nb));
+      ctx->sfcap = 2 * h->nb;
+    }
+    CK(cudaMemcpyAsync(ctx->d_tail, tail.data(), h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    if (sf) CK(cudaMemcpyAsync(ctx->d_sf, sf, 2 * h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    EvalTables T;
+    T.sf = sf ? ctx->d_sf : nullptr;
+    T.tail = ctx->d_tail;
+    T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = (double)P;
+    T.thresh = p->thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
+    CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
+    CK(launch_evalue(ctx->d_cov + (int64_t)q * plane, ctx->d_tiles, ctx->ntiles, L, T, nullptr, ctx->d_nhits,
+                     ctx->hitcap, ctx->d_hi, ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->st));
+    ctx->nlaunch += 1;
+    int nh = 0;
+    CK(cudaMemcpyAsync(&nh, ctx->d_nhits, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    R.nhit = nh;
+    const int nget = std::min(nh, hitcap);
+    if (nget > 0 && hits) {
+      std::vector<int> hi(nget), hj(nget);
+      std::vector<double> hs(nget), hE(nget), hp(nget);
+      CK(cudaMemcpyAsync(hi.data(), ctx->d_hi, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaMemcpyAsync(hj.data(), ctx->d_hj, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaMemcpyAsync(hs.data(), ctx->d_hsc, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaMemcpyAsync(hE.data(), ctx->d_hE, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaMemcpyAsync(hp.data(), ctx->d_hp, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaStreamSynchronize(ctx->st));
+      covgpu_hit* H = hits + (size_t)q * hitcap;
+      for (int k = 0; k < nget; k++) H[k] = covgpu_hit{hi[k], hj[k], hs[k], hE[k], hp[k]};
+      // the reference lists hits in row-major pair order (src/covariation.c:827-893)
+      std::sort(H, H + nget, [](const covgpu_hit& a, const covgpu_hit& b) {
+        return (a.i != b.i) ? a.i < b.i : a.j < b.j;
+      });
+    }
+    free(sf);
+    covh_Destroy(h);
+  }
+  CK(cudaEventRecord(ctx->ev[3], ctx->st));
+  CK(cudaEventSynchronize(ctx->ev[3]));
+  ctx->tms[0] = elapsed(ctx->ev[0], ctx->ev[1]);
+  ctx->tms[1] = ctx->counted ? elapsed(ctx->ev[4], ctx->ev[5]) : 0.0;
+  ctx->tms[2] = elapsed(ctx->ev[1], ctx->ev[2]);
+  ctx->tms[3] = elapsed(ctx->ev[2], ctx->ev[3]);
+  ctx->tms[4] = elapsed(ctx->ev[0], ctx->ev[3]);
+  return 0;
+}
+
+extern "C" int covgpu_last_timing(const covgpu_ctx* ctx, double* ms5, int* nlaunch) {
+  for (int k = 0; k < 5; k++) ms5[k] = ctx->tms[k];
+  if (nlaunch) *nlaunch = ctx->nlaunch;
+  return 0;
+}
+
+// overwrite a buffer larger than L2 (129 MB) so that the next call starts
+// from a cold cache
+extern "C" int covgpu_flush_l2(covgpu_ctx* ctx) {
+  CK(cudaSetDevice(ctx->dev));
+  const size_t n = (size_t)256 << 20;
+  if (!ctx->d_flush) CK(dalloc(&ctx->d_flush, n));
+  CK(cudaMemsetAsync(ctx->d_flush, ctx->nlaunch & 0xff, n, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return 0;
+}
+
+// ------------------------------------------------------------------------
+// single-matrix operations for the reference-named entry points: the score
+// matrix comes from the host (full L x L, both triangles) or, when NULL, is
+// the device's latest score of slot 0 / type 0.
+// ------------------------------------------------------------------------
+static int upload_full(covgpu_ctx* ctx, const double* COV) {
+  if (!COV) {
+    if (ctx->last_nout < 1 || ctx->last_first != 0) return fail(ctx, 11, "no device score matrix for slot 0");
+    return 0;
+  }
+  if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->L * ctx->L));
+  CK(cudaMemcpyAsync(ctx->d_full, COV, (size_t)ctx->L * ctx->L * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  CK(launch_tile(ctx->d_full, ctx->d_tiles, ctx->ntiles, ctx->L, ctx->d_cov, ctx->st));
+  ctx->last_nout = 1; ctx->last_first = 0; ctx->last_nslots = 1;
+  return 0;
+}
+
+extern "C" int covgpu_correct(covgpu_ctx* ctx, const double* COV, int actype, double* out, double* minmax) {
+  CK(cudaSetDevice(ctx->dev));
+  if (actype != 0 && actype != 1) return fail(ctx, 11, "wrong correction type");
+  int s = upload_full(ctx, COV);
+  if (s) return s;
+  const int nout = ctx->last_nout;
+  // the corrected plane is slot 0 / type 0 of the tile layout
+  CK(launch_tile_rowsums(ctx->d_cov, ctx->d_tiles, ctx->ntiles, ctx->nT, ctx->L, ctx->d_part1, ctx->st));
+  CorrTypes ct;
+  ct.nout = 1; ct.act[0] = actype; ct.act[1] = ct.act[2] = ct.act[3] = -1;
+  CK(launch_apc(ctx->d_cov, ctx->d_part1, ctx->d_colx, ctx->d_avg, ct, ctx->d_tiles, ctx->ntiles, ctx->nT, ctx->L,
+                ctx->Lp, 1, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status, ctx->st));
+  ctx->last_nout = 1;
+  (void)nout;
+  if (minmax) CK(cudaMemcpyAsync(minmax, ctx->d_mm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if ((s = check_status(ctx))) return s;
+  if (out) return covgpu_get_cov(ctx, 0, 0, out);
+  return 0;
+}
+
+extern "C" int covgpu_hist_full(covgpu_ctx* ctx, const double* COV, double bmin, double w, int nb, uint64_t* obs) {
+  CK(cudaSetDevice(ctx->dev));
+  int s = upload_full(ctx, COV);
+  if (s) return s;
+  if (nb < 1 || !(w > 0.0)) return fail(ctx, 11, "bad histogram shape");
+  if (ctx->nbcap < nb) {
+    if (ctx->d_obs) cudaFree(ctx->d_obs);
+    CK(dalloc(&ctx->d_obs, nb));
+    ctx->nbcap = nb;
+  }
+  CK(cudaMemsetAsync(ctx->d_obs, 0, (size_t)nb * sizeof(unsigned long long), ctx->st));
+  CK(launch_hist(ctx->d_cov, 0, ctx->d_tiles, ctx->ntiles, ctx->L, 1, bmin, w, nb, ctx->d_obs, ctx->d_status, ctx->st));
+  CK(cudaMemcpyAsync(obs, ctx->d_obs, (size_t)nb * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return check_status(ctx);
+}
+
+extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void* hv, const double* survfit,
+                                  double Nt, double thresh, double* Eval, covgpu_hit* hits, int hitcap, int* nhit) {
+  CK(cudaSetDevice(ctx->dev));
+  const ESL_HISTOGRAM* h = (const ESL_HISTOGRAM*)hv;
+  int s = upload_full(ctx, COV);
+  if (s) return s;
+  std::vector<double> tail(h->nb, 0.0);
+  double c = 0.0;
+  for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tail[b] = c; }
+  if (ctx->sfcap < 2 * h->nb) {
+    if (ctx->d_sf) cudaFree(ctx->d_sf);
+    if (ctx->d_tail) cudaFree(ctx->d_tail);
+    CK(dalloc(&ctx->d_sf, 2 * h->nb));
+    CK(dalloc(&ctx->d_tail, 2 * h->nb));
+    ctx->sfcap = 2 * h->nb;
+  }
+  CK(cudaMemcpyAsync(ctx->d_tail, tail.data(), h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  if (survfit) CK(cudaMemcpyAsync(ctx->d_sf, survfit, 2 * h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  if (hitcap > 0 && ctx->hitcap < hitcap) {
+    cudaFree(ctx->d_hi); cudaFree(ctx->d_hj); cudaFree(ctx->d_hsc); cudaFree(ctx->d_hE); cudaFree(ctx->d_hp);
+    CK(dalloc(&ctx->d_hi, hitcap)); CK(dalloc(&ctx->d_hj, hitcap));
+    CK(dalloc(&ctx->d_hsc, hitcap)); CK(dalloc(&ctx->d_hE, hitcap)); CK(dalloc(&ctx->d_hp, hitcap));
+    ctx->hitcap = hitcap;
+  }
+  EvalTables T;
+  T.sf = survfit ? ctx->d_sf : nullptr;
+  T.tail = ctx->d_tail;
+  T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = Nt;
+  T.thresh = thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
+  const int64_t plane = (int64_t)ctx->ntiles * TPP;
+  double* evt = nullptr;
+  if (Eval) {
+    if (!ctx->d_cov2) CK(dalloc(&ctx->d_cov2, (size_t)ctx->maxslots * plane));
+    evt = ctx->d_cov2;
+  }
+  CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
+  CK(launch_evalue(ctx->d_cov, ctx->d_tiles, ctx->ntiles, ctx->L, T, evt, ctx->d_nhits, ctx->hitcap, ctx->d_hi,
+                   ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->st));
+  int nh = 0;
+  CK(cudaMemcpyAsync(&nh, ctx->d_nhits, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  if (Eval) {
+    if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->L * ctx->L));
+    CK(launch_untile(evt, ctx->d_tiles, ctx->ntiles, ctx->L, INFINITY, ctx->d_full, ctx->st));
+    CK(cudaMemcpyAsync(Eval, ctx->d_full, (size_t)ctx->L * ctx->L * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  }
+  CK(cudaStreamSynchronize(ctx->st));
+  *nhit = nh;
+  const int nget = std::min(nh, hitcap);
+  if (nget > 0 && hits) {
+    std::vector<int> hi(nget), hj(nget);
+    std::vector<double> hs(nget), hE(nget), hp(nget);
+    CK(cudaMemcpy(hi.data(), ctx->d_hi, nget * sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hj.data(), ctx->d_hj, nget * sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hs.data(), ctx->d_hsc, nget * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hE.data(), ctx->d_hE, nget * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(hp.data(), ctx->d_hp, nget * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < nget; k++) hits[k] = covgpu_hit{hi[k], hj[k], hs[k], hE[k], hp[k]};
+    std::sort(hits, hits + nget, [](const covgpu_hit& a, const covgpu_hit& b) {
+      return (a.i != b.i) ? a.i < b.i : a.j < b.j;
+    });
+  }
+  return 0;
+}

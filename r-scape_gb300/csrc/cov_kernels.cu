@@ -1,0 +1,841 @@
+// cov_kernels.cu -- SIMT kernels of the covariation path (sm_103a).
+//
+//   k_count_simt    weighted (or unit-weight) 4x4 joint counts of every
+//                   column pair: mutual_naive_ppij, src/correlators.c:1695-1780
+//   k_pair_marg     per-tile partial sums of the pair-normalised marginals:
+//                   corr_Marginals, src/correlators.c:1337-1375
+//   k_pm_final      marginals pm and the CCF column means (:1030-1036)
+//   k_ps            single-column frequencies: mutual_naive_psi, :1782-1817
+//   k_stats         CHI/GT/MI/MIr/MIg/OMES (C16, C2, GT-CWC), RAF, CCF per
+//                   pair from the counts (:92-1061) + row/column sums for APC
+//   k_rafs          RAFS stencil on RAF (:935-982)
+//   k_apc_*         corr_CalculateCOVCorrected APC/ASC (:1063-1157)
+//   k_hist          histogram of pair scores (src/covariation.c:414-457)
+//   k_evalue        per-pair E-values and the hit list (:2369-2400, :778-1006)
+//   k_untile        tile-packed scores -> full L x L matrix for the host
+#include "cov_dev.cuh"
+#include "cov_kernels.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+namespace covgpu {
+
+// Easel's bin of x: ceil((x - bmin)/w - 1).  The quotient is first formed
+// with the reciprocal; only when it lies within 1e-9 of an integer (where
+// the last ulp could move the ceiling) is the IEEE division redone, so the
+// bin always equals the one the division gives.
+__device__ __forceinline__ int exact_bin(double x, double bmin, double w, double invw) {
+  double q = (x - bmin) * invw;
+  if (fabs(q - rint(q)) < 1e-9) q = (x - bmin) / w;
+  return (int)ceil(q - 1.0);
+}
+
+// ------------------------------------------------------------------------
+// Counting (plain SIMT path): one CTA per (tile, alignment); 256 threads,
+// each owning a 2x2 block of pairs and 4x16 fp32 accumulators.  Sequences
+// are staged 32 at a time in shared memory as float4 one-hot (i side) and
+// weight-scaled one-hot (j side) vectors; every pair then takes 16 FMAs per
+// sequence.  With unit weights the counts are exact integers (< 2^24).
+// ------------------------------------------------------------------------
+template <bool UNIT>
+__global__ void __launch_bounds__(256, 2)
+k_count_simt(const uint8_t* __restrict__ ax, int64_t slot_stride, const float* __restrict__ w,
+             int N, int Lp, const TileRC* __restrict__ tiles, int ntiles, float* __restrict__ cnt) {
+  __shared__ float4 ohi[32][TP];
+  __shared__ float4 whj[32][TP];
+  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  const uint8_t* A = ax + (int64_t)slot * slot_stride;
+  const int ty = tid >> 4, tx = tid & 15;
+  float acc[4][16];
+#pragma unroll
+  for (int p = 0; p < 4; p++)
+#pragma unroll
+    for (int c = 0; c < 16; c++) acc[p][c] = 0.f;
+
+  for (int s0 = 0; s0 < N; s0 += 32) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int e = tid + 256 * k;          // 0..2047
+      const int half = e >> 10, s = (e >> 5) & 31, c = e & 31;
+      const int seq = s0 + s;
+      int code = 4;
+      float val = 0.f;
+      if (seq < N) {
+        code = A[(int64_t)seq * Lp + (half ? tr.J : tr.I) * TP + c];
+        val = half ? (UNIT ? 1.f : w[seq]) : 1.f;
+      }
+      float4 v;
+      v.x = (code == 0) ? val : 0.f;
+      v.y = (code == 1) ? val : 0.f;
+      v.z = (code == 2) ? val : 0.f;
+      v.w = (code == 3) ? val : 0.f;
+      if (half) whj[s][c] = v; else ohi[s][c] = v;
+    }
+    __syncthreads();
+    const int smax = min(32, N - s0);
+    for (int s = 0; s < smax; s++) {
+      const float4 i0 = ohi[s][2 * ty], i1 = ohi[s][2 * ty + 1];
+      const float4 j0 = whj[s][2 * tx], j1 = whj[s][2 * tx + 1];
+      const float iv[2][4] = {{i0.x, i0.y, i0.z, i0.w}, {i1.x, i1.y, i1.z, i1.w}};
+      const float jv[2][4] = {{j0.x, j0.y, j0.z, j0.w}, {j1.x, j1.y, j1.z, j1.w}};
+#pragma unroll
+      for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+#pragma unroll
+          for (int x = 0; x < 4; x++)
+#pragma unroll
+            for (int y = 0; y < 4; y++) acc[a * 2 + b][x * 4 + y] = fmaf(iv[a][x], jv[b][y], acc[a * 2 + b][x * 4 + y]);
+    }
+    __syncthreads();
+  }
+  float* out = cnt + ((int64_t)slot * ntiles + t) * 16 * TPP;
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int c = 0; c < 16; c++) {
+      float2 v = make_float2(acc[a * 2 + 0][c], acc[a * 2 + 1][c]);
+      *reinterpret_cast<float2*>(out + c * TPP + (2 * ty + a) * TP + 2 * tx) = v;
+    }
+}
+
+// ------------------------------------------------------------------------
+// Block helper for the per-tile kernels: 256 threads, thread tid owns the
+// pairs p = tid + 256k (k = 0..3): row a = (tid >> 5) + 8k, column b = lane.
+// Reduces NV channels of per-pair values into per-row sums (of rv) and
+// per-column sums (of cv) and stores them in the partial layout
+// part[I][J][a][c] (rows of tile (I,J)) and part[J][I][b][c] (columns);
+// a diagonal tile adds both roles into part[I][I].
+// ------------------------------------------------------------------------
+template <int NV>
+__device__ __forceinline__ void tile_rowcol_store2(const double (&rv)[4][NV], const double (&cv)[4][NV],
+                                                   double* __restrict__ part, int nT, int I, int J) {
+  __shared__ double colbuf[8][TP][NV];
+  __shared__ double rowbuf[TP][NV];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+#pragma unroll
+    for (int c = 0; c < NV; c++) {
+      double r = warp_sum_d(rv[k][c]);
+      if (lane == 0) rowbuf[warp + 8 * k][c] = r;
+    }
+#pragma unroll
+  for (int c = 0; c < NV; c++) colbuf[warp][lane][c] = cv[0][c] + cv[1][c] + cv[2][c] + cv[3][c];
+  __syncthreads();
+  if (tid < TP * NV) {
+    const int col = tid / NV, c = tid % NV;
+    double cs = 0.0;
+    for (int wv = 0; wv < 8; wv++) cs += colbuf[wv][col][c];
+    if (I == J) {
+      part[(((int64_t)I * nT + J) * TP + col) * NV + c] = rowbuf[col][c] + cs;
+    } else {
+      part[(((int64_t)I * nT + J) * TP + col) * NV + c] = rowbuf[col][c];
+      part[(((int64_t)J * nT + I) * TP + col) * NV + c] = cs;
+    }
+  }
+  __syncthreads();
+}
+
+template <int NV>
+__device__ __forceinline__ void tile_rowcol_store(const double (&v)[4][NV], double* __restrict__ part, int nT, int I,
+                                                  int J) {
+  tile_rowcol_store2<NV>(v, v, part, nT, I, J);
+}
+
+// Pair-normalised marginal contributions: for every pair with nseff > 0,
+// row i gains (4e-10 + sum_y C(x,y)) / S and column j gains
+// (4e-10 + sum_x C(x,y)) / S, S = 16e-10 + nseff (the prior of
+// src/correlators.c:1713 and the normalisation of :1758).  Also the
+// upper-triangle row sums of nseff for the CCF column means.
+__global__ void __launch_bounds__(256)
+k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ tiles, int ntiles, int nT,
+            double* __restrict__ part4, double* __restrict__ partR) {
+  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  const float* C = cnt + ((int64_t)slot * ntiles + t) * 16 * TPP;
+  double rv[4][4], cv[4][4], nr[4][1], zero[4][1];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    float c[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++) c[q] = C[q * TPP + p];
+    double ne = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; q++) ne += (double)c[q];
+    const bool pair = (i < j) && (j < L);
+    const bool ok = pair && (ne > 0.0);
+    const double invS = ok ? 1.0 / (16e-10 + ne) : 0.0;
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+      rv[k][x] = ok ? (4e-10 + (double)c[x * 4 + 0] + (double)c[x * 4 + 1] + (double)c[x * 4 + 2] + (double)c[x * 4 + 3]) * invS : 0.0;
+      cv[k][x] = ok ? (4e-10 + (double)c[0 * 4 + x] + (double)c[1 * 4 + x] + (double)c[2 * 4 + x] + (double)c[3 * 4 + x]) * invS : 0.0;
+    }
+    nr[k][0] = pair ? ne : 0.0;
+    zero[k][0] = 0.0;
+  }
+  tile_rowcol_store2<4>(rv, cv, part4 + (int64_t)slot * nT * nT * TP * 4, nT, tr.I, tr.J);
+  tile_rowcol_store2<1>(nr, zero, partR + (int64_t)slot * nT * nT * TP, nT, tr.I, tr.J);
+}
+
+// pm[c][x] = normalise(sum over every tile touching column c); one thread
+// per column.  mpc[c][x] = pm[c][x] * (sum_{j>c} nseff[c][j]) feeds the CCF
+// column means (src/correlators.c:1030-1036).
+__global__ void k_pm_final(const double* __restrict__ part4, const double* __restrict__ partR, int L, int Lp, int nT,
+                           double* __restrict__ pm, double* __restrict__ mpc, int* __restrict__ status) {
+  const int slot = blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L) return;
+  const double* P = part4 + (int64_t)slot * nT * nT * TP * 4;
+  const double* R = partR + (int64_t)slot * nT * nT * TP;
+  const int I = c / TP, a = c % TP;
+  double m[4] = {0, 0, 0, 0}, rs = 0.0;
+  for (int K = 0; K < nT; K++) {
+    const double4 v = *reinterpret_cast<const double4*>(P + (((int64_t)I * nT + K) * TP + a) * 4);
+    m[0] += v.x; m[1] += v.y; m[2] += v.z; m[3] += v.w;
+    rs += R[((int64_t)I * nT + K) * TP + a];
+  }
+  const double sum = m[0] + m[1] + m[2] + m[3];
+#pragma unroll
+  for (int x = 0; x < 4; x++) m[x] = (sum != 0.0) ? m[x] / sum : 0.25;
+  if (fabs(m[0] + m[1] + m[2] + m[3] - 1.0) > 1e-6) atomicExch(status, 2);
+#pragma unroll
+  for (int x = 0; x < 4; x++) {
+    pm[((int64_t)slot * Lp + c) * 4 + x] = m[x];
+    mpc[((int64_t)slot * Lp + c) * 4 + x] = rs * m[x];
+  }
+}
+
+__global__ void k_meanp(const double* __restrict__ mpc, int L, int Lp, double* __restrict__ meanp) {
+  const int slot = blockIdx.x;
+  __shared__ double buf[4][256];
+  double acc[4] = {0, 0, 0, 0};
+  for (int c = threadIdx.x; c < L; c += blockDim.x)
+#pragma unroll
+    for (int x = 0; x < 4; x++) acc[x] += mpc[((int64_t)slot * Lp + c) * 4 + x];
+#pragma unroll
+  for (int x = 0; x < 4; x++) buf[x][threadIdx.x] = acc[x];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+#pragma unroll
+      for (int x = 0; x < 4; x++) buf[x][threadIdx.x] += buf[x][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double s = buf[0][0] + buf[1][0] + buf[2][0] + buf[3][0];
+    for (int x = 0; x < 4; x++) meanp[slot * 4 + x] = (s != 0.0) ? buf[x][0] / s : 0.25;
+  }
+}
+
+// ps[c][x], x over the five codes 0..4 (gap included), prior 1e-5.
+__global__ void k_ps(const uint8_t* __restrict__ ax, int64_t slot_stride, const double* __restrict__ w, int N, int L,
+                     int Lp, double* __restrict__ ps) {
+  const int slot = blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= L) return;
+  const uint8_t* A = ax + (int64_t)slot * slot_stride;
+  double q[5] = {1e-5, 1e-5, 1e-5, 1e-5, 1e-5};
+  for (int s = 0; s < N; s++) {
+    const int r = A[(int64_t)s * Lp + c];
+    if (r < 5) q[r] += w[s];
+  }
+  double sum = q[0] + q[1] + q[2] + q[3] + q[4];
+  for (int x = 0; x < 5; x++) ps[((int64_t)slot * Lp + c) * 5 + x] = q[x] / sum;
+}
+
+// ------------------------------------------------------------------------
+// Statistics.  Per cell, o = nseff*pp and e = nseff*pm_i(x)*pm_j(y) are
+// formed in FP64 and their difference u = o - e is kept in FP64; the rest
+// is fp32.  The G-test is summed as 2*sum_e e*g(u/e) (each term >= 0), which
+// equals the reference's 2*sum o*ln(o/e) because sum u = 0 to rounding when
+// every cell enters (pp and pm are normalised); the CWC form, which sums a
+// subset of cells, adds its sum u explicitly.
+// ------------------------------------------------------------------------
+__device__ __forceinline__ float gterm(double u, double e, double o) {
+  const float ef = (float)e;
+  const float d = (float)u / ef;
+  if (d > -0.25f) return ef * gfun(d);
+  return ef * gfun_ratio((float)o / ef);
+}
+
+struct PairOut { double v[NSTAT]; };
+
+__device__ void pair_stats(const StatsArgs& A, const float (&c)[16], const float (&uc)[16], bool have_uc,
+                           const double* pmi, const double* pmj, const double* meanp, double ne, double wtot,
+                           PairOut& out) {
+  const unsigned S = A.stats;
+  const double ngap = wtot - ne;
+  // ---- RAF from unit-weight counts (src/correlators.c:897-925 reduced) ----
+  if ((S & (S_RAF | S_RAFS)) && have_uc) {
+    double nA = 0.0, r[4] = {0, 0, 0, 0}, cc[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int x = 0; x < 4; x++)
+#pragma unroll
+      for (int y = 0; y < 4; y++)
+        if (A.allow[x * 4 + y] > 0.f) { double n = (double)uc[x * 4 + y]; nA += n; r[x] += n; cc[y] += n; }
+    double sr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+    double sc = cc[0] * cc[0] + cc[1] * cc[1] + cc[2] * cc[2] + cc[3] * cc[3];
+    double cij = 0.5 * (2.0 * nA * nA - sr - sc);
+    const double Nd = (double)A.N;
+    cij /= (A.N > 1) ? Nd * (Nd - 1.0) : 1.0;
+    cij *= 2.0;
+    double qij = (Nd - nA) / Nd;
+    out.v[6] = cij - 1.0 * qij;
+  }
+  // ---- CCF (src/correlators.c:1038-1053) ----
+  if (S & S_CCF) {
+    double ccf = 0.0;
+#pragma unroll
+    for (int x = 0; x < 4; x++)
+#pragma unroll
+      for (int y = 0; y < 4; y++) {
+        double cc = (ne * pmi[x] - meanp[x]) * (ne * pmj[y] - meanp[y]);
+        ccf += cc * cc;
+      }
+    out.v[8] = sqrt(ccf);
+  }
+  const unsigned SP = S & (S_CHI | S_GT | S_MI | S_MIr | S_MIg | S_OMES);
+  if (!SP) return;
+
+  if (ne <= 0.0) {
+    // no sequence with both residues canonical: pp = 1/16 (prior only)
+    double mi = 0.0, hh = 0.0;
+    if (A.cls == 0) {
+      for (int x = 0; x < 4; x++)
+        for (int y = 0; y < 4; y++) {
+          const double p = 0.0625;
+          if (pmi[x] > 0.0 && pmj[y] > 0.0) mi += p * (log(p) - log(pmi[x]) - log(pmj[y]));
+          hh -= p * log(p);
+        }
+    } else {
+      double pw = 0, pn = 0, qw = 0, qn = 0;
+      for (int x = 0; x < 4; x++)
+        for (int y = 0; y < 4; y++) {
+          if (A.allow[x * 4 + y] > 0.f) { pw += 0.0625; qw += pmi[x] * pmj[y]; }
+          else                          { pn += 0.0625; qn += pmi[x] * pmj[y]; }
+        }
+      if (pw > 0.0) { mi += pw * (log(pw) - log(qw)); hh -= pw * log(pw); }
+      if (pn > 0.0) { mi += pn * (log(pn) - log(qn)); hh -= pn * log(pn); }
+    }
+    out.v[0] = 0.0; out.v[1] = 0.0; out.v[5] = 0.0;
+    out.v[2] = mi; out.v[3] = (hh > 1e-2) ? mi / hh : 0.0; out.v[4] = mi;
+    return;
+  }
+
+  // pp = (1e-10 + C) / S;  o = ne * pp = (1e-10 + C) * t,  t = ne / S
+  const double Ssum = 16e-10 + ne;
+  const double t = ne / Ssum;
+  if (A.cls == 0 || A.cls == 2) {
+    float gsum = 0.f, chi = 0.f, omes = 0.f, hh = 0.f;
+    double usum = 0.0;
+    const float invne = (float)(1.0 / ne);
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+      const double ax = ne * pmi[x];
+#pragma unroll
+      for (int y = 0; y < 4; y++) {
+        if (A.cls == 2 && !(A.allow[x * 4 + y] > 0.f)) continue;
+        const double o = (1e-10 + (double)c[x * 4 + y]) * t;
+        const double e = ax * pmj[y];
+        const double u = o - e;
+        if (e > 0.0) {
+          const float uf = (float)u;
+          gsum += gterm(u, e, o);
+          chi += uf * uf / (float)e;
+          omes += uf * uf;
+          usum += u;
+        }
+        const float p = (float)o * invne;
+        hh -= (p > 0.f) ? p * logf(p) : 0.f;
+      }
+    }
+    const double gt = (A.cls == 2) ? 2.0 * ((double)gsum + usum) : 2.0 * (double)gsum;
+    const double mi = (double)gsum / ne;
+    out.v[0] = chi;
+    out.v[1] = gt;
+    out.v[2] = mi;
+    out.v[3] = (hh > 1e-2f) ? mi / (double)hh : 0.0;
+    out.v[4] = mi - ngap / ne;
+    out.v[5] = (double)(omes * invne);
+  } else {
+    // C2: allowed / not-allowed merged cells (e.g. src/correlators.c:426-458)
+    double Cw = 0.0, Cn = 0.0, qw = 0.0, qn = 0.0;
+    int nal = 0;
+#pragma unroll
+    for (int x = 0; x < 4; x++)
+#pragma unroll
+      for (int y = 0; y < 4; y++) {
+        if (A.allow[x * 4 + y] > 0.f) { Cw += (double)c[x * 4 + y]; qw += pmi[x] * pmj[y]; nal++; }
+        else                          { Cn += (double)c[x * 4 + y]; qn += pmi[x] * pmj[y]; }
+      }
+    const double ow = (nal * 1e-10 + Cw) * t, on = ((16 - nal) * 1e-10 + Cn) * t;
+    const double ew = ne * qw, en = ne * qn;
+    const double uw = ow - ew, un = on - en;
+    float g = 0.f, chi = 0.f, om = 0.f;
+    if (ew > 0.0) { g += gterm(uw, ew, ow); chi += (float)(uw * uw / ew); om += (float)(uw * uw); }
+    if (en > 0.0) { g += gterm(un, en, on); chi += (float)(un * un / en); om += (float)(un * un); }
+    const double pw = ow / ne, pn = on / ne;
+    double hh = 0.0;
+    hh -= (pw > 0.0) ? pw * (double)logf((float)pw) : 0.0;
+    hh -= (pn > 0.0) ? pn * (double)logf((float)pn) : 0.0;
+    const double mi = (double)g / ne;
+    out.v[0] = chi;
+    out.v[1] = 2.0 * (double)g;
+    out.v[2] = mi;
+    out.v[3] = (hh > 1e-2) ? mi / hh : 0.0;
+    out.v[4] = mi - ngap / ne;
+    out.v[5] = (double)om / ne;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_stats(StatsArgs A) {
+  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+  const TileRC tr = A.tiles[t];
+  const float* C = A.cnt ? A.cnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
+  const float* U = A.ucnt ? A.ucnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
+  const double* pm = A.pm + (int64_t)slot * A.Lp * 4;
+  const double* meanp = A.meanp + slot * 4;
+  double rs[4][MAXOUT];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    const bool valid = (i < j) && (j < A.L);
+    float c[16], uc[16];
+#pragma unroll
+    for (int q = 0; q < 16; q++) { c[q] = C ? C[q * TPP + p] : 0.f; uc[q] = U ? U[q * TPP + p] : 0.f; }
+    double ne = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; q++) ne += (double)c[q];
+    PairOut o;
+#pragma unroll
+    for (int q = 0; q < NSTAT; q++) o.v[q] = 0.0;
+    if (valid) {
+      const int ii = i < A.L ? i : 0, jj = j < A.L ? j : 0;
+      pair_stats(A, c, uc, U != nullptr, pm + ii * 4, pm + jj * 4, meanp, ne, A.wtot, o);
+    }
+#pragma unroll
+    for (int q = 0; q < MAXOUT; q++) {
+      double v = 0.0;
+      if (q < A.nout) v = o.v[A.outstat[q]];
+      rs[k][q] = valid ? v : 0.0;
+      if (q < A.nout) {
+        A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = valid ? v : 0.0;
+      }
+    }
+  }
+  // per-statistic row/column sums for APC/ASC
+  for (int q = 0; q < A.nout; q++) {
+    double v[4][1];
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k][0] = rs[k][q];
+    tile_rowcol_store<1>(v, A.part1 + (((int64_t)slot * A.nout + q) * A.nT * A.nT) * TP, A.nT, tr.I, tr.J);
+  }
+}
+
+// RAFS from the RAF scores (both in tile layout); b_{i-1,j+1}, b_{i+1,j-1}
+__device__ __forceinline__ double tile_get(const double* cov, const int* tile_index, int nT, int i, int j) {
+  const int I = i / TP, J = j / TP;
+  const int t = tile_index[I * nT + J];
+  return cov[(int64_t)t * TPP + (i % TP) * TP + (j % TP)];
+}
+
+__global__ void __launch_bounds__(256)
+k_rafs(const double* __restrict__ raf, double* __restrict__ out, int64_t slot_stride_in, int64_t slot_stride_out,
+       const TileRC* __restrict__ tiles, const int* __restrict__ tile_index, int ntiles, int nT, int L,
+       double* __restrict__ part1, int64_t part_stride) {
+  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  const double* B = raf + slot * slot_stride_in;
+  double v[4][1];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    double r = 0.0;
+    if (i < j && j < L) {
+      r = 2.0 * B[(int64_t)t * TPP + p];
+      if (i > 0 && j < L - 1) r += tile_get(B, tile_index, nT, i - 1, j + 1);
+      if (j > 0 && i < L - 1 && i < j - 2) r += tile_get(B, tile_index, nT, i + 1, j - 1);
+      r *= 0.25;
+    }
+    out[slot * slot_stride_out + (int64_t)t * TPP + p] = r;
+    v[k][0] = r;
+  }
+  tile_rowcol_store<1>(v, part1 + slot * part_stride, nT, tr.I, tr.J);
+}
+
+// COVx[c] = sum_{j != c} COV[c][j] / (L-1), from the tile partials
+__global__ void k_apc_colx(const double* __restrict__ part1, int nT, int L, int Lp, double* __restrict__ colx) {
+  const int sq = blockIdx.y;   // (slot, stat) flattened
+  const double* P = part1 + (int64_t)sq * nT * nT * TP;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L; c += gridDim.x * blockDim.x) {
+    const int I = c / TP, a = c % TP;
+    double s = 0.0;
+    for (int K = 0; K < nT; K++) s += P[((int64_t)I * nT + K) * TP + a];
+    colx[(int64_t)sq * Lp + c] = (L > 1) ? s / ((double)L - 1.0) : s;
+  }
+}
+
+// avg = 2/(L(L-1)) * sum_{i<j} COV = sum_c COVx[c] / L
+__global__ void k_apc_avg(const double* __restrict__ colx, int L, int Lp, double* __restrict__ avg) {
+  const int sq = blockIdx.x;
+  __shared__ double buf[256];
+  double s = 0.0;
+  for (int c = threadIdx.x; c < L; c += blockDim.x) s += colx[(int64_t)sq * Lp + c];
+  buf[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) buf[threadIdx.x] += buf[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) avg[sq] = (L > 1) ? buf[0] * ((double)L - 1.0) / ((double)L * ((double)L - 1.0)) : 0.0;
+}
+
+// COV <- COV - COVx_i COVx_j / avg (APC) or COV - (COVx_i + COVx_j - avg) (ASC);
+// per-tile min/max of the corrected scores.
+__global__ void __launch_bounds__(256)
+k_apc_apply(double* __restrict__ cov, const double* __restrict__ colx, const double* __restrict__ avg, CorrTypes ct,
+            const TileRC* __restrict__ tiles, int ntiles, int L, int Lp, double* __restrict__ tmin,
+            double* __restrict__ tmax, int* __restrict__ status) {
+  const int t = blockIdx.x, sq = blockIdx.y, tid = threadIdx.x;
+  const int actype = ct.act[sq % ct.nout];
+  const TileRC tr = tiles[t];
+  const double A = avg[sq];
+  const double* X = colx + (int64_t)sq * Lp;
+  double* V = cov + ((int64_t)sq * ntiles + t) * TPP;
+  double lo = DBL_MAX, hi = -DBL_MAX;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    if (i < j && j < L) {
+      double v = V[p], r;
+      if (actype == 0)      r = (A != 0.0) ? v - X[i] * X[j] / A : 0.0;
+      else if (actype == 1) r = v - (X[i] + X[j] - A);
+      else                  r = v;
+      if (isnan(r)) atomicExch(status, 3);
+      if (actype >= 0) V[p] = r;
+      lo = fmin(lo, r); hi = fmax(hi, r);
+    }
+  }
+  __shared__ double smin[256], smax[256];
+  smin[tid] = lo; smax[tid] = hi;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (tid < o) { smin[tid] = fmin(smin[tid], smin[tid + o]); smax[tid] = fmax(smax[tid], smax[tid + o]); }
+    __syncthreads();
+  }
+  if (tid == 0) { tmin[(int64_t)sq * ntiles + t] = smin[0]; tmax[(int64_t)sq * ntiles + t] = smax[0]; }
+}
+
+// min/max of the scores of every valid pair (before any correction)
+__global__ void __launch_bounds__(256)
+k_tile_minmax(const double* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L,
+              double* __restrict__ tmin, double* __restrict__ tmax) {
+  const int t = blockIdx.x, sq = blockIdx.y, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  const double* V = cov + ((int64_t)sq * ntiles + t) * TPP;
+  double lo = DBL_MAX, hi = -DBL_MAX;
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    if (i < j && j < L) { lo = fmin(lo, V[p]); hi = fmax(hi, V[p]); }
+  }
+  __shared__ double smin[256], smax[256];
+  smin[tid] = lo; smax[tid] = hi;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (tid < o) { smin[tid] = fmin(smin[tid], smin[tid + o]); smax[tid] = fmax(smax[tid], smax[tid + o]); }
+    __syncthreads();
+  }
+  if (tid == 0) { tmin[(int64_t)sq * ntiles + t] = smin[0]; tmax[(int64_t)sq * ntiles + t] = smax[0]; }
+}
+
+__global__ void k_reduce_minmax(const double* __restrict__ tmin, const double* __restrict__ tmax, int ntiles,
+                                double* __restrict__ mm) {
+  const int sq = blockIdx.x;
+  __shared__ double smin[256], smax[256];
+  double lo = DBL_MAX, hi = -DBL_MAX;
+  for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
+    lo = fmin(lo, tmin[(int64_t)sq * ntiles + t]);
+    hi = fmax(hi, tmax[(int64_t)sq * ntiles + t]);
+  }
+  smin[threadIdx.x] = lo; smax[threadIdx.x] = hi;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+      smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { mm[sq * 2 + 0] = (smin[0] == DBL_MAX) ? INFINITY : smin[0]; mm[sq * 2 + 1] = (smax[0] == -DBL_MAX) ? -INFINITY : smax[0]; }
+}
+
+// Histogram of max(COV, bmin + w) over the valid pairs of several alignments
+// (src/covariation.c:431-432), bins b = ceil((x - bmin)/w - 1).  Each CTA
+// keeps a private histogram in shared memory over a grid-stride range of
+// (tile, alignment) items and adds it to the global one once.
+__global__ void __launch_bounds__(256)
+k_hist(const double* __restrict__ cov, int64_t slot_stride, const TileRC* __restrict__ tiles, int ntiles, int nslots,
+       int L, double bmin, double w, int nbcap, int b0, int nwin, unsigned long long* __restrict__ obs,
+       int* __restrict__ status) {
+  extern __shared__ unsigned int sh[];
+  const int tid = threadIdx.x;
+  for (int b = tid; b < nwin; b += blockDim.x) sh[b] = 0u;
+  __syncthreads();
+  const double lo = bmin + w, invw = 1.0 / w;
+  const int64_t nitems = (int64_t)ntiles * nslots;
+  for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int t = (int)(it % ntiles), slot = (int)(it / ntiles);
+    const TileRC tr = tiles[t];
+    const double* V = cov + slot * slot_stride + (int64_t)t * TPP;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+      const int i = tr.I * TP + a, j = tr.J * TP + b;
+      if (i < j && j < L) {
+        double x = V[p];
+        if (!(x > lo)) x = lo;
+        const int bin = exact_bin(x, bmin, w, invw);
+        if (bin < 0 || bin >= nbcap) atomicExch(status, 4);
+        else if (bin >= b0 && bin < b0 + nwin) atomicAdd(sh + (bin - b0), 1u);
+      }
+    }
+  }
+  __syncthreads();
+  for (int b = tid; b < nwin; b += blockDim.x)
+    if (sh[b]) atomicAdd(obs + b0 + b, (unsigned long long)sh[b]);
+}
+
+// the same with global atomics, for histograms too large for shared memory
+__global__ void __launch_bounds__(256)
+k_hist_global(const double* __restrict__ cov, int64_t slot_stride, const TileRC* __restrict__ tiles, int ntiles, int L,
+              double bmin, double w, int nbcap, unsigned long long* __restrict__ obs, int* __restrict__ status) {
+  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  const double* V = cov + slot * slot_stride + (int64_t)t * TPP;
+  const double lo = bmin + w, invw = 1.0 / w;
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    if (i < j && j < L) {
+      double x = V[p];
+      if (!(x > lo)) x = lo;
+      const int bin = exact_bin(x, bmin, w, invw);
+      if (bin >= 0 && bin < nbcap) atomicAdd(obs + bin, 1ull);
+      else atomicExch(status, 4);
+    }
+  }
+}
+
+// E-value of every pair (cov2evalue at src/covariation.c:2369-2400 with
+// Nc = 1, times the number of tests) and the compacted hit list.
+__global__ void __launch_bounds__(256)
+k_evalue(const double* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L, EvalTables T,
+         double* __restrict__ evt, int* __restrict__ nhits, int hitcap, int* __restrict__ hi, int* __restrict__ hj,
+         double* __restrict__ hsc, double* __restrict__ hE, double* __restrict__ hp) {
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  const double* V = cov + (int64_t)t * TPP;
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    double E = INFINITY;
+    if (i < j && j < L) {
+      const double x = V[p];
+      const int icov = exact_bin(x, T.bmin, T.w, 1.0 / T.w);
+      double pv;
+      if (T.sf && icov >= 2 * T.nb - 1)      pv = T.sf[2 * T.nb - 1];
+      else if (T.sf && x >= T.phi)           pv = T.sf[icov + 1];
+      else if (x >= T.xmax)                  pv = 1.0 / T.Nc;
+      else if (icov <= T.imax) {
+        const int ic = (icov < T.imin) ? T.imin : icov;
+        if (ic >= T.imax - 1) pv = 1.0 / T.Nc;
+        else                  pv = T.tail[ic] / T.Nc;
+      } else pv = INFINITY;
+      E = pv * T.Nt;
+      if (E < T.thresh || T.thresh > 1000.0) {
+        const int h = atomicAdd(nhits, 1);
+        if (h < hitcap) { hi[h] = i; hj[h] = j; hsc[h] = x; hE[h] = E; hp[h] = pv; }
+      }
+    }
+    if (evt) evt[(int64_t)t * TPP + p] = E;
+  }
+}
+
+// tile-packed -> full symmetric L x L (diagonal = diag)
+__global__ void __launch_bounds__(256)
+k_untile(const double* __restrict__ tilev, const TileRC* __restrict__ tiles, int L, double diag,
+         double* __restrict__ full) {
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  __shared__ double s[TP][TP + 1];
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    s[a][b] = tilev[(int64_t)t * TPP + p];
+  }
+  __syncthreads();
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    // upper: row i = I*TP + a, col j = J*TP + b
+    int i = tr.I * TP + a, j = tr.J * TP + b;
+    if (i < L && j < L) {
+      if (i < j) full[(int64_t)i * L + j] = s[a][b];
+      else if (i == j) full[(int64_t)i * L + j] = diag;
+    }
+    // lower: row J*TP + a, col I*TP + b holds s[b][a]
+    i = tr.J * TP + a; j = tr.I * TP + b;
+    if (i < L && j < L && j < i) full[(int64_t)i * L + j] = s[b][a];
+  }
+}
+
+// full symmetric L x L (host layout) -> tile-packed upper triangle
+__global__ void __launch_bounds__(256)
+k_tile(const double* __restrict__ full, const TileRC* __restrict__ tiles, int L, double* __restrict__ tilev) {
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    tilev[(int64_t)t * TPP + p] = (i < j && j < L) ? full[(int64_t)i * L + j] : 0.0;
+  }
+}
+
+// per-tile row/column sums of a tile-packed score matrix (for APC/ASC of a
+// matrix handed in by the caller)
+__global__ void __launch_bounds__(256)
+k_tile_rowsums(const double* __restrict__ tilev, const TileRC* __restrict__ tiles, int nT, int L,
+               double* __restrict__ part1) {
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  double v[4][1];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    v[k][0] = (i < j && j < L) ? tilev[(int64_t)t * TPP + p] : 0.0;
+  }
+  tile_rowcol_store<1>(v, part1, nT, tr.I, tr.J);
+}
+
+// ------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------
+cudaError_t launch_count_simt(const uint8_t* ax, int64_t slot_stride, const float* w, bool unit, int N, int Lp,
+                              const TileRC* tiles, int ntiles, int nslots, float* cnt, cudaStream_t st) {
+  dim3 grid(ntiles, nslots);
+  if (unit) k_count_simt<true><<<grid, 256, 0, st>>>(ax, slot_stride, w, N, Lp, tiles, ntiles, cnt);
+  else      k_count_simt<false><<<grid, 256, 0, st>>>(ax, slot_stride, w, N, Lp, tiles, ntiles, cnt);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_marg(const float* cnt, int L, const TileRC* tiles, int ntiles, int nT, int nslots,
+                             double* part4, double* partR, cudaStream_t st) {
+  k_pair_marg<<<dim3(ntiles, nslots), 256, 0, st>>>(cnt, L, tiles, ntiles, nT, part4, partR);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pm_final(const double* part4, const double* partR, int L, int Lp, int nT, int nslots, double* pm,
+                            double* mpc, double* meanp, int* status, cudaStream_t st) {
+  k_pm_final<<<dim3((L + 127) / 128, nslots), 128, 0, st>>>(part4, partR, L, Lp, nT, pm, mpc, status);
+  k_meanp<<<nslots, 256, 0, st>>>(mpc, L, Lp, meanp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ps(const uint8_t* ax, int64_t slot_stride, const double* w, int N, int L, int Lp, int nslots,
+                      double* ps, cudaStream_t st) {
+  k_ps<<<dim3((L + 127) / 128, nslots), 128, 0, st>>>(ax, slot_stride, w, N, L, Lp, ps);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st) {
+  k_stats<<<dim3(A.ntiles, nslots), 256, 0, st>>>(A);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rafs(const double* raf, double* out, int64_t sin, int64_t sout, const TileRC* tiles,
+                        const int* tile_index, int ntiles, int nT, int L, int nslots, double* part1, int64_t pstride,
+                        cudaStream_t st) {
+  k_rafs<<<dim3(ntiles, nslots), 256, 0, st>>>(raf, out, sin, sout, tiles, tile_index, ntiles, nT, L, part1, pstride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apc(double* cov, const double* part1, double* colx, double* avg, CorrTypes ct, const TileRC* tiles,
+                       int ntiles, int nT, int L, int Lp, int nsq, double* tmin, double* tmax, double* mm,
+                       int* status, cudaStream_t st) {
+  k_apc_colx<<<dim3((L + 255) / 256, nsq), 256, 0, st>>>(part1, nT, L, Lp, colx);
+  k_apc_avg<<<nsq, 256, 0, st>>>(colx, L, Lp, avg);
+  k_apc_apply<<<dim3(ntiles, nsq), 256, 0, st>>>(cov, colx, avg, ct, tiles, ntiles, L, Lp, tmin, tmax, status);
+  k_reduce_minmax<<<nsq, 256, 0, st>>>(tmin, tmax, ntiles, mm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_minmax(const double* cov, const TileRC* tiles, int ntiles, int L, int nsq, double* tmin,
+                          double* tmax, double* mm, cudaStream_t st) {
+  k_tile_minmax<<<dim3(ntiles, nsq), 256, 0, st>>>(cov, tiles, ntiles, L, tmin, tmax);
+  k_reduce_minmax<<<nsq, 256, 0, st>>>(tmin, tmax, ntiles, mm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hist(const double* cov, int64_t slot_stride, const TileRC* tiles, int ntiles, int L, int nslots,
+                        double bmin, double w, int nbcap, unsigned long long* obs, int* status, cudaStream_t st) {
+  // block-private histograms of up to 48K 32-bit counters (192 KB of shared
+  // memory); wider histograms take several windows, beyond 8 windows the
+  // global-atomic kernel
+  const int WIN = 48 * 1024;
+  const int nwin = (nbcap + WIN - 1) / WIN;
+  if (nwin > 8) {
+    k_hist_global<<<dim3(ntiles, nslots), 256, 0, st>>>(cov, slot_stride, tiles, ntiles, L, bmin, w, nbcap, obs, status);
+    return cudaGetLastError();
+  }
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, WIN * 4);
+    attr = true;
+  }
+  int nsm = 152;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, 0);
+  const int64_t items = (int64_t)ntiles * nslots;
+  const int grid = (int)std::min<int64_t>(items, (int64_t)nsm);
+  for (int b0 = 0; b0 < nbcap; b0 += WIN) {
+    const int n = std::min(WIN, nbcap - b0);
+    k_hist<<<grid, 256, (size_t)n * 4, st>>>(cov, slot_stride, tiles, ntiles, nslots, L, bmin, w, nbcap, b0, n, obs,
+                                             status);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_evalue(const double* cov, const TileRC* tiles, int ntiles, int L, const EvalTables& T, double* evt,
+                          int* nhits, int hitcap, int* hi, int* hj, double* hsc, double* hE, double* hp,
+                          cudaStream_t st) {
+  k_evalue<<<ntiles, 256, 0, st>>>(cov, tiles, ntiles, L, T, evt, nhits, hitcap, hi, hj, hsc, hE, hp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile(const double* full, const TileRC* tiles, int ntiles, int L, double* tilev, cudaStream_t st) {
+  k_tile<<<ntiles, 256, 0, st>>>(full, tiles, L, tilev);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_rowsums(const double* tilev, const TileRC* tiles, int ntiles, int nT, int L, double* part1,
+                                cudaStream_t st) {
+  k_tile_rowsums<<<ntiles, 256, 0, st>>>(tilev, tiles, nT, L, part1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_untile(const double* tilev, const TileRC* tiles, int ntiles, int L, double diag, double* full,
+                          cudaStream_t st) {
+  k_untile<<<ntiles, 256, 0, st>>>(tilev, tiles, L, diag, full);
+  return cudaGetLastError();
+}
+
+}  // namespace covgpu

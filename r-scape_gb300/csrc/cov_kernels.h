@@ -1,0 +1,80 @@
+// cov_kernels.h -- launchers of the covariation kernels (internal).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "cov_dev.cuh"
+
+namespace covgpu {
+
+constexpr int MAXOUT = 4;   // score matrices produced by one k_stats launch
+
+struct StatsArgs {
+  const float*  cnt;        // weighted counts  [slot][tile][16][TPP]
+  const float*  ucnt;       // unit-weight counts (RAF) or nullptr
+  const double* pm;         // [slot][Lp][4]
+  const double* meanp;      // [slot][4]
+  double*       cov;        // [slot][nout][tile][TPP]
+  double*       part1;      // [slot][nout][nT][nT][TP]
+  const TileRC* tiles;
+  int           ntiles, nT, L, Lp, N;
+  double        wtot;       // sum of the sequence weights (ngap = wtot - nseff)
+  unsigned      stats;      // StatBit mask of what pair_stats must compute
+  int           cls;        // 0 = C16, 1 = C2, 2 = CWC (GT)
+  int           nout;       // number of output matrices (<= MAXOUT)
+  int           outstat[MAXOUT];  // index into PairOut.v for output q
+  float         allow[16];
+};
+
+// tables of cov2evalue for one null histogram
+struct EvalTables {
+  const double* sf;         // survival fit [2*nb] or nullptr
+  const double* tail;       // tail[b] = sum_{i>=b}^{imax} obs[i]
+  double        bmin, w, phi, xmax, Nc, Nt, thresh;
+  int           nb, imin, imax;
+};
+
+cudaError_t launch_count_simt(const uint8_t* ax, int64_t slot_stride, const float* w, bool unit, int N, int Lp,
+                              const TileRC* tiles, int ntiles, int nslots, float* cnt, cudaStream_t st);
+cudaError_t launch_pair_marg(const float* cnt, int L, const TileRC* tiles, int ntiles, int nT, int nslots,
+                             double* part4, double* partR, cudaStream_t st);
+cudaError_t launch_pm_final(const double* part4, const double* partR, int L, int Lp, int nT, int nslots, double* pm,
+                            double* mpc, double* meanp, int* status, cudaStream_t st);
+cudaError_t launch_ps(const uint8_t* ax, int64_t slot_stride, const double* w, int N, int L, int Lp, int nslots,
+                      double* ps, cudaStream_t st);
+cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st);
+cudaError_t launch_rafs(const double* raf, double* out, int64_t sin, int64_t sout, const TileRC* tiles,
+                        const int* tile_index, int ntiles, int nT, int L, int nslots, double* part1, int64_t pstride,
+                        cudaStream_t st);
+// actype per output q (sq = slot * nout + q): 0 = APC, 1 = ASC, -1 = none
+struct CorrTypes { int act[MAXOUT]; int nout; };
+cudaError_t launch_apc(double* cov, const double* part1, double* colx, double* avg, CorrTypes ct, const TileRC* tiles,
+                       int ntiles, int nT, int L, int Lp, int nsq, double* tmin, double* tmax, double* mm,
+                       int* status, cudaStream_t st);
+cudaError_t launch_tile(const double* full, const TileRC* tiles, int ntiles, int L, double* tilev, cudaStream_t st);
+cudaError_t launch_tile_rowsums(const double* tilev, const TileRC* tiles, int ntiles, int nT, int L, double* part1,
+                                cudaStream_t st);
+cudaError_t launch_minmax(const double* cov, const TileRC* tiles, int ntiles, int L, int nsq, double* tmin,
+                          double* tmax, double* mm, cudaStream_t st);
+cudaError_t launch_hist(const double* cov, int64_t slot_stride, const TileRC* tiles, int ntiles, int L, int nslots,
+                        double bmin, double w, int nbcap, unsigned long long* obs, int* status, cudaStream_t st);
+cudaError_t launch_evalue(const double* cov, const TileRC* tiles, int ntiles, int L, const EvalTables& T, double* evt,
+                          int* nhits, int hitcap, int* hi, int* hj, double* hsc, double* hE, double* hp,
+                          cudaStream_t st);
+cudaError_t launch_untile(const double* tilev, const TileRC* tiles, int ntiles, int L, double diag, double* full,
+                          cudaStream_t st);
+
+// null alignments (cov_null.cu)
+struct NullTree {
+  int        N;
+  const int* left;    // [N-1] device, Easel convention (<= 0: leaf -value)
+  const int* right;   // [N-1] device
+};
+// level_nodes: device list of internal nodes ordered by depth; level_off:
+// host offsets of each depth in that list (nlevels + 1 entries)
+cudaError_t launch_nullgen(const uint8_t* ax, int N, int L, int Lp, const NullTree& T, const int* level_nodes,
+                           const int* level_off, int nlevels, uint64_t seed, uint32_t first_null, int nnull,
+                           uint8_t* fitch, uint8_t* scratch, uint8_t* out_ax, int64_t out_slot_stride,
+                           cudaStream_t st);
+
+}  // namespace covgpu

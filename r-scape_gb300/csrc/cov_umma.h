@@ -1,0 +1,21 @@
+// cov_umma.h -- tensor-core (tcgen05) counting of the pair count tensor.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "cov_dev.cuh"
+
+namespace covgpu {
+
+struct UmmaPlan;
+
+// nullptr when the shape cannot be served by the tensor path
+UmmaPlan*   umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, int ntiles, int maxslots);
+void        umma_plan_destroy(UmmaPlan* p);
+void        umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t st);
+// counts of nslots alignments (slot stride in bytes of the code buffer) into
+// cnt [slot][tile][16][TPP]; unit = unit weights (RAF)
+cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
+                       cudaStream_t st);
+
+}  // namespace covgpu

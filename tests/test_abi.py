@@ -1,0 +1,108 @@
+"""The C-ABI library loads without a GPU and exports every function that
+include/*.h declares (no compute calls here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(path):
+    src = open(path).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = set()
+    for m in re.finditer(r"^\s*(?:extern\s+)?[A-Za-z_][\w\s\*]*?\b([a-z][A-Za-z0-9_]+)\s*\(", src, flags=re.M):
+        name = m.group(1)
+        if name in ("if", "for", "while", "return", "sizeof"):
+            continue
+        names.add(name)
+    return names
+
+
+def test_headers_parse():
+    names = declared(os.path.join(ROOT, "include", "rscape_cov.h"))
+    assert "corr_CalculateGT" in names and "cov_Calculate" in names
+    names = declared(os.path.join(ROOT, "include", "covgpu.h"))
+    assert "covgpu_rscape" in names
+
+
+@pytest.mark.parametrize("header", ["covgpu.h", "rscape_cov.h"])
+def test_every_declared_symbol_is_exported(covgpu, header):
+    lib = ctypes.CDLL(covgpu.LIBPATH)
+    missing = [n for n in sorted(declared(os.path.join(ROOT, "include", header))) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_reference_entry_points_present(covgpu):
+    """The correlators.h / covariation.h names the hot path binds."""
+    lib = ctypes.CDLL(covgpu.LIBPATH)
+    for n in ["corr_Create", "corr_Reuse", "corr_ReuseCOV", "corr_Destroy", "corr_NaivePP", "corr_NaivePS",
+              "corr_Marginals", "corr_Probs", "corr_ValidateProbs", "corr_CalculateCHI", "corr_CalculateCHI_C16",
+              "corr_CalculateCHI_C2", "corr_CalculateOMES", "corr_CalculateOMES_C16", "corr_CalculateOMES_C2",
+              "corr_CalculateGT", "corr_CalculateGT_C16", "corr_CalculateGT_C2", "corr_CalculateGT_CWC",
+              "corr_CalculateMI", "corr_CalculateMI_C16", "corr_CalculateMI_C2", "corr_CalculateMIr",
+              "corr_CalculateMIr_C16", "corr_CalculateMIr_C2", "corr_CalculateMIg", "corr_CalculateMIg_C16",
+              "corr_CalculateMIg_C2", "corr_CalculateRAF", "corr_CalculateRAFS", "corr_CalculateCCF",
+              "corr_CalculateCCF_C16", "corr_CalculateCOVCorrected", "corr_COVTYPEString", "corr_String2COVTYPE",
+              "cov_Calculate", "cov_SignificantPairs_Ranking", "cov_CreateRankList", "cov_GrowRankList",
+              "cov_CreateHitList", "cov_NullFitGamma", "cov_NullFitExponential", "cov_histogram_SetSurvFitTail",
+              "cov_ReadNullHistogram", "cov_WriteNullHistogram", "cov_ranklist_Bin2Bin", "cov_FreeRankList",
+              "cov_FreeHitList"]:
+        assert hasattr(lib, n), n
+
+
+def test_host_utilities_without_gpu(covgpu):
+    """Synthetic alignments, weights and the gap filter are host code."""
+    import numpy as np
+    s = covgpu.Synth(50, 80, 1.5, 12, 2, 6, 6, 0.1, seed=3)
+    assert s.ax.shape == (50, 80) and s.ax.max() <= 4
+    # Easel convention: parent < child for internal nodes, every leaf once
+    leaves = sorted([-c for c in np.concatenate([s.left, s.right]) if c <= 0])
+    assert leaves == list(range(50))
+    for v in range(49):
+        for c in (s.left[v], s.right[v]):
+            if c > 0:
+                assert c > v and s.parent[c] == v
+    assert np.sum(s.ct >= 0) == 24
+    for i in np.nonzero(s.ct >= 0)[0]:
+        assert s.ct[s.ct[i]] == i
+    gap = np.mean(s.ax == 4)
+    assert 0.04 < gap < 0.2
+    w = covgpu.weights_pb(s.ax)
+    assert abs(w.sum() - 50) < 1e-9
+    assert covgpu.gapfilter(s.ax).all()
+
+
+def test_host_weights_match_oracle(covgpu, oracle):
+    s = covgpu.Synth(40, 60, 1.0, 0, 0, 0, 0, 0.1, seed=9)
+    import numpy as np
+    assert np.allclose(covgpu.weights_pb(s.ax), oracle.weights_pb(s.ax), rtol=1e-12)
+    assert np.array_equal(covgpu.gapfilter(s.ax, None, 0.5), oracle.gapfilter(s.ax, None, 0.5))
+
+
+def test_histogram_io_roundtrip(covgpu, tmp_path):
+    """cov_WriteNullHistogram / cov_ReadNullHistogram keep 'score count'
+    lines (src/covariation.c:1717-1867)."""
+    lib = ctypes.CDLL(covgpu.LIBPATH)
+    lib.cov_CreateRankList.restype = ctypes.c_void_p
+    lib.cov_CreateRankList.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    lib.cov_WriteNullHistogram.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+    lib.cov_ReadNullHistogram.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p), ctypes.c_char_p,
+                                          ctypes.c_int]
+    lib.cov_FreeRankList.argtypes = [ctypes.c_void_p]
+    lib.covh_Add.argtypes = [ctypes.c_void_p, ctypes.c_double]
+    r = lib.cov_CreateRankList(20.0, -10.0, 0.5)
+    ha = ctypes.cast(r, ctypes.POINTER(ctypes.c_void_p))[0]
+    for x in (-3.2, 0.1, 0.2, 4.9, 4.9, 17.0):
+        assert lib.covh_Add(ha, x) == 0
+    f = str(tmp_path / "null.his").encode()
+    eb = ctypes.create_string_buffer(256)
+    assert lib.cov_WriteNullHistogram(f, r, eb, 0) == 0
+    r2 = ctypes.c_void_p()
+    assert lib.cov_ReadNullHistogram(f, ctypes.byref(r2), eb, 0) == 0
+    lines = [l.split() for l in open(f.decode())]
+    assert sum(int(c) for s, c in lines) == 6
+    lib.cov_FreeRankList(r)
+    lib.cov_FreeRankList(r2)

@@ -1,0 +1,185 @@
+"""GPU library vs the CPU oracle on the same inputs (needs a GB300).
+
+Tolerances: pair counts and nseff are compared bit-exactly under unit
+weights; probabilities within 1e-12; every statistic within 1e-5 relative,
+|gpu - ref| <= 1e-5 |ref| + a * S with S the largest magnitude of the
+statistic before APC/ASC and a = 2e-7 (unit weights) or 1e-6 (float weights,
+where the SIMT path accumulates in fp32); null alignments byte for byte; the
+E < 0.05 pair set exactly, E-values within 1e-6.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+ATOL_SCALE = 2e-7      # unit weights: counts are exact
+ATOL_SCALE_FP32 = 1e-6  # float weights on the SIMT path: fp32 accumulation
+
+
+def close(gpu, ref, scale=None, atol_scale=ATOL_SCALE):
+    """|gpu - ref| <= RTOL |ref| + ATOL_SCALE * scale, where scale is the
+    largest magnitude of the statistic before any APC/ASC correction (the
+    correction subtracts terms of that size, so rounding scales with it)."""
+    gpu = np.asarray(gpu)
+    ref = np.asarray(ref)
+    if scale is None:
+        scale = np.max(np.abs(ref)) if ref.size else 0.0
+    err = np.abs(gpu - ref)
+    return bool(np.all(err <= RTOL * np.abs(ref) + atol_scale * scale + 1e-300)), float(err.max(initial=0.0))
+
+
+def make(covgpu, N, L, seed, unit=False, tree_kind=1, nbp=None):
+    nbp = nbp if nbp is not None else max(0, min(L // 6, 20))
+    nh = max(1, nbp // 8) if nbp else 0
+    hmin = 1 if nbp else 0
+    s = covgpu.Synth(N, L, 1.5, nbp, nh, hmin, max(1, nbp), 0.1, seed=seed, tree_kind=tree_kind)
+    w = np.ones(N) if unit else covgpu.weights_pb(s.ax) * np.random.default_rng(seed).uniform(0.7, 1.3, N)
+    return s, w
+
+
+SHAPES = [(50, 40), (97, 70), (200, 130), (33, 64), (5, 100), (64, 33)]
+
+
+@pytest.mark.parametrize("N,L", SHAPES)
+def test_counts_unit_weights_bit_exact(covgpu, oracle, N, L):
+    s, w = make(covgpu, N, L, 3, unit=True)
+    e = covgpu.Engine(N, L)
+    e.set_weights(w)
+    e.set_alignment(0, s.ax)
+    e.score(["GT"])
+    pp, ne, ng, pm, ps = e.get_probs(0, w)
+    opp, one, ong, opm, ops = oracle.probs(s.ax, w)
+    iu = np.triu_indices(L, 1)
+    assert np.array_equal(ne[iu], one[iu])
+    assert np.array_equal(ng[iu], ong[iu])
+    assert np.allclose(pp[iu], opp[iu], rtol=1e-14, atol=0)
+    assert np.allclose(pm, opm, rtol=1e-12, atol=1e-15)
+    assert np.allclose(ps, ops, rtol=1e-12, atol=1e-15)
+    e.close()
+
+
+STATS = ["CHI", "GT", "MI", "MIr", "MIg", "OMES", "RAF", "RAFS", "CCF"]
+
+
+@pytest.mark.parametrize("N,L", [(97, 70), (200, 130), (5, 100), (50, 40)])
+@pytest.mark.parametrize("unit", [True, False])
+@pytest.mark.parametrize("corr", ["", "p", "a"])
+def test_statistics(covgpu, oracle, N, L, unit, corr):
+    s, w = make(covgpu, N, L, 5, unit=unit)
+    e = covgpu.Engine(N, L)
+    e.set_weights(w)
+    e.set_alignment(0, s.ax)
+    for k in range(0, len(STATS), 4):
+        types = [t + corr for t in STATS[k:k + 4]]
+        mm = e.score(types)
+        for q, t in enumerate(types):
+            ref, (rmin, rmax) = oracle.cov_calculate(t, s.ax, w)
+            raw, _ = oracle.cov_calculate(t.rstrip("pa") if corr else t, s.ax, w)
+            got = e.get_cov(0, q)
+            iu = np.triu_indices(L, 1)
+            tol = ATOL_SCALE if unit else ATOL_SCALE_FP32
+            ok, err = close(got[iu], ref[iu], np.max(np.abs(raw[iu])), tol)
+            assert ok, "%s N=%d L=%d unit=%s max err %g" % (t, N, L, unit, err)
+            assert np.allclose(got.T[iu], got[iu])
+            ok, _ = close(mm[0, q], [rmin, rmax], np.max(np.abs(raw[iu])), tol)
+            assert ok, (t, mm[0, q], rmin, rmax)
+    e.close()
+
+
+@pytest.mark.parametrize("cls", [0, 1, 2])
+def test_classes(covgpu, oracle, cls):
+    N, L = 120, 90
+    s, w = make(covgpu, N, L, 9)
+    e = covgpu.Engine(N, L)
+    e.set_weights(w)
+    e.set_alignment(0, s.ax)
+    types = ["GTp"] if cls == 2 else ["GTp", "MIp", "CHIp", "OMES"]
+    e.score(types, covclass=cls)
+    for q, t in enumerate(types):
+        ref, _ = oracle.cov_calculate(t, s.ax, w, covclass=cls)
+        raw, _ = oracle.cov_calculate(t.rstrip("p"), s.ax, w, covclass=cls)
+        got = e.get_cov(0, q)
+        iu = np.triu_indices(L, 1)
+        ok, err = close(got[iu], ref[iu], np.max(np.abs(raw[iu])), ATOL_SCALE_FP32)
+        assert ok, (t, cls, err)
+    e.close()
+
+
+@pytest.mark.parametrize("N,L", [(40, 60), (150, 97), (7, 45)])
+def test_null_alignments_identical(covgpu, oracle, N, L):
+    s, w = make(covgpu, N, L, 13)
+    s.ax[0, :5] = 15    # unknown residues take random Fitch states
+    e = covgpu.Engine(N, L, maxslots=4, maxnull=3)
+    e.set_weights(w)
+    e.set_alignment(0, s.ax)
+    e.set_tree(s.parent, s.left, s.right)
+    e.make_nulls(42, 0, 3, 1)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    for q in range(3):
+        ref = oracle.null_msa(s.ax, T, 42, q)
+        got = e.get_alignment(1 + q)
+        assert np.array_equal(got, ref), "null %d differs in %d cells" % (q, int((got != ref).sum()))
+    e.close()
+
+
+@pytest.mark.parametrize("N,L,types", [
+    (200, 120, ["GTp"]),
+    (150, 100, ["GTp", "MIp", "CHIp", "RAFp"]),
+    (60, 45, ["MIa"]),
+])
+def test_rscape_pipeline(covgpu, oracle, N, L, types):
+    s, w = make(covgpu, N, L, 42, nbp=L // 5)
+    ns = 8
+    e = covgpu.Engine(N, L, maxslots=ns + 1, maxnull=ns)
+    e.set_tree(s.parent, s.left, s.right)
+    res = e.rscape(s.ax, w, types, nshuffle=ns)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    for q, t in enumerate(types):
+        ref = oracle.rscape(s.ax, w, T, covtype=t, nshuffle=ns)
+        g = res[q]
+        assert g["status"] == 0
+        assert abs(g["w"] - ref["w"]) <= 1e-9 * abs(ref["w"])
+        for k in ("h_nb", "h_imin", "h_imax", "h_cmin", "h_n", "h_Nc", "h_No"):
+            assert g[k] == ref[k], (t, k, g[k], ref[k])
+        assert abs(g["mu"] - ref["mu"]) < 1e-9
+        assert abs(g["lambda_"] - ref["lambda_"]) <= 1e-6 * abs(ref["lambda_"])
+        assert abs(g["tau"] - ref["tau"]) <= 1e-6 * max(1e-12, abs(ref["tau"]))
+        gh = {(i, j): (sc, E) for (i, j, sc, E, p) in g["hits"]}
+        rh = {(i, j): (sc, E) for (i, j, sc, E, p) in ref["hits"]}
+        assert set(gh) == set(rh), (t, sorted(set(gh) ^ set(rh))[:10])
+        for k in rh:
+            assert abs(gh[k][1] - rh[k][1]) <= 1e-6 * rh[k][1] + 1e-300, (t, k, gh[k], rh[k])
+    e.close()
+
+
+def test_one_sequence(covgpu):
+    s, w = make(covgpu, 2, 40, 1)
+    e = covgpu.Engine(1, 40, maxslots=2, maxnull=1)
+    r = e.rscape(s.ax[:1], np.ones(1), ["GTp"])
+    assert r[0]["status"] == 2 and r[0]["nhit"] == 0
+    e.close()
+
+
+def test_constant_alignment(covgpu):
+    N, L = 30, 40
+    ax = np.zeros((N, L), dtype=np.uint8)
+    s, _ = make(covgpu, N, L, 2)
+    e = covgpu.Engine(N, L, maxslots=6, maxnull=5)
+    e.set_tree(s.parent, s.left, s.right)
+    r = e.rscape(ax, np.ones(N), ["GTp"], nshuffle=5)
+    assert r[0]["status"] == 1 and r[0]["nhit"] == 0
+    e.close()
+
+
+def test_bad_inputs_rejected(covgpu):
+    e = covgpu.Engine(10, 20)
+    with pytest.raises(RuntimeError):
+        e.set_alignment(0, np.full((10, 20), 99, dtype=np.uint8))
+    with pytest.raises(RuntimeError):
+        w = np.ones(10)
+        w[3] = -1.0
+        e.set_weights(w)
+    with pytest.raises(RuntimeError):
+        e.set_tree(np.zeros(9, np.int32), np.zeros(9, np.int32), np.zeros(9, np.int32))
+    e.close()

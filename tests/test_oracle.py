@@ -1,0 +1,154 @@
+"""CPU oracle pinned against the reference's published outputs and against
+published known-answer vectors (no GPU)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def arisong(O):
+    d = np.load(os.path.join(HERE, "golden", "arisong.npz"))
+    ax = d["ax"]
+    use = O.gapfilter(ax, None, 0.75)
+    f = ax[:, use].copy()
+    f[(f > 4) & (f < 15)] = 15
+    f[f > 15] = 4
+    return ax, f, np.nonzero(use)[0]
+
+
+def test_philox_known_answers(oracle):
+    # Random123 known-answer vectors for philox4x32-10
+    assert oracle.philox([0, 0], [0, 0, 0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert oracle.philox([0xFFFFFFFF] * 2, [0xFFFFFFFF] * 4) == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
+
+
+def test_arisong_gap_filter(oracle):
+    gold = json.load(open(os.path.join(HERE, "golden", "arisong_gtp.json")))
+    ax, f, cols = arisong(oracle)
+    assert ax.shape == (gold["nseq"], gold["alen"])
+    assert f.shape[1] == gold["alen_filtered"]
+
+
+def test_arisong_gtp_scores(oracle):
+    """GTp + APC on the gap-filtered Arisong alignment with GSC weights
+    reproduces the tutorial's table (documentation/tutorial.tex:186-212).
+    The weights are a restatement of Easel's GSC, so the pin is 0.06 absolute
+    on scores of 45-122 (10 of the 11 pairs agree to < 4e-3)."""
+    gold = json.load(open(os.path.join(HERE, "golden", "arisong_gtp.json")))
+    ax, f, cols = arisong(oracle)
+    w = oracle.weights_gsc(f)
+    assert abs(w.sum() - f.shape[0]) < 1e-9
+    COV, (mn, mx) = oracle.cov_calculate("GTp", f, w)
+    assert abs(mx - 121.65824) < 0.01
+    errs = []
+    for r in gold["pairs"]:
+        i = int(np.nonzero(cols == r["left"] - 1)[0][0])
+        j = int(np.nonzero(cols == r["right"] - 1)[0][0])
+        errs.append(abs(COV[i, j] - r["score"]))
+    errs = np.array(errs)
+    assert errs.max() < 0.06
+    assert np.sum(errs < 4e-3) >= 10
+    # the table lists the base pairs by decreasing score; ours keep that order
+    sc = []
+    for r in gold["pairs"]:
+        i = int(np.nonzero(cols == r["left"] - 1)[0][0])
+        j = int(np.nonzero(cols == r["right"] - 1)[0][0])
+        sc.append(COV[i, j])
+    assert all(sc[k] > sc[k + 1] for k in range(len(sc) - 1))
+
+
+def test_probs_normalised(oracle):
+    ax, f, cols = arisong(oracle)
+    w = oracle.weights_gsc(f)
+    pp, ne, ng, pm, ps = oracle.probs(f, w)
+    L = f.shape[1]
+    iu = np.triu_indices(L, 1)
+    assert np.allclose(pp[iu].sum(-1), 1.0, atol=1e-12)
+    assert np.allclose(pm.sum(-1), 1.0, atol=1e-12)
+    assert np.allclose(ps.sum(-1), 1.0, atol=1e-12)
+    assert np.allclose(ne[iu] + ng[iu], w.sum(), atol=1e-9)
+    # pp[j][i] is the transpose of pp[i][j]
+    assert np.allclose(pp[3, 7].reshape(4, 4), pp[7, 3].reshape(4, 4).T)
+
+
+def _direct_raf(ax, allow):
+    """RAF from its O(N^2) definition, src/correlators.c:897-925."""
+    N, L = ax.shape
+    A = allow.reshape(4, 4)
+    out = np.zeros((L, L))
+    for i in range(L - 1):
+        for j in range(i + 1, L):
+            ok = np.array([(a < 4 and b < 4 and A[a, b] > 0) for a, b in zip(ax[:, i], ax[:, j])])
+            c = 0.0
+            for s1 in range(N):
+                for s2 in range(s1 + 1, N):
+                    if ok[s1] and ok[s2]:
+                        d = int(ax[s1, i] != ax[s2, i]) + int(ax[s1, j] != ax[s2, j])
+                        c += d
+            q = (N - ok.sum()) / N
+            out[i, j] = 2 * c / (N * (N - 1)) - q
+    return out
+
+
+def test_raf_matches_definition(oracle):
+    rng = np.random.default_rng(3)
+    ax = rng.integers(0, 5, size=(9, 7)).astype(np.uint8)
+    COV, _ = oracle.cov_calculate("RAF", ax, np.ones(9))
+    ref = _direct_raf(ax, oracle.default_allow())
+    iu = np.triu_indices(7, 1)
+    assert np.allclose(COV[iu], ref[iu], atol=1e-12)
+
+
+def test_apc_definition(oracle):
+    rng = np.random.default_rng(5)
+    ax = rng.integers(0, 5, size=(30, 12)).astype(np.uint8)
+    w = rng.uniform(0.5, 1.5, 30)
+    C, _ = oracle.cov_calculate("MI", ax, w)
+    P, _ = oracle.cov_calculate("MIp", ax, w)
+    L = 12
+    off = ~np.eye(L, dtype=bool)
+    colx = np.where(off, C, 0).sum(1) / (L - 1)
+    avg = C[np.triu_indices(L, 1)].sum() * 2 / (L * (L - 1))
+    ref = C - np.outer(colx, colx) / avg
+    assert np.allclose(P[off], ref[off], atol=1e-12)
+
+
+def test_null_preserves_composition(oracle, covgpu):
+    """A null alignment keeps the number of sequences and columns, holds only
+    canonical codes and gaps, and every branch replays exactly the
+    substitution counts of its Fitch reconstruction."""
+    s = covgpu.Synth(40, 60, 1.0, 10, 1, 10, 10, 0.1, seed=7)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    nm = oracle.null_msa(s.ax, T, 42, 3)
+    assert nm.shape == s.ax.shape
+    assert set(np.unique(nm)) <= {0, 1, 2, 3, 4}
+    nm2 = oracle.null_msa(s.ax, T, 42, 3)
+    assert np.array_equal(nm, nm2)
+    nm3 = oracle.null_msa(s.ax, T, 42, 4)
+    assert not np.array_equal(nm, nm3)
+
+
+def test_feistel_is_permutation(oracle):
+    for L in (1, 2, 3, 17, 64, 100, 1000):
+        rk = [0x12345678, 0x9ABCDEF0, 7, 11, 13, 17]
+        p = [oracle.feistel_perm(t, L, rk) for t in range(L)]
+        assert sorted(p) == list(range(L))
+
+
+def test_rscape_pipeline_small(oracle, covgpu):
+    s = covgpu.Synth(200, 120, 1.5, 30, 3, 10, 10, 0.08, seed=42, tree_kind=1)
+    w = oracle.weights_pb(s.ax)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    r = oracle.rscape(s.ax, w, T, covtype="GTp", nshuffle=5)
+    assert r["nshuffle"] == 5
+    assert r["fit_ok"] == 1
+    assert r["h_n"] == 5 * 120 * 119 // 2
+    assert len(r["hits"]) >= 10
+    assert r["null_obs"].sum() == r["h_Nc"]
+    # planted pairs dominate the hit list
+    ct = s.ct
+    planted = sum(1 for (i, j, sc, E, p) in r["hits"] if ct[i] == j)
+    assert planted >= max(1, len(r["hits"]) // 2)
