@@ -849,18 +849,21 @@ exp_surv(double x, double mu, double lambda)
   return exp(-lambda * (x - mu));
 }
 
-/* binned gamma log likelihood over the tail bins [cmin, imax], mu = phi */
+/* binned gamma log likelihood over the tail bins [cmin, imax], mu = phi;
+ * consecutive bins share their common boundary's survival value */
 static double
 gam_binned_nll(const orc_hist_t *h, double mu, double lambda, double tau)
 {
-  double nll = 0.0;
-  int b;
+  double nll = 0.0, s_hi = 0.0;
+  int b, have = 0;
   for (b = h->cmin; b <= h->imax; b++) {
-    double lo, hi, p;
-    if (h->obs[b] == 0) continue;
-    lo = orc_hist_lbound(h, b); if (lo < mu) lo = mu;
-    hi = orc_hist_ubound(h, b);
-    p  = gam_surv(lo, mu, lambda, tau) - gam_surv(hi, mu, lambda, tau);
+    double lo, slo, p;
+    if (h->obs[b] == 0) { have = 0; continue; }
+    lo  = orc_hist_lbound(h, b); if (lo < mu) lo = mu;
+    slo = have ? s_hi : gam_surv(lo, mu, lambda, tau);
+    s_hi = gam_surv(orc_hist_ubound(h, b), mu, lambda, tau);
+    have = 1;
+    p = slo - s_hi;
     if (!(p > 0.0)) p = 1e-300;
     nll -= (double)h->obs[b] * log(p);
   }
@@ -897,8 +900,8 @@ fit_gamma(const orc_hist_t *h, double *ret_mu, double *ret_lambda, double *ret_t
     double c0, c1, r0, r1, fr;
     for (k = 1; k < 3; k++) { if (F[k] < F[lo]) lo = k; if (F[k] > F[hi]) hi = k; }
     md = 3 - lo - hi; if (md == lo || md == hi || md < 0 || md > 2) md = (hi == 0) ? ((lo == 1) ? 2 : 1) : ((hi == 1) ? ((lo == 0) ? 2 : 0) : ((lo == 0) ? 1 : 0));
-    if (fabs(F[hi] - F[lo]) <= 1e-13 * (fabs(F[lo]) + 1e-30) &&
-        fabs(S[hi][0] - S[lo][0]) < 1e-11 && fabs(S[hi][1] - S[lo][1]) < 1e-11) break;
+    if (fabs(F[hi] - F[lo]) <= 1e-12 * (fabs(F[lo]) + 1e-30) &&
+        fabs(S[hi][0] - S[lo][0]) < 1e-9 && fabs(S[hi][1] - S[lo][1]) < 1e-9) break;
     c0 = 0.5 * (S[lo][0] + S[md][0]); c1 = 0.5 * (S[lo][1] + S[md][1]);
     r0 = c0 + (c0 - S[hi][0]); r1 = c1 + (c1 - S[hi][1]);
     fr = gam_binned_nll(h, mu, exp(r0), exp(r1));

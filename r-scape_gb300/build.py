@@ -15,7 +15,7 @@ LIB = os.path.join(HERE, "libcovgpu.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC]
-CFLAGS = ["-O2", "-fPIC", "-std=c11", "-D_DEFAULT_SOURCE", "-Wall", "-I", INC]
+CFLAGS = ["-O2", "-fPIC", "-std=c11", "-fopenmp", "-D_DEFAULT_SOURCE", "-Wall", "-I", INC]
 
 
 def _needs(src, obj, deps):
@@ -54,7 +54,7 @@ def build(verbose=False, force=False):
                 if verbose:
                     print("built", os.path.basename(o))
     if force or jobs or not os.path.exists(LIB):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm", "-Xcompiler", "-fopenmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))

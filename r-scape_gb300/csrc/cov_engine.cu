@@ -382,6 +382,10 @@ static int check_status(covgpu_ctx* ctx) {
   int s = 0;
   CK(cudaMemcpyAsync(&s, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
+  if (ctx->umma) {
+    const int ue = umma_error(ctx->umma);
+    if (ue) return fail(ctx, 24, "tensor counting kernel: barrier wait timed out (code %d)", ue);
+  }
   if (s) {
     cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->st);
     if (s == 2) return fail(ctx, 20, "marginal probabilities failed validation");

@@ -179,21 +179,41 @@ covh_exp_surv(double x, void *params)
   return exp(-p[1] * (x - p[0]));
 }
 
+/* binned negative log likelihood of the tail bins [cmin, imax] with data;
+ * the survival function is evaluated once per needed bin boundary, and the
+ * bins are split into fixed contiguous chunks summed in chunk order, so the
+ * result does not depend on the number of threads */
+#define NLL_CHUNKS 64
 static double
 gam_nll(const ESL_HISTOGRAM *h, double mu, double lambda, double tau)
 {
-  double nll = 0.0, prm[3];
-  int b;
+  double part[NLL_CHUNKS], prm[3], nll = 0.0;
+  const int b0 = h->cmin, nbins = h->imax - h->cmin + 1;
+  int c;
   prm[0] = mu; prm[1] = lambda; prm[2] = tau;
-  for (b = h->cmin; b <= h->imax; b++) {
-    double lo, hi, p;
-    if (h->obs[b] == 0) continue;
-    lo = covh_Bin2LBound(h, b); if (lo < mu) lo = mu;
-    hi = covh_Bin2UBound(h, b);
-    p  = covh_gamma_surv(lo, prm) - covh_gamma_surv(hi, prm);
-    if (!(p > 0.0)) p = 1e-300;
-    nll -= (double)h->obs[b] * log(p);
+  if (nbins <= 0) return 0.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static, 1) if (nbins > 512)
+#endif
+  for (c = 0; c < NLL_CHUNKS; c++) {
+    const int lo_b = b0 + (int)((int64_t)nbins * c / NLL_CHUNKS);
+    const int hi_b = b0 + (int)((int64_t)nbins * (c + 1) / NLL_CHUNKS);
+    double acc = 0.0, s_hi = 0.0;
+    int b, have = 0;
+    for (b = lo_b; b < hi_b; b++) {
+      double lo, slo, p;
+      if (h->obs[b] == 0) { have = 0; continue; }
+      lo = covh_Bin2LBound(h, b); if (lo < mu) lo = mu;
+      slo = have ? s_hi : covh_gamma_surv(lo, prm);
+      s_hi = covh_gamma_surv(covh_Bin2UBound(h, b), prm);
+      have = 1;
+      p = slo - s_hi;
+      if (!(p > 0.0)) p = 1e-300;
+      acc -= (double)h->obs[b] * log(p);
+    }
+    part[c] = acc;
   }
+  for (c = 0; c < NLL_CHUNKS; c++) nll += part[c];
   return nll;
 }
 
@@ -228,8 +248,8 @@ fit_gamma(const ESL_HISTOGRAM *h, double *ret_mu, double *ret_lambda, double *re
     md = 3 - lo - hi;
     if (md == lo || md == hi || md < 0 || md > 2)
       md = (hi == 0) ? ((lo == 1) ? 2 : 1) : ((hi == 1) ? ((lo == 0) ? 2 : 0) : ((lo == 0) ? 1 : 0));
-    if (fabs(F[hi] - F[lo]) <= 1e-13 * (fabs(F[lo]) + 1e-30) &&
-        fabs(S[hi][0] - S[lo][0]) < 1e-11 && fabs(S[hi][1] - S[lo][1]) < 1e-11) break;
+    if (fabs(F[hi] - F[lo]) <= 1e-12 * (fabs(F[lo]) + 1e-30) &&
+        fabs(S[hi][0] - S[lo][0]) < 1e-9 && fabs(S[hi][1] - S[lo][1]) < 1e-9) break;
     c0 = 0.5 * (S[lo][0] + S[md][0]); c1 = 0.5 * (S[lo][1] + S[md][1]);
     r0 = c0 + (c0 - S[hi][0]);       r1 = c1 + (c1 - S[hi][1]);
     fr = gam_nll(h, mu, exp(r0), exp(r1));

@@ -1,16 +1,446 @@
-// cov_umma.cu -- tensor-core counting (placeholder until the tcgen05 kernel
-// lands): the plan reports the path as unavailable.
+// cov_umma.cu -- pair counting on the 5th-generation tensor cores (sm_103a).
+//
+// The 4x4 joint counts of every column pair are the one-hot contraction
+//   C = X^T diag(w) X,   X[s, 4i+x] = [a_si == x]  (x = A,C,G,U; gaps and
+//                                                    unknown residues: 0)
+// of mutual_naive_ppij (src/correlators.c:1695-1780) for all pairs at once.
+// Operands, K-major (sequences contiguous), BF16:
+//   A      = X^T                         (0/1, exact)
+//   B_l    = l_l(s) X^T,  l = 0..nl-1     weight limbs: each weight is
+//            quantised to q_s = round(w_s 2^E) < 2^24 and split into 8-bit
+//            limbs q = l0 + 2^8 l1 + 2^16 l2 (integers <= 255, exact in BF16)
+// Each limb accumulates in its own FP32 TMEM accumulator, where the sum
+// (<= 255 N < 2^24 for N <= 65536) is an exact integer; the epilogue forms
+// C = (D0 + 2^8 D1 + 2^16 D2) 2^-E in FP64, so the counts are exact for the
+// quantised weights (exact integers under unit weights, one limb).
+//
+// Kernel: one CTA per (column tile I <= J, alignment); M = N = 128 (32
+// columns x 4 states each side), K in blocks of 64 sequences.  Warp 0 lane 0
+// issues TMA loads (128B-swizzled boxes) into a 3-4 stage ring guarded by
+// mbarriers, warp 1 lane 0 issues tcgen05.mma (kind::f16, 128x128x16) into
+// TMEM and frees stages with tcgen05.commit; after the last block all four
+// warps read TMEM (tcgen05.ld 32x32b) and write the counts tile in the same
+// layout as the SIMT kernel.  Every wait is bounded: on timeout the kernel
+// records an error code, drains its copies with a bounded wait and frees
+// TMEM before returning.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
 #include "cov_umma.h"
 
 namespace covgpu {
 
-struct UmmaPlan { int dummy; };
+constexpr int UM = 128;          // rows of A tile (32 columns x 4 states)
+constexpr int UN = 128;          // rows of B tile
+constexpr int UK = 64;           // sequences per stage (128 bytes of BF16)
+constexpr int TILE_BYTES = UM * UK * 2;   // 16 KB per operand tile
+constexpr uint64_t WAIT_NS = 2000000000ull;   // every barrier wait gives up after 2 s
 
-UmmaPlan* umma_plan_create(int, int, int, int, const TileRC*, int, int) { return nullptr; }
-void umma_plan_destroy(UmmaPlan* p) { delete p; }
-void umma_set_weights(UmmaPlan*, const double*, int, cudaStream_t) {}
-cudaError_t umma_count(UmmaPlan*, const uint8_t*, int64_t, int, bool, float*, cudaStream_t) {
-  return cudaErrorNotSupported;
+struct UmmaPlan {
+  int N = 0, L = 0, Lp = 0, nT = 0, ntiles = 0, maxslots = 0;
+  int Npad = 0;                  // sequences padded to UK
+  const TileRC* d_tiles = nullptr;
+  __nv_bfloat16* d_ops = nullptr;   // [(1 + 3) * maxslots * 4Lp][Npad]
+  uint8_t* d_limbs = nullptr;       // [3][Npad] weight limbs
+  int nl = 3;                       // limbs in use (1 when all weights are equal)
+  double scale = 1.0;               // count = limb sum * scale
+  CUtensorMap tmap;
+  int* d_err = nullptr;
+  bool prepared_unit = false;
+};
+
+// ---------------------------------------------------------------------------
+// device helpers (inline PTX)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// bounded wait for the phase with the given parity; false after WAIT_NS
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  uint64_t t0 = 0;
+  for (uint32_t it = 0;; it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 255u) == 0) {
+      const uint64_t now = globaltimer();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > WAIT_NS) return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (start address and offsets in 16-byte units)
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);          // start address
+  d |= (uint64_t)1 << 16;                           // leading byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;                 // stride byte offset
+  d |= (uint64_t)1 << 46;                           // descriptor version
+  d |= (uint64_t)2 << 61;                           // SWIZZLE_128B
+  return d;
+}
+
+// instruction descriptor, kind::f16: BF16 x BF16 -> F32, both K-major
+__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
+}
+
+// ---------------------------------------------------------------------------
+// operand preparation: codes [slot][N][Lp] -> BF16 one-hot rows [4Lp][Npad]
+// (A) and limb-scaled rows (B_l); one CTA per (64 sequences, 32 columns, slot)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, int Npad, int nslots, int nl,
+            const uint8_t* __restrict__ limbs, bool unit, __nv_bfloat16* __restrict__ ops) {
+  __shared__ uint8_t cs[64][33];
+  __shared__ uint8_t lb[3][64];
+  const int s0 = blockIdx.x * 64, c0 = blockIdx.y * 32, slot = blockIdx.z, tid = threadIdx.x;
+  const uint8_t* A = ax + (int64_t)slot * slot_stride;
+  for (int e = tid; e < 64 * 32; e += 256) {
+    const int s = e / 32, c = e % 32;
+    cs[s][c] = (s0 + s < N) ? A[(int64_t)(s0 + s) * Lp + c0 + c] : (uint8_t)4;
+  }
+  if (tid < 64)
+    for (int l = 0; l < nl; l++) lb[l][tid] = (s0 + tid < N) ? (unit ? 1 : limbs[l * Npad + s0 + tid]) : 0;
+  __syncthreads();
+  // 128 rows (4 states x 32 columns) x 64 sequences; each thread writes
+  // 8 consecutive sequences (16 bytes) of one row
+  const int64_t rows_per_buf = (int64_t)nslots * 4 * Lp;
+  for (int e = tid; e < 128 * 8; e += 256) {
+    const int r = e / 8, chunk = e % 8;
+    const int c = r / 4, x = r % 4;
+    const int64_t row = (int64_t)slot * 4 * Lp + 4 * (c0 + c) + x;
+    __align__(16) __nv_bfloat16 va[8];
+    __align__(16) __nv_bfloat16 vb[3][8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int s = chunk * 8 + k;
+      const bool on = (cs[s][c] == x);
+      va[k] = __float2bfloat16(on ? 1.f : 0.f);
+#pragma unroll
+      for (int l = 0; l < 3; l++) vb[l][k] = __float2bfloat16((on && l < nl) ? (float)lb[l][s] : 0.f);
+    }
+    *reinterpret_cast<uint4*>(ops + row * Npad + s0 + chunk * 8) = *reinterpret_cast<uint4*>(va);
+    for (int l = 0; l < nl; l++)
+      *reinterpret_cast<uint4*>(ops + ((1 + l) * rows_per_buf + row) * Npad + s0 + chunk * 8) =
+          *reinterpret_cast<uint4*>(vb[l]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the counting kernel
+// ---------------------------------------------------------------------------
+template <int NL, int STAGES>
+__global__ void __launch_bounds__(128, 1)
+k_count_umma(const __grid_constant__ CUtensorMap tmap, const TileRC* __restrict__ tiles, int ntiles, int nslots,
+             int Lp, int nkb, double scale, float* __restrict__ cnt, int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // 1024-byte aligned ring: stage s = [A | B_0 .. B_{NL-1}], 16 KB each
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* ring = smem;
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int t = blockIdx.x, slot = blockIdx.y;
+  const TileRC tr = tiles[t];
+  const int64_t rows_per_buf = (int64_t)nslots * 4 * Lp;
+  const int rowA = (int)((int64_t)slot * 4 * Lp + (int64_t)tr.I * UM);
+  const int rowB = (int)((int64_t)slot * 4 * Lp + (int64_t)tr.J * UN);
+  constexpr int STAGE_BYTES = TILE_BYTES * (1 + NL);
+  constexpr uint32_t TMEM_COLS = (NL * UN <= 128) ? 128 : (NL * UN <= 256 ? 256 : 512);
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; s++) { mbar_init(&full_bar[s], 1); mbar_init(&empty_bar[s], 1); }
+    mbar_init(&done_bar, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmap) : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  int issued = 0;
+
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer ----
+    for (int kb = 0; kb < nkb; kb++) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+      if (kb >= STAGES) {
+        if (!mbar_wait(&empty_bar[s], ph ^ 1u)) { atomicExch(err, 101); abort_flag = 1; break; }
+      }
+      if (*(volatile int*)&abort_flag) break;
+      uint8_t* st = ring + (size_t)s * STAGE_BYTES;
+      mbar_expect_tx(&full_bar[s], STAGE_BYTES);
+      tma_load_2d(st, &tmap, kb * UK, rowA, &full_bar[s]);
+#pragma unroll
+      for (int l = 0; l < NL; l++)
+        tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * UK, (int)((1 + l) * rows_per_buf) + rowB,
+                    &full_bar[s]);
+      issued = kb + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer ----
+    constexpr uint32_t idesc = make_idesc(UM, UN);
+    for (int kb = 0; kb < nkb; kb++) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+      if (!mbar_wait(&full_bar[s], ph)) { atomicExch(err, 102); abort_flag = 1; break; }
+      if (*(volatile int*)&abort_flag) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = smem_u32(ring + (size_t)s * STAGE_BYTES);
+#pragma unroll
+      for (int k16 = 0; k16 < UK / 16; k16++) {
+        const uint64_t ad = make_desc(sa + k16 * 32);
+#pragma unroll
+        for (int l = 0; l < NL; l++) {
+          const uint64_t bd = make_desc(sa + (uint32_t)(1 + l) * TILE_BYTES + k16 * 32);
+          umma_f16(tmem + (uint32_t)(l * UN), ad, bd, idesc, (kb > 0 || k16 > 0) ? 1u : 0u);
+        }
+      }
+      umma_commit(&empty_bar[s]);
+    }
+    umma_commit(&done_bar);
+  }
+  __syncwarp();
+  // ---- epilogue: all four warps ----
+  bool ok = mbar_wait(&done_bar, 0);
+  if (!ok) { atomicExch(err, 103); abort_flag = 1; }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  float* stage = reinterpret_cast<float*>(smem);   // [16 cells][32][33] (ring is idle now)
+  const int m = warp * 32 + lane;                  // accumulator row = TMEM lane
+  const int a = m >> 2, x = m & 3;
+  if (!abort_flag) {
+#pragma unroll 1
+    for (int c0 = 0; c0 < UN; c0 += 16) {
+      float d[NL][16];
+#pragma unroll
+      for (int l = 0; l < NL; l++)
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * UN + c0), d[l]);
+#pragma unroll
+      for (int k = 0; k < 16; k++) {
+        double v = (double)d[0][k];
+        if (NL > 1) v += 256.0 * (double)d[1][k];
+        if (NL > 2) v += 65536.0 * (double)d[NL > 2 ? 2 : 0][k];
+        const int n = c0 + k, b = n >> 2, y = n & 3;
+        stage[(x * 4 + y) * (32 * 33) + a * 33 + b] = (float)(v * scale);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (!abort_flag) {
+    float* out = cnt + ((int64_t)slot * ntiles + t) * 16 * TPP;
+    for (int e = tid; e < 16 * TPP; e += 128) {
+      const int cell = e / TPP, p = e % TPP;
+      out[e] = stage[cell * (32 * 33) + (p >> 5) * 33 + (p & 31)];
+    }
+  } else if (tid == 0) {
+    // drain the copies this CTA issued before freeing its shared memory
+    for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; kb++)
+      mbar_wait(&full_bar[kb % STAGES], (uint32_t)(kb / STAGES) & 1u);
+  }
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+constexpr int STAGES3 = 3;   // 3 limbs: 64 KB per stage
+constexpr int STAGES1 = 4;   // 1 limb : 32 KB per stage
+
+static size_t smem_bytes(int nl) {
+  const int stages = (nl == 1) ? STAGES1 : STAGES3;
+  const size_t ring = (size_t)stages * TILE_BYTES * (1 + nl);
+  const size_t stage_out = (size_t)16 * 32 * 33 * sizeof(float);
+  return std::max(ring, stage_out) + 1024;
+}
+
+UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, int ntiles, int maxslots) {
+  int dev = 0, major = 0, minor = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  if (major != 10) return nullptr;               // tcgen05 needs a Blackwell datacenter part
+  if (N < 1 || N > 65536) return nullptr;       // limb sums stay exact in FP32 up to here
+  if (!get_encode()) return nullptr;
+  UmmaPlan* p = new UmmaPlan();
+  p->N = N; p->L = L; p->Lp = Lp; p->nT = nT; p->ntiles = ntiles; p->maxslots = maxslots; p->d_tiles = d_tiles;
+  p->Npad = (N + UK - 1) / UK * UK;
+  const int64_t rows = (int64_t)4 * maxslots * 4 * Lp;
+  if (rows >= ((int64_t)1 << 31)) { delete p; return nullptr; }
+  if (cudaMalloc(&p->d_ops, (size_t)rows * p->Npad * sizeof(__nv_bfloat16)) != cudaSuccess) { delete p; return nullptr; }
+  if (cudaMemset(p->d_ops, 0, (size_t)rows * p->Npad * sizeof(__nv_bfloat16)) != cudaSuccess ||
+      cudaMalloc(&p->d_limbs, (size_t)3 * p->Npad) != cudaSuccess || cudaMalloc(&p->d_err, sizeof(int)) != cudaSuccess) {
+    umma_plan_destroy(p);
+    return nullptr;
+  }
+  cudaMemset(p->d_err, 0, sizeof(int));
+  cuuint64_t gdim[2] = {(cuuint64_t)p->Npad, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)p->Npad * sizeof(__nv_bfloat16)};
+  cuuint32_t box[2] = {UK, UM};
+  cuuint32_t estride[2] = {1, 1};
+  CUresult r = get_encode()(&p->tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, p->d_ops, gdim, gstride, box, estride,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) { umma_plan_destroy(p); return nullptr; }
+  cudaFuncSetAttribute(k_count_umma<3, STAGES3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(3));
+  cudaFuncSetAttribute(k_count_umma<1, STAGES1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(1));
+  return p;
+}
+
+void umma_plan_destroy(UmmaPlan* p) {
+  if (!p) return;
+  if (p->d_ops) cudaFree(p->d_ops);
+  if (p->d_limbs) cudaFree(p->d_limbs);
+  if (p->d_err) cudaFree(p->d_err);
+  delete p;
+}
+
+void umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t st) {
+  double wmax = 0.0;
+  bool equal = true;
+  for (int s = 0; s < N; s++) { wmax = std::max(wmax, wgt[s]); if (wgt[s] != wgt[0]) equal = false; }
+  std::vector<uint8_t> lim((size_t)3 * p->Npad, 0);
+  if (equal || wmax <= 0.0) {
+    p->nl = 1;
+    p->scale = (N > 0) ? wgt[0] : 1.0;
+    for (int s = 0; s < N; s++) lim[s] = 1;
+  } else {
+    // q = round(w 2^E) < 2^24
+    int e2;
+    std::frexp(wmax, &e2);                 // wmax = f 2^e2, f in [0.5,1)
+    const int E = 24 - e2;                 // wmax 2^E < 2^24
+    p->nl = 3;
+    p->scale = std::ldexp(1.0, -E);
+    for (int s = 0; s < N; s++) {
+      double qd = std::nearbyint(std::ldexp(wgt[s], E));
+      if (qd > 16777215.0) qd = 16777215.0;
+      const uint32_t q = (uint32_t)qd;
+      lim[s] = (uint8_t)(q & 255u);
+      lim[p->Npad + s] = (uint8_t)((q >> 8) & 255u);
+      lim[2 * (size_t)p->Npad + s] = (uint8_t)(q >> 16);
+    }
+  }
+  cudaMemcpyAsync(p->d_limbs, lim.data(), lim.size(), cudaMemcpyHostToDevice, st);
+  cudaStreamSynchronize(st);
+}
+
+cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
+                       cudaStream_t st) {
+  if (nslots > p->maxslots) return cudaErrorInvalidValue;
+  const int nl = unit ? 1 : p->nl;
+  dim3 pg(p->Npad / 64, p->Lp / 32, nslots);
+  k_umma_prep<<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, nl, p->d_limbs, unit, p->d_ops);
+  const int nkb = p->Npad / UK;
+  const double scale = unit ? 1.0 : p->scale;
+  dim3 grid(p->ntiles, nslots);
+  if (nl == 1)
+    k_count_umma<1, STAGES1><<<grid, 128, smem_bytes(1), st>>>(p->tmap, p->d_tiles, p->ntiles, p->maxslots, p->Lp,
+                                                               nkb, scale, cnt, p->d_err);
+  else
+    k_count_umma<3, STAGES3><<<grid, 128, smem_bytes(3), st>>>(p->tmap, p->d_tiles, p->ntiles, p->maxslots, p->Lp,
+                                                               nkb, scale, cnt, p->d_err);
+  return cudaGetLastError();
+}
+
+int umma_error(UmmaPlan* p) {
+  int e = 0;
+  cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e) cudaMemset(p->d_err, 0, sizeof(int));
+  return e;
 }
 
 }  // namespace covgpu
