@@ -174,7 +174,22 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--counter", default="auto", choices=["auto", "simt", "tensor"])
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline sampling")
+    ap.add_argument("--once", action="store_true",
+                    help="one covgpu_rscape call of the workload and exit (for profiler captures)")
+    ap.add_argument("--N", type=int, default=None, help="override N (profiling a smaller case)")
+    ap.add_argument("--L", type=int, default=None, help="override L (profiling a smaller case)")
+    ap.add_argument("--nshuffle", type=int, default=None, help="override the number of nulls")
+    ap.add_argument("--types", default=None, help="comma-separated statistics (default GTp,MIp,CHIp,RAFp)")
     args = ap.parse_args()
+    if args.N:
+        CFG["N"] = args.N
+    if args.L:
+        CFG["L"] = args.L
+        CFG["nbp"] = min(CFG["nbp"], args.L // 4)
+    if args.nshuffle is not None:
+        CFG["nshuffle"] = args.nshuffle
+    if args.types:
+        TYPES[:] = args.types.split(",")
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -215,15 +230,7 @@ def main():
     counter = {"auto": 0, "simt": 0, "tensor": 1}[args.counter]
     if args.counter == "auto":
         counter = 1 if os.environ.get("COVGPU_COUNTER", "tensor") == "tensor" else 0
-    e = cg.Engine(N, L, maxslots=ns + 1, maxnull=ns, device=local)
-    e.set_tree(s.parent, s.left, s.right)
-    e.set_weights(w)
-    e.set_alignment(0, ax)
-    try:
-        e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)
-    except RuntimeError:
-        counter = 0      # the tensor counter refuses this shape: plain path
-    kind = "tensor" if counter == 1 else "simt"
+XX
     for _ in range(args.warmup):
         e.flush_l2()
         e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)

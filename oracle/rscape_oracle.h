@@ -8,9 +8,9 @@
  * CPU-baseline leg of the benchmark may load it.  Nothing in the shipped
  * GPU library links, calls or falls back to it.
  *
- * Parity status: counting, marginals, statistics and APC/ASC are pinned by
- * the golden GTp scores and nseff values published for
- * tutorial/updated_Arisong.sto (documentation/tutorial.tex:186-212).  The
+ * Parity status: counting, marginals, GTp and APC are pinned by the golden
+ * GTp scores published for tutorial/updated_Arisong.sto
+ * (documentation/tutorial.tex:186-212).  The
  * Easel pieces (sequence weights, histogram binning, binned tail fits, RNG)
  * are absent from the reference tree and are restated from their published
  * mathematics; E-values are therefore pinned only against this oracle's own
