@@ -124,6 +124,21 @@ int  covgpu_hist_full(covgpu_ctx *ctx, const double *COV, double bmin, double w,
 int  covgpu_evalue_full(covgpu_ctx *ctx, const double *COV, const void *h, const double *survfit, double Nt,
                         double thresh, double *Eval, covgpu_hit *hits, int hitcap, int *nhit);
 
+/* APC (actype 0) or ASC (1) of a device-resident L x L score matrix (both
+ * triangles; the diagonal is ignored) into the device buffer d_out (diagonal
+ * set to -inf), with the min/max of the corrected scores in d_minmax[2],
+ * enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream).
+ * No counterpart in the reference: this entry point allocates no device
+ * memory, for callers that cannot call cudaMalloc (code running inside a
+ * stream capture, pooled-memory hosts, real-time callers).  Its scratch is a
+ * fixed device array sized for L <= COVGPU_NOALLOC_MAX_L; larger L returns
+ * 11.  The first call on a device looks up that array's device address, so
+ * make it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.  Returns 0,
+ * 11 (bad arguments) or 90 (CUDA error). */
+#define COVGPU_NOALLOC_MAX_L 16384
+int  covgpu_correct_noalloc(const double *d_cov, double *d_out, int L, int actype, double *d_minmax, void *stream);
+
 /* writes a 256 MB device buffer (larger than L2) on the context's stream */
 int  covgpu_flush_l2(covgpu_ctx *ctx);
 
