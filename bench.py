@@ -186,6 +186,8 @@ def main():
     if args.L:
         CFG["L"] = args.L
         CFG["nbp"] = min(CFG["nbp"], args.L // 4)
+        CFG["nhelix"] = max(1, min(CFG["nhelix"], CFG["nbp"] // 8))
+        CFG["hmin"] = max(1, min(CFG["hmin"], CFG["nbp"] // CFG["nhelix"]))
     if args.nshuffle is not None:
         CFG["nshuffle"] = args.nshuffle
     if args.types:
@@ -230,7 +232,21 @@ def main():
     counter = {"auto": 0, "simt": 0, "tensor": 1}[args.counter]
     if args.counter == "auto":
         counter = 1 if os.environ.get("COVGPU_COUNTER", "tensor") == "tensor" else 0
-XX
+    e = cg.Engine(N, L, maxslots=ns + 1, maxnull=ns, device=local)
+    e.set_tree(s.parent, s.left, s.right)
+    e.set_weights(w)
+    e.set_alignment(0, ax)
+    try:
+        r = e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)
+    except RuntimeError:
+        counter = 0      # the tensor counter refuses this shape: plain path
+        r = e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)
+    if args.once:
+        ms, n = e.last_timing()
+        print(json.dumps({"once": True, "N": N, "L": L, "nshuffle": ns, "types": TYPES, "counter": counter,
+                          "device_ms": list(ms), "launches": n, "hits": [len(x["hits"]) for x in r]}))
+        return
+    kind = "tensor" if counter == 1 else "simt"
     for _ in range(args.warmup):
         e.flush_l2()
         e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)

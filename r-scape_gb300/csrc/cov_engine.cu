@@ -36,6 +36,7 @@ struct covgpu_ctx {
   float* d_cnt = nullptr;
   float* d_ucnt = nullptr;
   double *d_part4 = nullptr, *d_partR = nullptr, *d_pm = nullptr, *d_meanp = nullptr, *d_ps = nullptr;
+  float2* d_pmdf = nullptr;
   double *d_cov = nullptr, *d_cov2 = nullptr, *d_part1 = nullptr, *d_colx = nullptr, *d_avg = nullptr;
   double *d_tmin = nullptr, *d_tmax = nullptr, *d_mm = nullptr;
   int* d_status = nullptr;
@@ -124,6 +125,7 @@ extern "C" int covgpu_create(covgpu_ctx** ret, int device, int N, int L, int max
   CK(dalloc(&ctx->d_part4, S * nT2 * TP * 4));
   CK(dalloc(&ctx->d_partR, S * nT2 * TP));
   CK(dalloc(&ctx->d_pm, S * ctx->Lp * 4));
+  CK(dalloc(&ctx->d_pmdf, S * ctx->Lp * 4));
   CK(dalloc(&ctx->d_meanp, S * 4));
   CK(dalloc(&ctx->d_ps, S * ctx->Lp * 5));
   CK(dalloc(&ctx->d_cov, S * MAXOUT * ntl * TPP));
@@ -153,7 +155,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
                   ctx->d_part1, ctx->d_colx, ctx->d_avg, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status,
                   ctx->d_left, ctx->d_right, ctx->d_lnodes, ctx->d_fitch, ctx->d_scratch, ctx->d_obs, ctx->d_sf,
                   ctx->d_tail, ctx->d_nhits, ctx->d_hi, ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->d_full,
-                  ctx->d_flush};
+                  ctx->d_flush, ctx->d_pmdf};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (ctx->umma) umma_plan_destroy(ctx->umma);
   for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
@@ -328,8 +330,8 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
     cudaEventRecord(ctx->ev[5], ctx->st);
     ctx->counted = true;
     CK(launch_pair_marg(ctx->d_cnt, L, ctx->d_tiles, ntiles, nT, nslots, ctx->d_part4, ctx->d_partR, ctx->st));
-    CK(launch_pm_final(ctx->d_part4, ctx->d_partR, L, Lp, nT, nslots, ctx->d_pm, ctx->d_ps, ctx->d_meanp,
-                       ctx->d_status, ctx->st));
+    CK(launch_pm_final(ctx->d_part4, ctx->d_partR, L, Lp, nT, nslots, ctx->d_pm, ctx->d_pmdf, ctx->d_ps,
+                       ctx->d_meanp, ctx->d_status, ctx->st));
     ctx->nlaunch += 4;
   }
   if (need_u) {
@@ -344,12 +346,16 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   A.cnt = need_w ? ctx->d_cnt : nullptr;
   A.ucnt = need_u ? ctx->d_ucnt : nullptr;
   A.pm = ctx->d_pm;
+  A.pmdf = ctx->d_pmdf;
   A.meanp = ctx->d_meanp;
   A.cov = ctx->d_cov;
   A.part1 = ctx->d_part1;
   A.tiles = ctx->d_tiles;
   A.ntiles = ntiles; A.nT = nT; A.L = L; A.Lp = Lp; A.N = N;
-  A.wtot = ctx->wtot;
+  {
+    const float hi = (float)ctx->wtot;
+    A.wtot = make_float2(hi, (float)(ctx->wtot - (double)hi));
+  }
   A.stats = mask;
   A.cls = cls;
   A.nout = ntypes;
@@ -357,6 +363,7 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   if (!need_w) {
     // RAF only: pm is never read, but keep the pointers valid
     CK(cudaMemsetAsync(ctx->d_pm, 0, (size_t)nslots * Lp * 4 * sizeof(double), ctx->st));
+    CK(cudaMemsetAsync(ctx->d_pmdf, 0, (size_t)nslots * Lp * 4 * sizeof(float2), ctx->st));
   }
   CK(launch_stats(A, nslots, ctx->st));
   ctx->nlaunch += 1;

@@ -27,6 +27,11 @@ namespace covgpu {
 // the last ulp could move the ceiling) is the IEEE division redone, so the
 // bin always equals the one the division gives.
 __device__ __forceinline__ int exact_bin(double x, double bmin, double w, double invw) {
+  // fp32 estimate first: three roundings put it within 1.8e-7 |q| of the
+  // exact quotient, so away from integers it has the same ceiling
+  const float qf = (float)(x - bmin) * (float)invw;
+  const float fr = qf - rintf(qf);
+  if (fabsf(qf) < 4194304.f && fabsf(fr) > 4e-7f * fabsf(qf) + 1e-6f) return (int)ceilf(qf - 1.0f);
   double q = (x - bmin) * invw;
   if (fabs(q - rint(q)) < 1e-9) q = (x - bmin) / w;
   return (int)ceil(q - 1.0);
@@ -149,8 +154,10 @@ __device__ __forceinline__ void tile_rowcol_store(const double (&v)[4][NV], doub
 // Pair-normalised marginal contributions: for every pair with nseff > 0,
 // row i gains (4e-10 + sum_y C(x,y)) / S and column j gains
 // (4e-10 + sum_x C(x,y)) / S, S = 16e-10 + nseff (the prior of
-// src/correlators.c:1713 and the normalisation of :1758).  Also the
-// upper-triangle row sums of nseff for the CCF column means.
+// src/correlators.c:1713 and the normalisation of :1758).  Each pair's
+// contribution is formed in fp32 (relative error ~1e-7, independent from pair
+// to pair) and summed over partners in FP64, so the marginals keep ~1e-9.
+// Also the upper-triangle row sums of nseff for the CCF column means.
 __global__ void __launch_bounds__(256)
 k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ tiles, int ntiles, int nT,
             double* __restrict__ part4, double* __restrict__ partR) {
@@ -165,18 +172,22 @@ k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ til
     float c[16];
 #pragma unroll
     for (int q = 0; q < 16; q++) c[q] = C[q * TPP + p];
-    double ne = 0.0;
-#pragma unroll
-    for (int q = 0; q < 16; q++) ne += (double)c[q];
-    const bool pair = (i < j) && (j < L);
-    const bool ok = pair && (ne > 0.0);
-    const double invS = ok ? 1.0 / (16e-10 + ne) : 0.0;
+    float row[4], col[4];
 #pragma unroll
     for (int x = 0; x < 4; x++) {
-      rv[k][x] = ok ? (4e-10 + (double)c[x * 4 + 0] + (double)c[x * 4 + 1] + (double)c[x * 4 + 2] + (double)c[x * 4 + 3]) * invS : 0.0;
-      cv[k][x] = ok ? (4e-10 + (double)c[0 * 4 + x] + (double)c[1 * 4 + x] + (double)c[2 * 4 + x] + (double)c[3 * 4 + x]) * invS : 0.0;
+      row[x] = (c[x * 4 + 0] + c[x * 4 + 1]) + (c[x * 4 + 2] + c[x * 4 + 3]);
+      col[x] = (c[0 * 4 + x] + c[1 * 4 + x]) + (c[2 * 4 + x] + c[3 * 4 + x]);
     }
-    nr[k][0] = pair ? ne : 0.0;
+    const float ne = (row[0] + row[1]) + (row[2] + row[3]);
+    const bool pair = (i < j) && (j < L);
+    const bool ok = pair && (ne > 0.f);
+    const float invS = ok ? 1.0f / (16e-10f + ne) : 0.f;
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+      rv[k][x] = ok ? (double)((4e-10f + row[x]) * invS) : 0.0;
+      cv[k][x] = ok ? (double)((4e-10f + col[x]) * invS) : 0.0;
+    }
+    nr[k][0] = pair ? (double)ne : 0.0;
     zero[k][0] = 0.0;
   }
   tile_rowcol_store2<4>(rv, cv, part4 + (int64_t)slot * nT * nT * TP * 4, nT, tr.I, tr.J);
@@ -187,7 +198,8 @@ k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ til
 // per column.  mpc[c][x] = pm[c][x] * (sum_{j>c} nseff[c][j]) feeds the CCF
 // column means (src/correlators.c:1030-1036).
 __global__ void k_pm_final(const double* __restrict__ part4, const double* __restrict__ partR, int L, int Lp, int nT,
-                           double* __restrict__ pm, double* __restrict__ mpc, int* __restrict__ status) {
+                           double* __restrict__ pm, float2* __restrict__ pmdf, double* __restrict__ mpc,
+                           int* __restrict__ status) {
   const int slot = blockIdx.y;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= L) return;
@@ -207,6 +219,8 @@ __global__ void k_pm_final(const double* __restrict__ part4, const double* __res
 #pragma unroll
   for (int x = 0; x < 4; x++) {
     pm[((int64_t)slot * Lp + c) * 4 + x] = m[x];
+    const float hi = (float)m[x];
+    pmdf[((int64_t)slot * Lp + c) * 4 + x] = make_float2(hi, (float)(m[x] - (double)hi));
     mpc[((int64_t)slot * Lp + c) * 4 + x] = rs * m[x];
   }
 }
@@ -251,146 +265,211 @@ __global__ void k_ps(const uint8_t* __restrict__ ax, int64_t slot_stride, const 
 
 // ------------------------------------------------------------------------
 // Statistics.  Per cell, o = nseff*pp and e = nseff*pm_i(x)*pm_j(y) are
-// formed in FP64 and their difference u = o - e is kept in FP64; the rest
-// is fp32.  The G-test is summed as 2*sum_e e*g(u/e) (each term >= 0), which
-// equals the reference's 2*sum o*ln(o/e) because sum u = 0 to rounding when
-// every cell enters (pp and pm are normalised); the CWC form, which sums a
-// subset of cells, adds its sum u explicitly.
+// formed in double-float arithmetic (pairs of fp32 values, ~48-bit
+// significand; GB300 runs fp32 at 64x its FP64 rate) and their difference
+// u = o - e is rounded once to fp32; the rest is fp32.  The G-test is summed
+// as 2*sum_e e*g(u/e) (each term >= 0), which equals the reference's
+// 2*sum o*ln(o/e) because sum u = 0 to rounding when every cell enters (pp
+// and pm are normalised); the CWC form, which sums a subset of cells, adds
+// its sum u explicitly.
+//
+// o = (1e-10 + C) ne / (16e-10 + ne) is written as C + do with
+// do = 1e-10 - 16e-10 C / ne (to 1e-18 absolute), the prior of
+// src/correlators.c:1713 and the normalisation of :1758.
 // ------------------------------------------------------------------------
-__device__ __forceinline__ float gterm(double u, double e, double o) {
-  const float ef = (float)e;
-  const float d = (float)u / ef;
-  if (d > -0.25f) return ef * gfun(d);
-  return ef * gfun_ratio((float)o / ef);
+struct df { float hi, lo; };
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {   // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ df df_add_f(df a, float b) {
+  const df s = two_sum(a.hi, b);
+  return fast_two_sum(s.hi, s.lo + a.lo);
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  const df s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = a.hi * b.hi;
+  const float e = fmaf(a.hi, b.hi, -p);
+  return fast_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ df df_of(double x) {
+  const float hi = (float)x;
+  return {hi, (float)(x - (double)hi)};
+}
+__device__ __forceinline__ double df_to_d(df a) { return (double)a.hi + (double)a.lo; }
+
+// u = o - e with o = c + dc (c >= 0 exact fp32, |dc| tiny), e in double-float
+__device__ __forceinline__ float diff_oe(float c, float dc, df e) {
+  const df s = two_sum(c, -e.hi);
+  return s.hi + (s.lo + (dc - e.lo));
 }
 
-struct PairOut { double v[NSTAT]; };
+// G-test term e*g(u/e); o = c + dc when the ratio form is needed
+__device__ __forceinline__ float gterm_f(float u, float e, float o) {
+  const float d = __fdividef(u, e);
+  if (d > -0.25f) return e * gfun(d);
+  return e * gfun_ratio(__fdividef(o, e));
+}
 
-__device__ void pair_stats(const StatsArgs& A, const float (&c)[16], const float (&uc)[16], bool have_uc,
-                           const double* pmi, const double* pmj, const double* meanp, double ne, double wtot,
-                           PairOut& out) {
+struct PairOut { float chi, gt, mi, mir, mig, omes; double raf, ccf; };
+
+__device__ __forceinline__ double pick(const PairOut& o, int k) {
+  switch (k) {
+    case 0: return o.chi;
+    case 1: return o.gt;
+    case 2: return o.mi;
+    case 3: return o.mir;
+    case 4: return o.mig;
+    case 5: return o.omes;
+    case 6: return o.raf;
+    case 8: return o.ccf;
+  }
+  return 0.0;
+}
+
+__device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[16], const float (&uc)[16], bool have_uc,
+                           const float2* pmi, const float2* pmj, const double* pmid, const double* pmjd,
+                           const double* meanp, df ne, PairOut& out) {
   const unsigned S = A.stats;
-  const double ngap = wtot - ne;
-  // ---- RAF from unit-weight counts (src/correlators.c:897-925 reduced) ----
+  // ---- RAF from unit-weight counts (src/correlators.c:897-925 reduced):
+  // integer counts, exact in 64-bit integer arithmetic; the two divisions
+  // in the reference's order ----
   if ((S & (S_RAF | S_RAFS)) && have_uc) {
-    double nA = 0.0, r[4] = {0, 0, 0, 0}, cc[4] = {0, 0, 0, 0};
+    long long nA = 0, r[4] = {0, 0, 0, 0}, cc[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int x = 0; x < 4; x++)
 #pragma unroll
       for (int y = 0; y < 4; y++)
-        if (A.allow[x * 4 + y] > 0.f) { double n = (double)uc[x * 4 + y]; nA += n; r[x] += n; cc[y] += n; }
-    double sr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
-    double sc = cc[0] * cc[0] + cc[1] * cc[1] + cc[2] * cc[2] + cc[3] * cc[3];
-    double cij = 0.5 * (2.0 * nA * nA - sr - sc);
+        if (A.allow[x * 4 + y] > 0.f) {
+          const long long n = (long long)uc[x * 4 + y];
+          nA += n; r[x] += n; cc[y] += n;
+        }
+    const long long sr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+    const long long sc = cc[0] * cc[0] + cc[1] * cc[1] + cc[2] * cc[2] + cc[3] * cc[3];
+    const long long twice = 2 * nA * nA - sr - sc;     // 2 c_ij, even
+    double cij = (double)(twice / 2);
     const double Nd = (double)A.N;
     cij /= (A.N > 1) ? Nd * (Nd - 1.0) : 1.0;
     cij *= 2.0;
-    double qij = (Nd - nA) / Nd;
-    out.v[6] = cij - 1.0 * qij;
+    const double qij = (double)((long long)A.N - nA) / Nd;
+    out.raf = cij - 1.0 * qij;
   }
-  // ---- CCF (src/correlators.c:1038-1053) ----
+  // ---- CCF (src/correlators.c:1038-1053), FP64 ----
   if (S & S_CCF) {
+    const double ned = df_to_d(ne);
     double ccf = 0.0;
 #pragma unroll
     for (int x = 0; x < 4; x++)
 #pragma unroll
       for (int y = 0; y < 4; y++) {
-        double cc = (ne * pmi[x] - meanp[x]) * (ne * pmj[y] - meanp[y]);
+        const double cc = (ned * pmid[x] - meanp[x]) * (ned * pmjd[y] - meanp[y]);
         ccf += cc * cc;
       }
-    out.v[8] = sqrt(ccf);
+    out.ccf = sqrt(ccf);
   }
   const unsigned SP = S & (S_CHI | S_GT | S_MI | S_MIr | S_MIg | S_OMES);
   if (!SP) return;
 
-  if (ne <= 0.0) {
+  if (ne.hi <= 0.f) {
     // no sequence with both residues canonical: pp = 1/16 (prior only)
     double mi = 0.0, hh = 0.0;
-    if (A.cls == 0) {
+    if (A.cls != 1) {
       for (int x = 0; x < 4; x++)
         for (int y = 0; y < 4; y++) {
           const double p = 0.0625;
-          if (pmi[x] > 0.0 && pmj[y] > 0.0) mi += p * (log(p) - log(pmi[x]) - log(pmj[y]));
+          if (pmid[x] > 0.0 && pmjd[y] > 0.0) mi += p * (log(p) - log(pmid[x]) - log(pmjd[y]));
           hh -= p * log(p);
         }
     } else {
       double pw = 0, pn = 0, qw = 0, qn = 0;
       for (int x = 0; x < 4; x++)
         for (int y = 0; y < 4; y++) {
-          if (A.allow[x * 4 + y] > 0.f) { pw += 0.0625; qw += pmi[x] * pmj[y]; }
-          else                          { pn += 0.0625; qn += pmi[x] * pmj[y]; }
+          if (A.allow[x * 4 + y] > 0.f) { pw += 0.0625; qw += pmid[x] * pmjd[y]; }
+          else                          { pn += 0.0625; qn += pmid[x] * pmjd[y]; }
         }
       if (pw > 0.0) { mi += pw * (log(pw) - log(qw)); hh -= pw * log(pw); }
       if (pn > 0.0) { mi += pn * (log(pn) - log(qn)); hh -= pn * log(pn); }
     }
-    out.v[0] = 0.0; out.v[1] = 0.0; out.v[5] = 0.0;
-    out.v[2] = mi; out.v[3] = (hh > 1e-2) ? mi / hh : 0.0; out.v[4] = mi;
+    out.chi = 0.f; out.gt = 0.f; out.omes = 0.f;
+    out.mi = (float)mi; out.mir = (float)((hh > 1e-2) ? mi / hh : 0.0); out.mig = (float)mi;
     return;
   }
 
-  // pp = (1e-10 + C) / S;  o = ne * pp = (1e-10 + C) * t,  t = ne / S
-  const double Ssum = 16e-10 + ne;
-  const double t = ne / Ssum;
+  const float inv_ne = 1.0f / ne.hi;
+  const df ng = df_add({A.wtot.x, A.wtot.y}, {-ne.hi, -ne.lo});   // ngap = sum w - nseff
   if (A.cls == 0 || A.cls == 2) {
-    float gsum = 0.f, chi = 0.f, omes = 0.f, hh = 0.f;
-    double usum = 0.0;
-    const float invne = (float)(1.0 / ne);
+    float gsum = 0.f, chi = 0.f, omes = 0.f, hh = 0.f, usum = 0.f;
 #pragma unroll
     for (int x = 0; x < 4; x++) {
-      const double ax = ne * pmi[x];
+      const df ax = df_mul(ne, {pmi[x].x, pmi[x].y});
 #pragma unroll
       for (int y = 0; y < 4; y++) {
         if (A.cls == 2 && !(A.allow[x * 4 + y] > 0.f)) continue;
-        const double o = (1e-10 + (double)c[x * 4 + y]) * t;
-        const double e = ax * pmj[y];
-        const double u = o - e;
-        if (e > 0.0) {
-          const float uf = (float)u;
-          gsum += gterm(u, e, o);
-          chi += uf * uf / (float)e;
-          omes += uf * uf;
+        const float C = c[x * 4 + y];
+        const float dc = 1e-10f - 16e-10f * C * inv_ne;
+        const df e = df_mul(ax, {pmj[y].x, pmj[y].y});
+        const float u = diff_oe(C, dc, e);
+        const float o = C + dc;
+        if (e.hi > 0.f) {
+          gsum += gterm_f(u, e.hi, o);
+          chi += __fdividef(u * u, e.hi);
+          omes += u * u;
           usum += u;
         }
-        const float p = (float)o * invne;
-        hh -= (p > 0.f) ? p * logf(p) : 0.f;
+        const float p = o * inv_ne;
+        hh -= (p > 0.f) ? p * __logf(p) : 0.f;
       }
     }
-    const double gt = (A.cls == 2) ? 2.0 * ((double)gsum + usum) : 2.0 * (double)gsum;
-    const double mi = (double)gsum / ne;
-    out.v[0] = chi;
-    out.v[1] = gt;
-    out.v[2] = mi;
-    out.v[3] = (hh > 1e-2f) ? mi / (double)hh : 0.0;
-    out.v[4] = mi - ngap / ne;
-    out.v[5] = (double)(omes * invne);
+    const float gt = (A.cls == 2) ? 2.f * (gsum + usum) : 2.f * gsum;
+    const float mi = gsum * inv_ne;
+    out.chi = chi;
+    out.gt = gt;
+    out.mi = mi;
+    out.mir = (hh > 1e-2f) ? mi / hh : 0.f;
+    out.mig = mi - (ng.hi + ng.lo) * inv_ne;
+    out.omes = omes * inv_ne;
   } else {
     // C2: allowed / not-allowed merged cells (e.g. src/correlators.c:426-458)
-    double Cw = 0.0, Cn = 0.0, qw = 0.0, qn = 0.0;
+    df Cw = {0.f, 0.f}, Cn = {0.f, 0.f}, qw = {0.f, 0.f}, qn = {0.f, 0.f};
     int nal = 0;
 #pragma unroll
     for (int x = 0; x < 4; x++)
 #pragma unroll
       for (int y = 0; y < 4; y++) {
-        if (A.allow[x * 4 + y] > 0.f) { Cw += (double)c[x * 4 + y]; qw += pmi[x] * pmj[y]; nal++; }
-        else                          { Cn += (double)c[x * 4 + y]; qn += pmi[x] * pmj[y]; }
+        const df pq = df_mul({pmi[x].x, pmi[x].y}, {pmj[y].x, pmj[y].y});
+        if (A.allow[x * 4 + y] > 0.f) { Cw = df_add_f(Cw, c[x * 4 + y]); qw = df_add(qw, pq); nal++; }
+        else                          { Cn = df_add_f(Cn, c[x * 4 + y]); qn = df_add(qn, pq); }
       }
-    const double ow = (nal * 1e-10 + Cw) * t, on = ((16 - nal) * 1e-10 + Cn) * t;
-    const double ew = ne * qw, en = ne * qn;
-    const double uw = ow - ew, un = on - en;
+    const float dw = nal * 1e-10f - 16e-10f * Cw.hi * inv_ne;
+    const float dn = (16 - nal) * 1e-10f - 16e-10f * Cn.hi * inv_ne;
+    const df ew = df_mul(ne, qw), en = df_mul(ne, qn);
+    // u = (Cw.hi + Cw.lo + dw) - ew
+    const float uw = diff_oe(Cw.hi, Cw.lo + dw, ew);
+    const float un = diff_oe(Cn.hi, Cn.lo + dn, en);
+    const float ow = Cw.hi + (Cw.lo + dw), on = Cn.hi + (Cn.lo + dn);
     float g = 0.f, chi = 0.f, om = 0.f;
-    if (ew > 0.0) { g += gterm(uw, ew, ow); chi += (float)(uw * uw / ew); om += (float)(uw * uw); }
-    if (en > 0.0) { g += gterm(un, en, on); chi += (float)(un * un / en); om += (float)(un * un); }
-    const double pw = ow / ne, pn = on / ne;
-    double hh = 0.0;
-    hh -= (pw > 0.0) ? pw * (double)logf((float)pw) : 0.0;
-    hh -= (pn > 0.0) ? pn * (double)logf((float)pn) : 0.0;
-    const double mi = (double)g / ne;
-    out.v[0] = chi;
-    out.v[1] = 2.0 * (double)g;
-    out.v[2] = mi;
-    out.v[3] = (hh > 1e-2) ? mi / hh : 0.0;
-    out.v[4] = mi - ngap / ne;
-    out.v[5] = (double)om / ne;
+    if (ew.hi > 0.f) { g += gterm_f(uw, ew.hi, ow); chi += __fdividef(uw * uw, ew.hi); om += uw * uw; }
+    if (en.hi > 0.f) { g += gterm_f(un, en.hi, on); chi += __fdividef(un * un, en.hi); om += un * un; }
+    const float pw = ow * inv_ne, pn = on * inv_ne;
+    float hh = 0.f;
+    hh -= (pw > 0.f) ? pw * __logf(pw) : 0.f;
+    hh -= (pn > 0.f) ? pn * __logf(pn) : 0.f;
+    const float mi = g * inv_ne;
+    out.chi = chi;
+    out.gt = 2.f * g;
+    out.mi = mi;
+    out.mir = (hh > 1e-2f) ? mi / hh : 0.f;
+    out.mig = mi - (ng.hi + ng.lo) * inv_ne;
+    out.omes = om * inv_ne;
   }
 }
 
@@ -401,6 +480,7 @@ k_stats(StatsArgs A) {
   const float* C = A.cnt ? A.cnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
   const float* U = A.ucnt ? A.ucnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
   const double* pm = A.pm + (int64_t)slot * A.Lp * 4;
+  const float2* pmdf = A.pmdf + (int64_t)slot * A.Lp * 4;
   const double* meanp = A.meanp + slot * 4;
   double rs[4][MAXOUT];
 #pragma unroll
@@ -411,24 +491,21 @@ k_stats(StatsArgs A) {
     float c[16], uc[16];
 #pragma unroll
     for (int q = 0; q < 16; q++) { c[q] = C ? C[q * TPP + p] : 0.f; uc[q] = U ? U[q * TPP + p] : 0.f; }
-    double ne = 0.0;
+    df ne = {0.f, 0.f};
 #pragma unroll
-    for (int q = 0; q < 16; q++) ne += (double)c[q];
+    for (int q = 0; q < 16; q++) ne = df_add_f(ne, c[q]);
     PairOut o;
-#pragma unroll
-    for (int q = 0; q < NSTAT; q++) o.v[q] = 0.0;
+    o.chi = o.gt = o.mi = o.mir = o.mig = o.omes = 0.f;
+    o.raf = o.ccf = 0.0;
     if (valid) {
       const int ii = i < A.L ? i : 0, jj = j < A.L ? j : 0;
-      pair_stats(A, c, uc, U != nullptr, pm + ii * 4, pm + jj * 4, meanp, ne, A.wtot, o);
+      pair_stats(A, c, uc, U != nullptr, pmdf + ii * 4, pmdf + jj * 4, pm + ii * 4, pm + jj * 4, meanp, ne, o);
     }
 #pragma unroll
     for (int q = 0; q < MAXOUT; q++) {
-      double v = 0.0;
-      if (q < A.nout) v = o.v[A.outstat[q]];
-      rs[k][q] = valid ? v : 0.0;
-      if (q < A.nout) {
-        A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = valid ? v : 0.0;
-      }
+      const double v = (q < A.nout && valid) ? pick(o, A.outstat[q]) : 0.0;
+      rs[k][q] = v;
+      if (q < A.nout) A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = v;
     }
   }
   // per-statistic row/column sums for APC/ASC
@@ -509,6 +586,7 @@ k_apc_apply(double* __restrict__ cov, const double* __restrict__ colx, const dou
   const int actype = ct.act[sq % ct.nout];
   const TileRC tr = tiles[t];
   const double A = avg[sq];
+  const double invA = (A != 0.0) ? 1.0 / A : 0.0;
   const double* X = colx + (int64_t)sq * Lp;
   double* V = cov + ((int64_t)sq * ntiles + t) * TPP;
   double lo = DBL_MAX, hi = -DBL_MAX;
@@ -518,7 +596,7 @@ k_apc_apply(double* __restrict__ cov, const double* __restrict__ colx, const dou
     const int i = tr.I * TP + a, j = tr.J * TP + b;
     if (i < j && j < L) {
       double v = V[p], r;
-      if (actype == 0)      r = (A != 0.0) ? v - X[i] * X[j] / A : 0.0;
+      if (actype == 0)      r = (A != 0.0) ? v - X[i] * X[j] * invA : 0.0;
       else if (actype == 1) r = v - (X[i] + X[j] - A);
       else                  r = v;
       if (isnan(r)) atomicExch(status, 3);
@@ -745,8 +823,8 @@ cudaError_t launch_pair_marg(const float* cnt, int L, const TileRC* tiles, int n
 }
 
 cudaError_t launch_pm_final(const double* part4, const double* partR, int L, int Lp, int nT, int nslots, double* pm,
-                            double* mpc, double* meanp, int* status, cudaStream_t st) {
-  k_pm_final<<<dim3((L + 127) / 128, nslots), 128, 0, st>>>(part4, partR, L, Lp, nT, pm, mpc, status);
+                            float2* pmdf, double* mpc, double* meanp, int* status, cudaStream_t st) {
+  k_pm_final<<<dim3((L + 127) / 128, nslots), 128, 0, st>>>(part4, partR, L, Lp, nT, pm, pmdf, mpc, status);
   k_meanp<<<nslots, 256, 0, st>>>(mpc, L, Lp, meanp);
   return cudaGetLastError();
 }

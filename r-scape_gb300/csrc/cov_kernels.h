@@ -13,12 +13,13 @@ struct StatsArgs {
   const float*  cnt;        // weighted counts  [slot][tile][16][TPP]
   const float*  ucnt;       // unit-weight counts (RAF) or nullptr
   const double* pm;         // [slot][Lp][4]
+  const float2* pmdf;       // [slot][Lp][4] pm as double-float (hi, lo)
   const double* meanp;      // [slot][4]
   double*       cov;        // [slot][nout][tile][TPP]
   double*       part1;      // [slot][nout][nT][nT][TP]
   const TileRC* tiles;
   int           ntiles, nT, L, Lp, N;
-  double        wtot;       // sum of the sequence weights (ngap = wtot - nseff)
+  float2        wtot;       // sum of the weights as double-float (ngap = wtot - nseff)
   unsigned      stats;      // StatBit mask of what pair_stats must compute
   int           cls;        // 0 = C16, 1 = C2, 2 = CWC (GT)
   int           nout;       // number of output matrices (<= MAXOUT)
@@ -39,7 +40,7 @@ cudaError_t launch_count_simt(const uint8_t* ax, int64_t slot_stride, const floa
 cudaError_t launch_pair_marg(const float* cnt, int L, const TileRC* tiles, int ntiles, int nT, int nslots,
                              double* part4, double* partR, cudaStream_t st);
 cudaError_t launch_pm_final(const double* part4, const double* partR, int L, int Lp, int nT, int nslots, double* pm,
-                            double* mpc, double* meanp, int* status, cudaStream_t st);
+                            float2* pmdf, double* mpc, double* meanp, int* status, cudaStream_t st);
 cudaError_t launch_ps(const uint8_t* ax, int64_t slot_stride, const double* w, int N, int L, int Lp, int nslots,
                       double* ps, cudaStream_t st);
 cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st);
