@@ -248,6 +248,7 @@ extern double         covh_Bin2LBound(const ESL_HISTOGRAM *h, int b);
 extern double         covh_Bin2UBound(const ESL_HISTOGRAM *h, int b);
 extern int            covh_Add(ESL_HISTOGRAM *h, double x);
 extern double         covh_pmass(const ESL_HISTOGRAM *h, double target_pmass, double target_fracfit);
+extern double         covh_SetTailByMass(ESL_HISTOGRAM *h, double pmass);   /* returns the tail's mass */
 extern double         covh_cov2evalue(double cov, double Nc, const ESL_HISTOGRAM *h, const double *survfit);
 extern double         covh_evalue2cov(double eval_thresh, double Nc, const ESL_HISTOGRAM *h, const double *survfit);
 extern double         covh_gamma_surv(double x, void *params);   /* params = {mu, lambda, tau} */

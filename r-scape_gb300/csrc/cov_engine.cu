@@ -14,6 +14,7 @@
 
 #include "cov_dev.cuh"
 #include "cov_kernels.h"
+#include "cov_fit.h"
 #include "cov_umma.h"
 #include "covgpu.h"
 #include "rscape_cov.h"
@@ -57,6 +58,7 @@ struct covgpu_ctx {
   int hitcap = 0;
   double* d_full = nullptr;
   UmmaPlan* umma = nullptr;
+  FitWork* fitw = nullptr;
   unsigned char* d_flush = nullptr;
   bool counted = false;
   cudaEvent_t ev[6] = {};
@@ -158,6 +160,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
                   ctx->d_flush, ctx->d_pmdf};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (ctx->umma) umma_plan_destroy(ctx->umma);
+  if (ctx->fitw) fitwork_destroy(ctx->fitw);
   for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
@@ -358,6 +361,8 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   }
   A.stats = mask;
   A.cls = cls;
+  A.invD = 1.0 / ((N > 1) ? (double)N * ((double)N - 1.0) : 1.0);
+  A.invN = 1.0 / (double)N;
   A.nout = ntypes;
   for (int k = 0; k < 16; k++) A.allow[k] = (float)allow[k];
   if (!need_w) {
@@ -612,17 +617,44 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
     }
     const double pmass = covh_pmass(h, p->pmass, fracfit);
     if (std::isnan(pmass)) { covh_Destroy(h); return fail(ctx, 31, "bad null histogram fit, pmass is nan"); }
-    double* sf = nullptr;
+    // tail by mass, then the tail fit (gamma: likelihood on the device) and
+    // the survival table on the device (src/covariation.c:1914-1973)
     double newmass = 0, mu = 0, lambda = 0, tau = 0;
-    char eb[256];
     auto tf0 = std::chrono::steady_clock::now();
-    int fs = p->doexpfit ? cov_NullFitExponential(h, &sf, pmass, &newmass, &mu, &lambda, 0, eb)
-                         : cov_NullFitGamma(h, &sf, pmass, &newmass, &mu, &lambda, &tau, 0, eb);
+    newmass = covh_SetTailByMass(h, pmass);
+    int evals = 0;
+    if (p->doexpfit) {
+      double n = 0.0, sk = 0.0;
+      for (int b = h->cmin; b <= h->imax; b++) { n += (double)h->obs[b]; sk += (double)(b - h->cmin) * (double)h->obs[b]; }
+      if (n <= 0) { covh_Destroy(h); return fail(ctx, 32, "could not do exponential fit"); }
+      mu = h->phi;
+      lambda = (sk > 0.0) ? log(1.0 + n / sk) / h->w : INFINITY;
+    } else {
+      if (!ctx->fitw) ctx->fitw = fitwork_create();
+      const int fs = gamma_fit_gpu(ctx->fitw, h->obs, h->cmin, h->imax, h->bmin, h->w, h->phi, ctx->st, &mu,
+                                   &lambda, &tau, &evals);
+      if (fs) { covh_Destroy(h); return fail(ctx, 32, "could not do a Gamma fit (%d)", fs); }
+    }
+    if (ctx->sfcap < 2 * h->nb) {
+      if (ctx->d_sf) cudaFree(ctx->d_sf);
+      if (ctx->d_tail) cudaFree(ctx->d_tail);
+      CK(dalloc(&ctx->d_sf, 2 * h->nb));
+      CK(dalloc(&ctx->d_tail, 2 * h->nb));
+      ctx->sfcap = 2 * h->nb;
+    }
+    std::vector<double> sfh;
+    double* sf = nullptr;
+    if (!std::isinf(lambda)) {
+      CK(launch_survfit(h->cmin, h->nb, h->bmin, h->w, newmass, p->doexpfit, mu, lambda, tau, ctx->d_sf, ctx->st));
+      sfh.resize(2 * (size_t)h->nb);
+      CK(cudaMemcpyAsync(sfh.data(), ctx->d_sf, sfh.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+      CK(cudaStreamSynchronize(ctx->st));
+      sf = sfh.data();
+    }
     ctx->fit_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tf0).count();
     if (getenv("COVGPU_DEBUG"))
-      fprintf(stderr, "covgpu: type %d nb %d tail bins %d fit %.2f ms mu %g lambda %g tau %g\n", covtypes[q], h->nb,
-              h->imax - h->cmin + 1, ctx->fit_ms, mu, lambda, tau);
-    if (fs) { covh_Destroy(h); free(sf); return fail(ctx, 32, "%s", eb); }
+      fprintf(stderr, "covgpu: type %d nb %d tail bins %d fit %.2f ms (%d evaluations) mu %g lambda %g tau %g\n",
+              covtypes[q], h->nb, h->imax - h->cmin + 1, ctx->fit_ms, evals, mu, lambda, tau);
     R.pmass = pmass; R.newmass = newmass; R.mu = mu; R.lambda = lambda; R.tau = tau;
     R.Nt = (uint64_t)P;
     R.sc_thresh = covh_evalue2cov(p->thresh, (double)P, h, sf);
@@ -634,15 +666,7 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
       double c = 0.0;
       for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tail[b] = c; }
     }
-    if (ctx->sfcap < 2 * h->nb) {
-      if (ctx->d_sf) cudaFree(ctx->d_sf);
-      if (ctx->d_tail) cudaFree(ctx->d_tail);
-      CK(dalloc(&ctx->d_sf, 2 * h->nb));
-      CK(dalloc(&ctx->d_tail, 2 * h->nb));
-      ctx->sfcap = 2 * h->nb;
-    }
     CK(cudaMemcpyAsync(ctx->d_tail, tail.data(), h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-    if (sf) CK(cudaMemcpyAsync(ctx->d_sf, sf, 2 * h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
     EvalTables T;
     T.sf = sf ? ctx->d_sf : nullptr;
     T.tail = ctx->d_tail;
@@ -673,7 +697,6 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
         return (a.i != b.i) ? a.i < b.i : a.j < b.j;
       });
     }
-    free(sf);
     covh_Destroy(h);
   }
   CK(cudaEventRecord(ctx->ev[3], ctx->st));

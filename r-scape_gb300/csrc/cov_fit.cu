@@ -1,0 +1,414 @@
+// cov_fit.cu -- binned maximum-likelihood gamma fit of the null tail with
+// the likelihood evaluated on the GPU (FP64).
+//
+// esl_gam_FitCompleteBinned (called at src/covariation.c:1956) is restated
+// as: location mu = phi (the tail's lower bound, fixed), rate lambda and
+// shape tau maximising sum_b obs_b log(S(lo_b) - S(hi_b)) over the tail bins
+// [cmin, imax], S(x) = Q(tau, lambda (x - mu)); Nelder-Mead (1965) on
+// (log lambda, log tau) from moment estimates.  The whole simplex search is
+// one cooperative launch: every iteration evaluates its reflection,
+// expansion and contraction points together (the same points a sequential
+// Nelder-Mead visits), each block summing a fixed chunk of the non-empty
+// tail bins; after a grid barrier every block adds the block sums in the
+// same fixed order, so all blocks hold bit-identical likelihoods and take
+// the same simplex decisions without a second barrier.  Results do not
+// depend on timing.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "cov_fit.h"
+
+namespace covgpu {
+
+// regularised upper incomplete gamma Q(a, x): series for x < a + 1, Lentz's
+// continued fraction otherwise (Abramowitz & Stegun 6.5.29, 6.5.31)
+__device__ double gamma_q_dev(double a, double x, double lga) {
+  if (x <= 0.0) return 1.0;
+  if (x < a + 1.0) {
+    double sum = 1.0 / a, del = sum, ap = a;
+    for (int n = 0; n < 10000; n++) {
+      ap += 1.0; del *= x / ap; sum += del;
+      if (fabs(del) < fabs(sum) * 1e-16) break;
+    }
+    return 1.0 - sum * exp(-x + a * log(x) - lga);
+  }
+  double b = x + 1.0 - a, c = 1.0 / 1e-300, d = 1.0 / b, h = d;
+  for (int i = 1; i < 10000; i++) {
+    const double an = -i * (i - a);
+    b += 2.0;
+    d = an * d + b; if (fabs(d) < 1e-300) d = 1e-300;
+    c = b + an / c; if (fabs(c) < 1e-300) c = 1e-300;
+    d = 1.0 / d;
+    const double del = d * c;
+    h *= del;
+    if (fabs(del - 1.0) < 1e-16) break;
+  }
+  return exp(-x + a * log(x) - lga) * h;
+}
+
+struct FitPoint { double lambda, tau, lga, lconst; };   // lconst = tau log lambda - lgamma(tau)
+
+// log of the gamma probability of the bin [lo, lo + h), location mu, with
+// logx = log(lo - mu) when lo > mu.
+// Far enough above mu (h <= (lo - mu) / 16, lambda h <= 1/2) the probability
+// is computed as f(x) * integral_0^h exp(g(t)) dt,  x = lo - mu,
+//   g(t) = (tau - 1) log(1 + t/x) - lambda t,
+// with exp(g) = sum_k c_k t^k from (x + t) E' = (tau - 1 - lambda (x + t)) E:
+//   c_{k+1} = ((tau - 1 - lambda x - k) c_k - lambda c_{k-1}) / (x (k + 1)),
+// summed as d_k = c_k h^k, which needs one log and avoids the cancellation
+// of Q(lo) - Q(hi); closer to mu the difference of Q is used.
+__constant__ double c_inv[64];   // c_inv[k] = 1 / (k + 1)
+
+__device__ double gam_logp_bin(double lo, double h, double mu, double logx, const FitPoint& P) {
+  const double x = lo - mu;
+  if (x > 0.0 && h <= 0.0625 * x && P.lambda * h <= 0.5) {
+    const double r = h / x, s = P.lambda * h;
+    double dkm1 = 0.0, dk = 1.0, sum = 1.0;
+    for (int k = 0; k < 60; k++) {
+      const double dk1 = (((P.tau - 1.0 - k) * r - s) * dk - s * r * dkm1) * c_inv[k];
+      const double term = dk1 * c_inv[k + 1];
+      sum += term;
+      dkm1 = dk; dk = dk1;
+      if (fabs(term) <= 1e-17 * fabs(sum)) break;
+    }
+    return P.lconst + (P.tau - 1.0) * logx - P.lambda * x + log(h * sum);
+  }
+  const double l = (lo < mu) ? mu : lo, hi = lo + h;
+  const double slo = (l <= mu) ? 1.0 : gamma_q_dev(P.tau, P.lambda * (l - mu), P.lga);
+  const double shi = (hi <= mu) ? 1.0 : gamma_q_dev(P.tau, P.lambda * (hi - mu), P.lga);
+  const double p = slo - shi;
+  return log(p > 0.0 ? p : 1e-300);
+}
+
+__device__ __forceinline__ uint64_t fit_clock() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+constexpr uint64_t kFitWaitNs = 2000000000ull;   // grid barrier gives up after 2 s
+
+struct FitOut { double lambda, tau; int evals, status; };
+
+struct FitGrid {
+  const int* bins;       // non-empty tail bins, in bin order
+  const double* cnts;    // their counts
+  double* logx;          // scratch: log(lower bound - mu) per bin
+  int nnz;
+  double bmin, w, mu;
+  double* part;          // [2][3][gridDim.x] block sums
+  unsigned* bar;         // arrival counter, zero at launch
+  FitOut* out;
+};
+
+// evaluates the npts points in pts (shared) over the tail.  The work items
+// (point q, bin k), point-major, are spread over all threads of the grid:
+// FP64 throughput is per SM, so the grid is sized to use every SM's FP64
+// unit before it stacks warps on one.  Each block sums its items per point,
+// arrives at the grid barrier, then adds all block sums in block order into
+// F (shared).  False when the barrier timed out.
+__device__ bool fit_eval(const FitGrid& g, const FitPoint* pts, int npts, unsigned& phase, double* F, double* red,
+                         int* flag) {
+  const int G = gridDim.x, T = G * blockDim.x, nw = blockDim.x >> 5;
+  const int nitems = npts * g.nnz;
+  double* part = g.part + (size_t)(phase & 1u) * 3 * G;
+  double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitems; it += T) {
+    const int q = it / g.nnz, k = it - q * g.nnz;
+    const int b = g.bins[k];
+    const double lo = g.w * b + g.bmin, hi = g.w * (b + 1) + g.bmin;
+    const double v = g.cnts[k] * gam_logp_bin(lo, hi - lo, g.mu, g.logx[k], pts[q]);
+    if (q == 0) acc0 -= v;
+    else if (q == 1) acc1 -= v;
+    else acc2 -= v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
+    acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
+    acc2 += __shfl_xor_sync(0xffffffffu, acc2, o);
+  }
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { red[warp * 3] = acc0; red[warp * 3 + 1] = acc1; red[warp * 3 + 2] = acc2; }
+  __syncthreads();
+  if (threadIdx.x < npts) {
+    double t = 0.0;
+    for (int i = 0; i < nw; i++) t += red[i * 3 + threadIdx.x];
+    part[threadIdx.x * G + blockIdx.x] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(g.bar, 1u);
+    const unsigned target = (phase + 1u) * (unsigned)G;
+    uint64_t t0 = 0;
+    int ok = 1;
+    while (ld_acquire(g.bar) < target) {
+      const uint64_t now = fit_clock();
+      if (t0 == 0) t0 = now;
+      else if (now - t0 > kFitWaitNs) { ok = 0; break; }
+    }
+    *flag = ok;
+  }
+  __syncthreads();
+  if (!*flag) return false;
+  if (threadIdx.x < 32) {
+    for (int q = 0; q < npts; q++) {
+      double t = 0.0;
+      for (int i = threadIdx.x; i < G; i += 32) t += __ldcg(part + q * G + i);
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (threadIdx.x == 0) F[q] = t;
+    }
+  }
+  __syncthreads();
+  phase++;
+  return true;
+}
+
+__device__ void fit_set_point(FitPoint* P, double l0, double l1) {
+  P->lambda = exp(l0);
+  P->tau = exp(l1);
+  P->lga = lgamma(P->tau);
+  P->lconst = P->tau * log(P->lambda) - P->lga;
+}
+
+// thread 0 has written the n simplex coordinates pc; lanes 0..n-1 turn them
+// into likelihood points in parallel
+__device__ __forceinline__ void fit_set_points(FitPoint* pts, const double (*pc)[2], int n) {
+  __syncthreads();
+  if ((int)threadIdx.x < n) fit_set_point(&pts[threadIdx.x], pc[threadIdx.x][0], pc[threadIdx.x][1]);
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256)
+k_gam_fit(FitGrid g, double s00, double s01) {
+  __shared__ FitPoint pts[3];
+  __shared__ double F[3], red[8 * 3], pc[3][2];
+  __shared__ int flag, ctl;
+  {
+    const int T = gridDim.x * blockDim.x;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.nnz; k += T) {
+      const double x = (g.w * g.bins[k] + g.bmin) - g.mu;
+      g.logx[k] = (x > 0.0) ? log(x) : 0.0;
+    }
+  }
+  // the bins' log x are read by other blocks' threads: made visible by the
+  // first grid barrier (fence before arrival), read after it
+  unsigned phase = 0;
+  int evals = 0, status = 0;
+  double S[3][2], SF[3];   // the simplex, kept by thread 0
+  if (threadIdx.x == 0) {
+    S[0][0] = s00;       S[0][1] = s01;
+    S[1][0] = s00 + 0.5; S[1][1] = s01;
+    S[2][0] = s00;       S[2][1] = s01 + 0.5;
+    for (int k = 0; k < 3; k++) { pc[k][0] = S[k][0]; pc[k][1] = S[k][1]; }
+    // a barrier round with no points publishes log x grid-wide
+  }
+  if (!fit_eval(g, pts, 0, phase, F, red, &flag)) status = 2;
+  fit_set_points(pts, pc, 3);
+  if (!status && !fit_eval(g, pts, 3, phase, F, red, &flag)) status = 2;
+  evals += 3;
+  if (threadIdx.x == 0) for (int k = 0; k < 3; k++) SF[k] = F[k];
+  for (int it = 0; it < 4000 && !status; it++) {
+    int lo = 0, hi = 0, md = 0;
+    if (threadIdx.x == 0) {
+      for (int k = 1; k < 3; k++) { if (SF[k] < SF[lo]) lo = k; if (SF[k] > SF[hi]) hi = k; }
+      md = 3 - lo - hi;
+      if (md == lo || md == hi || md < 0 || md > 2)
+        md = (hi == 0) ? ((lo == 1) ? 2 : 1) : ((hi == 1) ? ((lo == 0) ? 2 : 0) : ((lo == 0) ? 1 : 0));
+      if (fabs(SF[hi] - SF[lo]) <= 1e-12 * (fabs(SF[lo]) + 1e-30) && fabs(S[hi][0] - S[lo][0]) < 1e-9 &&
+          fabs(S[hi][1] - S[lo][1]) < 1e-9) {
+        ctl = 0;
+      } else {
+        const double c0 = 0.5 * (S[lo][0] + S[md][0]), c1 = 0.5 * (S[lo][1] + S[md][1]);
+        pc[0][0] = c0 + (c0 - S[hi][0]);       pc[0][1] = c1 + (c1 - S[hi][1]);         // reflection
+        pc[1][0] = c0 + 2.0 * (c0 - S[hi][0]); pc[1][1] = c1 + 2.0 * (c1 - S[hi][1]);   // expansion
+        pc[2][0] = c0 + 0.5 * (S[hi][0] - c0); pc[2][1] = c1 + 0.5 * (S[hi][1] - c1);   // contraction
+        ctl = 1;
+      }
+    }
+    __syncthreads();
+    if (!ctl) break;
+    fit_set_points(pts, pc, 3);
+    if (!fit_eval(g, pts, 3, phase, F, red, &flag)) { status = 2; break; }
+    evals += 3;
+    if (threadIdx.x == 0) {
+      const double fr = F[0];
+      ctl = 1;
+      if (fr < SF[lo]) {
+        if (F[1] < fr) { S[hi][0] = pc[1][0]; S[hi][1] = pc[1][1]; SF[hi] = F[1]; }
+        else           { S[hi][0] = pc[0][0]; S[hi][1] = pc[0][1]; SF[hi] = fr; }
+      } else if (fr < SF[md]) {
+        S[hi][0] = pc[0][0]; S[hi][1] = pc[0][1]; SF[hi] = fr;
+      } else if (F[2] < SF[hi]) {
+        S[hi][0] = pc[2][0]; S[hi][1] = pc[2][1]; SF[hi] = F[2];
+      } else {   // shrink towards the best vertex
+        int nq = 0;
+        for (int k = 0; k < 3; k++)
+          if (k != lo) {
+            pc[nq][0] = S[lo][0] + 0.5 * (S[k][0] - S[lo][0]);
+            pc[nq][1] = S[lo][1] + 0.5 * (S[k][1] - S[lo][1]);
+            nq++;
+          }
+        ctl = 2;
+      }
+    }
+    __syncthreads();
+    if (ctl == 2) {
+      fit_set_points(pts, pc, 2);
+      if (!fit_eval(g, pts, 2, phase, F, red, &flag)) { status = 2; break; }
+      evals += 2;
+      if (threadIdx.x == 0) {
+        int nq = 0;
+        for (int k = 0; k < 3; k++)
+          if (k != lo) { S[k][0] = pc[nq][0]; S[k][1] = pc[nq][1]; SF[k] = F[nq]; nq++; }
+      }
+    }
+    __syncthreads();
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int lo = 0;
+    for (int k = 1; k < 3; k++) if (SF[k] < SF[lo]) lo = k;
+    g.out->lambda = exp(S[lo][0]);
+    g.out->tau = exp(S[lo][1]);
+    g.out->evals = evals;
+    g.out->status = status;
+  }
+}
+
+struct FitWork {
+  int* d_bins = nullptr;
+  double* d_cnts = nullptr;
+  double* d_logx = nullptr;
+  int cap_bins = 0;
+  double* d_part = nullptr;
+  unsigned* d_bar = nullptr;
+  FitOut* d_out = nullptr;
+  FitOut* h_out = nullptr;   // pinned
+  int max_grid = 0;
+};
+
+FitWork* fitwork_create() { return new FitWork(); }
+void fitwork_destroy(FitWork* fw) {
+  if (!fw) return;
+  if (fw->d_bins) cudaFree(fw->d_bins);
+  if (fw->d_cnts) cudaFree(fw->d_cnts);
+  if (fw->d_logx) cudaFree(fw->d_logx);
+  if (fw->d_part) cudaFree(fw->d_part);
+  if (fw->d_bar) cudaFree(fw->d_bar);
+  if (fw->d_out) cudaFree(fw->d_out);
+  if (fw->h_out) cudaFreeHost(fw->h_out);
+  delete fw;
+}
+
+// survfit[b] = mass * S(upper bound of bin b) for b in [cmin, 2 nb), 0 below
+// (cov_histogram_SetSurvFitTail, src/covariation.c:1676-1699)
+__global__ void k_survfit(int cmin, int nb, double bmin, double w, double mass, int doexp, double mu, double lambda,
+                          double tau, double lga, double* __restrict__ sf) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < 2 * nb; b += gridDim.x * blockDim.x) {
+    double v = 0.0;
+    if (b >= cmin) {
+      const double x = w * (b + 1) + bmin;
+      double S;
+      if (x <= mu) S = 1.0;
+      else if (doexp) S = exp(-lambda * (x - mu));
+      else S = gamma_q_dev(tau, lambda * (x - mu), lga);
+      v = mass * S;
+    }
+    sf[b] = v;
+  }
+}
+
+cudaError_t launch_survfit(int cmin, int nb, double bmin, double w, double mass, int doexp, double mu, double lambda,
+                           double tau, double* d_sf, cudaStream_t st) {
+  const int n = 2 * nb;
+  k_survfit<<<std::max(1, std::min(1024, (n + 255) / 256)), 256, 0, st>>>(cmin, nb, bmin, w, mass, doexp, mu, lambda,
+                                                                          tau, doexp ? 0.0 : std::lgamma(tau), d_sf);
+  return cudaGetLastError();
+}
+
+// 0 ok, 1 empty tail, 2 barrier timeout, 90 CUDA error
+int gamma_fit_gpu(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, double bmin, double w, double phi,
+                  cudaStream_t st, double* ret_mu, double* ret_lambda, double* ret_tau, int* ret_evals) {
+  FitWork& fw = *fwp;
+  const double mu = phi;
+  // moment estimates of the start, and the non-empty tail bins
+  double m = 0.0, v = 0.0, n = 0.0;
+  std::vector<int> bins;
+  std::vector<double> cnts;
+  for (int b = cmin; b <= imax; b++) {
+    const double mid = (w * b + bmin) + 0.5 * w - mu;
+    n += (double)h_obs[b]; m += (double)h_obs[b] * mid;
+    if (h_obs[b]) { bins.push_back(b); cnts.push_back((double)h_obs[b]); }
+  }
+  if (n <= 0) return 1;
+  m /= n;
+  for (int b = cmin; b <= imax; b++) {
+    const double mid = (w * b + bmin) + 0.5 * w - mu;
+    v += (double)h_obs[b] * (mid - m) * (mid - m);
+  }
+  v /= n;
+  if (!(v > 0.0) || !(m > 0.0)) { v = w * w; if (!(m > 0.0)) m = w; }
+
+  if (!fw.max_grid) {
+    int dev = 0, nsm = 0, occ = 0, coop = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 90;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gam_fit, 256, 0) != cudaSuccess || !coop || occ < 1)
+      return 90;
+    fw.max_grid = nsm;   // one block per SM is co-resident
+    double inv[64];
+    for (int k = 0; k < 64; k++) inv[k] = 1.0 / (k + 1);
+    if (cudaMemcpyToSymbol(c_inv, inv, sizeof(inv)) != cudaSuccess) return 90;
+    if (cudaMalloc(&fw.d_part, sizeof(double) * 2 * 3 * fw.max_grid) != cudaSuccess) return 90;
+    if (cudaMalloc(&fw.d_bar, sizeof(unsigned)) != cudaSuccess) return 90;
+    if (cudaMalloc(&fw.d_out, sizeof(FitOut)) != cudaSuccess) return 90;
+    if (cudaMallocHost(&fw.h_out, sizeof(FitOut)) != cudaSuccess) return 90;
+  }
+  const int nnz = (int)bins.size();
+  if (fw.cap_bins < nnz) {
+    if (fw.d_bins) cudaFree(fw.d_bins);
+    if (fw.d_cnts) cudaFree(fw.d_cnts);
+    if (fw.d_logx) cudaFree(fw.d_logx);
+    fw.d_bins = nullptr; fw.d_cnts = nullptr; fw.d_logx = nullptr; fw.cap_bins = 0;
+    if (cudaMalloc(&fw.d_bins, sizeof(int) * nnz) != cudaSuccess) return 90;
+    if (cudaMalloc(&fw.d_cnts, sizeof(double) * nnz) != cudaSuccess) return 90;
+    if (cudaMalloc(&fw.d_logx, sizeof(double) * nnz) != cudaSuccess) return 90;
+    fw.cap_bins = nnz;
+  }
+  if (cudaMemcpyAsync(fw.d_bins, bins.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice, st) != cudaSuccess) return 90;
+  if (cudaMemcpyAsync(fw.d_cnts, cnts.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice, st) != cudaSuccess) return 90;
+  if (cudaMemsetAsync(fw.d_bar, 0, sizeof(unsigned), st) != cudaSuccess) return 90;
+
+  FitGrid g;
+  g.bins = fw.d_bins; g.cnts = fw.d_cnts; g.logx = fw.d_logx; g.nnz = nnz;
+  g.bmin = bmin; g.w = w; g.mu = mu;
+  g.part = fw.d_part; g.bar = fw.d_bar; g.out = fw.d_out;
+  double s00 = std::log(m / v), s01 = std::log(m * m / v);
+  void* args[] = {&g, &s00, &s01};
+  // one warp per SM until every SM has one, then up to 8 warps per block
+  const int nitems = 3 * nnz;
+  const int W = std::max(1, std::min(8, (nitems + 32 * fw.max_grid - 1) / (32 * fw.max_grid)));
+  const int G = std::max(1, std::min(fw.max_grid, (nitems + 32 * W - 1) / (32 * W)));
+  if (cudaLaunchCooperativeKernel((const void*)k_gam_fit, dim3(G), dim3(32 * W), args, 0, st) != cudaSuccess)
+    return 90;
+  if (cudaMemcpyAsync(fw.h_out, fw.d_out, sizeof(FitOut), cudaMemcpyDeviceToHost, st) != cudaSuccess) return 90;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return 90;
+  if (fw.h_out->status) return fw.h_out->status;
+  *ret_mu = mu;
+  *ret_lambda = fw.h_out->lambda;
+  *ret_tau = fw.h_out->tau;
+  if (ret_evals) *ret_evals = fw.h_out->evals;
+  return 0;
+}
+
+}  // namespace covgpu

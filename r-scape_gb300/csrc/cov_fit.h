@@ -1,0 +1,22 @@
+// cov_fit.h -- GPU pieces of the null-tail fit (internal).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace covgpu {
+
+struct FitWork;
+FitWork* fitwork_create();
+void     fitwork_destroy(FitWork* fw);
+
+// binned ML gamma fit of the tail bins [cmin, imax] of the histogram with
+// counts h_obs, location phi, likelihood evaluated on the device; 0 on success
+int gamma_fit_gpu(FitWork* fw, const uint64_t* h_obs, int cmin, int imax, double bmin,
+                  double w, double phi, cudaStream_t st, double* ret_mu, double* ret_lambda, double* ret_tau,
+                  int* ret_evals);
+
+// survfit table [2 nb] of a gamma (doexp = 0) or exponential tail
+cudaError_t launch_survfit(int cmin, int nb, double bmin, double w, double mass, int doexp, double mu, double lambda,
+                           double tau, double* d_sf, cudaStream_t st);
+
+}  // namespace covgpu

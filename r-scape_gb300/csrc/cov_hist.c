@@ -116,8 +116,8 @@ covh_pmass(const ESL_HISTOGRAM *h, double target_pmass, double target_fracfit)
 }
 
 /* the tail holding >= pmass of the samples; returns the tail's mass */
-static double
-covh_set_tail(ESL_HISTOGRAM *h, double pmass)
+double
+covh_SetTailByMass(ESL_HISTOGRAM *h, double pmass)
 {
   uint64_t sum = 0;
   int b;
@@ -179,16 +179,46 @@ covh_exp_surv(double x, void *params)
   return exp(-p[1] * (x - p[0]));
 }
 
-/* binned negative log likelihood of the tail bins [cmin, imax] with data;
- * the survival function is evaluated once per needed bin boundary, and the
- * bins are split into fixed contiguous chunks summed in chunk order, so the
- * result does not depend on the number of threads */
 #define NLL_CHUNKS 64
+
+/* log of the gamma probability of the bin [lo, lo + hw) when the bin is far
+ * enough above mu (hw <= (lo - mu) / 16, lambda hw <= 1/2): f(x) times
+ * integral_0^hw exp(g(t)) dt, x = lo - mu, g(t) = (tau-1) log(1 + t/x) - lambda t,
+ * from the power series of exp(g), whose coefficients follow
+ * (x + t) E' = (tau - 1 - lambda (x + t)) E:
+ *   c_{k+1} = ((tau - 1 - lambda x - k) c_k - lambda c_{k-1}) / (x (k + 1)).
+ * Returns 0 and leaves *ret_logp alone when the bin is too close to mu. */
+static int
+gam_logp_series(double lo, double hw, double mu, double lambda, double tau, double lconst, double *ret_logp)
+{
+  const double x = lo - mu;
+  double r, s, dkm1 = 0.0, dk = 1.0, sum = 1.0;
+  int k;
+  if (!(x > 0.0) || hw > 0.0625 * x || lambda * hw > 0.5) return 0;
+  r = hw / x; s = lambda * hw;
+  for (k = 0; k < 60; k++) {
+    const double dk1 = (((tau - 1.0 - k) * r - s) * dk - s * r * dkm1) / (k + 1);
+    const double term = dk1 / (k + 2);
+    sum += term;
+    dkm1 = dk; dk = dk1;
+    if (fabs(term) <= 1e-17 * fabs(sum)) break;
+  }
+  *ret_logp = lconst + (tau - 1.0) * log(x) - lambda * x + log(hw * sum);
+  return 1;
+}
+
+/* negative log-likelihood of the tail bins [cmin, imax] under a gamma at
+ * location mu: -sum_b obs_b log(S(lo_b) - S(hi_b)), the bin probability
+ * taken from the series above where it applies.  The bins are summed in a
+ * fixed number of chunks (in parallel when OpenMP is on) whose partial sums
+ * are added in chunk order, so the result does not depend on the number of
+ * threads */
 static double
 gam_nll(const ESL_HISTOGRAM *h, double mu, double lambda, double tau)
 {
   double part[NLL_CHUNKS], prm[3], nll = 0.0;
   const int b0 = h->cmin, nbins = h->imax - h->cmin + 1;
+  const double lconst = tau * log(lambda) - lgamma(tau);
   int c;
   prm[0] = mu; prm[1] = lambda; prm[2] = tau;
   if (nbins <= 0) return 0.0;
@@ -201,11 +231,17 @@ gam_nll(const ESL_HISTOGRAM *h, double mu, double lambda, double tau)
     double acc = 0.0, s_hi = 0.0;
     int b, have = 0;
     for (b = lo_b; b < hi_b; b++) {
-      double lo, slo, p;
+      double lo, hi, slo, p, lp;
       if (h->obs[b] == 0) { have = 0; continue; }
-      lo = covh_Bin2LBound(h, b); if (lo < mu) lo = mu;
+      lo = covh_Bin2LBound(h, b); hi = covh_Bin2UBound(h, b);
+      if (gam_logp_series(lo, hi - lo, mu, lambda, tau, lconst, &lp)) {
+        acc -= (double)h->obs[b] * lp;
+        have = 0;
+        continue;
+      }
+      if (lo < mu) lo = mu;
       slo = have ? s_hi : covh_gamma_surv(lo, prm);
-      s_hi = covh_gamma_surv(covh_Bin2UBound(h, b), prm);
+      s_hi = covh_gamma_surv(hi, prm);
       have = 1;
       p = slo - s_hi;
       if (!(p > 0.0)) p = 1e-300;
@@ -312,7 +348,7 @@ cov_NullFitExponential(ESL_HISTOGRAM *h, double **ret_survfit, double pmass, dou
 {
   double ep[2], newmass;
   (void)verbose;
-  newmass = covh_set_tail(h, pmass);
+  newmass = covh_SetTailByMass(h, pmass);
   if (fit_exp(h, &ep[0], &ep[1]) != eslOK) {
     if (errbuf) snprintf(errbuf, 256, "could not do exponential fit");
     return eslFAIL;
@@ -329,7 +365,7 @@ cov_NullFitGamma(ESL_HISTOGRAM *h, double **ret_survfit, double pmass, double *r
 {
   double ep[3], newmass;
   (void)verbose;
-  newmass = covh_set_tail(h, pmass);
+  newmass = covh_SetTailByMass(h, pmass);
   if (fit_gamma(h, &ep[0], &ep[1], &ep[2]) != eslOK) {
     if (errbuf) snprintf(errbuf, 256, "could not do a Gamma fit");
     return eslFAIL;

@@ -107,46 +107,88 @@ k_count_simt(const uint8_t* __restrict__ ax, int64_t slot_stride, const float* _
     }
 }
 
+// double-float arithmetic (pairs of fp32 values, ~48-bit significand)
+struct df { float hi, lo; };
+
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {   // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ df df_add_f(df a, float b) {
+  const df s = two_sum(a.hi, b);
+  return fast_two_sum(s.hi, s.lo + a.lo);
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  const df s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = a.hi * b.hi;
+  const float e = fmaf(a.hi, b.hi, -p);
+  return fast_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ df df_of(double x) {
+  const float hi = (float)x;
+  return {hi, (float)(x - (double)hi)};
+}
+__device__ __forceinline__ double df_to_d(df a) { return (double)a.hi + (double)a.lo; }
+
+
 // ------------------------------------------------------------------------
 // Block helper for the per-tile kernels: 256 threads, thread tid owns the
 // pairs p = tid + 256k (k = 0..3): row a = (tid >> 5) + 8k, column b = lane.
 // Reduces NV channels of per-pair values into per-row sums (of rv) and
-// per-column sums (of cv) and stores them in the partial layout
-// part[I][J][a][c] (rows of tile (I,J)) and part[J][I][b][c] (columns);
-// a diagonal tile adds both roles into part[I][I].
+// per-column sums (of cv) in double-float arithmetic and stores them as FP64
+// in the partial layout part[I][J][a][c] (rows of tile (I,J)) and
+// part[J][I][b][c] (columns); a diagonal tile adds both roles into
+// part[I][I].
 // ------------------------------------------------------------------------
+__device__ __forceinline__ df warp_sum_df(df v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const df w = {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = df_add(v, w);
+  }
+  return v;
+}
+
 template <int NV>
-__device__ __forceinline__ void tile_rowcol_store2(const double (&rv)[4][NV], const double (&cv)[4][NV],
+__device__ __forceinline__ void tile_rowcol_store2(const df (&rv)[4][NV], const df (&cv)[4][NV],
                                                    double* __restrict__ part, int nT, int I, int J) {
-  __shared__ double colbuf[8][TP][NV];
-  __shared__ double rowbuf[TP][NV];
+  __shared__ df colbuf[8][TP][NV];
+  __shared__ df rowbuf[TP][NV];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #pragma unroll
   for (int k = 0; k < 4; k++)
 #pragma unroll
     for (int c = 0; c < NV; c++) {
-      double r = warp_sum_d(rv[k][c]);
+      const df r = warp_sum_df(rv[k][c]);
       if (lane == 0) rowbuf[warp + 8 * k][c] = r;
     }
 #pragma unroll
-  for (int c = 0; c < NV; c++) colbuf[warp][lane][c] = cv[0][c] + cv[1][c] + cv[2][c] + cv[3][c];
+  for (int c = 0; c < NV; c++) colbuf[warp][lane][c] = df_add(df_add(cv[0][c], cv[1][c]), df_add(cv[2][c], cv[3][c]));
   __syncthreads();
   if (tid < TP * NV) {
     const int col = tid / NV, c = tid % NV;
-    double cs = 0.0;
-    for (int wv = 0; wv < 8; wv++) cs += colbuf[wv][col][c];
+    df cs = {0.f, 0.f};
+    for (int wv = 0; wv < 8; wv++) cs = df_add(cs, colbuf[wv][col][c]);
     if (I == J) {
-      part[(((int64_t)I * nT + J) * TP + col) * NV + c] = rowbuf[col][c] + cs;
+      part[(((int64_t)I * nT + J) * TP + col) * NV + c] = df_to_d(df_add(rowbuf[col][c], cs));
     } else {
-      part[(((int64_t)I * nT + J) * TP + col) * NV + c] = rowbuf[col][c];
-      part[(((int64_t)J * nT + I) * TP + col) * NV + c] = cs;
+      part[(((int64_t)I * nT + J) * TP + col) * NV + c] = df_to_d(rowbuf[col][c]);
+      part[(((int64_t)J * nT + I) * TP + col) * NV + c] = df_to_d(cs);
     }
   }
   __syncthreads();
 }
 
 template <int NV>
-__device__ __forceinline__ void tile_rowcol_store(const double (&v)[4][NV], double* __restrict__ part, int nT, int I,
+__device__ __forceinline__ void tile_rowcol_store(const df (&v)[4][NV], double* __restrict__ part, int nT, int I,
                                                   int J) {
   tile_rowcol_store2<NV>(v, v, part, nT, I, J);
 }
@@ -164,7 +206,7 @@ k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ til
   const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   const float* C = cnt + ((int64_t)slot * ntiles + t) * 16 * TPP;
-  double rv[4][4], cv[4][4], nr[4][1], zero[4][1];
+  df rv[4][4], cv[4][4], nr[4][1], zero[4][1];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
@@ -184,11 +226,11 @@ k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ til
     const float invS = ok ? 1.0f / (16e-10f + ne) : 0.f;
 #pragma unroll
     for (int x = 0; x < 4; x++) {
-      rv[k][x] = ok ? (double)((4e-10f + row[x]) * invS) : 0.0;
-      cv[k][x] = ok ? (double)((4e-10f + col[x]) * invS) : 0.0;
+      rv[k][x] = {ok ? (4e-10f + row[x]) * invS : 0.f, 0.f};
+      cv[k][x] = {ok ? (4e-10f + col[x]) * invS : 0.f, 0.f};
     }
-    nr[k][0] = pair ? (double)ne : 0.0;
-    zero[k][0] = 0.0;
+    nr[k][0] = {pair ? ne : 0.f, 0.f};
+    zero[k][0] = {0.f, 0.f};
   }
   tile_rowcol_store2<4>(rv, cv, part4 + (int64_t)slot * nT * nT * TP * 4, nT, tr.I, tr.J);
   tile_rowcol_store2<1>(nr, zero, partR + (int64_t)slot * nT * nT * TP, nT, tr.I, tr.J);
@@ -277,36 +319,6 @@ __global__ void k_ps(const uint8_t* __restrict__ ax, int64_t slot_stride, const 
 // do = 1e-10 - 16e-10 C / ne (to 1e-18 absolute), the prior of
 // src/correlators.c:1713 and the normalisation of :1758.
 // ------------------------------------------------------------------------
-struct df { float hi, lo; };
-
-__device__ __forceinline__ df two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  return {s, (a - (s - bb)) + (b - bb)};
-}
-__device__ __forceinline__ df fast_two_sum(float a, float b) {   // |a| >= |b|
-  const float s = a + b;
-  return {s, b - (s - a)};
-}
-__device__ __forceinline__ df df_add_f(df a, float b) {
-  const df s = two_sum(a.hi, b);
-  return fast_two_sum(s.hi, s.lo + a.lo);
-}
-__device__ __forceinline__ df df_add(df a, df b) {
-  const df s = two_sum(a.hi, b.hi);
-  return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
-}
-__device__ __forceinline__ df df_mul(df a, df b) {
-  const float p = a.hi * b.hi;
-  const float e = fmaf(a.hi, b.hi, -p);
-  return fast_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
-}
-__device__ __forceinline__ df df_of(double x) {
-  const float hi = (float)x;
-  return {hi, (float)(x - (double)hi)};
-}
-__device__ __forceinline__ double df_to_d(df a) { return (double)a.hi + (double)a.lo; }
-
 // u = o - e with o = c + dc (c >= 0 exact fp32, |dc| tiny), e in double-float
 __device__ __forceinline__ float diff_oe(float c, float dc, df e) {
   const df s = two_sum(c, -e.hi);
@@ -356,12 +368,16 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
     const long long sr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
     const long long sc = cc[0] * cc[0] + cc[1] * cc[1] + cc[2] * cc[2] + cc[3] * cc[3];
     const long long twice = 2 * nA * nA - sr - sc;     // 2 c_ij, even
-    double cij = (double)(twice / 2);
+    // cij / (N(N-1)) and (N - nA) / N, each correctly rounded: a reciprocal
+    // product refined by one FMA residual step (Markstein)
     const double Nd = (double)A.N;
-    cij /= (A.N > 1) ? Nd * (Nd - 1.0) : 1.0;
-    cij *= 2.0;
-    const double qij = (double)((long long)A.N - nA) / Nd;
-    out.raf = cij - 1.0 * qij;
+    const double D = (A.N > 1) ? Nd * (Nd - 1.0) : 1.0;
+    const double cnum = (double)(twice / 2), qnum = (double)((long long)A.N - nA);
+    double q1 = cnum * A.invD;
+    q1 = fma(fma(-q1, D, cnum), A.invD, q1);
+    double q2 = qnum * A.invN;
+    q2 = fma(fma(-q2, Nd, qnum), A.invN, q2);
+    out.raf = 2.0 * q1 - 1.0 * q2;
   }
   // ---- CCF (src/correlators.c:1038-1053), FP64 ----
   if (S & S_CCF) {
@@ -482,7 +498,7 @@ k_stats(StatsArgs A) {
   const double* pm = A.pm + (int64_t)slot * A.Lp * 4;
   const float2* pmdf = A.pmdf + (int64_t)slot * A.Lp * 4;
   const double* meanp = A.meanp + slot * 4;
-  double rs[4][MAXOUT];
+  df rs[4][MAXOUT];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
@@ -503,17 +519,27 @@ k_stats(StatsArgs A) {
     }
 #pragma unroll
     for (int q = 0; q < MAXOUT; q++) {
-      const double v = (q < A.nout && valid) ? pick(o, A.outstat[q]) : 0.0;
-      rs[k][q] = v;
-      if (q < A.nout) A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = v;
+      const int st = (q < A.nout) ? A.outstat[q] : -1;
+      if (st == 6 || st == 8) {   // FP64 results
+        const double v = valid ? pick(o, st) : 0.0;
+        rs[k][q] = df_of(v);
+        A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = v;
+      } else {
+        const float v = (st >= 0 && valid) ? (float)pick(o, st) : 0.f;
+        rs[k][q] = {v, 0.f};
+        if (st >= 0) A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = (double)v;
+      }
     }
   }
   // per-statistic row/column sums for APC/ASC
-  for (int q = 0; q < A.nout; q++) {
-    double v[4][1];
 #pragma unroll
-    for (int k = 0; k < 4; k++) v[k][0] = rs[k][q];
-    tile_rowcol_store<1>(v, A.part1 + (((int64_t)slot * A.nout + q) * A.nT * A.nT) * TP, A.nT, tr.I, tr.J);
+  for (int q = 0; q < MAXOUT; q++) {
+    if (q < A.nout) {
+      df v[4][1];
+#pragma unroll
+      for (int k = 0; k < 4; k++) v[k][0] = rs[k][q];
+      tile_rowcol_store<1>(v, A.part1 + (((int64_t)slot * A.nout + q) * A.nT * A.nT) * TP, A.nT, tr.I, tr.J);
+    }
   }
 }
 
@@ -531,7 +557,7 @@ k_rafs(const double* __restrict__ raf, double* __restrict__ out, int64_t slot_st
   const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   const double* B = raf + slot * slot_stride_in;
-  double v[4][1];
+  df v[4][1];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
@@ -544,7 +570,7 @@ k_rafs(const double* __restrict__ raf, double* __restrict__ out, int64_t slot_st
       r *= 0.25;
     }
     out[slot * slot_stride_out + (int64_t)t * TPP + p] = r;
-    v[k][0] = r;
+    v[k][0] = df_of(r);
   }
   tile_rowcol_store<1>(v, part1 + slot * part_stride, nT, tr.I, tr.J);
 }
@@ -680,13 +706,17 @@ k_hist(const double* __restrict__ cov, int64_t slot_stride, const TileRC* __rest
     for (int k = 0; k < 4; k++) {
       const int p = tid + 256 * k, a = p >> 5, b = p & 31;
       const int i = tr.I * TP + a, j = tr.J * TP + b;
+      int bin = -1;
       if (i < j && j < L) {
         double x = V[p];
         if (!(x > lo)) x = lo;
-        const int bin = exact_bin(x, bmin, w, invw);
-        if (bin < 0 || bin >= nbcap) atomicExch(status, 4);
-        else if (bin >= b0 && bin < b0 + nwin) atomicAdd(sh + (bin - b0), 1u);
+        bin = exact_bin(x, bmin, w, invw);
+        if (bin < 0 || bin >= nbcap) { atomicExch(status, 4); bin = -1; }
+        else if (bin < b0 || bin >= b0 + nwin) bin = -1;
       }
+      // one shared-memory atomic per distinct bin of the warp
+      const unsigned grp = __match_any_sync(0xffffffffu, bin);
+      if (bin >= 0 && (__ffs(grp) - 1) == (int)(threadIdx.x & 31)) atomicAdd(sh + (bin - b0), (unsigned)__popc(grp));
     }
   }
   __syncthreads();
@@ -795,12 +825,12 @@ k_tile_rowsums(const double* __restrict__ tilev, const TileRC* __restrict__ tile
                double* __restrict__ part1) {
   const int t = blockIdx.x, tid = threadIdx.x;
   const TileRC tr = tiles[t];
-  double v[4][1];
+  df v[4][1];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
-    v[k][0] = (i < j && j < L) ? tilev[(int64_t)t * TPP + p] : 0.0;
+    v[k][0] = df_of((i < j && j < L) ? tilev[(int64_t)t * TPP + p] : 0.0);
   }
   tile_rowcol_store<1>(v, part1, nT, tr.I, tr.J);
 }

@@ -11,18 +11,27 @@
 //            limbs q = l0 + 2^8 l1 + 2^16 l2 (integers <= 255, exact in BF16)
 // Each limb accumulates in its own FP32 TMEM accumulator, where the sum
 // (<= 255 N < 2^24 for N <= 65536) is an exact integer; the epilogue forms
-// C = (D0 + 2^8 D1 + 2^16 D2) 2^-E in FP64, so the counts are exact for the
-// quantised weights (exact integers under unit weights, one limb).
+// the 40-bit integer D0 + 2^8 D1 + 2^16 D2 in 64-bit integer arithmetic and
+// rounds it once to FP32 (times the power of two 2^-E), so each count is the
+// correctly rounded value of the exact count of the quantised weights, with
+// no FP64 on the path (exact integers under unit weights, one limb).
+//
+// Operand rows are state-major inside each 32-column tile
+// (row = 128 tile + 32 x + column), so accumulator row m = 32 x + a and
+// column n = 32 y + b: warp x, lane a of the epilogue holds cell (x, y) of
+// the pairs (a, b = 0..31), one contiguous 128-byte row of the count tile.
 //
 // Kernel: one CTA per (column tile I <= J, alignment); M = N = 128 (32
 // columns x 4 states each side), K in blocks of 64 sequences.  Warp 0 lane 0
 // issues TMA loads (128B-swizzled boxes) into a 3-4 stage ring guarded by
 // mbarriers, warp 1 lane 0 issues tcgen05.mma (kind::f16, 128x128x16) into
-// TMEM and frees stages with tcgen05.commit; after the last block all four
-// warps read TMEM (tcgen05.ld 32x32b) and write the counts tile in the same
-// layout as the SIMT kernel.  Every wait is bounded: on timeout the kernel
-// records an error code, drains its copies with a bounded wait and frees
-// TMEM before returning.
+// TMEM and frees stages with tcgen05.commit; after the last block each warp
+// reads its 32 TMEM lanes (tcgen05.ld 32x32b.x32), combines the limbs, writes
+// the 32x32 block of one cell into a 128B-swizzled shared buffer (conflict
+// free) and stores it with a TMA tensor store, double-buffered.  The counts
+// land in the layout of the SIMT kernel, [slot][tile][cell][32 a][32 b].
+// Every wait is bounded: on timeout the kernel records an error code, drains
+// its copies with a bounded wait and frees TMEM before returning.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -150,9 +159,36 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
 }
 
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, const void* src, int x, int y) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(map),
+               "r"(smem_u32(src)), "r"(x), "r"(y)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // operand preparation: codes [slot][N][Lp] -> BF16 one-hot rows [4Lp][Npad]
-// (A) and limb-scaled rows (B_l); one CTA per (64 sequences, 32 columns, slot)
+// (A) and limb-scaled rows (B_l), row 128 t + 32 x + c for column 32 t + c
+// and state x; one CTA per (64 sequences, 32 columns, slot)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
 k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, int Npad, int nslots, int nl,
@@ -168,13 +204,13 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
   if (tid < 64)
     for (int l = 0; l < nl; l++) lb[l][tid] = (s0 + tid < N) ? (unit ? 1 : limbs[l * Npad + s0 + tid]) : 0;
   __syncthreads();
-  // 128 rows (4 states x 32 columns) x 64 sequences; each thread writes
-  // 8 consecutive sequences (16 bytes) of one row
+  // 128 rows (4 states x 32 columns, state-major) x 64 sequences; each
+  // thread writes 8 consecutive sequences (16 bytes) of one row
   const int64_t rows_per_buf = (int64_t)nslots * 4 * Lp;
   for (int e = tid; e < 128 * 8; e += 256) {
     const int r = e / 8, chunk = e % 8;
-    const int c = r / 4, x = r % 4;
-    const int64_t row = (int64_t)slot * 4 * Lp + 4 * (c0 + c) + x;
+    const int x = r / 32, c = r % 32;
+    const int64_t row = (int64_t)slot * 4 * Lp + 4 * c0 + r;
     __align__(16) __nv_bfloat16 va[8];
     __align__(16) __nv_bfloat16 vb[3][8];
 #pragma unroll
@@ -197,8 +233,9 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
 // ---------------------------------------------------------------------------
 template <int NL, int STAGES>
 __global__ void __launch_bounds__(128, 1)
-k_count_umma(const __grid_constant__ CUtensorMap tmap, const TileRC* __restrict__ tiles, int ntiles, int nslots,
-             int Lp, int nkb, double scale, float* __restrict__ cnt, int* __restrict__ err) {
+k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
+             const TileRC* __restrict__ tiles, int ntiles, int nslots, int Lp, int nkb, float s_hi, float s_lo,
+             int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // 1024-byte aligned ring: stage s = [A | B_0 .. B_{NL-1}], 16 KB each
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -279,44 +316,63 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const TileRC* __restrict_
     umma_commit(&done_bar);
   }
   __syncwarp();
-  // ---- epilogue: all four warps ----
+  // ---- epilogue: warp x owns TMEM lanes 32x..32x+31 = cell row x ----
   bool ok = mbar_wait(&done_bar, 0);
   if (!ok) { atomicExch(err, 103); abort_flag = 1; }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   __syncthreads();
-  float* stage = reinterpret_cast<float*>(smem);   // [16 cells][32][33] (ring is idle now)
-  const int m = warp * 32 + lane;                  // accumulator row = TMEM lane
-  const int a = m >> 2, x = m & 3;
   if (!abort_flag) {
+    // two 4 KB staging buffers per warp in the idle ring (1024-byte aligned)
+    uint8_t* wbuf = smem + (size_t)warp * 8192;
+    const int orow0 = ((slot * ntiles + t) * 16 + warp * 4) * 32;   // cell (x = warp, y = 0), a = 0
 #pragma unroll 1
-    for (int c0 = 0; c0 < UN; c0 += 16) {
-      float d[NL][16];
+    for (int y = 0; y < 4; y++) {
+      uint32_t d[NL][32];
 #pragma unroll
       for (int l = 0; l < NL; l++)
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * UN + c0), d[l]);
+        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * UN + y * 32), d[l]);
+      tmem_ld_wait();
+      float v[32];
 #pragma unroll
-      for (int k = 0; k < 16; k++) {
-        double v = (double)d[0][k];
-        if (NL > 1) v += 256.0 * (double)d[1][k];
-        if (NL > 2) v += 65536.0 * (double)d[NL > 2 ? 2 : 0][k];
-        const int n = c0 + k, b = n >> 2, y = n & 3;
-        stage[(x * 4 + y) * (32 * 33) + a * 33 + b] = (float)(v * scale);
+      for (int k = 0; k < 32; k++) {
+        if (NL == 1) {
+          // exact integer times the scale, rounded once (s_lo carries the
+          // part of the scale below FP32 precision)
+          const float c = __uint_as_float(d[0][k]);
+          const float p = c * s_hi;
+          v[k] = p + (fmaf(c, s_hi, -p) + c * s_lo);
+        } else {
+          uint64_t q = (uint64_t)__float2uint_rn(__uint_as_float(d[0][k]));
+          q += (uint64_t)__float2uint_rn(__uint_as_float(d[1][k])) << 8;
+          if (NL > 2) q += (uint64_t)__float2uint_rn(__uint_as_float(d[NL > 2 ? 2 : 0][k])) << 16;
+          v[k] = __ull2float_rn(q) * s_hi;   // s_hi = 2^-E, exact
+        }
+      }
+      uint8_t* buf = wbuf + (y & 1) * 4096;
+      if (y >= 2) {
+        if (lane == 0) bulk_wait_read<1>();   // the store of y - 2 has read this buffer
+        __syncwarp();
+      }
+      // row a = lane, 16-byte chunk c at position c ^ (a & 7) (128B swizzle)
+#pragma unroll
+      for (int c = 0; c < 8; c++)
+        *reinterpret_cast<float4*>(buf + lane * 128 + ((c ^ (lane & 7)) << 4)) =
+            make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+      fence_proxy_async();
+      __syncwarp();
+      if (lane == 0) {
+        tma_store_2d(&omap, buf, 0, orow0 + y * 32);
+        bulk_commit();
       }
     }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (!abort_flag) {
-    float* out = cnt + ((int64_t)slot * ntiles + t) * 16 * TPP;
-    for (int e = tid; e < 16 * TPP; e += 128) {
-      const int cell = e / TPP, p = e % TPP;
-      out[e] = stage[cell * (32 * 33) + (p >> 5) * 33 + (p & 31)];
-    }
+    if (lane == 0) bulk_wait_all();
+    __syncwarp();
   } else if (tid == 0) {
     // drain the copies this CTA issued before freeing its shared memory
     for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; kb++)
       mbar_wait(&full_bar[kb % STAGES], (uint32_t)(kb / STAGES) & 1u);
   }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
@@ -344,7 +400,7 @@ constexpr int STAGES1 = 4;   // 1 limb : 32 KB per stage
 static size_t smem_bytes(int nl) {
   const int stages = (nl == 1) ? STAGES1 : STAGES3;
   const size_t ring = (size_t)stages * TILE_BYTES * (1 + nl);
-  const size_t stage_out = (size_t)16 * 32 * 33 * sizeof(float);
+  const size_t stage_out = (size_t)4 * 8192;   // two 4 KB buffers per warp
   return std::max(ring, stage_out) + 1024;
 }
 
@@ -418,21 +474,40 @@ void umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t st) {
   cudaStreamSynchronize(st);
 }
 
+// TMA store map over the count buffer [maxslots][ntiles][16][32][32] FP32,
+// viewed as rows of 32 counts, box 32 x 32, 128-byte swizzle
+static bool encode_out_map(UmmaPlan* p, float* cnt, CUtensorMap* m) {
+  const uint64_t rows = (uint64_t)p->maxslots * p->ntiles * 16 * 32;
+  if (rows >= ((uint64_t)1 << 31)) return false;
+  cuuint64_t gdim[2] = {32, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {32 * sizeof(float)};
+  cuuint32_t box[2] = {32, 32};
+  cuuint32_t estride[2] = {1, 1};
+  return get_encode()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, cnt, gdim, gstride, box, estride,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
                        cudaStream_t st) {
   if (nslots > p->maxslots) return cudaErrorInvalidValue;
+  if (((uintptr_t)cnt & 15u) != 0) return cudaErrorInvalidValue;
+  CUtensorMap omap;
+  if (!encode_out_map(p, cnt, &omap)) return cudaErrorInvalidValue;
   const int nl = unit ? 1 : p->nl;
   dim3 pg(p->Npad / 64, p->Lp / 32, nslots);
   k_umma_prep<<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, nl, p->d_limbs, unit, p->d_ops);
   const int nkb = p->Npad / UK;
+  // the scale as an unevaluated FP32 pair (a power of two with limbs)
   const double scale = unit ? 1.0 : p->scale;
+  const float s_hi = (float)scale, s_lo = (float)(scale - (double)s_hi);
   dim3 grid(p->ntiles, nslots);
   if (nl == 1)
-    k_count_umma<1, STAGES1><<<grid, 128, smem_bytes(1), st>>>(p->tmap, p->d_tiles, p->ntiles, p->maxslots, p->Lp,
-                                                               nkb, scale, cnt, p->d_err);
+    k_count_umma<1, STAGES1><<<grid, 128, smem_bytes(1), st>>>(p->tmap, omap, p->d_tiles, p->ntiles, p->maxslots,
+                                                               p->Lp, nkb, s_hi, s_lo, p->d_err);
   else
-    k_count_umma<3, STAGES3><<<grid, 128, smem_bytes(3), st>>>(p->tmap, p->d_tiles, p->ntiles, p->maxslots, p->Lp,
-                                                               nkb, scale, cnt, p->d_err);
+    k_count_umma<3, STAGES3><<<grid, 128, smem_bytes(3), st>>>(p->tmap, omap, p->d_tiles, p->ntiles, p->maxslots,
+                                                               p->Lp, nkb, s_hi, s_lo, p->d_err);
   return cudaGetLastError();
 }
 
