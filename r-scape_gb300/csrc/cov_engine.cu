@@ -38,7 +38,11 @@ struct covgpu_ctx {
   float* d_ucnt = nullptr;
   double *d_part4 = nullptr, *d_partR = nullptr, *d_pm = nullptr, *d_meanp = nullptr, *d_ps = nullptr;
   float2* d_pmdf = nullptr;
-  double *d_cov = nullptr, *d_cov2 = nullptr, *d_part1 = nullptr, *d_colx = nullptr, *d_avg = nullptr;
+  float2 *d_cov = nullptr, *d_cov2 = nullptr;   // score planes as double-float pairs
+  float2* d_colxf = nullptr;
+  float4* d_apcf = nullptr;
+  double* d_evt = nullptr;                      // E-value planes for the host
+  double *d_part1 = nullptr, *d_colx = nullptr, *d_avg = nullptr;
   double *d_tmin = nullptr, *d_tmax = nullptr, *d_mm = nullptr;
   int* d_status = nullptr;
   int last_nout = 0, last_first = 0, last_nslots = 0;
@@ -133,7 +137,9 @@ extern "C" int covgpu_create(covgpu_ctx** ret, int device, int N, int L, int max
   CK(dalloc(&ctx->d_cov, S * MAXOUT * ntl * TPP));
   CK(dalloc(&ctx->d_part1, S * MAXOUT * nT2 * TP));
   CK(dalloc(&ctx->d_colx, S * MAXOUT * ctx->Lp));
+  CK(dalloc(&ctx->d_colxf, S * MAXOUT * ctx->Lp));
   CK(dalloc(&ctx->d_avg, S * MAXOUT));
+  CK(dalloc(&ctx->d_apcf, S * MAXOUT));
   CK(dalloc(&ctx->d_tmin, S * MAXOUT * ntl));
   CK(dalloc(&ctx->d_tmax, S * MAXOUT * ntl));
   CK(dalloc(&ctx->d_mm, S * MAXOUT * 2));
@@ -157,7 +163,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
                   ctx->d_part1, ctx->d_colx, ctx->d_avg, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status,
                   ctx->d_left, ctx->d_right, ctx->d_lnodes, ctx->d_fitch, ctx->d_scratch, ctx->d_obs, ctx->d_sf,
                   ctx->d_tail, ctx->d_nhits, ctx->d_hi, ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->d_full,
-                  ctx->d_flush, ctx->d_pmdf};
+                  ctx->d_flush, ctx->d_pmdf, ctx->d_colxf, ctx->d_apcf, ctx->d_evt};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (ctx->umma) umma_plan_destroy(ctx->umma);
   if (ctx->fitw) fitwork_destroy(ctx->fitw);
@@ -377,14 +383,14 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   for (int r = 0; r < nrafs; r++) {
     const int q = rafs_q[r];
     if (!ctx->d_cov2) CK(dalloc(&ctx->d_cov2, (size_t)ctx->maxslots * plane));
-    CK(cudaMemcpy2DAsync(ctx->d_cov2, plane * sizeof(double), ctx->d_cov + q * plane, ntypes * plane * sizeof(double),
-                         plane * sizeof(double), nslots, cudaMemcpyDeviceToDevice, ctx->st));
+    CK(cudaMemcpy2DAsync(ctx->d_cov2, plane * sizeof(float2), ctx->d_cov + q * plane, ntypes * plane * sizeof(float2),
+                         plane * sizeof(float2), nslots, cudaMemcpyDeviceToDevice, ctx->st));
     CK(launch_rafs(ctx->d_cov2, ctx->d_cov + q * plane, plane, ntypes * plane, ctx->d_tiles, ctx->d_tile_index, ntiles,
                    nT, L, nslots, ctx->d_part1 + q * pplane, ntypes * pplane, ctx->st));
     ctx->nlaunch += 1;
   }
-  CK(launch_apc(ctx->d_cov, ctx->d_part1, ctx->d_colx, ctx->d_avg, ct, ctx->d_tiles, ntiles, nT, L, Lp,
-                nslots * ntypes, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status, ctx->st));
+  CK(launch_apc(ctx->d_cov, ctx->d_part1, ctx->d_colx, ctx->d_colxf, ctx->d_avg, ctx->d_apcf, ct, ctx->d_tiles,
+                ntiles, nT, L, Lp, nslots * ntypes, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status, ctx->st));
   ctx->nlaunch += 4;
   ctx->last_nout = ntypes; ctx->last_first = first; ctx->last_nslots = nslots;
   return 0;
@@ -589,8 +595,10 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
       ctx->nbcap = nbcum;
     }
     CK(cudaMemsetAsync(ctx->d_obs, 0, (size_t)nbcum * sizeof(unsigned long long), ctx->st));
+    // the window starts one bin below the smallest null score's bin
+    const int wbase = std::isfinite(xmin) ? std::max(0, (int)std::floor((xmin - p->bmin) / w) - 2) : 0;
     CK(launch_hist(ctx->d_cov + ((int64_t)1 * ntypes + q) * plane, ntypes * plane, ctx->d_tiles, ctx->ntiles, L, ns,
-                   p->bmin, w, nbcum, ctx->d_obs, ctx->d_status, ctx->st));
+                   p->bmin, w, nbcum, wbase, ctx->d_obs, ctx->d_status, ctx->st));
     ctx->nlaunch += 1;
     std::vector<uint64_t> obs(nbcum);
     CK(cudaMemcpyAsync(obs.data(), ctx->d_obs, nbcum * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->st));
@@ -753,8 +761,9 @@ extern "C" int covgpu_correct(covgpu_ctx* ctx, const double* COV, int actype, do
   CK(launch_tile_rowsums(ctx->d_cov, ctx->d_tiles, ctx->ntiles, ctx->nT, ctx->L, ctx->d_part1, ctx->st));
   CorrTypes ct;
   ct.nout = 1; ct.act[0] = actype; ct.act[1] = ct.act[2] = ct.act[3] = -1;
-  CK(launch_apc(ctx->d_cov, ctx->d_part1, ctx->d_colx, ctx->d_avg, ct, ctx->d_tiles, ctx->ntiles, ctx->nT, ctx->L,
-                ctx->Lp, 1, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status, ctx->st));
+  CK(launch_apc(ctx->d_cov, ctx->d_part1, ctx->d_colx, ctx->d_colxf, ctx->d_avg, ctx->d_apcf, ct, ctx->d_tiles,
+                ctx->ntiles, ctx->nT, ctx->L, ctx->Lp, 1, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status,
+                ctx->st));
   ctx->last_nout = 1;
   (void)nout;
   if (minmax) CK(cudaMemcpyAsync(minmax, ctx->d_mm, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
@@ -775,7 +784,8 @@ extern "C" int covgpu_hist_full(covgpu_ctx* ctx, const double* COV, double bmin,
     ctx->nbcap = nb;
   }
   CK(cudaMemsetAsync(ctx->d_obs, 0, (size_t)nb * sizeof(unsigned long long), ctx->st));
-  CK(launch_hist(ctx->d_cov, 0, ctx->d_tiles, ctx->ntiles, ctx->L, 1, bmin, w, nb, ctx->d_obs, ctx->d_status, ctx->st));
+  CK(launch_hist(ctx->d_cov, 0, ctx->d_tiles, ctx->ntiles, ctx->L, 1, bmin, w, nb, 0, ctx->d_obs, ctx->d_status,
+                 ctx->st));
   CK(cudaMemcpyAsync(obs, ctx->d_obs, (size_t)nb * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   return check_status(ctx);
@@ -813,8 +823,8 @@ extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void
   const int64_t plane = (int64_t)ctx->ntiles * TPP;
   double* evt = nullptr;
   if (Eval) {
-    if (!ctx->d_cov2) CK(dalloc(&ctx->d_cov2, (size_t)ctx->maxslots * plane));
-    evt = ctx->d_cov2;
+    if (!ctx->d_evt) CK(dalloc(&ctx->d_evt, (size_t)plane));
+    evt = ctx->d_evt;
   }
   CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
   CK(launch_evalue(ctx->d_cov, ctx->d_tiles, ctx->ntiles, ctx->L, T, evt, ctx->d_nhits, ctx->hitcap, ctx->d_hi,

@@ -13,6 +13,12 @@
 //   k_hist          histogram of pair scores (src/covariation.c:414-457)
 //   k_evalue        per-pair E-values and the hit list (:2369-2400, :778-1006)
 //   k_untile        tile-packed scores -> full L x L matrix for the host
+//
+// Score matrices live on the device as double-float pairs (float2: hi + lo,
+// ~48-bit significand): GB300 issues FP64 at 1/64 of its FP32 rate, so the
+// per-pair passes (APC/ASC, min/max, histogram bins) run on the FP32 pipes;
+// FP64 is kept for the row/column means, a bin next to a bin boundary, and
+// the E-value tables.
 #include "cov_dev.cuh"
 #include "cov_kernels.h"
 
@@ -26,7 +32,7 @@ namespace covgpu {
 // with the reciprocal; only when it lies within 1e-9 of an integer (where
 // the last ulp could move the ceiling) is the IEEE division redone, so the
 // bin always equals the one the division gives.
-__device__ __forceinline__ int exact_bin(double x, double bmin, double w, double invw) {
+__host__ __device__ __forceinline__ int exact_bin(double x, double bmin, double w, double invw) {
   // fp32 estimate first: three roundings put it within 1.8e-7 |q| of the
   // exact quotient, so away from integers it has the same ceiling
   const float qf = (float)(x - bmin) * (float)invw;
@@ -137,6 +143,75 @@ __device__ __forceinline__ df df_of(double x) {
   return {hi, (float)(x - (double)hi)};
 }
 __device__ __forceinline__ double df_to_d(df a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df ld_df(const float2* p) { const float2 v = *p; return {v.x, v.y}; }
+__device__ __forceinline__ void st_df(float2* p, df v) { *p = make_float2(v.hi, v.lo); }
+// order of normalised double-float values (|lo| <= ulp(hi)/2)
+__device__ __forceinline__ bool df_lt(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ df df_min(df a, df b) { return df_lt(b, a) ? b : a; }
+__device__ __forceinline__ df df_max(df a, df b) { return df_lt(a, b) ? b : a; }
+
+// constants of the bin function, split on the host
+struct BinC {
+  float2 nbmin;    // -bmin
+  float2 invw;     // 1/w
+  float2 lo;       // bmin + w (scores are clamped up to it)
+  float  mconst;   // absolute part of the fast-path margin
+  int    bin_lo;   // bin of the clamp value bmin + w, from its FP64 value
+  double bmin, w;
+};
+
+static BinC make_binc(double bmin, double w) {
+  auto split = [](double x) { const float h = (float)x; return make_float2(h, (float)(x - (double)h)); };
+  BinC B;
+  B.nbmin = split(-bmin);
+  B.invw = split(1.0 / w);
+  B.lo = split(bmin + w);
+  B.mconst = (float)(1e-11 * (std::fabs(bmin) / w + 1.0));
+  B.bin_lo = exact_bin(bmin + w, bmin, w, 1.0 / w);
+  B.bmin = bmin; B.w = w;
+  return B;
+}
+
+// Easel's bin of x = hi + lo: ceil((x - bmin)/w - 1).  The quotient is
+// formed in double-float (error < 1e-12 (|q| + |bmin|/w + 1) against the FP64
+// expression); when it lies closer than that to an integer the FP64
+// expression of exact_bin decides, so the bin is the one FP64 gives.
+__device__ __forceinline__ int bin_df(df x, const BinC& B) {
+  const df q = df_mul(df_add(x, {B.nbmin.x, B.nbmin.y}), {B.invw.x, B.invw.y});
+  const float n = rintf(q.hi);
+  const float f = (q.hi - n) + q.lo;
+  if (fabsf(q.hi) < 4194304.f && fabsf(f) > 1e-11f * fabsf(q.hi) + B.mconst) return (f > 0.f) ? (int)n : (int)n - 1;
+  return exact_bin(df_to_d(x), B.bmin, B.w, 1.0 / B.w);
+}
+
+// bin of max(x, bmin + w) (src/covariation.c:431-432); NaN goes to the
+// clamp, whose bin comes from the FP64 value of bmin + w
+__device__ __forceinline__ int bin_clamped(df x, const BinC& B) {
+  return df_lt({B.lo.x, B.lo.y}, x) ? bin_df(x, B) : B.bin_lo;
+}
+
+// block min/max of double-float values (256 threads) -> FP64 per block
+__device__ __forceinline__ void block_minmax_store(df lo, df hi, double* tmin, double* tmax) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const df l2 = {__shfl_xor_sync(0xffffffffu, lo.hi, o), __shfl_xor_sync(0xffffffffu, lo.lo, o)};
+    const df h2 = {__shfl_xor_sync(0xffffffffu, hi.hi, o), __shfl_xor_sync(0xffffffffu, hi.lo, o)};
+    lo = df_min(lo, l2); hi = df_max(hi, h2);
+  }
+  __shared__ float4 sm[8];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = make_float4(lo.hi, lo.lo, hi.hi, hi.lo);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    df l = {sm[0].x, sm[0].y}, h = {sm[0].z, sm[0].w};
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+      l = df_min(l, {sm[w].x, sm[w].y});
+      h = df_max(h, {sm[w].z, sm[w].w});
+    }
+    *tmin = (l.hi == INFINITY) ? DBL_MAX : df_to_d(l);
+    *tmax = (h.hi == -INFINITY) ? -DBL_MAX : df_to_d(h);
+  }
+}
 
 
 // ------------------------------------------------------------------------
@@ -523,11 +598,11 @@ k_stats(StatsArgs A) {
       if (st == 6 || st == 8) {   // FP64 results
         const double v = valid ? pick(o, st) : 0.0;
         rs[k][q] = df_of(v);
-        A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = v;
+        st_df(A.cov + (((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p, rs[k][q]);
       } else {
         const float v = (st >= 0 && valid) ? (float)pick(o, st) : 0.f;
         rs[k][q] = {v, 0.f};
-        if (st >= 0) A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = (double)v;
+        if (st >= 0) A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = make_float2(v, 0.f);
       }
     }
   }
@@ -544,51 +619,56 @@ k_stats(StatsArgs A) {
 }
 
 // RAFS from the RAF scores (both in tile layout); b_{i-1,j+1}, b_{i+1,j-1}
-__device__ __forceinline__ double tile_get(const double* cov, const int* tile_index, int nT, int i, int j) {
+__device__ __forceinline__ df tile_get(const float2* cov, const int* tile_index, int nT, int i, int j) {
   const int I = i / TP, J = j / TP;
   const int t = tile_index[I * nT + J];
-  return cov[(int64_t)t * TPP + (i % TP) * TP + (j % TP)];
+  return ld_df(cov + (int64_t)t * TPP + (i % TP) * TP + (j % TP));
 }
 
 __global__ void __launch_bounds__(256)
-k_rafs(const double* __restrict__ raf, double* __restrict__ out, int64_t slot_stride_in, int64_t slot_stride_out,
+k_rafs(const float2* __restrict__ raf, float2* __restrict__ out, int64_t slot_stride_in, int64_t slot_stride_out,
        const TileRC* __restrict__ tiles, const int* __restrict__ tile_index, int ntiles, int nT, int L,
        double* __restrict__ part1, int64_t part_stride) {
   const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
-  const double* B = raf + slot * slot_stride_in;
+  const float2* B = raf + slot * slot_stride_in;
   df v[4][1];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
-    double r = 0.0;
+    df r = {0.f, 0.f};
     if (i < j && j < L) {
-      r = 2.0 * B[(int64_t)t * TPP + p];
-      if (i > 0 && j < L - 1) r += tile_get(B, tile_index, nT, i - 1, j + 1);
-      if (j > 0 && i < L - 1 && i < j - 2) r += tile_get(B, tile_index, nT, i + 1, j - 1);
-      r *= 0.25;
+      const df c = ld_df(B + (int64_t)t * TPP + p);
+      r = {2.f * c.hi, 2.f * c.lo};
+      if (i > 0 && j < L - 1) r = df_add(r, tile_get(B, tile_index, nT, i - 1, j + 1));
+      if (j > 0 && i < L - 1 && i < j - 2) r = df_add(r, tile_get(B, tile_index, nT, i + 1, j - 1));
+      r = {0.25f * r.hi, 0.25f * r.lo};
     }
-    out[slot * slot_stride_out + (int64_t)t * TPP + p] = r;
-    v[k][0] = df_of(r);
+    st_df(out + slot * slot_stride_out + (int64_t)t * TPP + p, r);
+    v[k][0] = r;
   }
   tile_rowcol_store<1>(v, part1 + slot * part_stride, nT, tr.I, tr.J);
 }
 
 // COVx[c] = sum_{j != c} COV[c][j] / (L-1), from the tile partials
-__global__ void k_apc_colx(const double* __restrict__ part1, int nT, int L, int Lp, double* __restrict__ colx) {
+__global__ void k_apc_colx(const double* __restrict__ part1, int nT, int L, int Lp, double* __restrict__ colx,
+                           float2* __restrict__ colxf) {
   const int sq = blockIdx.y;   // (slot, stat) flattened
   const double* P = part1 + (int64_t)sq * nT * nT * TP;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L; c += gridDim.x * blockDim.x) {
     const int I = c / TP, a = c % TP;
     double s = 0.0;
     for (int K = 0; K < nT; K++) s += P[((int64_t)I * nT + K) * TP + a];
-    colx[(int64_t)sq * Lp + c] = (L > 1) ? s / ((double)L - 1.0) : s;
+    const double x = (L > 1) ? s / ((double)L - 1.0) : s;
+    colx[(int64_t)sq * Lp + c] = x;
+    st_df(colxf + (int64_t)sq * Lp + c, df_of(x));
   }
 }
 
 // avg = 2/(L(L-1)) * sum_{i<j} COV = sum_c COVx[c] / L
-__global__ void k_apc_avg(const double* __restrict__ colx, int L, int Lp, double* __restrict__ avg) {
+__global__ void k_apc_avg(const double* __restrict__ colx, int L, int Lp, double* __restrict__ avg,
+                          float4* __restrict__ apcf) {
   const int sq = blockIdx.x;
   __shared__ double buf[256];
   double s = 0.0;
@@ -599,68 +679,65 @@ __global__ void k_apc_avg(const double* __restrict__ colx, int L, int Lp, double
     if ((int)threadIdx.x < o) buf[threadIdx.x] += buf[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) avg[sq] = (L > 1) ? buf[0] * ((double)L - 1.0) / ((double)L * ((double)L - 1.0)) : 0.0;
+  if (threadIdx.x == 0) {
+    const double A = (L > 1) ? buf[0] * ((double)L - 1.0) / ((double)L * ((double)L - 1.0)) : 0.0;
+    avg[sq] = A;
+    const df a = df_of(A), ia = df_of(A != 0.0 ? 1.0 / A : 0.0);
+    apcf[sq] = make_float4(a.hi, a.lo, ia.hi, ia.lo);
+  }
 }
 
 // COV <- COV - COVx_i COVx_j / avg (APC) or COV - (COVx_i + COVx_j - avg) (ASC);
-// per-tile min/max of the corrected scores.
+// per-tile min/max of the corrected scores.  Double-float arithmetic.
 __global__ void __launch_bounds__(256)
-k_apc_apply(double* __restrict__ cov, const double* __restrict__ colx, const double* __restrict__ avg, CorrTypes ct,
-            const TileRC* __restrict__ tiles, int ntiles, int L, int Lp, double* __restrict__ tmin,
-            double* __restrict__ tmax, int* __restrict__ status) {
+k_apc_apply(float2* __restrict__ cov, const float2* __restrict__ colxf, const double* __restrict__ avg,
+            const float4* __restrict__ apcf, CorrTypes ct, const TileRC* __restrict__ tiles, int ntiles, int L, int Lp,
+            double* __restrict__ tmin, double* __restrict__ tmax, int* __restrict__ status) {
   const int t = blockIdx.x, sq = blockIdx.y, tid = threadIdx.x;
   const int actype = ct.act[sq % ct.nout];
   const TileRC tr = tiles[t];
-  const double A = avg[sq];
-  const double invA = (A != 0.0) ? 1.0 / A : 0.0;
-  const double* X = colx + (int64_t)sq * Lp;
-  double* V = cov + ((int64_t)sq * ntiles + t) * TPP;
-  double lo = DBL_MAX, hi = -DBL_MAX;
+  const bool Anz = (avg[sq] != 0.0);
+  const float4 af = apcf[sq];
+  const df A = {af.x, af.y}, invA = {af.z, af.w};
+  const float2* X = colxf + (int64_t)sq * Lp;
+  float2* V = cov + ((int64_t)sq * ntiles + t) * TPP;
+  df lo = {INFINITY, 0.f}, hi = {-INFINITY, 0.f};
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
     if (i < j && j < L) {
-      double v = V[p], r;
-      if (actype == 0)      r = (A != 0.0) ? v - X[i] * X[j] * invA : 0.0;
-      else if (actype == 1) r = v - (X[i] + X[j] - A);
-      else                  r = v;
-      if (isnan(r)) atomicExch(status, 3);
-      if (actype >= 0) V[p] = r;
-      lo = fmin(lo, r); hi = fmax(hi, r);
+      const df v = ld_df(V + p);
+      df r;
+      if (actype == 0) {
+        r = Anz ? df_add(v, df_neg(df_mul(df_mul(ld_df(X + i), ld_df(X + j)), invA))) : df{0.f, 0.f};
+      } else if (actype == 1) {
+        r = df_add(v, df_neg(df_add(df_add(ld_df(X + i), ld_df(X + j)), df_neg(A))));
+      } else {
+        r = v;
+      }
+      if (isnan(r.hi)) atomicExch(status, 3);
+      if (actype >= 0) st_df(V + p, r);
+      lo = df_min(lo, r); hi = df_max(hi, r);
     }
   }
-  __shared__ double smin[256], smax[256];
-  smin[tid] = lo; smax[tid] = hi;
-  __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (tid < o) { smin[tid] = fmin(smin[tid], smin[tid + o]); smax[tid] = fmax(smax[tid], smax[tid + o]); }
-    __syncthreads();
-  }
-  if (tid == 0) { tmin[(int64_t)sq * ntiles + t] = smin[0]; tmax[(int64_t)sq * ntiles + t] = smax[0]; }
+  block_minmax_store(lo, hi, tmin + (int64_t)sq * ntiles + t, tmax + (int64_t)sq * ntiles + t);
 }
 
 // min/max of the scores of every valid pair (before any correction)
 __global__ void __launch_bounds__(256)
-k_tile_minmax(const double* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L,
+k_tile_minmax(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L,
               double* __restrict__ tmin, double* __restrict__ tmax) {
   const int t = blockIdx.x, sq = blockIdx.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
-  const double* V = cov + ((int64_t)sq * ntiles + t) * TPP;
-  double lo = DBL_MAX, hi = -DBL_MAX;
+  const float2* V = cov + ((int64_t)sq * ntiles + t) * TPP;
+  df lo = {INFINITY, 0.f}, hi = {-INFINITY, 0.f};
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
-    if (i < j && j < L) { lo = fmin(lo, V[p]); hi = fmax(hi, V[p]); }
+    if (i < j && j < L) { const df v = ld_df(V + p); lo = df_min(lo, v); hi = df_max(hi, v); }
   }
-  __shared__ double smin[256], smax[256];
-  smin[tid] = lo; smax[tid] = hi;
-  __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (tid < o) { smin[tid] = fmin(smin[tid], smin[tid + o]); smax[tid] = fmax(smax[tid], smax[tid + o]); }
-    __syncthreads();
-  }
-  if (tid == 0) { tmin[(int64_t)sq * ntiles + t] = smin[0]; tmax[(int64_t)sq * ntiles + t] = smax[0]; }
+  block_minmax_store(lo, hi, tmin + (int64_t)sq * ntiles + t, tmax + (int64_t)sq * ntiles + t);
 }
 
 __global__ void k_reduce_minmax(const double* __restrict__ tmin, const double* __restrict__ tmax, int ntiles,
@@ -685,82 +762,77 @@ __global__ void k_reduce_minmax(const double* __restrict__ tmin, const double* _
 }
 
 // Histogram of max(COV, bmin + w) over the valid pairs of several alignments
-// (src/covariation.c:431-432), bins b = ceil((x - bmin)/w - 1).  Each CTA
-// keeps a private histogram in shared memory over a grid-stride range of
-// (tile, alignment) items and adds it to the global one once.
-__global__ void __launch_bounds__(256)
-k_hist(const double* __restrict__ cov, int64_t slot_stride, const TileRC* __restrict__ tiles, int ntiles, int nslots,
-       int L, double bmin, double w, int nbcap, int b0, int nwin, unsigned long long* __restrict__ obs,
-       int* __restrict__ status) {
-  extern __shared__ unsigned int sh[];
-  const int tid = threadIdx.x;
-  for (int b = tid; b < nwin; b += blockDim.x) sh[b] = 0u;
-  __syncthreads();
-  const double lo = bmin + w, invw = 1.0 / w;
-  const int64_t nitems = (int64_t)ntiles * nslots;
-  for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const int t = (int)(it % ntiles), slot = (int)(it / ntiles);
-    const TileRC tr = tiles[t];
-    const double* V = cov + slot * slot_stride + (int64_t)t * TPP;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const int p = tid + 256 * k, a = p >> 5, b = p & 31;
-      const int i = tr.I * TP + a, j = tr.J * TP + b;
-      int bin = -1;
-      if (i < j && j < L) {
-        double x = V[p];
-        if (!(x > lo)) x = lo;
-        bin = exact_bin(x, bmin, w, invw);
-        if (bin < 0 || bin >= nbcap) { atomicExch(status, 4); bin = -1; }
-        else if (bin < b0 || bin >= b0 + nwin) bin = -1;
-      }
-      // one shared-memory atomic per distinct bin of the warp
-      const unsigned grp = __match_any_sync(0xffffffffu, bin);
-      if (bin >= 0 && (__ffs(grp) - 1) == (int)(threadIdx.x & 31)) atomicAdd(sh + (bin - b0), (unsigned)__popc(grp));
-    }
-  }
-  __syncthreads();
-  for (int b = tid; b < nwin; b += blockDim.x)
-    if (sh[b]) atomicAdd(obs + b0 + b, (unsigned long long)sh[b]);
-}
+// (src/covariation.c:431-432), bins b = ceil((x - bmin)/w - 1).  One pass:
+// each CTA (1024 threads, one per pair of a tile) keeps a private window of
+// up to 48K 32-bit counters in shared memory starting at bin wbase (the bin
+// of the smallest score), counts its (tile, alignment) items there with one
+// atomic per distinct bin of a warp, and sends the sparse bins above the
+// window straight to the global histogram.  Four tiles' loads are issued
+// before any is binned.
+constexpr int HIST_WIN = 48 * 1024;
+constexpr int HIST_UNROLL = 4;
 
-// the same with global atomics, for histograms too large for shared memory
-__global__ void __launch_bounds__(256)
-k_hist_global(const double* __restrict__ cov, int64_t slot_stride, const TileRC* __restrict__ tiles, int ntiles, int L,
-              double bmin, double w, int nbcap, unsigned long long* __restrict__ obs, int* __restrict__ status) {
-  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
-  const TileRC tr = tiles[t];
-  const double* V = cov + slot * slot_stride + (int64_t)t * TPP;
-  const double lo = bmin + w, invw = 1.0 / w;
-  for (int k = 0; k < 4; k++) {
-    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
-    const int i = tr.I * TP + a, j = tr.J * TP + b;
-    if (i < j && j < L) {
-      double x = V[p];
-      if (!(x > lo)) x = lo;
-      const int bin = exact_bin(x, bmin, w, invw);
-      if (bin >= 0 && bin < nbcap) atomicAdd(obs + bin, 1ull);
-      else atomicExch(status, 4);
+__global__ void __launch_bounds__(1024, 1)
+k_hist(const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __restrict__ tiles, int ntiles, int nslots,
+       int L, BinC B, int nbcap, int wbase, int nwin, unsigned long long* __restrict__ obs, int* __restrict__ status) {
+  extern __shared__ unsigned int sh[];
+  const int tid = threadIdx.x, a = tid >> 5, b = tid & 31;
+  for (int k = tid; k < nwin; k += blockDim.x) sh[k] = 0u;
+  __syncthreads();
+  const int64_t nitems = (int64_t)ntiles * nslots, G = gridDim.x;
+  for (int64_t base = blockIdx.x; base < nitems; base += HIST_UNROLL * G) {
+    float2 v[HIST_UNROLL];
+    bool ok[HIST_UNROLL];
+#pragma unroll
+    for (int u = 0; u < HIST_UNROLL; u++) {
+      const int64_t it = base + u * G;
+      ok[u] = false;
+      if (it < nitems) {
+        const int t = (int)(it % ntiles), slot = (int)(it / ntiles);
+        const TileRC tr = tiles[t];
+        const int i = tr.I * TP + a, j = tr.J * TP + b;
+        ok[u] = (i < j && j < L);
+        if (ok[u]) v[u] = cov[slot * slot_stride + (int64_t)t * TPP + tid];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < HIST_UNROLL; u++) {
+      int bin = -1;
+      if (ok[u]) {
+        bin = bin_clamped({v[u].x, v[u].y}, B);
+        if (bin < 0 || bin >= nbcap) { atomicExch(status, 4); bin = -1; }
+      }
+      // one atomic per distinct bin of the warp
+      const unsigned grp = __match_any_sync(0xffffffffu, bin);
+      if (bin >= 0 && (__ffs(grp) - 1) == b) {
+        const int rel = bin - wbase;
+        if (rel >= 0 && rel < nwin) atomicAdd(sh + rel, (unsigned)__popc(grp));
+        else                        atomicAdd(obs + bin, (unsigned long long)__popc(grp));
+      }
     }
   }
+  __syncthreads();
+  for (int k = tid; k < nwin; k += blockDim.x)
+    if (sh[k]) atomicAdd(obs + wbase + k, (unsigned long long)sh[k]);
 }
 
 // E-value of every pair (cov2evalue at src/covariation.c:2369-2400 with
 // Nc = 1, times the number of tests) and the compacted hit list.
 __global__ void __launch_bounds__(256)
-k_evalue(const double* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L, EvalTables T,
+k_evalue(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L, EvalTables T, BinC B,
          double* __restrict__ evt, int* __restrict__ nhits, int hitcap, int* __restrict__ hi, int* __restrict__ hj,
          double* __restrict__ hsc, double* __restrict__ hE, double* __restrict__ hp) {
   const int t = blockIdx.x, tid = threadIdx.x;
   const TileRC tr = tiles[t];
-  const double* V = cov + (int64_t)t * TPP;
+  const float2* V = cov + (int64_t)t * TPP;
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
     double E = INFINITY;
     if (i < j && j < L) {
-      const double x = V[p];
-      const int icov = exact_bin(x, T.bmin, T.w, 1.0 / T.w);
+      const df xv = ld_df(V + p);
+      const double x = df_to_d(xv);
+      const int icov = bin_df(xv, B);
       double pv;
       if (T.sf && icov >= 2 * T.nb - 1)      pv = T.sf[2 * T.nb - 1];
       else if (T.sf && x >= T.phi)           pv = T.sf[icov + 1];
@@ -781,15 +853,18 @@ k_evalue(const double* __restrict__ cov, const TileRC* __restrict__ tiles, int n
 }
 
 // tile-packed -> full symmetric L x L (diagonal = diag)
+__device__ __forceinline__ double to_d(double v) { return v; }
+__device__ __forceinline__ double to_d(float2 v) { return (double)v.x + (double)v.y; }
+
+template <typename T>
 __global__ void __launch_bounds__(256)
-k_untile(const double* __restrict__ tilev, const TileRC* __restrict__ tiles, int L, double diag,
-         double* __restrict__ full) {
+k_untile(const T* __restrict__ tilev, const TileRC* __restrict__ tiles, int L, double diag, double* __restrict__ full) {
   const int t = blockIdx.x, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   __shared__ double s[TP][TP + 1];
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
-    s[a][b] = tilev[(int64_t)t * TPP + p];
+    s[a][b] = to_d(tilev[(int64_t)t * TPP + p]);
   }
   __syncthreads();
   for (int k = 0; k < 4; k++) {
@@ -808,20 +883,20 @@ k_untile(const double* __restrict__ tilev, const TileRC* __restrict__ tiles, int
 
 // full symmetric L x L (host layout) -> tile-packed upper triangle
 __global__ void __launch_bounds__(256)
-k_tile(const double* __restrict__ full, const TileRC* __restrict__ tiles, int L, double* __restrict__ tilev) {
+k_tile(const double* __restrict__ full, const TileRC* __restrict__ tiles, int L, float2* __restrict__ tilev) {
   const int t = blockIdx.x, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
-    tilev[(int64_t)t * TPP + p] = (i < j && j < L) ? full[(int64_t)i * L + j] : 0.0;
+    st_df(tilev + (int64_t)t * TPP + p, df_of((i < j && j < L) ? full[(int64_t)i * L + j] : 0.0));
   }
 }
 
 // per-tile row/column sums of a tile-packed score matrix (for APC/ASC of a
 // matrix handed in by the caller)
 __global__ void __launch_bounds__(256)
-k_tile_rowsums(const double* __restrict__ tilev, const TileRC* __restrict__ tiles, int nT, int L,
+k_tile_rowsums(const float2* __restrict__ tilev, const TileRC* __restrict__ tiles, int nT, int L,
                double* __restrict__ part1) {
   const int t = blockIdx.x, tid = threadIdx.x;
   const TileRC tr = tiles[t];
@@ -830,7 +905,7 @@ k_tile_rowsums(const double* __restrict__ tilev, const TileRC* __restrict__ tile
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
-    v[k][0] = df_of((i < j && j < L) ? tilev[(int64_t)t * TPP + p] : 0.0);
+    v[k][0] = (i < j && j < L) ? ld_df(tilev + (int64_t)t * TPP + p) : df{0.f, 0.f};
   }
   tile_rowcol_store<1>(v, part1, nT, tr.I, tr.J);
 }
@@ -870,79 +945,79 @@ cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_rafs(const double* raf, double* out, int64_t sin, int64_t sout, const TileRC* tiles,
+cudaError_t launch_rafs(const float2* raf, float2* out, int64_t sin, int64_t sout, const TileRC* tiles,
                         const int* tile_index, int ntiles, int nT, int L, int nslots, double* part1, int64_t pstride,
                         cudaStream_t st) {
   k_rafs<<<dim3(ntiles, nslots), 256, 0, st>>>(raf, out, sin, sout, tiles, tile_index, ntiles, nT, L, part1, pstride);
   return cudaGetLastError();
 }
 
-cudaError_t launch_apc(double* cov, const double* part1, double* colx, double* avg, CorrTypes ct, const TileRC* tiles,
-                       int ntiles, int nT, int L, int Lp, int nsq, double* tmin, double* tmax, double* mm,
-                       int* status, cudaStream_t st) {
-  k_apc_colx<<<dim3((L + 255) / 256, nsq), 256, 0, st>>>(part1, nT, L, Lp, colx);
-  k_apc_avg<<<nsq, 256, 0, st>>>(colx, L, Lp, avg);
-  k_apc_apply<<<dim3(ntiles, nsq), 256, 0, st>>>(cov, colx, avg, ct, tiles, ntiles, L, Lp, tmin, tmax, status);
+cudaError_t launch_apc(float2* cov, const double* part1, double* colx, float2* colxf, double* avg, float4* apcf,
+                       CorrTypes ct, const TileRC* tiles, int ntiles, int nT, int L, int Lp, int nsq, double* tmin,
+                       double* tmax, double* mm, int* status, cudaStream_t st) {
+  k_apc_colx<<<dim3((L + 255) / 256, nsq), 256, 0, st>>>(part1, nT, L, Lp, colx, colxf);
+  k_apc_avg<<<nsq, 256, 0, st>>>(colx, L, Lp, avg, apcf);
+  k_apc_apply<<<dim3(ntiles, nsq), 256, 0, st>>>(cov, colxf, avg, apcf, ct, tiles, ntiles, L, Lp, tmin, tmax, status);
   k_reduce_minmax<<<nsq, 256, 0, st>>>(tmin, tmax, ntiles, mm);
   return cudaGetLastError();
 }
 
-cudaError_t launch_minmax(const double* cov, const TileRC* tiles, int ntiles, int L, int nsq, double* tmin,
+cudaError_t launch_minmax(const float2* cov, const TileRC* tiles, int ntiles, int L, int nsq, double* tmin,
                           double* tmax, double* mm, cudaStream_t st) {
   k_tile_minmax<<<dim3(ntiles, nsq), 256, 0, st>>>(cov, tiles, ntiles, L, tmin, tmax);
   k_reduce_minmax<<<nsq, 256, 0, st>>>(tmin, tmax, ntiles, mm);
   return cudaGetLastError();
 }
 
-cudaError_t launch_hist(const double* cov, int64_t slot_stride, const TileRC* tiles, int ntiles, int L, int nslots,
-                        double bmin, double w, int nbcap, unsigned long long* obs, int* status, cudaStream_t st) {
-  // block-private histograms of up to 48K 32-bit counters (192 KB of shared
-  // memory); wider histograms take several windows, beyond 8 windows the
-  // global-atomic kernel
-  const int WIN = 48 * 1024;
-  const int nwin = (nbcap + WIN - 1) / WIN;
-  if (nwin > 8) {
-    k_hist_global<<<dim3(ntiles, nslots), 256, 0, st>>>(cov, slot_stride, tiles, ntiles, L, bmin, w, nbcap, obs, status);
-    return cudaGetLastError();
-  }
+cudaError_t launch_hist(const float2* cov, int64_t slot_stride, const TileRC* tiles, int ntiles, int L, int nslots,
+                        double bmin, double w, int nbcap, int wbase, unsigned long long* obs, int* status,
+                        cudaStream_t st) {
+  const BinC B = make_binc(bmin, w);
+  wbase = std::max(0, std::min(wbase, nbcap - 1));
+  const int nwin = std::min(HIST_WIN, nbcap - wbase);
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, WIN * 4);
+    cudaFuncSetAttribute(k_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, HIST_WIN * 4);
     attr = true;
   }
-  int nsm = 152;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, 0);
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int64_t items = (int64_t)ntiles * nslots;
-  const int grid = (int)std::min<int64_t>(items, (int64_t)nsm);
-  for (int b0 = 0; b0 < nbcap; b0 += WIN) {
-    const int n = std::min(WIN, nbcap - b0);
-    k_hist<<<grid, 256, (size_t)n * 4, st>>>(cov, slot_stride, tiles, ntiles, nslots, L, bmin, w, nbcap, b0, n, obs,
-                                             status);
-  }
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)nsm));
+  k_hist<<<grid, 1024, (size_t)nwin * 4, st>>>(cov, slot_stride, tiles, ntiles, nslots, L, B, nbcap, wbase, nwin, obs,
+                                               status);
   return cudaGetLastError();
 }
 
-cudaError_t launch_evalue(const double* cov, const TileRC* tiles, int ntiles, int L, const EvalTables& T, double* evt,
+cudaError_t launch_evalue(const float2* cov, const TileRC* tiles, int ntiles, int L, const EvalTables& T, double* evt,
                           int* nhits, int hitcap, int* hi, int* hj, double* hsc, double* hE, double* hp,
                           cudaStream_t st) {
-  k_evalue<<<ntiles, 256, 0, st>>>(cov, tiles, ntiles, L, T, evt, nhits, hitcap, hi, hj, hsc, hE, hp);
+  k_evalue<<<ntiles, 256, 0, st>>>(cov, tiles, ntiles, L, T, make_binc(T.bmin, T.w), evt, nhits, hitcap, hi, hj, hsc,
+                                   hE, hp);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tile(const double* full, const TileRC* tiles, int ntiles, int L, double* tilev, cudaStream_t st) {
+cudaError_t launch_tile(const double* full, const TileRC* tiles, int ntiles, int L, float2* tilev, cudaStream_t st) {
   k_tile<<<ntiles, 256, 0, st>>>(full, tiles, L, tilev);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tile_rowsums(const double* tilev, const TileRC* tiles, int ntiles, int nT, int L, double* part1,
+cudaError_t launch_tile_rowsums(const float2* tilev, const TileRC* tiles, int ntiles, int nT, int L, double* part1,
                                 cudaStream_t st) {
   k_tile_rowsums<<<ntiles, 256, 0, st>>>(tilev, tiles, nT, L, part1);
   return cudaGetLastError();
 }
 
+cudaError_t launch_untile(const float2* tilev, const TileRC* tiles, int ntiles, int L, double diag, double* full,
+                          cudaStream_t st) {
+  k_untile<float2><<<ntiles, 256, 0, st>>>(tilev, tiles, L, diag, full);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_untile(const double* tilev, const TileRC* tiles, int ntiles, int L, double diag, double* full,
                           cudaStream_t st) {
-  k_untile<<<ntiles, 256, 0, st>>>(tilev, tiles, L, diag, full);
+  k_untile<double><<<ntiles, 256, 0, st>>>(tilev, tiles, L, diag, full);
   return cudaGetLastError();
 }
 

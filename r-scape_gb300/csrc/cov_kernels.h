@@ -15,7 +15,7 @@ struct StatsArgs {
   const double* pm;         // [slot][Lp][4]
   const float2* pmdf;       // [slot][Lp][4] pm as double-float (hi, lo)
   const double* meanp;      // [slot][4]
-  double*       cov;        // [slot][nout][tile][TPP]
+  float2*       cov;        // [slot][nout][tile][TPP] scores as double-float (hi, lo)
   double*       part1;      // [slot][nout][nT][nT][TP]
   const TileRC* tiles;
   int           ntiles, nT, L, Lp, N;
@@ -45,23 +45,30 @@ cudaError_t launch_pm_final(const double* part4, const double* partR, int L, int
 cudaError_t launch_ps(const uint8_t* ax, int64_t slot_stride, const double* w, int N, int L, int Lp, int nslots,
                       double* ps, cudaStream_t st);
 cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st);
-cudaError_t launch_rafs(const double* raf, double* out, int64_t sin, int64_t sout, const TileRC* tiles,
+cudaError_t launch_rafs(const float2* raf, float2* out, int64_t sin, int64_t sout, const TileRC* tiles,
                         const int* tile_index, int ntiles, int nT, int L, int nslots, double* part1, int64_t pstride,
                         cudaStream_t st);
 // actype per output q (sq = slot * nout + q): 0 = APC, 1 = ASC, -1 = none
 struct CorrTypes { int act[MAXOUT]; int nout; };
-cudaError_t launch_apc(double* cov, const double* part1, double* colx, double* avg, CorrTypes ct, const TileRC* tiles,
-                       int ntiles, int nT, int L, int Lp, int nsq, double* tmin, double* tmax, double* mm,
-                       int* status, cudaStream_t st);
-cudaError_t launch_tile(const double* full, const TileRC* tiles, int ntiles, int L, double* tilev, cudaStream_t st);
-cudaError_t launch_tile_rowsums(const double* tilev, const TileRC* tiles, int ntiles, int nT, int L, double* part1,
+// colx [nsq][Lp] (FP64) with its double-float copy colxf; avg [nsq] (FP64)
+// with apcf [nsq] = (avg, 1/avg) as double-float pairs
+cudaError_t launch_apc(float2* cov, const double* part1, double* colx, float2* colxf, double* avg, float4* apcf,
+                       CorrTypes ct, const TileRC* tiles, int ntiles, int nT, int L, int Lp, int nsq, double* tmin,
+                       double* tmax, double* mm, int* status, cudaStream_t st);
+cudaError_t launch_tile(const double* full, const TileRC* tiles, int ntiles, int L, float2* tilev, cudaStream_t st);
+cudaError_t launch_tile_rowsums(const float2* tilev, const TileRC* tiles, int ntiles, int nT, int L, double* part1,
                                 cudaStream_t st);
-cudaError_t launch_minmax(const double* cov, const TileRC* tiles, int ntiles, int L, int nsq, double* tmin,
+cudaError_t launch_minmax(const float2* cov, const TileRC* tiles, int ntiles, int L, int nsq, double* tmin,
                           double* tmax, double* mm, cudaStream_t st);
-cudaError_t launch_hist(const double* cov, int64_t slot_stride, const TileRC* tiles, int ntiles, int L, int nslots,
-                        double bmin, double w, int nbcap, unsigned long long* obs, int* status, cudaStream_t st);
-cudaError_t launch_evalue(const double* cov, const TileRC* tiles, int ntiles, int L, const EvalTables& T, double* evt,
+// histogram of nslots score planes into obs[nbcap]; wbase = a bin at or below
+// the smallest score's bin (the shared-memory window starts there)
+cudaError_t launch_hist(const float2* cov, int64_t slot_stride, const TileRC* tiles, int ntiles, int L, int nslots,
+                        double bmin, double w, int nbcap, int wbase, unsigned long long* obs, int* status,
+                        cudaStream_t st);
+cudaError_t launch_evalue(const float2* cov, const TileRC* tiles, int ntiles, int L, const EvalTables& T, double* evt,
                           int* nhits, int hitcap, int* hi, int* hj, double* hsc, double* hE, double* hp,
+                          cudaStream_t st);
+cudaError_t launch_untile(const float2* tilev, const TileRC* tiles, int ntiles, int L, double diag, double* full,
                           cudaStream_t st);
 cudaError_t launch_untile(const double* tilev, const TileRC* tiles, int ntiles, int L, double diag, double* full,
                           cudaStream_t st);
