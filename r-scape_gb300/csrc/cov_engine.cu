@@ -367,8 +367,11 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   }
   A.stats = mask;
   A.cls = cls;
-  A.invD = 1.0 / ((N > 1) ? (double)N * ((double)N - 1.0) : 1.0);
-  A.invN = 1.0 / (double)N;
+  {
+    auto split = [](double x) { const float h = (float)x; return make_float2(h, (float)(x - (double)h)); };
+    A.invD = split(1.0 / ((N > 1) ? (double)N * ((double)N - 1.0) : 1.0));
+    A.invN = split(1.0 / (double)N);
+  }
   A.nout = ntypes;
   for (int k = 0; k < 16; k++) A.allow[k] = (float)allow[k];
   if (!need_w) {

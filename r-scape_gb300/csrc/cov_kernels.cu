@@ -407,52 +407,61 @@ __device__ __forceinline__ float gterm_f(float u, float e, float o) {
   return e * gfun_ratio(__fdividef(o, e));
 }
 
-struct PairOut { float chi, gt, mi, mir, mig, omes; double raf, ccf; };
+struct PairOut { float chi, gt, mi, mir, mig, omes; df raf, ccf; };
 
-__device__ __forceinline__ double pick(const PairOut& o, int k) {
+__device__ __forceinline__ df pick_df(const PairOut& o, int k) {
   switch (k) {
-    case 0: return o.chi;
-    case 1: return o.gt;
-    case 2: return o.mi;
-    case 3: return o.mir;
-    case 4: return o.mig;
-    case 5: return o.omes;
+    case 0: return {o.chi, 0.f};
+    case 1: return {o.gt, 0.f};
+    case 2: return {o.mi, 0.f};
+    case 3: return {o.mir, 0.f};
+    case 4: return {o.mig, 0.f};
+    case 5: return {o.omes, 0.f};
     case 6: return o.raf;
     case 8: return o.ccf;
   }
-  return 0.0;
+  return {0.f, 0.f};
 }
 
-__device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[16], const float (&uc)[16], bool have_uc,
-                           const float2* pmi, const float2* pmj, const double* pmid, const double* pmjd,
-                           const double* meanp, df ne, PairOut& out) {
+// per-cell terms a k_stats variant computes (the C16/CWC cell loop is the
+// hot part; a variant carries only what its statistics read)
+enum CellF : unsigned { CF_G = 1u, CF_CHI = 2u, CF_OMES = 4u, CF_H = 8u, CF_ALL = 15u };
+
+// the exact int64 v as double-float (|v| < 2^48)
+__device__ __forceinline__ df df_of_ll(long long v) {
+  const float hi = (float)v;
+  return {hi, (float)(v - (long long)hi)};
+}
+
+template <unsigned CF>
+__device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[16], const float (&uc)[16],
+                                           bool have_uc, const float2* pmi, const float2* pmj, const double* pmid,
+                                           const double* pmjd, const double* meanp, df ne, PairOut& out) {
   const unsigned S = A.stats;
   // ---- RAF from unit-weight counts (src/correlators.c:897-925 reduced):
-  // integer counts, exact in 64-bit integer arithmetic; the two divisions
-  // in the reference's order ----
+  // the sums are exact integers in fp32 (< 2^24), c_ij in 64-bit integers,
+  // the two ratios in double-float ----
   if ((S & (S_RAF | S_RAFS)) && have_uc) {
-    long long nA = 0, r[4] = {0, 0, 0, 0}, cc[4] = {0, 0, 0, 0};
+    float nAf = 0.f, r[4] = {0.f, 0.f, 0.f, 0.f}, cc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int x = 0; x < 4; x++)
 #pragma unroll
       for (int y = 0; y < 4; y++)
         if (A.allow[x * 4 + y] > 0.f) {
-          const long long n = (long long)uc[x * 4 + y];
-          nA += n; r[x] += n; cc[y] += n;
+          const float n = uc[x * 4 + y];
+          nAf += n; r[x] += n; cc[y] += n;
         }
-    const long long sr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
-    const long long sc = cc[0] * cc[0] + cc[1] * cc[1] + cc[2] * cc[2] + cc[3] * cc[3];
-    const long long twice = 2 * nA * nA - sr - sc;     // 2 c_ij, even
-    // cij / (N(N-1)) and (N - nA) / N, each correctly rounded: a reciprocal
-    // product refined by one FMA residual step (Markstein)
-    const double Nd = (double)A.N;
-    const double D = (A.N > 1) ? Nd * (Nd - 1.0) : 1.0;
-    const double cnum = (double)(twice / 2), qnum = (double)((long long)A.N - nA);
-    double q1 = cnum * A.invD;
-    q1 = fma(fma(-q1, D, cnum), A.invD, q1);
-    double q2 = qnum * A.invN;
-    q2 = fma(fma(-q2, Nd, qnum), A.invN, q2);
-    out.raf = 2.0 * q1 - 1.0 * q2;
+    const long long nA = (long long)nAf;
+    long long sr = 0, sc = 0;
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+      const long long a = (long long)r[x], b = (long long)cc[x];
+      sr += a * a; sc += b * b;
+    }
+    const long long cnum = (2 * nA * nA - sr - sc) / 2;   // c_ij
+    const df q1 = df_mul(df_of_ll(cnum), {A.invD.x, A.invD.y});
+    const df q2 = df_mul(df_of_ll((long long)A.N - nA), {A.invN.x, A.invN.y});
+    out.raf = df_add({2.f * q1.hi, 2.f * q1.lo}, df_neg(q2));
   }
   // ---- CCF (src/correlators.c:1038-1053), FP64 ----
   if (S & S_CCF) {
@@ -465,7 +474,7 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
         const double cc = (ned * pmid[x] - meanp[x]) * (ned * pmjd[y] - meanp[y]);
         ccf += cc * cc;
       }
-    out.ccf = sqrt(ccf);
+    out.ccf = df_of(sqrt(ccf));
   }
   const unsigned SP = S & (S_CHI | S_GT | S_MI | S_MIr | S_MIg | S_OMES);
   if (!SP) return;
@@ -507,17 +516,20 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
         if (A.cls == 2 && !(A.allow[x * 4 + y] > 0.f)) continue;
         const float C = c[x * 4 + y];
         const float dc = 1e-10f - 16e-10f * C * inv_ne;
-        const df e = df_mul(ax, {pmj[y].x, pmj[y].y});
-        const float u = diff_oe(C, dc, e);
         const float o = C + dc;
-        if (e.hi > 0.f) {
-          gsum += gterm_f(u, e.hi, o);
-          chi += __fdividef(u * u, e.hi);
-          omes += u * u;
-          usum += u;
+        if (CF & (CF_G | CF_CHI | CF_OMES)) {
+          const df e = df_mul(ax, {pmj[y].x, pmj[y].y});
+          const float u = diff_oe(C, dc, e);
+          if (e.hi > 0.f) {
+            if (CF & CF_G) { gsum += gterm_f(u, e.hi, o); usum += u; }
+            if (CF & CF_CHI) chi += __fdividef(u * u, e.hi);
+            if (CF & CF_OMES) omes += u * u;
+          }
         }
-        const float p = o * inv_ne;
-        hh -= (p > 0.f) ? p * __logf(p) : 0.f;
+        if (CF & CF_H) {
+          const float p = o * inv_ne;
+          hh -= (p > 0.f) ? p * __logf(p) : 0.f;
+        }
       }
     }
     const float gt = (A.cls == 2) ? 2.f * (gsum + usum) : 2.f * gsum;
@@ -564,17 +576,27 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
   }
 }
 
+// One CTA per (tile, alignment), 256 threads, thread tid owns the pairs
+// p = tid + 256k (row a = warp + 8k, column b = lane).  Each pair's scores
+// go straight to the score planes; their row sums are reduced per warp as
+// they are made and their column sums kept as one running double-float per
+// output, so the APC/ASC partials cost no per-pair registers.
+template <unsigned CF>
 __global__ void __launch_bounds__(256)
 k_stats(StatsArgs A) {
-  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const TileRC tr = A.tiles[t];
   const float* C = A.cnt ? A.cnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
   const float* U = A.ucnt ? A.ucnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
   const double* pm = A.pm + (int64_t)slot * A.Lp * 4;
   const float2* pmdf = A.pmdf + (int64_t)slot * A.Lp * 4;
   const double* meanp = A.meanp + slot * 4;
-  df rs[4][MAXOUT];
+  __shared__ df rowbuf[TP][MAXOUT];
+  __shared__ df colbuf[8][TP][MAXOUT];
+  df colacc[MAXOUT];
 #pragma unroll
+  for (int q = 0; q < MAXOUT; q++) colacc[q] = {0.f, 0.f};
+#pragma unroll 1
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
@@ -587,33 +609,37 @@ k_stats(StatsArgs A) {
     for (int q = 0; q < 16; q++) ne = df_add_f(ne, c[q]);
     PairOut o;
     o.chi = o.gt = o.mi = o.mir = o.mig = o.omes = 0.f;
-    o.raf = o.ccf = 0.0;
+    o.raf = o.ccf = df{0.f, 0.f};
     if (valid) {
       const int ii = i < A.L ? i : 0, jj = j < A.L ? j : 0;
-      pair_stats(A, c, uc, U != nullptr, pmdf + ii * 4, pmdf + jj * 4, pm + ii * 4, pm + jj * 4, meanp, ne, o);
+      pair_stats<CF>(A, c, uc, U != nullptr, pmdf + ii * 4, pmdf + jj * 4, pm + ii * 4, pm + jj * 4, meanp, ne, o);
     }
 #pragma unroll
     for (int q = 0; q < MAXOUT; q++) {
-      const int st = (q < A.nout) ? A.outstat[q] : -1;
-      if (st == 6 || st == 8) {   // FP64 results
-        const double v = valid ? pick(o, st) : 0.0;
-        rs[k][q] = df_of(v);
-        st_df(A.cov + (((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p, rs[k][q]);
-      } else {
-        const float v = (st >= 0 && valid) ? (float)pick(o, st) : 0.f;
-        rs[k][q] = {v, 0.f};
-        if (st >= 0) A.cov[(((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p] = make_float2(v, 0.f);
+      if (q < A.nout) {
+        const df v = valid ? pick_df(o, A.outstat[q]) : df{0.f, 0.f};
+        st_df(A.cov + (((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p, v);
+        const df rsum = warp_sum_df(v);
+        if (lane == 0) rowbuf[a][q] = rsum;
+        colacc[q] = df_add(colacc[q], v);
       }
     }
   }
-  // per-statistic row/column sums for APC/ASC
+  // column sums across the 8 warps; rows of tile (I,J) and columns stored
+  // as FP64 partials (a diagonal tile adds both into part[I][I])
 #pragma unroll
-  for (int q = 0; q < MAXOUT; q++) {
-    if (q < A.nout) {
-      df v[4][1];
-#pragma unroll
-      for (int k = 0; k < 4; k++) v[k][0] = rs[k][q];
-      tile_rowcol_store<1>(v, A.part1 + (((int64_t)slot * A.nout + q) * A.nT * A.nT) * TP, A.nT, tr.I, tr.J);
+  for (int q = 0; q < MAXOUT; q++) colbuf[warp][lane][q] = colacc[q];
+  __syncthreads();
+  if (tid < TP * A.nout) {
+    const int col = tid / A.nout, q = tid % A.nout;
+    df cs = {0.f, 0.f};
+    for (int wv = 0; wv < 8; wv++) cs = df_add(cs, colbuf[wv][col][q]);
+    double* part = A.part1 + ((int64_t)slot * A.nout + q) * A.nT * A.nT * TP;
+    if (tr.I == tr.J) {
+      part[((int64_t)tr.I * A.nT + tr.J) * TP + col] = df_to_d(df_add(rowbuf[col][q], cs));
+    } else {
+      part[((int64_t)tr.I * A.nT + tr.J) * TP + col] = df_to_d(rowbuf[col][q]);
+      part[((int64_t)tr.J * A.nT + tr.I) * TP + col] = df_to_d(cs);
     }
   }
 }
@@ -941,7 +967,17 @@ cudaError_t launch_ps(const uint8_t* ax, int64_t slot_stride, const double* w, i
 }
 
 cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st) {
-  k_stats<<<dim3(A.ntiles, nslots), 256, 0, st>>>(A);
+  // the smallest cell-loop variant covering the requested statistics
+  unsigned cf = 0;
+  if (A.stats & (S_GT | S_MI | S_MIr | S_MIg)) cf |= CF_G;
+  if (A.stats & S_CHI) cf |= CF_CHI;
+  if (A.stats & S_OMES) cf |= CF_OMES;
+  if (A.stats & S_MIr) cf |= CF_H;
+  const dim3 grid(A.ntiles, nslots);
+  if (cf == 0 || cf == CF_G)          k_stats<CF_G><<<grid, 256, 0, st>>>(A);
+  else if (cf == CF_CHI)              k_stats<CF_CHI><<<grid, 256, 0, st>>>(A);
+  else if (cf == (CF_G | CF_CHI))     k_stats<CF_G | CF_CHI><<<grid, 256, 0, st>>>(A);
+  else                                k_stats<CF_ALL><<<grid, 256, 0, st>>>(A);
   return cudaGetLastError();
 }
 

@@ -20,7 +20,7 @@ struct StatsArgs {
   const TileRC* tiles;
   int           ntiles, nT, L, Lp, N;
   float2        wtot;       // sum of the weights as double-float (ngap = wtot - nseff)
-  double        invD, invN; // 1/(N(N-1)) and 1/N for RAF
+  float2        invD, invN; // 1/(N(N-1)) and 1/N for RAF, as double-float
   unsigned      stats;      // StatBit mask of what pair_stats must compute
   int           cls;        // 0 = C16, 1 = C2, 2 = CWC (GT)
   int           nout;       // number of output matrices (<= MAXOUT)
