@@ -57,6 +57,7 @@ struct UmmaPlan {
   int N = 0, L = 0, Lp = 0, nT = 0, ntiles = 0, maxslots = 0;
   int Npad = 0;                  // sequences padded to UK
   const TileRC* d_tiles = nullptr;
+  int* d_order = nullptr;           // launch order of the tiles (blocked raster)
   __nv_bfloat16* d_ops = nullptr;   // [(1 + 3) * maxslots * 4Lp][Npad]
   uint8_t* d_limbs = nullptr;       // [3][Npad] weight limbs
   int nl = 3;                       // limbs in use (1 when all weights are equal)
@@ -234,8 +235,8 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
 template <int NL, int STAGES>
 __global__ void __launch_bounds__(128, 1)
 k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
-             const TileRC* __restrict__ tiles, int ntiles, int nslots, int Lp, int nkb, float s_hi, float s_lo,
-             int* __restrict__ err) {
+             const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles, int nslots, int Lp, int nkb,
+             float s_hi, float s_lo, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // 1024-byte aligned ring: stage s = [A | B_0 .. B_{NL-1}], 16 KB each
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -247,7 +248,7 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
   __shared__ int abort_flag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int t = blockIdx.x, slot = blockIdx.y;
+  const int t = order[blockIdx.x], slot = blockIdx.y;
   const TileRC tr = tiles[t];
   const int64_t rows_per_buf = (int64_t)nslots * 4 * Lp;
   const int rowA = (int)((int64_t)slot * 4 * Lp + (int64_t)tr.I * UM);
@@ -424,6 +425,23 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
     return nullptr;
   }
   cudaMemset(p->d_err, 0, sizeof(int));
+  // blocked raster: super-blocks of SB x SB tiles (I <= J) in turn, so the
+  // CTAs resident at one time share a few operand row blocks in L2
+  {
+    std::vector<int> order;
+    order.reserve(ntiles);
+    auto tindex = [nT](int I, int J) { return I * nT - I * (I - 1) / 2 + (J - I); };   // I-major tile list
+    constexpr int SB = 10;
+    for (int bI = 0; bI < nT; bI += SB)
+      for (int bJ = bI; bJ < nT; bJ += SB)
+        for (int I = bI; I < std::min(nT, bI + SB); I++)
+          for (int J = std::max(I, bJ); J < std::min(nT, bJ + SB); J++) order.push_back(tindex(I, J));
+    if ((int)order.size() != ntiles || cudaMalloc(&p->d_order, sizeof(int) * ntiles) != cudaSuccess) {
+      umma_plan_destroy(p);
+      return nullptr;
+    }
+    cudaMemcpy(p->d_order, order.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice);
+  }
   cuuint64_t gdim[2] = {(cuuint64_t)p->Npad, (cuuint64_t)rows};
   cuuint64_t gstride[1] = {(cuuint64_t)p->Npad * sizeof(__nv_bfloat16)};
   cuuint32_t box[2] = {UK, UM};
@@ -440,6 +458,7 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
 void umma_plan_destroy(UmmaPlan* p) {
   if (!p) return;
   if (p->d_ops) cudaFree(p->d_ops);
+  if (p->d_order) cudaFree(p->d_order);
   if (p->d_limbs) cudaFree(p->d_limbs);
   if (p->d_err) cudaFree(p->d_err);
   delete p;
@@ -503,11 +522,11 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
   const float s_hi = (float)scale, s_lo = (float)(scale - (double)s_hi);
   dim3 grid(p->ntiles, nslots);
   if (nl == 1)
-    k_count_umma<1, STAGES1><<<grid, 128, smem_bytes(1), st>>>(p->tmap, omap, p->d_tiles, p->ntiles, p->maxslots,
-                                                               p->Lp, nkb, s_hi, s_lo, p->d_err);
+    k_count_umma<1, STAGES1><<<grid, 128, smem_bytes(1), st>>>(p->tmap, omap, p->d_tiles, p->d_order, p->ntiles,
+                                                               p->maxslots, p->Lp, nkb, s_hi, s_lo, p->d_err);
   else
-    k_count_umma<3, STAGES3><<<grid, 128, smem_bytes(3), st>>>(p->tmap, omap, p->d_tiles, p->ntiles, p->maxslots,
-                                                               p->Lp, nkb, s_hi, s_lo, p->d_err);
+    k_count_umma<3, STAGES3><<<grid, 128, smem_bytes(3), st>>>(p->tmap, omap, p->d_tiles, p->d_order, p->ntiles,
+                                                               p->maxslots, p->Lp, nkb, s_hi, s_lo, p->d_err);
   return cudaGetLastError();
 }
 
