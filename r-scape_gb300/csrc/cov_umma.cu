@@ -10,28 +10,30 @@
 //            quantised to q_s = round(w_s 2^E) < 2^24 and split into 8-bit
 //            limbs q = l0 + 2^8 l1 + 2^16 l2 (integers <= 255, exact in BF16)
 // Each limb accumulates in its own FP32 TMEM accumulator, where the sum
-// (<= 255 N < 2^24 for N <= 65536) is an exact integer; the epilogue forms
-// the 40-bit integer D0 + 2^8 D1 + 2^16 D2 in 64-bit integer arithmetic and
-// rounds it once to FP32 (times the power of two 2^-E), so each count is the
-// correctly rounded value of the exact count of the quantised weights, with
-// no FP64 on the path (exact integers under unit weights, one limb).
+// (<= 255 N < 2^24 for N <= 65536) is an exact integer; the epilogue adds
+// D0 + 2^8 D1 + 2^16 D2 with error-free FP32 sums (two_sum) and one final
+// rounding, so each count is within one FP32 rounding of the exact count of
+// the quantised weights, times the power of two 2^-E, with no FP64 and no
+// integer conversion on the path (exact integers under unit weights).
 //
 // Operand rows are state-major inside each 32-column tile
 // (row = 128 tile + 32 x + column), so accumulator row m = 32 x + a and
 // column n = 32 y + b: warp x, lane a of the epilogue holds cell (x, y) of
 // the pairs (a, b = 0..31), one contiguous 128-byte row of the count tile.
 //
-// Kernel: one CTA per (column tile I <= J, alignment); M = N = 128 (32
-// columns x 4 states each side), K in blocks of 64 sequences.  Warp 0 lane 0
-// issues TMA loads (128B-swizzled boxes) into a 3-4 stage ring guarded by
-// mbarriers, warp 1 lane 0 issues tcgen05.mma (kind::f16, 128x128x16) into
-// TMEM and frees stages with tcgen05.commit; after the last block each warp
-// reads its 32 TMEM lanes (tcgen05.ld 32x32b.x32), combines the limbs, writes
-// the 32x32 block of one cell into a 128B-swizzled shared buffer (conflict
-// free) and stores it with a TMA tensor store, double-buffered.  The counts
-// land in the layout of the SIMT kernel, [slot][tile][cell][32 a][32 b].
-// Every wait is bounded: on timeout the kernel records an error code, drains
-// its copies with a bounded wait and frees TMEM before returning.
+// Kernel: persistent, one CTA per SM working through (column tile I <= J,
+// alignment) tasks in a blocked raster order; M = N = 128 (32 columns x 4
+// states each side), K in blocks of 64 sequences.  Warp 0 lane 0 issues TMA
+// loads (128B-swizzled boxes) into a 3-4 stage ring guarded by mbarriers,
+// warp 1 lane 0 issues tcgen05.mma (kind::f16, 128x128x16) into TMEM and
+// frees stages with tcgen05.commit; four epilogue warps read their 32 TMEM
+// lanes each (tcgen05.ld 32x32b.x32), hand the accumulators back, combine
+// the limbs, write the 32x32 block of one cell into a 128B-swizzled shared
+// buffer (conflict free) and store it with a TMA tensor store,
+// double-buffered, while the next task's MMAs run.  The counts land in the
+// layout of the SIMT kernel, [slot][tile][cell][32 a][32 b].  Every wait is
+// bounded: on timeout the kernel records an error code, drains its copies
+// with a bounded wait and frees TMEM before returning.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -64,6 +66,7 @@ struct UmmaPlan {
   double scale = 1.0;               // count = limb sum * scale
   CUtensorMap tmap;
   int* d_err = nullptr;
+  int nsm = 152;
   bool prepared_unit = false;
 };
 
@@ -148,18 +151,6 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
-}
-
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -230,38 +221,49 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
 }
 
 // ---------------------------------------------------------------------------
-// the counting kernel
+// the counting kernel: persistent, one CTA (6 warps) per SM
+//   warp 0 lane 0   TMA producer over all of the CTA's (tile, alignment)
+//                   tasks: the stage ring and its phases run on across tasks
+//   warp 1 lane 0   MMA issuer: per task, waits until the epilogue has
+//                   drained the accumulator set it will use
+//   warps 2..5      epilogue: warp w reads TMEM lanes 32 (w % 4) (cell row
+//                   x = w % 4), releases the accumulator set after its last
+//                   TMEM load, then combines, stages and stores while the
+//                   next task's MMAs run
 // ---------------------------------------------------------------------------
-template <int NL, int STAGES>
-__global__ void __launch_bounds__(128, 1)
+template <int NL, int STAGES, int ACC>
+__global__ void __launch_bounds__(192, 1)
 k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
-             const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles, int nslots, int Lp, int nkb,
-             float s_hi, float s_lo, int* __restrict__ err) {
+             const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles, int nslots_buf,
+             int nslots, int Lp, int nkb, float s_hi, float s_lo, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  // 1024-byte aligned ring: stage s = [A | B_0 .. B_{NL-1}], 16 KB each
+  constexpr int STAGE_BYTES = TILE_BYTES * (1 + NL);
+  constexpr uint32_t ACC_COLS = NL * UN;   // one accumulator set: NL limbs x 128 columns
+  constexpr uint32_t TMEM_COLS = (ACC * ACC_COLS <= 128) ? 128 : (ACC * ACC_COLS <= 256 ? 256 : 512);
+  static_assert(ACC * ACC_COLS <= 512, "TMEM holds 512 columns");
+  // 1024-byte aligned: the stage ring, then two 4 KB staging buffers per
+  // epilogue warp
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* ring = smem;
+  uint8_t* stagebuf = smem + (size_t)STAGES * STAGE_BYTES;
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
-  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ __align__(8) uint64_t tfull_bar[ACC];    // MMA -> epilogue: accumulator set ready
+  __shared__ __align__(8) uint64_t tempty_bar[ACC];   // epilogue -> MMA: accumulator set drained
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int t = order[blockIdx.x], slot = blockIdx.y;
-  const TileRC tr = tiles[t];
-  const int64_t rows_per_buf = (int64_t)nslots * 4 * Lp;
-  const int rowA = (int)((int64_t)slot * 4 * Lp + (int64_t)tr.I * UM);
-  const int rowB = (int)((int64_t)slot * 4 * Lp + (int64_t)tr.J * UN);
-  constexpr int STAGE_BYTES = TILE_BYTES * (1 + NL);
-  constexpr uint32_t TMEM_COLS = (NL * UN <= 128) ? 128 : (NL * UN <= 256 ? 256 : 512);
+  const int64_t ntask = (int64_t)ntiles * nslots;
+  const int64_t rows_per_buf = (int64_t)nslots_buf * 4 * Lp;
 
   if (tid == 0) {
     for (int s = 0; s < STAGES; s++) { mbar_init(&full_bar[s], 1); mbar_init(&empty_bar[s], 1); }
-    mbar_init(&done_bar, 1);
+    for (int a = 0; a < ACC; a++) { mbar_init(&tfull_bar[a], 1); mbar_init(&tempty_bar[a], 4); }
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(&tmap) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&omap) : "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -273,109 +275,158 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
-  int issued = 0;
+  uint32_t issued = 0;   // k-blocks whose loads the producer issued
 
-  if (warp == 0 && lane == 0) {
-    // ---- TMA producer ----
-    for (int kb = 0; kb < nkb; kb++) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-      if (kb >= STAGES) {
-        if (!mbar_wait(&empty_bar[s], ph ^ 1u)) { atomicExch(err, 101); abort_flag = 1; break; }
-      }
-      if (*(volatile int*)&abort_flag) break;
-      uint8_t* st = ring + (size_t)s * STAGE_BYTES;
-      mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-      tma_load_2d(st, &tmap, kb * UK, rowA, &full_bar[s]);
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer ----
+      uint32_t g = 0;
+      for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x) {
+        const int slot = (int)(task / ntiles), t = order[task % ntiles];
+        const TileRC tr = tiles[t];
+        const int rowA = (int)((int64_t)slot * 4 * Lp + (int64_t)tr.I * UM);
+        const int rowB = (int)((int64_t)slot * 4 * Lp + (int64_t)tr.J * UN);
+        for (int kb = 0; kb < nkb; kb++, g++) {
+          const int s = (int)(g % STAGES);
+          const uint32_t ph = (g / STAGES) & 1u;
+          if (g >= STAGES) {
+            if (!mbar_wait(&empty_bar[s], ph ^ 1u)) { atomicExch(err, 101); abort_flag = 1; }
+          }
+          if (*(volatile int*)&abort_flag) break;
+          uint8_t* st = ring + (size_t)s * STAGE_BYTES;
+          mbar_expect_tx(&full_bar[s], STAGE_BYTES);
+          tma_load_2d(st, &tmap, kb * UK, rowA, &full_bar[s]);
 #pragma unroll
-      for (int l = 0; l < NL; l++)
-        tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * UK, (int)((1 + l) * rows_per_buf) + rowB,
-                    &full_bar[s]);
-      issued = kb + 1;
+          for (int l = 0; l < NL; l++)
+            tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * UK, (int)((1 + l) * rows_per_buf) + rowB,
+                        &full_bar[s]);
+          issued = g + 1;
+        }
+        if (*(volatile int*)&abort_flag) break;
+      }
     }
-  } else if (warp == 1 && lane == 0) {
-    // ---- MMA issuer ----
-    constexpr uint32_t idesc = make_idesc(UM, UN);
-    for (int kb = 0; kb < nkb; kb++) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-      if (!mbar_wait(&full_bar[s], ph)) { atomicExch(err, 102); abort_flag = 1; break; }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      constexpr uint32_t idesc = make_idesc(UM, UN);
+      uint32_t g = 0;
+      int i = 0;
+      for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x, i++) {
+        const int a = i % ACC;
+        const uint32_t aph = (uint32_t)(i / ACC) & 1u;
+        if (i >= ACC && !mbar_wait(&tempty_bar[a], aph ^ 1u)) { atomicExch(err, 105); abort_flag = 1; }
+        if (*(volatile int*)&abort_flag) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dacc = tmem + (uint32_t)a * ACC_COLS;
+        for (int kb = 0; kb < nkb; kb++, g++) {
+          const int s = (int)(g % STAGES);
+          const uint32_t ph = (g / STAGES) & 1u;
+          if (!mbar_wait(&full_bar[s], ph)) { atomicExch(err, 102); abort_flag = 1; }
+          if (*(volatile int*)&abort_flag) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sa = smem_u32(ring + (size_t)s * STAGE_BYTES);
+#pragma unroll
+          for (int k16 = 0; k16 < UK / 16; k16++) {
+            const uint64_t ad = make_desc(sa + k16 * 32);
+#pragma unroll
+            for (int l = 0; l < NL; l++) {
+              const uint64_t bd = make_desc(sa + (uint32_t)(1 + l) * TILE_BYTES + k16 * 32);
+              umma_f16(dacc + (uint32_t)(l * UN), ad, bd, idesc, (kb > 0 || k16 > 0) ? 1u : 0u);
+            }
+          }
+          umma_commit(&empty_bar[s]);
+        }
+        if (*(volatile int*)&abort_flag) break;
+        umma_commit(&tfull_bar[a]);
+      }
+    }
+  } else {
+    // ---- epilogue ----
+    const int x = warp & 3;                         // TMEM lane quarter = cell row x
+    uint8_t* wbuf = stagebuf + (size_t)(warp - 2) * 8192;
+    uint32_t nst = 0;                               // TMA stores issued by this warp
+    int i = 0;
+    for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x, i++) {
+      const int a = i % ACC;
+      const uint32_t aph = (uint32_t)(i / ACC) & 1u;
+      if (!mbar_wait(&tfull_bar[a], aph)) { atomicExch(err, 103); abort_flag = 1; }
+      __syncwarp();
       if (*(volatile int*)&abort_flag) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t sa = smem_u32(ring + (size_t)s * STAGE_BYTES);
-#pragma unroll
-      for (int k16 = 0; k16 < UK / 16; k16++) {
-        const uint64_t ad = make_desc(sa + k16 * 32);
-#pragma unroll
-        for (int l = 0; l < NL; l++) {
-          const uint64_t bd = make_desc(sa + (uint32_t)(1 + l) * TILE_BYTES + k16 * 32);
-          umma_f16(tmem + (uint32_t)(l * UN), ad, bd, idesc, (kb > 0 || k16 > 0) ? 1u : 0u);
-        }
-      }
-      umma_commit(&empty_bar[s]);
-    }
-    umma_commit(&done_bar);
-  }
-  __syncwarp();
-  // ---- epilogue: warp x owns TMEM lanes 32x..32x+31 = cell row x ----
-  bool ok = mbar_wait(&done_bar, 0);
-  if (!ok) { atomicExch(err, 103); abort_flag = 1; }
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (!abort_flag) {
-    // two 4 KB staging buffers per warp in the idle ring (1024-byte aligned)
-    uint8_t* wbuf = smem + (size_t)warp * 8192;
-    const int orow0 = ((slot * ntiles + t) * 16 + warp * 4) * 32;   // cell (x = warp, y = 0), a = 0
+      const int slot = (int)(task / ntiles), t = order[task % ntiles];
+      const int orow0 = ((slot * ntiles + t) * 16 + x * 4) * 32;   // cell (x, y = 0), a = 0
+      const uint32_t taddr = tmem + ((uint32_t)(x * 32) << 16) + (uint32_t)a * ACC_COLS;
 #pragma unroll 1
-    for (int y = 0; y < 4; y++) {
-      uint32_t d[NL][32];
+      for (int y = 0; y < 4; y++) {
+        uint32_t d[NL][32];
 #pragma unroll
-      for (int l = 0; l < NL; l++)
-        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(l * UN + y * 32), d[l]);
-      tmem_ld_wait();
-      float v[32];
-#pragma unroll
-      for (int k = 0; k < 32; k++) {
-        if (NL == 1) {
-          // exact integer times the scale, rounded once (s_lo carries the
-          // part of the scale below FP32 precision)
-          const float c = __uint_as_float(d[0][k]);
-          const float p = c * s_hi;
-          v[k] = p + (fmaf(c, s_hi, -p) + c * s_lo);
-        } else {
-          uint64_t q = (uint64_t)__float2uint_rn(__uint_as_float(d[0][k]));
-          q += (uint64_t)__float2uint_rn(__uint_as_float(d[1][k])) << 8;
-          if (NL > 2) q += (uint64_t)__float2uint_rn(__uint_as_float(d[NL > 2 ? 2 : 0][k])) << 16;
-          v[k] = __ull2float_rn(q) * s_hi;   // s_hi = 2^-E, exact
+        for (int l = 0; l < NL; l++) tmem_ld32(taddr + (uint32_t)(l * UN + y * 32), d[l]);
+        tmem_ld_wait();
+        if (y == 3) {
+          // this warp's last read of the accumulator set: hand it back
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty_bar[a])) : "memory");
         }
-      }
-      uint8_t* buf = wbuf + (y & 1) * 4096;
-      if (y >= 2) {
-        if (lane == 0) bulk_wait_read<1>();   // the store of y - 2 has read this buffer
-        __syncwarp();
-      }
-      // row a = lane, 16-byte chunk c at position c ^ (a & 7) (128B swizzle)
+        float v[32];
 #pragma unroll
-      for (int c = 0; c < 8; c++)
-        *reinterpret_cast<float4*>(buf + lane * 128 + ((c ^ (lane & 7)) << 4)) =
-            make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
-      fence_proxy_async();
-      __syncwarp();
-      if (lane == 0) {
-        tma_store_2d(&omap, buf, 0, orow0 + y * 32);
-        bulk_commit();
+        for (int k = 0; k < 32; k++) {
+          if (NL == 1) {
+            // exact integer times the scale, rounded once (s_lo carries the
+            // part of the scale below FP32 precision)
+            const float c = __uint_as_float(d[0][k]);
+            const float p = c * s_hi;
+            v[k] = p + (fmaf(c, s_hi, -p) + c * s_lo);
+          } else {
+            // D0 + 2^8 D1 + 2^16 D2 with two error-free sums (each limb sum
+            // is an exact integer, the scalings are exact): within one
+            // rounding of the exact count, all on the FP32 pipe
+            const float c0 = __uint_as_float(d[0][k]);
+            const float c1 = __uint_as_float(d[1][k]) * 256.f;
+            const float c2 = (NL > 2) ? __uint_as_float(d[NL > 2 ? 2 : 0][k]) * 65536.f : 0.f;
+            const float s1 = c2 + c1;
+            const float b1 = s1 - c2;
+            const float e1 = (c2 - (s1 - b1)) + (c1 - b1);
+            const float s2 = s1 + c0;
+            const float b2 = s2 - s1;
+            const float e2 = (s1 - (s2 - b2)) + (c0 - b2);
+            v[k] = (s2 + (e1 + e2)) * s_hi;   // s_hi = 2^-E, exact
+          }
+        }
+        uint8_t* buf = wbuf + (nst & 1u) * 4096;
+        if (nst >= 2) {
+          if (lane == 0) bulk_wait_read<1>();   // the store two back has read this buffer
+          __syncwarp();
+        }
+        // row a = lane, 16-byte chunk c at position c ^ (a & 7) (128B swizzle)
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+          *reinterpret_cast<float4*>(buf + lane * 128 + ((c ^ (lane & 7)) << 4)) =
+              make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) {
+          tma_store_2d(&omap, buf, 0, orow0 + y * 32);
+          bulk_commit();
+        }
+        nst++;
       }
     }
     if (lane == 0) bulk_wait_all();
     __syncwarp();
-  } else if (tid == 0) {
-    // drain the copies this CTA issued before freeing its shared memory
-    for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; kb++)
-      mbar_wait(&full_bar[kb % STAGES], (uint32_t)(kb / STAGES) & 1u);
+  }
+  // teardown: after an abort, drain the copies still in flight into the
+  // ring before the shared memory is released
+  if (warp == 0 && lane == 0 && *(volatile int*)&abort_flag) {
+    for (uint32_t g = (issued > (uint32_t)STAGES ? issued - STAGES : 0u); g < issued; g++)
+      mbar_wait(&full_bar[g % STAGES], (g / STAGES) & 1u);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
 }
@@ -398,11 +449,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 constexpr int STAGES3 = 3;   // 3 limbs: 64 KB per stage
 constexpr int STAGES1 = 4;   // 1 limb : 32 KB per stage
 
+constexpr int ACC3 = 1;      // 3 limbs: 384 TMEM columns, one accumulator set
+constexpr int ACC1 = 2;      // 1 limb : two 128-column sets, epilogue overlapped
+
 static size_t smem_bytes(int nl) {
   const int stages = (nl == 1) ? STAGES1 : STAGES3;
   const size_t ring = (size_t)stages * TILE_BYTES * (1 + nl);
-  const size_t stage_out = (size_t)4 * 8192;   // two 4 KB buffers per warp
-  return std::max(ring, stage_out) + 1024;
+  const size_t stage_out = (size_t)4 * 8192;   // two 4 KB buffers per epilogue warp
+  return ring + stage_out + 1024;
 }
 
 UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, int ntiles, int maxslots) {
@@ -450,8 +504,11 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) { umma_plan_destroy(p); return nullptr; }
-  cudaFuncSetAttribute(k_count_umma<3, STAGES3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(3));
-  cudaFuncSetAttribute(k_count_umma<1, STAGES1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes(1));
+  cudaFuncSetAttribute(k_count_umma<3, STAGES3, ACC3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_bytes(3));
+  cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_bytes(1));
+  cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev);
   return p;
 }
 
@@ -520,13 +577,17 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
   // the scale as an unevaluated FP32 pair (a power of two with limbs)
   const double scale = unit ? 1.0 : p->scale;
   const float s_hi = (float)scale, s_lo = (float)(scale - (double)s_hi);
-  dim3 grid(p->ntiles, nslots);
+  // persistent: one CTA per SM, tasks (alignment, tile in raster order)
+  const int64_t ntask = (int64_t)p->ntiles * nslots;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntask, p->nsm));
   if (nl == 1)
-    k_count_umma<1, STAGES1><<<grid, 128, smem_bytes(1), st>>>(p->tmap, omap, p->d_tiles, p->d_order, p->ntiles,
-                                                               p->maxslots, p->Lp, nkb, s_hi, s_lo, p->d_err);
+    k_count_umma<1, STAGES1, ACC1><<<grid, 192, smem_bytes(1), st>>>(p->tmap, omap, p->d_tiles, p->d_order,
+                                                                     p->ntiles, p->maxslots, nslots, p->Lp, nkb, s_hi,
+                                                                     s_lo, p->d_err);
   else
-    k_count_umma<3, STAGES3><<<grid, 128, smem_bytes(3), st>>>(p->tmap, omap, p->d_tiles, p->d_order, p->ntiles,
-                                                               p->maxslots, p->Lp, nkb, s_hi, s_lo, p->d_err);
+    k_count_umma<3, STAGES3, ACC3><<<grid, 192, smem_bytes(3), st>>>(p->tmap, omap, p->d_tiles, p->d_order,
+                                                                     p->ntiles, p->maxslots, nslots, p->Lp, nkb, s_hi,
+                                                                     s_lo, p->d_err);
   return cudaGetLastError();
 }
 

@@ -17,7 +17,7 @@ void        umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t
 // cnt [slot][tile][16][TPP]; unit = unit weights (RAF)
 cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
                        cudaStream_t st);
-// error code recorded by the kernel (0 = none; 101-103 = a barrier wait
+// error code recorded by the kernel (0 = none; 101-105 = a barrier wait
 // timed out); reading it resets it
 int         umma_error(UmmaPlan* p);
 
