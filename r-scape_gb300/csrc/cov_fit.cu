@@ -5,14 +5,13 @@
 // as: location mu = phi (the tail's lower bound, fixed), rate lambda and
 // shape tau maximising sum_b obs_b log(S(lo_b) - S(hi_b)) over the tail bins
 // [cmin, imax], S(x) = Q(tau, lambda (x - mu)); Nelder-Mead (1965) on
-// (log lambda, log tau) from moment estimates.  The whole simplex search is
-// one cooperative launch: every iteration evaluates its reflection,
-// expansion and contraction points together (the same points a sequential
-// Nelder-Mead visits), each block summing a fixed chunk of the non-empty
-// tail bins; after a grid barrier every block adds the block sums in the
-// same fixed order, so all blocks hold bit-identical likelihoods and take
-// the same simplex decisions without a second barrier.  Results do not
-// depend on timing.
+// (log lambda, log tau) from moment estimates.  The whole search (Newton
+// rounds, Nelder-Mead if they do not converge; see k_gam_fit) is one
+// cooperative launch: each round evaluates all its likelihood points
+// together, each block summing a fixed chunk of the non-empty tail bins;
+// after a grid barrier every block adds the block sums in the same fixed
+// order, so all blocks hold bit-identical likelihoods and take the same
+// decisions without a second barrier.  Results do not depend on timing.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -96,6 +95,7 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
 }
 
 constexpr uint64_t kFitWaitNs = 2000000000ull;   // grid barrier gives up after 2 s
+constexpr int kFitMaxPts = 6;                      // likelihood points per evaluation round
 
 struct FitOut { double lambda, tau; int evals, status; };
 
@@ -105,7 +105,7 @@ struct FitGrid {
   double* logx;          // scratch: log(lower bound - mu) per bin
   int nnz;
   double bmin, w, mu;
-  double* part;          // [2][3][gridDim.x] block sums
+  double* part;          // [2][6][gridDim.x] block sums
   unsigned* bar;         // arrival counter, zero at launch
   FitOut* out;
 };
@@ -120,28 +120,30 @@ __device__ bool fit_eval(const FitGrid& g, const FitPoint* pts, int npts, unsign
                          int* flag) {
   const int G = gridDim.x, T = G * blockDim.x, nw = blockDim.x >> 5;
   const int nitems = npts * g.nnz;
-  double* part = g.part + (size_t)(phase & 1u) * 3 * G;
-  double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+  double* part = g.part + (size_t)(phase & 1u) * kFitMaxPts * G;
+  double acc[kFitMaxPts];
+#pragma unroll
+  for (int q = 0; q < kFitMaxPts; q++) acc[q] = 0.0;
   for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitems; it += T) {
     const int q = it / g.nnz, k = it - q * g.nnz;
     const int b = g.bins[k];
     const double lo = g.w * b + g.bmin, hi = g.w * (b + 1) + g.bmin;
     const double v = g.cnts[k] * gam_logp_bin(lo, hi - lo, g.mu, g.logx[k], pts[q]);
-    if (q == 0) acc0 -= v;
-    else if (q == 1) acc1 -= v;
-    else acc2 -= v;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
-    acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
-    acc2 += __shfl_xor_sync(0xffffffffu, acc2, o);
+#pragma unroll
+    for (int r = 0; r < kFitMaxPts; r++)
+      if (q == r) acc[r] -= v;
   }
   const int warp = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) { red[warp * 3] = acc0; red[warp * 3 + 1] = acc1; red[warp * 3 + 2] = acc2; }
+#pragma unroll
+  for (int q = 0; q < kFitMaxPts; q++) {
+    double a = acc[q];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) red[warp * kFitMaxPts + q] = a;
+  }
   __syncthreads();
   if (threadIdx.x < npts) {
     double t = 0.0;
-    for (int i = 0; i < nw; i++) t += red[i * 3 + threadIdx.x];
+    for (int i = 0; i < nw; i++) t += red[i * kFitMaxPts + threadIdx.x];
     part[threadIdx.x * G + blockIdx.x] = t;
   }
   __syncthreads();
@@ -188,10 +190,19 @@ __device__ __forceinline__ void fit_set_points(FitPoint* pts, const double (*pc)
   __syncthreads();
 }
 
+// The search.  Phase 1, Newton on theta = (log lambda, log tau): every round
+// evaluates the 6-point stencil theta, theta +- h e1, theta +- h e2,
+// theta + h (e1 + e2) (h = 1e-5) for the gradient and Hessian by central
+// differences, steps -H^-1 g (a scaled gradient step where H is not
+// positive definite, steps capped at 1 in log space), and halves a step that
+// raised the likelihood's negative; it stops when the step is below 1e-10.
+// Phase 2, only when phase 1 did not converge in 40 rounds: Nelder-Mead from
+// the best point of phase 1, the same points a sequential Nelder-Mead
+// visits, to 1e-12 in F and 1e-9 in theta.
 __global__ void __launch_bounds__(256)
 k_gam_fit(FitGrid g, double s00, double s01) {
-  __shared__ FitPoint pts[3];
-  __shared__ double F[3], red[8 * 3], pc[3][2];
+  __shared__ FitPoint pts[kFitMaxPts];
+  __shared__ double F[kFitMaxPts], red[8 * kFitMaxPts], pc[kFitMaxPts][2];
   __shared__ int flag, ctl;
   {
     const int T = gridDim.x * blockDim.x;
@@ -200,85 +211,147 @@ k_gam_fit(FitGrid g, double s00, double s01) {
       g.logx[k] = (x > 0.0) ? log(x) : 0.0;
     }
   }
-  // the bins' log x are read by other blocks' threads: made visible by the
-  // first grid barrier (fence before arrival), read after it
+  // the bins' log x are read by other blocks' threads: a barrier round with
+  // no points publishes them grid-wide
   unsigned phase = 0;
   int evals = 0, status = 0;
-  double S[3][2], SF[3];   // the simplex, kept by thread 0
-  if (threadIdx.x == 0) {
-    S[0][0] = s00;       S[0][1] = s01;
-    S[1][0] = s00 + 0.5; S[1][1] = s01;
-    S[2][0] = s00;       S[2][1] = s01 + 0.5;
-    for (int k = 0; k < 3; k++) { pc[k][0] = S[k][0]; pc[k][1] = S[k][1]; }
-    // a barrier round with no points publishes log x grid-wide
-  }
   if (!fit_eval(g, pts, 0, phase, F, red, &flag)) status = 2;
-  fit_set_points(pts, pc, 3);
-  if (!status && !fit_eval(g, pts, 3, phase, F, red, &flag)) status = 2;
-  evals += 3;
-  if (threadIdx.x == 0) for (int k = 0; k < 3; k++) SF[k] = F[k];
-  for (int it = 0; it < 4000 && !status; it++) {
-    int lo = 0, hi = 0, md = 0;
+
+  // ---- phase 1: Newton ----
+  constexpr double H = 1e-5;
+  double th0 = s00, th1 = s01;               // thread 0's state
+  double bth0 = s00, bth1 = s01, bF = INFINITY;
+  double d0 = 0.0, d1 = 0.0;                 // last step
+  int converged = 0;
+  for (int r = 0; r < 40 && !status; r++) {
     if (threadIdx.x == 0) {
-      for (int k = 1; k < 3; k++) { if (SF[k] < SF[lo]) lo = k; if (SF[k] > SF[hi]) hi = k; }
-      md = 3 - lo - hi;
-      if (md == lo || md == hi || md < 0 || md > 2)
-        md = (hi == 0) ? ((lo == 1) ? 2 : 1) : ((hi == 1) ? ((lo == 0) ? 2 : 0) : ((lo == 0) ? 1 : 0));
-      if (fabs(SF[hi] - SF[lo]) <= 1e-12 * (fabs(SF[lo]) + 1e-30) && fabs(S[hi][0] - S[lo][0]) < 1e-9 &&
-          fabs(S[hi][1] - S[lo][1]) < 1e-9) {
-        ctl = 0;
+      pc[0][0] = th0;     pc[0][1] = th1;
+      pc[1][0] = th0 + H; pc[1][1] = th1;
+      pc[2][0] = th0 - H; pc[2][1] = th1;
+      pc[3][0] = th0;     pc[3][1] = th1 + H;
+      pc[4][0] = th0;     pc[4][1] = th1 - H;
+      pc[5][0] = th0 + H; pc[5][1] = th1 + H;
+    }
+    fit_set_points(pts, pc, 6);
+    if (!fit_eval(g, pts, 6, phase, F, red, &flag)) { status = 2; break; }
+    evals += 6;
+    if (threadIdx.x == 0) {
+      ctl = 1;
+      const double F0 = F[0];
+      if (!(F0 <= bF) && r > 0) {
+        // the step raised -log L (or gave NaN): back off towards the best point
+        d0 *= 0.5; d1 *= 0.5;
+        th0 = bth0 + d0; th1 = bth1 + d1;
+        if (fabs(d0) < 1e-10 && fabs(d1) < 1e-10) { th0 = bth0; th1 = bth1; converged = 1; ctl = 0; }
       } else {
-        const double c0 = 0.5 * (S[lo][0] + S[md][0]), c1 = 0.5 * (S[lo][1] + S[md][1]);
-        pc[0][0] = c0 + (c0 - S[hi][0]);       pc[0][1] = c1 + (c1 - S[hi][1]);         // reflection
-        pc[1][0] = c0 + 2.0 * (c0 - S[hi][0]); pc[1][1] = c1 + 2.0 * (c1 - S[hi][1]);   // expansion
-        pc[2][0] = c0 + 0.5 * (S[hi][0] - c0); pc[2][1] = c1 + 0.5 * (S[hi][1] - c1);   // contraction
-        ctl = 1;
+        bth0 = th0; bth1 = th1; bF = F0;
+        const double g0 = (F[1] - F[2]) / (2.0 * H), g1 = (F[3] - F[4]) / (2.0 * H);
+        const double h00 = (F[1] - 2.0 * F0 + F[2]) / (H * H), h11 = (F[3] - 2.0 * F0 + F[4]) / (H * H);
+        const double h01 = (F[5] - F[1] - F[3] + F0) / (H * H);
+        const double det = h00 * h11 - h01 * h01;
+        if (h00 > 0.0 && h11 > 0.0 && det > 0.0) {
+          d0 = -(h11 * g0 - h01 * g1) / det;
+          d1 = -(h00 * g1 - h01 * g0) / det;
+        } else {
+          const double sc = fmax(fmax(fabs(h00), fabs(h11)), 1.0);
+          d0 = -g0 / sc; d1 = -g1 / sc;
+        }
+        const double m = fmax(fabs(d0), fabs(d1));
+        if (m > 1.0) { d0 /= m; d1 /= m; }
+        if (m < 1e-10) { converged = 1; ctl = 0; }
+        else { th0 = bth0 + d0; th1 = bth1 + d1; }
       }
     }
     __syncthreads();
     if (!ctl) break;
-    fit_set_points(pts, pc, 3);
-    if (!fit_eval(g, pts, 3, phase, F, red, &flag)) { status = 2; break; }
-    evals += 3;
-    if (threadIdx.x == 0) {
-      const double fr = F[0];
-      ctl = 1;
-      if (fr < SF[lo]) {
-        if (F[1] < fr) { S[hi][0] = pc[1][0]; S[hi][1] = pc[1][1]; SF[hi] = F[1]; }
-        else           { S[hi][0] = pc[0][0]; S[hi][1] = pc[0][1]; SF[hi] = fr; }
-      } else if (fr < SF[md]) {
-        S[hi][0] = pc[0][0]; S[hi][1] = pc[0][1]; SF[hi] = fr;
-      } else if (F[2] < SF[hi]) {
-        S[hi][0] = pc[2][0]; S[hi][1] = pc[2][1]; SF[hi] = F[2];
-      } else {   // shrink towards the best vertex
-        int nq = 0;
-        for (int k = 0; k < 3; k++)
-          if (k != lo) {
-            pc[nq][0] = S[lo][0] + 0.5 * (S[k][0] - S[lo][0]);
-            pc[nq][1] = S[lo][1] + 0.5 * (S[k][1] - S[lo][1]);
-            nq++;
-          }
-        ctl = 2;
-      }
-    }
-    __syncthreads();
-    if (ctl == 2) {
-      fit_set_points(pts, pc, 2);
-      if (!fit_eval(g, pts, 2, phase, F, red, &flag)) { status = 2; break; }
-      evals += 2;
-      if (threadIdx.x == 0) {
-        int nq = 0;
-        for (int k = 0; k < 3; k++)
-          if (k != lo) { S[k][0] = pc[nq][0]; S[k][1] = pc[nq][1]; SF[k] = F[nq]; nq++; }
-      }
-    }
     __syncthreads();
   }
+
+  // ---- phase 2: Nelder-Mead when Newton did not converge ----
+  double S[3][2], SF[3];   // the simplex, kept by thread 0
+  if (threadIdx.x == 0) {
+    flag = converged;
+    const double c0 = isfinite(bF) ? bth0 : s00, c1 = isfinite(bF) ? bth1 : s01;
+    S[0][0] = c0;       S[0][1] = c1;
+    S[1][0] = c0 + 0.5; S[1][1] = c1;
+    S[2][0] = c0;       S[2][1] = c1 + 0.5;
+    for (int k = 0; k < 3; k++) { pc[k][0] = S[k][0]; pc[k][1] = S[k][1]; }
+  }
+  __syncthreads();
+  const bool need_nm = !flag;
+  __syncthreads();
+  if (need_nm && !status) {
+    fit_set_points(pts, pc, 3);
+    if (!fit_eval(g, pts, 3, phase, F, red, &flag)) status = 2;
+    evals += 3;
+    if (threadIdx.x == 0) for (int k = 0; k < 3; k++) SF[k] = F[k];
+    for (int it = 0; it < 4000 && !status; it++) {
+      int lo = 0, hi = 0, md = 0;
+      if (threadIdx.x == 0) {
+        for (int k = 1; k < 3; k++) { if (SF[k] < SF[lo]) lo = k; if (SF[k] > SF[hi]) hi = k; }
+        md = 3 - lo - hi;
+        if (md == lo || md == hi || md < 0 || md > 2)
+          md = (hi == 0) ? ((lo == 1) ? 2 : 1) : ((hi == 1) ? ((lo == 0) ? 2 : 0) : ((lo == 0) ? 1 : 0));
+        if (fabs(SF[hi] - SF[lo]) <= 1e-12 * (fabs(SF[lo]) + 1e-30) && fabs(S[hi][0] - S[lo][0]) < 1e-9 &&
+            fabs(S[hi][1] - S[lo][1]) < 1e-9) {
+          ctl = 0;
+        } else {
+          const double c0 = 0.5 * (S[lo][0] + S[md][0]), c1 = 0.5 * (S[lo][1] + S[md][1]);
+          pc[0][0] = c0 + (c0 - S[hi][0]);       pc[0][1] = c1 + (c1 - S[hi][1]);         // reflection
+          pc[1][0] = c0 + 2.0 * (c0 - S[hi][0]); pc[1][1] = c1 + 2.0 * (c1 - S[hi][1]);   // expansion
+          pc[2][0] = c0 + 0.5 * (S[hi][0] - c0); pc[2][1] = c1 + 0.5 * (S[hi][1] - c1);   // contraction
+          ctl = 1;
+        }
+      }
+      __syncthreads();
+      if (!ctl) break;
+      fit_set_points(pts, pc, 3);
+      if (!fit_eval(g, pts, 3, phase, F, red, &flag)) { status = 2; break; }
+      evals += 3;
+      if (threadIdx.x == 0) {
+        const double fr = F[0];
+        ctl = 1;
+        if (fr < SF[lo]) {
+          if (F[1] < fr) { S[hi][0] = pc[1][0]; S[hi][1] = pc[1][1]; SF[hi] = F[1]; }
+          else           { S[hi][0] = pc[0][0]; S[hi][1] = pc[0][1]; SF[hi] = fr; }
+        } else if (fr < SF[md]) {
+          S[hi][0] = pc[0][0]; S[hi][1] = pc[0][1]; SF[hi] = fr;
+        } else if (F[2] < SF[hi]) {
+          S[hi][0] = pc[2][0]; S[hi][1] = pc[2][1]; SF[hi] = F[2];
+        } else {   // shrink towards the best vertex
+          int nq = 0;
+          for (int k = 0; k < 3; k++)
+            if (k != lo) {
+              pc[nq][0] = S[lo][0] + 0.5 * (S[k][0] - S[lo][0]);
+              pc[nq][1] = S[lo][1] + 0.5 * (S[k][1] - S[lo][1]);
+              nq++;
+            }
+          ctl = 2;
+        }
+      }
+      __syncthreads();
+      if (ctl == 2) {
+        fit_set_points(pts, pc, 2);
+        if (!fit_eval(g, pts, 2, phase, F, red, &flag)) { status = 2; break; }
+        evals += 2;
+        if (threadIdx.x == 0) {
+          int nq = 0;
+          for (int k = 0; k < 3; k++)
+            if (k != lo) { S[k][0] = pc[nq][0]; S[k][1] = pc[nq][1]; SF[k] = F[nq]; nq++; }
+        }
+      }
+      __syncthreads();
+    }
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    int lo = 0;
-    for (int k = 1; k < 3; k++) if (SF[k] < SF[lo]) lo = k;
-    g.out->lambda = exp(S[lo][0]);
-    g.out->tau = exp(S[lo][1]);
+    double l0 = bth0, l1 = bth1;
+    if (need_nm) {
+      int lo = 0;
+      for (int k = 1; k < 3; k++) if (SF[k] < SF[lo]) lo = k;
+      l0 = S[lo][0]; l1 = S[lo][1];
+    }
+    g.out->lambda = exp(l0);
+    g.out->tau = exp(l1);
     g.out->evals = evals;
     g.out->status = status;
   }
@@ -369,7 +442,7 @@ int gamma_fit_gpu(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, doubl
     double inv[64];
     for (int k = 0; k < 64; k++) inv[k] = 1.0 / (k + 1);
     if (cudaMemcpyToSymbol(c_inv, inv, sizeof(inv)) != cudaSuccess) return 90;
-    if (cudaMalloc(&fw.d_part, sizeof(double) * 2 * 3 * fw.max_grid) != cudaSuccess) return 90;
+    if (cudaMalloc(&fw.d_part, sizeof(double) * 2 * kFitMaxPts * fw.max_grid) != cudaSuccess) return 90;
     if (cudaMalloc(&fw.d_bar, sizeof(unsigned)) != cudaSuccess) return 90;
     if (cudaMalloc(&fw.d_out, sizeof(FitOut)) != cudaSuccess) return 90;
     if (cudaMallocHost(&fw.h_out, sizeof(FitOut)) != cudaSuccess) return 90;
@@ -396,7 +469,7 @@ int gamma_fit_gpu(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, doubl
   double s00 = std::log(m / v), s01 = std::log(m * m / v);
   void* args[] = {&g, &s00, &s01};
   // one warp per SM until every SM has one, then up to 8 warps per block
-  const int nitems = 3 * nnz;
+  const int nitems = kFitMaxPts * nnz;
   const int W = std::max(1, std::min(8, (nitems + 32 * fw.max_grid - 1) / (32 * fw.max_grid)));
   const int G = std::max(1, std::min(fw.max_grid, (nitems + 32 * W - 1) / (32 * W)));
   if (cudaLaunchCooperativeKernel((const void*)k_gam_fit, dim3(G), dim3(32 * W), args, 0, st) != cudaSuccess)

@@ -235,7 +235,7 @@ template <int NL, int STAGES, int ACC>
 __global__ void __launch_bounds__(192, 1)
 k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
              const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles, int nslots_buf,
-             int nslots, int Lp, int nkb, float s_hi, float s_lo, int* __restrict__ err) {
+             int nslots, int Lp, int nkb, int bbuf, float s_hi, float s_lo, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   constexpr int STAGE_BYTES = TILE_BYTES * (1 + NL);
   constexpr uint32_t ACC_COLS = NL * UN;   // one accumulator set: NL limbs x 128 columns
@@ -298,7 +298,7 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
           tma_load_2d(st, &tmap, kb * UK, rowA, &full_bar[s]);
 #pragma unroll
           for (int l = 0; l < NL; l++)
-            tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * UK, (int)((1 + l) * rows_per_buf) + rowB,
+            tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * UK, (int)((bbuf + l) * rows_per_buf) + rowB,
                         &full_bar[s]);
           issued = g + 1;
         }
@@ -564,15 +564,20 @@ static bool encode_out_map(UmmaPlan* p, float* cnt, CUtensorMap* m) {
                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
-                       cudaStream_t st) {
+cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, bool a_ready,
+                       float* cnt, cudaStream_t st) {
   if (nslots > p->maxslots) return cudaErrorInvalidValue;
   if (((uintptr_t)cnt & 15u) != 0) return cudaErrorInvalidValue;
   CUtensorMap omap;
   if (!encode_out_map(p, cnt, &omap)) return cudaErrorInvalidValue;
   const int nl = unit ? 1 : p->nl;
   dim3 pg(p->Npad / 64, p->Lp / 32, nslots);
-  k_umma_prep<<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, nl, p->d_limbs, unit, p->d_ops);
+  // unit weights: B is the one-hot of A itself (buffer 0), so only A needs
+  // preparing, and not even that when the weighted pass just wrote it
+  if (!(unit && a_ready))
+    k_umma_prep<<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, unit ? 0 : nl, p->d_limbs,
+                                    unit, p->d_ops);
+  const int bbuf = unit ? 0 : 1;
   const int nkb = p->Npad / UK;
   // the scale as an unevaluated FP32 pair (a power of two with limbs)
   const double scale = unit ? 1.0 : p->scale;
@@ -582,12 +587,12 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntask, p->nsm));
   if (nl == 1)
     k_count_umma<1, STAGES1, ACC1><<<grid, 192, smem_bytes(1), st>>>(p->tmap, omap, p->d_tiles, p->d_order,
-                                                                     p->ntiles, p->maxslots, nslots, p->Lp, nkb, s_hi,
-                                                                     s_lo, p->d_err);
+                                                                     p->ntiles, p->maxslots, nslots, p->Lp, nkb, bbuf,
+                                                                     s_hi, s_lo, p->d_err);
   else
     k_count_umma<3, STAGES3, ACC3><<<grid, 192, smem_bytes(3), st>>>(p->tmap, omap, p->d_tiles, p->d_order,
-                                                                     p->ntiles, p->maxslots, nslots, p->Lp, nkb, s_hi,
-                                                                     s_lo, p->d_err);
+                                                                     p->ntiles, p->maxslots, nslots, p->Lp, nkb, bbuf,
+                                                                     s_hi, s_lo, p->d_err);
   return cudaGetLastError();
 }
 
