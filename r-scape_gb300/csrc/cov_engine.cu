@@ -262,7 +262,7 @@ static int make_nulls_async(covgpu_ctx* ctx, uint64_t seed, int first_null, int 
   CK(launch_nullgen(ctx->d_ax, ctx->N, ctx->L, ctx->Lp, T, ctx->d_lnodes, ctx->loff.data(),
                     (int)ctx->loff.size() - 1, seed, (uint32_t)first_null, nnull, ctx->d_fitch, ctx->d_scratch,
                     ctx->d_ax + first_slot * sstride, sstride, ctx->st));
-  ctx->nlaunch += 2 + (int)ctx->loff.size() - 1;
+  ctx->nlaunch += 2 + 2 * ((int)ctx->loff.size() - 1);
   return 0;
 }
 

@@ -1,28 +1,34 @@
 // cov_null.cu -- null alignments on the GPU: Fitch ancestral states and the
 // shuffled-substitution replay of R-scape's default null (--nullphylo).
 //
-//   k_fitch      one thread per (column, null): Tree_FitchAlgorithmAncenstral
-//                / tree_fitch_column (src/msatree.c:173-227, 1700-1838); up
-//                pass = intersection over the five states, else the union of
-//                residues only (tree_fitch_upwards :1877-1908); down pass
-//                keeps the parent's state when the child's set holds it.
-//   k_colperm    msamanip_ShuffleColumns (src/msamanip.c:1164-1233) on the
-//                internal-node rows of the reconstruction.
-//   k_branch     one CTA per (branch, null), tree levels in order:
+// The work goes by tree depth (nodes of one depth are independent):
+//   k_fitch_up   deepest depth first, one thread per (internal node, 16
+//                columns, null): the up pass of Tree_FitchAlgorithmAncenstral
+//                / tree_fitch_column (src/msatree.c:173-227, 1700-1838):
+//                intersection of the children's sets over the five states,
+//                else the union of residues only (tree_fitch_upwards
+//                :1877-1908), as byte-SIMD on 16-column vectors.
+//   k_root       the root's state per column, then its row with the columns
+//                shuffled (msamanip_ShuffleColumns, src/msamanip.c:1164-1233).
+//                Only the root's shuffled row is ever read: every other row
+//                is replaced by its parent's row before use.
+//   k_replay     top depth first, one warp per (branch, null):
 //                shuffle_tree_substitutions + shuffle_tree_substitute_all
-//                (src/msamanip.c:1597-1747).  The child takes a copy of its
-//                shuffled parent; the branch's substitution counts (measured
-//                on the unshuffled reconstruction) are replayed on positions
-//                of the shuffled parent holding the old state, visited in a
-//                random order (a Feistel permutation; a block-wide scan gives
-//                each position its rank within its state class).
+//                (src/msamanip.c:1597-1747).  The warp finishes the child's
+//                Fitch state (down pass: keep the parent's state when the
+//                child's set holds it), counts the branch's substitutions on
+//                the unshuffled reconstruction, copies the parent's current
+//                row and replays the substitutions on positions of that row
+//                holding the old state, visited in a random order (a Feistel
+//                permutation); each class's positions are ranked with warp
+//                ballots and the pass stops once every substitution is placed.
 //
 // Random draws are counter-based (Philox keyed by the seed, the null index,
 // the node and the column), so the result does not depend on scheduling.
 //
-// Buffers (per null q): fitch[q][v][Lp] and S[q][v][Lp] for internal nodes v,
-// shint[q][v][Lp] their shuffled rows; leaf rows go straight to the output
-// alignment slot.
+// Buffers (per null q): F[q][v][Lp] the Fitch states of internal node v;
+// SR[q][v][Lp] first its Fitch set, then (once the set is used) its row of
+// the null alignment; leaf rows go straight to the output alignment slot.
 #include "cov_dev.cuh"
 #include "cov_kernels.h"
 
@@ -37,162 +43,188 @@ __device__ __forceinline__ int choose_member(unsigned S, uint64_t seed, uint32_t
   return 4;
 }
 
-__device__ __forceinline__ unsigned leaf_set(const uint8_t* ax, int Lp, int n, int c, uint64_t seed, uint32_t nid) {
-  const int x = ax[(int64_t)n * Lp + c];
+
+// set of a leaf residue: one state, a random one for ambiguity codes
+__device__ __forceinline__ uint32_t leaf_byte(uint32_t x, int n, int c, uint64_t seed, uint32_t nid) {
   if (x <= 4) return 1u << x;
   return 1u << (int)(((uint64_t)rng_u32(seed, TAG_FLEAF, nid, (uint32_t)n, (uint32_t)c) * 5u) >> 32);
 }
 
-__global__ void __launch_bounds__(128)
-k_fitch(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
-        const int* __restrict__ right, uint64_t seed, uint32_t first_null, uint8_t* __restrict__ fitch,
-        uint8_t* __restrict__ Sbuf) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  const int q = blockIdx.y;
+// the sets of 16 consecutive columns of child ch (internal row or leaf)
+__device__ __forceinline__ uint4 child_sets(int ch, const uint8_t* ax, const uint8_t* S, int Lp, int c0, uint64_t seed,
+                                           uint32_t nid) {
+  if (ch > 0) return *reinterpret_cast<const uint4*>(S + (int64_t)ch * Lp + c0);
+  const uint4 a = *reinterpret_cast<const uint4*>(ax + (int64_t)(-ch) * Lp + c0);
+  uint32_t w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int b = 0; b < 4; b++) o |= leaf_byte((w[k] >> (8 * b)) & 0xFFu, -ch, c0 + 4 * k + b, seed, nid) << (8 * b);
+    w[k] = o;
+  }
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// per byte: I = a & b if nonzero, else (a | b) without the gap bit
+__device__ __forceinline__ uint32_t fitch_word(uint32_t a, uint32_t b) {
+  const uint32_t I = a & b, U = (a | b) & 0x0F0F0F0Fu;
+  const uint32_t z = __vcmpeq4(I, 0u);   // 0xFF in the bytes where I == 0
+  return (I & ~z) | (U & z);
+}
+
+// up pass for the internal nodes of one depth
+__global__ void __launch_bounds__(256)
+k_fitch_up(const uint8_t* __restrict__ ax, int N, int Lp, const int* __restrict__ left, const int* __restrict__ right,
+           const int* __restrict__ nodes, int nn, uint64_t seed, uint32_t first_null, uint8_t* __restrict__ SR) {
+  const int chunks = Lp >> 4;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nn * chunks) return;
+  const int q = blockIdx.y, v = nodes[idx / chunks], c0 = (idx % chunks) << 4;
+  const uint32_t nid = first_null + q;
+  uint8_t* S = SR + (int64_t)q * (N - 1) * Lp;
+  const uint4 a = child_sets(left[v], ax, S, Lp, c0, seed, nid);
+  const uint4 b = child_sets(right[v], ax, S, Lp, c0, seed, nid);
+  *reinterpret_cast<uint4*>(S + (int64_t)v * Lp + c0) =
+      make_uint4(fitch_word(a.x, b.x), fitch_word(a.y, b.y), fitch_word(a.z, b.z), fitch_word(a.w, b.w));
+}
+
+// the root's states F[q][0][c] from its sets
+__global__ void __launch_bounds__(256)
+k_root_state(int N, int L, int Lp, uint64_t seed, uint32_t first_null, const uint8_t* __restrict__ SR,
+             uint8_t* __restrict__ F) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
   if (c >= L) return;
+  const int64_t off = (int64_t)q * (N - 1) * Lp;
+  F[off + c] = (uint8_t)choose_member(SR[off + c], seed, first_null + q, 0u, (uint32_t)c);
+}
+
+// the root's row of the null: its states with the columns shuffled
+__global__ void __launch_bounds__(256)
+k_root_row(int N, int L, int Lp, uint64_t seed, uint32_t first_null, const uint8_t* __restrict__ F,
+           uint8_t* __restrict__ SR) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
+  if (c >= Lp) return;
+  uint32_t rk[6];
+  round_keys(seed, TAG_COLPERM, first_null + q, 0, rk);
+  const int64_t off = (int64_t)q * (N - 1) * Lp;
+  SR[off + c] = (c < L) ? F[off + feistel_perm((uint32_t)c, feistel_hbits((uint32_t)L), (uint32_t)L, rk)] : (uint8_t)4;
+}
+
+// one warp per (branch, null) for the internal nodes v of one depth
+__global__ void __launch_bounds__(256)
+k_replay(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
+         const int* __restrict__ right, const int* __restrict__ nodes, int nn, uint64_t seed, uint32_t first_null,
+         uint8_t* __restrict__ F, uint8_t* __restrict__ SR, uint8_t* __restrict__ out_ax, int64_t out_slot_stride) {
+  __shared__ int nsub_s[8][25];
+  __shared__ int cum_s[8][5][6];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * 8 + warp;
+  if (item >= 2 * nn) return;
+  const int q = blockIdx.y;
+  const int v = nodes[item >> 1];
+  const int ch = (item & 1) ? right[v] : left[v];
+  const int cidx = (ch <= 0) ? -ch : N + ch;
   const uint32_t nid = first_null + q;
   const int64_t qoff = (int64_t)q * (N - 1) * Lp;
-  uint8_t* S = Sbuf + qoff;
-  uint8_t* F = fitch + qoff;
-  for (int v = N - 2; v >= 0; v--) {
-    const int l = left[v], r = right[v];
-    const unsigned Sl = (l <= 0) ? leaf_set(ax, Lp, -l, c, seed, nid) : S[(int64_t)l * Lp + c];
-    const unsigned Sr = (r <= 0) ? leaf_set(ax, Lp, -r, c, seed, nid) : S[(int64_t)r * Lp + c];
-    const unsigned I = Sl & Sr;
-    S[(int64_t)v * Lp + c] = (uint8_t)(I ? I : ((Sl | Sr) & 0xFu));
-  }
-  F[c] = (uint8_t)choose_member(S[c], seed, nid, 0, (uint32_t)c);
-  for (int v = 0; v < N - 1; v++) {
-    const int a = F[(int64_t)v * Lp + c];
-    const int ch[2] = {left[v], right[v]};
+  const uint8_t* Fp = F + qoff + (int64_t)v * Lp;
+  const uint8_t* Rp = SR + qoff + (int64_t)v * Lp;          // parent's current row
+  uint8_t* Fc = F + qoff + (int64_t)(ch > 0 ? ch : 0) * Lp;  // written for an internal child only
+  const uint8_t* Sc = SR + qoff + (int64_t)(ch > 0 ? ch : 0) * Lp;
+  const uint8_t* Lc = ax + (int64_t)(ch <= 0 ? -ch : 0) * Lp;
+  uint8_t* Cc = (ch <= 0) ? out_ax + (int64_t)q * out_slot_stride + (int64_t)(-ch) * Lp
+                          : SR + qoff + (int64_t)ch * Lp;
+  int* nsub = nsub_s[warp];
+  if (lane < 25) nsub[lane] = 0;
+  __syncwarp();
+
+  // child's states (down pass for an internal child) and the substitution
+  // counts parent -> child, 16 columns per lane and step
+  for (int c0 = lane * 16; c0 < Lp; c0 += 32 * 16) {
+    const uint4 pv = *reinterpret_cast<const uint4*>(Fp + c0);
+    uint4 cv;
+    if (ch > 0) {
+      const uint4 sv = *reinterpret_cast<const uint4*>(Sc + c0);
+      uint32_t pw[4] = {pv.x, pv.y, pv.z, pv.w}, sw[4] = {sv.x, sv.y, sv.z, sv.w}, ow[4];
 #pragma unroll
-    for (int k = 0; k < 2; k++) {
-      if (ch[k] > 0) {
-        unsigned Sc = S[(int64_t)ch[k] * Lp + c];
-        if (Sc & (1u << a)) Sc = 1u << a;
-        F[(int64_t)ch[k] * Lp + c] = (uint8_t)choose_member(Sc, seed, nid, (uint32_t)ch[k], (uint32_t)c);
+      for (int k = 0; k < 4; k++) {
+        uint32_t o = 0;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          const int c = c0 + 4 * k + b;
+          uint32_t st = 4;
+          if (c < L) {
+            const uint32_t a = (pw[k] >> (8 * b)) & 0xFFu;
+            unsigned set = (sw[k] >> (8 * b)) & 0xFFu;
+            if (set & (1u << a)) set = 1u << a;
+            st = (uint32_t)choose_member(set, seed, nid, (uint32_t)ch, (uint32_t)c);
+          }
+          o |= st << (8 * b);
+        }
+        ow[k] = o;
+      }
+      cv = make_uint4(ow[0], ow[1], ow[2], ow[3]);
+      *reinterpret_cast<uint4*>(Fc + c0) = cv;
+    } else {
+      cv = *reinterpret_cast<const uint4*>(Lc + c0);
+    }
+    const uint32_t pw[4] = {pv.x, pv.y, pv.z, pv.w}, cw[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (pw[k] == cw[k]) continue;
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        const int c = c0 + 4 * k + b;
+        const uint32_t a = (pw[k] >> (8 * b)) & 0xFFu, d = (cw[k] >> (8 * b)) & 0xFFu;
+        if (c < L && a != d && a <= 4 && d <= 4) atomicAdd(&nsub[a * 5 + d], 1);
       }
     }
   }
-}
-
-// internal rows: shint[q][v][c] = fitch[q][v][perm_q(c)], padding = gap
-__global__ void __launch_bounds__(256)
-k_colperm(const uint8_t* __restrict__ fitch, int N, int L, int Lp, uint64_t seed, uint32_t first_null,
-          uint8_t* __restrict__ shint) {
-  const int q = blockIdx.z;
-  const int v = blockIdx.y;
-  const uint32_t nid = first_null + q;
-  uint32_t rk[6];
-  round_keys(seed, TAG_COLPERM, nid, 0, rk);
-  const uint32_t hb = feistel_hbits((uint32_t)L);
-  const int64_t row = ((int64_t)q * (N - 1) + v) * Lp;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < Lp; c += gridDim.x * blockDim.x) {
-    uint8_t x = 4;
-    if (c < L) x = fitch[row + feistel_perm((uint32_t)c, hb, (uint32_t)L, rk)];
-    shint[row + c] = x;
+  // the child's row starts as a copy of the parent's row
+  for (int c0 = lane * 16; c0 < Lp; c0 += 32 * 16)
+    *reinterpret_cast<uint4*>(Cc + c0) = *reinterpret_cast<const uint4*>(Rp + c0);
+  __syncwarp();
+  int (*cum)[6] = cum_s[warp];
+  if (lane < 5) {
+    cum[lane][0] = 0;
+    for (int d = 0; d < 5; d++) cum[lane][d + 1] = cum[lane][d] + nsub[lane * 5 + d];
   }
-}
+  __syncwarp();
+  int need[5], run[5] = {0, 0, 0, 0, 0}, total = 0;
+#pragma unroll
+  for (int o = 0; o < 5; o++) { need[o] = cum[o][5]; total += need[o]; }
+  if (total == 0) return;
 
-// one CTA per (branch, null) for the internal nodes of one tree level
-__global__ void __launch_bounds__(1024)
-k_branch(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
-         const int* __restrict__ right, const int* __restrict__ nodes, uint64_t seed, uint32_t first_null,
-         const uint8_t* __restrict__ fitch, uint8_t* __restrict__ shint, uint8_t* __restrict__ out_ax,
-         int64_t out_slot_stride) {
-  extern __shared__ uint8_t psh[];         // shuffled parent row, L bytes
-  __shared__ int nsub[25];
-  __shared__ int cum[5][6];
-  __shared__ int wtot[32][5];
-  const int q = blockIdx.y;
-  const int v = nodes[blockIdx.x >> 1];
-  const int side = blockIdx.x & 1;
-  const int ch = side ? right[v] : left[v];
-  const int cidx = (ch <= 0) ? -ch : N + ch;
-  const uint32_t nid = first_null + q;
-  const int tid = threadIdx.x, nth = blockDim.x;
-  const int64_t qoff = (int64_t)q * (N - 1) * Lp;
-  const uint8_t* Fp = fitch + qoff + (int64_t)v * Lp;
-  const uint8_t* Fc = (ch <= 0) ? ax + (int64_t)(-ch) * Lp : fitch + qoff + (int64_t)ch * Lp;
-  const uint8_t* Pp = shint + qoff + (int64_t)v * Lp;
-  uint8_t* Cc = (ch <= 0) ? out_ax + (int64_t)q * out_slot_stride + (int64_t)(-ch) * Lp
-                          : shint + qoff + (int64_t)ch * Lp;
-
-  if (tid < 25) nsub[tid] = 0;
-  __syncthreads();
-  for (int c = tid; c < Lp; c += nth) {
-    const uint8_t p = Pp[c];
-    if (c < L) {
-      psh[c] = p;
-      const int a = Fp[c], b = Fc[c];
-      if (a != b && a <= 4 && b <= 4) atomicAdd(&nsub[a * 5 + b], 1);
-    }
-    Cc[c] = (c < L) ? p : (uint8_t)4;
-  }
-  __syncthreads();
-  if (tid < 5) {
-    cum[tid][0] = 0;
-    for (int d = 0; d < 5; d++) cum[tid][d + 1] = cum[tid][d] + nsub[tid * 5 + d];
-  }
+  // slot t -> position perm(t) of the parent's row; the r-th slot holding
+  // state o (in slot order) takes substitution r of class o while r < need[o]
   uint32_t rk[6];
   round_keys(seed, TAG_SUBST, nid, (uint32_t)cidx, rk);
   const uint32_t hb = feistel_hbits((uint32_t)L);
-  __syncthreads();
-  const int total = cum[0][5] + cum[1][5] + cum[2][5] + cum[3][5] + cum[4][5];
-  if (total == 0) return;
-
-  // slot t -> position perm(t); each thread takes a contiguous run of slots
-  const int per = (L + nth - 1) / nth;
-  const int t0 = tid * per, t1 = min(L, t0 + per);
-  int cnt[5] = {0, 0, 0, 0, 0};
-  for (int t = t0; t < t1; t++) {
-    const int o = psh[feistel_perm((uint32_t)t, hb, (uint32_t)L, rk)];
-    if (o <= 4) cnt[o]++;
-  }
-  // exclusive block scan of the five class counters
-  const int lane = tid & 31, warp = tid >> 5;
-  int inc[5];
-#pragma unroll
-  for (int k = 0; k < 5; k++) {
-    int x = cnt[k];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int t0 = 0; t0 < L; t0 += 32) {
+    const int t = t0 + lane;
+    uint32_t p = 0;
+    int o = 5;
+    if (t < L) {
+      p = feistel_perm((uint32_t)t, hb, (uint32_t)L, rk);
+      o = Rp[p];
     }
-    inc[k] = x;
-  }
-  if (lane == 31)
+    bool done = true;
 #pragma unroll
-    for (int k = 0; k < 5; k++) wtot[warp][k] = inc[k];
-  __syncthreads();
-  if (warp == 0) {
-    const int nw = nth >> 5;
-#pragma unroll
-    for (int k = 0; k < 5; k++) {
-      int x = (lane < nw) ? wtot[lane][k] : 0;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
+    for (int oc = 0; oc < 5; oc++) {
+      const unsigned m = __ballot_sync(0xffffffffu, o == oc);
+      if (o == oc) {
+        const int r = run[oc] + __popc(m & lt);
+        if (r < need[oc]) {
+          int d = 0;
+          while (r >= cum[oc][d + 1]) d++;
+          Cc[p] = (uint8_t)d;
+        }
       }
-      if (lane < nw) wtot[lane][k] = x;     // inclusive over warps
+      run[oc] += __popc(m);
+      done = done && (run[oc] >= need[oc]);
     }
-  }
-  __syncthreads();
-  int rank[5];
-#pragma unroll
-  for (int k = 0; k < 5; k++) rank[k] = inc[k] - cnt[k] + ((warp > 0) ? wtot[warp - 1][k] : 0);
-  for (int t = t0; t < t1; t++) {
-    const uint32_t p = feistel_perm((uint32_t)t, hb, (uint32_t)L, rk);
-    const int o = psh[p];
-    if (o > 4) continue;
-    const int r = rank[o]++;
-    if (r < cum[o][5]) {
-      int d = 0;
-      while (r >= cum[o][d + 1]) d++;
-      Cc[p] = (uint8_t)d;
-    }
+    if (done) break;
   }
 }
 
@@ -200,15 +232,23 @@ cudaError_t launch_nullgen(const uint8_t* ax, int N, int L, int Lp, const NullTr
                            const int* level_off, int nlevels, uint64_t seed, uint32_t first_null, int nnull,
                            uint8_t* fitch, uint8_t* scratch, uint8_t* out_ax, int64_t out_slot_stride,
                            cudaStream_t st) {
-  // scratch holds the Fitch sets first, then the shuffled internal rows
-  k_fitch<<<dim3((L + 127) / 128, nnull), 128, 0, st>>>(ax, N, L, Lp, T.left, T.right, seed, first_null, fitch,
-                                                        scratch);
-  k_colperm<<<dim3((Lp + 255) / 256, N - 1, nnull), 256, 0, st>>>(fitch, N, L, Lp, seed, first_null, scratch);
+  // scratch holds the Fitch sets, each row replaced by the null's row once used
+  const int chunks = Lp / 16;
+  for (int d = nlevels - 1; d >= 0; d--) {
+    const int nn = level_off[d + 1] - level_off[d];
+    if (nn <= 0) continue;
+    k_fitch_up<<<dim3((nn * chunks + 255) / 256, nnull), 256, 0, st>>>(ax, N, Lp, T.left, T.right,
+                                                                       level_nodes + level_off[d], nn, seed,
+                                                                       first_null, scratch);
+  }
+  k_root_state<<<dim3((L + 255) / 256, nnull), 256, 0, st>>>(N, L, Lp, seed, first_null, scratch, fitch);
+  k_root_row<<<dim3((Lp + 255) / 256, nnull), 256, 0, st>>>(N, L, Lp, seed, first_null, fitch, scratch);
   for (int d = 0; d < nlevels; d++) {
     const int nn = level_off[d + 1] - level_off[d];
     if (nn <= 0) continue;
-    k_branch<<<dim3(2 * nn, nnull), 1024, L, st>>>(ax, N, L, Lp, T.left, T.right, level_nodes + level_off[d], seed,
-                                                   first_null, fitch, scratch, out_ax, out_slot_stride);
+    k_replay<<<dim3((2 * nn + 7) / 8, nnull), 256, 0, st>>>(ax, N, L, Lp, T.left, T.right, level_nodes + level_off[d],
+                                                             nn, seed, first_null, fitch, scratch, out_ax,
+                                                             out_slot_stride);
   }
   return cudaGetLastError();
 }
