@@ -332,7 +332,7 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
         if (!ctx->umma) return fail(ctx, 12, "tensor counting not available for this shape");
         umma_set_weights(ctx->umma, ctx->h_w.data(), N, ctx->st);
       }
-      CK(umma_count(ctx->umma, ax, sstride, nslots, false, false, ctx->d_cnt, ctx->st));
+      CK(umma_count(ctx->umma, ax, sstride, nslots, false, ctx->d_cnt, ctx->st));
     } else {
       CK(launch_count_simt(ax, sstride, ctx->d_wf, false, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_cnt, ctx->st));
     }
@@ -346,9 +346,7 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   if (need_u) {
     if (!ctx->d_ucnt) CK(dalloc(&ctx->d_ucnt, (size_t)ctx->maxslots * cstride));
     if (counter == COVGPU_COUNT_TENSOR && ctx->umma) {
-      // the weighted pass of this call (tensor path) left the one-hot operand
-      CK(umma_count(ctx->umma, ax, sstride, nslots, true, need_w && counter == COVGPU_COUNT_TENSOR, ctx->d_ucnt,
-                    ctx->st));
+      CK(umma_count(ctx->umma, ax, sstride, nslots, true, ctx->d_ucnt, ctx->st));
     } else {
       CK(launch_count_simt(ax, sstride, ctx->d_wf, true, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_ucnt, ctx->st));
     }

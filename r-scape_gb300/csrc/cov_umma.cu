@@ -52,6 +52,7 @@ namespace covgpu {
 constexpr int UM = 128;          // rows of A tile (32 columns x 4 states)
 constexpr int UN = 128;          // rows of B tile
 constexpr int UK = 64;           // sequences per stage (128 bytes of BF16)
+constexpr int UK8 = 128;         // sequences per stage of the FP8 operands (128 bytes)
 constexpr int TILE_BYTES = UM * UK * 2;   // 16 KB per operand tile
 constexpr uint64_t WAIT_NS = 2000000000ull;   // every barrier wait gives up after 2 s
 
@@ -61,6 +62,9 @@ struct UmmaPlan {
   const TileRC* d_tiles = nullptr;
   int* d_order = nullptr;           // launch order of the tiles (blocked raster)
   __nv_bfloat16* d_ops = nullptr;   // [(1 + 3) * maxslots * 4Lp][Npad]
+  uint8_t* d_ops8 = nullptr;        // [maxslots * 4Lp][Npad8] FP8 E4M3 one-hot (unit weights)
+  int Npad8 = 0;                    // sequences padded to UK8
+  CUtensorMap tmap8;
   uint8_t* d_limbs = nullptr;       // [3][Npad] weight limbs
   int nl = 3;                       // limbs in use (1 when all weights are equal)
   double scale = 1.0;               // count = limb sum * scale
@@ -135,6 +139,20 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
 // instruction descriptor, kind::f16: BF16 x BF16 -> F32, both K-major
 __host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// instruction descriptor, kind::f8f6f4: E4M3 x E4M3 -> F32, both K-major
+__host__ __device__ constexpr uint32_t make_idesc_e4m3(int M, int N) {
+  return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_e4m3(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum)
+      : "memory");
 }
 
 __device__ __forceinline__ void umma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
@@ -220,6 +238,37 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
   }
 }
 
+// FP8 E4M3 one-hot rows [4Lp][Npad8] (1.0 = 0x38), state-major as above;
+// one CTA per (128 sequences, 32 columns, slot)
+__global__ void __launch_bounds__(256)
+k_umma_prep8(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, int Npad8, int nslots,
+             uint8_t* __restrict__ ops8) {
+  __shared__ uint8_t cs[128][33];
+  const int s0 = blockIdx.x * 128, c0 = blockIdx.y * 32, slot = blockIdx.z, tid = threadIdx.x;
+  const uint8_t* A = ax + (int64_t)slot * slot_stride;
+  for (int e = tid; e < 128 * 32; e += 256) {
+    const int s = e / 32, c = e % 32;
+    cs[s][c] = (s0 + s < N) ? A[(int64_t)(s0 + s) * Lp + c0 + c] : (uint8_t)4;
+  }
+  __syncthreads();
+  // 128 rows x 128 sequences; each thread writes 16 sequences of one row
+  for (int e = tid; e < 128 * 8; e += 256) {
+    const int r = e / 8, chunk = e % 8;
+    const int x = r / 32, c = r % 32;
+    const int64_t row = (int64_t)slot * 4 * Lp + 4 * c0 + r;
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      uint32_t v = 0;
+#pragma unroll
+      for (int b = 0; b < 4; b++) v |= (cs[chunk * 16 + 4 * k + b][c] == x ? 0x38u : 0u) << (8 * b);
+      w[k] = v;
+    }
+    *reinterpret_cast<uint4*>(ops8 + row * Npad8 + s0 + chunk * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+  (void)nslots;
+}
+
 // ---------------------------------------------------------------------------
 // the counting kernel: persistent, one CTA (6 warps) per SM
 //   warp 0 lane 0   TMA producer over all of the CTA's (tile, alignment)
@@ -231,13 +280,14 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
 //                   TMEM load, then combines, stages and stores while the
 //                   next task's MMAs run
 // ---------------------------------------------------------------------------
-template <int NL, int STAGES, int ACC>
+template <int NL, int STAGES, int ACC, bool F8>
 __global__ void __launch_bounds__(192, 1)
 k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
              const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles, int nslots_buf,
              int nslots, int Lp, int nkb, int bbuf, float s_hi, float s_lo, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   constexpr int STAGE_BYTES = TILE_BYTES * (1 + NL);
+  constexpr int KE = F8 ? UK8 : UK;        // sequences per stage (one 128-byte row)
   constexpr uint32_t ACC_COLS = NL * UN;   // one accumulator set: NL limbs x 128 columns
   constexpr uint32_t TMEM_COLS = (ACC * ACC_COLS <= 128) ? 128 : (ACC * ACC_COLS <= 256 ? 256 : 512);
   static_assert(ACC * ACC_COLS <= 512, "TMEM holds 512 columns");
@@ -295,10 +345,10 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
           if (*(volatile int*)&abort_flag) break;
           uint8_t* st = ring + (size_t)s * STAGE_BYTES;
           mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-          tma_load_2d(st, &tmap, kb * UK, rowA, &full_bar[s]);
+          tma_load_2d(st, &tmap, kb * KE, rowA, &full_bar[s]);
 #pragma unroll
           for (int l = 0; l < NL; l++)
-            tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * UK, (int)((bbuf + l) * rows_per_buf) + rowB,
+            tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * KE, (int)((bbuf + l) * rows_per_buf) + rowB,
                         &full_bar[s]);
           issued = g + 1;
         }
@@ -308,7 +358,7 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
   } else if (warp == 1) {
     if (lane == 0) {
       // ---- MMA issuer ----
-      constexpr uint32_t idesc = make_idesc(UM, UN);
+      constexpr uint32_t idesc = F8 ? make_idesc_e4m3(UM, UN) : make_idesc(UM, UN);
       uint32_t g = 0;
       int i = 0;
       for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x, i++) {
@@ -326,12 +376,14 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t sa = smem_u32(ring + (size_t)s * STAGE_BYTES);
 #pragma unroll
-          for (int k16 = 0; k16 < UK / 16; k16++) {
+          // four MMAs of 32 bytes of K each (16 BF16 or 32 FP8 sequences)
+          for (int k16 = 0; k16 < 4; k16++) {
             const uint64_t ad = make_desc(sa + k16 * 32);
 #pragma unroll
             for (int l = 0; l < NL; l++) {
               const uint64_t bd = make_desc(sa + (uint32_t)(1 + l) * TILE_BYTES + k16 * 32);
-              umma_f16(dacc + (uint32_t)(l * UN), ad, bd, idesc, (kb > 0 || k16 > 0) ? 1u : 0u);
+              if (F8) umma_e4m3(dacc + (uint32_t)(l * UN), ad, bd, idesc, (kb > 0 || k16 > 0) ? 1u : 0u);
+              else    umma_f16(dacc + (uint32_t)(l * UN), ad, bd, idesc, (kb > 0 || k16 > 0) ? 1u : 0u);
             }
           }
           umma_commit(&empty_bar[s]);
@@ -504,9 +556,11 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) { umma_plan_destroy(p); return nullptr; }
-  cudaFuncSetAttribute(k_count_umma<3, STAGES3, ACC3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_count_umma<3, STAGES3, ACC3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes(3));
-  cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_bytes(1));
+  cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes(1));
   cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev);
   return p;
@@ -515,6 +569,7 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
 void umma_plan_destroy(UmmaPlan* p) {
   if (!p) return;
   if (p->d_ops) cudaFree(p->d_ops);
+  if (p->d_ops8) cudaFree(p->d_ops8);
   if (p->d_order) cudaFree(p->d_order);
   if (p->d_limbs) cudaFree(p->d_limbs);
   if (p->d_err) cudaFree(p->d_err);
@@ -564,35 +619,62 @@ static bool encode_out_map(UmmaPlan* p, float* cnt, CUtensorMap* m) {
                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, bool a_ready,
-                       float* cnt, cudaStream_t st) {
+// FP8 operand buffer and its tensor map, made on the first unit-weight pass
+static cudaError_t ensure_fp8(UmmaPlan* p) {
+  if (p->d_ops8) return cudaSuccess;
+  p->Npad8 = (p->N + UK8 - 1) / UK8 * UK8;
+  const int64_t rows = (int64_t)p->maxslots * 4 * p->Lp;
+  cudaError_t e = cudaMalloc(&p->d_ops8, (size_t)rows * p->Npad8);
+  if (e != cudaSuccess) { p->d_ops8 = nullptr; return e; }
+  if ((e = cudaMemset(p->d_ops8, 0, (size_t)rows * p->Npad8)) != cudaSuccess) return e;
+  cuuint64_t gdim[2] = {(cuuint64_t)p->Npad8, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)p->Npad8};
+  cuuint32_t box[2] = {UK8, UM};
+  cuuint32_t estride[2] = {1, 1};
+  if (get_encode()(&p->tmap8, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, p->d_ops8, gdim, gstride, box, estride,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+    cudaFree(p->d_ops8);
+    p->d_ops8 = nullptr;
+    return cudaErrorInvalidValue;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
+                       cudaStream_t st) {
   if (nslots > p->maxslots) return cudaErrorInvalidValue;
   if (((uintptr_t)cnt & 15u) != 0) return cudaErrorInvalidValue;
   CUtensorMap omap;
   if (!encode_out_map(p, cnt, &omap)) return cudaErrorInvalidValue;
-  const int nl = unit ? 1 : p->nl;
-  dim3 pg(p->Npad / 64, p->Lp / 32, nslots);
-  // unit weights: B is the one-hot of A itself (buffer 0), so only A needs
-  // preparing, and not even that when the weighted pass just wrote it
-  if (!(unit && a_ready))
-    k_umma_prep<<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, unit ? 0 : nl, p->d_limbs,
-                                    unit, p->d_ops);
-  const int bbuf = unit ? 0 : 1;
-  const int nkb = p->Npad / UK;
-  // the scale as an unevaluated FP32 pair (a power of two with limbs)
-  const double scale = unit ? 1.0 : p->scale;
-  const float s_hi = (float)scale, s_lo = (float)(scale - (double)s_hi);
   // persistent: one CTA per SM, tasks (alignment, tile in raster order)
   const int64_t ntask = (int64_t)p->ntiles * nslots;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntask, p->nsm));
+  if (unit) {
+    // unit weights: the one-hot itself on both sides, exact in FP8 E4M3
+    cudaError_t e = ensure_fp8(p);
+    if (e != cudaSuccess) return e;
+    k_umma_prep8<<<dim3(p->Npad8 / 128, p->Lp / 32, nslots), 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad8,
+                                                                            nslots, p->d_ops8);
+    k_count_umma<1, STAGES1, ACC1, true><<<grid, 192, smem_bytes(1), st>>>(
+        p->tmap8, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, p->Npad8 / UK8, 0, 1.0f, 0.0f,
+        p->d_err);
+    return cudaGetLastError();
+  }
+  const int nl = p->nl;
+  dim3 pg(p->Npad / 64, p->Lp / 32, nslots);
+  k_umma_prep<<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, nl, p->d_limbs, false,
+                                  p->d_ops);
+  const int nkb = p->Npad / UK;
+  // the scale as an unevaluated FP32 pair (a power of two with limbs)
+  const double scale = p->scale;
+  const float s_hi = (float)scale, s_lo = (float)(scale - (double)s_hi);
   if (nl == 1)
-    k_count_umma<1, STAGES1, ACC1><<<grid, 192, smem_bytes(1), st>>>(p->tmap, omap, p->d_tiles, p->d_order,
-                                                                     p->ntiles, p->maxslots, nslots, p->Lp, nkb, bbuf,
-                                                                     s_hi, s_lo, p->d_err);
+    k_count_umma<1, STAGES1, ACC1, false><<<grid, 192, smem_bytes(1), st>>>(
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
   else
-    k_count_umma<3, STAGES3, ACC3><<<grid, 192, smem_bytes(3), st>>>(p->tmap, omap, p->d_tiles, p->d_order,
-                                                                     p->ntiles, p->maxslots, nslots, p->Lp, nkb, bbuf,
-                                                                     s_hi, s_lo, p->d_err);
+    k_count_umma<3, STAGES3, ACC3, false><<<grid, 192, smem_bytes(3), st>>>(
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
   return cudaGetLastError();
 }
 

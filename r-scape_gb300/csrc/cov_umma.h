@@ -14,10 +14,10 @@ UmmaPlan*   umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles
 void        umma_plan_destroy(UmmaPlan* p);
 void        umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t st);
 // counts of nslots alignments (slot stride in bytes of the code buffer) into
-// cnt [slot][tile][16][TPP]; unit = unit weights (RAF); a_ready = the one-hot
-// operand of these alignments was prepared by the call just before
-cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, bool a_ready,
-                       float* cnt, cudaStream_t st);
+// cnt [slot][tile][16][TPP]; unit = unit weights (RAF), counted on FP8 E4M3
+// one-hot operands
+cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
+                       cudaStream_t st);
 // error code recorded by the kernel (0 = none; 101-105 = a barrier wait
 // timed out); reading it resets it
 int         umma_error(UmmaPlan* p);
