@@ -87,6 +87,26 @@ int  covgpu_set_tree(covgpu_ctx *ctx, const int *parent, const int *left, const 
  * alignment in slot 0, written to slots first_slot .. */
 int  covgpu_make_nulls(covgpu_ctx *ctx, uint64_t seed, int first_null, int nnull, int first_slot);
 
+/* P(t) alignment simulator on the device (replaces cov_GenerateAlignment's
+ * ungapped evolution, src/cov_simulate.c:61-159,288-324,388-451,586-798,
+ * with ratematrix_ConditionalsFromRate, src/ratematrix.c:185-233): nrep
+ * alignments evolved down the context's tree (covgpu_set_tree) with branch
+ * lengths ld/rd [N-1], written to slots first_slot .. first_slot+nrep-1.
+ * Unpaired columns follow the 4x4 rate matrix Q4 (row-major, ACGU), base
+ * pairs the 16x16 pair rate matrix Q16 (state 4x+y); ct[L] = partner column
+ * or -1.  The root is root[L] (canonical residues) or, when NULL, drawn from
+ * the backgrounds pi4 / pi16.  Then each leaf row gets gap runs: a gapped
+ * column continues its run with probability 1 - 1/gap_mean, any other
+ * column opens one with probability gap_rate/gap_mean (gap_rate 0: none).
+ * Replicate r uses the random streams of replicate id rep0 + r.  Returns 0,
+ * 11 (bad arguments), 41/42 (a branch time or P(t) the reference rejects). */
+int  covgpu_simulate(covgpu_ctx *ctx, const double *ld, const double *rd, const double *Q4, const double *pi4,
+                     const double *Q16, const double *pi16, const int *ct, const uint8_t *root, double gap_rate,
+                     double gap_mean, uint64_t seed, uint32_t rep0, int first_slot, int nrep);
+/* the per-branch conditionals of the last covgpu_simulate: P4 [2(N-1)][4][4]
+ * and P16 [2(N-1)][16][16], branch 2v (left child of v) and 2v+1 (right) */
+int  covgpu_sim_tables(covgpu_ctx *ctx, double *P4, double *P16);
+
 /* scores: covtypes are COVTYPE codes (CHI=0, CHIp=1, CHIa=2, GT=3, GTp=4,
  * ... CCFa=26), at most 4 per call; minmax[slot][type][2] on return */
 int  covgpu_score(covgpu_ctx *ctx, int first_slot, int nslots, int ntypes, const int *covtypes, int covclass,
@@ -155,6 +175,9 @@ int  covgpu_synth(int N, int L, double tree_len, int nbp, int nhelix, int hmin, 
 int  covgpu_synth2(int N, int L, int tree_kind, double tree_len, int nbp, int nhelix, int hmin, int hmax,
                    double gap_rate, double gap_mean, uint64_t seed, uint8_t *ax, int *parent, int *left, int *right,
                    double *ld, double *rd, int *ct);
+/* the rate matrices and backgrounds of covgpu_synth's model (K80 singles,
+ * 16-state pair model), for covgpu_simulate */
+int  covgpu_synth_model(double *Q4, double *pi4, double *Q16, double *pi16);
 /* position-based weights (Henikoff & Henikoff 1994), summing to N */
 int  covgpu_weights_pb(const uint8_t *ax, int N, int L, double *wgt);
 /* R-scape's gap-column filter: useme[c] = 1 to keep column c */

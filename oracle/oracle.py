@@ -93,6 +93,11 @@ def lib():
         L.orc_faithful_rows.restype = C.c_double
         L.orc_faithful_raf.argtypes = [u8p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.orc_faithful_raf.restype = C.c_double
+        L.orc_sim_conditionals.argtypes = [f64p, C.c_int, C.c_double, f64p]
+        L.orc_sim_cdf.argtypes = [f64p, C.c_int, C.c_int, u64p]
+        L.orc_sim_cdf.restype = None
+        L.orc_simulate.argtypes = [C.POINTER(Tree), C.c_int, C.c_int, i32p, u64p, u64p, u64p, u64p, C.c_void_p,
+                                   C.c_double, C.c_double, C.c_uint64, C.c_uint32, u8p]
         _LIB = L
     return _LIB
 
@@ -204,6 +209,44 @@ def null_msa(ax, tree, seed, null_id):
     st = lib().orc_null_msa(ax, N, L, C.byref(tree.ct), seed, null_id, out)
     if st:
         raise RuntimeError("orc_null_msa failed")
+    return out.reshape(N, L)
+
+
+def sim_conditionals(Q, rt):
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    n = Q.shape[0]
+    P = np.zeros((n, n))
+    st = lib().orc_sim_conditionals(Q, n, float(rt), P)
+    if st:
+        raise RuntimeError("orc_sim_conditionals failed (%d)" % st)
+    return P
+
+
+def sim_cdf(P):
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    n = P.shape[-1]
+    rows = P.size // n
+    out = np.zeros(P.size, dtype=np.uint64)
+    lib().orc_sim_cdf(P, n, rows, out)
+    return out.reshape(P.shape)
+
+
+def simulate(tree, L, ct, P4, P16, pi4, pi16, root, gap_rate, gap_mean, seed, rep):
+    """One simulated alignment [N][L] from per-branch P tables (branch 2v+side)."""
+    N = tree.N
+    C4 = sim_cdf(np.asarray(P4).reshape(-1, 4, 4))
+    C16 = sim_cdf(np.asarray(P16).reshape(-1, 16, 16))
+    R4 = sim_cdf(np.asarray(pi4, dtype=np.float64).reshape(1, 4))
+    R16 = sim_cdf(np.asarray(pi16, dtype=np.float64).reshape(1, 16))
+    ctv = np.ascontiguousarray(ct, dtype=np.int32)
+    out = np.zeros(N * L, dtype=np.uint8)
+    rt = None if root is None else np.ascontiguousarray(root, dtype=np.uint8)
+    st = lib().orc_simulate(C.byref(tree.ct), N, L, ctv, np.ascontiguousarray(C4), np.ascontiguousarray(C16),
+                            np.ascontiguousarray(R4), np.ascontiguousarray(R16),
+                            None if rt is None else rt.ctypes.data, float(gap_rate), float(gap_mean), seed, rep,
+                            out)
+    if st:
+        raise RuntimeError("orc_simulate failed (%d)" % st)
     return out.reshape(N, L)
 
 

@@ -46,11 +46,14 @@ orc_philox4x32(const uint32_t key[2], const uint32_t ctr[4], uint32_t out[4])
   out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-/* stream tags of the null-alignment generator */
+/* stream tags of the null-alignment generator and of the simulator */
 #define TAG_FLEAF   0x11u
 #define TAG_FCHOOSE 0x12u
 #define TAG_COLPERM 0x13u
 #define TAG_SUBST   0x14u
+#define TAG_SIMROOT 0x21u
+#define TAG_SIMSUB  0x22u
+#define TAG_SIMGAP  0x23u
 
 static uint32_t
 rng_u32(uint64_t seed, uint32_t tag, uint32_t null_id, uint32_t a, uint32_t b)
@@ -60,6 +63,16 @@ rng_u32(uint64_t seed, uint32_t tag, uint32_t null_id, uint32_t a, uint32_t b)
   uint32_t out[4];
   orc_philox4x32(key, ctr, out);
   return out[0];
+}
+
+static uint64_t
+rng_u64(uint64_t seed, uint32_t tag, uint32_t rep, uint32_t a, uint32_t b)
+{
+  uint32_t key[2] = { (uint32_t)seed, (uint32_t)(seed >> 32) };
+  uint32_t ctr[4] = { tag, rep, a, b };
+  uint32_t out[4];
+  orc_philox4x32(key, ctr, out);
+  return (uint64_t)out[0] | ((uint64_t)out[1] << 32);
 }
 
 static void
@@ -1319,4 +1332,177 @@ orc_faithful_raf(const uint8_t *ax, int N, int L, int npairs, int nthreads, doub
   free(pi); free(pj);
   if (checksum) *checksum = total;
   return (double)n;
+}
+
+/* ------------------------------------------------------------------ */
+/* P(t) alignment simulator                                            */
+/* ------------------------------------------------------------------ */
+
+/* P = exp(t Q) (esl_dmx_Exp at src/ratematrix.c:208): A = t Q / 2^k with
+ * the largest absolute row sum of A at most 1/2, P = sum_{m <= 18} A^m / m!,
+ * then k squarings */
+int
+orc_sim_expm(const double *Q, int n, double t, double *P)
+{
+  double A[256], term[256], tmp[256], nrm = 0.0, r;
+  int i, j, l, m, k = 0;
+  if (n < 1 || n > 16) return 1;
+  for (i = 0; i < n; i++) {
+    r = 0.0;
+    for (j = 0; j < n; j++) r += fabs(Q[i * n + j] * t);
+    if (r > nrm) nrm = r;
+  }
+  while (nrm > 0.5) { nrm *= 0.5; k++; }
+  for (i = 0; i < n * n; i++) A[i] = Q[i] * t / ldexp(1.0, k);
+  for (i = 0; i < n * n; i++) { P[i] = (i % (n + 1) == 0) ? 1.0 : 0.0; term[i] = P[i]; }
+  for (m = 1; m <= 18; m++) {
+    for (i = 0; i < n; i++)
+      for (j = 0; j < n; j++) {
+        double s = 0.0;
+        for (l = 0; l < n; l++) s += term[i * n + l] * A[l * n + j];
+        tmp[i * n + j] = s / m;
+      }
+    for (i = 0; i < n * n; i++) { term[i] = tmp[i]; P[i] += term[i]; }
+  }
+  for (; k > 0; k--) {
+    for (i = 0; i < n; i++)
+      for (j = 0; j < n; j++) {
+        double s = 0.0;
+        for (l = 0; l < n; l++) s += P[i * n + l] * P[l * n + j];
+        tmp[i * n + j] = s;
+      }
+    for (i = 0; i < n * n; i++) P[i] = tmp[i];
+  }
+  return 0;
+}
+
+/* ratematrix_ConditionalsFromRate (src/ratematrix.c:185-233): a time in
+ * (-1e-5, 0) becomes 1e-5, a more negative one fails; times above 1e4 are
+ * capped (the branch that maps 0 to 1e-4 is overwritten by the cap's else
+ * branch, so time 0 gives the identity); negative entries above -1e-3 are
+ * zeroed, others fail; rows are renormalised */
+int
+orc_sim_conditionals(const double *Q, int n, double rt, double *P)
+{
+  double time;
+  int i, j;
+  if (rt < 0.0) {
+    if (rt > -1e-5) rt = 1e-5;
+    else return 1;
+  }
+  time = (rt > 10000.0) ? 10000.0 : rt;
+  if (orc_sim_expm(Q, n, time, P)) return 1;
+  for (i = 0; i < n; i++) {
+    double s = 0.0;
+    for (j = 0; j < n; j++) {
+      if (P[i * n + j] < 0.0) {
+        if (fabs(P[i * n + j]) < 0.001) P[i * n + j] = 0.0;
+        else return 2;
+      }
+    }
+    for (j = 0; j < n; j++) s += P[i * n + j];
+    if (!(s > 0.0)) return 2;
+    for (j = 0; j < n; j++) P[i * n + j] /= s;
+  }
+  return 0;
+}
+
+void
+orc_sim_cdf(const double *P, int n, int nrows, uint64_t *C)
+{
+  int i, j;
+  for (i = 0; i < nrows; i++) {
+    double c = 0.0;
+    for (j = 0; j < n; j++) {
+      c += P[i * n + j];
+      if (j == n - 1 || c >= 1.0) C[i * n + j] = UINT64_MAX;
+      else                        C[i * n + j] = (uint64_t)ldexp(c, 64);
+    }
+  }
+}
+
+/* cov_addres / cov_addpair: the first state whose running sum exceeds the
+ * uniform (here the 64-bit draw U against the thresholds) */
+static int
+sim_draw(const uint64_t *C, int n, uint64_t U)
+{
+  int i;
+  for (i = 0; i < n - 1; i++) if (U < C[i]) return i;
+  return n - 1;
+}
+
+/* units: an unpaired column c (partner -1) or a base pair c < ct[c], in
+ * column order */
+static int
+sim_units(int L, const int *ct, int *ua, int *ub)
+{
+  int c, n = 0;
+  for (c = 0; c < L; c++) {
+    if (ct[c] >= 0 && ct[c] < c) continue;
+    ua[n] = c; ub[n] = (ct[c] > c) ? ct[c] : -1; n++;
+  }
+  return n;
+}
+
+/* cov_evolve_root_ungapped_tree + cov_emit_ungapped + cov_substitute
+ * (src/cov_simulate.c:288-324,586-631,725-798): internal nodes in index
+ * order, each child drawn from its branch's conditional on the parent's
+ * state; then per leaf the gap process: a gapped column continues the run
+ * with probability pext, any other column opens one with probability popen
+ * (gap_rate / gap_mean, mean run length gap_mean) */
+int
+orc_simulate(const orc_tree_t *T, int N, int L, const int *ct, const uint64_t *C4, const uint64_t *C16,
+             const uint64_t *R4, const uint64_t *R16, const uint8_t *root, double gap_rate, double gap_mean,
+             uint64_t seed, uint32_t rep, uint8_t *out)
+{
+  int *ua = malloc(sizeof(int) * (L + 1)), *ub = malloc(sizeof(int) * (L + 1));
+  uint8_t *st = NULL;
+  int nu, u, v, s, n, c;
+  const double popen = (gap_mean > 0.0) ? gap_rate / gap_mean : 0.0;
+  const double pext = (gap_mean > 1.0) ? 1.0 - 1.0 / gap_mean : 0.0;
+  if (!ua || !ub) { free(ua); free(ub); return 5; }
+  nu = sim_units(L, ct, ua, ub);
+  st = malloc((size_t)(N > 1 ? N - 1 : 1) * nu);
+  if (!st) { free(ua); free(ub); return 5; }
+  for (u = 0; u < nu; u++) {
+    int x;
+    if (root) {
+      if (root[ua[u]] > 3 || (ub[u] >= 0 && root[ub[u]] > 3)) { free(ua); free(ub); free(st); return 11; }
+      x = (ub[u] >= 0) ? root[ua[u]] * 4 + root[ub[u]] : root[ua[u]];
+    } else {
+      const uint64_t U = rng_u64(seed, TAG_SIMROOT, rep, 0u, (uint32_t)u);
+      x = (ub[u] >= 0) ? sim_draw(R16, 16, U) : sim_draw(R4, 4, U);
+    }
+    st[u] = (uint8_t)x;
+  }
+  for (v = 0; v < N - 1; v++)
+    for (s = 0; s < 2; s++) {
+      const int ch = s ? T->right[v] : T->left[v];
+      const int b = 2 * v + s;
+      const uint32_t cid = (uint32_t)((ch <= 0) ? -ch : N + ch);
+      for (u = 0; u < nu; u++) {
+        const int a = st[(size_t)v * nu + u];
+        const uint64_t U = rng_u64(seed, TAG_SIMSUB, rep, cid, (uint32_t)u);
+        const int x = (ub[u] >= 0) ? sim_draw(C16 + ((size_t)b * 16 + a) * 16, 16, U)
+                                   : sim_draw(C4 + ((size_t)b * 4 + a) * 4, 4, U);
+        if (ch > 0) st[(size_t)ch * nu + u] = (uint8_t)x;
+        else if (ub[u] >= 0) { out[(size_t)(-ch) * L + ua[u]] = (uint8_t)(x / 4); out[(size_t)(-ch) * L + ub[u]] = (uint8_t)(x % 4); }
+        else out[(size_t)(-ch) * L + ua[u]] = (uint8_t)x;
+      }
+    }
+  for (n = 0; n < N; n++) {
+    int run = 0;
+    for (c = 0; c < L; c++) {
+      uint32_t key[2] = { (uint32_t)seed, (uint32_t)(seed >> 32) };
+      uint32_t ctr[4] = { TAG_SIMGAP, rep, (uint32_t)n, (uint32_t)c }, o[4];
+      double ue, uo;
+      orc_philox4x32(key, ctr, o);
+      ue = (double)o[0] * (1.0 / 4294967296.0);
+      uo = (double)o[1] * (1.0 / 4294967296.0);
+      if ((run && ue < pext) || uo < popen) { out[(size_t)n * L + c] = 4; run = 1; }
+      else run = 0;
+    }
+  }
+  free(ua); free(ub); free(st);
+  return 0;
 }

@@ -135,6 +135,23 @@ int  orc_fitch(const uint8_t *ax, int N, int L, const orc_tree_t *T, uint64_t se
 int  orc_null_msa(const uint8_t *ax, int N, int L, const orc_tree_t *T, uint64_t seed, uint32_t null_id,
                   uint8_t *out_ax);
 
+/* ---- P(t) alignment simulator (src/cov_simulate.c:288-451,586-798; src/ratematrix.c:185-233) ---- */
+/* P = exp(t Q) for an n x n rate matrix: scaling and squaring of a Taylor series */
+int  orc_sim_expm(const double *Q, int n, double t, double *P);
+/* ratematrix_ConditionalsFromRate: P(t) with the reference's time rules, small
+ * negative entries zeroed (others fail), rows renormalised */
+int  orc_sim_conditionals(const double *Q, int n, double rt, double *P);
+/* inverse-CDF thresholds of the n rows of P: C[i][k] = floor(cdf 2^64) of the
+ * running sum, the last of each row 2^64 - 1 */
+void orc_sim_cdf(const double *P, int n, int nrows, uint64_t *C);
+/* one alignment [N][L]: root (or a draw from the root CDFs R4/R16 when root
+ * is NULL) evolved down T with the per-branch thresholds C4 [2(N-1)][4][4]
+ * and C16 [2(N-1)][16][16] (branch 2v + side), ct[c] = partner or -1, then
+ * gap runs; rep selects the replicate's random streams */
+int  orc_simulate(const orc_tree_t *T, int N, int L, const int *ct, const uint64_t *C4, const uint64_t *C16,
+                  const uint64_t *R4, const uint64_t *R16, const uint8_t *root, double gap_rate,
+                  double gap_mean, uint64_t seed, uint32_t rep, uint8_t *out);
+
 /* ---- the whole per-alignment path (src/R-scape.c:1281-1371, 1564-1724, 2335-2724) ---- */
 void orc_params_default(orc_params_t *p);
 int  orc_rscape(const orc_params_t *p, const uint8_t *ax, const double *wgt, int N, int L,

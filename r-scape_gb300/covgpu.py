@@ -72,6 +72,10 @@ def lib():
         L.covgpu_get_alignment.argtypes = [vp, C.c_int, u8p]
         L.covgpu_set_tree.argtypes = [vp, i32p, i32p, i32p]
         L.covgpu_make_nulls.argtypes = [vp, C.c_uint64, C.c_int, C.c_int, C.c_int]
+        L.covgpu_simulate.argtypes = [vp, f64p, f64p, f64p, f64p, f64p, f64p, i32p, vp, C.c_double, C.c_double,
+                                      C.c_uint64, C.c_uint32, C.c_int, C.c_int]
+        L.covgpu_sim_tables.argtypes = [vp, f64p, f64p]
+        L.covgpu_synth_model.argtypes = [f64p, f64p, f64p, f64p]
         L.covgpu_score.argtypes = [vp, C.c_int, C.c_int, C.c_int, i32p, C.c_int, C.c_int, C.c_int, f64p, C.c_int,
                                    f64p]
         L.covgpu_get_cov.argtypes = [vp, C.c_int, C.c_int, f64p]
@@ -128,6 +132,13 @@ class Synth:
                                  self.ax, self.parent, self.left, self.right, self.ld, self.rd, self.ct)
         if st:
             raise ValueError("covgpu_synth: bad sizes (status %d)" % st)
+
+
+def synth_model():
+    """(Q4, pi4, Q16, pi16) of the synthetic-alignment model."""
+    Q4, pi4, Q16, pi16 = np.zeros(16), np.zeros(4), np.zeros(256), np.zeros(16)
+    lib().covgpu_synth_model(Q4, pi4, Q16, pi16)
+    return Q4.reshape(4, 4), pi4, Q16.reshape(16, 16), pi16
 
 
 def weights_pb(ax):
@@ -191,6 +202,24 @@ class Engine:
 
     def make_nulls(self, seed, first_null, nnull, first_slot):
         self._ck(lib().covgpu_make_nulls(self.h, seed, first_null, nnull, first_slot))
+
+    def simulate(self, ld, rd, Q4, pi4, Q16, pi16, ct, root=None, gap_rate=0.0, gap_mean=0.0, seed=42, rep0=0,
+                 first_slot=0, nrep=1):
+        """nrep alignments evolved down the tree set by set_tree (branch lengths ld, rd)
+        into slots first_slot..; see covgpu_simulate."""
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        rt = None if root is None else np.ascontiguousarray(root, dtype=np.uint8)
+        self._ck(lib().covgpu_simulate(self.h, f(ld), f(rd), f(Q4), f(pi4), f(Q16), f(pi16),
+                                       np.ascontiguousarray(ct, dtype=np.int32),
+                                       None if rt is None else rt.ctypes.data, float(gap_rate), float(gap_mean),
+                                       seed, rep0, first_slot, nrep))
+
+    def sim_tables(self):
+        nb = 2 * (self.N - 1)
+        P4 = np.zeros(nb * 16)
+        P16 = np.zeros(nb * 256)
+        self._ck(lib().covgpu_sim_tables(self.h, P4, P16))
+        return P4.reshape(nb, 4, 4), P16.reshape(nb, 16, 16)
 
     def score(self, types, first_slot=0, nslots=1, covclass=CSELECT, nseqthresh=8, alenthresh=50, allow=None,
               counter=SIMT):

@@ -15,6 +15,7 @@
 #include "cov_dev.cuh"
 #include "cov_kernels.h"
 #include "cov_fit.h"
+#include "cov_sim.h"
 #include "cov_umma.h"
 #include "covgpu.h"
 #include "rscape_cov.h"
@@ -63,6 +64,13 @@ struct covgpu_ctx {
   double* d_full = nullptr;
   UmmaPlan* umma = nullptr;
   FitWork* fitw = nullptr;
+  // simulator
+  double *d_simQ = nullptr, *d_simT = nullptr, *d_P4 = nullptr, *d_P16 = nullptr;
+  unsigned long long *d_C4 = nullptr, *d_C16 = nullptr, *d_R = nullptr;
+  int2* d_units = nullptr;
+  uint8_t *d_simroot = nullptr, *d_simstate = nullptr;
+  size_t simstate_cap = 0;
+  int sim_branches = 0;
   unsigned char* d_flush = nullptr;
   bool counted = false;
   cudaEvent_t ev[6] = {};
@@ -167,6 +175,9 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
   for (void* p : ptrs) if (p) cudaFree(p);
   if (ctx->umma) umma_plan_destroy(ctx->umma);
   if (ctx->fitw) fitwork_destroy(ctx->fitw);
+  void* sims[] = {ctx->d_simQ, ctx->d_simT, ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16, ctx->d_R, ctx->d_units,
+                  ctx->d_simroot, ctx->d_simstate};
+  for (void* p : sims) if (p) cudaFree(p);
   for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
@@ -266,6 +277,92 @@ static int make_nulls_async(covgpu_ctx* ctx, uint64_t seed, int first_null, int 
   return 0;
 }
 
+static int check_status(covgpu_ctx* ctx);
+
+extern "C" int covgpu_simulate(covgpu_ctx* ctx, const double* ld, const double* rd, const double* Q4,
+                               const double* pi4, const double* Q16, const double* pi16, const int* ct,
+                               const uint8_t* root, double gap_rate, double gap_mean, uint64_t seed, uint32_t rep0,
+                               int first_slot, int nrep) {
+  CK(cudaSetDevice(ctx->dev));
+  const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
+  if (!ctx->have_tree) return fail(ctx, 11, "no tree set");
+  if (N < 2) return fail(ctx, 11, "the simulator needs a tree of at least two leaves");
+  if (!ld || !rd || !Q4 || !pi4 || !Q16 || !pi16 || !ct) return fail(ctx, 11, "missing simulator argument");
+  if (nrep < 1 || first_slot < 0 || first_slot + nrep > ctx->maxslots) return fail(ctx, 11, "slots out of range");
+  if (gap_rate < 0.0 || gap_rate > 1.0 || (gap_rate > 0.0 && !(gap_mean >= 1.0)))
+    return fail(ctx, 11, "gap_rate in [0,1] and gap_mean >= 1");
+  double s4 = 0.0, s16 = 0.0;
+  for (int k = 0; k < 4; k++) { if (!(pi4[k] >= 0.0)) return fail(ctx, 11, "bad background"); s4 += pi4[k]; }
+  for (int k = 0; k < 16; k++) { if (!(pi16[k] >= 0.0)) return fail(ctx, 11, "bad background"); s16 += pi16[k]; }
+  if (fabs(s4 - 1.0) > 1e-6 || fabs(s16 - 1.0) > 1e-6) return fail(ctx, 11, "backgrounds must sum to 1");
+  // units: unpaired columns and base pairs (c < partner), in column order
+  std::vector<int2> units;
+  for (int c = 0; c < L; c++) {
+    const int p = ct[c];
+    if (p < -1 || p >= L || p == c || (p >= 0 && ct[p] != c)) return fail(ctx, 11, "ct: bad partner of column %d", c);
+    if (p >= 0 && p < c) continue;
+    units.push_back(make_int2(c, p));
+    if (root && (root[c] > 3 || (p >= 0 && root[p] > 3))) return fail(ctx, 11, "root: non-canonical residue");
+  }
+  const int nunits = (int)units.size();
+  const int nb = 2 * (N - 1);
+  std::vector<double> times(nb), Q(16 + 256 + 4 + 16);
+  for (int v = 0; v < N - 1; v++) { times[2 * v] = ld[v]; times[2 * v + 1] = rd[v]; }
+  for (int k = 0; k < 16; k++) Q[k] = Q4[k];
+  for (int k = 0; k < 256; k++) Q[16 + k] = Q16[k];
+  for (int k = 0; k < 4; k++) Q[272 + k] = pi4[k];
+  for (int k = 0; k < 16; k++) Q[276 + k] = pi16[k];
+  if (ctx->sim_branches != nb) {
+    void* old[] = {ctx->d_simT, ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16};
+    for (void* p : old) if (p) cudaFree(p);
+    CK(dalloc(&ctx->d_simT, nb));
+    CK(dalloc(&ctx->d_P4, (size_t)nb * 16));
+    CK(dalloc(&ctx->d_P16, (size_t)nb * 256));
+    CK(dalloc(&ctx->d_C4, (size_t)nb * 16));
+    CK(dalloc(&ctx->d_C16, (size_t)nb * 256));
+    ctx->sim_branches = nb;
+  }
+  if (!ctx->d_simQ) {
+    CK(dalloc(&ctx->d_simQ, 16 + 256 + 4 + 16));
+    CK(dalloc(&ctx->d_R, 4 + 16));
+    CK(dalloc(&ctx->d_units, L));
+    CK(dalloc(&ctx->d_simroot, Lp));
+  }
+  const size_t need = (size_t)nrep * (N - 1) * nunits;
+  if (ctx->simstate_cap < need) {
+    if (ctx->d_simstate) cudaFree(ctx->d_simstate);
+    CK(dalloc(&ctx->d_simstate, need));
+    ctx->simstate_cap = need;
+  }
+  CK(cudaMemcpyAsync(ctx->d_simT, times.data(), nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_simQ, Q.data(), Q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_units, units.data(), nunits * sizeof(int2), cudaMemcpyHostToDevice, ctx->st));
+  if (root) CK(cudaMemcpyAsync(ctx->d_simroot, root, L, cudaMemcpyHostToDevice, ctx->st));
+  CK(launch_sim_tables(ctx->d_simQ, ctx->d_simQ + 16, ctx->d_simQ + 272, ctx->d_simQ + 276, ctx->d_simT, nb,
+                       ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16, ctx->d_R, ctx->d_R + 4, ctx->d_status, ctx->st));
+  const int64_t sstride = (int64_t)N * Lp;
+  CK(launch_sim_evolve(ctx->d_left, ctx->d_right, N, L, Lp, ctx->d_units, nunits, ctx->d_C4, ctx->d_C16, ctx->d_R,
+                       ctx->d_R + 4, root ? ctx->d_simroot : nullptr, gap_rate, gap_mean, seed, rep0, nrep,
+                       ctx->d_simstate, ctx->d_ax + first_slot * sstride, sstride, ctx->st));
+  ctx->nlaunch += 6;
+  int s = 0;
+  CK(cudaMemcpyAsync(&s, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (s == 41 || s == 42) {
+    cudaMemset(ctx->d_status, 0, sizeof(int));
+    return fail(ctx, s, s == 41 ? "negative branch length" : "P(t) needed regularisation beyond -1e-3");
+  }
+  return check_status(ctx);
+}
+
+extern "C" int covgpu_sim_tables(covgpu_ctx* ctx, double* P4, double* P16) {
+  CK(cudaSetDevice(ctx->dev));
+  if (!ctx->sim_branches) return fail(ctx, 11, "no simulation yet");
+  if (P4) CK(cudaMemcpy(P4, ctx->d_P4, (size_t)ctx->sim_branches * 16 * sizeof(double), cudaMemcpyDeviceToHost));
+  if (P16) CK(cudaMemcpy(P16, ctx->d_P16, (size_t)ctx->sim_branches * 256 * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
 extern "C" int covgpu_make_nulls(covgpu_ctx* ctx, uint64_t seed, int first_null, int nnull, int first_slot) {
   CK(cudaSetDevice(ctx->dev));
   int s = make_nulls_async(ctx, seed, first_null, nnull, first_slot);
@@ -325,18 +422,18 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   const uint8_t* ax = ctx->d_ax + first * sstride;
   const int64_t cstride = (int64_t)ntiles * 16 * TPP;
   if (need_w) {
-    cudaEventRecord(ctx->ev[4], ctx->st);
     if (counter == COVGPU_COUNT_TENSOR) {
       if (!ctx->umma) {
         ctx->umma = umma_plan_create(N, L, Lp, ctx->nT, ctx->d_tiles, ntiles, ctx->maxslots);
         if (!ctx->umma) return fail(ctx, 12, "tensor counting not available for this shape");
         umma_set_weights(ctx->umma, ctx->h_w.data(), N, ctx->st);
       }
-      CK(umma_count(ctx->umma, ax, sstride, nslots, false, ctx->d_cnt, ctx->st));
+      CK(umma_count(ctx->umma, ax, sstride, nslots, false, ctx->d_cnt, ctx->st, ctx->ev[4], ctx->ev[5]));
     } else {
+      cudaEventRecord(ctx->ev[4], ctx->st);
       CK(launch_count_simt(ax, sstride, ctx->d_wf, false, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_cnt, ctx->st));
+      cudaEventRecord(ctx->ev[5], ctx->st);
     }
-    cudaEventRecord(ctx->ev[5], ctx->st);
     ctx->counted = true;
     CK(launch_pair_marg(ctx->d_cnt, L, ctx->d_tiles, ntiles, nT, nslots, ctx->d_part4, ctx->d_partR, ctx->st));
     CK(launch_pm_final(ctx->d_part4, ctx->d_partR, L, Lp, nT, nslots, ctx->d_pm, ctx->d_pmdf, ctx->d_ps,

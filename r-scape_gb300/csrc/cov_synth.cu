@@ -283,6 +283,19 @@ extern "C" int covgpu_synth2(int N, int L, int tree_kind, double tree_len, int n
   return 0;
 }
 
+extern "C" int covgpu_synth_model(double* Q4, double* pi4, double* Q16, double* pi16) {
+  std::vector<double> q4, q16, p16;
+  rate4(q4);
+  rate16(q16, p16);
+  for (int k = 0; k < 16; k++) Q4[k] = q4[k];
+  for (int k = 0; k < 4; k++) pi4[k] = 0.25;
+  for (int k = 0; k < 256; k++) Q16[k] = q16[k];
+  double s = 0.0;
+  for (int k = 0; k < 16; k++) s += p16[k];
+  for (int k = 0; k < 16; k++) pi16[k] = p16[k] / s;
+  return 0;
+}
+
 // Henikoff & Henikoff position-based weights over canonical residues,
 // renormalised to sum to N (R-scape's choice for nseq > 1000,
 // src/R-scape.c:1556)

@@ -642,7 +642,7 @@ static cudaError_t ensure_fp8(UmmaPlan* p) {
 }
 
 cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
-                       cudaStream_t st) {
+                       cudaStream_t st, cudaEvent_t ev0, cudaEvent_t ev1) {
   if (nslots > p->maxslots) return cudaErrorInvalidValue;
   if (((uintptr_t)cnt & 15u) != 0) return cudaErrorInvalidValue;
   CUtensorMap omap;
@@ -669,12 +669,14 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
   // the scale as an unevaluated FP32 pair (a power of two with limbs)
   const double scale = p->scale;
   const float s_hi = (float)scale, s_lo = (float)(scale - (double)s_hi);
+  if (ev0) cudaEventRecord(ev0, st);
   if (nl == 1)
     k_count_umma<1, STAGES1, ACC1, false><<<grid, 192, smem_bytes(1), st>>>(
         p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
   else
     k_count_umma<3, STAGES3, ACC3, false><<<grid, 192, smem_bytes(3), st>>>(
         p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
+  if (ev1) cudaEventRecord(ev1, st);
   return cudaGetLastError();
 }
 

@@ -15,9 +15,10 @@ void        umma_plan_destroy(UmmaPlan* p);
 void        umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t st);
 // counts of nslots alignments (slot stride in bytes of the code buffer) into
 // cnt [slot][tile][16][TPP]; unit = unit weights (RAF), counted on FP8 E4M3
-// one-hot operands
+// one-hot operands; ev0/ev1 (optional) are recorded around the weighted
+// count kernel itself
 cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
-                       cudaStream_t st);
+                       cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 // error code recorded by the kernel (0 = none; 101-105 = a barrier wait
 // timed out); reading it resets it
 int         umma_error(UmmaPlan* p);
