@@ -131,6 +131,30 @@ def profile_traffic(kernel):
     return None
 
 
+def simulator_rate(cg, e, s, N, L, nrep):
+    """Alignments per second of the P(t) simulator on the workload's tree and
+    structure (the planted pairs of the kept columns; nrep replicates per
+    call, no gaps), measured after the timed steps."""
+    Q4, pi4, Q16, pi16 = cg.synth_model()
+    keep = np.flatnonzero(cg.gapfilter(s.ax, None, 0.75))
+    new = -np.ones(len(s.ct), dtype=np.int64)
+    new[keep] = np.arange(len(keep))
+    ct = np.full(L, -1, dtype=np.int32)
+    for c_new, c_old in enumerate(keep):
+        p = s.ct[c_old]
+        if p >= 0 and new[p] >= 0:
+            ct[c_new] = new[p]
+    e.simulate(s.ld, s.rd, Q4, pi4, Q16, pi16, ct, seed=3, first_slot=1, nrep=nrep)   # warm-up
+    reps = 3
+    t0 = time.perf_counter()
+    for r in range(reps):
+        e.simulate(s.ld, s.rd, Q4, pi4, Q16, pi16, ct, seed=3, rep0=r * nrep, first_slot=1, nrep=nrep)
+    dt = (time.perf_counter() - t0) / reps
+    return {"alignments_per_s": nrep / dt, "ms_per_call": 1000.0 * dt, "alignments_per_call": nrep,
+            "codes_GB_per_s": nrep * N * L / dt / 1e9, "N": N, "L": L,
+            "note": "host-timed covgpu_simulate calls (P tables, evolution, synchronise)"}
+
+
 def cpu_reference(ax, w, budget_s, threads):
     """pairs/s of the reference loops on the host: counting + statistic per
     pair (x3: GTp, MIp, CHIp are three runs) and RAF's O(N^2) loop."""
@@ -174,6 +198,8 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--counter", default="auto", choices=["auto", "simt", "tensor"])
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU baseline sampling")
+    ap.add_argument("--once-sim", action="store_true",
+                    help="one call of the P(t) simulator on the workload's tree (for profiler captures)")
     ap.add_argument("--once", action="store_true",
                     help="one covgpu_rscape call of the workload and exit (for profiler captures)")
     ap.add_argument("--N", type=int, default=None, help="override N (profiling a smaller case)")
@@ -241,6 +267,9 @@ def main():
     except RuntimeError:
         counter = 0      # the tensor counter refuses this shape: plain path
         r = e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)
+    if args.once_sim:
+        print(json.dumps({"once_sim": True, **simulator_rate(cg, e, s, N, L, ns)}))
+        return
     if args.once:
         ms, n = e.last_timing()
         print(json.dumps({"once": True, "N": N, "L": L, "nshuffle": ns, "types": TYPES, "counter": counter,
@@ -288,6 +317,7 @@ def main():
     kname = "k_count_umma" if kind == "tensor" else "k_count_simt"
     traffic = profile_traffic(kname)
     cpu_v, cpu_sample, _ = cpu_reference(ax, w, args.cpu_budget, threads)
+    sim = simulator_rate(cg, e, s, N, L, ns)
     out = {
         "metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * step_s, "higher_is_better": True, "scaling": "weak",
@@ -305,6 +335,7 @@ def main():
         "cpu_baseline": {"value": cpu_v, "unit": "column-pairs/s", "cores": threads, "kind": "port",
                          "sample": cpu_sample},
         "hits": [len(x["hits"]) for x in res],
+        "simulator": sim,
         "clocks": clk.summary(),
     }
     print(json.dumps(out))

@@ -71,6 +71,7 @@ struct covgpu_ctx {
   uint8_t *d_simroot = nullptr, *d_simstate = nullptr;
   size_t simstate_cap = 0;
   int sim_branches = 0;
+  std::vector<double> sim_key;   // times and model of the tables on the device
   unsigned char* d_flush = nullptr;
   bool counted = false;
   cudaEvent_t ev[6] = {};
@@ -334,14 +335,23 @@ extern "C" int covgpu_simulate(covgpu_ctx* ctx, const double* ld, const double* 
     CK(dalloc(&ctx->d_simstate, need));
     ctx->simstate_cap = need;
   }
-  CK(cudaMemcpyAsync(ctx->d_simT, times.data(), nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-  CK(cudaMemcpyAsync(ctx->d_simQ, Q.data(), Q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
   CK(cudaMemcpyAsync(ctx->d_units, units.data(), nunits * sizeof(int2), cudaMemcpyHostToDevice, ctx->st));
   if (root) CK(cudaMemcpyAsync(ctx->d_simroot, root, L, cudaMemcpyHostToDevice, ctx->st));
-  CK(launch_sim_tables(ctx->d_simQ, ctx->d_simQ + 16, ctx->d_simQ + 272, ctx->d_simQ + 276, ctx->d_simT, nb,
-                       ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16, ctx->d_R, ctx->d_R + 4, ctx->d_status, ctx->st));
+  // the tables depend on the branch times and the model only: keep them
+  // across calls on the same tree and model
+  std::vector<double> key(times);
+  key.insert(key.end(), Q.begin(), Q.end());
+  if (key != ctx->sim_key) {
+    CK(cudaMemcpyAsync(ctx->d_simT, times.data(), nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->d_simQ, Q.data(), Q.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    CK(launch_sim_tables(ctx->d_simQ, ctx->d_simQ + 16, ctx->d_simQ + 272, ctx->d_simQ + 276, ctx->d_simT, nb,
+                         ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16, ctx->d_R, ctx->d_R + 4, ctx->d_status,
+                         ctx->st));
+    ctx->sim_key.swap(key);
+  }
   const int64_t sstride = (int64_t)N * Lp;
-  CK(launch_sim_evolve(ctx->d_left, ctx->d_right, N, L, Lp, ctx->d_units, nunits, ctx->d_C4, ctx->d_C16, ctx->d_R,
+  CK(launch_sim_evolve(ctx->d_left, ctx->d_right, ctx->d_lnodes, ctx->loff.data(), (int)ctx->loff.size() - 1, N, L,
+                       Lp, ctx->d_units, nunits, ctx->d_C4, ctx->d_C16, ctx->d_R,
                        ctx->d_R + 4, root ? ctx->d_simroot : nullptr, gap_rate, gap_mean, seed, rep0, nrep,
                        ctx->d_simstate, ctx->d_ax + first_slot * sstride, sstride, ctx->st));
   ctx->nlaunch += 6;

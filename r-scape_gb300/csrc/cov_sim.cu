@@ -10,16 +10,17 @@
 //                 regularisation (small negatives zeroed, rows renormalised),
 //                 then per row the inverse-CDF thresholds
 //                 C[k] = floor(running sum 2^64) as 64-bit integers.
-//   k_sim_evolve  one thread per (column unit, replicate): a unit is an
-//                 unpaired column (4 states) or a base pair (16 states); the
-//                 root state is given or drawn from the background, then the
-//                 internal nodes are visited in index order (parents first)
-//                 and each child draws its state from its branch's
-//                 conditional on the parent's state: the first state whose
-//                 threshold exceeds a 64-bit Philox draw.  Internal states
-//                 live in a node-major buffer (consecutive units in
-//                 consecutive threads: coalesced); leaf states go to the
-//                 output alignment slot.
+//   k_sim_root    the root state of every (column unit, replicate): a unit
+//                 is an unpaired column (4 states) or a base pair (16
+//                 states); given, or drawn from the background.
+//   k_sim_level   one launch per tree depth, one thread per (branch of the
+//                 depth's internal nodes, unit, replicate): the child draws
+//                 its state from its branch's conditional on the parent's
+//                 state, the first state whose threshold exceeds a 64-bit
+//                 Philox draw (the same draws as visiting the internal nodes
+//                 in index order, parents first).  Internal states live in
+//                 a node-major buffer (consecutive units in consecutive
+//                 threads: coalesced); leaf states go to the output slot.
 //   k_sim_gaps    one thread per (leaf, replicate): gap runs along the row
 //                 (a gapped column continues the run with probability pext,
 //                 any other column opens one with probability popen).
@@ -135,48 +136,53 @@ __device__ __forceinline__ int sim_draw(const unsigned long long* __restrict__ C
   return n - 1;
 }
 
-// one thread per (unit, replicate)
+// the root's state of every (unit, replicate): given, or drawn from the
+// background
 __global__ void __launch_bounds__(256)
-k_sim_evolve(const int* __restrict__ left, const int* __restrict__ right, int N, int Lp, const int2* __restrict__ units,
-             int nunits, const unsigned long long* __restrict__ C4, const unsigned long long* __restrict__ C16,
-             const unsigned long long* __restrict__ R4, const unsigned long long* __restrict__ R16,
-             const uint8_t* __restrict__ root, uint64_t seed, uint32_t first_rep, uint8_t* __restrict__ state,
-             uint8_t* __restrict__ out, int64_t out_slot_stride) {
-  const int u = blockIdx.x * blockDim.x + threadIdx.x;
-  const int rep = blockIdx.y;
+k_sim_root(int N, const int2* __restrict__ units, int nunits, const unsigned long long* __restrict__ R4,
+           const unsigned long long* __restrict__ R16, const uint8_t* __restrict__ root, uint64_t seed,
+           uint32_t first_rep, uint8_t* __restrict__ state) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x, rep = blockIdx.y;
   if (u >= nunits) return;
   const int2 un = units[u];
   const bool paired = un.y >= 0;
-  const uint32_t rid = first_rep + rep;
-  uint8_t* S = state + (size_t)rep * (N - 1) * nunits;
-  uint8_t* O = out + (int64_t)rep * out_slot_stride;
   int x;
   if (root) {
     x = paired ? root[un.x] * 4 + root[un.y] : root[un.x];
   } else {
-    const uint64_t U = rng_u64(seed, TAG_SIMROOT, rid, 0u, (uint32_t)u);
+    const uint64_t U = rng_u64(seed, TAG_SIMROOT, first_rep + rep, 0u, (uint32_t)u);
     x = paired ? sim_draw(R16, 16, U) : sim_draw(R4, 4, U);
   }
-  S[u] = (uint8_t)x;
-  for (int v = 0; v < N - 1; v++) {
-    const int a = S[(size_t)v * nunits + u];
-#pragma unroll
-    for (int s = 0; s < 2; s++) {
-      const int ch = s ? right[v] : left[v];
-      const int b = 2 * v + s;
-      const uint32_t cid = (uint32_t)((ch <= 0) ? -ch : N + ch);
-      const uint64_t U = rng_u64(seed, TAG_SIMSUB, rid, cid, (uint32_t)u);
-      const int y = paired ? sim_draw(C16 + ((size_t)b * 16 + a) * 16, 16, U)
-                           : sim_draw(C4 + ((size_t)b * 4 + a) * 4, 4, U);
-      if (ch > 0) {
-        S[(size_t)ch * nunits + u] = (uint8_t)y;
-      } else if (paired) {
-        O[(int64_t)(-ch) * Lp + un.x] = (uint8_t)(y >> 2);
-        O[(int64_t)(-ch) * Lp + un.y] = (uint8_t)(y & 3);
-      } else {
-        O[(int64_t)(-ch) * Lp + un.x] = (uint8_t)y;
-      }
-    }
+  state[(size_t)rep * (N - 1) * nunits + u] = (uint8_t)x;
+}
+
+// the branches of the internal nodes of one tree depth: one thread per
+// (branch, unit), consecutive units in consecutive threads
+__global__ void __launch_bounds__(256)
+k_sim_level(const int* __restrict__ left, const int* __restrict__ right, const int* __restrict__ nodes, int nn, int N,
+            int Lp, const int2* __restrict__ units, int nunits, const unsigned long long* __restrict__ C4,
+            const unsigned long long* __restrict__ C16, uint64_t seed, uint32_t first_rep,
+            uint8_t* __restrict__ state, uint8_t* __restrict__ out, int64_t out_slot_stride) {
+  const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int rep = blockIdx.y;
+  if (item >= (int64_t)2 * nn * nunits) return;
+  const int kb = (int)(item / nunits), u = (int)(item % nunits);
+  const int v = nodes[kb >> 1], side = kb & 1;
+  const int ch = side ? right[v] : left[v];
+  const int b = 2 * v + side;
+  const int2 un = units[u];
+  const bool paired = un.y >= 0;
+  uint8_t* S = state + (size_t)rep * (N - 1) * nunits;
+  const int a = S[(size_t)v * nunits + u];
+  const uint32_t cid = (uint32_t)((ch <= 0) ? -ch : N + ch);
+  const uint64_t U = rng_u64(seed, TAG_SIMSUB, first_rep + rep, cid, (uint32_t)u);
+  const int y = paired ? sim_draw(C16 + ((size_t)b * 16 + a) * 16, 16, U) : sim_draw(C4 + ((size_t)b * 4 + a) * 4, 4, U);
+  if (ch > 0) {
+    S[(size_t)ch * nunits + u] = (uint8_t)y;
+  } else {
+    uint8_t* O = out + (int64_t)rep * out_slot_stride + (int64_t)(-ch) * Lp;
+    if (paired) { O[un.x] = (uint8_t)(y >> 2); O[un.y] = (uint8_t)(y & 3); }
+    else        { O[un.x] = (uint8_t)y; }
   }
 }
 
@@ -220,13 +226,22 @@ cudaError_t launch_sim_tables(const double* Q4, const double* Q16, const double*
   return cudaGetLastError();
 }
 
-cudaError_t launch_sim_evolve(const int* left, const int* right, int N, int L, int Lp, const int2* units, int nunits,
+cudaError_t launch_sim_evolve(const int* left, const int* right, const int* level_nodes, const int* level_off,
+                              int nlevels, int N, int L, int Lp, const int2* units, int nunits,
                               const unsigned long long* C4, const unsigned long long* C16,
                               const unsigned long long* R4, const unsigned long long* R16, const uint8_t* root,
                               double gap_rate, double gap_mean, uint64_t seed, uint32_t first_rep, int nrep,
                               uint8_t* state, uint8_t* out, int64_t out_slot_stride, cudaStream_t st) {
-  k_sim_evolve<<<dim3((nunits + 255) / 256, nrep), 256, 0, st>>>(left, right, N, Lp, units, nunits, C4, C16, R4, R16,
-                                                                  root, seed, first_rep, state, out, out_slot_stride);
+  k_sim_root<<<dim3((nunits + 255) / 256, nrep), 256, 0, st>>>(N, units, nunits, R4, R16, root, seed, first_rep,
+                                                                state);
+  for (int d = 0; d < nlevels; d++) {
+    const int nn = level_off[d + 1] - level_off[d];
+    if (nn <= 0) continue;
+    const int64_t items = (int64_t)2 * nn * nunits;
+    k_sim_level<<<dim3((unsigned)((items + 255) / 256), nrep), 256, 0, st>>>(
+        left, right, level_nodes + level_off[d], nn, N, Lp, units, nunits, C4, C16, seed, first_rep, state, out,
+        out_slot_stride);
+  }
   const double popen = (gap_mean > 0.0) ? gap_rate / gap_mean : 0.0;
   const double pext = (gap_mean > 1.0) ? 1.0 - 1.0 / gap_mean : 0.0;
   if (popen > 0.0)

@@ -15,10 +15,12 @@ cudaError_t launch_sim_tables(const double* Q4, const double* Q16, const double*
                               cudaStream_t st);
 
 // nrep alignments: units (column, partner or -1) evolved down the tree from
-// root (or the background when root is null), leaves into out (slot stride
-// out_slot_stride, rows Lp), then gap runs; state is scratch
-// [nrep][N-1][nunits]
-cudaError_t launch_sim_evolve(const int* left, const int* right, int N, int L, int Lp, const int2* units, int nunits,
+// root (or the background when root is null), depth by depth (device list of
+// internal nodes by depth, host offsets level_off[nlevels + 1]), leaves into
+// out (slot stride out_slot_stride, rows Lp), then gap runs; state is
+// scratch [nrep][N-1][nunits]
+cudaError_t launch_sim_evolve(const int* left, const int* right, const int* level_nodes, const int* level_off,
+                              int nlevels, int N, int L, int Lp, const int2* units, int nunits,
                               const unsigned long long* C4, const unsigned long long* C16,
                               const unsigned long long* R4, const unsigned long long* R16, const uint8_t* root,
                               double gap_rate, double gap_mean, uint64_t seed, uint32_t first_rep, int nrep,
