@@ -103,6 +103,19 @@ int  covgpu_make_nulls(covgpu_ctx *ctx, uint64_t seed, int first_null, int nnull
 int  covgpu_simulate(covgpu_ctx *ctx, const double *ld, const double *rd, const double *Q4, const double *pi4,
                      const double *Q16, const double *pi16, const int *ct, const uint8_t *root, double gap_rate,
                      double gap_mean, uint64_t seed, uint32_t rep0, int first_slot, int nrep);
+/* alignment preparation on the device, for the alignment in a slot:
+ * position-based weights (Henikoff & Henikoff 1994; esl_msaweight_PB, which
+ * R-scape uses for nseq > 1000, src/R-scape.c:1556) summing to N, written to
+ * wgt[N] and, with set != 0, made the context's weights; and R-scape's gap
+ * column filter (msamanip_RemoveGapColumns, src/msamanip.c:461-501):
+ * useme[c] = 1 to keep column c (wgt NULL: unit weights) */
+int  covgpu_weights_pb_dev(covgpu_ctx *ctx, int slot, int set, double *wgt);
+/* Gerstein/Sonnhammer/Chothia tree weights (esl_msaweight_GSC, R-scape's
+ * choice for nseq <= 1000, src/R-scape.c:1555) on the device: distances
+ * 1 - identities/min(residues), UPGMA, each new branch shared among the
+ * leaves below it in proportion to their weights; summing to N */
+int  covgpu_weights_gsc_dev(covgpu_ctx *ctx, int slot, int set, double *wgt);
+int  covgpu_gapfilter_dev(covgpu_ctx *ctx, int slot, const double *wgt, double gapthresh, int *useme);
 /* the per-branch conditionals of the last covgpu_simulate: P4 [2(N-1)][4][4]
  * and P16 [2(N-1)][16][16], branch 2v (left child of v) and 2v+1 (right) */
 int  covgpu_sim_tables(covgpu_ctx *ctx, double *P4, double *P16);

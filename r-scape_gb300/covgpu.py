@@ -75,6 +75,9 @@ def lib():
         L.covgpu_simulate.argtypes = [vp, f64p, f64p, f64p, f64p, f64p, f64p, i32p, vp, C.c_double, C.c_double,
                                       C.c_uint64, C.c_uint32, C.c_int, C.c_int]
         L.covgpu_sim_tables.argtypes = [vp, f64p, f64p]
+        L.covgpu_weights_pb_dev.argtypes = [vp, C.c_int, C.c_int, f64p]
+        L.covgpu_weights_gsc_dev.argtypes = [vp, C.c_int, C.c_int, f64p]
+        L.covgpu_gapfilter_dev.argtypes = [vp, C.c_int, vp, C.c_double, i32p]
         L.covgpu_synth_model.argtypes = [f64p, f64p, f64p, f64p]
         L.covgpu_score.argtypes = [vp, C.c_int, C.c_int, C.c_int, i32p, C.c_int, C.c_int, C.c_int, f64p, C.c_int,
                                    f64p]
@@ -213,6 +216,25 @@ class Engine:
                                        np.ascontiguousarray(ct, dtype=np.int32),
                                        None if rt is None else rt.ctypes.data, float(gap_rate), float(gap_mean),
                                        seed, rep0, first_slot, nrep))
+
+    def weights_pb(self, slot=0, set=True):
+        """Position-based weights of the alignment in slot, computed on the device."""
+        w = np.zeros(self.N)
+        self._ck(lib().covgpu_weights_pb_dev(self.h, slot, 1 if set else 0, w))
+        return w
+
+    def weights_gsc(self, slot=0, set=True):
+        """GSC tree weights of the alignment in slot, computed on the device."""
+        w = np.zeros(self.N)
+        self._ck(lib().covgpu_weights_gsc_dev(self.h, slot, 1 if set else 0, w))
+        return w
+
+    def gapfilter(self, slot=0, wgt=None, gapthresh=0.75):
+        """Columns of the alignment in slot that the gap filter keeps (bool[L])."""
+        use = np.zeros(self.L, dtype=np.int32)
+        wv = None if wgt is None else np.ascontiguousarray(wgt, dtype=np.float64)
+        self._ck(lib().covgpu_gapfilter_dev(self.h, slot, None if wv is None else wv.ctypes.data, gapthresh, use))
+        return use.astype(bool)
 
     def sim_tables(self):
         nb = 2 * (self.N - 1)

@@ -15,6 +15,7 @@
 #include "cov_dev.cuh"
 #include "cov_kernels.h"
 #include "cov_fit.h"
+#include "cov_prep.h"
 #include "cov_sim.h"
 #include "cov_umma.h"
 #include "covgpu.h"
@@ -279,6 +280,69 @@ static int make_nulls_async(covgpu_ctx* ctx, uint64_t seed, int first_null, int 
 }
 
 static int check_status(covgpu_ctx* ctx);
+
+extern "C" int covgpu_weights_pb_dev(covgpu_ctx* ctx, int slot, int set, double* wgt) {
+  CK(cudaSetDevice(ctx->dev));
+  const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
+  if (slot < 0 || slot >= ctx->maxslots || !wgt) return fail(ctx, 11, "bad slot or output");
+  double *d_inv = nullptr, *d_w = nullptr;
+  CK(dalloc(&d_inv, (size_t)L * 4));
+  cudaError_t e = dalloc(&d_w, (size_t)N);
+  if (e == cudaSuccess) e = launch_weights_pb(ctx->d_ax + (size_t)slot * N * Lp, N, L, Lp, d_inv, d_w, ctx->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(wgt, d_w, N * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+  cudaFree(d_inv);
+  if (d_w) cudaFree(d_w);
+  if (e != cudaSuccess) return fail(ctx, 90, "CUDA error %s", cudaGetErrorString(e));
+  // renormalised to sum to N (the sum in sequence order, as the reference)
+  double sum = 0.0;
+  for (int s = 0; s < N; s++) sum += wgt[s];
+  for (int s = 0; s < N; s++) wgt[s] = (sum > 0.0) ? wgt[s] * (double)N / sum : 1.0;
+  return set ? covgpu_set_weights(ctx, wgt) : 0;
+}
+
+extern "C" int covgpu_weights_gsc_dev(covgpu_ctx* ctx, int slot, int set, double* wgt) {
+  CK(cudaSetDevice(ctx->dev));
+  const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
+  if (slot < 0 || slot >= ctx->maxslots || !wgt) return fail(ctx, 11, "bad slot or output");
+  if (N > 16384) return fail(ctx, 11, "GSC weights are for up to 16384 sequences (N^2 distances)");
+  if (N == 1) { wgt[0] = 1.0; return set ? covgpu_set_weights(ctx, wgt) : 0; }
+  void* scratch = nullptr;
+  double* d_w = nullptr;
+  CK(cudaMalloc(&scratch, gsc_scratch_bytes(N, L)));
+  cudaError_t e = dalloc(&d_w, (size_t)N);
+  if (e == cudaSuccess) e = launch_weights_gsc(ctx->d_ax + (size_t)slot * N * Lp, N, L, Lp, scratch, d_w, ctx->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(wgt, d_w, N * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+  cudaFree(scratch);
+  if (d_w) cudaFree(d_w);
+  if (e != cudaSuccess) return fail(ctx, 90, "CUDA error %s", cudaGetErrorString(e));
+  double sum = 0.0;
+  for (int s = 0; s < N; s++) sum += wgt[s];
+  for (int s = 0; s < N; s++) wgt[s] = (sum > 0.0) ? wgt[s] * (double)N / sum : 1.0;
+  return set ? covgpu_set_weights(ctx, wgt) : 0;
+}
+
+extern "C" int covgpu_gapfilter_dev(covgpu_ctx* ctx, int slot, const double* wgt, double gapthresh, int* useme) {
+  CK(cudaSetDevice(ctx->dev));
+  const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
+  if (slot < 0 || slot >= ctx->maxslots || !useme) return fail(ctx, 11, "bad slot or output");
+  double* d_w = nullptr;
+  int* d_use = nullptr;
+  CK(dalloc(&d_use, (size_t)L));
+  cudaError_t e = cudaSuccess;
+  if (wgt) {
+    e = dalloc(&d_w, (size_t)N);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_w, wgt, N * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
+  }
+  if (e == cudaSuccess) e = launch_gapfilter(ctx->d_ax + (size_t)slot * N * Lp, d_w, N, L, Lp, gapthresh, d_use, ctx->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(useme, d_use, L * sizeof(int), cudaMemcpyDeviceToHost, ctx->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+  cudaFree(d_use);
+  if (d_w) cudaFree(d_w);
+  if (e != cudaSuccess) return fail(ctx, 90, "CUDA error %s", cudaGetErrorString(e));
+  return 0;
+}
 
 extern "C" int covgpu_simulate(covgpu_ctx* ctx, const double* ld, const double* rd, const double* Q4,
                                const double* pi4, const double* Q16, const double* pi16, const int* ct,

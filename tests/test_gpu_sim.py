@@ -110,3 +110,22 @@ def test_distribution_matches_host_generator(covgpu):
     for a, b, what in [(Hg, Hh, "column entropy"), (Gg, Gh, "G of unpaired pairs"), (Pg, Ph, "G of base pairs")]:
         p = stats.ks_2samp(a, b).pvalue
         assert p > 1e-3, (what, p, np.mean(a), np.mean(b))
+
+
+@pytest.mark.parametrize("N,L", [(40, 60), (1200, 150), (7, 45)])
+def test_device_weights_and_gapfilter(covgpu, oracle, N, L):
+    s = covgpu.Synth(N, L, 1.0, 6, 1, 2, 6, 0.3, seed=4, tree_kind=1)
+    ax = s.ax.copy()
+    ax[0, :3] = [5, 15, 16]     # degenerate, N and '*' codes
+    ax[1, 3] = 17               # '~' is skipped by the gap filter
+    e = covgpu.Engine(N, L)
+    e.set_alignment(0, ax)
+    w = e.weights_pb(0, set=True)
+    assert np.allclose(w, oracle.weights_pb(ax), rtol=1e-12, atol=0)
+    if N <= 1200:
+        g = e.weights_gsc(0, set=False)
+        assert np.allclose(g, oracle.weights_gsc(ax), rtol=1e-10, atol=1e-13)
+    for wgt in (None, w):
+        for thr in (0.5, 0.75, 0.95):
+            assert np.array_equal(e.gapfilter(0, wgt, thr), oracle.gapfilter(ax, wgt, thr) == 1)
+    e.close()
