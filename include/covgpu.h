@@ -116,6 +116,23 @@ int  covgpu_weights_pb_dev(covgpu_ctx *ctx, int slot, int set, double *wgt);
  * leaves below it in proportion to their weights; summing to N */
 int  covgpu_weights_gsc_dev(covgpu_ctx *ctx, int slot, int set, double *wgt);
 int  covgpu_gapfilter_dev(covgpu_ctx *ctx, int slot, const double *wgt, double gapthresh, int *useme);
+/* substitutions on the branches of the context's tree (Tree_Substitutions,
+ * src/msatree.c:1423-1554) for the alignment in slot, on its Fitch
+ * reconstruction (random tie-breaks from seed): nsubs[L] per column; ndouble
+ * and njoin [L][L] per pair i < j (upper triangle, the rest 0): branches
+ * where both / at least one of the columns change; both ends canonical unless
+ * includegaps.  Outputs may be NULL; the last result stays on the device for
+ * covgpu_power. */
+int  covgpu_substitutions(covgpu_ctx *ctx, int slot, uint64_t seed, int includegaps, int *nsubs, int *ndouble,
+                          int *njoin);
+/* power of every pair i < j, in row-major order of the upper triangle
+ * (power_SPAIR_Create, src/power.c:65-218): the probability of the last of
+ * the ns curve points whose substitution count the pair's exceeds, for the
+ * single (nsubs_i + nsubs_j), join and double counts; a curve given as NULL
+ * gives 0 (single) or -1 (join, double) */
+int  covgpu_power(covgpu_ctx *ctx, int ns, const double *subs, const double *prob, const double *subs_join,
+                  const double *prob_join, const double *subs_double, const double *prob_double, double *power,
+                  double *power_join, double *power_double);
 /* the per-branch conditionals of the last covgpu_simulate: P4 [2(N-1)][4][4]
  * and P16 [2(N-1)][16][16], branch 2v (left child of v) and 2v+1 (right) */
 int  covgpu_sim_tables(covgpu_ctx *ctx, double *P4, double *P16);

@@ -94,6 +94,10 @@ def lib():
         L.orc_faithful_raf.argtypes = [u8p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
         L.orc_faithful_raf.restype = C.c_double
         L.orc_sim_conditionals.argtypes = [f64p, C.c_int, C.c_double, f64p]
+        L.orc_substitutions.argtypes = [u8p, C.c_int, C.c_int, C.POINTER(Tree), C.c_uint64, C.c_uint32, C.c_int,
+                                        i32p, i32p, i32p]
+        L.orc_power_step.argtypes = [C.c_double, C.c_int, f64p, f64p]
+        L.orc_power_step.restype = C.c_double
         L.orc_sim_cdf.argtypes = [f64p, C.c_int, C.c_int, u64p]
         L.orc_sim_cdf.restype = None
         L.orc_simulate.argtypes = [C.POINTER(Tree), C.c_int, C.c_int, i32p, u64p, u64p, u64p, u64p, C.c_void_p,
@@ -210,6 +214,24 @@ def null_msa(ax, tree, seed, null_id):
     if st:
         raise RuntimeError("orc_null_msa failed")
     return out.reshape(N, L)
+
+
+def substitutions(ax, tree, seed, null_id, includegaps=False):
+    ax = np.ascontiguousarray(ax, dtype=np.uint8)
+    N, L = ax.shape
+    ns = np.zeros(L, dtype=np.int32)
+    nd = np.zeros(L * L, dtype=np.int32)
+    nj = np.zeros(L * L, dtype=np.int32)
+    st = lib().orc_substitutions(ax, N, L, C.byref(tree.ct), seed, null_id, 1 if includegaps else 0, ns, nd, nj)
+    if st:
+        raise RuntimeError("orc_substitutions failed (%d)" % st)
+    return ns, nd.reshape(L, L), nj.reshape(L, L)
+
+
+def power_step(n, subs, prob):
+    subs = np.ascontiguousarray(subs, dtype=np.float64)
+    prob = np.ascontiguousarray(prob, dtype=np.float64)
+    return lib().orc_power_step(float(n), len(subs), subs, prob)
 
 
 def sim_conditionals(Q, rt):

@@ -1506,3 +1506,54 @@ orc_simulate(const orc_tree_t *T, int N, int L, const int *ct, const uint64_t *C
   free(ua); free(ub); free(st);
   return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Tree_Substitutions (src/msatree.c:1423-1554) and the power lookups of */
+/* power_SPAIR_Create (src/power.c:65-218)                              */
+/* ------------------------------------------------------------------ */
+int
+orc_substitutions(const uint8_t *ax, int N, int L, const orc_tree_t *T, uint64_t seed, uint32_t null_id,
+                  int includegaps, int *nsubs, int *ndouble, int *njoin)
+{
+  uint8_t *all = malloc((size_t)(2 * N - 1) * L);
+  int i, j, v, k;
+  if (!all) return 5;
+  if (orc_fitch(ax, N, L, T, seed, null_id, all)) { free(all); return 1; }
+  for (i = 0; i < L; i++) nsubs[i] = 0;
+  for (i = 0; i < L * L; i++) { ndouble[i] = 0; njoin[i] = 0; }
+  for (v = 0; v < N - 1; v++) {
+    const uint8_t *p = all + (int64_t)(N + v) * L;
+    for (k = 0; k < 2; k++) {
+      const int ch = k ? T->right[v] : T->left[v];
+      const uint8_t *c = all + (int64_t)((ch > 0) ? N + ch : -ch) * L;
+      for (i = 0; i < L; i++) {
+        if (includegaps) { if (c[i] != p[i]) nsubs[i]++; }
+        else if (p[i] < 4 && c[i] < 4 && c[i] != p[i]) nsubs[i]++;
+      }
+      for (i = 0; i < L - 1; i++)
+        for (j = i + 1; j < L; j++) {
+          if (includegaps) {
+            if (c[i] != p[i] && c[j] != p[j]) ndouble[i * L + j]++;
+            if (c[i] != p[i] || c[j] != p[j]) njoin[i * L + j]++;
+          } else if (p[i] < 4 && p[j] < 4 && c[i] < 4 && c[j] < 4) {
+            if (c[i] != p[i] && c[j] != p[j]) ndouble[i * L + j]++;
+            if (c[i] != p[i] || c[j] != p[j]) njoin[i * L + j]++;
+          }
+        }
+    }
+  }
+  free(all);
+  return 0;
+}
+
+double
+orc_power_step(double n, int ns, const double *subs, const double *prob)
+{
+  double p = 0.0;
+  int s;
+  for (s = 0; s < ns; s++) {
+    if (n > subs[s]) p = prob[s];
+    else break;
+  }
+  return p;
+}

@@ -152,6 +152,11 @@ int  orc_simulate(const orc_tree_t *T, int N, int L, const int *ct, const uint64
                   const uint64_t *R4, const uint64_t *R16, const uint8_t *root, double gap_rate,
                   double gap_mean, uint64_t seed, uint32_t rep, uint8_t *out);
 
+/* ---- substitutions and power (src/msatree.c:1423-1554; src/power.c:65-218) ---- */
+int    orc_substitutions(const uint8_t *ax, int N, int L, const orc_tree_t *T, uint64_t seed, uint32_t null_id,
+                         int includegaps, int *nsubs, int *ndouble, int *njoin);
+double orc_power_step(double n, int ns, const double *subs, const double *prob);
+
 /* ---- the whole per-alignment path (src/R-scape.c:1281-1371, 1564-1724, 2335-2724) ---- */
 void orc_params_default(orc_params_t *p);
 int  orc_rscape(const orc_params_t *p, const uint8_t *ax, const double *wgt, int N, int L,

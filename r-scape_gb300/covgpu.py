@@ -77,6 +77,8 @@ def lib():
         L.covgpu_sim_tables.argtypes = [vp, f64p, f64p]
         L.covgpu_weights_pb_dev.argtypes = [vp, C.c_int, C.c_int, f64p]
         L.covgpu_weights_gsc_dev.argtypes = [vp, C.c_int, C.c_int, f64p]
+        L.covgpu_substitutions.argtypes = [vp, C.c_int, C.c_uint64, C.c_int, i32p, i32p, i32p]
+        L.covgpu_power.argtypes = [vp, C.c_int] + [vp] * 9
         L.covgpu_gapfilter_dev.argtypes = [vp, C.c_int, vp, C.c_double, i32p]
         L.covgpu_synth_model.argtypes = [f64p, f64p, f64p, f64p]
         L.covgpu_score.argtypes = [vp, C.c_int, C.c_int, C.c_int, i32p, C.c_int, C.c_int, C.c_int, f64p, C.c_int,
@@ -222,6 +224,33 @@ class Engine:
         w = np.zeros(self.N)
         self._ck(lib().covgpu_weights_pb_dev(self.h, slot, 1 if set else 0, w))
         return w
+
+    def substitutions(self, slot=0, seed=42, includegaps=False):
+        """(nsubs[L], ndouble[L,L], njoin[L,L]) on the Fitch reconstruction of the alignment in slot."""
+        ns = np.zeros(self.L, dtype=np.int32)
+        nd = np.zeros((self.L, self.L), dtype=np.int32)
+        nj = np.zeros((self.L, self.L), dtype=np.int32)
+        self._ck(lib().covgpu_substitutions(self.h, slot, seed, 1 if includegaps else 0, ns, nd, nj))
+        return ns, nd, nj
+
+    def power(self, single=None, join=None, double=None):
+        """Pair power (i < j, row-major) from step curves given as (subs, prob) arrays of one length."""
+        curves = [single, join, double]
+        ns = max([len(c[0]) for c in curves if c is not None] + [0])
+        keep = []
+        def ptr(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            return a.ctypes.data
+        args = []
+        for c in curves:
+            args += [ptr(None if c is None else c[0]), ptr(None if c is None else c[1])]
+        P = self.L * (self.L - 1) // 2
+        outs = [np.zeros(P) for _ in range(3)]
+        self._ck(lib().covgpu_power(self.h, ns, *args, *[o.ctypes.data for o in outs]))
+        return outs
 
     def weights_gsc(self, slot=0, set=True):
         """GSC tree weights of the alignment in slot, computed on the device."""

@@ -17,6 +17,7 @@
 #include "cov_fit.h"
 #include "cov_prep.h"
 #include "cov_sim.h"
+#include "cov_subst.h"
 #include "cov_umma.h"
 #include "covgpu.h"
 #include "rscape_cov.h"
@@ -73,6 +74,8 @@ struct covgpu_ctx {
   size_t simstate_cap = 0;
   int sim_branches = 0;
   std::vector<double> sim_key;   // times and model of the tables on the device
+  // substitutions of the last covgpu_substitutions
+  int *d_nsubs = nullptr, *d_ndouble = nullptr, *d_njoin = nullptr;
   unsigned char* d_flush = nullptr;
   bool counted = false;
   cudaEvent_t ev[6] = {};
@@ -178,7 +181,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
   if (ctx->umma) umma_plan_destroy(ctx->umma);
   if (ctx->fitw) fitwork_destroy(ctx->fitw);
   void* sims[] = {ctx->d_simQ, ctx->d_simT, ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16, ctx->d_R, ctx->d_units,
-                  ctx->d_simroot, ctx->d_simstate};
+                  ctx->d_simroot, ctx->d_simstate, ctx->d_nsubs, ctx->d_ndouble, ctx->d_njoin};
   for (void* p : sims) if (p) cudaFree(p);
   for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -321,6 +324,82 @@ extern "C" int covgpu_weights_gsc_dev(covgpu_ctx* ctx, int slot, int set, double
   for (int s = 0; s < N; s++) sum += wgt[s];
   for (int s = 0; s < N; s++) wgt[s] = (sum > 0.0) ? wgt[s] * (double)N / sum : 1.0;
   return set ? covgpu_set_weights(ctx, wgt) : 0;
+}
+
+// random stream of the reconstruction's tie-breaks (null alignments use
+// stream ids 0 .. nshuffle-1)
+constexpr uint32_t kReconStream = 0xFFFFFFFFu;
+
+extern "C" int covgpu_substitutions(covgpu_ctx* ctx, int slot, uint64_t seed, int includegaps, int* nsubs,
+                                    int* ndouble, int* njoin) {
+  CK(cudaSetDevice(ctx->dev));
+  const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
+  if (!ctx->have_tree) return fail(ctx, 11, "no tree set");
+  if (N < 2) return fail(ctx, 11, "substitutions need a tree of at least two leaves");
+  if (slot < 0 || slot >= ctx->maxslots) return fail(ctx, 11, "bad slot");
+  const size_t rows = (size_t)(N - 1) * Lp;
+  uint8_t *F = ctx->d_fitch, *S = ctx->d_scratch, *tmp = nullptr;
+  if (!F || !S) {
+    CK(cudaMalloc(&tmp, 2 * rows));
+    F = tmp; S = tmp + rows;
+  }
+  const int Wb = (2 * (N - 1) + 31) / 32;
+  uint32_t* bits = nullptr;
+  cudaError_t e = cudaMalloc(&bits, 2 * (size_t)L * Wb * sizeof(uint32_t));
+  if (e == cudaSuccess && !ctx->d_nsubs) {
+    e = dalloc(&ctx->d_nsubs, (size_t)L);
+    if (e == cudaSuccess) e = dalloc(&ctx->d_ndouble, (size_t)L * L);
+    if (e == cudaSuccess) e = dalloc(&ctx->d_njoin, (size_t)L * L);
+  }
+  const uint8_t* ax = ctx->d_ax + (size_t)slot * N * Lp;
+  NullTree T{N, ctx->d_left, ctx->d_right};
+  if (e == cudaSuccess)
+    e = launch_fitch_recon(ax, N, L, Lp, T, ctx->d_lnodes, ctx->loff.data(), (int)ctx->loff.size() - 1, seed,
+                           kReconStream, F, S, ctx->st);
+  if (e == cudaSuccess)
+    e = launch_substitutions(ax, F, ctx->d_left, ctx->d_right, N, L, Lp, includegaps ? 1 : 0, bits,
+                             bits + (size_t)L * Wb, ctx->d_nsubs, ctx->d_ndouble, ctx->d_njoin, ctx->st);
+  if (e == cudaSuccess && nsubs) e = cudaMemcpyAsync(nsubs, ctx->d_nsubs, L * sizeof(int), cudaMemcpyDeviceToHost, ctx->st);
+  if (e == cudaSuccess && ndouble)
+    e = cudaMemcpyAsync(ndouble, ctx->d_ndouble, (size_t)L * L * sizeof(int), cudaMemcpyDeviceToHost, ctx->st);
+  if (e == cudaSuccess && njoin)
+    e = cudaMemcpyAsync(njoin, ctx->d_njoin, (size_t)L * L * sizeof(int), cudaMemcpyDeviceToHost, ctx->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+  if (bits) cudaFree(bits);
+  if (tmp) cudaFree(tmp);
+  if (e != cudaSuccess) return fail(ctx, 90, "CUDA error %s", cudaGetErrorString(e));
+  ctx->nlaunch += 4 + 2 * ((int)ctx->loff.size() - 1);
+  return 0;
+}
+
+extern "C" int covgpu_power(covgpu_ctx* ctx, int ns, const double* subs, const double* prob, const double* subs_join,
+                            const double* prob_join, const double* subs_double, const double* prob_double,
+                            double* power, double* power_join, double* power_double) {
+  CK(cudaSetDevice(ctx->dev));
+  const int L = ctx->L;
+  if (!ctx->d_nsubs) return fail(ctx, 11, "no substitutions yet");
+  if (ns < 0 || ns > 100000) return fail(ctx, 11, "bad number of power curve points");
+  std::vector<double> tab(6 * (size_t)std::max(ns, 1), 0.0);
+  const double* src[6] = {subs, prob, subs_join, prob_join, subs_double, prob_double};
+  for (int k = 0; k < 6; k++)
+    if (src[k]) for (int s = 0; s < ns; s++) tab[(size_t)k * ns + s] = src[k][s];
+  const int64_t P = (int64_t)L * (L - 1) / 2;
+  double *d_tab = nullptr, *d_out = nullptr;
+  CK(dalloc(&d_tab, tab.size()));
+  cudaError_t e = dalloc(&d_out, (size_t)3 * std::max<int64_t>(P, 1));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_tab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
+  if (e == cudaSuccess)
+    e = launch_power(ctx->d_nsubs, ctx->d_ndouble, ctx->d_njoin, L, ns, d_tab, subs && prob, subs_join && prob_join,
+                     subs_double && prob_double, d_out, d_out + P, d_out + 2 * P, ctx->st);
+  double* outs[3] = {power, power_join, power_double};
+  for (int k = 0; k < 3 && e == cudaSuccess; k++)
+    if (outs[k] && P > 0)
+      e = cudaMemcpyAsync(outs[k], d_out + k * P, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+  cudaFree(d_tab);
+  if (d_out) cudaFree(d_out);
+  if (e != cudaSuccess) return fail(ctx, 90, "CUDA error %s", cudaGetErrorString(e));
+  return 0;
 }
 
 extern "C" int covgpu_gapfilter_dev(covgpu_ctx* ctx, int slot, const double* wgt, double gapthresh, int* useme) {

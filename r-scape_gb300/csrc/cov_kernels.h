@@ -81,6 +81,11 @@ struct NullTree {
 };
 // level_nodes: device list of internal nodes ordered by depth; level_off:
 // host offsets of each depth in that list (nlevels + 1 entries)
+// the Fitch reconstruction of one alignment (random tie-breaks from stream
+// nid): F [N-1][Lp] states of the internal nodes, S [N-1][Lp] scratch sets
+cudaError_t launch_fitch_recon(const uint8_t* ax, int N, int L, int Lp, const NullTree& T, const int* level_nodes,
+                               const int* level_off, int nlevels, uint64_t seed, uint32_t nid, uint8_t* F, uint8_t* S,
+                               cudaStream_t st);
 cudaError_t launch_nullgen(const uint8_t* ax, int N, int L, int Lp, const NullTree& T, const int* level_nodes,
                            const int* level_off, int nlevels, uint64_t seed, uint32_t first_null, int nnull,
                            uint8_t* fitch, uint8_t* scratch, uint8_t* out_ax, int64_t out_slot_stride,

@@ -228,6 +228,53 @@ k_replay(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __rest
   }
 }
 
+// down pass of the Fitch reconstruction for the internal children of one
+// depth: one thread per (branch, 16 columns); a child keeps its parent's
+// state when its set holds it, else a random member of its set
+__global__ void __launch_bounds__(256)
+k_fitch_down(int N, int L, int Lp, const int* __restrict__ left, const int* __restrict__ right,
+             const int* __restrict__ nodes, int nn, uint64_t seed, uint32_t nid, const uint8_t* __restrict__ S,
+             uint8_t* __restrict__ F) {
+  const int chunks = Lp >> 4;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 2 * nn * chunks) return;
+  const int kb = idx / chunks, c0 = (idx % chunks) << 4;
+  const int v = nodes[kb >> 1];
+  const int ch = (kb & 1) ? right[v] : left[v];
+  if (ch <= 0) return;
+  for (int k = 0; k < 16; k++) {
+    const int c = c0 + k;
+    uint8_t st = 4;
+    if (c < L) {
+      const int a = F[(int64_t)v * Lp + c];
+      unsigned set = S[(int64_t)ch * Lp + c];
+      if (set & (1u << a)) set = 1u << a;
+      st = (uint8_t)choose_member(set, seed, nid, (uint32_t)ch, (uint32_t)c);
+    }
+    F[(int64_t)ch * Lp + c] = st;
+  }
+}
+
+cudaError_t launch_fitch_recon(const uint8_t* ax, int N, int L, int Lp, const NullTree& T, const int* level_nodes,
+                               const int* level_off, int nlevels, uint64_t seed, uint32_t nid, uint8_t* F, uint8_t* S,
+                               cudaStream_t st) {
+  const int chunks = Lp / 16;
+  for (int d = nlevels - 1; d >= 0; d--) {
+    const int nn = level_off[d + 1] - level_off[d];
+    if (nn <= 0) continue;
+    k_fitch_up<<<dim3((nn * chunks + 255) / 256, 1), 256, 0, st>>>(ax, N, Lp, T.left, T.right,
+                                                                    level_nodes + level_off[d], nn, seed, nid, S);
+  }
+  k_root_state<<<dim3((L + 255) / 256, 1), 256, 0, st>>>(N, L, Lp, seed, nid, S, F);
+  for (int d = 0; d < nlevels; d++) {
+    const int nn = level_off[d + 1] - level_off[d];
+    if (nn <= 0) continue;
+    k_fitch_down<<<(2 * nn * chunks + 255) / 256, 256, 0, st>>>(N, L, Lp, T.left, T.right, level_nodes + level_off[d],
+                                                                 nn, seed, nid, S, F);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_nullgen(const uint8_t* ax, int N, int L, int Lp, const NullTree& T, const int* level_nodes,
                            const int* level_off, int nlevels, uint64_t seed, uint32_t first_null, int nnull,
                            uint8_t* fitch, uint8_t* scratch, uint8_t* out_ax, int64_t out_slot_stride,
