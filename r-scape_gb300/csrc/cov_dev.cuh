@@ -8,7 +8,8 @@
 //                    I <= J), enumerated row by row of the upper triangle.
 //   counts           float [slot][tile][16][TP*TP]: the 4x4 weighted joint
 //                    counts of every pair of the tile, cell-major.
-//   scores           double [slot][stat][tile][TP*TP] (tile-packed COV).
+//   scores           float2 [slot][stat][tile][TP*TP], double-float (hi, lo)
+//                    values of the tile-packed COV.
 //   column partials  double [slot][nT][nT][TP][...]: per-tile row sums
 //                    (index [I][J]) and column sums (index [J][I]).
 #pragma once
@@ -88,17 +89,21 @@ __host__ __device__ __forceinline__ uint32_t feistel_hbits(uint32_t L) {
 constexpr uint32_t TAG_FLEAF = 0x11u, TAG_FCHOOSE = 0x12u, TAG_COLPERM = 0x13u, TAG_SUBST = 0x14u;
 
 // g(d) = (1+d) ln(1+d) - d, the non-negative per-cell term of the G-test
-// written as o ln(o/e) - (o - e) = e g((o-e)/e).  A 14-term Taylor series
-// for |d| < 1/4 (truncation < 1e-9 relative), the closed form beyond.
+// written as o ln(o/e) - (o - e) = e g((o-e)/e).  For |d| < 1/4,
+// g(d) = d^2 h(d) with h(d) = sum_m (-d)^m / ((m+1)(m+2)) replaced by its
+// degree-7 Chebyshev fit on [-1/4, 1/4] (fit error 3e-9 relative, below the
+// FP32 rounding of the Horner evaluation, 7e-8, as with the full series);
+// the closed form beyond.
 __device__ __forceinline__ float gfun(float d) {
   if (fabsf(d) < 0.25f) {
-    // g(d) = d^2 * sum_m (-d)^m / ((m+1)(m+2)), Horner in x = -d
-    const float x = -d;
-    float s = 1.f / 182.f;
-    s = 1.f / 156.f + x * s; s = 1.f / 132.f + x * s; s = 1.f / 110.f + x * s;
-    s = 1.f / 90.f + x * s;  s = 1.f / 72.f + x * s;  s = 1.f / 56.f + x * s;
-    s = 1.f / 42.f + x * s;  s = 1.f / 30.f + x * s;  s = 1.f / 20.f + x * s;
-    s = 1.f / 12.f + x * s;  s = 1.f / 6.f + x * s;   s = 0.5f + x * s;
+    float s = -1.525888499e-02f;
+    s = fmaf(s, d, 1.933413558e-02f);
+    s = fmaf(s, d, -2.374382876e-02f);
+    s = fmaf(s, d, 3.327445686e-02f);
+    s = fmaf(s, d, -5.000115186e-02f);
+    s = fmaf(s, d, 8.333407342e-02f);
+    s = fmaf(s, d, -1.666666567e-01f);
+    s = fmaf(s, d, 0.5f);
     return d * d * s;
   }
   return (1.f + d) * log1pf(d) - d;

@@ -144,6 +144,11 @@ __device__ __forceinline__ df df_of(double x) {
 }
 __device__ __forceinline__ double df_to_d(df a) { return (double)a.hi + (double)a.lo; }
 __device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
+// a * b exactly as a double-float (FMA residual)
+__device__ __forceinline__ df two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
 __device__ __forceinline__ df ld_df(const float2* p) { const float2 v = *p; return {v.x, v.y}; }
 __device__ __forceinline__ void st_df(float2* p, df v) { *p = make_float2(v.hi, v.lo); }
 // order of normalised double-float values (|lo| <= ulp(hi)/2)
@@ -427,11 +432,6 @@ __device__ __forceinline__ df pick_df(const PairOut& o, int k) {
 // hot part; a variant carries only what its statistics read)
 enum CellF : unsigned { CF_G = 1u, CF_CHI = 2u, CF_OMES = 4u, CF_H = 8u, CF_ALL = 15u };
 
-// the exact int64 v as double-float (|v| < 2^48)
-__device__ __forceinline__ df df_of_ll(long long v) {
-  const float hi = (float)v;
-  return {hi, (float)(v - (long long)hi)};
-}
 
 template <unsigned CF>
 __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[16], const float (&uc)[16],
@@ -439,8 +439,9 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
                                            const double* pmjd, const double* meanp, df ne, PairOut& out) {
   const unsigned S = A.stats;
   // ---- RAF from unit-weight counts (src/correlators.c:897-925 reduced):
-  // the sums are exact integers in fp32 (< 2^24), c_ij in 64-bit integers,
-  // the two ratios in double-float ----
+  // the sums are exact integers in fp32 (< 2^24); c_ij = nA^2 - (sum r_x^2
+  // + sum c_y^2)/2 is an integer below 2^48, formed exactly in double-float
+  // from exact FP32 products; the two ratios are double-float products ----
   if ((S & (S_RAF | S_RAFS)) && have_uc) {
     float nAf = 0.f, r[4] = {0.f, 0.f, 0.f, 0.f}, cc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
@@ -451,16 +452,16 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
           const float n = uc[x * 4 + y];
           nAf += n; r[x] += n; cc[y] += n;
         }
-    const long long nA = (long long)nAf;
-    long long sr = 0, sc = 0;
+    df sq = {0.f, 0.f};   // sum of the squared row and column counts (exact)
 #pragma unroll
     for (int x = 0; x < 4; x++) {
-      const long long a = (long long)r[x], b = (long long)cc[x];
-      sr += a * a; sc += b * b;
+      sq = df_add(sq, two_prod(r[x], r[x]));
+      sq = df_add(sq, two_prod(cc[x], cc[x]));
     }
-    const long long cnum = (2 * nA * nA - sr - sc) / 2;   // c_ij
-    const df q1 = df_mul(df_of_ll(cnum), {A.invD.x, A.invD.y});
-    const df q2 = df_mul(df_of_ll((long long)A.N - nA), {A.invN.x, A.invN.y});
+    const df nA2 = two_prod(nAf, nAf);
+    const df cnum = df_add(nA2, {-0.5f * sq.hi, -0.5f * sq.lo});   // c_ij, exact
+    const df q1 = df_mul(cnum, {A.invD.x, A.invD.y});
+    const df q2 = df_mul({(float)A.N - nAf, 0.f}, {A.invN.x, A.invN.y});
     out.raf = df_add({2.f * q1.hi, 2.f * q1.lo}, df_neg(q2));
   }
   // ---- CCF (src/correlators.c:1038-1053), FP64 ----
@@ -578,24 +579,21 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
 
 // One CTA per (tile, alignment), 256 threads, thread tid owns the pairs
 // p = tid + 256k (row a = warp + 8k, column b = lane).  Each pair's scores
-// go straight to the score planes; their row sums are reduced per warp as
-// they are made and their column sums kept as one running double-float per
-// output, so the APC/ASC partials cost no per-pair registers.
+// go straight to the score planes and into a shared-memory copy of the
+// tile; after the tile, one thread per (row, output) adds its row and one
+// per (column, output) its column in double-float, in a fixed order, for the
+// APC/ASC partials.
 template <unsigned CF>
 __global__ void __launch_bounds__(256)
 k_stats(StatsArgs A) {
-  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
   const TileRC tr = A.tiles[t];
   const float* C = A.cnt ? A.cnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
   const float* U = A.ucnt ? A.ucnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
   const double* pm = A.pm + (int64_t)slot * A.Lp * 4;
   const float2* pmdf = A.pmdf + (int64_t)slot * A.Lp * 4;
   const double* meanp = A.meanp + slot * 4;
-  __shared__ df rowbuf[TP][MAXOUT];
-  __shared__ df colbuf[8][TP][MAXOUT];
-  df colacc[MAXOUT];
-#pragma unroll
-  for (int q = 0; q < MAXOUT; q++) colacc[q] = {0.f, 0.f};
+  __shared__ float2 vs[MAXOUT][TP][TP + 1];   // the tile's scores, [q][a][b]
 #pragma unroll 1
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
@@ -619,28 +617,31 @@ k_stats(StatsArgs A) {
       if (q < A.nout) {
         const df v = valid ? pick_df(o, A.outstat[q]) : df{0.f, 0.f};
         st_df(A.cov + (((int64_t)slot * A.nout + q) * A.ntiles + t) * TPP + p, v);
-        const df rsum = warp_sum_df(v);
-        if (lane == 0) rowbuf[a][q] = rsum;
-        colacc[q] = df_add(colacc[q], v);
+        vs[q][a][b] = make_float2(v.hi, v.lo);
       }
     }
   }
-  // column sums across the 8 warps; rows of tile (I,J) and columns stored
-  // as FP64 partials (a diagonal tile adds both into part[I][I])
-#pragma unroll
-  for (int q = 0; q < MAXOUT; q++) colbuf[warp][lane][q] = colacc[q];
   __syncthreads();
-  if (tid < TP * A.nout) {
-    const int col = tid / A.nout, q = tid % A.nout;
-    df cs = {0.f, 0.f};
-    for (int wv = 0; wv < 8; wv++) cs = df_add(cs, colbuf[wv][col][q]);
-    double* part = A.part1 + ((int64_t)slot * A.nout + q) * A.nT * A.nT * TP;
-    if (tr.I == tr.J) {
-      part[((int64_t)tr.I * A.nT + tr.J) * TP + col] = df_to_d(df_add(rowbuf[col][q], cs));
-    } else {
-      part[((int64_t)tr.I * A.nT + tr.J) * TP + col] = df_to_d(rowbuf[col][q]);
-      part[((int64_t)tr.J * A.nT + tr.I) * TP + col] = df_to_d(cs);
+  // rows of tile (I,J) at part[I][J], columns at part[J][I]; a diagonal tile
+  // adds both roles into part[I][I]
+  double* base = A.part1 + (int64_t)slot * A.nout * A.nT * A.nT * TP;
+  const int64_t qstride = (int64_t)A.nT * A.nT * TP;
+  if (tr.I != tr.J) {
+    if (tid < 2 * TP * A.nout) {
+      const int role = tid / (TP * A.nout), rem = tid % (TP * A.nout);
+      const int line = rem / A.nout, q = rem % A.nout;
+      df sum = {0.f, 0.f};
+      if (role == 0) { for (int b = 0; b < TP; b++) sum = df_add(sum, {vs[q][line][b].x, vs[q][line][b].y}); }
+      else           { for (int a = 0; a < TP; a++) sum = df_add(sum, {vs[q][a][line].x, vs[q][a][line].y}); }
+      const int64_t cell = (role == 0) ? ((int64_t)tr.I * A.nT + tr.J) : ((int64_t)tr.J * A.nT + tr.I);
+      base[q * qstride + cell * TP + line] = df_to_d(sum);
     }
+  } else if (tid < TP * A.nout) {
+    const int line = tid / A.nout, q = tid % A.nout;
+    df r = {0.f, 0.f}, c = {0.f, 0.f};
+    for (int b = 0; b < TP; b++) r = df_add(r, {vs[q][line][b].x, vs[q][line][b].y});
+    for (int a = 0; a < TP; a++) c = df_add(c, {vs[q][a][line].x, vs[q][a][line].y});
+    base[q * qstride + ((int64_t)tr.I * A.nT + tr.I) * TP + line] = df_to_d(df_add(r, c));
   }
 }
 
