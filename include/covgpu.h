@@ -192,6 +192,93 @@ int  covgpu_correct_noalloc(const double *d_cov, double *d_out, int L, int actyp
 /* writes a 256 MB device buffer (larger than L2) on the context's stream */
 int  covgpu_flush_l2(covgpu_ctx *ctx);
 
+/* ---- learned null (no counterpart in the reference) ----
+ * R-scape gets the null score tail of every alignment from simulated null
+ * alignments (null_rscape, src/R-scape.c:1614-1724, and the gamma fit of
+ * cov_NullFitGamma, src/covariation.c:1943-1973).  The learned null predicts
+ * that tail from 64 summary features of the alignment with a multilayer
+ * perceptron 64 -> 256 -> 256 -> 256 -> 3 (SiLU; BF16 weights, FP32
+ * activations and accumulation), trained on the device on fits from
+ * simulated nulls.  Its three outputs correct the gamma tail fitted to a few
+ * quick nulls (location mu_q, mean excess m_q = tau_q/lambda_q, shape tau_q;
+ * features 60-62) towards the tail of many nulls: mu = mu_q + y0 m_q,
+ * log(tau/lambda) = log m_q + y1, log tau = log tau_q + y2. */
+#define COVGPU_NFEAT 64
+#define COVGPU_NOUT 3
+#define COVGPU_MLP_NPARAM 148995
+typedef struct covgpu_mlp covgpu_mlp;
+
+/* the alignment part (features 0-46; 47-63 are set to 0) of the learned
+ * null's input for the alignment in slot, with the context's weights:
+ * log N, log L, log effective N, pairwise identity (mean, sd), column
+ * entropy and gap fraction (mean, sd, 16-bin histograms), residue
+ * composition, weight spread and tree_len, the caller's tree-length summary
+ * (the mean root-to-leaf length of the alignment's tree) */
+int  covgpu_features(covgpu_ctx *ctx, int slot, double tree_len, float *feat);
+/* all 64 features of the alignment in slot 0: the alignment part and, in
+ * 47-63, a summary of the scores of nquick null alignments of covtype (run
+ * as covgpu_rscape with nshuffle = nquick): log of their number, mean, sd,
+ * upper quantiles at survival 0.5 ... 0.0005, their tail fit (mu, log mean
+ * excess, log shape) and the largest null score */
+int  covgpu_learned_features(covgpu_ctx *ctx, const covgpu_params *p, double tree_len, int covtype, int nquick,
+                             float *feat);
+
+/* a network with LeCun-uniform weights from seed; batch_cap rows per batch.
+ * Parameters are FP32 masters, layer by layer W[out][in] then b[out]. */
+int  covgpu_mlp_create(covgpu_mlp **ret, int device, int batch_cap, uint64_t seed);
+void covgpu_mlp_destroy(covgpu_mlp *net);
+const char *covgpu_mlp_errmsg(const covgpu_mlp *net);
+int  covgpu_mlp_set_params(covgpu_mlp *net, const float *params);
+int  covgpu_mlp_get_params(covgpu_mlp *net, float *params);
+/* inputs x' = (x - xmean)/xstd, outputs y = y' ystd + ymean; features within
+ * [xlo, xhi] (may be NULL: unbounded) are inside the training range */
+int  covgpu_mlp_set_norm(covgpu_mlp *net, const float *xmean, const float *xstd, const float *ymean,
+                         const float *ystd, const float *xlo, const float *xhi);
+int  covgpu_mlp_get_norm(const covgpu_mlp *net, float *xmean, float *xstd, float *ymean, float *ystd, float *xlo,
+                         float *xhi);
+/* 1 if every feature lies inside the training range */
+int  covgpu_mlp_in_range(const covgpu_mlp *net, const float *feat);
+/* Y[n][3] = network(X[n][64]) */
+int  covgpu_mlp_forward(covgpu_mlp *net, const float *X, int n, float *Y);
+/* the mean squared error on standardised targets of one batch of n rows
+ * (n <= batch_cap) and its gradient grad[COVGPU_MLP_NPARAM]; no update */
+int  covgpu_mlp_grad(covgpu_mlp *net, const float *X, const float *T, int n, float *grad, float *loss);
+/* AdamW (beta 0.9/0.999, cosine decay of lr to 5%) over epochs of shuffled
+ * batches, each step one replayed CUDA graph; epoch_loss[epochs] (may be NULL) */
+int  covgpu_mlp_train(covgpu_mlp *net, const float *X, const float *T, int n, int epochs, int batch, float lr,
+                      float wd, uint64_t seed, float *epoch_loss);
+/* covgpu_rscape for one covariation type with the learned null: simulates
+ * nquick null alignments (instead of p->nshuffle), and when the 64 features
+ * are inside the network's training range takes the null tail (mass
+ * p->pmass) from the network; otherwise falls back to covgpu_rscape with
+ * p->nshuffle simulated nulls.  *used_net tells which.  The result's mu,
+ * lambda, tau are the tail used; its nshuffle the nulls simulated. */
+int  covgpu_rscape_learned(covgpu_ctx *ctx, const covgpu_params *p, const uint8_t *ax, const double *wgt,
+                           covgpu_mlp *net, double tree_len, int covtype, int nquick, covgpu_result *result,
+                           covgpu_hit *hits, int hitcap, int *used_net);
+
+/* ---- helix aggregation (agg_CalculatePvalues, src/aggregate.c:41-128) ----
+ * covgpu_helices splits a nested consensus structure ct[L] (0-based partner
+ * or -1) into helices as R-scape does (ct_split_rmlist,
+ * src/structure.c:2990-3142): a pair opens a new helix when it closes a
+ * hairpin, a multiloop, or more than helix_unpaired (R-scape: 2) unpaired
+ * residues around one inner helix.  Output: *nh helices, helix_off[nh+1]
+ * (room for L/2+1), pairs bp_i < bp_j [L/2] grouped by helix, each helix in
+ * increasing i.  Host code.  Returns 0, 11 (ct not a pairing) or 13
+ * (pseudoknot). */
+int  covgpu_helices(const int *ct, int L, int helix_unpaired, int *nh, int *helix_off, int *bp_i, int *bp_j);
+/* the aggregated p-value of each helix on the device from the p-values of
+ * its pairs, pval[helix_off[nh]] in covgpu_helices order:
+ * COVGPU_AGG_FISHER (agg_FISHER, src/aggregate.c:141-176), _LANCASTER
+ * (:189-236; aux = the pairs' substitution counts, weights 1 + aux),
+ * _WFISHER (:248-289; aux = the pairs' power, weights 0.01 + aux scaled to
+ * sum 2 nbp), _SIDAK (:297-322).  A helix of one pair keeps its p-value.
+ * Eagg (may be NULL) = nh * pagg.  Chi-square quantiles are taken on the
+ * upper tail (Q^-1(w/2, p)), not as the lower-tail inverse at 1 - p. */
+enum { COVGPU_AGG_FISHER = 0, COVGPU_AGG_LANCASTER = 1, COVGPU_AGG_WFISHER = 2, COVGPU_AGG_SIDAK = 3 };
+int  covgpu_aggregate(covgpu_ctx *ctx, int method, int nh, const int *helix_off, const double *pval,
+                      const double *aux, double *pagg, double *Eagg);
+
 /* ---- host utilities for preparing alignments ---- */
 /* synthetic RNA alignment: coalescent tree of leaf-to-root length tree_len
  * (Easel convention, arrays of N-1),

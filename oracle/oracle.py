@@ -102,6 +102,13 @@ def lib():
         L.orc_sim_cdf.restype = None
         L.orc_simulate.argtypes = [C.POINTER(Tree), C.c_int, C.c_int, i32p, u64p, u64p, u64p, u64p, C.c_void_p,
                                    C.c_double, C.c_double, C.c_uint64, C.c_uint32, u8p]
+        f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.orc_features.argtypes = [u8p, C.c_int, C.c_int, f64p, C.c_double, f64p]
+        L.orc_features.restype = None
+        L.orc_mlp_forward.argtypes = [f32p, f32p, f32p, C.c_int, f64p]
+        L.orc_mlp_forward.restype = None
+        L.orc_mlp_grad.argtypes = [f32p, f32p, f32p, f32p, C.c_int, f64p]
+        L.orc_mlp_grad.restype = C.c_double
         _LIB = L
     return _LIB
 
@@ -335,3 +342,31 @@ def faithful_raf(ax, npairs, nthreads=0):
     cs = C.c_double()
     n = lib().orc_faithful_raf(ax, N, L, npairs, nthreads, C.byref(cs))
     return int(n), cs.value
+
+
+def features(ax, wgt, tree_len):
+    """The 64 learned-null features of ax [N][L] with weights wgt, in FP64."""
+    ax = np.ascontiguousarray(ax, dtype=np.uint8)
+    N, L = ax.shape
+    f = np.zeros(64)
+    lib().orc_features(ax, N, L, np.ascontiguousarray(wgt, dtype=np.float64), float(tree_len), f)
+    return f
+
+
+def mlp_forward(params, nrm, X):
+    """De-standardised outputs [n][3] of the learned-null network in FP64."""
+    X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, 64)
+    Y = np.zeros((X.shape[0], 3))
+    lib().orc_mlp_forward(np.ascontiguousarray(params, dtype=np.float32), np.ascontiguousarray(nrm, dtype=np.float32),
+                          X, X.shape[0], Y)
+    return Y
+
+
+def mlp_grad(params, nrm, X, T):
+    """(loss, gradient[148995]) of the network's mean squared error in FP64."""
+    X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, 64)
+    T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1, 3)
+    g = np.zeros(148995)
+    loss = lib().orc_mlp_grad(np.ascontiguousarray(params, dtype=np.float32),
+                              np.ascontiguousarray(nrm, dtype=np.float32), X, T, X.shape[0], g)
+    return loss, g

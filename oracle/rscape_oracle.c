@@ -1557,3 +1557,214 @@ orc_power_step(double n, int ns, const double *subs, const double *prob)
   }
   return p;
 }
+
+/* ------------------------------------------------------------------------
+ * Learned null: features and the network, restated in FP64 from the
+ * library's own definitions (no reference counterpart).
+ * ------------------------------------------------------------------------ */
+static uint64_t orc_splitmix64(uint64_t x) {   /* Steele, Lea & Flood 2014 */
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+static int orc_bin16(double v, double scale) {
+  const double q = v * scale;
+  if (!(q >= 0.0)) return 0;
+  return q >= 15.0 ? 15 : (int)q;
+}
+
+void orc_features(const uint8_t *ax, int N, int L, const double *w, double tree_len, double *feat) {
+  const int NPAIR = 4096;
+  double sw = 0.0, sw2 = 0.0;
+  for (int s = 0; s < N; s++) { sw += w[s]; sw2 += w[s] * w[s]; }
+  const double wmean = sw / N;
+  double wvar = 0.0;
+  for (int s = 0; s < N; s++) wvar += (w[s] - wmean) * (w[s] - wmean);
+  wvar /= N;
+  double *H = malloc(sizeof(double) * L), *g = malloc(sizeof(double) * L);
+  double comp[4] = {0, 0, 0, 0};
+  int hist[2][16];
+  memset(hist, 0, sizeof(hist));
+  for (int c = 0; c < L; c++) {
+    double n[4] = {0, 0, 0, 0};
+    for (int s = 0; s < N; s++) {
+      const int x = ax[(size_t)s * L + c];
+      if (x < 4) n[x] += w[s];
+    }
+    const double r = (n[0] + n[1]) + (n[2] + n[3]);
+    double h = 0.0;
+    if (r > 0.0)
+      for (int x = 0; x < 4; x++)
+        if (n[x] > 0.0) { const double p = n[x] / r; h -= p * log2(p); }
+    H[c] = h;
+    g[c] = sw > 0.0 ? fmax(0.0, (sw - r) / sw) : 0.0;
+    for (int x = 0; x < 4; x++) comp[x] += n[x];
+    hist[0][orc_bin16(H[c], 8.0)]++;
+    hist[1][orc_bin16(g[c], 16.0)]++;
+  }
+  double mH = 0, mg = 0, vH = 0, vg = 0;
+  for (int c = 0; c < L; c++) { mH += H[c]; mg += g[c]; }
+  mH /= L; mg /= L;
+  for (int c = 0; c < L; c++) { vH += (H[c] - mH) * (H[c] - mH); vg += (g[c] - mg) * (g[c] - mg); }
+  vH /= L; vg /= L;
+  const long long npair_all = (long long)N * (N - 1) / 2;
+  const int M = npair_all < NPAIR ? (int)npair_all : NPAIR;
+  double *id = malloc(sizeof(double) * (M > 0 ? M : 1));
+  for (int k = 0; k < M; k++) {
+    int i, j;
+    if (npair_all <= NPAIR) {
+      int rem = k;
+      i = 0;
+      while (rem >= N - 1 - i) { rem -= N - 1 - i; i++; }
+      j = i + 1 + rem;
+    } else {
+      const uint64_t h = orc_splitmix64(0x5EED1DE7ull + (uint64_t)k);
+      i = (int)((uint32_t)h % (uint32_t)N);
+      j = (int)((uint32_t)(h >> 32) % (uint32_t)(N - 1));
+      if (j >= i) j++;
+    }
+    int both = 0, same = 0;
+    for (int c = 0; c < L; c++) {
+      const int x = ax[(size_t)i * L + c], y = ax[(size_t)j * L + c];
+      if (x < 4 && y < 4) { both++; same += (x == y); }
+    }
+    id[k] = both ? (double)same / (double)both : 0.0;
+  }
+  double mid = 0, vid = 0;
+  for (int k = 0; k < M; k++) mid += id[k];
+  if (M) mid /= M;
+  for (int k = 0; k < M; k++) vid += (id[k] - mid) * (id[k] - mid);
+  if (M) vid /= M;
+  const double rtot = (comp[0] + comp[1]) + (comp[2] + comp[3]);
+  feat[0] = log((double)N);
+  feat[1] = log((double)L);
+  feat[2] = sw2 > 0.0 ? log(sw * sw / sw2) : 0.0;
+  feat[3] = mid;
+  feat[4] = tree_len;
+  for (int q = 0; q < 2; q++)
+    for (int b = 0; b < 16; b++) feat[5 + 16 * q + b] = (double)hist[q][b] / (double)L;
+  feat[37] = sqrt(vid);
+  feat[38] = mH;
+  feat[39] = sqrt(vH);
+  feat[40] = mg;
+  feat[41] = sqrt(vg);
+  feat[42] = wmean > 0.0 ? sqrt(wvar) / wmean : 0.0;
+  for (int x = 0; x < 4; x++) feat[43 + x] = rtot > 0.0 ? comp[x] / rtot : 0.0;
+  for (int k = 47; k < 64; k++) feat[k] = 0.0;   /* null-score summary: filled by the engine */
+  free(H); free(g); free(id);
+}
+
+/* round-to-nearest-even of an FP32 value to BF16, returned as a double */
+static double orc_bf16(float f) {
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  if ((u & 0x7F800000u) == 0x7F800000u) return (double)f;   /* inf/NaN kept */
+  u += 0x7FFFu + ((u >> 16) & 1u);
+  u &= 0xFFFF0000u;
+  float r;
+  memcpy(&r, &u, 4);
+  return (double)r;
+}
+
+enum { MF = 64, MH = 256, MO = 3 };
+#define OW1 0
+#define OB1 (OW1 + MH * MF)
+#define OW2 (OB1 + MH)
+#define OB2 (OW2 + MH * MH)
+#define OW3 (OB2 + MH)
+#define OB3 (OW3 + MH * MH)
+#define OW4 (OB3 + MH)
+#define OB4 (OW4 + MO * MH)
+#define ONP (OB4 + MO)
+
+static double orc_sig(double z) { return 1.0 / (1.0 + exp(-z)); }
+
+/* forward of one standardised row x[64]: pre-activations z[3][256],
+ * activations h[3][256], outputs y[3] (standardised) */
+static void orc_mlp_row(const double *W, const float *params, const double *x, double z[3][MH], double h[3][MH],
+                        double *y) {
+  const int off_w[3] = {OW1, OW2, OW3}, off_b[3] = {OB1, OB2, OB3};
+  const double *in = x;
+  int nin = MF;
+  for (int l = 0; l < 3; l++) {
+    for (int o = 0; o < MH; o++) {
+      double a = 0.0;
+      for (int i = 0; i < nin; i++) a += W[off_w[l] + o * nin + i] * in[i];
+      z[l][o] = a + (double)params[off_b[l] + o];
+      h[l][o] = z[l][o] * orc_sig(z[l][o]);
+    }
+    in = h[l];
+    nin = MH;
+  }
+  for (int o = 0; o < MO; o++) {
+    double a = 0.0;
+    for (int i = 0; i < MH; i++) a += W[OW4 + o * MH + i] * h[2][i];
+    y[o] = a + (double)params[OB4 + o];
+  }
+}
+
+static double *orc_mlp_weights(const float *params) {
+  double *W = malloc(sizeof(double) * ONP);
+  for (int k = 0; k < ONP; k++) W[k] = orc_bf16(params[k]);
+  return W;
+}
+
+void orc_mlp_forward(const float *params, const float *nrm, const float *X, int n, double *Y) {
+  double *W = orc_mlp_weights(params);
+  double x[MF], z[3][MH], h[3][MH], y[MO];
+  for (int r = 0; r < n; r++) {
+    for (int f = 0; f < MF; f++) x[f] = ((double)X[(size_t)r * MF + f] - nrm[f]) / nrm[MF + f];
+    orc_mlp_row(W, params, x, z, h, y);
+    for (int o = 0; o < MO; o++) Y[(size_t)r * MO + o] = y[o] * nrm[2 * MF + MO + o] + nrm[2 * MF + o];
+  }
+  free(W);
+}
+
+double orc_mlp_grad(const float *params, const float *nrm, const float *X, const float *T, int n, double *grad) {
+  double *W = orc_mlp_weights(params);
+  double x[MF], z[3][MH], h[3][MH], y[MO], dy[MO], d[3][MH];
+  double loss = 0.0;
+  const double sc = 2.0 / ((double)n * MO);
+  memset(grad, 0, sizeof(double) * ONP);
+  for (int r = 0; r < n; r++) {
+    for (int f = 0; f < MF; f++) x[f] = ((double)X[(size_t)r * MF + f] - nrm[f]) / nrm[MF + f];
+    orc_mlp_row(W, params, x, z, h, y);
+    for (int o = 0; o < MO; o++) {
+      const double t = ((double)T[(size_t)r * MO + o] - nrm[2 * MF + o]) / nrm[2 * MF + MO + o];
+      loss += (y[o] - t) * (y[o] - t);
+      dy[o] = sc * (y[o] - t);
+    }
+    /* layer 4 */
+    for (int o = 0; o < MO; o++) {
+      for (int i = 0; i < MH; i++) grad[OW4 + o * MH + i] += dy[o] * h[2][i];
+      grad[OB4 + o] += dy[o];
+    }
+    for (int i = 0; i < MH; i++) {
+      double a = 0.0;
+      for (int o = 0; o < MO; o++) a += dy[o] * W[OW4 + o * MH + i];
+      const double s = orc_sig(z[2][i]);
+      d[2][i] = a * s * (1.0 + z[2][i] * (1.0 - s));
+    }
+    /* layers 3, 2, 1 */
+    const int off_w[3] = {OW1, OW2, OW3}, off_b[3] = {OB1, OB2, OB3};
+    for (int l = 2; l >= 0; l--) {
+      const double *in = l ? h[l - 1] : x;
+      const int nin = l ? MH : MF;
+      for (int o = 0; o < MH; o++) {
+        for (int i = 0; i < nin; i++) grad[off_w[l] + o * nin + i] += d[l][o] * in[i];
+        grad[off_b[l] + o] += d[l][o];
+      }
+      if (l == 0) break;
+      for (int i = 0; i < MH; i++) {
+        double a = 0.0;
+        for (int o = 0; o < MH; o++) a += d[l][o] * W[off_w[l] + o * MH + i];
+        const double s = orc_sig(z[l - 1][i]);
+        d[l - 1][i] = a * s * (1.0 + z[l - 1][i] * (1.0 - s));
+      }
+    }
+  }
+  free(W);
+  return loss / ((double)n * MO);
+}

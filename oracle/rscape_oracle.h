@@ -171,6 +171,19 @@ double orc_faithful_rows(const uint8_t *ax, const double *wgt, int N, int L, int
                          int nthreads, double *checksum);
 double orc_faithful_raf(const uint8_t *ax, int N, int L, int npairs, int nthreads, double *checksum);
 
+/* ---- learned null (the library's own definitions; no reference counterpart) ----
+ * feat[64] of ax [N][L] with weights w: the alignment features 0-46 of the
+ * library's covgpu_features, computed here in FP64 in sequence order
+ * (47-63, the null-score summary, are 0). */
+void   orc_features(const uint8_t *ax, int N, int L, const double *w, double tree_len, double *feat);
+/* the 64-256-256-256-3 SiLU network with FP32 master parameters params
+ * (weights rounded to BF16 by round-to-nearest-even, biases as given) and
+ * standardisation nrm = xmean[64] xstd[64] ymean[3] ystd[3], in FP64:
+ * Y[n][3] de-standardised outputs; orc_mlp_grad returns the mean squared
+ * error on standardised targets and its gradient grad[148995] */
+void   orc_mlp_forward(const float *params, const float *nrm, const float *X, int n, double *Y);
+double orc_mlp_grad(const float *params, const float *nrm, const float *X, const float *T, int n, double *grad);
+
 #ifdef __cplusplus
 }
 #endif

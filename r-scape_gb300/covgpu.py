@@ -15,6 +15,7 @@ _LIB = None
 
 u8p = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 COVTYPES = {"CHI": 0, "GT": 3, "MI": 6, "MIr": 9, "MIg": 12, "OMES": 15, "RAF": 18, "RAFS": 21, "CCF": 24}
@@ -97,6 +98,25 @@ def lib():
                                     C.c_double, C.c_double, C.c_uint64, u8p, i32p, i32p, i32p, f64p, f64p, i32p]
         L.covgpu_weights_pb.argtypes = [u8p, C.c_int, C.c_int, f64p]
         L.covgpu_gapfilter.argtypes = [u8p, f64p, C.c_int, C.c_int, C.c_double, i32p]
+        L.covgpu_features.argtypes = [vp, C.c_int, C.c_double, f32p]
+        L.covgpu_mlp_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_uint64]
+        L.covgpu_mlp_destroy.argtypes = [vp]
+        L.covgpu_mlp_errmsg.argtypes = [vp]
+        L.covgpu_mlp_errmsg.restype = C.c_char_p
+        L.covgpu_mlp_set_params.argtypes = [vp, f32p]
+        L.covgpu_mlp_get_params.argtypes = [vp, f32p]
+        L.covgpu_mlp_set_norm.argtypes = [vp, f32p, f32p, f32p, f32p, vp, vp]
+        L.covgpu_mlp_get_norm.argtypes = [vp, f32p, f32p, f32p, f32p, f32p, f32p]
+        L.covgpu_mlp_in_range.argtypes = [vp, f32p]
+        L.covgpu_mlp_forward.argtypes = [vp, f32p, C.c_int, f32p]
+        L.covgpu_mlp_grad.argtypes = [vp, f32p, f32p, C.c_int, f32p, C.POINTER(C.c_float)]
+        L.covgpu_mlp_train.argtypes = [vp, f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint64,
+                                       f32p]
+        L.covgpu_helices.argtypes = [i32p, C.c_int, C.c_int, C.POINTER(C.c_int), i32p, i32p, i32p]
+        L.covgpu_aggregate.argtypes = [vp, C.c_int, C.c_int, i32p, f64p, vp, f64p, f64p]
+        L.covgpu_learned_features.argtypes = [vp, C.POINTER(Params), C.c_double, C.c_int, C.c_int, f32p]
+        L.covgpu_rscape_learned.argtypes = [vp, C.POINTER(Params), vp, vp, vp, C.c_double, C.c_int, C.c_int,
+                                            C.POINTER(Result), C.POINTER(Hit), C.c_int, C.POINTER(C.c_int)]
         _LIB = L
     return _LIB
 
@@ -160,6 +180,24 @@ def gapfilter(ax, wgt=None, gapthresh=0.75):
     use = np.zeros(L, dtype=np.int32)
     lib().covgpu_gapfilter(ax, w, N, L, gapthresh, use)
     return use.astype(bool)
+
+
+AGG_FISHER, AGG_LANCASTER, AGG_WFISHER, AGG_SIDAK = 0, 1, 2, 3
+
+
+def helices(ct, helix_unpaired=2):
+    """R-scape's helices of a nested structure ct (0-based partner or -1):
+    list of [(i, j), ...] per helix, each in increasing i."""
+    ct = np.ascontiguousarray(ct, dtype=np.int32)
+    L = len(ct)
+    off = np.zeros(L // 2 + 2, dtype=np.int32)
+    bi = np.zeros(L // 2 + 1, dtype=np.int32)
+    bj = np.zeros(L // 2 + 1, dtype=np.int32)
+    nh = C.c_int(0)
+    st = lib().covgpu_helices(ct, L, helix_unpaired, C.byref(nh), off, bi, bj)
+    if st:
+        raise ValueError("covgpu_helices: status %d" % st)
+    return [[(int(bi[k]), int(bj[k])) for k in range(off[h], off[h + 1])] for h in range(nh.value)]
 
 
 class Engine:
@@ -318,6 +356,49 @@ class Engine:
             out.append(r)
         return out
 
+    def features(self, slot=0, tree_len=0.0):
+        """Features 0-46 of the learned null for the alignment in slot (float32[64], 47-63 zero)."""
+        f = np.zeros(64, dtype=np.float32)
+        self._ck(lib().covgpu_features(self.h, slot, float(tree_len), f))
+        return f
+
+    def learned_features(self, tree_len, nquick=4, covtype="GTp", **kw):
+        """All 64 learned-null features of slot 0 (with nquick simulated nulls)."""
+        p = params(**kw)
+        f = np.zeros(64, dtype=np.float32)
+        self._ck(lib().covgpu_learned_features(self.h, C.byref(p), float(tree_len), covtype_code(covtype), nquick, f))
+        return f
+
+    def rscape_learned(self, ax, wgt, net, tree_len, covtype="GTp", nquick=4, hitcap=1 << 16, **kw):
+        """covgpu_rscape with the learned null; returns (result dict, used_net)."""
+        p = params(**kw)
+        res = Result()
+        hits = (Hit * hitcap)()
+        used = C.c_int(0)
+        axc = None if ax is None else np.ascontiguousarray(ax, dtype=np.uint8)
+        wc = None if wgt is None else np.ascontiguousarray(wgt, dtype=np.float64)
+        self._ck(lib().covgpu_rscape_learned(self.h, C.byref(p), axc.ctypes.data if axc is not None else None,
+                                             wc.ctypes.data if wc is not None else None, net.h, float(tree_len),
+                                             covtype_code(covtype), nquick, C.byref(res), hits, hitcap,
+                                             C.byref(used)))
+        r = {f[0]: getattr(res, f[0]) for f in Result._fields_}
+        n = min(r["nhit"], hitcap)
+        r["hits"] = [(hits[k].i, hits[k].j, hits[k].sc, hits[k].E, hits[k].pval) for k in range(n)]
+        return r, bool(used.value)
+
+    def aggregate(self, method, helix_pvals, aux=None):
+        """Aggregated p-values and E-values of helices given as lists of pair p-values."""
+        off = np.zeros(len(helix_pvals) + 1, dtype=np.int32)
+        off[1:] = np.cumsum([len(h) for h in helix_pvals])
+        pv = np.ascontiguousarray(np.concatenate([np.asarray(h, float) for h in helix_pvals])
+                                  if helix_pvals else np.zeros(0), dtype=np.float64)
+        ax = None if aux is None else np.ascontiguousarray(np.concatenate([np.asarray(a, float) for a in aux]))
+        pagg = np.zeros(len(helix_pvals))
+        Eagg = np.zeros(len(helix_pvals))
+        self._ck(lib().covgpu_aggregate(self.h, method, len(helix_pvals), off, pv,
+                                        ax.ctypes.data if ax is not None else None, pagg, Eagg))
+        return pagg, Eagg
+
     def flush_l2(self):
         self._ck(lib().covgpu_flush_l2(self.h))
 
@@ -326,3 +407,84 @@ class Engine:
         n = C.c_int()
         lib().covgpu_last_timing(self.h, ms, C.byref(n))
         return ms, n.value
+
+
+NPARAM = 148995
+
+
+class MLP:
+    """The learned-null network on one device (include/covgpu.h, covgpu_mlp_*)."""
+
+    def __init__(self, batch_cap=512, seed=1, device=0):
+        self.h = C.c_void_p()
+        st = lib().covgpu_mlp_create(C.byref(self.h), device, batch_cap, seed)
+        if st:
+            msg = lib().covgpu_mlp_errmsg(self.h) if self.h else b""
+            lib().covgpu_mlp_destroy(self.h)
+            self.h = None
+            raise RuntimeError("covgpu_mlp_create failed (%d): %s" % (st, msg.decode() if msg else ""))
+
+    def close(self):
+        if self.h:
+            lib().covgpu_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st):
+        if st:
+            raise RuntimeError("covgpu_mlp error %d: %s" % (st, lib().covgpu_mlp_errmsg(self.h).decode()))
+
+    def params(self):
+        p = np.zeros(NPARAM, dtype=np.float32)
+        self._ck(lib().covgpu_mlp_get_params(self.h, p))
+        return p
+
+    def set_params(self, p):
+        self._ck(lib().covgpu_mlp_set_params(self.h, np.ascontiguousarray(p, dtype=np.float32)))
+
+    def set_norm(self, xmean, xstd, ymean, ystd, xlo=None, xhi=None):
+        f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+        lo, hi = f(xlo), f(xhi)
+        self._keep = (lo, hi)
+        self._ck(lib().covgpu_mlp_set_norm(self.h, f(xmean), f(xstd), f(ymean), f(ystd),
+                                           lo.ctypes.data if lo is not None else None,
+                                           hi.ctypes.data if hi is not None else None))
+
+    def norm(self):
+        out = [np.zeros(64, np.float32), np.zeros(64, np.float32), np.zeros(3, np.float32), np.zeros(3, np.float32),
+               np.zeros(64, np.float32), np.zeros(64, np.float32)]
+        self._ck(lib().covgpu_mlp_get_norm(self.h, *out))
+        return out
+
+    def norm_vector(self):
+        xm, xs, ym, ys, _, _ = self.norm()
+        return np.concatenate([xm, xs, ym, ys]).astype(np.float32)
+
+    def in_range(self, feat):
+        return bool(lib().covgpu_mlp_in_range(self.h, np.ascontiguousarray(feat, dtype=np.float32)))
+
+    def forward(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, 64)
+        Y = np.zeros((X.shape[0], 3), dtype=np.float32)
+        self._ck(lib().covgpu_mlp_forward(self.h, X, X.shape[0], Y))
+        return Y
+
+    def grad(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, 64)
+        T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1, 3)
+        g = np.zeros(NPARAM, dtype=np.float32)
+        loss = C.c_float(0)
+        self._ck(lib().covgpu_mlp_grad(self.h, X, T, X.shape[0], g, C.byref(loss)))
+        return loss.value, g
+
+    def train(self, X, T, epochs, batch=256, lr=1e-3, wd=1e-4, seed=1):
+        X = np.ascontiguousarray(X, dtype=np.float32).reshape(-1, 64)
+        T = np.ascontiguousarray(T, dtype=np.float32).reshape(-1, 3)
+        hist = np.zeros(epochs, dtype=np.float32)
+        self._ck(lib().covgpu_mlp_train(self.h, X, T, X.shape[0], epochs, batch, lr, wd, seed, hist))
+        return hist

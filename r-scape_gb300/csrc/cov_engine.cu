@@ -15,6 +15,7 @@
 #include "cov_dev.cuh"
 #include "cov_kernels.h"
 #include "cov_fit.h"
+#include "cov_learn.h"
 #include "cov_prep.h"
 #include "cov_sim.h"
 #include "cov_subst.h"
@@ -76,6 +77,12 @@ struct covgpu_ctx {
   std::vector<double> sim_key;   // times and model of the tables on the device
   // substitutions of the last covgpu_substitutions
   int *d_nsubs = nullptr, *d_ndouble = nullptr, *d_njoin = nullptr;
+  // learned-null features
+  double* d_featscr = nullptr;
+  float* d_feat = nullptr;
+  bool want_qsum = false;     // covgpu_rscape keeps the null-score summary of type 0
+  double qsum[17] = {0};
+  bool have_qsum = false;
   unsigned char* d_flush = nullptr;
   bool counted = false;
   cudaEvent_t ev[6] = {};
@@ -181,7 +188,8 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
   if (ctx->umma) umma_plan_destroy(ctx->umma);
   if (ctx->fitw) fitwork_destroy(ctx->fitw);
   void* sims[] = {ctx->d_simQ, ctx->d_simT, ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16, ctx->d_R, ctx->d_units,
-                  ctx->d_simroot, ctx->d_simstate, ctx->d_nsubs, ctx->d_ndouble, ctx->d_njoin};
+                  ctx->d_simroot, ctx->d_simstate, ctx->d_nsubs, ctx->d_ndouble, ctx->d_njoin, ctx->d_featscr,
+                  ctx->d_feat};
   for (void* p : sims) if (p) cudaFree(p);
   for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -763,6 +771,50 @@ static int bins_for(double bmin, double bmax, double w) {
   return nb < 1 ? 1 : nb;
 }
 
+// Summary of a null histogram (features 47-63 of the learned null): log of
+// the number of scores, their mean and deviation (bin midpoints), the upper
+// quantiles at survival 0.5 ... 0.0005 (linear within a bin), the tail fit
+// (mu, log mean excess, log shape; from the quantiles when the fit failed)
+// and the largest null score.
+static void null_summary(const ESL_HISTOGRAM* h, double xmax, double mu, double lambda, double tau, double* out) {
+  static const double lev[10] = {0.5, 0.3, 0.1, 0.05, 0.03, 0.01, 0.005, 0.003, 0.001, 0.0005};
+  double tot = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int b = 0; b < h->nb; b++) {
+    const double c = (double)h->obs[b];
+    tot += c;
+    s1 += c * (h->bmin + (b + 0.5) * h->w);
+  }
+  const double mean = tot > 0.0 ? s1 / tot : 0.0;
+  for (int b = 0; b < h->nb; b++) {
+    const double d = h->bmin + (b + 0.5) * h->w - mean;
+    s2 += (double)h->obs[b] * d * d;
+  }
+  out[0] = tot > 0.0 ? log(tot) : 0.0;
+  out[1] = mean;
+  out[2] = tot > 0.0 ? sqrt(s2 / tot) : 0.0;
+  for (int k = 0; k < 10; k++) {
+    const double target = lev[k] * tot;
+    double above = 0.0, qv = h->bmin;
+    for (int b = h->nb - 1; b >= 0; b--) {
+      const double c = (double)h->obs[b];
+      if (c > 0.0 && above + c >= target) {
+        qv = h->bmin + (b + 1) * h->w - (target - above) / c * h->w;
+        break;
+      }
+      above += c;
+    }
+    out[3 + k] = qv;
+  }
+  if (std::isfinite(mu) && lambda > 0.0 && std::isfinite(lambda) && tau > 0.0 && std::isfinite(tau)) {
+    out[13] = mu; out[14] = log(tau / lambda); out[15] = log(tau);
+  } else {
+    out[13] = out[12];
+    out[14] = log(std::max(h->w, (out[12] - out[9]) / log(10.0)));
+    out[15] = 0.0;
+  }
+  out[16] = xmax;
+}
+
 extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint8_t* ax, const double* wgt,
                              int ntypes, const int* covtypes, covgpu_result* results, covgpu_hit* hits, int hitcap) {
   CK(cudaSetDevice(ctx->dev));
@@ -958,6 +1010,10 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
         return (a.i != b.i) ? a.i < b.i : a.j < b.j;
       });
     }
+    if (q == 0 && ctx->want_qsum) {
+      null_summary(h, xmax, mu, lambda, tau, ctx->qsum);
+      ctx->have_qsum = true;
+    }
     covh_Destroy(h);
   }
   CK(cudaEventRecord(ctx->ev[3], ctx->st));
@@ -967,6 +1023,187 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   ctx->tms[2] = elapsed(ctx->ev[1], ctx->ev[2]);
   ctx->tms[3] = elapsed(ctx->ev[2], ctx->ev[3]);
   ctx->tms[4] = elapsed(ctx->ev[0], ctx->ev[3]);
+  return 0;
+}
+
+// ------------------------------------------------------------------------
+// learned null
+// ------------------------------------------------------------------------
+extern "C" int covgpu_features(covgpu_ctx* ctx, int slot, double tree_len, float* feat) {
+  CK(cudaSetDevice(ctx->dev));
+  if (slot < 0 || slot >= ctx->maxslots || !feat) return fail(ctx, 11, "bad slot or output");
+  if (!ctx->have_w) return fail(ctx, 11, "weights not set");
+  if (!std::isfinite(tree_len)) return fail(ctx, 11, "tree length is not finite");
+  if (!ctx->d_featscr) {
+    CK(dalloc(&ctx->d_featscr, feat_scratch_doubles(ctx->L)));
+    CK(dalloc(&ctx->d_feat, kNFeat));
+  }
+  CK(launch_features(ctx->d_ax + (size_t)slot * ctx->N * ctx->Lp, ctx->N, ctx->L, ctx->Lp, ctx->d_wd, tree_len,
+                     ctx->d_featscr, ctx->d_feat, ctx->st));
+  ctx->nlaunch += 4;
+  CK(cudaMemcpyAsync(feat, ctx->d_feat, kNFeat * sizeof(float), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return 0;
+}
+
+static int learned_features(covgpu_ctx* ctx, const covgpu_params* p, double tree_len, int covtype, int nquick,
+                            float* feat, covgpu_result* quick) {
+  int s;
+  if (nquick < 1) return fail(ctx, 11, "the learned null needs at least one quick null");
+  if ((s = covgpu_features(ctx, 0, tree_len, feat))) return s;
+  covgpu_params pq = *p;
+  pq.nshuffle = nquick;
+  ctx->want_qsum = true;
+  ctx->have_qsum = false;
+  s = covgpu_rscape(ctx, &pq, nullptr, nullptr, 1, &covtype, quick, nullptr, 0);
+  ctx->want_qsum = false;
+  if (s) return s;
+  for (int k = 0; k < 17; k++) feat[47 + k] = ctx->have_qsum ? (float)ctx->qsum[k] : NAN;
+  return 0;
+}
+
+extern "C" int covgpu_learned_features(covgpu_ctx* ctx, const covgpu_params* p, double tree_len, int covtype,
+                                       int nquick, float* feat) {
+  CK(cudaSetDevice(ctx->dev));
+  covgpu_result quick;
+  return learned_features(ctx, p, tree_len, covtype, nquick, feat, &quick);
+}
+
+extern "C" int covgpu_rscape_learned(covgpu_ctx* ctx, const covgpu_params* p, const uint8_t* ax, const double* wgt,
+                                     covgpu_mlp* net, double tree_len, int covtype, int nquick,
+                                     covgpu_result* result, covgpu_hit* hits, int hitcap, int* used_net) {
+  CK(cudaSetDevice(ctx->dev));
+  const int L = ctx->L;
+  const int64_t P = (int64_t)L * (L - 1) / 2;
+  if (!net) return fail(ctx, 11, "no network");
+  *used_net = 0;
+  int s;
+  if (wgt && (s = covgpu_set_weights(ctx, wgt))) return s;
+  if (ax && (s = covgpu_set_alignment(ctx, 0, ax))) return s;
+  float feat[kNFeat], out[COVGPU_NOUT];
+  covgpu_result quick;
+  memset(&quick, 0, sizeof(quick));
+  if (ctx->N < 2 || L < 2 || (s = learned_features(ctx, p, tree_len, covtype, nquick, feat, &quick)) ||
+      quick.status != 0 || !covgpu_mlp_in_range(net, feat))
+    return covgpu_rscape(ctx, p, nullptr, nullptr, 1, &covtype, result, hits, hitcap);
+  if (covgpu_mlp_forward(net, feat, 1, out)) return fail(ctx, 25, "network: %s", covgpu_mlp_errmsg(net));
+  // the outputs correct the quick nulls' tail (features 60-62: mu, log mean
+  // excess, log shape): mu + out0 * excess, log excess + out1, log shape + out2
+  const double mq = std::exp((double)feat[61]);
+  const double mu = (double)feat[60] + (double)out[0] * mq;
+  const double tau = std::exp((double)feat[62] + (double)out[2]);
+  const double lambda = tau / std::exp((double)feat[61] + (double)out[1]);
+  if (!std::isfinite(mu) || !(tau > 0.0) || !std::isfinite(tau) || !(lambda > 0.0) || !std::isfinite(lambda))
+    return covgpu_rscape(ctx, p, nullptr, nullptr, 1, &covtype, result, hits, hitcap);
+  *used_net = 1;
+  // the quick run scored the alignment (slot 0, type 0) and fixed the width
+  // from its first null, as the full run would
+  covgpu_result& R = *result;
+  R = quick;
+  R.nhit = 0;
+  R.mu = mu; R.lambda = lambda; R.tau = tau; R.pmass = p->pmass; R.newmass = p->pmass;
+  R.Nt = (uint64_t)P;
+  const double w = R.w;
+  CK(cudaEventRecord(ctx->ev[2], ctx->st));
+  double bmax = R.maxCOV + 5 * w;
+  while (fabs(bmax - p->bmin) < p->tol) bmax += w;
+  const int nb = bins_for(p->bmin, bmax, w);
+  if (ctx->sfcap < 2 * nb) {
+    if (ctx->d_sf) cudaFree(ctx->d_sf);
+    if (ctx->d_tail) cudaFree(ctx->d_tail);
+    CK(dalloc(&ctx->d_sf, 2 * nb));
+    CK(dalloc(&ctx->d_tail, 2 * nb));
+    ctx->sfcap = 2 * nb;
+  }
+  // survival at every bin's upper bound, mass pmass above mu
+  CK(launch_survfit(0, nb, p->bmin, w, p->pmass, 0, mu, lambda, tau, ctx->d_sf, ctx->st));
+  if (hitcap > 0 && ctx->hitcap < hitcap) {
+    cudaFree(ctx->d_hi); cudaFree(ctx->d_hj); cudaFree(ctx->d_hsc); cudaFree(ctx->d_hE); cudaFree(ctx->d_hp);
+    CK(dalloc(&ctx->d_hi, hitcap)); CK(dalloc(&ctx->d_hj, hitcap));
+    CK(dalloc(&ctx->d_hsc, hitcap)); CK(dalloc(&ctx->d_hE, hitcap)); CK(dalloc(&ctx->d_hp, hitcap));
+    ctx->hitcap = hitcap;
+  }
+  EvalTables T;
+  T.sf = ctx->d_sf;
+  T.tail = ctx->d_tail;   // not read: every score takes the fitted branch
+  T.bmin = p->bmin; T.w = w; T.phi = -INFINITY; T.xmax = INFINITY; T.Nc = 1.0; T.Nt = (double)P;
+  T.thresh = p->thresh; T.nb = nb; T.imin = 0; T.imax = nb - 1;
+  CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
+  CK(launch_evalue(ctx->d_cov, ctx->d_tiles, ctx->ntiles, L, T, nullptr, ctx->d_nhits, ctx->hitcap, ctx->d_hi,
+                   ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->st));
+  ctx->nlaunch += 2;
+  std::vector<double> sf(2 * (size_t)nb);
+  int nh = 0;
+  CK(cudaMemcpyAsync(sf.data(), ctx->d_sf, sf.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaMemcpyAsync(&nh, ctx->d_nhits, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  // score at the threshold: the lower bound of the first bin whose E-value
+  // falls below it
+  R.sc_thresh = INFINITY;
+  for (int b = 0; b < 2 * nb; b++)
+    if (sf[b] * (double)P < p->thresh) { R.sc_thresh = p->bmin + b * w; break; }
+  R.nhit = nh;
+  const int nget = std::min(nh, hitcap);
+  if (nget > 0 && hits) {
+    std::vector<int> hi(nget), hj(nget);
+    std::vector<double> hs(nget), hE(nget), hp(nget);
+    CK(cudaMemcpyAsync(hi.data(), ctx->d_hi, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hj.data(), ctx->d_hj, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hs.data(), ctx->d_hsc, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hE.data(), ctx->d_hE, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hp.data(), ctx->d_hp, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int k = 0; k < nget; k++) hits[k] = covgpu_hit{hi[k], hj[k], hs[k], hE[k], hp[k]};
+    std::sort(hits, hits + nget, [](const covgpu_hit& a, const covgpu_hit& b) {
+      return (a.i != b.i) ? a.i < b.i : a.j < b.j;
+    });
+  }
+  CK(cudaEventRecord(ctx->ev[3], ctx->st));
+  CK(cudaEventSynchronize(ctx->ev[3]));
+  ctx->tms[3] += elapsed(ctx->ev[2], ctx->ev[3]);
+  ctx->tms[4] += elapsed(ctx->ev[2], ctx->ev[3]);
+  return 0;
+}
+
+// ------------------------------------------------------------------------
+// helix aggregation (agg_CalculatePvalues, src/aggregate.c:41-128)
+// ------------------------------------------------------------------------
+extern "C" int covgpu_aggregate(covgpu_ctx* ctx, int method, int nh, const int* helix_off, const double* pval,
+                                const double* aux, double* pagg, double* Eagg) {
+  CK(cudaSetDevice(ctx->dev));
+  if (method < COVGPU_AGG_FISHER || method > COVGPU_AGG_SIDAK) return fail(ctx, 11, "unknown aggregation method");
+  if (nh < 0 || (nh > 0 && (!helix_off || !pval || !pagg))) return fail(ctx, 11, "bad helix arguments");
+  if (nh == 0) return 0;
+  if (helix_off[0] != 0) return fail(ctx, 11, "helix offsets must start at 0");
+  for (int h = 0; h < nh; h++)
+    if (helix_off[h + 1] < helix_off[h]) return fail(ctx, 11, "helix offsets decrease at %d", h);
+  const int nbp = helix_off[nh];
+  const bool need_aux = (method == COVGPU_AGG_LANCASTER || method == COVGPU_AGG_WFISHER);
+  if (need_aux && !aux) return fail(ctx, 11, "this method needs per-pair weights");
+  for (int k = 0; k < nbp; k++) {
+    if (!(pval[k] >= 0.0 && pval[k] <= 1.0)) return fail(ctx, 11, "p-value %d outside [0, 1]", k);
+    if (need_aux && !(aux[k] >= 0.0 && std::isfinite(aux[k]))) return fail(ctx, 11, "weight %d is negative", k);
+  }
+  const size_t nd = (size_t)nbp * 4 + nh + 1;   // pval, aux, term[2], pagg
+  double* d = nullptr;
+  int* d_off = nullptr;
+  CK(dalloc(&d, nd));
+  cudaError_t e = dalloc(&d_off, (size_t)nh + 1);
+  double *d_pval = d, *d_aux = d + nbp, *d_term = d + 2 * (size_t)nbp, *d_pagg = d + 4 * (size_t)nbp;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_off, helix_off, ((size_t)nh + 1) * sizeof(int), cudaMemcpyHostToDevice, ctx->st);
+  if (e == cudaSuccess && nbp)
+    e = cudaMemcpyAsync(d_pval, pval, (size_t)nbp * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
+  if (e == cudaSuccess && need_aux && nbp)
+    e = cudaMemcpyAsync(d_aux, aux, (size_t)nbp * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
+  if (e == cudaSuccess) e = launch_aggregate(method, nh, d_off, d_pval, d_aux, d_term, d_pagg, ctx->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(pagg, d_pagg, (size_t)nh * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+  cudaFree(d);
+  if (d_off) cudaFree(d_off);
+  if (e != cudaSuccess) return fail(ctx, 90, "CUDA error %s", cudaGetErrorString(e));
+  // E-value: times the number of helices tested (rm->Eval, src/aggregate.c:114)
+  if (Eagg)
+    for (int h = 0; h < nh; h++) Eagg[h] = (pagg[h] < 0.0) ? -1.0 : (double)nh * pagg[h];
   return 0;
 }
 

@@ -484,4 +484,72 @@ int gamma_fit_gpu(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, doubl
   return 0;
 }
 
+
+
+// ------------------------------------------------------------------------
+// helix aggregation of pair p-values (agg_FISHER, agg_LANCASTER,
+// agg_WFISHER, agg_SIDAK of src/aggregate.c:141-322): one warp per helix
+// ------------------------------------------------------------------------
+// y >= 0 with Q(a, y) = p, by doubling then bisection on the upper tail (the
+// chi-square quantile of the complement of p, formed without 1 - p)
+__device__ double gamma_q_inv(double a, double p) {
+  if (!(p > 0.0)) return INFINITY;
+  if (p >= 1.0) return 0.0;
+  const double lga = lgamma(a);
+  double lo = 0.0, hi = fmax(1.0, a);
+  for (int k = 0; k < 1000 && gamma_q_dev(a, hi, lga) > p; k++) { lo = hi; hi *= 2.0; }
+  for (int k = 0; k < 200 && hi - lo > 1e-15 * hi; k++) {
+    const double mid = 0.5 * (lo + hi);
+    if (gamma_q_dev(a, mid, lga) > p) lo = mid; else hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+__global__ void k_aggregate(int method, int nh, const int* __restrict__ off, const double* __restrict__ pval,
+                            const double* __restrict__ aux, double* __restrict__ term, double* __restrict__ pagg) {
+  const int h = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (h >= nh) return;
+  const int a = off[h], n = off[h + 1] - a;
+  if (n <= 0) { if (lane == 0) pagg[h] = -1.0; return; }
+  if (n == 1) { if (lane == 0) pagg[h] = pval[a]; return; }
+  if (method == 1 || method == 2) {
+    // weights: Lancaster 1 + substitutions; weighted Fisher (0.01 + power)
+    // scaled to sum 2n (extract_rm_weights_*, src/aggregate.c:375-482)
+    double wsum = 0.0;
+    if (method == 2)
+      for (int k = 0; k < n; k++) wsum += 0.01 + aux[a + k];
+    const double f = (method == 2 && wsum > 0.0) ? 2.0 * n / wsum : 1.0;
+    for (int k = lane; k < n; k += 32) {
+      const double w = (method == 1) ? 1.0 + aux[a + k] : (0.01 + aux[a + k]) * f;
+      term[2 * (a + k)] = w;
+      term[2 * (a + k) + 1] = 2.0 * gamma_q_inv(0.5 * w, pval[a + k]);   // chi-square(w) quantile at 1 - p
+    }
+  }
+  __syncwarp();
+  if (lane != 0) return;
+  double r;
+  if (method == 0) {           // Fisher: chi-square with 2n degrees of freedom
+    double chi = 0.0;
+    for (int k = 0; k < n; k++) chi += -2.0 * log(pval[a + k]);
+    r = isnan(chi) ? NAN : gamma_q_dev((double)n, 0.5 * chi, lgamma((double)n));
+  } else if (method == 3) {    // Sidak
+    double pmin = pval[a];
+    for (int k = 1; k < n; k++) pmin = fmin(pmin, pval[a + k]);
+    r = 1.0 - exp((double)n * log(1.0 - pmin));
+  } else {                     // Lancaster / weighted Fisher
+    double df = 0.0, chi = 0.0;
+    for (int k = 0; k < n; k++) df += term[2 * (a + k)];
+    for (int k = 0; k < n; k++) chi += term[2 * (a + k) + 1];
+    r = isnan(chi) ? NAN : gamma_q_dev(0.5 * df, 0.5 * chi, lgamma(0.5 * df));
+  }
+  pagg[h] = r;
+}
+
+cudaError_t launch_aggregate(int method, int nh, const int* d_off, const double* d_pval, const double* d_aux,
+                             double* d_term, double* d_pagg, cudaStream_t st) {
+  if (nh <= 0) return cudaSuccess;
+  k_aggregate<<<(nh + 7) / 8, 256, 0, st>>>(method, nh, d_off, d_pval, d_aux, d_term, d_pagg);
+  return cudaGetLastError();
+}
+
 }  // namespace covgpu

@@ -19,4 +19,10 @@ int gamma_fit_gpu(FitWork* fw, const uint64_t* h_obs, int cmin, int imax, double
 cudaError_t launch_survfit(int cmin, int nb, double bmin, double w, double mass, int doexp, double mu, double lambda,
                            double tau, double* d_sf, cudaStream_t st);
 
+// aggregated p-value of each helix (pairs d_off[h] .. d_off[h+1]-1 of
+// d_pval): method 0 Fisher, 1 Lancaster (d_aux: substitutions per pair),
+// 2 weighted Fisher (d_aux: power per pair), 3 Sidak; d_term scratch [2 nbp]
+cudaError_t launch_aggregate(int method, int nh, const int* d_off, const double* d_pval, const double* d_aux,
+                             double* d_term, double* d_pagg, cudaStream_t st);
+
 }  // namespace covgpu

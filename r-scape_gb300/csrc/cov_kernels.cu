@@ -862,7 +862,7 @@ k_evalue(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int n
       const int icov = bin_df(xv, B);
       double pv;
       if (T.sf && icov >= 2 * T.nb - 1)      pv = T.sf[2 * T.nb - 1];
-      else if (T.sf && x >= T.phi)           pv = T.sf[icov + 1];
+      else if (T.sf && x >= T.phi)           pv = T.sf[max(icov + 1, 0)];
       else if (x >= T.xmax)                  pv = 1.0 / T.Nc;
       else if (icov <= T.imax) {
         const int ic = (icov < T.imin) ? T.imin : icov;
