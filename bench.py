@@ -155,6 +155,63 @@ def simulator_rate(cg, e, s, N, L, nrep):
             "note": "host-timed covgpu_simulate calls (P tables, evolution, synchronise)"}
 
 
+def load_learned_null():
+    import __graft_entry__ as g
+    return g._load("learned_null", os.path.join(ROOT, "r-scape_gb300", "learned_null.py"))
+
+
+def ragged_families(cg, nfam, counter, device):
+    """E-valued MSAs/s over a stream of families drawn as the ragged-family
+    workload draws them (N ~ U[20,2000], L ~ logU[50,1500], tree length
+    ~ U[0.5,3], base-pair fraction ~ U[0.1,0.35]; seeds 1..nfam): one context
+    made for the largest size and resized per family; per family the
+    alignment and tree go in, R-scape's weights (GSC up to 1000 sequences,
+    else position-based) and its null count rule run on the device, GTp with
+    APC, and the hit list comes out.  Families are synthesised before the
+    timed region."""
+    ln = load_learned_null()
+    fams = [ln.draw_family(k) for k in range(1, nfam + 1)]
+    data = [ln.make_family(f) for f in fams]
+    e = cg.Engine(2000, 1500, maxslots=21, maxnull=20, device=device)
+    pairs = 0
+    t0 = time.perf_counter()
+    for f, (s, _) in zip(fams, data):
+        e.resize(f["N"], f["L"])
+        e.set_alignment(0, s.ax)
+        if f["N"] <= 1000:
+            e.weights_gsc(0, set=True)
+        else:
+            e.weights_pb(0, set=True)
+        e.set_tree(s.parent, s.left, s.right)
+        r = e.rscape(None, None, ["GTp"], counter=counter)[0]
+        pairs += (r["nshuffle"] + 1) * f["L"] * (f["L"] - 1) // 2
+    dt = time.perf_counter() - t0    # every call returns after its hit list reached the host
+    e.close()
+    return {"families": nfam, "seconds": dt, "msas_per_s": nfam / dt, "column_pairs_per_s": pairs / dt,
+            "statistic": "GTp", "nulls": "R-scape rule (20 here)", "timing": "host wall clock, host buffers in/out"}
+
+
+def batched_nulls(cg, counter, device, steps=3):
+    """One N=500 x L=400 alignment (tree length 1.5, 100 base pairs) with 200
+    null alignments on its tree, all scored in one batch (GTp with APC)."""
+    s = cg.Synth(500, 400, 1.5, 100, 10, 6, 14, 0.08, seed=7)
+    w = cg.weights_pb(s.ax)
+    e = cg.Engine(500, 400, maxslots=201, maxnull=200, device=device)
+    e.set_tree(s.parent, s.left, s.right)
+    e.set_weights(w)
+    e.set_alignment(0, s.ax)
+    e.rscape(None, None, ["GTp"], nshuffle=200, counter=counter)
+    ms = []
+    for _ in range(steps):
+        e.flush_l2()
+        e.rscape(None, None, ["GTp"], nshuffle=200, counter=counter)
+        ms.append(e.last_timing()[0][4])
+    e.close()
+    t = statistics.median(ms)
+    return {"N": 500, "L": 400, "nulls": 200, "ms_per_msa": t, "msas_per_s": 1000.0 / t,
+            "column_pairs_per_s": 201 * 400 * 399 / 2 / (t / 1000.0), "timing": "CUDA events, device-resident"}
+
+
 def cpu_reference(ax, w, budget_s, threads):
     """pairs/s of the reference loops on the host: counting + statistic per
     pair (x3: GTp, MIp, CHIp are three runs) and RAF's O(N^2) loop."""
@@ -206,6 +263,8 @@ def main():
     ap.add_argument("--L", type=int, default=None, help="override L (profiling a smaller case)")
     ap.add_argument("--nshuffle", type=int, default=None, help="override the number of nulls")
     ap.add_argument("--types", default=None, help="comma-separated statistics (default GTp,MIp,CHIp,RAFp)")
+    ap.add_argument("--families", type=int, default=200,
+                    help="families of the ragged-family stream timed after the main workload (0: skip)")
     args = ap.parse_args()
     if args.N:
         CFG["N"] = args.N
@@ -318,6 +377,8 @@ def main():
     traffic = profile_traffic(kname)
     cpu_v, cpu_sample, _ = cpu_reference(ax, w, args.cpu_budget, threads)
     sim = simulator_rate(cg, e, s, N, L, ns)
+    fam = ragged_families(cg, args.families, counter, local) if (args.families > 0 and rank == 0) else None
+    bnull = batched_nulls(cg, counter, local) if rank == 0 else None
     out = {
         "metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * step_s, "higher_is_better": True, "scaling": "weak",
@@ -336,6 +397,8 @@ def main():
                          "sample": cpu_sample},
         "hits": [len(x["hits"]) for x in res],
         "simulator": sim,
+        "ragged_families": fam,
+        "batched_nulls": bnull,
         "clocks": clk.summary(),
     }
     print(json.dumps(out))

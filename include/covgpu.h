@@ -75,6 +75,10 @@ const char *covgpu_errmsg(const covgpu_ctx *ctx);
 
 int  covgpu_create(covgpu_ctx **ret, int device, int N, int L, int maxslots, int maxnull);
 void covgpu_destroy(covgpu_ctx *ctx);
+/* switch the context to alignments of N x L, N and L at most those it was
+ * created for, without allocating: for streams of families of different
+ * sizes.  Alignment, weights and tree must be set again afterwards. */
+int  covgpu_resize(covgpu_ctx *ctx, int N, int L);
 
 /* inputs: codes are Easel RNA digital codes, row-major [N][L] */
 int  covgpu_set_weights(covgpu_ctx *ctx, const double *wgt);

@@ -112,6 +112,7 @@ def lib():
         L.covgpu_mlp_grad.argtypes = [vp, f32p, f32p, C.c_int, f32p, C.POINTER(C.c_float)]
         L.covgpu_mlp_train.argtypes = [vp, f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint64,
                                        f32p]
+        L.covgpu_resize.argtypes = [vp, C.c_int, C.c_int]
         L.covgpu_helices.argtypes = [i32p, C.c_int, C.c_int, C.POINTER(C.c_int), i32p, i32p, i32p]
         L.covgpu_aggregate.argtypes = [vp, C.c_int, C.c_int, i32p, f64p, vp, f64p, f64p]
         L.covgpu_learned_features.argtypes = [vp, C.POINTER(Params), C.c_double, C.c_int, C.c_int, f32p]
@@ -211,6 +212,11 @@ class Engine:
             msg = lib().covgpu_errmsg(self.h).decode() if self.h else ""
             self.close()
             raise RuntimeError("covgpu_create failed (%d): %s" % (st, msg))
+
+    def resize(self, N, L):
+        """Work on alignments of N x L (within the dimensions the context was made for)."""
+        self._ck(lib().covgpu_resize(self.h, N, L))
+        self.N, self.L = N, L
 
     def close(self):
         if self.h:

@@ -29,6 +29,8 @@ struct covgpu_ctx {
   int dev = 0;
   cudaStream_t st = nullptr;
   int N = 0, L = 0, Lp = 0, nT = 0, ntiles = 0, maxslots = 0, maxnull = 0;
+  // the dimensions the buffers were made for (covgpu_resize stays within them)
+  int capN = 0, capL = 0, capLp = 0, capnT = 0, capntiles = 0;
   char err[512] = {0};
   TileRC* d_tiles = nullptr;
   int* d_tile_index = nullptr;
@@ -130,6 +132,7 @@ extern "C" int covgpu_create(covgpu_ctx** ret, int device, int N, int L, int max
   ctx->nT = (L + TP - 1) / TP;
   ctx->Lp = ctx->nT * TP;
   ctx->ntiles = ctx->nT * (ctx->nT + 1) / 2;
+  ctx->capN = N; ctx->capL = L; ctx->capLp = ctx->Lp; ctx->capnT = ctx->nT; ctx->capntiles = ctx->ntiles;
   *ret = ctx;
   CK(cudaSetDevice(device));
   CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
@@ -194,6 +197,43 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
   for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
+}
+
+// tile lists of the current nT
+static int build_tiles(covgpu_ctx* ctx) {
+  const int nT = ctx->nT;
+  std::vector<TileRC> tiles;
+  std::vector<int> tindex((size_t)nT * nT, -1);
+  for (int I = 0; I < nT; I++)
+    for (int J = I; J < nT; J++) { tindex[(size_t)I * nT + J] = (int)tiles.size(); tiles.push_back({I, J}); }
+  CK(cudaMemcpy(ctx->d_tiles, tiles.data(), tiles.size() * sizeof(TileRC), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_tile_index, tindex.data(), tindex.size() * sizeof(int), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+extern "C" int covgpu_resize(covgpu_ctx* ctx, int N, int L) {
+  CK(cudaSetDevice(ctx->dev));
+  if (N < 1 || L < 1 || N > ctx->capN || L > ctx->capL)
+    return fail(ctx, 11, "%d x %d is outside the context's %d x %d", N, L, ctx->capN, ctx->capL);
+  CK(cudaStreamSynchronize(ctx->st));
+  ctx->N = N; ctx->L = L;
+  ctx->nT = (L + TP - 1) / TP;
+  ctx->Lp = ctx->nT * TP;
+  ctx->ntiles = ctx->nT * (ctx->nT + 1) / 2;
+  int s;
+  if ((s = build_tiles(ctx))) return s;
+  // gap codes in every slot's rows (columns past L are never scored)
+  CK(cudaMemset(ctx->d_ax, 4, (size_t)ctx->maxslots * N * ctx->Lp));
+  ctx->have_w = false;
+  ctx->have_tree = false;
+  ctx->counted = false;
+  ctx->last_nout = ctx->last_first = ctx->last_nslots = 0;
+  ctx->sim_key.clear();
+  if (ctx->umma && !umma_plan_resize(ctx->umma, N, L, ctx->Lp, ctx->nT, ctx->ntiles)) {
+    umma_plan_destroy(ctx->umma);
+    ctx->umma = nullptr;
+  }
+  return 0;
 }
 
 extern "C" int covgpu_set_weights(covgpu_ctx* ctx, const double* wgt) {
@@ -264,9 +304,9 @@ extern "C" int covgpu_set_tree(covgpu_ctx* ctx, const int* parent, const int* le
   }
   ctx->loff[maxd + 1] = (int)order.size();
   if (!ctx->d_left) {
-    CK(dalloc(&ctx->d_left, N - 1));
-    CK(dalloc(&ctx->d_right, N - 1));
-    CK(dalloc(&ctx->d_lnodes, N - 1));
+    CK(dalloc(&ctx->d_left, ctx->capN - 1));
+    CK(dalloc(&ctx->d_right, ctx->capN - 1));
+    CK(dalloc(&ctx->d_lnodes, ctx->capN - 1));
   }
   CK(cudaMemcpy(ctx->d_left, left, (N - 1) * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(ctx->d_right, right, (N - 1) * sizeof(int), cudaMemcpyHostToDevice));
@@ -355,9 +395,9 @@ extern "C" int covgpu_substitutions(covgpu_ctx* ctx, int slot, uint64_t seed, in
   uint32_t* bits = nullptr;
   cudaError_t e = cudaMalloc(&bits, 2 * (size_t)L * Wb * sizeof(uint32_t));
   if (e == cudaSuccess && !ctx->d_nsubs) {
-    e = dalloc(&ctx->d_nsubs, (size_t)L);
-    if (e == cudaSuccess) e = dalloc(&ctx->d_ndouble, (size_t)L * L);
-    if (e == cudaSuccess) e = dalloc(&ctx->d_njoin, (size_t)L * L);
+    e = dalloc(&ctx->d_nsubs, (size_t)ctx->capL);
+    if (e == cudaSuccess) e = dalloc(&ctx->d_ndouble, (size_t)ctx->capL * ctx->capL);
+    if (e == cudaSuccess) e = dalloc(&ctx->d_njoin, (size_t)ctx->capL * ctx->capL);
   }
   const uint8_t* ax = ctx->d_ax + (size_t)slot * N * Lp;
   NullTree T{N, ctx->d_left, ctx->d_right};
@@ -477,8 +517,8 @@ extern "C" int covgpu_simulate(covgpu_ctx* ctx, const double* ld, const double* 
   if (!ctx->d_simQ) {
     CK(dalloc(&ctx->d_simQ, 16 + 256 + 4 + 16));
     CK(dalloc(&ctx->d_R, 4 + 16));
-    CK(dalloc(&ctx->d_units, L));
-    CK(dalloc(&ctx->d_simroot, Lp));
+    CK(dalloc(&ctx->d_units, ctx->capL));
+    CK(dalloc(&ctx->d_simroot, ctx->capLp));
   }
   const size_t need = (size_t)nrep * (N - 1) * nunits;
   if (ctx->simstate_cap < need) {
@@ -585,7 +625,8 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   if (need_w) {
     if (counter == COVGPU_COUNT_TENSOR) {
       if (!ctx->umma) {
-        ctx->umma = umma_plan_create(N, L, Lp, ctx->nT, ctx->d_tiles, ntiles, ctx->maxslots);
+        ctx->umma = umma_plan_create(N, L, Lp, ctx->nT, ctx->d_tiles, ntiles, ctx->maxslots, ctx->capN, ctx->capLp,
+                                     ctx->capntiles);
         if (!ctx->umma) return fail(ctx, 12, "tensor counting not available for this shape");
         umma_set_weights(ctx->umma, ctx->h_w.data(), N, ctx->st);
       }
@@ -602,7 +643,7 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
     ctx->nlaunch += 4;
   }
   if (need_u) {
-    if (!ctx->d_ucnt) CK(dalloc(&ctx->d_ucnt, (size_t)ctx->maxslots * cstride));
+    if (!ctx->d_ucnt) CK(dalloc(&ctx->d_ucnt, (size_t)ctx->maxslots * ctx->capntiles * 16 * TPP));
     if (counter == COVGPU_COUNT_TENSOR && ctx->umma) {
       CK(umma_count(ctx->umma, ax, sstride, nslots, true, ctx->d_ucnt, ctx->st));
     } else {
@@ -643,7 +684,7 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   const int64_t pplane = (int64_t)nT * nT * TP;
   for (int r = 0; r < nrafs; r++) {
     const int q = rafs_q[r];
-    if (!ctx->d_cov2) CK(dalloc(&ctx->d_cov2, (size_t)ctx->maxslots * plane));
+    if (!ctx->d_cov2) CK(dalloc(&ctx->d_cov2, (size_t)ctx->maxslots * ctx->capntiles * TPP));
     CK(cudaMemcpy2DAsync(ctx->d_cov2, plane * sizeof(float2), ctx->d_cov + q * plane, ntypes * plane * sizeof(float2),
                          plane * sizeof(float2), nslots, cudaMemcpyDeviceToDevice, ctx->st));
     CK(launch_rafs(ctx->d_cov2, ctx->d_cov + q * plane, plane, ntypes * plane, ctx->d_tiles, ctx->d_tile_index, ntiles,
@@ -693,7 +734,7 @@ extern "C" int covgpu_get_cov(covgpu_ctx* ctx, int slot, int which, double* COV)
   const int rel = slot - ctx->last_first;
   if (rel < 0 || rel >= ctx->last_nslots || which < 0 || which >= ctx->last_nout)
     return fail(ctx, 11, "no scores for slot %d / type %d", slot, which);
-  if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->L * ctx->L));
+  if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->capL * ctx->capL));
   const int64_t plane = (int64_t)ctx->ntiles * TPP;
   CK(launch_untile(ctx->d_cov + ((int64_t)rel * ctx->last_nout + which) * plane, ctx->d_tiles, ctx->ntiles, ctx->L,
                    -INFINITY, ctx->d_full, ctx->st));
@@ -1035,7 +1076,7 @@ extern "C" int covgpu_features(covgpu_ctx* ctx, int slot, double tree_len, float
   if (!ctx->have_w) return fail(ctx, 11, "weights not set");
   if (!std::isfinite(tree_len)) return fail(ctx, 11, "tree length is not finite");
   if (!ctx->d_featscr) {
-    CK(dalloc(&ctx->d_featscr, feat_scratch_doubles(ctx->L)));
+    CK(dalloc(&ctx->d_featscr, feat_scratch_doubles(ctx->capL)));
     CK(dalloc(&ctx->d_feat, kNFeat));
   }
   CK(launch_features(ctx->d_ax + (size_t)slot * ctx->N * ctx->Lp, ctx->N, ctx->L, ctx->Lp, ctx->d_wd, tree_len,
@@ -1234,7 +1275,7 @@ static int upload_full(covgpu_ctx* ctx, const double* COV) {
     if (ctx->last_nout < 1 || ctx->last_first != 0) return fail(ctx, 11, "no device score matrix for slot 0");
     return 0;
   }
-  if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->L * ctx->L));
+  if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->capL * ctx->capL));
   CK(cudaMemcpyAsync(ctx->d_full, COV, (size_t)ctx->L * ctx->L * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
   CK(launch_tile(ctx->d_full, ctx->d_tiles, ctx->ntiles, ctx->L, ctx->d_cov, ctx->st));
   ctx->last_nout = 1; ctx->last_first = 0; ctx->last_nslots = 1;
@@ -1313,7 +1354,7 @@ extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void
   const int64_t plane = (int64_t)ctx->ntiles * TPP;
   double* evt = nullptr;
   if (Eval) {
-    if (!ctx->d_evt) CK(dalloc(&ctx->d_evt, (size_t)plane));
+    if (!ctx->d_evt) CK(dalloc(&ctx->d_evt, (size_t)ctx->capntiles * TPP));
     evt = ctx->d_evt;
   }
   CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
@@ -1322,7 +1363,7 @@ extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void
   int nh = 0;
   CK(cudaMemcpyAsync(&nh, ctx->d_nhits, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
   if (Eval) {
-    if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->L * ctx->L));
+    if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->capL * ctx->capL));
     CK(launch_untile(evt, ctx->d_tiles, ctx->ntiles, ctx->L, INFINITY, ctx->d_full, ctx->st));
     CK(cudaMemcpyAsync(Eval, ctx->d_full, (size_t)ctx->L * ctx->L * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
   }

@@ -71,7 +71,9 @@ struct UmmaPlan {
   CUtensorMap tmap;
   int* d_err = nullptr;
   int nsm = 152;
-  bool prepared_unit = false;
+  // capacity of the buffers (the plan can be resized within it)
+  int capN = 0, capLp = 0, order_cap = 0;
+  size_t ops_bytes = 0, ops8_bytes = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -511,51 +513,67 @@ static size_t smem_bytes(int nl) {
   return ring + stage_out + 1024;
 }
 
-UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, int ntiles, int maxslots) {
+// dimensions of the current alignments within the plan's buffers: tile
+// order, operand tensor maps; false when they do not fit
+static bool plan_dims(UmmaPlan* p, int N, int L, int Lp, int nT, int ntiles) {
+  const int Npad = (N + UK - 1) / UK * UK;
+  const int64_t rows = (int64_t)4 * p->maxslots * 4 * Lp;
+  if (N < 1 || N > p->capN || Lp > p->capLp || ntiles > p->order_cap || rows >= ((int64_t)1 << 31) ||
+      (size_t)rows * Npad * sizeof(__nv_bfloat16) > p->ops_bytes)
+    return false;
+  p->N = N; p->L = L; p->Lp = Lp; p->nT = nT; p->ntiles = ntiles; p->Npad = Npad;
+  // blocked raster: super-blocks of SB x SB tiles (I <= J) in turn, so the
+  // CTAs resident at one time share a few operand row blocks in L2
+  std::vector<int> order;
+  order.reserve(ntiles);
+  auto tindex = [nT](int I, int J) { return I * nT - I * (I - 1) / 2 + (J - I); };   // I-major tile list
+  constexpr int SB = 10;
+  for (int bI = 0; bI < nT; bI += SB)
+    for (int bJ = bI; bJ < nT; bJ += SB)
+      for (int I = bI; I < std::min(nT, bI + SB); I++)
+        for (int J = std::max(I, bJ); J < std::min(nT, bJ + SB); J++) order.push_back(tindex(I, J));
+  if ((int)order.size() != ntiles) return false;
+  if (cudaMemcpy(p->d_order, order.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice) != cudaSuccess) return false;
+  cuuint64_t gdim[2] = {(cuuint64_t)p->Npad, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)p->Npad * sizeof(__nv_bfloat16)};
+  cuuint32_t box[2] = {UK, UM};
+  cuuint32_t estride[2] = {1, 1};
+  if (get_encode()(&p->tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, p->d_ops, gdim, gstride, box, estride,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  if (p->d_ops8) {   // the FP8 operands are re-encoded on their next use
+    p->Npad8 = 0;
+  }
+  return true;
+}
+
+UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, int ntiles, int maxslots, int capN,
+                           int capLp, int capntiles) {
   int dev = 0, major = 0, minor = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
   cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
   if (major != 10) return nullptr;               // tcgen05 needs a Blackwell datacenter part
-  if (N < 1 || N > 65536) return nullptr;       // limb sums stay exact in FP32 up to here
+  if (capN < 1 || capN > 65536) return nullptr;  // limb sums stay exact in FP32 up to here
   if (!get_encode()) return nullptr;
   UmmaPlan* p = new UmmaPlan();
-  p->N = N; p->L = L; p->Lp = Lp; p->nT = nT; p->ntiles = ntiles; p->maxslots = maxslots; p->d_tiles = d_tiles;
-  p->Npad = (N + UK - 1) / UK * UK;
-  const int64_t rows = (int64_t)4 * maxslots * 4 * Lp;
-  if (rows >= ((int64_t)1 << 31)) { delete p; return nullptr; }
-  if (cudaMalloc(&p->d_ops, (size_t)rows * p->Npad * sizeof(__nv_bfloat16)) != cudaSuccess) { delete p; return nullptr; }
-  if (cudaMemset(p->d_ops, 0, (size_t)rows * p->Npad * sizeof(__nv_bfloat16)) != cudaSuccess ||
-      cudaMalloc(&p->d_limbs, (size_t)3 * p->Npad) != cudaSuccess || cudaMalloc(&p->d_err, sizeof(int)) != cudaSuccess) {
+  p->maxslots = maxslots; p->d_tiles = d_tiles;
+  p->capN = capN; p->capLp = capLp; p->order_cap = capntiles;
+  const int Npad_cap = (capN + UK - 1) / UK * UK;
+  const int64_t rows_cap = (int64_t)4 * maxslots * 4 * capLp;
+  if (rows_cap >= ((int64_t)1 << 31)) { delete p; return nullptr; }
+  p->ops_bytes = (size_t)rows_cap * Npad_cap * sizeof(__nv_bfloat16);
+  if (cudaMalloc(&p->d_ops, p->ops_bytes) != cudaSuccess) { p->d_ops = nullptr; umma_plan_destroy(p); return nullptr; }
+  if (cudaMemset(p->d_ops, 0, p->ops_bytes) != cudaSuccess ||
+      cudaMalloc(&p->d_limbs, (size_t)3 * Npad_cap) != cudaSuccess ||
+      cudaMalloc(&p->d_order, sizeof(int) * std::max(1, capntiles)) != cudaSuccess ||
+      cudaMalloc(&p->d_err, sizeof(int)) != cudaSuccess) {
     umma_plan_destroy(p);
     return nullptr;
   }
   cudaMemset(p->d_err, 0, sizeof(int));
-  // blocked raster: super-blocks of SB x SB tiles (I <= J) in turn, so the
-  // CTAs resident at one time share a few operand row blocks in L2
-  {
-    std::vector<int> order;
-    order.reserve(ntiles);
-    auto tindex = [nT](int I, int J) { return I * nT - I * (I - 1) / 2 + (J - I); };   // I-major tile list
-    constexpr int SB = 10;
-    for (int bI = 0; bI < nT; bI += SB)
-      for (int bJ = bI; bJ < nT; bJ += SB)
-        for (int I = bI; I < std::min(nT, bI + SB); I++)
-          for (int J = std::max(I, bJ); J < std::min(nT, bJ + SB); J++) order.push_back(tindex(I, J));
-    if ((int)order.size() != ntiles || cudaMalloc(&p->d_order, sizeof(int) * ntiles) != cudaSuccess) {
-      umma_plan_destroy(p);
-      return nullptr;
-    }
-    cudaMemcpy(p->d_order, order.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice);
-  }
-  cuuint64_t gdim[2] = {(cuuint64_t)p->Npad, (cuuint64_t)rows};
-  cuuint64_t gstride[1] = {(cuuint64_t)p->Npad * sizeof(__nv_bfloat16)};
-  cuuint32_t box[2] = {UK, UM};
-  cuuint32_t estride[2] = {1, 1};
-  CUresult r = get_encode()(&p->tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, p->d_ops, gdim, gstride, box, estride,
-                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) { umma_plan_destroy(p); return nullptr; }
+  if (!plan_dims(p, N, L, Lp, nT, ntiles)) { umma_plan_destroy(p); return nullptr; }
   cudaFuncSetAttribute(k_count_umma<3, STAGES3, ACC3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes(3));
   cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -564,6 +582,10 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
                        (int)smem_bytes(1));
   cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev);
   return p;
+}
+
+bool umma_plan_resize(UmmaPlan* p, int N, int L, int Lp, int nT, int ntiles) {
+  return plan_dims(p, N, L, Lp, nT, ntiles);
 }
 
 void umma_plan_destroy(UmmaPlan* p) {
@@ -619,25 +641,31 @@ static bool encode_out_map(UmmaPlan* p, float* cnt, CUtensorMap* m) {
                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// FP8 operand buffer and its tensor map, made on the first unit-weight pass
+// FP8 operand buffer (allocated once, at capacity) and its tensor map for
+// the current dimensions, made on the first unit-weight pass after a resize
 static cudaError_t ensure_fp8(UmmaPlan* p) {
-  if (p->d_ops8) return cudaSuccess;
-  p->Npad8 = (p->N + UK8 - 1) / UK8 * UK8;
+  if (p->d_ops8 && p->Npad8) return cudaSuccess;
+  cudaError_t e;
+  if (!p->d_ops8) {
+    const int64_t rows_cap = (int64_t)p->maxslots * 4 * p->capLp;
+    const int Npad8_cap = (p->capN + UK8 - 1) / UK8 * UK8;
+    p->ops8_bytes = (size_t)rows_cap * Npad8_cap;
+    e = cudaMalloc(&p->d_ops8, p->ops8_bytes);
+    if (e != cudaSuccess) { p->d_ops8 = nullptr; p->ops8_bytes = 0; return e; }
+    if ((e = cudaMemset(p->d_ops8, 0, p->ops8_bytes)) != cudaSuccess) return e;
+  }
+  const int Npad8 = (p->N + UK8 - 1) / UK8 * UK8;
   const int64_t rows = (int64_t)p->maxslots * 4 * p->Lp;
-  cudaError_t e = cudaMalloc(&p->d_ops8, (size_t)rows * p->Npad8);
-  if (e != cudaSuccess) { p->d_ops8 = nullptr; return e; }
-  if ((e = cudaMemset(p->d_ops8, 0, (size_t)rows * p->Npad8)) != cudaSuccess) return e;
-  cuuint64_t gdim[2] = {(cuuint64_t)p->Npad8, (cuuint64_t)rows};
-  cuuint64_t gstride[1] = {(cuuint64_t)p->Npad8};
+  if ((size_t)rows * Npad8 > p->ops8_bytes) return cudaErrorInvalidValue;
+  cuuint64_t gdim[2] = {(cuuint64_t)Npad8, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)Npad8};
   cuuint32_t box[2] = {UK8, UM};
   cuuint32_t estride[2] = {1, 1};
   if (get_encode()(&p->tmap8, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, p->d_ops8, gdim, gstride, box, estride,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
-    cudaFree(p->d_ops8);
-    p->d_ops8 = nullptr;
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return cudaErrorInvalidValue;
-  }
+  p->Npad8 = Npad8;
   return cudaSuccess;
 }
 

@@ -10,7 +10,12 @@ namespace covgpu {
 struct UmmaPlan;
 
 // nullptr when the shape cannot be served by the tensor path
-UmmaPlan*   umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, int ntiles, int maxslots);
+// a plan for alignments of N x L, with buffers for up to capN sequences,
+// capLp padded columns and capntiles tiles
+UmmaPlan*   umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, int ntiles, int maxslots, int capN,
+                             int capLp, int capntiles);
+// the plan for other dimensions within its capacity; false if they do not fit
+bool        umma_plan_resize(UmmaPlan* p, int N, int L, int Lp, int nT, int ntiles);
 void        umma_plan_destroy(UmmaPlan* p);
 void        umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t st);
 // counts of nslots alignments (slot stride in bytes of the code buffer) into

@@ -179,9 +179,42 @@ def train(X, T, epochs=300, batch=256, lr=2e-3, wd=1e-4, seed=1, log=None):
     return net, hist
 
 
-def save(net, path):
+def val_loss(net, X, T):
+    """Mean squared error on standardised targets."""
+    ym, ys = net.norm()[2:4]
+    return float(np.mean(((net.forward(X) - T) / ys) ** 2))
+
+
+def train_selected(X, T, grid_epochs=(5, 10, 20, 40, 80, 160), grid_wd=(1e-4, 1e-2, 1e-1), val_frac=0.15, batch=256,
+                   lr=2e-3, seed=1, log=None):
+    """Epochs and weight decay chosen on a held-out split of the families;
+    the network kept is the one trained with the chosen setting on the rest."""
+    rng = np.random.default_rng(seed)
+    idx = rng.permutation(len(X))
+    nv = max(1, int(val_frac * len(X)))
+    va, tr = idx[:nv], idx[nv:]
+    best = None
+    for wd in grid_wd:
+        for ep in grid_epochs:
+            net, hist = train(X[tr], T[tr], epochs=ep, batch=batch, lr=lr, wd=wd, seed=seed)
+            v = val_loss(net, X[va], T[va])
+            if log:
+                print("select: wd %g epochs %d train %.4f val %.4f" % (wd, ep, hist[-1], v), file=log, flush=True)
+            if best is None or v < best[0]:
+                if best is not None:
+                    best[1].close()
+                best = (v, net, ep, wd)
+            else:
+                net.close()
+    zero = float(np.mean(((T[va] - T[tr].mean(0)) / T[tr].std(0)) ** 2))
+    return best[1], dict(val_loss=best[0], epochs=best[2], wd=best[3], val_loss_mean_predictor=zero,
+                         train_rows=len(tr), val_rows=len(va))
+
+
+def save(net, path, nquick):
     xm, xs, ym, ys, lo, hi = net.norm()
-    np.savez_compressed(path, params=net.params(), xmean=xm, xstd=xs, ymean=ym, ystd=ys, xlo=lo, xhi=hi)
+    np.savez_compressed(path, params=net.params(), xmean=xm, xstd=xs, ymean=ym, ystd=ys, xlo=lo, xhi=hi,
+                        nquick=np.int32(nquick))
 
 
 def load(path, batch_cap=512):
@@ -237,7 +270,8 @@ def evaluate(net, first, count, nnull, nquick=10, few=20, log=None):
             fr = run.full(few, thresh=10.0, hitcap=1 << 20) if few else None
         finally:
             run.close()
-        row = dict(seed=fam["seed"], N=fam["N"], L=fam["L"], used_net=used, ntrue=0)
+        ntail = sum(1 for h in truth["hits"] if h[3] < 1.0)
+        row = dict(seed=fam["seed"], N=fam["N"], L=fam["L"], used_net=used, ntrue=0, ntail=ntail)
         for name, r in (("net", lr), ("mean", mr), ("quick", qr), ("few", fr)):
             if r is None:
                 continue
@@ -245,6 +279,7 @@ def evaluate(net, first, count, nnull, nquick=10, few=20, log=None):
             row[name + "_med"] = float(np.median(errs)) if errs else 0.0
             row[name + "_p90"] = float(np.percentile(errs, 90)) if errs else 0.0
             row[name + "_agree"] = agree
+            row[name + "_nsig"] = nb
             row["ntrue"] = na
         row["sim_nulls"] = nquick if used else nquick + nnull
         rows.append(row)
@@ -255,24 +290,26 @@ def evaluate(net, first, count, nnull, nquick=10, few=20, log=None):
 
 
 def summarize(rows, nnull):
-    def med(key, sel=None):
-        v = [r[key] for r in rows if key in r and (sel is None or sel(r)) and np.isfinite(r[key])]
-        return float(np.median(v)) if v else float("nan")
-
-    def frac_fin(key):
-        v = [r[key] for r in rows if key in r]
-        return float(np.mean([np.isfinite(x) for x in v])) if v else float("nan")
-
+    """Medians over the families the network handled that have at least one
+    pair with true E < 1 (the others have no tail to compare); pair-set
+    agreement over the families where either method finds an E < 0.05 pair."""
     used = [r for r in rows if r["used_net"]]
+    tail = [r for r in used if r["ntail"] > 0]
     sims = sum(r["sim_nulls"] for r in rows)
     out = dict(families=len(rows), used_net=len(used), fallback=len(rows) - len(used),
-               simulated_nulls=sims, full_nulls=nnull * len(rows),
+               families_with_tail=len(tail), simulated_nulls=sims, full_nulls=nnull * len(rows),
                null_reduction=(nnull * len(rows) / sims) if sims else float("inf"))
     for name in ("net", "mean", "quick", "few"):
-        out[name + "_median_rel_E_error"] = med(name + "_med", lambda r: r["used_net"])
-        out[name + "_p90_rel_E_error"] = med(name + "_p90", lambda r: r["used_net"])
-        out[name + "_pairset_agreement"] = med(name + "_agree", lambda r: r["used_net"])
-        out[name + "_finite_frac"] = frac_fin(name + "_p90")
+        v = [r[name + "_med"] for r in tail if name + "_med" in r]
+        if not v:
+            continue
+        fin = [x for x in v if np.isfinite(x)]
+        out[name + "_median_rel_E_error"] = float(np.median(v))
+        out[name + "_p75_rel_E_error"] = float(np.percentile(fin, 75)) if fin else float("nan")
+        out[name + "_finite_frac"] = len(fin) / len(v)
+        ag = [r[name + "_agree"] for r in used if r["ntrue"] > 0 or r.get(name + "_nsig", 0) > 0]
+        out[name + "_pairset_agreement_mean"] = float(np.mean(ag)) if ag else 1.0
+    out["net_better_than_quick"] = sum(1 for r in tail if r["net_med"] < r["quick_med"])
     return out
 
 
@@ -287,7 +324,6 @@ def main(argv=None):
     g.add_argument("--out", required=True)
     t = sub.add_parser("train")
     t.add_argument("--data", nargs="+", required=True)
-    t.add_argument("--epochs", type=int, default=300)
     t.add_argument("--batch", type=int, default=256)
     t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--out", required=True)
@@ -308,9 +344,12 @@ def main(argv=None):
         zs = [np.load(p) for p in a.data]
         X = np.concatenate([z["X"] for z in zs])
         T = np.concatenate([z["T"] for z in zs])
-        net, hist = train(X, T, epochs=a.epochs, batch=a.batch, lr=a.lr, log=sys.stderr)
-        save(net, a.out)
-        print(json.dumps(dict(rows=len(X), loss_first=float(hist[0]), loss_last=float(hist[-1]))))
+        net, info = train_selected(X, T, batch=a.batch, lr=a.lr, log=sys.stderr)
+        nq = {int(z["nquick"]) for z in zs if "nquick" in z}
+        if len(nq) != 1:
+            raise SystemExit("training files mix numbers of quick nulls: %s" % sorted(nq))
+        save(net, a.out, nq.pop())
+        print(json.dumps(dict(rows=len(X), **info)))
     else:
         net = load(a.net)
         rows = evaluate(net, a.first, a.count, a.nnull, nquick=a.nquick, few=a.few, log=sys.stderr)

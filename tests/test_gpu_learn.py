@@ -176,3 +176,24 @@ def test_out_of_range_falls_back_to_simulation(covgpu):
     assert not net.in_range(e.learned_features(1.5, nquick=2))
     net.close()
     e.close()
+
+
+def test_shipped_network_on_held_out_families(covgpu):
+    """The shipped network on families it was not trained on (seeds outside
+    its training and evaluation ranges): it runs on the quick nulls, and its
+    E-values stay near the 200-null ones."""
+    import importlib.util
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("learned_null", os.path.join(root, "r-scape_gb300",
+                                                                                "learned_null.py"))
+    ln = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(ln)
+    net = ln.load(os.path.join(root, "r-scape_gb300", "learned_null_gtp.npz"))
+    nq = int(np.load(os.path.join(root, "r-scape_gb300", "learned_null_gtp.npz"))["nquick"])
+    rows = ln.evaluate(net, 300001, 16, 200, nquick=nq, few=0)
+    s = ln.summarize(rows, 200)
+    net.close()
+    assert s["used_net"] >= 14 and s["null_reduction"] >= 5
+    assert s["net_finite_frac"] == 1.0
+    assert s["net_median_rel_E_error"] < 0.35

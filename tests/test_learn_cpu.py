@@ -156,3 +156,16 @@ def test_evalue_errors():
     errs, agree, na, nb = ln.evalue_errors(truth, other)
     assert errs[0] == pytest.approx(0.1) and errs[1] == float("inf") and len(errs) == 2
     assert na == 1 and nb == 2 and agree == pytest.approx(0.5)
+
+
+def test_shipped_network_file(oracle):
+    """The trained network shipped with the package: complete, finite, and
+    its training range contains its own mean features."""
+    z = np.load(os.path.join(ROOT, "r-scape_gb300", "learned_null_gtp.npz"))
+    assert z["params"].shape == (148995,) and np.all(np.isfinite(z["params"]))
+    assert int(z["nquick"]) >= 1
+    assert np.all(z["xstd"] > 0) and np.all(z["ystd"] > 0)
+    assert np.all(z["xlo"] <= z["xmean"]) and np.all(z["xmean"] <= z["xhi"])
+    nrm = np.concatenate([z["xmean"], z["xstd"], z["ymean"], z["ystd"]]).astype(np.float32)
+    y = oracle.mlp_forward(z["params"], nrm, z["xmean"][None, :])
+    assert np.all(np.isfinite(y)) and np.all(np.abs(y) < 5)
