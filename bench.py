@@ -265,6 +265,9 @@ def main():
     ap.add_argument("--types", default=None, help="comma-separated statistics (default GTp,MIp,CHIp,RAFp)")
     ap.add_argument("--families", type=int, default=200,
                     help="families of the ragged-family stream timed after the main workload (0: skip)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="only the main workload: no CPU baseline, simulator, families or batched nulls "
+                         "(for profiler launch lists)")
     args = ap.parse_args()
     if args.N:
         CFG["N"] = args.N
@@ -375,10 +378,13 @@ def main():
     achieved = flop_launch / cnt_s / 1e12
     kname = "k_count_umma" if kind == "tensor" else "k_count_simt"
     traffic = profile_traffic(kname)
-    cpu_v, cpu_sample, _ = cpu_reference(ax, w, args.cpu_budget, threads)
-    sim = simulator_rate(cg, e, s, N, L, ns)
-    fam = ragged_families(cg, args.families, counter, local) if (args.families > 0 and rank == 0) else None
-    bnull = batched_nulls(cg, counter, local) if rank == 0 else None
+    if args.no_extras:
+        cpu_v, cpu_sample, sim, fam, bnull = None, "skipped (--no-extras)", None, None, None
+    else:
+        cpu_v, cpu_sample, _ = cpu_reference(ax, w, args.cpu_budget, threads)
+        sim = simulator_rate(cg, e, s, N, L, ns)
+        fam = ragged_families(cg, args.families, counter, local) if args.families > 0 else None
+        bnull = batched_nulls(cg, counter, local)
     out = {
         "metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * step_s, "higher_is_better": True, "scaling": "weak",

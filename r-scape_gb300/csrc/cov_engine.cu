@@ -82,6 +82,8 @@ struct covgpu_ctx {
   // learned-null features
   double* d_featscr = nullptr;
   float* d_feat = nullptr;
+  void* d_gsc = nullptr;       // GSC scratch, kept across calls
+  size_t gsc_cap = 0;
   bool want_qsum = false;     // covgpu_rscape keeps the null-score summary of type 0
   double qsum[17] = {0};
   bool have_qsum = false;
@@ -192,7 +194,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
   if (ctx->fitw) fitwork_destroy(ctx->fitw);
   void* sims[] = {ctx->d_simQ, ctx->d_simT, ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16, ctx->d_R, ctx->d_units,
                   ctx->d_simroot, ctx->d_simstate, ctx->d_nsubs, ctx->d_ndouble, ctx->d_njoin, ctx->d_featscr,
-                  ctx->d_feat};
+                  ctx->d_feat, ctx->d_gsc};
   for (void* p : sims) if (p) cudaFree(p);
   for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -358,16 +360,23 @@ extern "C" int covgpu_weights_gsc_dev(covgpu_ctx* ctx, int slot, int set, double
   if (slot < 0 || slot >= ctx->maxslots || !wgt) return fail(ctx, 11, "bad slot or output");
   if (N > 16384) return fail(ctx, 11, "GSC weights are for up to 16384 sequences (N^2 distances)");
   if (N == 1) { wgt[0] = 1.0; return set ? covgpu_set_weights(ctx, wgt) : 0; }
-  void* scratch = nullptr;
-  double* d_w = nullptr;
-  CK(cudaMalloc(&scratch, gsc_scratch_bytes(N, L)));
-  cudaError_t e = dalloc(&d_w, (size_t)N);
-  if (e == cudaSuccess) e = launch_weights_gsc(ctx->d_ax + (size_t)slot * N * Lp, N, L, Lp, scratch, d_w, ctx->st);
+  // scratch kept across calls (families of a resized context reuse it)
+  const size_t need = gsc_scratch_bytes(N, L) + ((size_t)N * sizeof(double) + 256);
+  if (ctx->gsc_cap < need) {
+    if (ctx->d_gsc) cudaFree(ctx->d_gsc);
+    ctx->d_gsc = nullptr;
+    ctx->gsc_cap = 0;
+    const size_t cap = std::max(need, gsc_scratch_bytes(ctx->capN, ctx->capL) + (size_t)ctx->capN * sizeof(double) + 256);
+    CK(cudaMalloc(&ctx->d_gsc, cap));
+    ctx->gsc_cap = cap;
+  }
+  uint8_t* scratch = (uint8_t*)ctx->d_gsc;
+  double* d_w = (double*)(scratch + ((gsc_scratch_bytes(N, L) + 255) & ~(size_t)255));
+  cudaError_t e = launch_weights_gsc(ctx->d_ax + (size_t)slot * N * Lp, N, L, Lp, scratch, d_w, ctx->st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(wgt, d_w, N * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
-  cudaFree(scratch);
-  if (d_w) cudaFree(d_w);
   if (e != cudaSuccess) return fail(ctx, 90, "CUDA error %s", cudaGetErrorString(e));
+  if (gsc_error(scratch, ctx->st)) return fail(ctx, 24, "GSC weights: a grid barrier timed out");
   double sum = 0.0;
   for (int s = 0; s < N; s++) sum += wgt[s];
   for (int s = 0; s < N; s++) wgt[s] = (sum > 0.0) ? wgt[s] * (double)N / sum : 1.0;

@@ -129,3 +129,23 @@ def test_device_weights_and_gapfilter(covgpu, oracle, N, L):
         for thr in (0.5, 0.75, 0.95):
             assert np.array_equal(e.gapfilter(0, wgt, thr), oracle.gapfilter(ax, wgt, thr) == 1)
     e.close()
+
+
+@pytest.mark.parametrize("N,L,dup", [(300, 80, 0), (257, 33, 40), (999, 120, 200), (2, 10, 0), (4800, 20, 0)])
+def test_gsc_single_launch_upgma(covgpu, oracle, N, L, dup):
+    """GSC weights from the one-launch UPGMA (cached row minima) against the
+    oracle, with duplicated sequences (exact distance ties, tie-breaking by
+    pair order) and at the largest size that still takes this kernel."""
+    s = covgpu.Synth(N, L, 0.8, 2, 1, 1, 2, 0.1, seed=N + dup, tree_kind=1)
+    ax = s.ax.copy()
+    rng = np.random.default_rng(N)
+    for k in range(dup):               # copies of earlier rows
+        i, j = rng.integers(0, N, size=2)
+        ax[j] = ax[i]
+    e = covgpu.Engine(N, L)
+    e.set_alignment(0, ax)
+    g = e.weights_gsc(0, set=False)
+    e.close()
+    if N <= 1200:
+        assert np.allclose(g, oracle.weights_gsc(ax), rtol=1e-10, atol=1e-13)
+    assert np.all(np.isfinite(g)) and abs(g.sum() - N) < 1e-6 * N
