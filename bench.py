@@ -160,35 +160,55 @@ def load_learned_null():
     return g._load("learned_null", os.path.join(ROOT, "r-scape_gb300", "learned_null.py"))
 
 
-def ragged_families(cg, nfam, counter, device):
+def ragged_families(cg, nfam, counter, device, workers=4):
     """E-valued MSAs/s over a stream of families drawn as the ragged-family
     workload draws them (N ~ U[20,2000], L ~ logU[50,1500], tree length
-    ~ U[0.5,3], base-pair fraction ~ U[0.1,0.35]; seeds 1..nfam): one context
-    made for the largest size and resized per family; per family the
-    alignment and tree go in, R-scape's weights (GSC up to 1000 sequences,
-    else position-based) and its null count rule run on the device, GTp with
-    APC, and the hit list comes out.  Families are synthesised before the
-    timed region."""
+    ~ U[0.5,3], base-pair fraction ~ U[0.1,0.35]; seeds 1..nfam).  `workers`
+    host threads each drive one context (its own CUDA stream), made for the
+    largest size and resized per family, so small families' kernels overlap
+    on the GPU.  Per family the alignment and tree go in, R-scape's weights
+    (GSC up to 1000 sequences, else position-based) and its null count rule
+    run on the device, GTp with APC, and the hit list comes out.  Families
+    are synthesised before the timed region."""
+    import threading
     ln = load_learned_null()
     fams = [ln.draw_family(k) for k in range(1, nfam + 1)]
     data = [ln.make_family(f) for f in fams]
-    e = cg.Engine(2000, 1500, maxslots=21, maxnull=20, device=device)
-    pairs = 0
+    engines = [cg.Engine(2000, 1500, maxslots=21, maxnull=20, device=device) for _ in range(workers)]
+    pairs = [0] * workers
+    errors = []
+
+    def work(k):
+        e = engines[k]
+        try:
+            for i in range(k, nfam, workers):
+                f, (s, _) = fams[i], data[i]
+                e.resize(f["N"], f["L"])
+                e.set_alignment(0, s.ax)
+                if f["N"] <= 1000:
+                    e.weights_gsc(0, set=True)
+                else:
+                    e.weights_pb(0, set=True)
+                e.set_tree(s.parent, s.left, s.right)
+                r = e.rscape(None, None, ["GTp"], counter=counter)[0]
+                pairs[k] += (r["nshuffle"] + 1) * f["L"] * (f["L"] - 1) // 2
+        except Exception as err:   # reported after the join
+            errors.append(err)
+
     t0 = time.perf_counter()
-    for f, (s, _) in zip(fams, data):
-        e.resize(f["N"], f["L"])
-        e.set_alignment(0, s.ax)
-        if f["N"] <= 1000:
-            e.weights_gsc(0, set=True)
-        else:
-            e.weights_pb(0, set=True)
-        e.set_tree(s.parent, s.left, s.right)
-        r = e.rscape(None, None, ["GTp"], counter=counter)[0]
-        pairs += (r["nshuffle"] + 1) * f["L"] * (f["L"] - 1) // 2
+    th = [threading.Thread(target=work, args=(k,)) for k in range(workers)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
     dt = time.perf_counter() - t0    # every call returns after its hit list reached the host
-    e.close()
-    return {"families": nfam, "seconds": dt, "msas_per_s": nfam / dt, "column_pairs_per_s": pairs / dt,
-            "statistic": "GTp", "nulls": "R-scape rule (20 here)", "timing": "host wall clock, host buffers in/out"}
+    for e in engines:
+        e.close()
+    if errors:
+        raise errors[0]
+    return {"families": nfam, "workers": workers, "seconds": dt, "msas_per_s": nfam / dt,
+            "column_pairs_per_s": sum(pairs) / dt, "statistic": "GTp", "nulls": "R-scape rule (20 here)",
+            "timing": "host wall clock, host buffers in/out"}
 
 
 def batched_nulls(cg, counter, device, steps=3):
@@ -265,6 +285,8 @@ def main():
     ap.add_argument("--types", default=None, help="comma-separated statistics (default GTp,MIp,CHIp,RAFp)")
     ap.add_argument("--families", type=int, default=200,
                     help="families of the ragged-family stream timed after the main workload (0: skip)")
+    ap.add_argument("--family-workers", type=int, default=4,
+                    help="host threads (one context and stream each) for the ragged-family stream")
     ap.add_argument("--no-extras", action="store_true",
                     help="only the main workload: no CPU baseline, simulator, families or batched nulls "
                          "(for profiler launch lists)")
@@ -338,6 +360,10 @@ def main():
                           "device_ms": list(ms), "launches": n, "hits": [len(x["hits"]) for x in r]}))
         return
     kind = "tensor" if counter == 1 else "simt"
+    tune = None
+    if counter == 1:   # the count kernel's tile schedule, picked on this workload before timing
+        best, tms = e.autotune(ns + 1)
+        tune = {"raster_superblock": best, "ms": tms}
     for _ in range(args.warmup):
         e.flush_l2()
         e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)
@@ -383,7 +409,7 @@ def main():
     else:
         cpu_v, cpu_sample, _ = cpu_reference(ax, w, args.cpu_budget, threads)
         sim = simulator_rate(cg, e, s, N, L, ns)
-        fam = ragged_families(cg, args.families, counter, local) if args.families > 0 else None
+        fam = ragged_families(cg, args.families, counter, local, args.family_workers) if args.families > 0 else None
         bnull = batched_nulls(cg, counter, local)
     out = {
         "metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": world, "steps": args.steps,
@@ -403,6 +429,7 @@ def main():
                          "sample": cpu_sample},
         "hits": [len(x["hits"]) for x in res],
         "simulator": sim,
+        "autotune": tune,
         "ragged_families": fam,
         "batched_nulls": bnull,
         "clocks": clk.summary(),

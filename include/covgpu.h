@@ -193,6 +193,15 @@ int  covgpu_evalue_full(covgpu_ctx *ctx, const double *COV, const void *h, const
 #define COVGPU_NOALLOC_MAX_L 16384
 int  covgpu_correct_noalloc(const double *d_cov, double *d_out, int L, int actype, double *d_minmax, void *stream);
 
+/* schedule autotuner of the tensor count kernel: times the weighted count of
+ * slots first_slot .. first_slot+nslots-1 (weights set) for each raster
+ * super-block size in cand[ncand] (NULL: 4, 6, 8, 10, 12, 16, 24; the
+ * resident CTAs sweep blocks of size x size tiles so they share operand rows
+ * in L2), keeps the fastest for the context's later calls, and returns the
+ * median milliseconds of each in ms (may be NULL) and the choice in *best.
+ * The count buffer is overwritten. */
+int  covgpu_autotune(covgpu_ctx *ctx, int first_slot, int nslots, int ncand, const int *cand, float *ms, int *best);
+
 /* writes a 256 MB device buffer (larger than L2) on the context's stream */
 int  covgpu_flush_l2(covgpu_ctx *ctx);
 

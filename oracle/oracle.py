@@ -103,6 +103,8 @@ def lib():
         L.orc_simulate.argtypes = [C.POINTER(Tree), C.c_int, C.c_int, i32p, u64p, u64p, u64p, u64p, C.c_void_p,
                                    C.c_double, C.c_double, C.c_uint64, C.c_uint32, u8p]
         f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.orc_raf_pairs.argtypes = [u8p, C.c_int, C.c_int, f64p, C.c_int, i32p, i32p, f64p]
+        L.orc_raf_pairs.restype = None
         L.orc_features.argtypes = [u8p, C.c_int, C.c_int, f64p, C.c_double, f64p]
         L.orc_features.restype = None
         L.orc_mlp_forward.argtypes = [f32p, f32p, f32p, C.c_int, f64p]
@@ -370,3 +372,15 @@ def mlp_grad(params, nrm, X, T):
     loss = lib().orc_mlp_grad(np.ascontiguousarray(params, dtype=np.float32),
                               np.ascontiguousarray(nrm, dtype=np.float32), X, T, X.shape[0], g)
     return loss, g
+
+
+def raf_pairs(ax, pairs, allow=None):
+    """RAF of the listed (i, j) pairs with the reference's O(N^2) loop."""
+    ax = np.ascontiguousarray(ax, dtype=np.uint8)
+    N, L = ax.shape
+    pi = np.ascontiguousarray([p[0] for p in pairs], dtype=np.int32)
+    pj = np.ascontiguousarray([p[1] for p in pairs], dtype=np.int32)
+    out = np.zeros(len(pairs))
+    allow = default_allow() if allow is None else np.ascontiguousarray(allow, dtype=np.float64)
+    lib().orc_raf_pairs(ax, N, L, allow, len(pairs), pi, pj, out)
+    return out

@@ -335,9 +335,40 @@ orc_probs(const uint8_t *ax, const double *wgt, int N, int L, double tol,
   memset(nseff, 0, sizeof(double) * (size_t)L * L);
   memset(ngap,  0, sizeof(double) * (size_t)L * L);
 
-  for (i = 0; i < L - 1; i++)
-    for (j = i + 1; j < L; j++)
-      naive_ppij(ax, wgt, N, L, i, j, pp, nseff, ngap);
+  if ((double)N * L * L < 4e9) {
+    for (i = 0; i < L - 1; i++)
+      for (j = i + 1; j < L; j++)
+        naive_ppij(ax, wgt, N, L, i, j, pp, nseff, ngap);
+  } else {
+    /* deep alignments: the same sums (sequence order per pair) from a
+     * column-major copy, pairs spread over the host threads */
+    uint8_t *axT = malloc((size_t)N * L);
+    if (!axT) return 5;
+    for (s = 0; s < N; s++)
+      for (i = 0; i < L; i++) axT[(size_t)i * N + s] = ax[(size_t)s * L + i];
+#pragma omp parallel for schedule(dynamic, 1) private(j, x, y, s)
+    for (i = 0; i < L - 1; i++) {
+      const uint8_t *ci = axT + (size_t)i * N;
+      for (j = i + 1; j < L; j++) {
+        const uint8_t *cj = axT + (size_t)j * N;
+        double *p = pp + ((int64_t)i * L + j) * K16;
+        double  ne = 0.0, ng = 0.0;
+        for (x = 0; x < K16; x++) p[x] = 1e-10;
+        for (s = 0; s < N; s++) {
+          const int ri = ci[s], rj = cj[s];
+          if (IS_CANON(ri) && IS_CANON(rj)) { ne += wgt[s]; p[ri * K4 + rj] += wgt[s]; }
+          else                              { ng += wgt[s]; }
+        }
+        vec_norm(p, K16);
+        for (x = 0; x < K4; x++)
+          for (y = 0; y < K4; y++)
+            pp[((int64_t)j * L + i) * K16 + y * K4 + x] = p[x * K4 + y];
+        nseff[(int64_t)i * L + j] = nseff[(int64_t)j * L + i] = ne;
+        ngap[(int64_t)i * L + j] = ng;
+      }
+    }
+    free(axT);
+  }
 
   for (i = 0; i < L; i++) {
     double *q = ps + (int64_t)i * 5;
@@ -526,6 +557,37 @@ orc_raf(const uint8_t *ax, int N, int L, const double *allow, double *COV, doubl
       cov_set(L, COV, minmax, i, j, cij - 1.0 * qij);
     }
   return 0;
+}
+
+/* corr_CalculateRAF's loop (src/correlators.c:876-933) for npairs listed
+ * pairs (i < j) only, over the host threads: out[k] = RAF of (pi[k], pj[k]) */
+void
+orc_raf_pairs(const uint8_t *ax, int N, int L, const double *allow, int npairs, const int *pi, const int *pj,
+              double *out)
+{
+  int k;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (k = 0; k < npairs; k++) {
+    const int i = pi[k], j = pj[k];
+    double cij = 0.0, qij = 0.0;
+    int s1, s2;
+    for (s1 = 0; s1 < N; s1++) {
+      int ai = ax[(int64_t)s1 * L + i], aj = ax[(int64_t)s1 * L + j];
+      int al = is_allowed(ai, aj, allow);
+      if (!al) { qij += 1.0; continue; }
+      for (s2 = s1 + 1; s2 < N; s2++) {
+        int bi = ax[(int64_t)s2 * L + i], bj = ax[(int64_t)s2 * L + j];
+        if (is_allowed(bi, bj, allow)) {
+          if      (ai != bi && aj != bj) cij += 2.0;
+          else if (ai != bi || aj != bj) cij += 1.0;
+        }
+      }
+    }
+    qij /= N;
+    cij /= (N > 1) ? (double)N * ((double)N - 1.0) : 1.0;
+    cij *= 2.0;
+    out[k] = cij - 1.0 * qij;
+  }
 }
 
 /* corr_CalculateRAFS, src/correlators.c:935-982 */

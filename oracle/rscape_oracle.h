@@ -171,6 +171,10 @@ double orc_faithful_rows(const uint8_t *ax, const double *wgt, int N, int L, int
                          int nthreads, double *checksum);
 double orc_faithful_raf(const uint8_t *ax, int N, int L, int npairs, int nthreads, double *checksum);
 
+/* RAF (the reference's O(N^2) loop) of listed pairs only, on the host threads */
+void   orc_raf_pairs(const uint8_t *ax, int N, int L, const double *allow, int npairs, const int *pi, const int *pj,
+                     double *out);
+
 /* ---- learned null (the library's own definitions; no reference counterpart) ----
  * feat[64] of ax [N][L] with weights w: the alignment features 0-46 of the
  * library's covgpu_features, computed here in FP64 in sequence order

@@ -113,6 +113,7 @@ def lib():
         L.covgpu_mlp_train.argtypes = [vp, f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_uint64,
                                        f32p]
         L.covgpu_resize.argtypes = [vp, C.c_int, C.c_int]
+        L.covgpu_autotune.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, f32p, C.POINTER(C.c_int)]
         L.covgpu_helices.argtypes = [i32p, C.c_int, C.c_int, C.POINTER(C.c_int), i32p, i32p, i32p]
         L.covgpu_aggregate.argtypes = [vp, C.c_int, C.c_int, i32p, f64p, vp, f64p, f64p]
         L.covgpu_learned_features.argtypes = [vp, C.POINTER(Params), C.c_double, C.c_int, C.c_int, f32p]
@@ -404,6 +405,14 @@ class Engine:
         self._ck(lib().covgpu_aggregate(self.h, method, len(helix_pvals), off, pv,
                                         ax.ctypes.data if ax is not None else None, pagg, Eagg))
         return pagg, Eagg
+
+    def autotune(self, nslots, first_slot=0, candidates=(4, 6, 8, 10, 12, 16, 24)):
+        """Pick the tensor count kernel's raster super-block on these alignments: (best, {size: ms})."""
+        cand = np.ascontiguousarray(candidates, dtype=np.int32)
+        ms = np.zeros(len(cand), dtype=np.float32)
+        best = C.c_int(0)
+        self._ck(lib().covgpu_autotune(self.h, first_slot, nslots, len(cand), cand.ctypes.data, ms, C.byref(best)))
+        return best.value, {int(c): float(m) for c, m in zip(cand, ms)}
 
     def flush_l2(self):
         self._ck(lib().covgpu_flush_l2(self.h))

@@ -84,6 +84,7 @@ struct covgpu_ctx {
   float* d_feat = nullptr;
   void* d_gsc = nullptr;       // GSC scratch, kept across calls
   size_t gsc_cap = 0;
+  double* d_pbscr = nullptr;   // position-based weights scratch
   bool want_qsum = false;     // covgpu_rscape keeps the null-score summary of type 0
   double qsum[17] = {0};
   bool have_qsum = false;
@@ -194,7 +195,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
   if (ctx->fitw) fitwork_destroy(ctx->fitw);
   void* sims[] = {ctx->d_simQ, ctx->d_simT, ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16, ctx->d_R, ctx->d_units,
                   ctx->d_simroot, ctx->d_simstate, ctx->d_nsubs, ctx->d_ndouble, ctx->d_njoin, ctx->d_featscr,
-                  ctx->d_feat, ctx->d_gsc};
+                  ctx->d_feat, ctx->d_gsc, ctx->d_pbscr};
   for (void* p : sims) if (p) cudaFree(p);
   for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
   if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -338,14 +339,13 @@ extern "C" int covgpu_weights_pb_dev(covgpu_ctx* ctx, int slot, int set, double*
   CK(cudaSetDevice(ctx->dev));
   const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
   if (slot < 0 || slot >= ctx->maxslots || !wgt) return fail(ctx, 11, "bad slot or output");
-  double *d_inv = nullptr, *d_w = nullptr;
-  CK(dalloc(&d_inv, (size_t)L * 4));
-  cudaError_t e = dalloc(&d_w, (size_t)N);
-  if (e == cudaSuccess) e = launch_weights_pb(ctx->d_ax + (size_t)slot * N * Lp, N, L, Lp, d_inv, d_w, ctx->st);
+  // scratch kept across calls (a cudaFree per call would synchronise the device)
+  if (!ctx->d_pbscr) CK(dalloc(&ctx->d_pbscr, (size_t)ctx->capL * 4 + ctx->capN));
+  double* d_inv = ctx->d_pbscr;
+  double* d_w = ctx->d_pbscr + (size_t)ctx->capL * 4;
+  cudaError_t e = launch_weights_pb(ctx->d_ax + (size_t)slot * N * Lp, N, L, Lp, d_inv, d_w, ctx->st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(wgt, d_w, N * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
-  cudaFree(d_inv);
-  if (d_w) cudaFree(d_w);
   if (e != cudaSuccess) return fail(ctx, 90, "CUDA error %s", cudaGetErrorString(e));
   // renormalised to sum to N (the sum in sequence order, as the reference)
   double sum = 0.0;
@@ -1255,6 +1255,34 @@ extern "C" int covgpu_aggregate(covgpu_ctx* ctx, int method, int nh, const int* 
   if (Eagg)
     for (int h = 0; h < nh; h++) Eagg[h] = (pagg[h] < 0.0) ? -1.0 : (double)nh * pagg[h];
   return 0;
+}
+
+// ------------------------------------------------------------------------
+// schedule autotuner for the tensor count kernel
+// ------------------------------------------------------------------------
+extern "C" int covgpu_autotune(covgpu_ctx* ctx, int first_slot, int nslots, int ncand, const int* cand, float* ms,
+                               int* best) {
+  CK(cudaSetDevice(ctx->dev));
+  static const int defaults[] = {4, 6, 8, 10, 12, 16, 24};
+  if (!cand || ncand <= 0) { cand = defaults; ncand = (int)(sizeof(defaults) / sizeof(defaults[0])); }
+  if (first_slot < 0 || nslots < 1 || first_slot + nslots > ctx->maxslots) return fail(ctx, 11, "slots out of range");
+  if (!ctx->have_w) return fail(ctx, 11, "weights not set");
+  if (!ctx->umma) {
+    ctx->umma = umma_plan_create(ctx->N, ctx->L, ctx->Lp, ctx->nT, ctx->d_tiles, ctx->ntiles, ctx->maxslots,
+                                 ctx->capN, ctx->capLp, ctx->capntiles);
+    if (!ctx->umma) return fail(ctx, 12, "tensor counting not available for this shape");
+    umma_set_weights(ctx->umma, ctx->h_w.data(), ctx->N, ctx->st);
+  }
+  const int64_t sstride = (int64_t)ctx->N * ctx->Lp;
+  std::vector<float> t(ncand, 0.f);
+  int b = 0;
+  const int s = umma_autotune(ctx->umma, ctx->d_ax + first_slot * sstride, sstride, nslots, ctx->d_cnt, ctx->st, cand,
+                              ncand, 3, t.data(), &b);
+  if (s) return fail(ctx, s, "autotune failed (%d)", s);
+  if (ms) for (int k = 0; k < ncand; k++) ms[k] = t[k];
+  if (best) *best = b;
+  ctx->counted = false;
+  return check_status(ctx);
 }
 
 extern "C" int covgpu_last_timing(const covgpu_ctx* ctx, double* ms5, int* nlaunch) {

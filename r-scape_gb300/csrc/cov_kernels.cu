@@ -1012,11 +1012,12 @@ cudaError_t launch_hist(const float2* cov, int64_t slot_stride, const TileRC* ti
   const BinC B = make_binc(bmin, w);
   wbase = std::max(0, std::min(wbase, nbcap - 1));
   const int nwin = std::min(HIST_WIN, nbcap - wbase);
-  static bool attr = false;
-  if (!attr) {
+  // once per process (thread-safe static initialisation)
+  static const bool attr = [] {
     cudaFuncSetAttribute(k_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, HIST_WIN * 4);
-    attr = true;
-  }
+    return true;
+  }();
+  (void)attr;
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);

@@ -71,6 +71,7 @@ struct UmmaPlan {
   CUtensorMap tmap;
   int* d_err = nullptr;
   int nsm = 152;
+  int sb = 10;                      // raster super-block (tiles per side), set by umma_autotune
   // capacity of the buffers (the plan can be resized within it)
   int capN = 0, capLp = 0, order_cap = 0;
   size_t ops_bytes = 0, ops8_bytes = 0;
@@ -489,14 +490,15 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
 // host side
 // ---------------------------------------------------------------------------
 static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // looked up once per process (thread-safe static initialisation)
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     cudaDriverEntryPointQueryResult q;
     void* p = nullptr;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-  }
+      return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    return (PFN_cuTensorMapEncodeTiled_v12000)nullptr;
+  }();
   return fn;
 }
 
@@ -513,6 +515,22 @@ static size_t smem_bytes(int nl) {
   return ring + stage_out + 1024;
 }
 
+// blocked raster: super-blocks of SB x SB tiles (I <= J) in turn, so the
+// CTAs resident at one time share a few operand row blocks in L2
+static bool set_order(UmmaPlan* p, int SB) {
+  const int nT = p->nT;
+  std::vector<int> order;
+  order.reserve(p->ntiles);
+  auto tindex = [nT](int I, int J) { return I * nT - I * (I - 1) / 2 + (J - I); };   // I-major tile list
+  for (int bI = 0; bI < nT; bI += SB)
+    for (int bJ = bI; bJ < nT; bJ += SB)
+      for (int I = bI; I < std::min(nT, bI + SB); I++)
+        for (int J = std::max(I, bJ); J < std::min(nT, bJ + SB); J++) order.push_back(tindex(I, J));
+  if ((int)order.size() != p->ntiles) return false;
+  p->sb = SB;
+  return cudaMemcpy(p->d_order, order.data(), sizeof(int) * p->ntiles, cudaMemcpyHostToDevice) == cudaSuccess;
+}
+
 // dimensions of the current alignments within the plan's buffers: tile
 // order, operand tensor maps; false when they do not fit
 static bool plan_dims(UmmaPlan* p, int N, int L, int Lp, int nT, int ntiles) {
@@ -522,18 +540,7 @@ static bool plan_dims(UmmaPlan* p, int N, int L, int Lp, int nT, int ntiles) {
       (size_t)rows * Npad * sizeof(__nv_bfloat16) > p->ops_bytes)
     return false;
   p->N = N; p->L = L; p->Lp = Lp; p->nT = nT; p->ntiles = ntiles; p->Npad = Npad;
-  // blocked raster: super-blocks of SB x SB tiles (I <= J) in turn, so the
-  // CTAs resident at one time share a few operand row blocks in L2
-  std::vector<int> order;
-  order.reserve(ntiles);
-  auto tindex = [nT](int I, int J) { return I * nT - I * (I - 1) / 2 + (J - I); };   // I-major tile list
-  constexpr int SB = 10;
-  for (int bI = 0; bI < nT; bI += SB)
-    for (int bJ = bI; bJ < nT; bJ += SB)
-      for (int I = bI; I < std::min(nT, bI + SB); I++)
-        for (int J = std::max(I, bJ); J < std::min(nT, bJ + SB); J++) order.push_back(tindex(I, J));
-  if ((int)order.size() != ntiles) return false;
-  if (cudaMemcpy(p->d_order, order.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice) != cudaSuccess) return false;
+  if (!set_order(p, p->sb)) return false;
   cuuint64_t gdim[2] = {(cuuint64_t)p->Npad, (cuuint64_t)rows};
   cuuint64_t gstride[1] = {(cuuint64_t)p->Npad * sizeof(__nv_bfloat16)};
   cuuint32_t box[2] = {UK, UM};
@@ -706,6 +713,40 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
         p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
   if (ev1) cudaEventRecord(ev1, st);
   return cudaGetLastError();
+}
+
+// Schedule autotuner: times the weighted count launch on the alignments at
+// hand for each raster super-block in cand[] (median of reps launches, CUDA
+// events on the stream) and keeps the fastest; ms[k] gets each time.
+int umma_autotune(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, float* cnt, cudaStream_t st,
+                  const int* cand, int ncand, int reps, float* ms, int* best_sb) {
+  cudaEvent_t a, b;
+  if (cudaEventCreate(&a) != cudaSuccess) return 90;
+  if (cudaEventCreate(&b) != cudaSuccess) { cudaEventDestroy(a); return 90; }
+  int best = p->sb;
+  float bt = INFINITY;
+  int status = 0;
+  for (int k = 0; k < ncand && !status; k++) {
+    if (cand[k] < 1 || !set_order(p, cand[k])) { status = 11; break; }
+    std::vector<float> t;
+    for (int r = 0; r < reps + 1 && !status; r++) {   // the first launch warms up
+      if (umma_count(p, ax, slot_stride, nslots, false, cnt, st, a, b) != cudaSuccess ||
+          cudaEventSynchronize(b) != cudaSuccess) { status = 90; break; }
+      float x = 0.f;
+      cudaEventElapsedTime(&x, a, b);
+      if (r) t.push_back(x);
+    }
+    if (status) break;
+    std::sort(t.begin(), t.end());
+    const float med = t[t.size() / 2];
+    if (ms) ms[k] = med;
+    if (med < bt) { bt = med; best = cand[k]; }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (!set_order(p, best) && !status) status = 90;
+  if (best_sb) *best_sb = best;
+  return status;
 }
 
 int umma_error(UmmaPlan* p) {

@@ -27,5 +27,9 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
 // error code recorded by the kernel (0 = none; 101-105 = a barrier wait
 // timed out); reading it resets it
 int         umma_error(UmmaPlan* p);
+// times the weighted count for each raster super-block size in cand and
+// keeps the fastest (0 ok, 11 bad candidate, 90 CUDA error)
+int         umma_autotune(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, float* cnt,
+                          cudaStream_t st, const int* cand, int ncand, int reps, float* ms, int* best_sb);
 
 }  // namespace covgpu

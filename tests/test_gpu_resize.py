@@ -45,3 +45,24 @@ def test_resize_rejects_larger_sizes(covgpu):
     with pytest.raises(RuntimeError):
         e.resize(100, 81)
     e.close()
+
+
+def test_autotuned_schedule_gives_identical_scores(covgpu):
+    """The autotuner only reorders the count kernel's tiles: every score is
+    bit-identical whatever raster it picks."""
+    N, L = 500, 700
+    s = covgpu.Synth(N, L, 1.4, 60, 6, 6, 12, 0.08, seed=5)
+    e = covgpu.Engine(N, L, maxslots=3, maxnull=2)
+    e.set_tree(s.parent, s.left, s.right)
+    e.set_weights(covgpu.weights_pb(s.ax))
+    e.set_alignment(0, s.ax)
+    e.make_nulls(42, 0, 2, 1)
+    e.score(["GTp", "MIp"], nslots=3, counter=covgpu.TENSOR)
+    before = [e.get_cov(k, q) for k in range(3) for q in range(2)]
+    best, ms = e.autotune(3, candidates=(2, 5, 10, 23))
+    assert best in (2, 5, 10, 23) and all(v > 0 for v in ms.values())
+    e.score(["GTp", "MIp"], nslots=3, counter=covgpu.TENSOR)
+    after = [e.get_cov(k, q) for k in range(3) for q in range(2)]
+    for a, b in zip(before, after):
+        assert np.array_equal(a, b)
+    e.close()
