@@ -230,9 +230,10 @@ typedef struct covgpu_mlp covgpu_mlp;
 int  covgpu_features(covgpu_ctx *ctx, int slot, double tree_len, float *feat);
 /* all 64 features of the alignment in slot 0: the alignment part and, in
  * 47-63, a summary of the scores of nquick null alignments of covtype (run
- * as covgpu_rscape with nshuffle = nquick): log of their number, mean, sd,
- * upper quantiles at survival 0.5 ... 0.0005, their tail fit (mu, log mean
- * excess, log shape) and the largest null score */
+ * as covgpu_rscape with nshuffle = nquick): 47 log of their number; 60-62
+ * their tail fit (mu_q, log m_q, log tau_q; m_q the mean excess); and as
+ * offsets from mu_q in units of m_q: 48 their mean, 49 their sd, 50-59 the
+ * upper quantiles at survival 0.5 ... 0.0005, 63 the largest score */
 int  covgpu_learned_features(covgpu_ctx *ctx, const covgpu_params *p, double tree_len, int covtype, int nquick,
                              float *feat);
 

@@ -822,10 +822,11 @@ static int bins_for(double bmin, double bmax, double w) {
 }
 
 // Summary of a null histogram (features 47-63 of the learned null): log of
-// the number of scores, their mean and deviation (bin midpoints), the upper
-// quantiles at survival 0.5 ... 0.0005 (linear within a bin), the tail fit
-// (mu, log mean excess, log shape; from the quantiles when the fit failed)
-// and the largest null score.
+// the number of scores; the tail fit mu_q, log m_q (m_q = tau/lambda, the
+// mean excess), log tau_q (from the quantiles when the fit failed); and,
+// as offsets from mu_q in units of m_q, the mean of the scores (bin
+// midpoints), their deviation, the upper quantiles at survival 0.5 ...
+// 0.0005 (linear within a bin) and the largest null score.
 static void null_summary(const ESL_HISTOGRAM* h, double xmax, double mu, double lambda, double tau, double* out) {
   static const double lev[10] = {0.5, 0.3, 0.1, 0.05, 0.03, 0.01, 0.005, 0.003, 0.001, 0.0005};
   double tot = 0.0, s1 = 0.0, s2 = 0.0;
@@ -863,6 +864,12 @@ static void null_summary(const ESL_HISTOGRAM* h, double xmax, double mu, double 
     out[15] = 0.0;
   }
   out[16] = xmax;
+  // the location features relative to the tail fit, in its own scale
+  const double m = exp(out[14]);
+  out[1] = (out[1] - out[13]) / m;
+  out[2] = out[2] / m;
+  for (int k = 0; k < 10; k++) out[3 + k] = (out[3 + k] - out[13]) / m;
+  out[16] = (out[16] - out[13]) / m;
 }
 
 extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint8_t* ax, const double* wgt,

@@ -108,6 +108,19 @@ class FamilyRun:
         self.e.close()
 
 
+def relative_summary(X):
+    """Quick-null features stored as absolute scores (mean 48, quantiles 50-59,
+    maximum 63; deviation 49) re-expressed as covgpu_learned_features gives
+    them: offsets from mu_q (60) in units of m_q = exp(61)."""
+    X = np.array(X, dtype=np.float64)
+    mq, m = X[:, 60:61], np.exp(X[:, 61:62])
+    X[:, 48:49] = (X[:, 48:49] - mq) / m
+    X[:, 49:50] = X[:, 49:50] / m
+    X[:, 50:60] = (X[:, 50:60] - mq) / m
+    X[:, 63:64] = (X[:, 63:64] - mq) / m
+    return X.astype(np.float32)
+
+
 def tail_of(r):
     """(mu, log(tau/lambda), log tau) of a gamma tail fit, or None."""
     lam, tau = r["lambda_"], r["tau"]
@@ -325,6 +338,8 @@ def main(argv=None):
     t = sub.add_parser("train")
     t.add_argument("--data", nargs="+", required=True)
     t.add_argument("--batch", type=int, default=256)
+    t.add_argument("--absolute-summary", action="store_true",
+                   help="the data files hold the quick-null summary as absolute scores (older files)")
     t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--out", required=True)
     e = sub.add_parser("eval")
@@ -344,6 +359,8 @@ def main(argv=None):
         zs = [np.load(p) for p in a.data]
         X = np.concatenate([z["X"] for z in zs])
         T = np.concatenate([z["T"] for z in zs])
+        if a.absolute_summary:
+            X = relative_summary(X)
         net, info = train_selected(X, T, batch=a.batch, lr=a.lr, log=sys.stderr)
         nq = {int(z["nquick"]) for z in zs if "nquick" in z}
         if len(nq) != 1:

@@ -50,13 +50,16 @@ def test_quick_null_summary(covgpu):
     r = e.rscape(None, None, ["GTp"], nshuffle=nq)[0]
     P = L * (L - 1) // 2
     assert f[47] == pytest.approx(np.log(nq * P), rel=1e-6)
-    q = f[50:60]                         # survival 0.5 ... 0.0005: increasing scores
-    assert np.all(np.diff(q) >= 0) and q[0] >= f[48] - 3 * f[49]
     assert f[60] == pytest.approx(r["mu"], rel=1e-6)
     assert f[61] == pytest.approx(np.log(r["tau"] / r["lambda_"]), rel=1e-5, abs=1e-6)
     assert f[62] == pytest.approx(np.log(r["tau"]), rel=1e-5, abs=1e-6)
-    assert f[63] == pytest.approx(r["h_xmax"], rel=1e-6)
-    assert q[-1] <= f[63] + r["w"]
+    m = r["tau"] / r["lambda_"]
+    q = f[50:60]                         # survival 0.5 ... 0.0005: increasing offsets from mu_q
+    assert np.all(np.diff(q) >= 0) and q[0] >= f[48] - 3 * f[49]
+    # the tail's lower bound mu_q is the 0.0005 quantile's bin, within a bin width
+    assert abs(q[-1]) * m <= r["w"] * (1 + 1e-6)
+    assert f[63] == pytest.approx((r["h_xmax"] - r["mu"]) / m, rel=1e-5, abs=1e-6)
+    assert q[-1] <= f[63] + r["w"] / m
     e.close()
 
 

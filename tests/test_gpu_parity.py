@@ -250,3 +250,30 @@ def test_tensor_pipeline_same_pairs(covgpu, oracle):
     assert sorted((i, j) for (i, j, sc, E, p) in tens["hits"]) == exp
     assert sorted((i, j) for (i, j, sc, E, p) in simt["hits"]) == exp
     e.close()
+
+
+@pytest.mark.parametrize("seed", [2, 42])
+@pytest.mark.parametrize("counter", ["simt", "tensor"])
+def test_small_rna_workload(covgpu, oracle, counter, seed):
+    """The reference-scale CPU workload end to end: N=100 x L=120, coalescent
+    tree of length 1.5, three helices of 10 base pairs, 8% gaps in runs of
+    mean 3, position-based FP64 weights, GTp with APC, 20 null alignments.
+    The pairs with E < 10 and their E-values are the oracle's (so is the
+    E < 0.05 list among them, which this recipe keeps short)."""
+    N, L, ns = 100, 120, 20
+    s = covgpu.Synth(N, L, 1.5, 30, 3, 10, 10, 0.08, gap_mean=3.0, seed=seed, tree_kind=0)
+    assert covgpu.gapfilter(s.ax, None, 0.75).all()
+    w = covgpu.weights_pb(s.ax)
+    e = covgpu.Engine(N, L, maxslots=ns + 1, maxnull=ns)
+    e.set_tree(s.parent, s.left, s.right)
+    g = e.rscape(s.ax, w, ["GTp"], thresh=10.0, counter=covgpu.TENSOR if counter == "tensor" else covgpu.SIMT)[0]
+    e.close()
+    assert g["nshuffle"] == ns          # R-scape's rule gives 20 nulls at this size
+    ref = oracle.rscape(s.ax, w, oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd), covtype="GTp",
+                        nshuffle=ns, thresh=10.0)
+    gh = {(i, j): E for (i, j, sc, E, p) in g["hits"]}
+    rh = {(i, j): E for (i, j, sc, E, p) in ref["hits"]}
+    assert set(gh) == set(rh) and len(rh) > 0
+    for k in rh:
+        assert abs(gh[k] - rh[k]) <= 1e-3 * rh[k]
+    assert {k for k in gh if gh[k] < 0.05} == {k for k in rh if rh[k] < 0.05}
