@@ -92,26 +92,17 @@ constexpr uint32_t TAG_FLEAF = 0x11u, TAG_FCHOOSE = 0x12u, TAG_COLPERM = 0x13u, 
 // written as o ln(o/e) - (o - e) = e g((o-e)/e).  For |d| < 1/4,
 // g(d) = d^2 h(d) with h(d) = sum_m (-d)^m / ((m+1)(m+2)) replaced by its
 // degree-7 Chebyshev fit on [-1/4, 1/4] (fit error 3e-9 relative, below the
-// FP32 rounding of the Horner evaluation, 7e-8, as with the full series);
-// the closed form beyond.
-__device__ __forceinline__ float gfun(float d) {
-  if (fabsf(d) < 0.25f) {
-    float s = -1.525888499e-02f;
-    s = fmaf(s, d, 1.933413558e-02f);
-    s = fmaf(s, d, -2.374382876e-02f);
-    s = fmaf(s, d, 3.327445686e-02f);
-    s = fmaf(s, d, -5.000115186e-02f);
-    s = fmaf(s, d, 8.333407342e-02f);
-    s = fmaf(s, d, -1.666666567e-01f);
-    s = fmaf(s, d, 0.5f);
-    return d * d * s;
-  }
-  return (1.f + d) * log1pf(d) - d;
-}
-
-// g(o/e - 1) evaluated from the ratio when o << e (1 + d underflows)
-__device__ __forceinline__ float gfun_ratio(float r) {
-  return (r > 0.f) ? r * logf(r) - (r - 1.f) : 1.f;
+// FP32 rounding of the Horner evaluation, 7e-8, as with the full series).
+__device__ __forceinline__ float gfun_poly(float d) {
+  float s = -1.525888499e-02f;
+  s = fmaf(s, d, 1.933413558e-02f);
+  s = fmaf(s, d, -2.374382876e-02f);
+  s = fmaf(s, d, 3.327445686e-02f);
+  s = fmaf(s, d, -5.000115186e-02f);
+  s = fmaf(s, d, 8.333407342e-02f);
+  s = fmaf(s, d, -1.666666567e-01f);
+  s = fmaf(s, d, 0.5f);
+  return d * d * s;
 }
 
 __device__ __forceinline__ double warp_sum_d(double v) {

@@ -218,7 +218,11 @@ k_gam_fit(FitGrid g, double s00, double s01) {
   if (!fit_eval(g, pts, 0, phase, F, red, &flag)) status = 2;
 
   // ---- phase 1: Newton ----
-  constexpr double H = 1e-5;
+  // Steps below kNewtonTol in (log lambda, log tau) end the search: the
+  // 6-point stencil's gradient carries the FP64 rounding of -log L (~1e-16
+  // |F|) divided by H, which for tails of ~1e5 scores puts the smallest
+  // reachable step near 1e-11-1e-10; the oracle's Nelder-Mead stops at ~1e-8.
+  constexpr double H = 1e-5, kNewtonTol = 1e-9;
   double th0 = s00, th1 = s01;               // thread 0's state
   double bth0 = s00, bth1 = s01, bF = INFINITY;
   double d0 = 0.0, d1 = 0.0;                 // last step
@@ -242,7 +246,7 @@ k_gam_fit(FitGrid g, double s00, double s01) {
         // the step raised -log L (or gave NaN): back off towards the best point
         d0 *= 0.5; d1 *= 0.5;
         th0 = bth0 + d0; th1 = bth1 + d1;
-        if (fabs(d0) < 1e-10 && fabs(d1) < 1e-10) { th0 = bth0; th1 = bth1; converged = 1; ctl = 0; }
+        if (fabs(d0) < kNewtonTol && fabs(d1) < kNewtonTol) { th0 = bth0; th1 = bth1; converged = 1; ctl = 0; }
       } else {
         bth0 = th0; bth1 = th1; bF = F0;
         const double g0 = (F[1] - F[2]) / (2.0 * H), g1 = (F[3] - F[4]) / (2.0 * H);
@@ -258,7 +262,7 @@ k_gam_fit(FitGrid g, double s00, double s01) {
         }
         const double m = fmax(fabs(d0), fabs(d1));
         if (m > 1.0) { d0 /= m; d1 /= m; }
-        if (m < 1e-10) { converged = 1; ctl = 0; }
+        if (m < kNewtonTol) { converged = 1; ctl = 0; }
         else { th0 = bth0 + d0; th1 = bth1 + d1; }
       }
     }

@@ -405,11 +405,22 @@ __device__ __forceinline__ float diff_oe(float c, float dc, df e) {
   return s.hi + (s.lo + (dc - e.lo));
 }
 
-// G-test term e*g(u/e); o = c + dc when the ratio form is needed
-__device__ __forceinline__ float gterm_f(float u, float e, float o) {
+// G-test term e*g(d), d = u/e: for |d| < 1/4 the polynomial gfun_poly,
+// elsewhere (1+d) log1p(d) - d.  Below d = -1/4 the product (1+d) log1p(d)
+// carries the rounding of 1 + d, but where that matters (o << e: empty
+// cells) the product is negligible next to -d, so one form serves both
+// sides; at d = -1 (1 + d rounds to 0) the product is taken as 0.  Both
+// forms are evaluated and one is selected: a warp holds pairs whose cells
+// fall on both sides, and a branch would make every warp run every path.
+__device__ __forceinline__ float gterm_f(float u, float e) {
   const float d = __fdividef(u, e);
-  if (d > -0.25f) return e * gfun(d);
-  return e * gfun_ratio(__fdividef(o, e));
+  const float dn = fminf(fmaxf(d, -0.25f), 0.25f);     // the polynomial only where it is used
+  const float near = gfun_poly(dn);
+  const float dp = fmaxf(d, -1.f);
+  const float a = 1.f + dp;
+  const float l = log1pf(fmaxf(dp, -0.99999994f));     // finite where a rounds to 0
+  const float far = ((a > 0.f) ? a * l : 0.f) - dp;
+  return e * ((fabsf(d) < 0.25f) ? near : far);
 }
 
 struct PairOut { float chi, gt, mi, mir, mig, omes; df raf, ccf; };
@@ -522,7 +533,7 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
           const df e = df_mul(ax, {pmj[y].x, pmj[y].y});
           const float u = diff_oe(C, dc, e);
           if (e.hi > 0.f) {
-            if (CF & CF_G) { gsum += gterm_f(u, e.hi, o); usum += u; }
+            if (CF & CF_G) { gsum += gterm_f(u, e.hi); usum += u; }
             if (CF & CF_CHI) chi += __fdividef(u * u, e.hi);
             if (CF & CF_OMES) omes += u * u;
           }
@@ -561,8 +572,8 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
     const float un = diff_oe(Cn.hi, Cn.lo + dn, en);
     const float ow = Cw.hi + (Cw.lo + dw), on = Cn.hi + (Cn.lo + dn);
     float g = 0.f, chi = 0.f, om = 0.f;
-    if (ew.hi > 0.f) { g += gterm_f(uw, ew.hi, ow); chi += __fdividef(uw * uw, ew.hi); om += uw * uw; }
-    if (en.hi > 0.f) { g += gterm_f(un, en.hi, on); chi += __fdividef(un * un, en.hi); om += un * un; }
+    if (ew.hi > 0.f) { g += gterm_f(uw, ew.hi); chi += __fdividef(uw * uw, ew.hi); om += uw * uw; }
+    if (en.hi > 0.f) { g += gterm_f(un, en.hi); chi += __fdividef(un * un, en.hi); om += un * un; }
     const float pw = ow * inv_ne, pn = on * inv_ne;
     float hh = 0.f;
     hh -= (pw > 0.f) ? pw * __logf(pw) : 0.f;
