@@ -405,21 +405,22 @@ __device__ __forceinline__ float diff_oe(float c, float dc, df e) {
   return s.hi + (s.lo + (dc - e.lo));
 }
 
-// G-test term e*g(d), d = u/e: for |d| < 1/4 the polynomial gfun_poly,
-// elsewhere (1+d) log1p(d) - d.  Below d = -1/4 the product (1+d) log1p(d)
-// carries the rounding of 1 + d, but where that matters (o << e: empty
-// cells) the product is negligible next to -d, so one form serves both
-// sides; at d = -1 (1 + d rounds to 0) the product is taken as 0.  Both
-// forms are evaluated and one is selected: a warp holds pairs whose cells
-// fall on both sides, and a branch would make every warp run every path.
-__device__ __forceinline__ float gterm_f(float u, float e) {
+// G-test term e*g(d), d = u/e, o = c + dc: for |d| < 1/4 the polynomial
+// gfun_poly, elsewhere r ln r - (r - 1) with r = 1 + d, as
+// r log1p(d) - d.  Below zero r is the quotient o/e (relative error 2^-22,
+// so r ln r is off by at most 2.4e-7 r |ln r| <= 9e-8), not 1 + d: for
+// empty cells (r ~ 1e-10) 1 + d rounds to a multiple of 2^-24 and, times
+// log1p(d) ~ -20, would add ~1e-6 e per cell.  Both forms are evaluated and
+// one is selected: a warp holds pairs whose cells fall on both sides, and a
+// branch would make every warp run every path.
+__device__ __forceinline__ float gterm_f(float u, float e, float o) {
   const float d = __fdividef(u, e);
   const float dn = fminf(fmaxf(d, -0.25f), 0.25f);     // the polynomial only where it is used
   const float near = gfun_poly(dn);
   const float dp = fmaxf(d, -1.f);
-  const float a = 1.f + dp;
-  const float l = log1pf(fmaxf(dp, -0.99999994f));     // finite where a rounds to 0
-  const float far = ((a > 0.f) ? a * l : 0.f) - dp;
+  const float r = (d < 0.f) ? __fdividef(o, e) : 1.f + dp;
+  const float l = log1pf(fmaxf(dp, -0.99999994f));     // finite where 1 + d rounds to 0
+  const float far = r * l - dp;
   return e * ((fabsf(d) < 0.25f) ? near : far);
 }
 
@@ -533,7 +534,7 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
           const df e = df_mul(ax, {pmj[y].x, pmj[y].y});
           const float u = diff_oe(C, dc, e);
           if (e.hi > 0.f) {
-            if (CF & CF_G) { gsum += gterm_f(u, e.hi); usum += u; }
+            if (CF & CF_G) { gsum += gterm_f(u, e.hi, o); usum += u; }
             if (CF & CF_CHI) chi += __fdividef(u * u, e.hi);
             if (CF & CF_OMES) omes += u * u;
           }
@@ -572,8 +573,8 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
     const float un = diff_oe(Cn.hi, Cn.lo + dn, en);
     const float ow = Cw.hi + (Cw.lo + dw), on = Cn.hi + (Cn.lo + dn);
     float g = 0.f, chi = 0.f, om = 0.f;
-    if (ew.hi > 0.f) { g += gterm_f(uw, ew.hi); chi += __fdividef(uw * uw, ew.hi); om += uw * uw; }
-    if (en.hi > 0.f) { g += gterm_f(un, en.hi); chi += __fdividef(un * un, en.hi); om += un * un; }
+    if (ew.hi > 0.f) { g += gterm_f(uw, ew.hi, ow); chi += __fdividef(uw * uw, ew.hi); om += uw * uw; }
+    if (en.hi > 0.f) { g += gterm_f(un, en.hi, on); chi += __fdividef(un * un, en.hi); om += un * un; }
     const float pw = ow * inv_ne, pn = on * inv_ne;
     float hh = 0.f;
     hh -= (pw > 0.f) ? pw * __logf(pw) : 0.f;
