@@ -405,8 +405,20 @@ def main():
     kname = "k_count_umma" if kind == "tensor" else "k_count_simt"
     traffic = profile_traffic(kname)
     if args.no_extras:
-        cpu_v, cpu_sample, sim, fam, bnull = None, "skipped (--no-extras)", None, None, None
+        cpu_v, cpu_sample, sim, fam, bnull, plain = None, "skipped (--no-extras)", None, None, None, None
     else:
+        plain = None
+        if counter == 1:
+            # the plain SIMT counting path on the same workload, once: its step
+            # time and whether it gives the same E < 0.05 pair lists
+            e.flush_l2()
+            rs = e.rscape(None, None, TYPES, nshuffle=ns, counter=0)
+            ms_s = e.last_timing()[0][4]
+            same = all(sorted((h[0], h[1]) for h in a["hits"]) == sorted((h[0], h[1]) for h in b["hits"])
+                       for a, b in zip(res, rs))
+            plain = {"counter": "simt", "ms_per_step": ms_s, "value": pairs_step / (ms_s / 1000.0),
+                     "tensor_speedup": ms_s / (step_s * 1000.0), "same_pair_sets": same,
+                     "pairs_e_lt_thresh": [len(x["hits"]) for x in rs]}
         cpu_v, cpu_sample, _ = cpu_reference(ax, w, args.cpu_budget, threads)
         sim = simulator_rate(cg, e, s, N, L, ns)
         fam = ragged_families(cg, args.families, counter, local, args.family_workers) if args.families > 0 else None
@@ -429,6 +441,7 @@ def main():
                          "sample": cpu_sample},
         "hits": [len(x["hits"]) for x in res],
         "simulator": sim,
+        "plain_gpu": plain,
         "autotune": tune,
         "ragged_families": fam,
         "batched_nulls": bnull,
