@@ -4,17 +4,23 @@
 //   C = X^T diag(w) X,   X[s, 4i+x] = [a_si == x]  (x = A,C,G,U; gaps and
 //                                                    unknown residues: 0)
 // of mutual_naive_ppij (src/correlators.c:1695-1780) for all pairs at once.
-// Operands, K-major (sequences contiguous), BF16:
+// Operands, K-major (sequences contiguous):
 //   A      = X^T                         (0/1, exact)
 //   B_l    = l_l(s) X^T,  l = 0..nl-1     weight limbs: each weight is
-//            quantised to q_s = round(w_s 2^E) < 2^24 and split into 8-bit
-//            limbs q = l0 + 2^8 l1 + 2^16 l2 (integers <= 255, exact in BF16)
+//            quantised to q_s = round(w_s 2^E) and split into limbs
+//   * N <= 8196: q < 2^22, two 11-bit limbs q = l0 + 2^11 l1 (integers
+//     <= 2047, exact in FP16), FP16 operands;
+//   * larger N: q < 2^24, three 8-bit limbs q = l0 + 2^8 l1 + 2^16 l2
+//     (integers <= 255, exact in BF16), BF16 operands.
 // Each limb accumulates in its own FP32 TMEM accumulator, where the sum
-// (<= 255 N < 2^24 for N <= 65536) is an exact integer; the epilogue adds
-// D0 + 2^8 D1 + 2^16 D2 with error-free FP32 sums (two_sum) and one final
+// (<= 2047 N or 255 N, below 2^24 in both cases) is an exact integer; the
+// epilogue adds the limbs with error-free FP32 sums (two_sum) and one final
 // rounding, so each count is within one FP32 rounding of the exact count of
 // the quantised weights, times the power of two 2^-E, with no FP64 and no
-// integer conversion on the path (exact integers under unit weights).
+// integer conversion on the path (exact integers under unit weights).  Two
+// FP16 limbs carry a third less MMA work and operand traffic than three
+// BF16 ones, and their two accumulators (256 TMEM columns) leave room for a
+// second set, so the epilogue of one tile overlaps the MMAs of the next.
 //
 // Operand rows are state-major inside each 32-column tile
 // (row = 128 tile + 32 x + column), so accumulator row m = 32 x + a and
@@ -37,6 +43,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -61,12 +68,12 @@ struct UmmaPlan {
   int Npad = 0;                  // sequences padded to UK
   const TileRC* d_tiles = nullptr;
   int* d_order = nullptr;           // launch order of the tiles (blocked raster)
-  __nv_bfloat16* d_ops = nullptr;   // [(1 + 3) * maxslots * 4Lp][Npad]
+  __nv_bfloat16* d_ops = nullptr;   // [(1 + 3) * maxslots * 4Lp][Npad] (FP16 bits with two limbs)
   uint8_t* d_ops8 = nullptr;        // [maxslots * 4Lp][Npad8] FP8 E4M3 one-hot (unit weights)
   int Npad8 = 0;                    // sequences padded to UK8
   CUtensorMap tmap8;
-  uint8_t* d_limbs = nullptr;       // [3][Npad] weight limbs
-  int nl = 3;                       // limbs in use (1 when all weights are equal)
+  uint16_t* d_limbs = nullptr;      // [3][Npad] weight limbs
+  int nl = 3;                       // limbs in use (1 when all weights are equal; 2: FP16 operands)
   double scale = 1.0;               // count = limb sum * scale
   CUtensorMap tmap;
   int* d_err = nullptr;
@@ -144,6 +151,12 @@ __host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// instruction descriptor, kind::f16: F16 x F16 -> F32, both K-major (A and
+// B formats 0 = F16)
+__host__ __device__ constexpr uint32_t make_idesc_fp16(int M, int N) {
+  return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 // instruction descriptor, kind::f8f6f4: E4M3 x E4M3 -> F32, both K-major
 __host__ __device__ constexpr uint32_t make_idesc_e4m3(int M, int N) {
   return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
@@ -199,15 +212,22 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
-// operand preparation: codes [slot][N][Lp] -> BF16 one-hot rows [4Lp][Npad]
-// (A) and limb-scaled rows (B_l), row 128 t + 32 x + c for column 32 t + c
-// and state x; one CTA per (64 sequences, 32 columns, slot)
+// operand preparation: codes [slot][N][Lp] -> one-hot rows [4Lp][Npad] (A)
+// and limb-scaled rows (B_l), FP16 (HALF) or BF16, row 128 t + 32 x + c for
+// column 32 t + c and state x; one CTA per (64 sequences, 32 columns, slot)
 // ---------------------------------------------------------------------------
+template <bool HALF>
+__device__ __forceinline__ uint16_t op_bits(float v) {
+  if (HALF) return __half_as_ushort(__float2half_rn(v));
+  return __bfloat16_as_ushort(__float2bfloat16(v));
+}
+
+template <bool HALF>
 __global__ void __launch_bounds__(256)
 k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, int Npad, int nslots, int nl,
-            const uint8_t* __restrict__ limbs, bool unit, __nv_bfloat16* __restrict__ ops) {
+            const uint16_t* __restrict__ limbs, bool unit, uint16_t* __restrict__ ops) {
   __shared__ uint8_t cs[64][33];
-  __shared__ uint8_t lb[3][64];
+  __shared__ uint16_t lb[3][64];
   const int s0 = blockIdx.x * 64, c0 = blockIdx.y * 32, slot = blockIdx.z, tid = threadIdx.x;
   const uint8_t* A = ax + (int64_t)slot * slot_stride;
   for (int e = tid; e < 64 * 32; e += 256) {
@@ -220,24 +240,27 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
   // 128 rows (4 states x 32 columns, state-major) x 64 sequences; each
   // thread writes 8 consecutive sequences (16 bytes) of one row
   const int64_t rows_per_buf = (int64_t)nslots * 4 * Lp;
+  const uint16_t one = op_bits<HALF>(1.f), zero = op_bits<HALF>(0.f);
   for (int e = tid; e < 128 * 8; e += 256) {
     const int r = e / 8, chunk = e % 8;
     const int x = r / 32, c = r % 32;
     const int64_t row = (int64_t)slot * 4 * Lp + 4 * c0 + r;
-    __align__(16) __nv_bfloat16 va[8];
-    __align__(16) __nv_bfloat16 vb[3][8];
+    __align__(16) uint16_t va[8];
+    __align__(16) uint16_t vb[3][8];
 #pragma unroll
     for (int k = 0; k < 8; k++) {
       const int s = chunk * 8 + k;
       const bool on = (cs[s][c] == x);
-      va[k] = __float2bfloat16(on ? 1.f : 0.f);
+      va[k] = on ? one : zero;
 #pragma unroll
-      for (int l = 0; l < 3; l++) vb[l][k] = __float2bfloat16((on && l < nl) ? (float)lb[l][s] : 0.f);
+      for (int l = 0; l < 3; l++) vb[l][k] = (on && l < nl) ? op_bits<HALF>((float)lb[l][s]) : zero;
     }
     *reinterpret_cast<uint4*>(ops + row * Npad + s0 + chunk * 8) = *reinterpret_cast<uint4*>(va);
-    for (int l = 0; l < nl; l++)
-      *reinterpret_cast<uint4*>(ops + ((1 + l) * rows_per_buf + row) * Npad + s0 + chunk * 8) =
-          *reinterpret_cast<uint4*>(vb[l]);
+#pragma unroll
+    for (int l = 0; l < 3; l++)   // compile-time limb index: the arrays stay in registers
+      if (l < nl)
+        *reinterpret_cast<uint4*>(ops + ((1 + l) * rows_per_buf + row) * Npad + s0 + chunk * 8) =
+            *reinterpret_cast<uint4*>(vb[l]);
   }
 }
 
@@ -361,7 +384,7 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
   } else if (warp == 1) {
     if (lane == 0) {
       // ---- MMA issuer ----
-      constexpr uint32_t idesc = F8 ? make_idesc_e4m3(UM, UN) : make_idesc(UM, UN);
+      constexpr uint32_t idesc = F8 ? make_idesc_e4m3(UM, UN) : (NL == 2 ? make_idesc_fp16(UM, UN) : make_idesc(UM, UN));
       uint32_t g = 0;
       int i = 0;
       for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x, i++) {
@@ -434,12 +457,14 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
             const float p = c * s_hi;
             v[k] = p + (fmaf(c, s_hi, -p) + c * s_lo);
           } else {
-            // D0 + 2^8 D1 + 2^16 D2 with two error-free sums (each limb sum
-            // is an exact integer, the scalings are exact): within one
-            // rounding of the exact count, all on the FP32 pipe
+            // D0 + B D1 + B^2 D2 (B = 2^11 for two FP16 limbs, 2^8 for three
+            // BF16 ones) with two error-free sums (each limb sum is an
+            // exact integer, the scalings are exact): within one rounding
+            // of the exact count, all on the FP32 pipe
+            constexpr float LB = (NL == 2) ? 2048.f : 256.f;
             const float c0 = __uint_as_float(d[0][k]);
-            const float c1 = __uint_as_float(d[1][k]) * 256.f;
-            const float c2 = (NL > 2) ? __uint_as_float(d[NL > 2 ? 2 : 0][k]) * 65536.f : 0.f;
+            const float c1 = __uint_as_float(d[1][k]) * LB;
+            const float c2 = (NL > 2) ? __uint_as_float(d[NL > 2 ? 2 : 0][k]) * (LB * LB) : 0.f;
             const float s1 = c2 + c1;
             const float b1 = s1 - c2;
             const float e1 = (c2 - (s1 - b1)) + (c1 - b1);
@@ -503,13 +528,15 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 }
 
 constexpr int STAGES3 = 3;   // 3 limbs: 64 KB per stage
+constexpr int STAGES2 = 4;   // 2 limbs: 48 KB per stage
 constexpr int STAGES1 = 4;   // 1 limb : 32 KB per stage
 
 constexpr int ACC3 = 1;      // 3 limbs: 384 TMEM columns, one accumulator set
+constexpr int ACC2 = 2;      // 2 limbs: two 256-column sets, epilogue overlapped
 constexpr int ACC1 = 2;      // 1 limb : two 128-column sets, epilogue overlapped
 
 static size_t smem_bytes(int nl) {
-  const int stages = (nl == 1) ? STAGES1 : STAGES3;
+  const int stages = (nl == 1) ? STAGES1 : (nl == 2 ? STAGES2 : STAGES3);
   const size_t ring = (size_t)stages * TILE_BYTES * (1 + nl);
   const size_t stage_out = (size_t)4 * 8192;   // two 4 KB buffers per epilogue warp
   return ring + stage_out + 1024;
@@ -573,7 +600,7 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
   p->ops_bytes = (size_t)rows_cap * Npad_cap * sizeof(__nv_bfloat16);
   if (cudaMalloc(&p->d_ops, p->ops_bytes) != cudaSuccess) { p->d_ops = nullptr; umma_plan_destroy(p); return nullptr; }
   if (cudaMemset(p->d_ops, 0, p->ops_bytes) != cudaSuccess ||
-      cudaMalloc(&p->d_limbs, (size_t)3 * Npad_cap) != cudaSuccess ||
+      cudaMalloc(&p->d_limbs, (size_t)3 * Npad_cap * sizeof(uint16_t)) != cudaSuccess ||
       cudaMalloc(&p->d_order, sizeof(int) * std::max(1, capntiles)) != cudaSuccess ||
       cudaMalloc(&p->d_err, sizeof(int)) != cudaSuccess) {
     umma_plan_destroy(p);
@@ -583,6 +610,8 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
   if (!plan_dims(p, N, L, Lp, nT, ntiles)) { umma_plan_destroy(p); return nullptr; }
   cudaFuncSetAttribute(k_count_umma<3, STAGES3, ACC3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes(3));
+  cudaFuncSetAttribute(k_count_umma<2, STAGES2, ACC2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem_bytes(2));
   cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes(1));
   cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -609,28 +638,37 @@ void umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t st) {
   double wmax = 0.0;
   bool equal = true;
   for (int s = 0; s < N; s++) { wmax = std::max(wmax, wgt[s]); if (wgt[s] != wgt[0]) equal = false; }
-  std::vector<uint8_t> lim((size_t)3 * p->Npad, 0);
+  std::vector<uint16_t> lim((size_t)3 * p->Npad, 0);
   if (equal || wmax <= 0.0) {
     p->nl = 1;
     p->scale = (N > 0) ? wgt[0] : 1.0;
     for (int s = 0; s < N; s++) lim[s] = 1;
   } else {
-    // q = round(w 2^E) < 2^24
+    // q = round(w 2^E) < 2^bits: two 11-bit limbs while 2047 N < 2^24 (the
+    // FP32 limb sums stay exact), else three 8-bit limbs
+    const bool two = (N <= 8196);
+    const int bits = two ? 22 : 24;
     int e2;
     std::frexp(wmax, &e2);                 // wmax = f 2^e2, f in [0.5,1)
-    const int E = 24 - e2;                 // wmax 2^E < 2^24
-    p->nl = 3;
+    const int E = bits - e2;               // wmax 2^E < 2^bits
+    p->nl = two ? 2 : 3;
     p->scale = std::ldexp(1.0, -E);
+    const double qmax = std::ldexp(1.0, bits) - 1.0;
     for (int s = 0; s < N; s++) {
       double qd = std::nearbyint(std::ldexp(wgt[s], E));
-      if (qd > 16777215.0) qd = 16777215.0;
+      if (qd > qmax) qd = qmax;
       const uint32_t q = (uint32_t)qd;
-      lim[s] = (uint8_t)(q & 255u);
-      lim[p->Npad + s] = (uint8_t)((q >> 8) & 255u);
-      lim[2 * (size_t)p->Npad + s] = (uint8_t)(q >> 16);
+      if (two) {
+        lim[s] = (uint16_t)(q & 2047u);
+        lim[p->Npad + s] = (uint16_t)(q >> 11);
+      } else {
+        lim[s] = (uint16_t)(q & 255u);
+        lim[p->Npad + s] = (uint16_t)((q >> 8) & 255u);
+        lim[2 * (size_t)p->Npad + s] = (uint16_t)(q >> 16);
+      }
     }
   }
-  cudaMemcpyAsync(p->d_limbs, lim.data(), lim.size(), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(p->d_limbs, lim.data(), lim.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, st);
   cudaStreamSynchronize(st);
 }
 
@@ -698,8 +736,12 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
   }
   const int nl = p->nl;
   dim3 pg(p->Npad / 64, p->Lp / 32, nslots);
-  k_umma_prep<<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, nl, p->d_limbs, false,
-                                  p->d_ops);
+  if (nl == 2)
+    k_umma_prep<true><<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, nl, p->d_limbs, false,
+                                          reinterpret_cast<uint16_t*>(p->d_ops));
+  else
+    k_umma_prep<false><<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, nl, p->d_limbs, false,
+                                           reinterpret_cast<uint16_t*>(p->d_ops));
   const int nkb = p->Npad / UK;
   // the scale as an unevaluated FP32 pair (a power of two with limbs)
   const double scale = p->scale;
@@ -707,6 +749,9 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
   if (ev0) cudaEventRecord(ev0, st);
   if (nl == 1)
     k_count_umma<1, STAGES1, ACC1, false><<<grid, 192, smem_bytes(1), st>>>(
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
+  else if (nl == 2)
+    k_count_umma<2, STAGES2, ACC2, false><<<grid, 192, smem_bytes(2), st>>>(
         p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
   else
     k_count_umma<3, STAGES3, ACC3, false><<<grid, 192, smem_bytes(3), st>>>(
