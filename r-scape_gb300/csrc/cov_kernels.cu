@@ -818,16 +818,18 @@ k_hist(const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __rest
   const int tid = threadIdx.x, a = tid >> 5, b = tid & 31;
   for (int k = tid; k < nwin; k += blockDim.x) sh[k] = 0u;
   __syncthreads();
-  const int64_t nitems = (int64_t)ntiles * nslots, G = gridDim.x;
-  for (int64_t base = blockIdx.x; base < nitems; base += HIST_UNROLL * G) {
+  // items (slot, tile) in 32-bit arithmetic: ntiles * nslots < 2^31 (the
+  // host checks), and 64-bit division is emulated in software
+  const int nitems = ntiles * nslots, G = gridDim.x;
+  for (int base = blockIdx.x; base < nitems; base += HIST_UNROLL * G) {
     float2 v[HIST_UNROLL];
     bool ok[HIST_UNROLL];
 #pragma unroll
     for (int u = 0; u < HIST_UNROLL; u++) {
-      const int64_t it = base + u * G;
+      const int it = base + u * G;
       ok[u] = false;
       if (it < nitems) {
-        const int t = (int)(it % ntiles), slot = (int)(it / ntiles);
+        const int slot = it / ntiles, t = it - slot * ntiles;
         const TileRC tr = tiles[t];
         const int i = tr.I * TP + a, j = tr.J * TP + b;
         ok[u] = (i < j && j < L);
@@ -841,12 +843,13 @@ k_hist(const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __rest
         bin = bin_clamped({v[u].x, v[u].y}, B);
         if (bin < 0 || bin >= nbcap) { atomicExch(status, 4); bin = -1; }
       }
-      // one atomic per distinct bin of the warp
-      const unsigned grp = __match_any_sync(0xffffffffu, bin);
-      if (bin >= 0 && (__ffs(grp) - 1) == b) {
+      // one shared-memory atomic per score: null scores spread over many
+      // bins, so a warp rarely holds two of one bin and merging them first
+      // (match_any) costs more than it saves
+      if (bin >= 0) {
         const int rel = bin - wbase;
-        if (rel >= 0 && rel < nwin) atomicAdd(sh + rel, (unsigned)__popc(grp));
-        else                        atomicAdd(obs + bin, (unsigned long long)__popc(grp));
+        if (rel >= 0 && rel < nwin) atomicAdd(sh + rel, 1u);
+        else                        atomicAdd(obs + bin, 1ull);
       }
     }
   }
@@ -1034,6 +1037,7 @@ cudaError_t launch_hist(const float2* cov, int64_t slot_stride, const TileRC* ti
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int64_t items = (int64_t)ntiles * nslots;
+  if (items >= ((int64_t)1 << 30)) return cudaErrorInvalidValue;   // the kernel indexes items in 32 bits
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)nsm));
   k_hist<<<grid, 1024, (size_t)nwin * 4, st>>>(cov, slot_stride, tiles, ntiles, nslots, L, B, nbcap, wbase, nwin, obs,
                                                status);
