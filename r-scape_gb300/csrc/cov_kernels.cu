@@ -728,39 +728,54 @@ __global__ void k_apc_avg(const double* __restrict__ colx, int L, int Lp, double
 
 // COV <- COV - COVx_i COVx_j / avg (APC) or COV - (COVx_i + COVx_j - avg) (ASC);
 // per-tile min/max of the corrected scores.  Double-float arithmetic.
+// APC/ASC applied in place, APC_TILES tiles per block (the block's min/max
+// reduction amortised over them), two pairs per 16-byte access
+constexpr int APC_TILES = 4;
+
 __global__ void __launch_bounds__(256)
 k_apc_apply(float2* __restrict__ cov, const float2* __restrict__ colxf, const double* __restrict__ avg,
             const float4* __restrict__ apcf, CorrTypes ct, const TileRC* __restrict__ tiles, int ntiles, int L, int Lp,
             double* __restrict__ tmin, double* __restrict__ tmax, int* __restrict__ status) {
-  const int t = blockIdx.x, sq = blockIdx.y, tid = threadIdx.x;
+  const int sq = blockIdx.y, tid = threadIdx.x;
   const int actype = ct.act[sq % ct.nout];
-  const TileRC tr = tiles[t];
   const bool Anz = (avg[sq] != 0.0);
   const float4 af = apcf[sq];
   const df A = {af.x, af.y}, invA = {af.z, af.w};
   const float2* X = colxf + (int64_t)sq * Lp;
-  float2* V = cov + ((int64_t)sq * ntiles + t) * TPP;
   df lo = {INFINITY, 0.f}, hi = {-INFINITY, 0.f};
+  auto corrected = [&](df v, int i, int j) -> df {
+    if (actype == 0) return Anz ? df_add(v, df_neg(df_mul(df_mul(ld_df(X + i), ld_df(X + j)), invA))) : df{0.f, 0.f};
+    if (actype == 1) return df_add(v, df_neg(df_add(df_add(ld_df(X + i), ld_df(X + j)), df_neg(A))));
+    return v;
+  };
+  for (int tt = 0; tt < APC_TILES; tt++) {
+    const int t = blockIdx.x * APC_TILES + tt;
+    if (t >= ntiles) break;
+    const TileRC tr = tiles[t];
+    float4* V = reinterpret_cast<float4*>(cov + ((int64_t)sq * ntiles + t) * TPP);
 #pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
-    const int i = tr.I * TP + a, j = tr.J * TP + b;
-    if (i < j && j < L) {
-      const df v = ld_df(V + p);
-      df r;
-      if (actype == 0) {
-        r = Anz ? df_add(v, df_neg(df_mul(df_mul(ld_df(X + i), ld_df(X + j)), invA))) : df{0.f, 0.f};
-      } else if (actype == 1) {
-        r = df_add(v, df_neg(df_add(df_add(ld_df(X + i), ld_df(X + j)), df_neg(A))));
-      } else {
-        r = v;
+    for (int k = 0; k < 2; k++) {
+      const int q = tid + 256 * k;           // pairs 2q, 2q + 1: one row, adjacent columns
+      const int p = 2 * q, a = p >> 5, b = p & 31;
+      const int i = tr.I * TP + a, j = tr.J * TP + b;
+      const float4 w = V[q];
+      df v0 = {w.x, w.y}, v1 = {w.z, w.w};
+      const bool ok0 = (i < j && j < L), ok1 = (i < j + 1 && j + 1 < L);
+      if (ok0) {
+        v0 = corrected(v0, i, j);
+        if (isnan(v0.hi)) atomicExch(status, 3);
+        lo = df_min(lo, v0); hi = df_max(hi, v0);
       }
-      if (isnan(r.hi)) atomicExch(status, 3);
-      if (actype >= 0) st_df(V + p, r);
-      lo = df_min(lo, r); hi = df_max(hi, r);
+      if (ok1) {
+        v1 = corrected(v1, i, j + 1);
+        if (isnan(v1.hi)) atomicExch(status, 3);
+        lo = df_min(lo, v1); hi = df_max(hi, v1);
+      }
+      if (actype >= 0 && (ok0 || ok1)) V[q] = make_float4(v0.hi, v0.lo, v1.hi, v1.lo);
     }
   }
-  block_minmax_store(lo, hi, tmin + (int64_t)sq * ntiles + t, tmax + (int64_t)sq * ntiles + t);
+  const int nblk = gridDim.x;
+  block_minmax_store(lo, hi, tmin + (int64_t)sq * nblk + blockIdx.x, tmax + (int64_t)sq * nblk + blockIdx.x);
 }
 
 // min/max of the scores of every valid pair (before any correction)
@@ -1009,8 +1024,9 @@ cudaError_t launch_apc(float2* cov, const double* part1, double* colx, float2* c
                        double* tmax, double* mm, int* status, cudaStream_t st) {
   k_apc_colx<<<dim3((L + 255) / 256, nsq), 256, 0, st>>>(part1, nT, L, Lp, colx, colxf);
   k_apc_avg<<<nsq, 256, 0, st>>>(colx, L, Lp, avg, apcf);
-  k_apc_apply<<<dim3(ntiles, nsq), 256, 0, st>>>(cov, colxf, avg, apcf, ct, tiles, ntiles, L, Lp, tmin, tmax, status);
-  k_reduce_minmax<<<nsq, 256, 0, st>>>(tmin, tmax, ntiles, mm);
+  const int nblk = (ntiles + APC_TILES - 1) / APC_TILES;
+  k_apc_apply<<<dim3(nblk, nsq), 256, 0, st>>>(cov, colxf, avg, apcf, ct, tiles, ntiles, L, Lp, tmin, tmax, status);
+  k_reduce_minmax<<<nsq, 256, 0, st>>>(tmin, tmax, nblk, mm);
   return cudaGetLastError();
 }
 
