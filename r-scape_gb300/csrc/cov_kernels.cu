@@ -312,8 +312,54 @@ k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ til
     nr[k][0] = {pair ? ne : 0.f, 0.f};
     zero[k][0] = {0.f, 0.f};
   }
-  tile_rowcol_store2<4>(rv, cv, part4 + (int64_t)slot * nT * nT * TP * 4, nT, tr.I, tr.J);
-  tile_rowcol_store2<1>(nr, zero, partR + (int64_t)slot * nT * nT * TP, nT, tr.I, tr.J);
+  // row sums over b of rv and column sums over a of cv (both into the
+  // diagonal tile's rows), then row sums of nseff, through one shared tile:
+  // one thread per (value, line) adds its 32 entries in order
+  __shared__ float2 sb[4][TP][TP + 1];
+  double* P4 = part4 + (int64_t)slot * nT * nT * TP * 4;
+  double* PR = partR + (int64_t)slot * nT * nT * TP;
+  const bool diag = (tr.I == tr.J);
+  const int c4 = tid >> 5, line = tid & 31;   // threads < 128: value c4, line
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+#pragma unroll
+    for (int c = 0; c < 4; c++) sb[c][a][b] = make_float2(rv[k][c].hi, rv[k][c].lo);
+  }
+  __syncthreads();
+  df rsum = {0.f, 0.f};
+  if (tid < 128) {
+    for (int b = 0; b < TP; b++) rsum = df_add(rsum, {sb[c4][line][b].x, sb[c4][line][b].y});
+    if (!diag) P4[(((int64_t)tr.I * nT + tr.J) * TP + line) * 4 + c4] = df_to_d(rsum);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+#pragma unroll
+    for (int c = 0; c < 4; c++) sb[c][a][b] = make_float2(cv[k][c].hi, cv[k][c].lo);
+  }
+  __syncthreads();
+  if (tid < 128) {
+    df csum = {0.f, 0.f};
+    for (int a = 0; a < TP; a++) csum = df_add(csum, {sb[c4][a][line].x, sb[c4][a][line].y});
+    if (diag) P4[(((int64_t)tr.I * nT + tr.I) * TP + line) * 4 + c4] = df_to_d(df_add(rsum, csum));
+    else      P4[(((int64_t)tr.J * nT + tr.I) * TP + line) * 4 + c4] = df_to_d(csum);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    sb[0][a][b] = make_float2(nr[k][0].hi, nr[k][0].lo);
+  }
+  __syncthreads();
+  if (tid < TP) {
+    df ns = {0.f, 0.f};
+    for (int b = 0; b < TP; b++) ns = df_add(ns, {sb[0][tid][b].x, sb[0][tid][b].y});
+    PR[((int64_t)tr.I * nT + tr.J) * TP + tid] = df_to_d(ns);
+    if (!diag) PR[((int64_t)tr.J * nT + tr.I) * TP + tid] = 0.0;   // the column sums of nseff are not used
+  }
+  (void)zero;
 }
 
 // pm[c][x] = normalise(sum over every tile touching column c); one thread
