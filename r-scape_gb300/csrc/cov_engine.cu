@@ -654,7 +654,10 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   if (need_u) {
     if (!ctx->d_ucnt) CK(dalloc(&ctx->d_ucnt, (size_t)ctx->maxslots * ctx->capntiles * 16 * TPP));
     if (counter == COVGPU_COUNT_TENSOR && ctx->umma) {
-      CK(umma_count(ctx->umma, ax, sstride, nslots, true, ctx->d_ucnt, ctx->st));
+      // RAF reads the unit counts of the allowed cells only
+      unsigned mask = 0;
+      for (int k = 0; k < 16; k++) if (allow[k] > 0.0) mask |= 1u << k;
+      CK(umma_count(ctx->umma, ax, sstride, nslots, true, ctx->d_ucnt, ctx->st, nullptr, nullptr, mask));
     } else {
       CK(launch_count_simt(ax, sstride, ctx->d_wf, true, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_ucnt, ctx->st));
     }

@@ -659,7 +659,10 @@ k_stats(StatsArgs A) {
     const bool valid = (i < j) && (j < A.L);
     float c[16], uc[16];
 #pragma unroll
-    for (int q = 0; q < 16; q++) { c[q] = C ? C[q * TPP + p] : 0.f; uc[q] = U ? U[q * TPP + p] : 0.f; }
+    for (int q = 0; q < 16; q++) {
+      c[q] = C ? C[q * TPP + p] : 0.f;
+      uc[q] = (U && A.allow[q] > 0.f) ? U[q * TPP + p] : 0.f;   // RAF reads the allowed cells only
+    }
     df ne = {0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < 16; q++) ne = df_add_f(ne, c[q]);

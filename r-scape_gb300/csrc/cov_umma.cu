@@ -310,7 +310,8 @@ template <int NL, int STAGES, int ACC, bool F8>
 __global__ void __launch_bounds__(192, 1)
 k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
              const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles, int nslots_buf,
-             int nslots, int Lp, int nkb, int bbuf, float s_hi, float s_lo, int* __restrict__ err) {
+             int nslots, int Lp, int nkb, int bbuf, float s_hi, float s_lo, unsigned cellmask,
+             int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   constexpr int STAGE_BYTES = TILE_BYTES * (1 + NL);
   constexpr int KE = F8 ? UK8 : UK;        // sequences per stage (one 128-byte row)
@@ -474,6 +475,7 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
             v[k] = (s2 + (e1 + e2)) * s_hi;   // s_hi = 2^-E, exact
           }
         }
+        if (!((cellmask >> (x * 4 + y)) & 1u)) continue;   // a cell nobody reads is not stored
         uint8_t* buf = wbuf + (nst & 1u) * 4096;
         if (nst >= 2) {
           if (lane == 0) bulk_wait_read<1>();   // the store two back has read this buffer
@@ -715,7 +717,7 @@ static cudaError_t ensure_fp8(UmmaPlan* p) {
 }
 
 cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
-                       cudaStream_t st, cudaEvent_t ev0, cudaEvent_t ev1) {
+                       cudaStream_t st, cudaEvent_t ev0, cudaEvent_t ev1, unsigned cellmask) {
   if (nslots > p->maxslots) return cudaErrorInvalidValue;
   if (((uintptr_t)cnt & 15u) != 0) return cudaErrorInvalidValue;
   CUtensorMap omap;
@@ -731,7 +733,7 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
                                                                             nslots, p->d_ops8);
     k_count_umma<1, STAGES1, ACC1, true><<<grid, 192, smem_bytes(1), st>>>(
         p->tmap8, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, p->Npad8 / UK8, 0, 1.0f, 0.0f,
-        p->d_err);
+        cellmask, p->d_err);
     return cudaGetLastError();
   }
   const int nl = p->nl;
@@ -749,13 +751,13 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
   if (ev0) cudaEventRecord(ev0, st);
   if (nl == 1)
     k_count_umma<1, STAGES1, ACC1, false><<<grid, 192, smem_bytes(1), st>>>(
-        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, 0xFFFFu, p->d_err);
   else if (nl == 2)
     k_count_umma<2, STAGES2, ACC2, false><<<grid, 192, smem_bytes(2), st>>>(
-        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, 0xFFFFu, p->d_err);
   else
     k_count_umma<3, STAGES3, ACC3, false><<<grid, 192, smem_bytes(3), st>>>(
-        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, p->d_err);
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, 0xFFFFu, p->d_err);
   if (ev1) cudaEventRecord(ev1, st);
   return cudaGetLastError();
 }

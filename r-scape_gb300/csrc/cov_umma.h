@@ -22,8 +22,10 @@ void        umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t
 // cnt [slot][tile][16][TPP]; unit = unit weights (RAF), counted on FP8 E4M3
 // one-hot operands; ev0/ev1 (optional) are recorded around the weighted
 // count kernel itself
+// (unit counts: only the cells of cellmask, bit 4x + y, are stored)
 cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int nslots, bool unit, float* cnt,
-                       cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
+                       cudaStream_t st, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr,
+                       unsigned cellmask = 0xFFFFu);
 // error code recorded by the kernel (0 = none; 101-105 = a barrier wait
 // timed out); reading it resets it
 int         umma_error(UmmaPlan* p);
