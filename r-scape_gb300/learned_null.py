@@ -339,7 +339,7 @@ def main(argv=None):
     t.add_argument("--data", nargs="+", required=True)
     t.add_argument("--batch", type=int, default=256)
     t.add_argument("--absolute-summary", action="store_true",
-                   help="the data files hold the quick-null summary as absolute scores (older files)")
+                   help="treat every data file as holding the quick-null summary as absolute scores")
     t.add_argument("--lr", type=float, default=2e-3)
     t.add_argument("--out", required=True)
     e = sub.add_parser("eval")
@@ -353,14 +353,18 @@ def main(argv=None):
     a = ap.parse_args(argv)
     if a.cmd == "gen":
         X, T, meta = generate(a.first, a.count, a.nnull, nquick=a.nquick, log=sys.stderr)
-        np.savez_compressed(a.out, X=X, T=T, meta=meta, nnull=a.nnull, nquick=a.nquick)
+        np.savez_compressed(a.out, X=X, T=T, meta=meta, nnull=a.nnull, nquick=a.nquick, summary="relative")
         print(json.dumps(dict(rows=len(X), out=a.out)))
     elif a.cmd == "train":
         zs = [np.load(p) for p in a.data]
-        X = np.concatenate([z["X"] for z in zs])
+        # files written before the engine gave the quick summary as offsets
+        # carry no "summary" entry: convert those (or all, when asked)
+        Xs = []
+        for z in zs:
+            rel = "summary" in z and str(z["summary"]) == "relative"
+            Xs.append(z["X"] if (rel and not a.absolute_summary) else relative_summary(z["X"]))
+        X = np.concatenate(Xs)
         T = np.concatenate([z["T"] for z in zs])
-        if a.absolute_summary:
-            X = relative_summary(X)
         net, info = train_selected(X, T, batch=a.batch, lr=a.lr, log=sys.stderr)
         nq = {int(z["nquick"]) for z in zs if "nquick" in z}
         if len(nq) != 1:
