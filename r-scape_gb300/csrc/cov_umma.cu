@@ -386,6 +386,13 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
     if (lane == 0) {
       // ---- MMA issuer ----
       constexpr uint32_t idesc = F8 ? make_idesc_e4m3(UM, UN) : (NL == 2 ? make_idesc_fp16(UM, UN) : make_idesc(UM, UN));
+      // limbs 0 and 1 as one M = 128, N = 256 MMA: their B tiles are
+      // consecutive in the stage (256 rows, 1024-byte 8-row groups throughout)
+      // and their accumulators consecutive in TMEM, so A is read from shared
+      // memory once for both (the ring's shared-memory bandwidth, A read per
+      // limb, bounded the two-MMA form)
+      constexpr bool PAIR = !F8 && NL >= 2;
+      constexpr uint32_t idesc2 = NL == 2 ? make_idesc_fp16(UM, 2 * UN) : make_idesc(UM, 2 * UN);
       uint32_t g = 0;
       int i = 0;
       for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x, i++) {
@@ -406,6 +413,12 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
           // four MMAs of 32 bytes of K each (16 BF16 or 32 FP8 sequences)
           for (int k16 = 0; k16 < 4; k16++) {
             const uint64_t ad = make_desc(sa + k16 * 32);
+            const uint32_t acc = (kb > 0 || k16 > 0) ? 1u : 0u;
+            if (PAIR) {
+              umma_f16(dacc, ad, make_desc(sa + (uint32_t)TILE_BYTES + k16 * 32), idesc2, acc);
+              if (NL == 3) umma_f16(dacc + (uint32_t)(2 * UN), ad, make_desc(sa + 3u * TILE_BYTES + k16 * 32), idesc, acc);
+              continue;
+            }
 #pragma unroll
             for (int l = 0; l < NL; l++) {
               const uint64_t bd = make_desc(sa + (uint32_t)(1 + l) * TILE_BYTES + k16 * 32);
