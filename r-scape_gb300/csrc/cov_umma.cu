@@ -28,10 +28,12 @@
 // the pairs (a, b = 0..31), one contiguous 128-byte row of the count tile.
 //
 // Kernel: persistent, one CTA per SM working through (column tile I <= J,
-// alignment) tasks in a blocked raster order; M = N = 128 (32 columns x 4
-// states each side), K in blocks of 64 sequences.  Warp 0 lane 0 issues TMA
-// loads (128B-swizzled boxes) into a 3-4 stage ring guarded by mbarriers,
-// warp 1 lane 0 issues tcgen05.mma (kind::f16, 128x128x16) into TMEM and
+// alignment) tasks in a blocked raster order; 128-row operand tiles (32
+// columns x 4 states), K in blocks of 64 sequences (128 with FP8).  Warp 0
+// lane 0 issues TMA loads (128B-swizzled boxes) into a 3-4 stage ring guarded
+// by mbarriers, warp 1 lane 0 issues tcgen05.mma into TMEM (kind::f16
+// 128x256x16 over limbs 0 and 1, whose B tiles are adjacent; kind::f8f6f4
+// 128x256x32 over two column tiles for unit weights) and
 // frees stages with tcgen05.commit; four epilogue warps read their 32 TMEM
 // lanes each (tcgen05.ld 32x32b.x32), hand the accumulators back, combine
 // the limbs, write the 32x32 block of one cell into a 128B-swizzled shared
@@ -68,6 +70,8 @@ struct UmmaPlan {
   int Npad = 0;                  // sequences padded to UK
   const TileRC* d_tiles = nullptr;
   int* d_order = nullptr;           // launch order of the tiles (blocked raster)
+  int4* d_jpairs = nullptr;         // unit-weight tasks: {I, J0, tile (I, J0), tile (I, J0 + 1)}, same raster
+  int njpairs = 0;
   __nv_bfloat16* d_ops = nullptr;   // [(1 + 3) * maxslots * 4Lp][Npad] (FP16 bits with two limbs)
   uint8_t* d_ops8 = nullptr;        // [maxslots * 4Lp][Npad8] FP8 E4M3 one-hot (unit weights)
   int Npad8 = 0;                    // sequences padded to UK8
@@ -305,17 +309,24 @@ k_umma_prep8(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp,
 //                   x = w % 4), releases the accumulator set after its last
 //                   TMEM load, then combines, stages and stores while the
 //                   next task's MMAs run
+// The unit-weight (FP8) kernel takes two column tiles per task, J0 and
+// J0 + 1 (jpairs: I, J0 and the two tile indices, -1 for a tile outside
+// I <= J < nT, which is computed and not stored): one M = 128, N = 256 MMA
+// reads the A tile once for both, where the shared-memory bandwidth, A and B
+// read per MMA and written by TMA, bounded the one-tile form.
 // ---------------------------------------------------------------------------
 template <int NL, int STAGES, int ACC, bool F8>
 __global__ void __launch_bounds__(192, 1)
 k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
-             const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles, int nslots_buf,
+             const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles,
+             const int4* __restrict__ jpairs, int npairs, int nslots_buf,
              int nslots, int Lp, int nkb, int bbuf, float s_hi, float s_lo, unsigned cellmask,
              int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  constexpr int STAGE_BYTES = TILE_BYTES * (1 + NL);
+  constexpr int NB = F8 ? 2 : NL;          // B tiles per stage (limbs, or the column tiles J0, J0 + 1)
+  constexpr int STAGE_BYTES = TILE_BYTES * (1 + NB);
   constexpr int KE = F8 ? UK8 : UK;        // sequences per stage (one 128-byte row)
-  constexpr uint32_t ACC_COLS = NL * UN;   // one accumulator set: NL limbs x 128 columns
+  constexpr uint32_t ACC_COLS = NB * UN;   // one accumulator set: NB x 128 columns
   constexpr uint32_t TMEM_COLS = (ACC * ACC_COLS <= 128) ? 128 : (ACC * ACC_COLS <= 256 ? 256 : 512);
   static_assert(ACC * ACC_COLS <= 512, "TMEM holds 512 columns");
   // 1024-byte aligned: the stage ring, then two 4 KB staging buffers per
@@ -331,7 +342,8 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
   __shared__ int abort_flag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t ntask = (int64_t)ntiles * nslots;
+  const int64_t nunits = F8 ? npairs : ntiles;   // tasks per alignment
+  const int64_t ntask = nunits * nslots;
   const int64_t rows_per_buf = (int64_t)nslots_buf * 4 * Lp;
 
   if (tid == 0) {
@@ -359,10 +371,12 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
       // ---- TMA producer ----
       uint32_t g = 0;
       for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x) {
-        const int slot = (int)(task / ntiles), t = order[task % ntiles];
-        const TileRC tr = tiles[t];
-        const int rowA = (int)((int64_t)slot * 4 * Lp + (int64_t)tr.I * UM);
-        const int rowB = (int)((int64_t)slot * 4 * Lp + (int64_t)tr.J * UN);
+        const int slot = (int)(task / nunits);
+        int I, J0;
+        if (F8) { const int4 q = jpairs[task % nunits]; I = q.x; J0 = q.y; }
+        else    { const TileRC tr = tiles[order[task % nunits]]; I = tr.I; J0 = tr.J; }
+        const int rowA = (int)((int64_t)slot * 4 * Lp + (int64_t)I * UM);
+        const int rowB = (int)((int64_t)slot * 4 * Lp + (int64_t)J0 * UN);
         for (int kb = 0; kb < nkb; kb++, g++) {
           const int s = (int)(g % STAGES);
           const uint32_t ph = (g / STAGES) & 1u;
@@ -373,10 +387,12 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
           uint8_t* st = ring + (size_t)s * STAGE_BYTES;
           mbar_expect_tx(&full_bar[s], STAGE_BYTES);
           tma_load_2d(st, &tmap, kb * KE, rowA, &full_bar[s]);
+          // F8: the rows of J0 + 1 follow those of J0 (beyond the last
+          // alignment of the buffer they lie outside the map: zero fill)
 #pragma unroll
-          for (int l = 0; l < NL; l++)
-            tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * KE, (int)((bbuf + l) * rows_per_buf) + rowB,
-                        &full_bar[s]);
+          for (int l = 0; l < NB; l++)
+            tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * KE,
+                        F8 ? rowB + l * UN : (int)((bbuf + l) * rows_per_buf) + rowB, &full_bar[s]);
           issued = g + 1;
         }
         if (*(volatile int*)&abort_flag) break;
@@ -392,7 +408,8 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
       // memory once for both (the ring's shared-memory bandwidth, A read per
       // limb, bounded the two-MMA form)
       constexpr bool PAIR = !F8 && NL >= 2;
-      constexpr uint32_t idesc2 = NL == 2 ? make_idesc_fp16(UM, 2 * UN) : make_idesc(UM, 2 * UN);
+      constexpr uint32_t idesc2 = F8 ? make_idesc_e4m3(UM, 2 * UN)
+                                     : (NL == 2 ? make_idesc_fp16(UM, 2 * UN) : make_idesc(UM, 2 * UN));
       uint32_t g = 0;
       int i = 0;
       for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x, i++) {
@@ -414,16 +431,14 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
           for (int k16 = 0; k16 < 4; k16++) {
             const uint64_t ad = make_desc(sa + k16 * 32);
             const uint32_t acc = (kb > 0 || k16 > 0) ? 1u : 0u;
-            if (PAIR) {
-              umma_f16(dacc, ad, make_desc(sa + (uint32_t)TILE_BYTES + k16 * 32), idesc2, acc);
+            const uint64_t bd = make_desc(sa + (uint32_t)TILE_BYTES + k16 * 32);
+            if (F8) {              // column tiles J0 and J0 + 1
+              umma_e4m3(dacc, ad, bd, idesc2, acc);
+            } else if (PAIR) {     // limbs 0 and 1 (and limb 2 on its own)
+              umma_f16(dacc, ad, bd, idesc2, acc);
               if (NL == 3) umma_f16(dacc + (uint32_t)(2 * UN), ad, make_desc(sa + 3u * TILE_BYTES + k16 * 32), idesc, acc);
-              continue;
-            }
-#pragma unroll
-            for (int l = 0; l < NL; l++) {
-              const uint64_t bd = make_desc(sa + (uint32_t)(1 + l) * TILE_BYTES + k16 * 32);
-              if (F8) umma_e4m3(dacc + (uint32_t)(l * UN), ad, bd, idesc, (kb > 0 || k16 > 0) ? 1u : 0u);
-              else    umma_f16(dacc + (uint32_t)(l * UN), ad, bd, idesc, (kb > 0 || k16 > 0) ? 1u : 0u);
+            } else {
+              umma_f16(dacc, ad, bd, idesc, acc);
             }
           }
           umma_commit(&empty_bar[s]);
@@ -445,16 +460,21 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
       __syncwarp();
       if (*(volatile int*)&abort_flag) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int slot = (int)(task / ntiles), t = order[task % ntiles];
-      const int orow0 = ((slot * ntiles + t) * 16 + x * 4) * 32;   // cell (x, y = 0), a = 0
+      const int slot = (int)(task / nunits);
+      int t0, t1 = -1;
+      if (F8) { const int4 q = jpairs[task % nunits]; t0 = q.z; t1 = q.w; }
+      else    { t0 = order[task % nunits]; }
       const uint32_t taddr = tmem + ((uint32_t)(x * 32) << 16) + (uint32_t)a * ACC_COLS;
+      // F8: cells of tile J0 (h = 0), then of J0 + 1 (h = 1)
+      constexpr int NCHUNK = F8 ? 8 : 4;
 #pragma unroll 1
-      for (int y = 0; y < 4; y++) {
+      for (int cy = 0; cy < NCHUNK; cy++) {
+        const int h = cy >> 2, y = cy & 3;
         uint32_t d[NL][32];
 #pragma unroll
-        for (int l = 0; l < NL; l++) tmem_ld32(taddr + (uint32_t)(l * UN + y * 32), d[l]);
+        for (int l = 0; l < NL; l++) tmem_ld32(taddr + (uint32_t)((F8 ? h : l) * UN + y * 32), d[l]);
         tmem_ld_wait();
-        if (y == 3) {
+        if (cy == NCHUNK - 1) {
           // this warp's last read of the accumulator set: hand it back
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
@@ -488,7 +508,10 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
             v[k] = (s2 + (e1 + e2)) * s_hi;   // s_hi = 2^-E, exact
           }
         }
+        const int t = h ? t1 : t0;
+        if (t < 0) continue;                                // outside I <= J < nT
         if (!((cellmask >> (x * 4 + y)) & 1u)) continue;   // a cell nobody reads is not stored
+        const int orow0 = ((slot * ntiles + t) * 16 + x * 4) * 32;   // cell (x, y = 0), a = 0
         uint8_t* buf = wbuf + (nst & 1u) * 4096;
         if (nst >= 2) {
           if (lane == 0) bulk_wait_read<1>();   // the store two back has read this buffer
@@ -544,7 +567,8 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 
 constexpr int STAGES3 = 3;   // 3 limbs: 64 KB per stage
 constexpr int STAGES2 = 4;   // 2 limbs: 48 KB per stage
-constexpr int STAGES1 = 4;   // 1 limb : 32 KB per stage
+constexpr int STAGES1 = 4;   // 1 limb : 32 KB per stage (FP8, two column tiles: 48 KB)
+static_assert(STAGES1 == STAGES2, "the FP8 kernel's ring is sized as the two-limb one");
 
 constexpr int ACC3 = 1;      // 3 limbs: 384 TMEM columns, one accumulator set
 constexpr int ACC2 = 2;      // 2 limbs: two 256-column sets, epilogue overlapped
@@ -569,8 +593,24 @@ static bool set_order(UmmaPlan* p, int SB) {
       for (int I = bI; I < std::min(nT, bI + SB); I++)
         for (int J = std::max(I, bJ); J < std::min(nT, bJ + SB); J++) order.push_back(tindex(I, J));
   if ((int)order.size() != p->ntiles) return false;
+  // column-tile pairs (J0, J0 + 1), J0 even, for the unit-weight kernel:
+  // super-blocks of SB rows x SB/2 pairs; each tile I <= J lies in exactly
+  // one pair, so there are at most ntiles of them
+  std::vector<int4> jp;
+  jp.reserve(p->ntiles);
+  const int nP = (nT + 1) / 2, SP = std::max(1, SB / 2);
+  for (int bI = 0; bI < nT; bI += SB)
+    for (int bP = bI / 2; bP < nP; bP += SP)
+      for (int I = bI; I < std::min(nT, bI + SB); I++)
+        for (int q = std::max(I / 2, bP); q < std::min(nP, bP + SP); q++) {
+          const int J0 = 2 * q;
+          jp.push_back(make_int4(I, J0, J0 >= I ? tindex(I, J0) : -1, J0 + 1 < nT ? tindex(I, J0 + 1) : -1));
+        }
+  if ((int)jp.size() > p->ntiles) return false;
   p->sb = SB;
-  return cudaMemcpy(p->d_order, order.data(), sizeof(int) * p->ntiles, cudaMemcpyHostToDevice) == cudaSuccess;
+  p->njpairs = (int)jp.size();
+  return cudaMemcpy(p->d_order, order.data(), sizeof(int) * p->ntiles, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(p->d_jpairs, jp.data(), sizeof(int4) * jp.size(), cudaMemcpyHostToDevice) == cudaSuccess;
 }
 
 // dimensions of the current alignments within the plan's buffers: tile
@@ -617,6 +657,7 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
   if (cudaMemset(p->d_ops, 0, p->ops_bytes) != cudaSuccess ||
       cudaMalloc(&p->d_limbs, (size_t)3 * Npad_cap * sizeof(uint16_t)) != cudaSuccess ||
       cudaMalloc(&p->d_order, sizeof(int) * std::max(1, capntiles)) != cudaSuccess ||
+      cudaMalloc(&p->d_jpairs, sizeof(int4) * std::max(1, capntiles)) != cudaSuccess ||
       cudaMalloc(&p->d_err, sizeof(int)) != cudaSuccess) {
     umma_plan_destroy(p);
     return nullptr;
@@ -630,7 +671,7 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
   cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem_bytes(1));
   cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem_bytes(1));
+                       (int)smem_bytes(2));   // two B tiles per stage
   cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev);
   return p;
 }
@@ -644,6 +685,7 @@ void umma_plan_destroy(UmmaPlan* p) {
   if (p->d_ops) cudaFree(p->d_ops);
   if (p->d_ops8) cudaFree(p->d_ops8);
   if (p->d_order) cudaFree(p->d_order);
+  if (p->d_jpairs) cudaFree(p->d_jpairs);
   if (p->d_limbs) cudaFree(p->d_limbs);
   if (p->d_err) cudaFree(p->d_err);
   delete p;
@@ -744,9 +786,11 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
     if (e != cudaSuccess) return e;
     k_umma_prep8<<<dim3(p->Npad8 / 128, p->Lp / 32, nslots), 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad8,
                                                                             nslots, p->d_ops8);
-    k_count_umma<1, STAGES1, ACC1, true><<<grid, 192, smem_bytes(1), st>>>(
-        p->tmap8, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, p->Npad8 / UK8, 0, 1.0f, 0.0f,
-        cellmask, p->d_err);
+    const int64_t ntask8 = (int64_t)p->njpairs * nslots;
+    const int grid8 = (int)std::max<int64_t>(1, std::min<int64_t>(ntask8, p->nsm));
+    k_count_umma<1, STAGES1, ACC1, true><<<grid8, 192, smem_bytes(2), st>>>(
+        p->tmap8, omap, p->d_tiles, p->d_order, p->ntiles, p->d_jpairs, p->njpairs, p->maxslots, nslots, p->Lp,
+        p->Npad8 / UK8, 0, 1.0f, 0.0f, cellmask, p->d_err);
     return cudaGetLastError();
   }
   const int nl = p->nl;
@@ -764,13 +808,16 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
   if (ev0) cudaEventRecord(ev0, st);
   if (nl == 1)
     k_count_umma<1, STAGES1, ACC1, false><<<grid, 192, smem_bytes(1), st>>>(
-        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, 0xFFFFu, p->d_err);
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, nullptr, 0, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo,
+        0xFFFFu, p->d_err);
   else if (nl == 2)
     k_count_umma<2, STAGES2, ACC2, false><<<grid, 192, smem_bytes(2), st>>>(
-        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, 0xFFFFu, p->d_err);
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, nullptr, 0, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo,
+        0xFFFFu, p->d_err);
   else
     k_count_umma<3, STAGES3, ACC3, false><<<grid, 192, smem_bytes(3), st>>>(
-        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo, 0xFFFFu, p->d_err);
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, nullptr, 0, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo,
+        0xFFFFu, p->d_err);
   if (ev1) cudaEventRecord(ev1, st);
   return cudaGetLastError();
 }
