@@ -12,16 +12,17 @@
 //                shuffled (msamanip_ShuffleColumns, src/msamanip.c:1164-1233).
 //                Only the root's shuffled row is ever read: every other row
 //                is replaced by its parent's row before use.
-//   k_replay     top depth first, one warp per (branch, null):
+//   k_replay     top depth first, one CTA per (branch, null):
 //                shuffle_tree_substitutions + shuffle_tree_substitute_all
-//                (src/msamanip.c:1597-1747).  The warp finishes the child's
+//                (src/msamanip.c:1597-1747).  The CTA finishes the child's
 //                Fitch state (down pass: keep the parent's state when the
 //                child's set holds it), counts the branch's substitutions on
 //                the unshuffled reconstruction, copies the parent's current
 //                row and replays the substitutions on positions of that row
 //                holding the old state, visited in a random order (a Feistel
-//                permutation); each class's positions are ranked with warp
-//                ballots and the pass stops once every substitution is placed.
+//                permutation), 256 slots at a time; each class's positions
+//                are ranked with warp ballots and a prefix over the warps,
+//                and the pass stops once every substitution is placed.
 //
 // Random draws are counter-based (Philox keyed by the seed, the null index,
 // the node and the column), so the result does not depend on scheduling.
@@ -111,40 +112,52 @@ k_root_row(int N, int L, int Lp, uint64_t seed, uint32_t first_null, const uint8
   SR[off + c] = (c < L) ? F[off + feistel_perm((uint32_t)c, feistel_hbits((uint32_t)L), (uint32_t)L, rk)] : (uint8_t)4;
 }
 
-// one warp per (branch, null) for the internal nodes v of one depth
-__global__ void __launch_bounds__(256)
-k_replay(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
-         const int* __restrict__ right, const int* __restrict__ nodes, int nn, uint64_t seed, uint32_t first_null,
-         uint8_t* __restrict__ F, uint8_t* __restrict__ SR, uint8_t* __restrict__ out_ax, int64_t out_slot_stride) {
-  __shared__ int nsub_s[8][25];
-  __shared__ int cum_s[8][5][6];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int item = blockIdx.x * 8 + warp;
-  if (item >= 2 * nn) return;
-  const int q = blockIdx.y;
-  const int v = nodes[item >> 1];
-  const int ch = (item & 1) ? right[v] : left[v];
-  const int cidx = (ch <= 0) ? -ch : N + ch;
-  const uint32_t nid = first_null + q;
-  const int64_t qoff = (int64_t)q * (N - 1) * Lp;
-  const uint8_t* Fp = F + qoff + (int64_t)v * Lp;
-  const uint8_t* Rp = SR + qoff + (int64_t)v * Lp;          // parent's current row
-  uint8_t* Fc = F + qoff + (int64_t)(ch > 0 ? ch : 0) * Lp;  // written for an internal child only
-  const uint8_t* Sc = SR + qoff + (int64_t)(ch > 0 ? ch : 0) * Lp;
-  const uint8_t* Lc = ax + (int64_t)(ch <= 0 ? -ch : 0) * Lp;
-  uint8_t* Cc = (ch <= 0) ? out_ax + (int64_t)q * out_slot_stride + (int64_t)(-ch) * Lp
-                          : SR + qoff + (int64_t)ch * Lp;
-  int* nsub = nsub_s[warp];
-  if (lane < 25) nsub[lane] = 0;
-  __syncwarp();
+// The replay of one (branch, null) item: phase 1, the child's Fitch states
+// (down pass) and the branch's substitution counts, 16 columns per thread;
+// phase 2, the child's row starts as a copy of the parent's row (staged in
+// shared memory too when srow is given, for the random reads of phase 3);
+// phase 3 walks the slots t in order, maps each to position perm(t) of the
+// parent's row and, for the state o there, ranks the slot among the slots of
+// class o so far: the r-th takes substitution r of class o while r <
+// need[o].  Once every class has its substitutions the walk stops (later
+// slots would place nothing).  Two kernels run phase 3: one warp per item,
+// 32 slots a step (levels with many items), and one CTA per item, 256 slots
+// a step with a prefix over the warps (levels with few, long items).
+struct ReplayItem {
+  int ch, cidx;
+  uint32_t nid;
+  const uint8_t *Fp, *Rp, *Sc, *Lc;
+  uint8_t *Fc, *Cc;
+};
 
-  // child's states (down pass for an internal child) and the substitution
-  // counts parent -> child, 16 columns per lane and step
-  for (int c0 = lane * 16; c0 < Lp; c0 += 32 * 16) {
-    const uint4 pv = *reinterpret_cast<const uint4*>(Fp + c0);
+__device__ __forceinline__ ReplayItem replay_item(const uint8_t* ax, int N, int Lp, const int* left, const int* right,
+                                                  const int* nodes, int item, int q, uint32_t first_null,
+                                                  uint8_t* F, uint8_t* SR, uint8_t* out_ax, int64_t out_slot_stride) {
+  ReplayItem it;
+  const int v = nodes[item >> 1];
+  it.ch = (item & 1) ? right[v] : left[v];
+  it.cidx = (it.ch <= 0) ? -it.ch : N + it.ch;
+  it.nid = first_null + q;
+  const int64_t qoff = (int64_t)q * (N - 1) * Lp;
+  it.Fp = F + qoff + (int64_t)v * Lp;
+  it.Rp = SR + qoff + (int64_t)v * Lp;                            // parent's current row
+  it.Fc = F + qoff + (int64_t)(it.ch > 0 ? it.ch : 0) * Lp;       // written for an internal child only
+  it.Sc = SR + qoff + (int64_t)(it.ch > 0 ? it.ch : 0) * Lp;
+  it.Lc = ax + (int64_t)(it.ch <= 0 ? -it.ch : 0) * Lp;
+  it.Cc = (it.ch <= 0) ? out_ax + (int64_t)q * out_slot_stride + (int64_t)(-it.ch) * Lp
+                       : SR + qoff + (int64_t)it.ch * Lp;
+  return it;
+}
+
+// phases 1 and 2 by nthr threads (this one: tid); nsub (25 counters, zeroed)
+// and srow (nullptr or Lp bytes) in shared memory
+__device__ __forceinline__ void replay_prepare(const ReplayItem& it, int L, int Lp, uint64_t seed, int tid, int nthr,
+                                               int* nsub, uint8_t* srow) {
+  for (int c0 = tid * 16; c0 < Lp; c0 += nthr * 16) {
+    const uint4 pv = *reinterpret_cast<const uint4*>(it.Fp + c0);
     uint4 cv;
-    if (ch > 0) {
-      const uint4 sv = *reinterpret_cast<const uint4*>(Sc + c0);
+    if (it.ch > 0) {
+      const uint4 sv = *reinterpret_cast<const uint4*>(it.Sc + c0);
       uint32_t pw[4] = {pv.x, pv.y, pv.z, pv.w}, sw[4] = {sv.x, sv.y, sv.z, sv.w}, ow[4];
 #pragma unroll
       for (int k = 0; k < 4; k++) {
@@ -157,16 +170,16 @@ k_replay(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __rest
             const uint32_t a = (pw[k] >> (8 * b)) & 0xFFu;
             unsigned set = (sw[k] >> (8 * b)) & 0xFFu;
             if (set & (1u << a)) set = 1u << a;
-            st = (uint32_t)choose_member(set, seed, nid, (uint32_t)ch, (uint32_t)c);
+            st = (uint32_t)choose_member(set, seed, it.nid, (uint32_t)it.ch, (uint32_t)c);
           }
           o |= st << (8 * b);
         }
         ow[k] = o;
       }
       cv = make_uint4(ow[0], ow[1], ow[2], ow[3]);
-      *reinterpret_cast<uint4*>(Fc + c0) = cv;
+      *reinterpret_cast<uint4*>(it.Fc + c0) = cv;
     } else {
-      cv = *reinterpret_cast<const uint4*>(Lc + c0);
+      cv = *reinterpret_cast<const uint4*>(it.Lc + c0);
     }
     const uint32_t pw[4] = {pv.x, pv.y, pv.z, pv.w}, cw[4] = {cv.x, cv.y, cv.z, cv.w};
 #pragma unroll
@@ -180,9 +193,37 @@ k_replay(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __rest
       }
     }
   }
-  // the child's row starts as a copy of the parent's row
-  for (int c0 = lane * 16; c0 < Lp; c0 += 32 * 16)
-    *reinterpret_cast<uint4*>(Cc + c0) = *reinterpret_cast<const uint4*>(Rp + c0);
+  for (int c0 = tid * 16; c0 < Lp; c0 += nthr * 16) {   // Lp is a multiple of 32
+    const uint4 v4 = *reinterpret_cast<const uint4*>(it.Rp + c0);
+    *reinterpret_cast<uint4*>(it.Cc + c0) = v4;
+    if (srow) *reinterpret_cast<uint4*>(srow + c0) = v4;
+  }
+}
+
+__device__ __forceinline__ unsigned pick5(const unsigned (&m)[5], int k) {
+  return k == 0 ? m[0] : k == 1 ? m[1] : k == 2 ? m[2] : k == 3 ? m[3] : m[4];
+}
+
+// one warp per item, eight items per CTA (SROW: Lp bytes of row per warp)
+template <bool SROW>
+__global__ void __launch_bounds__(256)
+k_replay_warp(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
+              const int* __restrict__ right, const int* __restrict__ nodes, int nn, uint64_t seed,
+              uint32_t first_null, uint8_t* __restrict__ F, uint8_t* __restrict__ SR, uint8_t* __restrict__ out_ax,
+              int64_t out_slot_stride) {
+  extern __shared__ __align__(16) uint8_t rowbuf[];
+  __shared__ int nsub_s[8][25];
+  __shared__ int cum_s[8][5][6];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * 8 + warp;
+  if (item >= 2 * nn) return;
+  const ReplayItem it = replay_item(ax, N, Lp, left, right, nodes, item, blockIdx.y, first_null, F, SR, out_ax,
+                                    out_slot_stride);
+  int* nsub = nsub_s[warp];
+  if (lane < 25) nsub[lane] = 0;
+  __syncwarp();
+  uint8_t* srow = SROW ? rowbuf + (size_t)warp * Lp : nullptr;
+  replay_prepare(it, L, Lp, seed, lane, 32, nsub, srow);
   __syncwarp();
   int (*cum)[6] = cum_s[warp];
   if (lane < 5) {
@@ -194,20 +235,18 @@ k_replay(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __rest
 #pragma unroll
   for (int o = 0; o < 5; o++) { need[o] = cum[o][5]; total += need[o]; }
   if (total == 0) return;
-
-  // slot t -> position perm(t) of the parent's row; the r-th slot holding
-  // state o (in slot order) takes substitution r of class o while r < need[o]
   uint32_t rk[6];
-  round_keys(seed, TAG_SUBST, nid, (uint32_t)cidx, rk);
+  round_keys(seed, TAG_SUBST, it.nid, (uint32_t)it.cidx, rk);
   const uint32_t hb = feistel_hbits((uint32_t)L);
   const unsigned lt = (1u << lane) - 1u;
+  const uint8_t* R = SROW ? srow : it.Rp;
   for (int t0 = 0; t0 < L; t0 += 32) {
     const int t = t0 + lane;
     uint32_t p = 0;
     int o = 5;
     if (t < L) {
       p = feistel_perm((uint32_t)t, hb, (uint32_t)L, rk);
-      o = Rp[p];
+      o = R[p];
     }
     bool done = true;
 #pragma unroll
@@ -218,7 +257,7 @@ k_replay(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __rest
         if (r < need[oc]) {
           int d = 0;
           while (r >= cum[oc][d + 1]) d++;
-          Cc[p] = (uint8_t)d;
+          it.Cc[p] = (uint8_t)d;
         }
       }
       run[oc] += __popc(m);
@@ -226,6 +265,102 @@ k_replay(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __rest
     }
     if (done) break;
   }
+}
+
+// one CTA per item (SROW: Lp bytes of row)
+template <bool SROW>
+__global__ void __launch_bounds__(256)
+k_replay_cta(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
+             const int* __restrict__ right, const int* __restrict__ nodes, int nn, uint64_t seed,
+             uint32_t first_null, uint8_t* __restrict__ F, uint8_t* __restrict__ SR, uint8_t* __restrict__ out_ax,
+             int64_t out_slot_stride) {
+  extern __shared__ __align__(16) uint8_t rowbuf[];
+  __shared__ int nsub[25];
+  __shared__ int cum[5][6];
+  __shared__ int gcnt[8][5];   // slots per class in each warp's group of the chunk
+  __shared__ int base[5];      // slots per class before the chunk
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int item = blockIdx.x;
+  if (item >= 2 * nn) return;
+  const ReplayItem it = replay_item(ax, N, Lp, left, right, nodes, item, blockIdx.y, first_null, F, SR, out_ax,
+                                    out_slot_stride);
+  if (tid < 25) nsub[tid] = 0;
+  __syncthreads();
+  replay_prepare(it, L, Lp, seed, tid, 256, nsub, SROW ? rowbuf : nullptr);
+  __syncthreads();
+  if (tid < 5) {
+    cum[tid][0] = 0;
+    for (int d = 0; d < 5; d++) cum[tid][d + 1] = cum[tid][d] + nsub[tid * 5 + d];
+    base[tid] = 0;
+  }
+  __syncthreads();
+  int need[5], total = 0;
+#pragma unroll
+  for (int o = 0; o < 5; o++) { need[o] = cum[o][5]; total += need[o]; }
+  if (total == 0) return;   // the same in every thread
+  uint32_t rk[6];
+  round_keys(seed, TAG_SUBST, it.nid, (uint32_t)it.cidx, rk);
+  const uint32_t hb = feistel_hbits((uint32_t)L);
+  const unsigned lt = (1u << lane) - 1u;
+  const uint8_t* R = SROW ? rowbuf : it.Rp;
+  for (int t0 = 0; t0 < L; t0 += 256) {
+    const int t = t0 + tid;
+    uint32_t p = 0;
+    int o = 5;
+    if (t < L) {
+      p = feistel_perm((uint32_t)t, hb, (uint32_t)L, rk);
+      o = R[p];
+    }
+    unsigned m[5];
+#pragma unroll
+    for (int oc = 0; oc < 5; oc++) m[oc] = __ballot_sync(0xffffffffu, o == oc);
+    if (lane < 5) gcnt[warp][lane] = __popc(pick5(m, lane));
+    __syncthreads();
+    if (o < 5) {
+      int r = base[o] + __popc(pick5(m, o) & lt);
+      for (int w = 0; w < warp; w++) r += gcnt[w][o];
+      if (r < cum[o][5]) {   // need[o], read from shared memory (o varies by lane)
+        int d = 0;
+        while (r >= cum[o][d + 1]) d++;
+        it.Cc[p] = (uint8_t)d;
+      }
+    }
+    __syncthreads();   // base and gcnt read
+    if (tid < 5) {
+      int s2 = base[tid];
+      for (int w = 0; w < 8; w++) s2 += gcnt[w][tid];
+      base[tid] = s2;
+    }
+    __syncthreads();
+    bool all = true;
+#pragma unroll
+    for (int oc = 0; oc < 5; oc++) all = all && (base[oc] >= need[oc]);
+    if (all) break;   // the same in every thread
+  }
+}
+
+// items per level up to which the replay goes one CTA per item: measured on
+// N=2000 x L=3000 with 20 nulls, one CTA per item is faster up to about 3,000
+// items (long branches near the root), one warp per item beyond
+constexpr int64_t kReplayCtaItems = 3000;
+
+// the replay's shared-memory row buffers: the launch limit of both kernels
+// is raised once to the device's opt-in maximum; rows that do not fit are
+// read from global memory instead
+static int replay_smem_limit() {
+  static const int lim = [] {
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+      return 48 * 1024;
+    const int dyn = optin - 4096;   // room for the kernels' static arrays
+    if (dyn <= 48 * 1024 ||
+        cudaFuncSetAttribute(k_replay_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
+        cudaFuncSetAttribute(k_replay_cta<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
+      return 48 * 1024;
+    return dyn;
+  }();
+  return lim;
 }
 
 // down pass of the Fitch reconstruction for the internal children of one
@@ -290,12 +425,31 @@ cudaError_t launch_nullgen(const uint8_t* ax, int N, int L, int Lp, const NullTr
   }
   k_root_state<<<dim3((L + 255) / 256, nnull), 256, 0, st>>>(N, L, Lp, seed, first_null, scratch, fitch);
   k_root_row<<<dim3((Lp + 255) / 256, nnull), 256, 0, st>>>(N, L, Lp, seed, first_null, fitch, scratch);
+  // levels with few items (near the root and the leaves) go one CTA per
+  // item; the others one warp per item
+  const int lim = replay_smem_limit();
+  const bool srow_cta = (size_t)Lp <= (size_t)lim, srow_warp = (size_t)8 * Lp <= (size_t)lim;
   for (int d = 0; d < nlevels; d++) {
     const int nn = level_off[d + 1] - level_off[d];
     if (nn <= 0) continue;
-    k_replay<<<dim3((2 * nn + 7) / 8, nnull), 256, 0, st>>>(ax, N, L, Lp, T.left, T.right, level_nodes + level_off[d],
-                                                             nn, seed, first_null, fitch, scratch, out_ax,
-                                                             out_slot_stride);
+    const int* lv = level_nodes + level_off[d];
+    if ((int64_t)2 * nn * nnull <= kReplayCtaItems) {
+      const dim3 g(2 * nn, nnull);
+      if (srow_cta)
+        k_replay_cta<true><<<g, 256, (size_t)Lp, st>>>(ax, N, L, Lp, T.left, T.right, lv, nn, seed, first_null, fitch,
+                                                      scratch, out_ax, out_slot_stride);
+      else
+        k_replay_cta<false><<<g, 256, 0, st>>>(ax, N, L, Lp, T.left, T.right, lv, nn, seed, first_null, fitch,
+                                               scratch, out_ax, out_slot_stride);
+    } else {
+      const dim3 g((2 * nn + 7) / 8, nnull);
+      if (srow_warp)
+        k_replay_warp<true><<<g, 256, (size_t)8 * Lp, st>>>(ax, N, L, Lp, T.left, T.right, lv, nn, seed, first_null,
+                                                            fitch, scratch, out_ax, out_slot_stride);
+      else
+        k_replay_warp<false><<<g, 256, 0, st>>>(ax, N, L, Lp, T.left, T.right, lv, nn, seed, first_null, fitch,
+                                                scratch, out_ax, out_slot_stride);
+    }
   }
   return cudaGetLastError();
 }
