@@ -458,13 +458,14 @@ __device__ __forceinline__ float diff_oe(float c, float dc, df e) {
 // empty cells (r ~ 1e-10) 1 + d rounds to a multiple of 2^-24 and, times
 // log1p(d) ~ -20, would add ~1e-6 e per cell.  Both forms are evaluated and
 // one is selected: a warp holds pairs whose cells fall on both sides, and a
-// branch would make every warp run every path.
-__device__ __forceinline__ float gterm_f(float u, float e, float o) {
-  const float d = __fdividef(u, e);
+// branch would make every warp run every path.  ie = 1/e (approximate
+// reciprocal, shared with the caller's CHI term).
+__device__ __forceinline__ float gterm_f(float u, float e, float ie, float o) {
+  const float d = u * ie;
   const float dn = fminf(fmaxf(d, -0.25f), 0.25f);     // the polynomial only where it is used
   const float near = gfun_poly(dn);
   const float dp = fmaxf(d, -1.f);
-  const float r = (d < 0.f) ? __fdividef(o, e) : 1.f + dp;
+  const float r = (d < 0.f) ? o * ie : 1.f + dp;
   const float l = log1pf(fmaxf(dp, -0.99999994f));     // finite where 1 + d rounds to 0
   const float far = r * l - dp;
   return e * ((fabsf(d) < 0.25f) ? near : far);
@@ -510,14 +511,20 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
           const float n = uc[x * 4 + y];
           nAf += n; r[x] += n; cc[y] += n;
         }
-    df sq = {0.f, 0.f};   // sum of the squared row and column counts (exact)
+    // c_ij = nA^2 - (sum r_x^2 + sum c_y^2)/2 in 64-bit integers (the
+    // counts are integers below 2^24, c_ij below 2^48), then split exactly
+    // into a double-float
+    // (sum r_x^2 + sum c_y^2 is even: each sum has the parity of nA)
+    int64_t sq = 0;
 #pragma unroll
     for (int x = 0; x < 4; x++) {
-      sq = df_add(sq, two_prod(r[x], r[x]));
-      sq = df_add(sq, two_prod(cc[x], cc[x]));
+      const int a = (int)r[x], b = (int)cc[x];
+      sq += (int64_t)a * a + (int64_t)b * b;
     }
-    const df nA2 = two_prod(nAf, nAf);
-    const df cnum = df_add(nA2, {-0.5f * sq.hi, -0.5f * sq.lo});   // c_ij, exact
+    const int nA = (int)nAf;
+    const int64_t ci = (int64_t)nA * nA - sq / 2;
+    const float ci_hi = (float)ci;
+    const df cnum = {ci_hi, (float)(ci - (int64_t)ci_hi)};   // exact: the rest is an integer below 2^24
     const df q1 = df_mul(cnum, {A.invD.x, A.invD.y});
     const df q2 = df_mul({(float)A.N - nAf, 0.f}, {A.invN.x, A.invN.y});
     out.raf = df_add({2.f * q1.hi, 2.f * q1.lo}, df_neg(q2));
@@ -580,8 +587,9 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
           const df e = df_mul(ax, {pmj[y].x, pmj[y].y});
           const float u = diff_oe(C, dc, e);
           if (e.hi > 0.f) {
-            if (CF & CF_G) { gsum += gterm_f(u, e.hi, o); usum += u; }
-            if (CF & CF_CHI) chi += __fdividef(u * u, e.hi);
+            const float ie = __fdividef(1.f, e.hi);
+            if (CF & CF_G) { gsum += gterm_f(u, e.hi, ie, o); usum += u; }
+            if (CF & CF_CHI) chi += u * u * ie;
             if (CF & CF_OMES) omes += u * u;
           }
         }
@@ -619,8 +627,14 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
     const float un = diff_oe(Cn.hi, Cn.lo + dn, en);
     const float ow = Cw.hi + (Cw.lo + dw), on = Cn.hi + (Cn.lo + dn);
     float g = 0.f, chi = 0.f, om = 0.f;
-    if (ew.hi > 0.f) { g += gterm_f(uw, ew.hi, ow); chi += __fdividef(uw * uw, ew.hi); om += uw * uw; }
-    if (en.hi > 0.f) { g += gterm_f(un, en.hi, on); chi += __fdividef(un * un, en.hi); om += un * un; }
+    if (ew.hi > 0.f) {
+      const float ie = __fdividef(1.f, ew.hi);
+      g += gterm_f(uw, ew.hi, ie, ow); chi += uw * uw * ie; om += uw * uw;
+    }
+    if (en.hi > 0.f) {
+      const float ie = __fdividef(1.f, en.hi);
+      g += gterm_f(un, en.hi, ie, on); chi += un * un * ie; om += un * un;
+    }
     const float pw = ow * inv_ne, pn = on * inv_ne;
     float hh = 0.f;
     hh -= (pw > 0.f) ? pw * __logf(pw) : 0.f;
