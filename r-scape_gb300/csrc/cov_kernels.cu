@@ -162,6 +162,8 @@ struct BinC {
   float2 invw;     // 1/w
   float2 lo;       // bmin + w (scores are clamped up to it)
   float  mconst;   // absolute part of the fast-path margin
+  float  absb;     // |bmin|
+  float  mscale;   // 4e-7 / w: the FP32 estimate's error per unit of |x| + |bmin|
   int    bin_lo;   // bin of the clamp value bmin + w, from its FP64 value
   double bmin, w;
 };
@@ -173,6 +175,8 @@ static BinC make_binc(double bmin, double w) {
   B.invw = split(1.0 / w);
   B.lo = split(bmin + w);
   B.mconst = (float)(1e-11 * (std::fabs(bmin) / w + 1.0));
+  B.absb = (float)std::fabs(bmin);
+  B.mscale = (float)(4e-7 / w);
   B.bin_lo = exact_bin(bmin + w, bmin, w, 1.0 / w);
   B.bmin = bmin; B.w = w;
   return B;
@@ -182,7 +186,18 @@ static BinC make_binc(double bmin, double w) {
 // formed in double-float (error < 1e-12 (|q| + |bmin|/w + 1) against the FP64
 // expression); when it lies closer than that to an integer the FP64
 // expression of exact_bin decides, so the bin is the one FP64 gives.
+//
+// First an FP32 estimate: the dropped low parts of x and -bmin, the rounding
+// of 1/w and three roundings keep it within 2^-22 (|x| + |bmin|)/w (< the
+// 4e-7 scale of mscale) of the exact quotient, so away from integers it has
+// the same ceiling; most scores are decided there in a few instructions.
 __device__ __forceinline__ int bin_df(df x, const BinC& B) {
+  {
+    const float q = (x.hi + B.nbmin.x) * B.invw.x;
+    const float n = rintf(q);
+    const float marg = fmaf(fabsf(x.hi) + B.absb, B.mscale, 1e-6f);
+    if (fabsf(q) < 4194304.f && fabsf(q - n) > marg) return (q > n) ? (int)n : (int)n - 1;
+  }
   const df q = df_mul(df_add(x, {B.nbmin.x, B.nbmin.y}), {B.invw.x, B.invw.y});
   const float n = rintf(q.hi);
   const float f = (q.hi - n) + q.lo;
@@ -880,59 +895,71 @@ __global__ void k_reduce_minmax(const double* __restrict__ tmin, const double* _
 
 // Histogram of max(COV, bmin + w) over the valid pairs of several alignments
 // (src/covariation.c:431-432), bins b = ceil((x - bmin)/w - 1).  One pass:
-// each CTA (1024 threads, one per pair of a tile) keeps a private window of
-// up to 48K 32-bit counters in shared memory starting at bin wbase (the bin
-// of the smallest score), counts its (tile, alignment) items there with one
-// atomic per distinct bin of a warp, and sends the sparse bins above the
-// window straight to the global histogram.  Four tiles' loads are issued
-// before any is binned.
+// each CTA keeps a private window of up to 48K 32-bit counters in shared
+// memory starting at bin wbase (the bin of the smallest score), counts its
+// (tile, alignment) items there with one shared-memory atomic per score, and
+// sends the sparse bins above the window straight to the global histogram.
+// A CTA is R groups of 256 threads (R = 4 when the window leaves room for one
+// CTA per SM, else 1), each group walking its own items; a thread reads four
+// scores of a tile with two 16-byte loads, and the items advance by the
+// number of groups without divisions, two items' loads issued before either
+// is binned.
 constexpr int HIST_WIN = 48 * 1024;
-constexpr int HIST_UNROLL = 4;
 
-__global__ void __launch_bounds__(1024, 1)
+__device__ __forceinline__ void hist_add(df x, int i, int j, int L, const BinC& B, int nbcap, int wbase, int nwin,
+                                         unsigned int* sh, unsigned long long* obs, int* status) {
+  if (!(i < j && j < L)) return;
+  int bin = bin_clamped(x, B);
+  if (bin < 0 || bin >= nbcap) { atomicExch(status, 4); return; }
+  const int rel = bin - wbase;
+  if (rel >= 0 && rel < nwin) atomicAdd(sh + rel, 1u);
+  else                        atomicAdd(obs + bin, 1ull);
+}
+
+__global__ void __launch_bounds__(1024)
 k_hist(const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __restrict__ tiles, int ntiles, int nslots,
        int L, BinC B, int nbcap, int wbase, int nwin, unsigned long long* __restrict__ obs, int* __restrict__ status) {
   extern __shared__ unsigned int sh[];
-  const int tid = threadIdx.x, a = tid >> 5, b = tid & 31;
-  for (int k = tid; k < nwin; k += blockDim.x) sh[k] = 0u;
+  for (int k = threadIdx.x; k < nwin; k += blockDim.x) sh[k] = 0u;
   __syncthreads();
-  // items (slot, tile) in 32-bit arithmetic: ntiles * nslots < 2^31 (the
-  // host checks), and 64-bit division is emulated in software
-  const int nitems = ntiles * nslots, G = gridDim.x;
-  for (int base = blockIdx.x; base < nitems; base += HIST_UNROLL * G) {
-    float2 v[HIST_UNROLL];
-    bool ok[HIST_UNROLL];
+  // group vb of G = gridDim.x * R groups; its item (slot, t) advances by
+  // G = gs ntiles + gt
+  const int R = blockDim.x >> 8, tid = threadIdx.x & 255;
+  const int vb = blockIdx.x * R + (threadIdx.x >> 8);
+  const int G = gridDim.x * R, gs = G / ntiles, gt = G - gs * ntiles;
+  int slot = vb / ntiles, t = vb - slot * ntiles;
+  auto advance = [&](int& sl, int& tt) { tt += gt; sl += gs; if (tt >= ntiles) { tt -= ntiles; sl++; } };
+  // this thread's scores of a tile: p = 2 (tid + 256 k) + h, k, h in {0, 1}
+  while (slot < nslots) {
+    int slot2 = slot, t2 = t;
+    advance(slot2, t2);
+    const bool two = slot2 < nslots;
+    float4 v[2][2];
+    const float4* V0 = reinterpret_cast<const float4*>(cov + slot * slot_stride + (int64_t)t * TPP);
 #pragma unroll
-    for (int u = 0; u < HIST_UNROLL; u++) {
-      const int it = base + u * G;
-      ok[u] = false;
-      if (it < nitems) {
-        const int slot = it / ntiles, t = it - slot * ntiles;
-        const TileRC tr = tiles[t];
+    for (int k = 0; k < 2; k++) v[0][k] = V0[tid + 256 * k];
+    if (two) {
+      const float4* V1 = reinterpret_cast<const float4*>(cov + slot2 * slot_stride + (int64_t)t2 * TPP);
+#pragma unroll
+      for (int k = 0; k < 2; k++) v[1][k] = V1[tid + 256 * k];
+    }
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      if (u == 1 && !two) break;
+      const TileRC tr = tiles[u ? t2 : t];
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const int p = 2 * (tid + 256 * k), a = p >> 5, b = p & 31;
         const int i = tr.I * TP + a, j = tr.J * TP + b;
-        ok[u] = (i < j && j < L);
-        if (ok[u]) v[u] = cov[slot * slot_stride + (int64_t)t * TPP + tid];
+        hist_add({v[u][k].x, v[u][k].y}, i, j, L, B, nbcap, wbase, nwin, sh, obs, status);
+        hist_add({v[u][k].z, v[u][k].w}, i, j + 1, L, B, nbcap, wbase, nwin, sh, obs, status);
       }
     }
-#pragma unroll
-    for (int u = 0; u < HIST_UNROLL; u++) {
-      int bin = -1;
-      if (ok[u]) {
-        bin = bin_clamped({v[u].x, v[u].y}, B);
-        if (bin < 0 || bin >= nbcap) { atomicExch(status, 4); bin = -1; }
-      }
-      // one shared-memory atomic per score: null scores spread over many
-      // bins, so a warp rarely holds two of one bin and merging them first
-      // (match_any) costs more than it saves
-      if (bin >= 0) {
-        const int rel = bin - wbase;
-        if (rel >= 0 && rel < nwin) atomicAdd(sh + rel, 1u);
-        else                        atomicAdd(obs + bin, 1ull);
-      }
-    }
+    slot = slot2; t = t2;
+    advance(slot, t);
   }
   __syncthreads();
-  for (int k = tid; k < nwin; k += blockDim.x)
+  for (int k = threadIdx.x; k < nwin; k += blockDim.x)
     if (sh[k]) atomicAdd(obs + wbase + k, (unsigned long long)sh[k]);
 }
 
@@ -1112,14 +1139,23 @@ cudaError_t launch_hist(const float2* cov, int64_t slot_stride, const TileRC* ti
     return true;
   }();
   (void)attr;
-  int dev = 0, nsm = 152;
+  int dev = 0, nsm = 152, occ = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  // 256-thread CTAs while four or more fit on an SM, else 1024-thread ones
+  int threads = 256;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_hist, 256, (size_t)nwin * 4) != cudaSuccess || occ < 4) {
+    threads = 1024;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_hist, 1024, (size_t)nwin * 4) != cudaSuccess || occ < 1)
+      occ = 1;
+  }
+  const int R = threads / 256;
   const int64_t items = (int64_t)ntiles * nslots;
   if (items >= ((int64_t)1 << 30)) return cudaErrorInvalidValue;   // the kernel indexes items in 32 bits
-  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)nsm));
-  k_hist<<<grid, 1024, (size_t)nwin * 4, st>>>(cov, slot_stride, tiles, ntiles, nslots, L, B, nbcap, wbase, nwin, obs,
-                                               status);
+  // whole CTAs, every group with at least one item
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(items / R, (int64_t)nsm * occ));
+  k_hist<<<grid, threads, (size_t)nwin * 4, st>>>(cov, slot_stride, tiles, ntiles, nslots, L, B, nbcap, wbase, nwin,
+                                                  obs, status);
   return cudaGetLastError();
 }
 
