@@ -31,6 +31,14 @@ import time
 
 import numpy as np
 
+
+def pinned_copy(a):
+    """A copy of the array in page-locked host memory, so the end-to-end
+    host-to-device copies are DMA transfers (the array keeps the pinned
+    buffer alive)."""
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -379,8 +387,8 @@ def main():
             dev_ms.append(ms[4])
             cnt_ms.append(ms[1])
             nl += n
-        # end to end: host buffers in, hit lists out
-        pinned_ax, pinned_w = np.ascontiguousarray(ax), np.ascontiguousarray(w)
+        # end to end: host buffers in (page-locked), hit lists out
+        pinned_ax, pinned_w = pinned_copy(ax), pinned_copy(w)
         t0 = time.perf_counter()
         e2e_hits = 0
         for _ in range(args.steps):

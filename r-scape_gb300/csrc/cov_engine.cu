@@ -261,8 +261,14 @@ extern "C" int covgpu_set_weights(covgpu_ctx* ctx, const double* wgt) {
 extern "C" int covgpu_set_alignment(covgpu_ctx* ctx, int slot, const uint8_t* ax) {
   if (slot < 0 || slot >= ctx->maxslots) return fail(ctx, 11, "slot %d out of range", slot);
   CK(cudaSetDevice(ctx->dev));
-  for (int64_t k = 0; k < (int64_t)ctx->N * ctx->L; k++)
-    if (ax[k] > 17) return fail(ctx, 11, "code %d at %lld is not an RNA digital code", ax[k], (long long)k);
+  // the largest code first (a reduction the compiler vectorises); the
+  // position of a bad code is looked up only when there is one
+  const int64_t n = (int64_t)ctx->N * ctx->L;
+  uint8_t mx = 0;
+  for (int64_t k = 0; k < n; k++) mx = std::max(mx, ax[k]);
+  if (mx > 17)
+    for (int64_t k = 0; k < n; k++)
+      if (ax[k] > 17) return fail(ctx, 11, "code %d at %lld is not an RNA digital code", ax[k], (long long)k);
   uint8_t* dst = ctx->d_ax + (size_t)slot * ctx->N * ctx->Lp;
   CK(cudaMemcpy2DAsync(dst, ctx->Lp, ax, ctx->L, ctx->L, ctx->N, cudaMemcpyHostToDevice, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
