@@ -1044,12 +1044,14 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
     {
       double c = 0.0;
       for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tail[b] = c; }
+      for (int b = 0; b < h->nb; b++) tail[b] /= (double)h->Nc;   // the tail branch's p-values
     }
     CK(cudaMemcpyAsync(ctx->d_tail, tail.data(), h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
     EvalTables T;
     T.sf = sf ? ctx->d_sf : nullptr;
-    T.tail = ctx->d_tail;
+    T.ptail = ctx->d_tail;
     T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = (double)P;
+    T.pNc = 1.0 / T.Nc;
     T.thresh = p->thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
     CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
     CK(launch_evalue(ctx->d_cov + (int64_t)q * plane, ctx->d_tiles, ctx->ntiles, L, T, nullptr, ctx->d_nhits,
@@ -1191,8 +1193,9 @@ extern "C" int covgpu_rscape_learned(covgpu_ctx* ctx, const covgpu_params* p, co
   }
   EvalTables T;
   T.sf = ctx->d_sf;
-  T.tail = ctx->d_tail;   // not read: every score takes the fitted branch
+  T.ptail = ctx->d_tail;   // not read: every score takes the fitted branch
   T.bmin = p->bmin; T.w = w; T.phi = -INFINITY; T.xmax = INFINITY; T.Nc = 1.0; T.Nt = (double)P;
+  T.pNc = 1.0;
   T.thresh = p->thresh; T.nb = nb; T.imin = 0; T.imax = nb - 1;
   CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
   CK(launch_evalue(ctx->d_cov, ctx->d_tiles, ctx->ntiles, L, T, nullptr, ctx->d_nhits, ctx->hitcap, ctx->d_hi,
@@ -1384,6 +1387,7 @@ extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void
   std::vector<double> tail(h->nb, 0.0);
   double c = 0.0;
   for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tail[b] = c; }
+  for (int b = 0; b < h->nb; b++) tail[b] /= (double)h->Nc;   // the tail branch's p-values
   if (ctx->sfcap < 2 * h->nb) {
     if (ctx->d_sf) cudaFree(ctx->d_sf);
     if (ctx->d_tail) cudaFree(ctx->d_tail);
@@ -1401,8 +1405,9 @@ extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void
   }
   EvalTables T;
   T.sf = survfit ? ctx->d_sf : nullptr;
-  T.tail = ctx->d_tail;
+  T.ptail = ctx->d_tail;
   T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = Nt;
+  T.pNc = 1.0 / T.Nc;
   T.thresh = thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
   const int64_t plane = (int64_t)ctx->ntiles * TPP;
   double* evt = nullptr;

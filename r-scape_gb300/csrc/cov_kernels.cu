@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstring>
 
 namespace covgpu {
 
@@ -964,11 +965,28 @@ k_hist(const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __rest
 }
 
 // E-value of every pair (cov2evalue at src/covariation.c:2369-2400 with
-// Nc = 1, times the number of tests) and the compacted hit list.
+// Nc = 1, times the number of tests) and the compacted hit list.  The FP64
+// work per pair is one multiply: the quotients of the tail branch are a
+// table (ptail = tail / Nc, divided on the host), the comparisons of x with
+// phi and xmax are decided on x.hi against float brackets two ulps either
+// side (FP64 only inside them), and E < thresh is compared on the bit
+// patterns (non-negative doubles order as their bits).
+struct EvalCmp {
+  float phi_dn, phi_up, xmax_dn, xmax_up;   // x.hi < dn: x < y; x.hi > up: x > y
+  long long thresh_bits;
+  int all;                                   // thresh > 1000: every pair is listed
+};
+
+__device__ __forceinline__ bool ge_df(df x, float dn, float up, double y) {
+  if (x.hi > up) return true;
+  if (x.hi < dn) return false;
+  return df_to_d(x) >= y;
+}
+
 __global__ void __launch_bounds__(256)
 k_evalue(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L, EvalTables T, BinC B,
-         double* __restrict__ evt, int* __restrict__ nhits, int hitcap, int* __restrict__ hi, int* __restrict__ hj,
-         double* __restrict__ hsc, double* __restrict__ hE, double* __restrict__ hp) {
+         EvalCmp K, double* __restrict__ evt, int* __restrict__ nhits, int hitcap, int* __restrict__ hi,
+         int* __restrict__ hj, double* __restrict__ hsc, double* __restrict__ hE, double* __restrict__ hp) {
   const int t = blockIdx.x, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   const float2* V = cov + (int64_t)t * TPP;
@@ -978,21 +996,21 @@ k_evalue(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int n
     double E = INFINITY;
     if (i < j && j < L) {
       const df xv = ld_df(V + p);
-      const double x = df_to_d(xv);
       const int icov = bin_df(xv, B);
       double pv;
-      if (T.sf && icov >= 2 * T.nb - 1)      pv = T.sf[2 * T.nb - 1];
-      else if (T.sf && x >= T.phi)           pv = T.sf[max(icov + 1, 0)];
-      else if (x >= T.xmax)                  pv = 1.0 / T.Nc;
+      if (T.sf && icov >= 2 * T.nb - 1)                     pv = T.sf[2 * T.nb - 1];
+      else if (T.sf && ge_df(xv, K.phi_dn, K.phi_up, T.phi)) pv = T.sf[max(icov + 1, 0)];
+      else if (ge_df(xv, K.xmax_dn, K.xmax_up, T.xmax))      pv = T.pNc;
       else if (icov <= T.imax) {
         const int ic = (icov < T.imin) ? T.imin : icov;
-        if (ic >= T.imax - 1) pv = 1.0 / T.Nc;
-        else                  pv = T.tail[ic] / T.Nc;
+        pv = (ic >= T.imax - 1) ? T.pNc : T.ptail[ic];
       } else pv = INFINITY;
       E = pv * T.Nt;
-      if (E < T.thresh || T.thresh > 1000.0) {
+      const long long eb = __double_as_longlong(E);
+      const bool below = (eb >= 0) ? (eb < K.thresh_bits) : (E < T.thresh);
+      if (below || K.all) {
         const int h = atomicAdd(nhits, 1);
-        if (h < hitcap) { hi[h] = i; hj[h] = j; hsc[h] = x; hE[h] = E; hp[h] = pv; }
+        if (h < hitcap) { hi[h] = i; hj[h] = j; hsc[h] = df_to_d(xv); hE[h] = E; hp[h] = pv; }
       }
     }
     if (evt) evt[(int64_t)t * TPP + p] = E;
@@ -1162,8 +1180,20 @@ cudaError_t launch_hist(const float2* cov, int64_t slot_stride, const TileRC* ti
 cudaError_t launch_evalue(const float2* cov, const TileRC* tiles, int ntiles, int L, const EvalTables& T, double* evt,
                           int* nhits, int hitcap, int* hi, int* hj, double* hsc, double* hE, double* hp,
                           cudaStream_t st) {
-  k_evalue<<<ntiles, 256, 0, st>>>(cov, tiles, ntiles, L, T, make_binc(T.bmin, T.w), evt, nhits, hitcap, hi, hj, hsc,
-                                   hE, hp);
+  auto bracket = [](double y, float& dn, float& up) {
+    const float f = (float)y;
+    up = std::nextafter(std::nextafter(f, INFINITY), INFINITY);
+    dn = std::nextafter(std::nextafter(f, -INFINITY), -INFINITY);
+  };
+  EvalCmp K;
+  bracket(T.phi, K.phi_dn, K.phi_up);
+  bracket(T.xmax, K.xmax_dn, K.xmax_up);
+  // non-negative E < thresh as bit patterns; a negative thresh admits none
+  K.thresh_bits = 0;
+  if (T.thresh > 0.0) std::memcpy(&K.thresh_bits, &T.thresh, sizeof(double));
+  K.all = (T.thresh > 1000.0) ? 1 : 0;
+  k_evalue<<<ntiles, 256, 0, st>>>(cov, tiles, ntiles, L, T, make_binc(T.bmin, T.w), K, evt, nhits, hitcap, hi, hj,
+                                   hsc, hE, hp);
   return cudaGetLastError();
 }
 

@@ -31,8 +31,9 @@ struct StatsArgs {
 // tables of cov2evalue for one null histogram
 struct EvalTables {
   const double* sf;         // survival fit [2*nb] or nullptr
-  const double* tail;       // tail[b] = sum_{i>=b}^{imax} obs[i]
+  const double* ptail;      // ptail[b] = tail[b] / Nc, tail[b] = sum_{i>=b}^{imax} obs[i]
   double        bmin, w, phi, xmax, Nc, Nt, thresh;
+  double        pNc;        // 1 / Nc
   int           nb, imin, imax;
 };
 
