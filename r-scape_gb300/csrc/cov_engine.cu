@@ -68,7 +68,7 @@ struct covgpu_ctx {
   int hitcap = 0;
   double* d_full = nullptr;
   UmmaPlan* umma = nullptr;
-  FitWork* fitw = nullptr;
+  FitWork* fitw[MAXOUT] = {};
   // simulator
   double *d_simQ = nullptr, *d_simT = nullptr, *d_P4 = nullptr, *d_P16 = nullptr;
   unsigned long long *d_C4 = nullptr, *d_C16 = nullptr, *d_R = nullptr;
@@ -171,7 +171,7 @@ extern "C" int covgpu_create(covgpu_ctx** ret, int device, int N, int L, int max
   CK(dalloc(&ctx->d_mm, S * MAXOUT * 2));
   CK(dalloc(&ctx->d_status, 1));
   CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
-  CK(dalloc(&ctx->d_nhits, 1));
+  CK(dalloc(&ctx->d_nhits, MAXOUT));
   if (maxnull > 0 && N > 1) {
     CK(dalloc(&ctx->d_fitch, (size_t)maxnull * (N - 1) * ctx->Lp));
     CK(dalloc(&ctx->d_scratch, (size_t)maxnull * (N - 1) * ctx->Lp));
@@ -192,7 +192,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
                   ctx->d_flush, ctx->d_pmdf, ctx->d_colxf, ctx->d_apcf, ctx->d_evt};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (ctx->umma) umma_plan_destroy(ctx->umma);
-  if (ctx->fitw) fitwork_destroy(ctx->fitw);
+  for (FitWork* f : ctx->fitw) if (f) fitwork_destroy(f);
   void* sims[] = {ctx->d_simQ, ctx->d_simT, ctx->d_P4, ctx->d_P16, ctx->d_C4, ctx->d_C16, ctx->d_R, ctx->d_units,
                   ctx->d_simroot, ctx->d_simstate, ctx->d_nsubs, ctx->d_ndouble, ctx->d_njoin, ctx->d_featscr,
                   ctx->d_feat, ctx->d_gsc, ctx->d_pbscr};
@@ -926,14 +926,38 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   auto MMn = [&](int slot, int q, int k) { return mm[((size_t)slot * ntypes + q) * 2 + k]; };
 
   const int64_t plane = (int64_t)ctx->ntiles * TPP;
-  if (hitcap > 0 && ctx->hitcap < hitcap) {
+  // hit buffers: hitcap per statistic
+  if (hitcap > 0 && ctx->hitcap < hitcap * ntypes) {
     cudaFree(ctx->d_hi); cudaFree(ctx->d_hj); cudaFree(ctx->d_hsc); cudaFree(ctx->d_hE); cudaFree(ctx->d_hp);
-    CK(dalloc(&ctx->d_hi, hitcap)); CK(dalloc(&ctx->d_hj, hitcap));
-    CK(dalloc(&ctx->d_hsc, hitcap)); CK(dalloc(&ctx->d_hE, hitcap)); CK(dalloc(&ctx->d_hp, hitcap));
-    ctx->hitcap = hitcap;
+    const size_t n = (size_t)hitcap * ntypes;
+    CK(dalloc(&ctx->d_hi, n)); CK(dalloc(&ctx->d_hj, n));
+    CK(dalloc(&ctx->d_hsc, n)); CK(dalloc(&ctx->d_hE, n)); CK(dalloc(&ctx->d_hp, n));
+    ctx->hitcap = hitcap * ntypes;
   }
+  // The statistics go through the null histogram, the tail fit, the
+  // survival table and the E-values phase by phase, all statistics in each
+  // phase, so each phase costs one host round trip instead of one per
+  // statistic.
+  struct Stat {
+    bool active = false;
+    double w = 0.0, xmin = INFINITY, xmax = -INFINITY;
+    int nbcum = 0, nb_real = 0, wbase = 0;
+    int64_t obs_off = 0, sf_off = 0, tail_off = 0;
+    ESL_HISTOGRAM* h = nullptr;
+    double pmass = 0.0, newmass = 0.0, mu = 0.0, lambda = 0.0, tau = 0.0;
+    int evals = 0;
+    bool have_sf = false;
+  };
+  struct Stats {
+    Stat q[MAXOUT];
+    ~Stats() { for (auto& x : q) if (x.h) covh_Destroy(x.h); }
+  } S;
+
+  // phase 1: width and bins from the nulls' ranges, the histograms
+  int64_t obs_tot = 0;
   for (int q = 0; q < ntypes; q++) {
     covgpu_result& R = results[q];
+    Stat& X = S.q[q];
     R.nshuffle = ns;
     R.minCOV = MMn(0, q, 0); R.maxCOV = MMn(0, q, 1);
     if (N == 1) { R.status = 2; continue; }
@@ -959,130 +983,204 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
     }
     double bmax_r = R.maxCOV + 5 * w;
     while (fabs(bmax_r - p->bmin) < p->tol) bmax_r += w;
-    const int nb_real = bins_for(p->bmin, bmax_r, w);
-    if (ctx->nbcap < nbcum) {
-      if (ctx->d_obs) cudaFree(ctx->d_obs);
-      CK(dalloc(&ctx->d_obs, nbcum));
-      ctx->nbcap = nbcum;
-    }
-    CK(cudaMemsetAsync(ctx->d_obs, 0, (size_t)nbcum * sizeof(unsigned long long), ctx->st));
+    X.active = true;
+    X.w = w; X.xmin = xmin; X.xmax = xmax; X.nbcum = nbcum;
+    X.nb_real = bins_for(p->bmin, bmax_r, w);
     // the window starts one bin below the smallest null score's bin
-    const int wbase = std::isfinite(xmin) ? std::max(0, (int)std::floor((xmin - p->bmin) / w) - 2) : 0;
-    CK(launch_hist(ctx->d_cov + ((int64_t)1 * ntypes + q) * plane, ntypes * plane, ctx->d_tiles, ctx->ntiles, L, ns,
-                   p->bmin, w, nbcum, wbase, ctx->d_obs, ctx->d_status, ctx->st));
-    ctx->nlaunch += 1;
-    std::vector<uint64_t> obs(nbcum);
-    CK(cudaMemcpyAsync(obs.data(), ctx->d_obs, nbcum * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->st));
+    X.wbase = std::isfinite(xmin) ? std::max(0, (int)std::floor((xmin - p->bmin) / w) - 2) : 0;
+    X.obs_off = obs_tot;
+    obs_tot += nbcum;
+  }
+  if (ctx->nbcap < obs_tot) {
+    if (ctx->d_obs) cudaFree(ctx->d_obs);
+    ctx->d_obs = nullptr;
+    CK(dalloc(&ctx->d_obs, obs_tot));
+    ctx->nbcap = (int)obs_tot;
+  }
+  std::vector<uint64_t> obs(std::max<int64_t>(obs_tot, 1));
+  if (obs_tot > 0) {
+    CK(cudaMemsetAsync(ctx->d_obs, 0, (size_t)obs_tot * sizeof(unsigned long long), ctx->st));
+    for (int q = 0; q < ntypes; q++) {
+      const Stat& X = S.q[q];
+      if (!X.active) continue;
+      CK(launch_hist(ctx->d_cov + ((int64_t)1 * ntypes + q) * plane, ntypes * plane, ctx->d_tiles, ctx->ntiles, L, ns,
+                     p->bmin, X.w, X.nbcum, X.wbase, ctx->d_obs + X.obs_off, ctx->d_status, ctx->st));
+      ctx->nlaunch += 1;
+    }
+    CK(cudaMemcpyAsync(obs.data(), ctx->d_obs, (size_t)obs_tot * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     if ((s = check_status(ctx))) return s;
-    double bmax_c = p->bmin + nbcum * w;
-    ESL_HISTOGRAM* h = covh_Create(p->bmin, bmax_c, w);
+  }
+
+  // phase 2: the histograms on the host, tail by mass, the tail fits
+  // (gamma: likelihood on the device, one search per statistic back to back)
+  auto tf0 = std::chrono::steady_clock::now();
+  bool any_fit = false;
+  for (int q = 0; q < ntypes; q++) {
+    Stat& X = S.q[q];
+    if (!X.active) continue;
+    const int nbcum = X.nbcum;
+    const uint64_t* ob = obs.data() + X.obs_off;
+    double bmax_c = p->bmin + nbcum * X.w;
+    ESL_HISTOGRAM* h = covh_Create(p->bmin, bmax_c, X.w);
     if (!h) return fail(ctx, 5, "out of host memory");
+    X.h = h;
     if (h->nb != nbcum) {   // guard the rounding of (bmax - bmin)/w
       free(h->obs); h->nb = nbcum; h->obs = (uint64_t*)calloc(nbcum, sizeof(uint64_t));
     }
     uint64_t tot = 0;
     int imin = nbcum, imax = -1;
     for (int b = 0; b < nbcum; b++) {
-      h->obs[b] = obs[b]; tot += obs[b];
-      if (obs[b]) { imin = std::min(imin, b); imax = std::max(imax, b); }
+      h->obs[b] = ob[b]; tot += ob[b];
+      if (ob[b]) { imin = std::min(imin, b); imax = std::max(imax, b); }
     }
     h->n = (uint64_t)ns * (uint64_t)P; h->Nc = tot; h->No = tot;
-    h->xmin = xmin; h->xmax = xmax; h->imin = imin; h->imax = imax; h->cmin = imin;
-    if (h->nb < nb_real) {   // src/covariation.c:462-466
-      h->obs = (uint64_t*)realloc(h->obs, sizeof(uint64_t) * nb_real);
-      for (int b = h->nb; b < nb_real; b++) h->obs[b] = 0;
-      h->nb = nb_real;
+    h->xmin = X.xmin; h->xmax = X.xmax; h->imin = imin; h->imax = imax; h->cmin = imin;
+    if (h->nb < X.nb_real) {   // src/covariation.c:462-466
+      h->obs = (uint64_t*)realloc(h->obs, sizeof(uint64_t) * X.nb_real);
+      for (int b = h->nb; b < X.nb_real; b++) h->obs[b] = 0;
+      h->nb = X.nb_real;
     }
-    const double pmass = covh_pmass(h, p->pmass, fracfit);
-    if (std::isnan(pmass)) { covh_Destroy(h); return fail(ctx, 31, "bad null histogram fit, pmass is nan"); }
-    // tail by mass, then the tail fit (gamma: likelihood on the device) and
-    // the survival table on the device (src/covariation.c:1914-1973)
-    double newmass = 0, mu = 0, lambda = 0, tau = 0;
-    auto tf0 = std::chrono::steady_clock::now();
-    newmass = covh_SetTailByMass(h, pmass);
-    int evals = 0;
+    X.pmass = covh_pmass(h, p->pmass, fracfit);
+    if (std::isnan(X.pmass)) return fail(ctx, 31, "bad null histogram fit, pmass is nan");
+    // tail by mass, then the tail fit and the survival table on the device
+    // (src/covariation.c:1914-1973)
+    X.newmass = covh_SetTailByMass(h, X.pmass);
     if (p->doexpfit) {
       double n = 0.0, sk = 0.0;
       for (int b = h->cmin; b <= h->imax; b++) { n += (double)h->obs[b]; sk += (double)(b - h->cmin) * (double)h->obs[b]; }
-      if (n <= 0) { covh_Destroy(h); return fail(ctx, 32, "could not do exponential fit"); }
-      mu = h->phi;
-      lambda = (sk > 0.0) ? log(1.0 + n / sk) / h->w : INFINITY;
+      if (n <= 0) return fail(ctx, 32, "could not do exponential fit");
+      X.mu = h->phi;
+      X.lambda = (sk > 0.0) ? log(1.0 + n / sk) / h->w : INFINITY;
     } else {
-      if (!ctx->fitw) ctx->fitw = fitwork_create();
-      const int fs = gamma_fit_gpu(ctx->fitw, h->obs, h->cmin, h->imax, h->bmin, h->w, h->phi, ctx->st, &mu,
-                                   &lambda, &tau, &evals);
-      if (fs) { covh_Destroy(h); return fail(ctx, 32, "could not do a Gamma fit (%d)", fs); }
+      if (!ctx->fitw[q]) ctx->fitw[q] = fitwork_create();
+      const int fs = gamma_fit_launch(ctx->fitw[q], h->obs, h->cmin, h->imax, h->bmin, h->w, h->phi, ctx->st);
+      if (fs) return fail(ctx, 32, "could not do a Gamma fit (%d)", fs);
+      X.mu = h->phi;
+      any_fit = true;
     }
-    if (ctx->sfcap < 2 * h->nb) {
-      if (ctx->d_sf) cudaFree(ctx->d_sf);
-      if (ctx->d_tail) cudaFree(ctx->d_tail);
-      CK(dalloc(&ctx->d_sf, 2 * h->nb));
-      CK(dalloc(&ctx->d_tail, 2 * h->nb));
-      ctx->sfcap = 2 * h->nb;
+  }
+  if (any_fit) {
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int q = 0; q < ntypes; q++) {
+      Stat& X = S.q[q];
+      if (!X.active || p->doexpfit) continue;
+      const int fs = gamma_fit_collect(ctx->fitw[q], &X.lambda, &X.tau, &X.evals);
+      if (fs) return fail(ctx, 32, "could not do a Gamma fit (%d)", fs);
     }
-    std::vector<double> sfh;
-    double* sf = nullptr;
-    if (!std::isinf(lambda)) {
-      CK(launch_survfit(h->cmin, h->nb, h->bmin, h->w, newmass, p->doexpfit, mu, lambda, tau, ctx->d_sf, ctx->st));
-      sfh.resize(2 * (size_t)h->nb);
-      CK(cudaMemcpyAsync(sfh.data(), ctx->d_sf, sfh.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-      CK(cudaStreamSynchronize(ctx->st));
-      sf = sfh.data();
+  }
+
+  // phase 3: the survival tables on the device
+  int64_t sf_tot = 0, tail_tot = 0;
+  for (int q = 0; q < ntypes; q++) {
+    Stat& X = S.q[q];
+    if (!X.active) continue;
+    X.tail_off = tail_tot;
+    tail_tot += X.h->nb;
+    if (!std::isinf(X.lambda)) { X.have_sf = true; X.sf_off = sf_tot; sf_tot += 2 * (int64_t)X.h->nb; }
+  }
+  if ((int64_t)ctx->sfcap < std::max(sf_tot, tail_tot)) {
+    if (ctx->d_sf) cudaFree(ctx->d_sf);
+    if (ctx->d_tail) cudaFree(ctx->d_tail);
+    ctx->d_sf = nullptr; ctx->d_tail = nullptr; ctx->sfcap = 0;
+    const int64_t cap = std::max(sf_tot, tail_tot);
+    CK(dalloc(&ctx->d_sf, cap));
+    CK(dalloc(&ctx->d_tail, cap));
+    ctx->sfcap = (int)cap;
+  }
+  std::vector<double> sfh(std::max<int64_t>(sf_tot, 1));
+  if (sf_tot > 0) {
+    for (int q = 0; q < ntypes; q++) {
+      const Stat& X = S.q[q];
+      if (!X.have_sf) continue;
+      CK(launch_survfit(X.h->cmin, X.h->nb, X.h->bmin, X.h->w, X.newmass, p->doexpfit, X.mu, X.lambda, X.tau,
+                        ctx->d_sf + X.sf_off, ctx->st));
     }
-    ctx->fit_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tf0).count();
+    CK(cudaMemcpyAsync(sfh.data(), ctx->d_sf, (size_t)sf_tot * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+  }
+  ctx->fit_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tf0).count();
+
+  // phase 4: thresholds and E-value tables on the host, the E-values and
+  // hit lists on the device
+  std::vector<double> tail(std::max<int64_t>(tail_tot, 1), 0.0);
+  for (int q = 0; q < ntypes; q++) {
+    covgpu_result& R = results[q];
+    const Stat& X = S.q[q];
+    if (!X.active) continue;
+    const ESL_HISTOGRAM* h = X.h;
     if (getenv("COVGPU_DEBUG"))
       fprintf(stderr, "covgpu: type %d nb %d tail bins %d fit %.2f ms (%d evaluations) mu %g lambda %g tau %g\n",
-              covtypes[q], h->nb, h->imax - h->cmin + 1, ctx->fit_ms, evals, mu, lambda, tau);
-    R.pmass = pmass; R.newmass = newmass; R.mu = mu; R.lambda = lambda; R.tau = tau;
+              covtypes[q], h->nb, h->imax - h->cmin + 1, ctx->fit_ms, X.evals, X.mu, X.lambda, X.tau);
+    R.pmass = X.pmass; R.newmass = X.newmass; R.mu = X.mu; R.lambda = X.lambda; R.tau = X.tau;
     R.Nt = (uint64_t)P;
-    R.sc_thresh = covh_evalue2cov(p->thresh, (double)P, h, sf);
+    R.sc_thresh = covh_evalue2cov(p->thresh, (double)P, X.h, X.have_sf ? sfh.data() + X.sf_off : nullptr);
     R.h_bmin = h->bmin; R.h_w = h->w; R.h_nb = h->nb; R.h_imin = h->imin; R.h_imax = h->imax; R.h_cmin = h->cmin;
     R.h_n = h->n; R.h_Nc = h->Nc; R.h_No = h->No; R.h_xmin = h->xmin; R.h_xmax = h->xmax; R.h_phi = h->phi;
-    // cov2evalue tables
-    std::vector<double> tail(h->nb, 0.0);
-    {
-      double c = 0.0;
-      for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tail[b] = c; }
-      for (int b = 0; b < h->nb; b++) tail[b] /= (double)h->Nc;   // the tail branch's p-values
+    // cov2evalue tables: the tail branch's p-values tail[b] / Nc
+    double* tq = tail.data() + X.tail_off;
+    double c = 0.0;
+    for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tq[b] = c; }
+    for (int b = 0; b < h->nb; b++) tq[b] /= (double)h->Nc;
+  }
+  int nhit[MAXOUT] = {0, 0, 0, 0};
+  if (tail_tot > 0) {
+    CK(cudaMemcpyAsync(ctx->d_tail, tail.data(), (size_t)tail_tot * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctx->d_nhits, 0, MAXOUT * sizeof(int), ctx->st));
+    for (int q = 0; q < ntypes; q++) {
+      const Stat& X = S.q[q];
+      if (!X.active) continue;
+      const ESL_HISTOGRAM* h = X.h;
+      EvalTables T;
+      T.sf = X.have_sf ? ctx->d_sf + X.sf_off : nullptr;
+      T.ptail = ctx->d_tail + X.tail_off;
+      T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = (double)P;
+      T.pNc = 1.0 / T.Nc;
+      T.thresh = p->thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
+      const size_t ho = (size_t)q * hitcap;
+      CK(launch_evalue(ctx->d_cov + (int64_t)q * plane, ctx->d_tiles, ctx->ntiles, L, T, nullptr, ctx->d_nhits + q,
+                       hitcap, ctx->d_hi + ho, ctx->d_hj + ho, ctx->d_hsc + ho, ctx->d_hE + ho, ctx->d_hp + ho,
+                       ctx->st));
+      ctx->nlaunch += 1;
     }
-    CK(cudaMemcpyAsync(ctx->d_tail, tail.data(), h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-    EvalTables T;
-    T.sf = sf ? ctx->d_sf : nullptr;
-    T.ptail = ctx->d_tail;
-    T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = (double)P;
-    T.pNc = 1.0 / T.Nc;
-    T.thresh = p->thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
-    CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
-    CK(launch_evalue(ctx->d_cov + (int64_t)q * plane, ctx->d_tiles, ctx->ntiles, L, T, nullptr, ctx->d_nhits,
-                     ctx->hitcap, ctx->d_hi, ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->st));
-    ctx->nlaunch += 1;
-    int nh = 0;
-    CK(cudaMemcpyAsync(&nh, ctx->d_nhits, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(nhit, ctx->d_nhits, MAXOUT * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
-    R.nhit = nh;
-    const int nget = std::min(nh, hitcap);
+  }
+  // the hit lists of all statistics, read back together
+  std::vector<int> hi_((size_t)hitcap * ntypes), hj_((size_t)hitcap * ntypes);
+  std::vector<double> hs_((size_t)hitcap * ntypes), hE_((size_t)hitcap * ntypes), hp_((size_t)hitcap * ntypes);
+  bool any_hits = false;
+  for (int q = 0; q < ntypes; q++) {
+    if (!S.q[q].active) continue;
+    results[q].nhit = nhit[q];
+    const int nget = std::min(nhit[q], hitcap);
+    if (nget <= 0 || !hits) continue;
+    const size_t ho = (size_t)q * hitcap;
+    CK(cudaMemcpyAsync(hi_.data() + ho, ctx->d_hi + ho, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hj_.data() + ho, ctx->d_hj + ho, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hs_.data() + ho, ctx->d_hsc + ho, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hE_.data() + ho, ctx->d_hE + ho, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hp_.data() + ho, ctx->d_hp + ho, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    any_hits = true;
+  }
+  if (any_hits) CK(cudaStreamSynchronize(ctx->st));
+  for (int q = 0; q < ntypes; q++) {
+    const Stat& X = S.q[q];
+    if (!X.active) continue;
+    const int nget = std::min(nhit[q], hitcap);
     if (nget > 0 && hits) {
-      std::vector<int> hi(nget), hj(nget);
-      std::vector<double> hs(nget), hE(nget), hp(nget);
-      CK(cudaMemcpyAsync(hi.data(), ctx->d_hi, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
-      CK(cudaMemcpyAsync(hj.data(), ctx->d_hj, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
-      CK(cudaMemcpyAsync(hs.data(), ctx->d_hsc, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-      CK(cudaMemcpyAsync(hE.data(), ctx->d_hE, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-      CK(cudaMemcpyAsync(hp.data(), ctx->d_hp, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-      CK(cudaStreamSynchronize(ctx->st));
-      covgpu_hit* H = hits + (size_t)q * hitcap;
-      for (int k = 0; k < nget; k++) H[k] = covgpu_hit{hi[k], hj[k], hs[k], hE[k], hp[k]};
+      const size_t ho = (size_t)q * hitcap;
+      covgpu_hit* H = hits + ho;
+      for (int k = 0; k < nget; k++) H[k] = covgpu_hit{hi_[ho + k], hj_[ho + k], hs_[ho + k], hE_[ho + k], hp_[ho + k]};
       // the reference lists hits in row-major pair order (src/covariation.c:827-893)
       std::sort(H, H + nget, [](const covgpu_hit& a, const covgpu_hit& b) {
         return (a.i != b.i) ? a.i < b.i : a.j < b.j;
       });
     }
     if (q == 0 && ctx->want_qsum) {
-      null_summary(h, xmax, mu, lambda, tau, ctx->qsum);
+      null_summary(X.h, X.xmax, X.mu, X.lambda, X.tau, ctx->qsum);
       ctx->have_qsum = true;
     }
-    covh_Destroy(h);
   }
   CK(cudaEventRecord(ctx->ev[3], ctx->st));
   CK(cudaEventSynchronize(ctx->ev[3]));

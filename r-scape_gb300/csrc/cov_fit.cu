@@ -412,9 +412,10 @@ cudaError_t launch_survfit(int cmin, int nb, double bmin, double w, double mass,
   return cudaGetLastError();
 }
 
-// 0 ok, 1 empty tail, 2 barrier timeout, 90 CUDA error
-int gamma_fit_gpu(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, double bmin, double w, double phi,
-                  cudaStream_t st, double* ret_mu, double* ret_lambda, double* ret_tau, int* ret_evals) {
+// 0 ok, 1 empty tail, 90 CUDA error; the result is read by gamma_fit_collect
+// once the stream has passed the launch
+int gamma_fit_launch(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, double bmin, double w, double phi,
+                     cudaStream_t st) {
   FitWork& fw = *fwp;
   const double mu = phi;
   // moment estimates of the start, and the non-empty tail bins
@@ -479,14 +480,19 @@ int gamma_fit_gpu(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, doubl
   if (cudaLaunchCooperativeKernel((const void*)k_gam_fit, dim3(G), dim3(32 * W), args, 0, st) != cudaSuccess)
     return 90;
   if (cudaMemcpyAsync(fw.h_out, fw.d_out, sizeof(FitOut), cudaMemcpyDeviceToHost, st) != cudaSuccess) return 90;
-  if (cudaStreamSynchronize(st) != cudaSuccess) return 90;
+  return 0;
+}
+
+// 0 ok, 2 barrier timeout, else the search's status
+int gamma_fit_collect(FitWork* fwp, double* ret_lambda, double* ret_tau, int* ret_evals) {
+  const FitWork& fw = *fwp;
   if (fw.h_out->status) return fw.h_out->status;
-  *ret_mu = mu;
   *ret_lambda = fw.h_out->lambda;
   *ret_tau = fw.h_out->tau;
   if (ret_evals) *ret_evals = fw.h_out->evals;
   return 0;
 }
+
 
 
 

@@ -10,10 +10,14 @@ FitWork* fitwork_create();
 void     fitwork_destroy(FitWork* fw);
 
 // binned ML gamma fit of the tail bins [cmin, imax] of the histogram with
-// counts h_obs, location phi, likelihood evaluated on the device; 0 on success
-int gamma_fit_gpu(FitWork* fw, const uint64_t* h_obs, int cmin, int imax, double bmin,
-                  double w, double phi, cudaStream_t st, double* ret_mu, double* ret_lambda, double* ret_tau,
-                  int* ret_evals);
+// counts h_obs, location mu = phi, likelihood evaluated on the device, in
+// two steps: the launch (inputs copied, search launched, result copied back
+// asynchronously; 0, 1 empty tail or 90 CUDA error) and, once the caller has
+// synchronised the stream, the result (0, 2 barrier timeout, or the
+// search's status)
+int gamma_fit_launch(FitWork* fw, const uint64_t* h_obs, int cmin, int imax, double bmin, double w, double phi,
+                     cudaStream_t st);
+int gamma_fit_collect(FitWork* fw, double* ret_lambda, double* ret_tau, int* ret_evals);
 
 // survfit table [2 nb] of a gamma (doexp = 0) or exponential tail
 cudaError_t launch_survfit(int cmin, int nb, double bmin, double w, double mass, int doexp, double mu, double lambda,
