@@ -162,6 +162,37 @@ def test_rscape_pipeline(covgpu, oracle, N, L, types, counter):
     e.close()
 
 
+def test_rscape_pipeline_fine_bins(covgpu, oracle):
+    """A histogram width of 0.002 puts the null scores over ~10^4 bins, so the
+    histogram kernel runs with its widest shared-memory window (four groups of
+    256 threads per CTA, one CTA per SM); the histogram, the fit and the hits
+    must still match the oracle."""
+    N, L, ns = 200, 120, 8
+    s, w = make(covgpu, N, L, 42, nbp=24)
+    e = covgpu.Engine(N, L, maxslots=ns + 1, maxnull=ns)
+    e.set_tree(s.parent, s.left, s.right)
+    res = e.rscape(s.ax, w, ["GTp", "CHIp"], nshuffle=ns, counter=covgpu.TENSOR, w0=0.002)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    for q, t in enumerate(["GTp", "CHIp"]):
+        ref = oracle.rscape(s.ax, w, T, covtype=t, nshuffle=ns, w0=0.002)
+        g = res[q]
+        assert g["status"] == 0
+        # the bins between the smallest and the largest null score all lie in
+        # the shared-memory window: more than 14,000 of them is the wide launch
+        span = (g["h_xmax"] - g["h_xmin"]) / g["w"]
+        assert span > 14000, (t, span)
+        for k in ("h_nb", "h_imin", "h_imax", "h_cmin", "h_n", "h_Nc", "h_No"):
+            assert g[k] == ref[k], (t, k, g[k], ref[k])
+        assert abs(g["mu"] - ref["mu"]) <= 1e-6 * (abs(ref["mu"]) + 10.0)
+        assert abs(g["lambda_"] - ref["lambda_"]) <= 1e-4 * abs(ref["lambda_"])
+        gh = {(i, j): E for (i, j, sc, E, p) in g["hits"]}
+        rh = {(i, j): E for (i, j, sc, E, p) in ref["hits"]}
+        assert set(gh) == set(rh)
+        for k in rh:
+            assert abs(gh[k] - rh[k]) <= 1e-4 * rh[k] + 1e-300
+    e.close()
+
+
 def test_one_sequence(covgpu):
     s, w = make(covgpu, 2, 40, 1)
     e = covgpu.Engine(1, 40, maxslots=2, maxnull=1)
