@@ -302,7 +302,13 @@ k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ til
   const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   const float* C = cnt + ((int64_t)slot * ntiles + t) * 16 * TPP;
-  df rv[4][4], cv[4][4], nr[4][1], zero[4][1];
+  // every pair's row contributions, column contributions and nseff go to
+  // shared tiles as they are formed (FP32: the double-float sums below take
+  // them with a zero low part), so nothing is held in registers across pairs
+  __shared__ float sr[4][TP][TP + 1];
+  __shared__ float sc[4][TP][TP + 1];
+  __shared__ float sn[TP][TP + 1];
+  __shared__ float2 srow[4][TP];   // diagonal tiles: row sums, added to the column sums
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
@@ -322,60 +328,41 @@ k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ til
     const float invS = ok ? 1.0f / (16e-10f + ne) : 0.f;
 #pragma unroll
     for (int x = 0; x < 4; x++) {
-      rv[k][x] = {ok ? (4e-10f + row[x]) * invS : 0.f, 0.f};
-      cv[k][x] = {ok ? (4e-10f + col[x]) * invS : 0.f, 0.f};
+      sr[x][a][b] = ok ? (4e-10f + row[x]) * invS : 0.f;
+      sc[x][a][b] = ok ? (4e-10f + col[x]) * invS : 0.f;
     }
-    nr[k][0] = {pair ? ne : 0.f, 0.f};
-    zero[k][0] = {0.f, 0.f};
+    sn[a][b] = pair ? ne : 0.f;
   }
-  // row sums over b of rv and column sums over a of cv (both into the
-  // diagonal tile's rows), then row sums of nseff, through one shared tile:
-  // one thread per (value, line) adds its 32 entries in order
-  __shared__ float2 sb[4][TP][TP + 1];
+  __syncthreads();
+  // row sums over b (threads 0-127) and column sums over a (128-255), one
+  // thread per (value, line) adding its 32 entries in order; rows into
+  // part[I][J], columns into part[J][I], both into part[I][I] on a diagonal
+  // tile
   double* P4 = part4 + (int64_t)slot * nT * nT * TP * 4;
   double* PR = partR + (int64_t)slot * nT * nT * TP;
   const bool diag = (tr.I == tr.J);
-  const int c4 = tid >> 5, line = tid & 31;   // threads < 128: value c4, line
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
-#pragma unroll
-    for (int c = 0; c < 4; c++) sb[c][a][b] = make_float2(rv[k][c].hi, rv[k][c].lo);
-  }
-  __syncthreads();
-  df rsum = {0.f, 0.f};
+  const int c4 = (tid >> 5) & 3, line = tid & 31;
+  df sum = {0.f, 0.f};
   if (tid < 128) {
-    for (int b = 0; b < TP; b++) rsum = df_add(rsum, {sb[c4][line][b].x, sb[c4][line][b].y});
-    if (!diag) P4[(((int64_t)tr.I * nT + tr.J) * TP + line) * 4 + c4] = df_to_d(rsum);
+    for (int b = 0; b < TP; b++) sum = df_add_f(sum, sr[c4][line][b]);
+    if (!diag) P4[(((int64_t)tr.I * nT + tr.J) * TP + line) * 4 + c4] = df_to_d(sum);
+    else       srow[c4][line] = make_float2(sum.hi, sum.lo);
+  } else {
+    for (int a = 0; a < TP; a++) sum = df_add_f(sum, sc[c4][a][line]);
+    if (!diag) P4[(((int64_t)tr.J * nT + tr.I) * TP + line) * 4 + c4] = df_to_d(sum);
   }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
-#pragma unroll
-    for (int c = 0; c < 4; c++) sb[c][a][b] = make_float2(cv[k][c].hi, cv[k][c].lo);
+  if (diag) {
+    __syncthreads();
+    if (tid >= 128)
+      P4[(((int64_t)tr.I * nT + tr.I) * TP + line) * 4 + c4] =
+          df_to_d(df_add({srow[c4][line].x, srow[c4][line].y}, sum));
   }
-  __syncthreads();
-  if (tid < 128) {
-    df csum = {0.f, 0.f};
-    for (int a = 0; a < TP; a++) csum = df_add(csum, {sb[c4][a][line].x, sb[c4][a][line].y});
-    if (diag) P4[(((int64_t)tr.I * nT + tr.I) * TP + line) * 4 + c4] = df_to_d(df_add(rsum, csum));
-    else      P4[(((int64_t)tr.J * nT + tr.I) * TP + line) * 4 + c4] = df_to_d(csum);
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
-    sb[0][a][b] = make_float2(nr[k][0].hi, nr[k][0].lo);
-  }
-  __syncthreads();
   if (tid < TP) {
     df ns = {0.f, 0.f};
-    for (int b = 0; b < TP; b++) ns = df_add(ns, {sb[0][tid][b].x, sb[0][tid][b].y});
+    for (int b = 0; b < TP; b++) ns = df_add_f(ns, sn[tid][b]);
     PR[((int64_t)tr.I * nT + tr.J) * TP + tid] = df_to_d(ns);
     if (!diag) PR[((int64_t)tr.J * nT + tr.I) * TP + tid] = 0.0;   // the column sums of nseff are not used
   }
-  (void)zero;
 }
 
 // pm[c][x] = normalise(sum over every tile touching column c); one thread
