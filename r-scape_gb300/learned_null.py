@@ -121,6 +121,23 @@ def relative_summary(X):
     return X.astype(np.float32)
 
 
+def load_training_data(paths, absolute_summary=False):
+    """Features, targets and number of quick nulls of generated families.
+    Files written before the engine gave the quick-null summary as offsets
+    carry no summary="relative" entry; those (or all, with absolute_summary)
+    are converted by relative_summary.  ValueError when the files mix
+    numbers of quick nulls or name none."""
+    zs = [np.load(p) for p in paths]
+    Xs = []
+    for z in zs:
+        rel = "summary" in z and str(z["summary"]) == "relative"
+        Xs.append(z["X"] if (rel and not absolute_summary) else relative_summary(z["X"]))
+    nq = {int(z["nquick"]) for z in zs if "nquick" in z}
+    if len(nq) != 1:
+        raise ValueError("training files mix numbers of quick nulls: %s" % sorted(nq))
+    return np.concatenate(Xs), np.concatenate([z["T"] for z in zs]), nq.pop()
+
+
 def tail_of(r):
     """(mu, log(tau/lambda), log tau) of a gamma tail fit, or None."""
     lam, tau = r["lambda_"], r["tau"]
@@ -356,20 +373,12 @@ def main(argv=None):
         np.savez_compressed(a.out, X=X, T=T, meta=meta, nnull=a.nnull, nquick=a.nquick, summary="relative")
         print(json.dumps(dict(rows=len(X), out=a.out)))
     elif a.cmd == "train":
-        zs = [np.load(p) for p in a.data]
-        # files written before the engine gave the quick summary as offsets
-        # carry no "summary" entry: convert those (or all, when asked)
-        Xs = []
-        for z in zs:
-            rel = "summary" in z and str(z["summary"]) == "relative"
-            Xs.append(z["X"] if (rel and not a.absolute_summary) else relative_summary(z["X"]))
-        X = np.concatenate(Xs)
-        T = np.concatenate([z["T"] for z in zs])
+        try:
+            X, T, nquick = load_training_data(a.data, absolute_summary=a.absolute_summary)
+        except ValueError as e:
+            raise SystemExit(str(e))
         net, info = train_selected(X, T, batch=a.batch, lr=a.lr, log=sys.stderr)
-        nq = {int(z["nquick"]) for z in zs if "nquick" in z}
-        if len(nq) != 1:
-            raise SystemExit("training files mix numbers of quick nulls: %s" % sorted(nq))
-        save(net, a.out, nq.pop())
+        save(net, a.out, nquick)
         print(json.dumps(dict(rows=len(X), **info)))
     else:
         net = load(a.net)

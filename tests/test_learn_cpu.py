@@ -169,3 +169,31 @@ def test_shipped_network_file(oracle):
     nrm = np.concatenate([z["xmean"], z["xstd"], z["ymean"], z["ystd"]]).astype(np.float32)
     y = oracle.mlp_forward(z["params"], nrm, z["xmean"][None, :])
     assert np.all(np.isfinite(y)) and np.all(np.abs(y) < 5)
+
+
+def test_training_data_conversion(tmp_path):
+    """Files without the summary="relative" tag hold the quick-null summary as
+    absolute scores and are converted; tagged files are read as they are;
+    mixed numbers of quick nulls are refused."""
+    ln = _learned_null()
+    rng = np.random.default_rng(4)
+    X = rng.standard_normal((5, 64)).astype(np.float32)
+    X[:, 61] = rng.uniform(-1, 1, 5)             # log m_q
+    T = rng.standard_normal((5, 3)).astype(np.float32)
+    old, new = tmp_path / "old.npz", tmp_path / "new.npz"
+    np.savez(old, X=X, T=T, nquick=10)
+    np.savez(new, X=X, T=T, nquick=10, summary="relative")
+    Xa, Ta, nq = ln.load_training_data([str(old), str(new)])
+    assert nq == 10 and Xa.shape == (10, 64) and np.array_equal(Ta, np.concatenate([T, T]))
+    m = np.exp(X[:, 61].astype(np.float64))
+    assert np.allclose(Xa[:5, 48], (X[:, 48] - X[:, 60]) / m, rtol=1e-5, atol=1e-6)
+    assert np.allclose(Xa[:5, 55], (X[:, 55] - X[:, 60]) / m, rtol=1e-5, atol=1e-6)
+    assert np.allclose(Xa[:5, 49], X[:, 49] / m, rtol=1e-5, atol=1e-6)
+    assert np.array_equal(Xa[:5, :48], X[:, :48]) and np.array_equal(Xa[:5, 60:63], X[:, 60:63])
+    assert np.array_equal(Xa[5:], X)             # tagged: unchanged
+    Xb, _, _ = ln.load_training_data([str(new)], absolute_summary=True)
+    assert np.array_equal(Xb, Xa[:5])             # forced conversion
+    other = tmp_path / "other.npz"
+    np.savez(other, X=X, T=T, nquick=4, summary="relative")
+    with pytest.raises(ValueError):
+        ln.load_training_data([str(new), str(other)])
