@@ -38,6 +38,10 @@ struct covgpu_ctx {
   float* d_wf = nullptr;
   double* d_wd = nullptr;
   std::vector<double> h_w;
+  // host staging of covgpu_rscape (null histograms, survival tables, tail
+  // tables), kept across calls so same-sized calls neither allocate nor clear
+  std::vector<uint64_t> h_obs;
+  std::vector<double> h_sf, h_tail;
   double wtot = 0.0;
   bool have_w = false;
   float* d_cnt = nullptr;
@@ -997,7 +1001,8 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
     CK(dalloc(&ctx->d_obs, obs_tot));
     ctx->nbcap = (int)obs_tot;
   }
-  std::vector<uint64_t> obs(std::max<int64_t>(obs_tot, 1));
+  std::vector<uint64_t>& obs = ctx->h_obs;   // every entry is written by the copy below
+  obs.resize(std::max<int64_t>(obs_tot, 1));
   if (obs_tot > 0) {
     CK(cudaMemsetAsync(ctx->d_obs, 0, (size_t)obs_tot * sizeof(unsigned long long), ctx->st));
     for (int q = 0; q < ntypes; q++) {
@@ -1088,7 +1093,8 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
     CK(dalloc(&ctx->d_tail, cap));
     ctx->sfcap = (int)cap;
   }
-  std::vector<double> sfh(std::max<int64_t>(sf_tot, 1));
+  std::vector<double>& sfh = ctx->h_sf;      // every entry is written by the copy below
+  sfh.resize(std::max<int64_t>(sf_tot, 1));
   if (sf_tot > 0) {
     for (int q = 0; q < ntypes; q++) {
       const Stat& X = S.q[q];
@@ -1103,7 +1109,8 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
 
   // phase 4: thresholds and E-value tables on the host, the E-values and
   // hit lists on the device
-  std::vector<double> tail(std::max<int64_t>(tail_tot, 1), 0.0);
+  std::vector<double>& tail = ctx->h_tail;   // every entry of each statistic is written below
+  tail.resize(std::max<int64_t>(tail_tot, 1));
   for (int q = 0; q < ntypes; q++) {
     covgpu_result& R = results[q];
     const Stat& X = S.q[q];
@@ -1146,34 +1153,39 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
     CK(cudaMemcpyAsync(nhit, ctx->d_nhits, MAXOUT * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
   }
-  // the hit lists of all statistics, read back together
-  std::vector<int> hi_((size_t)hitcap * ntypes), hj_((size_t)hitcap * ntypes);
-  std::vector<double> hs_((size_t)hitcap * ntypes), hE_((size_t)hitcap * ntypes), hp_((size_t)hitcap * ntypes);
-  bool any_hits = false;
+  // the hit lists of all statistics, read back together into one host
+  // staging area sized by the hits found (statistic q's at hoff[q])
+  size_t hoff[MAXOUT + 1] = {0, 0, 0, 0, 0};
   for (int q = 0; q < ntypes; q++) {
-    if (!S.q[q].active) continue;
-    results[q].nhit = nhit[q];
-    const int nget = std::min(nhit[q], hitcap);
-    if (nget <= 0 || !hits) continue;
-    const size_t ho = (size_t)q * hitcap;
-    CK(cudaMemcpyAsync(hi_.data() + ho, ctx->d_hi + ho, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
-    CK(cudaMemcpyAsync(hj_.data() + ho, ctx->d_hj + ho, nget * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
-    CK(cudaMemcpyAsync(hs_.data() + ho, ctx->d_hsc + ho, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-    CK(cudaMemcpyAsync(hE_.data() + ho, ctx->d_hE + ho, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-    CK(cudaMemcpyAsync(hp_.data() + ho, ctx->d_hp + ho, nget * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-    any_hits = true;
+    size_t n = 0;
+    if (S.q[q].active) {
+      results[q].nhit = nhit[q];
+      if (hits) n = (size_t)std::max(0, std::min(nhit[q], hitcap));
+    }
+    hoff[q + 1] = hoff[q] + n;
   }
-  if (any_hits) CK(cudaStreamSynchronize(ctx->st));
+  const size_t nall = hoff[ntypes];
+  std::vector<int> hi_(nall), hj_(nall);
+  std::vector<double> hs_(nall), hE_(nall), hp_(nall);
+  for (int q = 0; q < ntypes; q++) {
+    const size_t n = hoff[q + 1] - hoff[q], o = hoff[q], ho = (size_t)q * hitcap;
+    if (n == 0) continue;
+    CK(cudaMemcpyAsync(hi_.data() + o, ctx->d_hi + ho, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hj_.data() + o, ctx->d_hj + ho, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hs_.data() + o, ctx->d_hsc + ho, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hE_.data() + o, ctx->d_hE + ho, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(hp_.data() + o, ctx->d_hp + ho, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  }
+  if (nall > 0) CK(cudaStreamSynchronize(ctx->st));
   for (int q = 0; q < ntypes; q++) {
     const Stat& X = S.q[q];
     if (!X.active) continue;
-    const int nget = std::min(nhit[q], hitcap);
-    if (nget > 0 && hits) {
-      const size_t ho = (size_t)q * hitcap;
-      covgpu_hit* H = hits + ho;
-      for (int k = 0; k < nget; k++) H[k] = covgpu_hit{hi_[ho + k], hj_[ho + k], hs_[ho + k], hE_[ho + k], hp_[ho + k]};
+    const size_t n = hoff[q + 1] - hoff[q], o = hoff[q];
+    if (n > 0) {
+      covgpu_hit* H = hits + (size_t)q * hitcap;
+      for (size_t k = 0; k < n; k++) H[k] = covgpu_hit{hi_[o + k], hj_[o + k], hs_[o + k], hE_[o + k], hp_[o + k]};
       // the reference lists hits in row-major pair order (src/covariation.c:827-893)
-      std::sort(H, H + nget, [](const covgpu_hit& a, const covgpu_hit& b) {
+      std::sort(H, H + n, [](const covgpu_hit& a, const covgpu_hit& b) {
         return (a.i != b.i) ? a.i < b.i : a.j < b.j;
       });
     }
