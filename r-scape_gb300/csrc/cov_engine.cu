@@ -659,7 +659,8 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
     CK(launch_pair_marg(ctx->d_cnt, L, ctx->d_tiles, ntiles, nT, nslots, ctx->d_part4, ctx->d_partR, ctx->st));
     CK(launch_pm_final(ctx->d_part4, ctx->d_partR, L, Lp, nT, nslots, ctx->d_pm, ctx->d_pmdf, ctx->d_ps,
                        ctx->d_meanp, ctx->d_status, ctx->st));
-    ctx->nlaunch += 4;
+    // operand preparation + count (tensor) or count; marginals, pm, mean p
+    ctx->nlaunch += (counter == COVGPU_COUNT_TENSOR ? 2 : 1) + 3;
   }
   if (need_u) {
     if (!ctx->d_ucnt) CK(dalloc(&ctx->d_ucnt, (size_t)ctx->maxslots * ctx->capntiles * 16 * TPP));
@@ -671,7 +672,7 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
     } else {
       CK(launch_count_simt(ax, sstride, ctx->d_wf, true, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_ucnt, ctx->st));
     }
-    ctx->nlaunch += 1;
+    ctx->nlaunch += (counter == COVGPU_COUNT_TENSOR && ctx->umma) ? 2 : 1;   // FP8 preparation + count
   }
   A.cnt = need_w ? ctx->d_cnt : nullptr;
   A.ucnt = need_u ? ctx->d_ucnt : nullptr;
@@ -1061,6 +1062,7 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
       if (!ctx->fitw[q]) ctx->fitw[q] = fitwork_create();
       const int fs = gamma_fit_launch(ctx->fitw[q], h->obs, h->cmin, h->imax, h->bmin, h->w, h->phi, ctx->st);
       if (fs) return fail(ctx, 32, "could not do a Gamma fit (%d)", fs);
+      ctx->nlaunch += 1;
       X.mu = h->phi;
       any_fit = true;
     }
@@ -1101,6 +1103,7 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
       if (!X.have_sf) continue;
       CK(launch_survfit(X.h->cmin, X.h->nb, X.h->bmin, X.h->w, X.newmass, p->doexpfit, X.mu, X.lambda, X.tau,
                         ctx->d_sf + X.sf_off, ctx->st));
+      ctx->nlaunch += 1;
     }
     CK(cudaMemcpyAsync(sfh.data(), ctx->d_sf, (size_t)sf_tot * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
