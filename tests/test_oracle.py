@@ -152,3 +152,33 @@ def test_rscape_pipeline_small(oracle, covgpu):
     ct = s.ct
     planted = sum(1 for (i, j, sc, E, p) in r["hits"] if ct[i] == j)
     assert planted >= max(1, len(r["hits"]) // 2)
+
+
+def test_c16_statistics_match_definitions(oracle):
+    """CHI, OMES, GT, MI, MIr and MIg of the C16 class from the oracle's own
+    pair probabilities, marginals and nseff, written out cell by cell
+    (src/correlators.c: CHI :92-122, OMES :224-252, GT :359-390, MI :536-561,
+    MIr :659-690, MIg :792-822)."""
+    rng = np.random.default_rng(11)
+    N, L = 40, 9
+    ax = rng.integers(0, 5, size=(N, L)).astype(np.uint8)
+    w = rng.uniform(0.5, 1.5, N)
+    pp, ne, ng, pm, _ = oracle.probs(ax, w)
+    ref = {k: np.zeros((L, L)) for k in ("CHI", "OMES", "GT", "MI", "MIr", "MIg")}
+    for i in range(L):
+        for j in range(i + 1, L):
+            p = pp[i, j].reshape(4, 4)
+            q = np.outer(pm[i], pm[j])
+            o, e = ne[i, j] * p, ne[i, j] * q
+            mi = float(np.sum(p * (np.log(p) - np.log(q))))
+            h = float(-np.sum(p * np.log(p)))
+            ref["CHI"][i, j] = np.sum((o - e) ** 2 / e)
+            ref["OMES"][i, j] = np.sum((o - e) ** 2) / ne[i, j]
+            ref["GT"][i, j] = 2.0 * np.sum(o * np.log(o / e))
+            ref["MI"][i, j] = mi
+            ref["MIr"][i, j] = mi / h if h > 1e-2 else 0.0
+            ref["MIg"][i, j] = mi - ng[i, j] / ne[i, j]
+    iu = np.triu_indices(L, 1)
+    for t, R in ref.items():
+        got, _ = oracle.cov_calculate(t, ax, w, covclass=oracle.C16)
+        assert np.allclose(got[iu], R[iu], rtol=1e-12, atol=1e-12), t
