@@ -182,3 +182,39 @@ def test_c16_statistics_match_definitions(oracle):
     for t, R in ref.items():
         got, _ = oracle.cov_calculate(t, ax, w, covclass=oracle.C16)
         assert np.allclose(got[iu], R[iu], rtol=1e-12, atol=1e-12), t
+
+
+def test_c2_and_cwc_statistics_match_definitions(oracle):
+    """The C2 class (cells merged into allowed and not allowed pairs) and the
+    GT CWC form (allowed cells only) from the oracle's pair probabilities
+    (src/correlators.c: CHI :137-168, OMES :269-301, GT :426-463 and
+    :393-423, MI :575-605, MIr :705-736)."""
+    rng = np.random.default_rng(12)
+    N, L = 30, 8
+    ax = rng.integers(0, 5, size=(N, L)).astype(np.uint8)
+    w = rng.uniform(0.5, 1.5, N)
+    pp, ne, ng, pm, _ = oracle.probs(ax, w)
+    allow = np.asarray(oracle.default_allow()).reshape(4, 4) > 0
+    ref = {k: np.zeros((L, L)) for k in ("CHI", "OMES", "GT", "MI", "MIr", "CWC")}
+    for i in range(L):
+        for j in range(i + 1, L):
+            p = pp[i, j].reshape(4, 4)
+            q = np.outer(pm[i], pm[j])
+            n = ne[i, j]
+            pw, pn, qw, qn = p[allow].sum(), p[~allow].sum(), q[allow].sum(), q[~allow].sum()
+            o, e = n * np.array([pw, pn]), n * np.array([qw, qn])
+            mi = pw * np.log(pw / qw) + pn * np.log(pn / qn)
+            h = -(pw * np.log(pw) + pn * np.log(pn))
+            ref["CHI"][i, j] = np.sum((o - e) ** 2 / e)
+            ref["OMES"][i, j] = np.sum((o - e) ** 2) / n
+            ref["GT"][i, j] = 2.0 * np.sum(o * np.log(o / e))
+            ref["MI"][i, j] = mi
+            ref["MIr"][i, j] = mi / h if h > 1e-2 else 0.0
+            oc, ec = n * p[allow], n * q[allow]
+            ref["CWC"][i, j] = 2.0 * np.sum(oc * np.log(oc / ec))
+    iu = np.triu_indices(L, 1)
+    for t in ("CHI", "OMES", "GT", "MI", "MIr"):
+        got, _ = oracle.cov_calculate(t, ax, w, covclass=oracle.C2)
+        assert np.allclose(got[iu], ref[t][iu], rtol=1e-12, atol=1e-12), t
+    got, _ = oracle.cov_calculate("GT", ax, w, covclass=oracle.CWC)
+    assert np.allclose(got[iu], ref["CWC"][iu], rtol=1e-12, atol=1e-12)
