@@ -106,3 +106,19 @@ def test_histogram_io_roundtrip(covgpu, tmp_path):
     assert sum(int(c) for s, c in lines) == 6
     lib.cov_FreeRankList(r)
     lib.cov_FreeRankList(r2)
+
+
+def test_default_parameters_are_the_reference_defaults(covgpu):
+    """covgpu_params_default against R-scape's defaults: -E 0.05
+    (src/R-scape.c:258), CSELECT with nseqthresh 8 and alenthresh 50 (:345-347),
+    --tol 1e-6 (:426), --fracfit 1.0 and --pmass 0.0005 (:428-429), the null
+    count chosen from the alignment size (:591), BMIN -10, HPTS 400 and W 0.05
+    (src/covariation.h:22-24), and the allowed pairs A-U, C-G and G-U
+    (src/R-scape.c:885-887), gamma tail fit."""
+    p = covgpu.params()
+    assert p.thresh == 0.05 and p.covclass == 3 and p.nseqthresh == 8 and p.alenthresh == 50
+    assert p.tol == 1e-6 and p.fracfit == 1.0 and p.pmass == 0.0005 and p.nshuffle == -1
+    assert p.bmin == -10.0 and p.hpts == 400 and p.w0 == 0.05 and p.doexpfit == 0
+    allow = [p.allow[k] for k in range(16)]
+    pairs = {(x, y) for x in range(4) for y in range(4) if allow[4 * x + y] > 0}
+    assert pairs == {(0, 3), (3, 0), (1, 2), (2, 1), (2, 3), (3, 2)}
