@@ -4,6 +4,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -122,3 +123,38 @@ def test_default_parameters_are_the_reference_defaults(covgpu):
     allow = [p.allow[k] for k in range(16)]
     pairs = {(x, y) for x in range(4) for y in range(4) if allow[4 * x + y] > 0}
     assert pairs == {(0, 3), (3, 0), (1, 2), (2, 1), (2, 3), (3, 2)}
+
+
+def test_histogram_bins_and_tail_survival(covgpu):
+    """Easel's bin rule b = ceil((x - bmin)/w) - 1 puts a score on a bin's upper
+    edge in that bin (bins are (lo, hi]), with the bounds bmin + b w and
+    bmin + (b + 1) w; the gamma and exponential tail survival functions are
+    Q(tau, lambda (x - mu)) and exp(-lambda (x - mu)) (scipy as the check)."""
+    sp = pytest.importorskip("scipy.special")
+    lib = ctypes.CDLL(covgpu.LIBPATH)
+    lib.covh_Create.restype = ctypes.c_void_p
+    lib.covh_Create.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    lib.covh_Destroy.argtypes = [ctypes.c_void_p]
+    lib.covh_Score2Bin.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(ctypes.c_int)]
+    lib.covh_Bin2LBound.restype = ctypes.c_double
+    lib.covh_Bin2LBound.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.covh_Bin2UBound.restype = ctypes.c_double
+    lib.covh_Bin2UBound.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.covh_gamma_surv.restype = ctypes.c_double
+    lib.covh_gamma_surv.argtypes = [ctypes.c_double, ctypes.c_void_p]
+    lib.covh_exp_surv.restype = ctypes.c_double
+    lib.covh_exp_surv.argtypes = [ctypes.c_double, ctypes.c_void_p]
+    h = lib.covh_Create(-10.0, 10.0, 0.5)
+    b = ctypes.c_int()
+    for k in range(1, 40):
+        x = -10.0 + 0.5 * k                       # exactly on an edge
+        assert lib.covh_Score2Bin(h, x, ctypes.byref(b)) == 0 and b.value == k - 1
+        assert lib.covh_Score2Bin(h, x + 0.25, ctypes.byref(b)) == 0 and b.value == k
+        assert lib.covh_Bin2LBound(h, k) == x and lib.covh_Bin2UBound(h, k) == x + 0.5
+    lib.covh_Destroy(h)
+    mu, lam, tau = 2.0, 0.7, 2.5
+    gp = (ctypes.c_double * 3)(mu, lam, tau)
+    ep = (ctypes.c_double * 2)(mu, lam)
+    for x in (2.5, 4.0, 9.0, 30.0):
+        assert lib.covh_gamma_surv(x, gp) == pytest.approx(sp.gammaincc(tau, lam * (x - mu)), rel=1e-10)
+        assert lib.covh_exp_surv(x, ep) == pytest.approx(np.exp(-lam * (x - mu)), rel=1e-12)
