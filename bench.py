@@ -434,7 +434,11 @@ def main():
     out = {
         "metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * step_s, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+f64" if kind == "simt" else "bf16-limbs+f64", "data": "synthetic",
+        # counts: FP16 weight limbs (BF16 beyond N = 8196) and FP8 one-hot on the tensor cores, exact
+        # integer sums in FP32; statistics in double-float (FP32 pairs) with FP64 means and tables
+        "vs_baseline": None, "dtype": ("f32+df32+f64" if kind == "simt"
+                                       else ("f16" if N <= 8196 else "bf16") + "-limbs+e4m3+df32+f64"),
+        "data": "synthetic",
         "config": {"workload": "rRNA-scale alignment N=%d x L=%d, %d nulls, %s" % (N, L, ns, ",".join(TYPES)),
                    "N": N, "L": L, "nshuffle": ns, "statistics": TYPES, "counter": kind,
                    "l2": "flushed (256 MB write) before every step; count tensors 6 GB per statistic pass"},
