@@ -197,3 +197,28 @@ def test_training_data_conversion(tmp_path):
     np.savez(other, X=X, T=T, nquick=4, summary="relative")
     with pytest.raises(ValueError):
         ln.load_training_data([str(new), str(other)])
+
+
+def test_summarize_counts_only_families_with_a_tail():
+    """Medians over the families the network handled that have a pair with
+    true E < 1; pair-set agreement over the families where either side finds
+    an E < 0.05 pair; the simulation saving from the null counts."""
+    ln = _learned_null()
+    rows = [
+        dict(used_net=True, ntail=3, ntrue=1, sim_nulls=10, net_med=0.1, net_agree=1.0, net_nsig=1,
+             quick_med=0.3, quick_agree=0.5, quick_nsig=2),
+        dict(used_net=True, ntail=2, ntrue=0, sim_nulls=10, net_med=0.2, net_agree=0.0, net_nsig=0,
+             quick_med=0.1, quick_agree=1.0, quick_nsig=1),
+        dict(used_net=True, ntail=0, ntrue=0, sim_nulls=10, net_med=float("inf"), net_agree=1.0, net_nsig=0,
+             quick_med=float("inf"), quick_agree=1.0, quick_nsig=0),
+        dict(used_net=False, ntail=4, ntrue=2, sim_nulls=200),
+    ]
+    s = ln.summarize(rows, 200)
+    assert s["families"] == 4 and s["used_net"] == 3 and s["fallback"] == 1 and s["families_with_tail"] == 2
+    assert s["simulated_nulls"] == 230 and s["full_nulls"] == 800
+    assert s["null_reduction"] == pytest.approx(800 / 230)
+    assert s["net_median_rel_E_error"] == pytest.approx(0.15) and s["quick_median_rel_E_error"] == pytest.approx(0.2)
+    assert s["net_better_than_quick"] == 1
+    # agreement: rows 0 (true pairs) and 1 (quick finds one; the net none)
+    assert s["net_pairset_agreement_mean"] == pytest.approx(1.0)
+    assert s["quick_pairset_agreement_mean"] == pytest.approx(0.75)
