@@ -19,6 +19,10 @@ E < 0.05 pair list of the input alignment.
 R-scape's per-pair counting loop (corr_NaivePP -> mutual_naive_ppij, then
 the statistic) and its O(N^2) RAF loop, FP64, on a bounded sample of the
 same pairs, one run per statistic as R-scape scores one statistic per run.
+That arm never loads the GPU library: its alignment comes from the
+generator library alone and the oracle's filter and weights.  Both arms
+also report the count+GT rate alone (count_gt_pairs_per_s), the
+like-for-like figure without RAF's O(N^2) loop.
 """
 import argparse
 import json
@@ -61,6 +65,39 @@ def workload(cg):
     ax = np.ascontiguousarray(s.ax[:, keep])
     w = cg.weights_pb(ax)
     return s, ax, w
+
+
+def workload_reference():
+    """The same alignment for the CPU reference arm, without the GPU library:
+    the generator alone (libcovsynth.so, host code) makes the alignment, and
+    the oracle applies R-scape's gap-column filter and position-based
+    weights."""
+    import ctypes as C
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("rscape_gb300_build", os.path.join(ROOT, "r-scape_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build()
+    lib = C.CDLL(b.SYNTHLIB)
+    u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+    i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    lib.covgpu_synth2.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                                  C.c_double, C.c_double, C.c_uint64, u8p, i32p, i32p, i32p, f64p, f64p, i32p]
+    c = CFG
+    N, L = c["N"], c["L"]
+    ax = np.zeros((N, L), dtype=np.uint8)
+    tree = [np.zeros(N - 1, dtype=np.int32) for _ in range(3)] + [np.zeros(N - 1) for _ in range(2)]
+    ct = np.zeros(L, dtype=np.int32)
+    st = lib.covgpu_synth2(N, L, 0, c["tree_len"], c["nbp"], c["nhelix"], c["hmin"], c["hmax"], c["gap_rate"],
+                           c["gap_mean"], c["seed"], ax, *tree, ct)
+    if st:
+        raise ValueError("synthetic alignment: bad sizes (status %d)" % st)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    ax = np.ascontiguousarray(ax[:, O.gapfilter(ax, None, 0.75)])
+    return ax, O.weights_pb(ax)
 
 
 class ClockSampler:
@@ -240,6 +277,52 @@ def batched_nulls(cg, counter, device, steps=3):
             "column_pairs_per_s": 201 * 400 * 399 / 2 / (t / 1000.0), "timing": "CUDA events, device-resident"}
 
 
+def dropin_flow(cg, e, ax, w, ns):
+    """R-scape's own calling sequence through the reference-named entry points
+    (rscape_cov.h), as R-scape would run it on this workload with GTp:
+    calculate_width_histo on the first null, cov_Calculate in RANSS mode on
+    each of the ns nulls merged into the cumulative null histogram, then
+    cov_Calculate in GIVSS mode on the alignment (src/R-scape.c:1281-1371,
+    1614-1724, 2502).  Timed once in the reference's host-array mode (pp,
+    nseff, ngap, COV and Eval filled on the host by every call) and once in
+    device-resident mode; host wall clock, host alignments in, hit list out.
+    The null alignments come from the engine before the timed region."""
+    import ctypes as C
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("rscape_abi", os.path.join(ROOT, "r-scape_gb300", "rscape_abi.py"))
+    abi = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(abi)
+    lib = abi.setup_lib(cg.LIBPATH)
+    N, L = ax.shape
+    e.make_nulls(CFG["seed"], 0, ns, 1)
+    abc = abi.Alphabet(1, 4, 18)
+    nulls = [abi.MsaHolder(e.get_alignment(1 + k), w, abc) for k in range(ns)]
+    real = abi.MsaHolder(ax, w, abc)
+    code = cg.covtype_code("GTp")
+    out = {"statistic": "GTp", "nulls": ns, "timing": "host wall clock, one flow after a warm-up flow"}
+    for mode, name in ((0, "host_arrays"), (1, "device_resident")):
+        mi = lib.corr_Create(L, N, 0, 8, 50, C.byref(abc), 3)
+        mi.contents.device_resident = mode
+        errbuf = C.create_string_buffer(256)
+        th = abi.Thresh(0, 0.05, 0.0, 0.0)
+        rnd = abi.Rand(CFG["seed"])
+        dt, nhit = None, 0
+        for rep in range(2):
+            data = abi.Data(C.pointer(rnd), 3, None, None, mi, C.pointer(th), 1, 0, abi.RANSS, code, N, -1.0, -10.0,
+                            0.05, 1.0, 0.0005, 0, 0.0, 0.0, 0.0, None, 1e-6, 0, C.cast(errbuf, C.c_char_p))
+            t0 = time.perf_counter()
+            rl, hl, cum = abi.rscape_flow(lib, mi, nulls, real, data, code)
+            dt = time.perf_counter() - t0
+            nhit = hl.contents.nhit
+            lib.cov_FreeHitList(hl)
+            lib.cov_FreeRankList(rl)
+            lib.cov_FreeRankList(cum)
+        lib.corr_Destroy(mi)
+        out[name] = {"seconds": dt, "msas_per_s": 1.0 / dt, "column_pairs_per_s": (ns + 2) * L * (L - 1) / 2 / dt,
+                     "hits": nhit}
+    return out
+
+
 def cpu_reference(ax, w, budget_s, threads):
     """pairs/s of the reference loops on the host: counting + statistic per
     pair (x3: GTp, MIp, CHIp are three runs) and RAF's O(N^2) loop."""
@@ -272,7 +355,8 @@ def cpu_reference(ax, w, budget_s, threads):
     per_pair = 3 * t_count + t_raf
     sample = ("%d pairs of count+GT (rows 0-%d) and %d pairs of RAF of the %dx%d alignment, %d threads; "
               "per pair = 3 x count+statistic + RAF" % (npairs, rows - 1, n, N, L, threads))
-    return 1.0 / per_pair, sample, {"count_stat_s_per_pair": t_count, "raf_s_per_pair": t_raf}
+    return 1.0 / per_pair, sample, {"count_stat_s_per_pair": t_count, "raf_s_per_pair": t_raf,
+                                    "count_gt_pairs_per_s": 1.0 / t_count}
 
 
 def main():
@@ -314,22 +398,22 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    cg = load_covgpu()
-    s, ax, w = workload(cg)
-    N, L = ax.shape
-    P = L * (L - 1) // 2
     ns = CFG["nshuffle"]
-    pairs_step = (ns + 1) * P
     threads = os.cpu_count() or 1
 
     if args.impl == "reference":
         if rank != 0:
             return
-        vals = []
+        ax, w = workload_reference()
+        N, L = ax.shape
+        P = L * (L - 1) // 2
+        pairs_step = (ns + 1) * P
+        vals, cgt = [], []
         for k in range(args.warmup + args.steps):
             v, sample, parts = cpu_reference(ax, w, args.cpu_budget / max(1, args.warmup + args.steps) * 2, threads)
             if k >= args.warmup:
                 vals.append(v)
+                cgt.append(parts["count_gt_pairs_per_s"])
         value = statistics.median(vals)
         out = {"metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": args.gpus,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * pairs_step / value,
@@ -338,12 +422,17 @@ def main():
                "config": {"workload": "rRNA-scale alignment N=%d x L=%d, %d nulls, %s" % (N, L, ns, ",".join(TYPES)),
                           "N": N, "L": L, "nshuffle": ns, "statistics": TYPES},
                "cpu_baseline": {"value": value, "unit": "column-pairs/s", "cores": threads, "kind": "port",
-                                "sample": sample},
+                                "sample": sample, "count_gt_pairs_per_s": statistics.median(cgt)},
                "e2e": {"value": value, "unit": "column-pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                "msas_per_s": value / pairs_step}
         print(json.dumps(out))
         return
 
+    cg = load_covgpu()
+    s, ax, w = workload(cg)
+    N, L = ax.shape
+    P = L * (L - 1) // 2
+    pairs_step = (ns + 1) * P
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
@@ -414,6 +503,7 @@ def main():
     traffic = profile_traffic(kname)
     if args.no_extras:
         cpu_v, cpu_sample, sim, fam, bnull, plain = None, "skipped (--no-extras)", None, None, None, None
+        cpu_parts, dflow = {}, None
     else:
         plain = None
         if counter == 1:
@@ -427,21 +517,23 @@ def main():
             plain = {"counter": "simt", "ms_per_step": ms_s, "value": pairs_step / (ms_s / 1000.0),
                      "tensor_speedup": ms_s / (step_s * 1000.0), "same_pair_sets": same,
                      "pairs_e_lt_thresh": [len(x["hits"]) for x in rs]}
-        cpu_v, cpu_sample, _ = cpu_reference(ax, w, args.cpu_budget, threads)
+        cpu_v, cpu_sample, cpu_parts = cpu_reference(ax, w, args.cpu_budget, threads)
         sim = simulator_rate(cg, e, s, N, L, ns)
         fam = ragged_families(cg, args.families, counter, local, args.family_workers) if args.families > 0 else None
         bnull = batched_nulls(cg, counter, local)
+        dflow = dropin_flow(cg, e, ax, w, ns)
     out = {
         "metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * step_s, "higher_is_better": True, "scaling": "weak",
-        # counts: FP16 weight limbs (BF16 beyond N = 8196) and FP8 one-hot on the tensor cores, exact
-        # integer sums in FP32; statistics in double-float (FP32 pairs) with FP64 means and tables
-        "vs_baseline": None, "dtype": ("f32+df32+f64" if kind == "simt"
-                                       else ("f16" if N <= 8196 else "bf16") + "-limbs+e4m3+df32+f64"),
+        # counts: three FP16 weight limbs (33-bit weights at this N) and the FP8 one-hot on the tensor
+        # cores (the SIMT path: the same limbs as FP32), exact integer sums in FP32 combined into
+        # double-float counts; statistics in double-float (FP32 pairs) with FP64 means and tables
+        "vs_baseline": None, "dtype": ("f32-limbs+df32+f64" if kind == "simt" else "f16x3-limbs+e4m3+df32+f64"),
         "data": "synthetic",
         "config": {"workload": "rRNA-scale alignment N=%d x L=%d, %d nulls, %s" % (N, L, ns, ",".join(TYPES)),
                    "N": N, "L": L, "nshuffle": ns, "statistics": TYPES, "counter": kind,
-                   "l2": "flushed (256 MB write) before every step; count tensors 6 GB per statistic pass"},
+                   "l2": "flushed (256 MB write) before every step; double-float count tensors "
+                         "%.1f GB per step" % ((ns + 1) * (L // 32 + 1) * (L // 32 + 2) / 2 * 1024 * 16 * 8 / 1e9)},
         "msas_per_s": world / step_s,
         "e2e": {"value": e2e_value, "unit": "column-pairs/s", "h2d_bytes_per_step": int(ax.nbytes + w.nbytes),
                 "d2h_bytes_per_step": int(e2e_hits * 36 + 4 * 200), "msas_per_s": world / e2e_s},
@@ -450,13 +542,15 @@ def main():
                      "frac": achieved / peak, "traffic": traffic, "kernel": kname,
                      "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback 1.9 PFLOP/s"},
         "cpu_baseline": {"value": cpu_v, "unit": "column-pairs/s", "cores": threads, "kind": "port",
-                         "sample": cpu_sample},
+                         "sample": cpu_sample,
+                         "count_gt_pairs_per_s": cpu_parts["count_gt_pairs_per_s"] if cpu_v else None},
         "hits": [len(x["hits"]) for x in res],
         "simulator": sim,
         "plain_gpu": plain,
         "autotune": tune,
         "ragged_families": fam,
         "batched_nulls": bnull,
+        "dropin_flow": dflow,
         "clocks": clk.summary(),
     }
     print(json.dumps(out))

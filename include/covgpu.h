@@ -168,6 +168,11 @@ int  covgpu_last_timing(const covgpu_ctx *ctx, double *ms5, int *nlaunch);
 /* ---- single-matrix steps behind the reference-named entry points ----
  * COV is a full L x L host matrix (both triangles); NULL uses the device's
  * latest score matrix of slot 0. */
+/* validation of the pair probabilities of slot 0 (corr_ValidateProbs,
+ * src/correlators.c:1499-1545) on the device: every pair's 16 probabilities
+ * (prior 1e-10, from the counts of the last covgpu_score) in [0, 1 + tol] and
+ * summing to 1 within tol.  Returns 0, or 20 when a pair fails. */
+int  covgpu_validate_probs(covgpu_ctx *ctx, double tol);
 /* APC (actype 0) or ASC (1) of COV into out (may alias COV or be NULL);
  * minmax[2] of the corrected off-diagonal scores */
 int  covgpu_correct(covgpu_ctx *ctx, const double *COV, int actype, double *out, double *minmax);
@@ -182,14 +187,19 @@ int  covgpu_evalue_full(covgpu_ctx *ctx, const double *COV, const void *h, const
  * triangles; the diagonal is ignored) into the device buffer d_out (diagonal
  * set to -inf), with the min/max of the corrected scores in d_minmax[2],
  * enqueued on `stream` (a cudaStream_t; NULL = the legacy default stream).
+ * d_out may be d_cov (in place); otherwise the two must not overlap.
  * No counterpart in the reference: this entry point allocates no device
  * memory, for callers that cannot call cudaMalloc (code running inside a
  * stream capture, pooled-memory hosts, real-time callers).  Its scratch is a
  * fixed device array sized for L <= COVGPU_NOALLOC_MAX_L; larger L returns
- * 11.  The first call on a device looks up that array's device address, so
- * make it before any stream capture.  All calls share the array: calls that
- * overlap on the GPU race and must be serialised by the caller.  Returns 0,
- * 11 (bad arguments) or 90 (CUDA error). */
+ * 11.  The first call on a device (and the first after the device's context
+ * was recreated, e.g. by a device reset) looks up that array's device
+ * address, so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  Returns 0, 11 (bad arguments) or 90 (CUDA error).  The work is
+ * asynchronous, so a NaN among the corrected scores (an error in the
+ * reference, "bad covariation") is reported in the result: d_minmax is
+ * then {NaN, NaN}. */
 #define COVGPU_NOALLOC_MAX_L 16384
 int  covgpu_correct_noalloc(const double *d_cov, double *d_out, int L, int actype, double *d_minmax, void *stream);
 

@@ -113,6 +113,15 @@ struct mutual_s {
   int           alenthresh;
   const ESL_ALPHABET *abc;
   void         *gpu;       /* engine state of this object (library-owned) */
+  int           device_resident;   /* 0 (corr_Create's default): every call leaves the reference's
+                                    * host arrays filled, as R-scape expects.  1: pp, nseff and ngap
+                                    * stay on the device (corr_ValidateProbs checks them there), and
+                                    * COV and Eval stay on the device from corr_Calculate* through
+                                    * corr_CalculateCOVCorrected, cov_SignificantPairs_Ranking and
+                                    * cov_CreateHitList (the hit list and minCOV/maxCOV come back);
+                                    * corr_SyncHost copies COV to the host.  A caller sets it after
+                                    * corr_Create when nothing reads those arrays (no power
+                                    * analysis, no CaCoFold), and must not write mi->COV meanwhile. */
 };
 
 typedef struct ranklist_s {
@@ -213,6 +222,9 @@ extern int  corr_Probs(ESL_RANDOMNESS *r, ESL_MSA *msa, ESL_TREE *T, void *ribos
                        METHOD method, double tol, int verbose, char *errbuf);
 extern int  corr_ValidateProbs(struct mutual_s *mi, double tol, int verbose, char *errbuf);
 extern int  corr_COVTYPEString(char **ret_covtype, COVTYPE type, char *errbuf);
+/* No counterpart in the reference: in device-resident mode (mi->device_resident = 1), copies the
+ * device's current score matrix into mi->COV (both triangles, diagonal -inf); a no-op otherwise. */
+extern int  corr_SyncHost(struct mutual_s *mi, char *errbuf);
 extern int  corr_String2COVTYPE(char *covtype, COVTYPE *ret_type, char *errbuf);
 
 /* ---------------- covariation.h (src/covariation.h:27-60) ---------------- */

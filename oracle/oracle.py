@@ -111,6 +111,15 @@ def lib():
         L.orc_mlp_forward.restype = None
         L.orc_mlp_grad.argtypes = [f32p, f32p, f32p, f32p, C.c_int, f64p]
         L.orc_mlp_grad.restype = C.c_double
+        L.orc_raf_counts.argtypes = [u8p, C.c_int, C.c_int, f64p, f64p, f64p]
+        for f in ("orc_agg_fisher", "orc_agg_sidak"):
+            getattr(L, f).argtypes = [C.c_int, f64p]
+            getattr(L, f).restype = C.c_double
+        L.orc_agg_weighted.argtypes = [C.c_int, f64p, f64p]
+        L.orc_agg_weighted.restype = C.c_double
+        for f in ("orc_agg_weights_lancaster", "orc_agg_weights_wfisher"):
+            getattr(L, f).argtypes = [C.c_int, f64p, f64p]
+            getattr(L, f).restype = None
         _LIB = L
     return _LIB
 
@@ -384,3 +393,32 @@ def raf_pairs(ax, pairs, allow=None):
     allow = default_allow() if allow is None else np.ascontiguousarray(allow, dtype=np.float64)
     lib().orc_raf_pairs(ax, N, L, allow, len(pairs), pi, pj, out)
     return out
+
+
+AGG_FISHER, AGG_LANCASTER, AGG_WFISHER, AGG_SIDAK = 0, 1, 2, 3
+
+
+def agg_weights(method, aux):
+    """extract_rm_weights_lancaster (1 + substitutions) or
+    extract_rm_weights_wfisher ((0.01 + power), scaled to sum 2n) of one
+    helix (src/aggregate.c:375-488)."""
+    aux = np.ascontiguousarray(aux, dtype=np.float64)
+    w = np.zeros(len(aux))
+    if method == AGG_LANCASTER:
+        lib().orc_agg_weights_lancaster(len(aux), aux, w)
+    else:
+        lib().orc_agg_weights_wfisher(len(aux), aux, w)
+    return w
+
+
+def agg_pvalue(method, pvals, aux=None):
+    """The aggregated p-value of one helix (agg_FISHER, agg_LANCASTER,
+    agg_WFISHER, agg_SIDAK of src/aggregate.c:146-322); aux holds the
+    pairs' substitution counts (Lancaster) or powers (weighted Fisher)."""
+    p = np.ascontiguousarray(pvals, dtype=np.float64)
+    n = len(p)
+    if method == AGG_FISHER:
+        return lib().orc_agg_fisher(n, p)
+    if method == AGG_SIDAK:
+        return lib().orc_agg_sidak(n, p)
+    return lib().orc_agg_weighted(n, p, agg_weights(method, aux))

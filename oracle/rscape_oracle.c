@@ -352,13 +352,14 @@ orc_probs(const uint8_t *ax, const double *wgt, int N, int L, double tol,
       for (j = i + 1; j < L; j++) {
         const uint8_t *cj = axT + (size_t)j * N;
         double *p = pp + ((int64_t)i * L + j) * K16;
-        double  ne = 0.0, ng = 0.0;
-        for (x = 0; x < K16; x++) p[x] = 1e-10;
+        double  ne = 0.0, ng = 0.0, c[K16];
+        for (x = 0; x < K16; x++) c[x] = 1e-10;
         for (s = 0; s < N; s++) {
           const int ri = ci[s], rj = cj[s];
-          if (IS_CANON(ri) && IS_CANON(rj)) { ne += wgt[s]; p[ri * K4 + rj] += wgt[s]; }
+          if (IS_CANON(ri) && IS_CANON(rj)) { ne += wgt[s]; c[ri * K4 + rj] += wgt[s]; }
           else                              { ng += wgt[s]; }
         }
+        for (x = 0; x < K16; x++) p[x] = c[x];
         vec_norm(p, K16);
         for (x = 0; x < K4; x++)
           for (y = 0; y < K4; y++)
@@ -518,6 +519,8 @@ orc_stat(int stat, int covclass, int N, int L, int nseqthresh, int alenthresh,
   if (cls == ORC_CSELECT) cls = (N <= nseqthresh || L <= alenthresh) ? ORC_C2 : ORC_C16;
   if (cls == ORC_CWC && stat != ORC_GT) return 1;
   cov_reset(L, COV, minmax);
+  /* pairs are independent: rows over the host threads, then min/max in order */
+#pragma omp parallel for schedule(dynamic, 4) private(j)
   for (i = 0; i < L - 1; i++)
     for (j = i + 1; j < L; j++) {
       const double *p  = pp + ((int64_t)i * L + j) * K16;
@@ -525,16 +528,76 @@ orc_stat(int stat, int covclass, int N, int L, int nseqthresh, int alenthresh,
       if      (cls == ORC_C16) v = pair_c16(stat, ne, ng, p, pm + i * K4, pm + j * K4);
       else if (cls == ORC_C2)  v = pair_c2 (stat, ne, ng, p, pm + i * K4, pm + j * K4, allow);
       else                     v = pair_gt_cwc(ne, p, pm + i * K4, pm + j * K4, allow);
-      cov_set(L, COV, minmax, i, j, v);
+      COV[(int64_t)i * L + j] = COV[(int64_t)j * L + i] = v;
+    }
+  for (i = 0; i < L - 1; i++)
+    for (j = i + 1; j < L; j++) {
+      const double v = COV[(int64_t)i * L + j];
+      if (v < minmax[0]) minmax[0] = v;
+      if (v > minmax[1]) minmax[1] = v;
     }
   return 0;
 }
 
-/* corr_CalculateRAF, src/correlators.c:876-933, unweighted, O(N^2) per pair */
+/* corr_CalculateRAF for deep alignments: the same sums from the unweighted
+ * counts of the allowed cells.  Over the unordered pairs of sequences whose
+ * residues at (i, j) are both allowed, the loop below adds [a_i != b_i] +
+ * [a_j != b_j]; with n_A allowed sequences, r_x of them with x at i and c_y
+ * with y at j, that is (n_A^2 - sum r_x^2)/2 + (n_A^2 - sum c_y^2)/2, an
+ * integer formed exactly.  The pairs are spread over the host threads. */
+int
+orc_raf_counts(const uint8_t *ax, int N, int L, const double *allow, double *COV, double *minmax)
+{
+  uint8_t *axT = malloc((size_t)N * L);
+  int      i, s;
+  if (!axT) return 5;
+  for (s = 0; s < N; s++)
+    for (i = 0; i < L; i++) axT[(size_t)i * N + s] = ax[(size_t)s * L + i];
+  cov_reset(L, COV, minmax);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (i = 0; i < L - 1; i++) {
+    const uint8_t *ci = axT + (size_t)i * N;
+    int j;
+    for (j = i + 1; j < L; j++) {
+      const uint8_t *cj = axT + (size_t)j * N;
+      long long n[K16] = {0}, r[K4] = {0}, c[K4] = {0}, nA = 0, sq = 0;
+      int x, y, t;
+      for (t = 0; t < N; t++) {
+        const int a = ci[t], b = cj[t];
+        if (a < K4 && b < K4) n[a * K4 + b]++;
+      }
+      for (x = 0; x < K4; x++)
+        for (y = 0; y < K4; y++)
+          if (is_allowed(x, y, allow)) { nA += n[x * K4 + y]; r[x] += n[x * K4 + y]; c[y] += n[x * K4 + y]; }
+      for (x = 0; x < K4; x++) sq += r[x] * r[x] + c[x] * c[x];
+      {
+        double cij = (double)(nA * nA - sq / 2), qij = (double)(N - nA);
+        qij /= N;
+        cij /= (N > 1) ? (double)N * ((double)N - 1.0) : 1.0;
+        cij *= 2.0;
+        COV[(int64_t)i * L + j] = COV[(int64_t)j * L + i] = cij - 1.0 * qij;
+      }
+    }
+  }
+  for (i = 0; i < L - 1; i++) {
+    int j;
+    for (j = i + 1; j < L; j++) {
+      const double v = COV[(int64_t)i * L + j];
+      if (v < minmax[0]) minmax[0] = v;
+      if (v > minmax[1]) minmax[1] = v;
+    }
+  }
+  free(axT);
+  return 0;
+}
+
+/* corr_CalculateRAF, src/correlators.c:876-933, unweighted, O(N^2) per pair;
+ * beyond 10^11 sequence-pair x column-pair steps the count form above */
 int
 orc_raf(const uint8_t *ax, int N, int L, const double *allow, double *COV, double *minmax)
 {
   int i, j, s1, s2;
+  if (0.5 * (double)N * N * 0.5 * (double)L * L > 1e11) return orc_raf_counts(ax, N, L, allow, COV, minmax);
   cov_reset(L, COV, minmax);
   for (i = 0; i < L - 1; i++)
     for (j = i + 1; j < L; j++) {
@@ -674,33 +737,53 @@ orc_cov_corrected(int actype, int L, double *COV, double *minmax)
   return 0;
 }
 
+/* the statistic of covtype and its correction, from probabilities already
+ * formed for this alignment (RAF and RAFS read the alignment itself) */
+static int
+cov_from_probs(int covtype, int covclass, const uint8_t *ax, int N, int L, int nseqthresh, int alenthresh,
+               const double *allow, const double *pp, const double *nseff, const double *ngap, const double *pm,
+               double *COV, double *minmax)
+{
+  int base = (covtype / 3) * 3, corr = covtype % 3;   /* 0 none, 1 APC, 2 ASC */
+  int status;
+  if (base == ORC_RAF)       status = orc_raf (ax, N, L, allow, COV, minmax);
+  else if (base == ORC_RAFS) status = orc_rafs(ax, N, L, allow, COV, minmax);
+  else if (base == ORC_CCF)  status = orc_ccf(L, pm, nseff, COV, minmax);
+  else status = orc_stat(base, covclass, N, L, nseqthresh, alenthresh, pp, pm, nseff, ngap, allow, COV, minmax);
+  if (status) return status;
+  if (corr == 1) status = orc_cov_corrected(ORC_APC, L, COV, minmax);
+  if (corr == 2) status = orc_cov_corrected(ORC_ASC, L, COV, minmax);
+  return status;
+}
+
+static int
+needs_probs(int covtype)
+{
+  const int base = (covtype / 3) * 3;
+  return base != ORC_RAF && base != ORC_RAFS;
+}
+
 /* cov_Calculate dispatch, src/covariation.c:63-306 (NONPARAM, no power) */
 int
 orc_cov_calculate(int covtype, int covclass, const uint8_t *ax, const double *wgt, int N, int L,
                   int nseqthresh, int alenthresh, const double *allow, double tol,
                   double *COV, double *minmax)
 {
-  int base = (covtype / 3) * 3, corr = covtype % 3;   /* 0 none, 1 APC, 2 ASC */
+  double *pp = NULL, *nseff = NULL, *ngap = NULL, *pm = NULL, *ps = NULL;
   int status = 0;
-  if (base == ORC_RAF)       status = orc_raf (ax, N, L, allow, COV, minmax);
-  else if (base == ORC_RAFS) status = orc_rafs(ax, N, L, allow, COV, minmax);
-  else {
-    double *pp    = malloc(sizeof(double) * (size_t)L * L * K16);
-    double *nseff = malloc(sizeof(double) * (size_t)L * L);
-    double *ngap  = malloc(sizeof(double) * (size_t)L * L);
-    double *pm    = malloc(sizeof(double) * (size_t)L * K4);
-    double *ps    = malloc(sizeof(double) * (size_t)L * 5);
-    if (!pp || !nseff || !ngap || !pm || !ps) return 1;
-    status = orc_probs(ax, wgt, N, L, tol, pp, nseff, ngap, pm, ps);
-    if (!status) {
-      if (base == ORC_CCF) status = orc_ccf(L, pm, nseff, COV, minmax);
-      else status = orc_stat(base, covclass, N, L, nseqthresh, alenthresh, pp, pm, nseff, ngap, allow, COV, minmax);
-    }
-    free(pp); free(nseff); free(ngap); free(pm); free(ps);
+  if (needs_probs(covtype)) {
+    pp    = malloc(sizeof(double) * (size_t)L * L * K16);
+    nseff = malloc(sizeof(double) * (size_t)L * L);
+    ngap  = malloc(sizeof(double) * (size_t)L * L);
+    pm    = malloc(sizeof(double) * (size_t)L * K4);
+    ps    = malloc(sizeof(double) * (size_t)L * 5);
+    if (!pp || !nseff || !ngap || !pm || !ps) status = 1;
+    if (!status) status = orc_probs(ax, wgt, N, L, tol, pp, nseff, ngap, pm, ps);
   }
-  if (status) return status;
-  if (corr == 1) status = orc_cov_corrected(ORC_APC, L, COV, minmax);
-  if (corr == 2) status = orc_cov_corrected(ORC_ASC, L, COV, minmax);
+  if (!status)
+    status = cov_from_probs(covtype, covclass, ax, N, L, nseqthresh, alenthresh, allow, pp, nseff, ngap, pm, COV,
+                            minmax);
+  free(pp); free(nseff); free(ngap); free(pm); free(ps);
   return status;
 }
 
@@ -1829,4 +1912,93 @@ double orc_mlp_grad(const float *params, const float *nrm, const float *X, const
   }
   free(W);
   return loss / ((double)n * MO);
+}
+
+/* ------------------------------------------------------------------ */
+/* Helix aggregation, src/aggregate.c                                  */
+/* ------------------------------------------------------------------ */
+/* chi-square upper tail Q(df/2, x/2): esl_stats_ChiSquaredTest and
+ * esl_stats_IncompleteGamma's Q, as the reference calls them
+ * (src/aggregate.c:171, 228, 281) */
+static double
+chisq_q(double df, double x)
+{
+  return gamma_q(df / 2.0, x / 2.0);
+}
+
+/* esl_gam_invcdf(P, 0, 1/2, w/2) of src/aggregate.c:216 and :269: the x with
+ * P(w/2, x/2) = P, the lower tail, by bisection of the regularised gamma.
+ * The reference passes P = 1 - p; the same rounding of 1 - p is kept here,
+ * so the upper tail inverted is q = 1 - (1 - p). */
+static double
+chisq_invcdf_lower(double P, double w)
+{
+  double q = 1.0 - P, lo = 0.0, hi = 1.0;
+  int    k;
+  if (q >= 1.0) return 0.0;
+  if (q <= 0.0) return INFINITY;
+  while (chisq_q(w, hi) > q && hi < 1e300) hi *= 2.0;
+  for (k = 0; k < 2000 && hi - lo > 1e-15 * hi; k++) {
+    double mid = 0.5 * (lo + hi);
+    if (chisq_q(w, mid) > q) lo = mid; else hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
+/* agg_FISHER, src/aggregate.c:146-179 */
+double
+orc_agg_fisher(int n, const double *p)
+{
+  double chival = 0.0;
+  int    i;
+  if (n == 1) return p[0];
+  for (i = 0; i < n; i++) chival += -2.0 * log(p[i]);
+  return chisq_q(2.0 * n, chival);
+}
+
+/* agg_LANCASTER, src/aggregate.c:195-238, and agg_WFISHER, :250-291: the
+ * weighted chi-square quantiles of the p-values summed, then the upper tail
+ * with sum_i w_i degrees of freedom */
+double
+orc_agg_weighted(int n, const double *p, const double *w)
+{
+  double df = 0.0, chival = 0.0;
+  int    i;
+  if (n == 1) return p[0];
+  for (i = 0; i < n; i++) df += w[i];
+  for (i = 0; i < n; i++) chival += chisq_invcdf_lower(1.0 - p[i], w[i]);
+  return chisq_q(df, chival);
+}
+
+/* agg_SIDAK, src/aggregate.c:299-322 */
+double
+orc_agg_sidak(int n, const double *p)
+{
+  double pmin = p[0];
+  int    i;
+  if (n == 1) return p[0];
+  for (i = 1; i < n; i++) if (p[i] < pmin) pmin = p[i];
+  return 1.0 - exp((double)n * log(1.0 - pmin));
+}
+
+/* extract_rm_weights_lancaster, src/aggregate.c:375-416 (AGG_SINGLE): the
+ * pair's substitution count plus delta = 1 */
+void
+orc_agg_weights_lancaster(int n, const double *nsubs, double *w)
+{
+  int i;
+  for (i = 0; i < n; i++) w[i] = 1.0 + nsubs[i];
+}
+
+/* extract_rm_weights_wfisher, src/aggregate.c:431-488 (AGG_SINGLE): the
+ * pair's power plus epsilon = 0.01, scaled so that the weights sum to 2n */
+void
+orc_agg_weights_wfisher(int n, const double *power, double *w)
+{
+  double sum = 0.0;
+  int    i;
+  for (i = 0; i < n; i++) w[i] = 0.01 + power[i];
+  for (i = 0; i < n; i++) sum += w[i];
+  if (sum > 0.0)
+    for (i = 0; i < n; i++) w[i] *= 2.0 * n / sum;
 }

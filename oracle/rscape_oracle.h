@@ -188,7 +188,18 @@ void   orc_features(const uint8_t *ax, int N, int L, const double *w, double tre
 void   orc_mlp_forward(const float *params, const float *nrm, const float *X, int n, double *Y);
 double orc_mlp_grad(const float *params, const float *nrm, const float *X, const float *T, int n, double *grad);
 
+/* corr_CalculateRAF from unit counts (exact; the deep-alignment form of orc_raf) */
+int    orc_raf_counts(const uint8_t *ax, int N, int L, const double *allow, double *COV, double *minmax);
+
+/* helix aggregation (src/aggregate.c:146-322, 375-488) */
+double orc_agg_fisher(int n, const double *p);
+double orc_agg_weighted(int n, const double *p, const double *w);   /* Lancaster and weighted Fisher */
+double orc_agg_sidak(int n, const double *p);
+void   orc_agg_weights_lancaster(int n, const double *nsubs, double *w);
+void   orc_agg_weights_wfisher(int n, const double *power, double *w);
+
 #ifdef __cplusplus
 }
 #endif
+
 #endif

@@ -1,5 +1,8 @@
 """Builds libcovgpu.so in place: every .cu with nvcc for sm_103a, every .c
-with gcc, linked into one shared library next to this file."""
+with gcc, linked into one shared library next to this file.  Also
+libcovsynth.so, the synthetic-alignment generator alone (host code of
+cov_synth.cu), which the benchmark's CPU reference arm uses to make its
+input without loading the GPU library."""
 import concurrent.futures as cf
 import glob
 import os
@@ -12,6 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 INC = os.path.join(ROOT, "include")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcovgpu.so")
+SYNTHLIB = os.path.join(HERE, "libcovsynth.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC]
@@ -55,6 +59,11 @@ def build(verbose=False, force=False):
                     print("built", os.path.basename(o))
     if force or jobs or not os.path.exists(LIB):
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lm", "-Xcompiler", "-fopenmp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    if force or jobs or not os.path.exists(SYNTHLIB):
+        cmd = [NVCC] + ARCH + ["-shared", "-o", SYNTHLIB, os.path.join(OBJ, "cov_synth.cu.o"), "-lm"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))

@@ -10,6 +10,10 @@
  * histograms and E-values run on the device from mi->COV.  The host keeps the
  * reference's arrays (pp, nseff, ngap, pm, ps, COV, Eval) so that callers
  * reading them (power_SPAIR_AddMI, CaCoFold, dot plots) see the same layout.
+ * With mi->device_resident set, pp/nseff/ngap and the score matrix stay on
+ * the device instead: no L x L array crosses the bus between
+ * corr_Calculate* and cov_CreateHitList, and corr_SyncHost copies COV back on
+ * request.
  *
  * Scope: the one-set test (SAMPLE_ALL; every pair tested alike).  Files the
  * reference writes from cov_CreateHitList (.cov, .sorted.cov, .power) and
@@ -33,8 +37,17 @@ typedef struct {
   covgpu_ctx *ctx;
   int         have_msa;
   int         have_counts;
+  int         cov_on_dev;  /* device-resident mode: the device holds mi's current scores */
   double     *wgt;        /* weights of the uploaded alignment */
 } gpu_state;
+
+/* the score matrix to hand to the engine: NULL = the device's own copy */
+static const double *
+cov_src(struct mutual_s *mi)
+{
+  gpu_state *g = (gpu_state *)mi->gpu;
+  return (mi->device_resident && g && g->cov_on_dev) ? NULL : mi->COV->mx[0];
+}
 
 static gpu_state *
 gpu(struct mutual_s *mi, char *errbuf)
@@ -207,14 +220,25 @@ allow16(const ESL_DMATRIX *allowpair, double *a)
     for (y = 0; y < 4; y++) a[x * 4 + y] = allowpair ? allowpair->mx[x][y] : ALLOW_DEFAULT[x * 4 + y];
 }
 
+/* covgpu_score on the tensor cores, or on SIMT where the tensor path does
+ * not serve the shape (status 12) */
+static int
+score_dev(gpu_state *g, struct mutual_s *mi, int covtype, int cls, const double *allow, double *mm)
+{
+  int st = covgpu_score(g->ctx, 0, 1, 1, &covtype, cls, mi->nseqthresh, mi->alenthresh, allow, COVGPU_COUNT_TENSOR,
+                        mm);
+  if (st == 12)
+    st = covgpu_score(g->ctx, 0, 1, 1, &covtype, cls, mi->nseqthresh, mi->alenthresh, allow, COVGPU_COUNT_SIMT, mm);
+  return st;
+}
+
 static int
 count_on_device(struct mutual_s *mi, char *errbuf)
 {
   gpu_state *g = (gpu_state *)mi->gpu;
-  int type = GT, st;
+  int st;
   if (!g || !g->have_msa) XFAIL(eslFAIL, errbuf, "no alignment uploaded (call corr_Probs first)");
-  st = covgpu_score(g->ctx, 0, 1, 1, &type, C16, mi->nseqthresh, mi->alenthresh, ALLOW_DEFAULT, COVGPU_COUNT_SIMT,
-                    NULL);
+  st = score_dev(g, mi, GT, C16, ALLOW_DEFAULT, NULL);
   if (st) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
   g->have_counts = 1;
   return eslOK;
@@ -230,6 +254,7 @@ corr_NaivePP(ESL_RANDOMNESS *r, ESL_MSA *msa, struct mutual_s *mi, double tol, i
   if ((st = upload_msa(mi, msa, errbuf))) return st;
   if ((st = count_on_device(mi, errbuf))) return st;
   g = (gpu_state *)mi->gpu;
+  if (mi->device_resident) return eslOK;   /* pp, nseff, ngap stay on the device */
   if (covgpu_get_probs(g->ctx, 0, g->wgt, mi->pp[0][0], mi->nseff[0], mi->ngap[0], NULL, NULL))
     XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
   return eslOK;
@@ -279,15 +304,21 @@ validate_vec(const double *v, int n, double tol)
   return fabs(s - 1.0) > tol;
 }
 
-/* corr_ValidateProbs, src/correlators.c:1499-1545 */
+/* corr_ValidateProbs, src/correlators.c:1499-1545; the pair probabilities
+ * are checked on the device in device-resident mode */
 int
 corr_ValidateProbs(struct mutual_s *mi, double tol, int verbose, char *errbuf)
 {
   int64_t i, j;
+  gpu_state *g = (gpu_state *)mi->gpu;
   (void)verbose;
-  for (i = 0; i < mi->alen - 1; i++)
-    for (j = i + 1; j < mi->alen; j++)
-      if (validate_vec(mi->pp[i][j], 16, tol)) XFAIL(eslFAIL, errbuf, "pp validation failed");
+  if (mi->device_resident && g && g->have_counts) {
+    if (covgpu_validate_probs(g->ctx, tol)) XFAIL(eslFAIL, errbuf, "pp validation failed");
+  } else {
+    for (i = 0; i < mi->alen - 1; i++)
+      for (j = i + 1; j < mi->alen; j++)
+        if (validate_vec(mi->pp[i][j], 16, tol)) XFAIL(eslFAIL, errbuf, "pp validation failed");
+  }
   for (i = 0; i < mi->alen; i++) {
     if (validate_vec(mi->pm[i], 4, tol)) XFAIL(eslFAIL, errbuf, "pm validation failed");
     if (validate_vec(mi->ps[i], 5, tol)) XFAIL(eslFAIL, errbuf, "ps validation failed");
@@ -320,9 +351,11 @@ score_into_cov(struct mutual_s *mi, int covtype, int cls, const ESL_DMATRIX *all
   int st;
   if (!g || !g->have_msa) XFAIL(eslFAIL, errbuf, "no alignment on the device (call corr_Probs first)");
   allow16(allowpair, a);
-  st = covgpu_score(g->ctx, 0, 1, 1, &covtype, cls, mi->nseqthresh, mi->alenthresh, a, COVGPU_COUNT_SIMT, mm);
+  st = score_dev(g, mi, covtype, cls, a, mm);
   if (st) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
-  if (covgpu_get_cov(g->ctx, 0, 0, mi->COV->mx[0])) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  g->cov_on_dev = mi->device_resident;
+  if (!mi->device_resident && covgpu_get_cov(g->ctx, 0, 0, mi->COV->mx[0]))
+    XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
   g->have_counts = 1;
   mi->type = (COVTYPE)covtype;
   mi->minCOV = mm[0];
@@ -447,15 +480,32 @@ corr_CalculateCOVCorrected(ACTYPE actype, struct data_s *data, int shiftnonneg)
   if (actype != APC && actype != ASC) XFAIL(eslFAIL, data->errbuf, "wrong correction type\n");
   if (mi->type >= PTFp) XFAIL(eslFAIL, data->errbuf, "wrong COVTYPE");
   base = ((int)mi->type / 3) * 3;
-  if (covgpu_correct(g->ctx, mi->COV->mx[0], (int)actype, mi->COV->mx[0], mm))
-    XFAIL(eslFAIL, data->errbuf, "bad covariation: %s", covgpu_errmsg(g->ctx));
+  {
+    const double *src = cov_src(mi);
+    if (covgpu_correct(g->ctx, src, (int)actype, src ? mi->COV->mx[0] : NULL, mm))
+      XFAIL(eslFAIL, data->errbuf, "bad covariation: %s", covgpu_errmsg(g->ctx));
+  }
   mi->type = (COVTYPE)(base + (actype == APC ? 1 : 2));
   mi->minCOV = mm[0];
   mi->maxCOV = mm[1];
-  if (shiftnonneg)
+  if (shiftnonneg) {
+    /* shifted on the host, which then holds the scores */
+    if (corr_SyncHost(mi, data->errbuf)) return eslFAIL;
+    g->cov_on_dev = 0;
     for (i = 0; i < L; i++)
       for (j = 0; j < L; j++)
         if (i != j) mi->COV->mx[i][j] -= mi->minCOV;
+  }
+  return eslOK;
+}
+
+/* device-resident mode: the device's score matrix into mi->COV */
+int
+corr_SyncHost(struct mutual_s *mi, char *errbuf)
+{
+  gpu_state *g = (gpu_state *)mi->gpu;
+  if (!mi->device_resident || !g || !g->cov_on_dev) return eslOK;
+  if (covgpu_get_cov(g->ctx, 0, 0, mi->COV->mx[0])) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
   return eslOK;
 }
 
@@ -534,16 +584,24 @@ rank_into(struct mutual_s *mi, ESL_HISTOGRAM *h, char *errbuf)
   int64_t i, j, L = mi->alen;
   int b;
   double lo = h->bmin + h->w, xmin = INFINITY, xmax = -INFINITY;
+  const double *src;
   if (!g) XFAIL(eslFAIL, errbuf, "no device context");
-  if (covgpu_hist_full(g->ctx, mi->COV->mx[0], h->bmin, h->w, h->nb, h->obs))
+  src = cov_src(mi);
+  if (covgpu_hist_full(g->ctx, src, h->bmin, h->w, h->nb, h->obs))
     XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
-  for (i = 0; i < L - 1; i++)
-    for (j = i + 1; j < L; j++) {
-      double v = mi->COV->mx[i][j];
-      double add = (v > lo) ? v : lo;
-      if (add < xmin) xmin = add;
-      if (add > xmax) xmax = add;
-    }
+  if (!src) {
+    /* the binned values are max(COV, lo): their range follows from the scores' */
+    xmin = (mi->minCOV > lo) ? mi->minCOV : lo;
+    xmax = (mi->maxCOV > lo) ? mi->maxCOV : lo;
+  } else {
+    for (i = 0; i < L - 1; i++)
+      for (j = i + 1; j < L; j++) {
+        double v = mi->COV->mx[i][j];
+        double add = (v > lo) ? v : lo;
+        if (add < xmin) xmin = add;
+        if (add > xmax) xmax = add;
+      }
+  }
   h->n = h->Nc = h->No = (uint64_t)(L * (L - 1) / 2);
   h->xmin = xmin; h->xmax = xmax;
   h->imin = h->nb; h->imax = -1;
@@ -637,6 +695,7 @@ cov_CreateHitList(struct data_s *data, struct mutual_s *mi, RANKLIST *ranklist, 
   hl->Nt = (int64_t)ranklist->ht->Nc;
   hl->Nb = (int64_t)ranklist->hb->Nc;
   if (!data->ranklist_null) {   /* naive: every pair with E = 0 */
+    if (corr_SyncHost(mi, data->errbuf)) { free(hl); return eslFAIL; }
     dmx_set(mi->Eval, INFINITY);
     cap = (thresh > 0.0) ? (int)P : 0;
     hl->hit = (HIT *)calloc(cap > 0 ? cap : 1, sizeof(HIT));
@@ -651,9 +710,13 @@ cov_CreateHitList(struct data_s *data, struct mutual_s *mi, RANKLIST *ranklist, 
     if (!g) { free(hl); XFAIL(eslFAIL, data->errbuf, "no device context"); }
     cap = (int)((P < (1 << 22)) ? P : (1 << 22));
     hits = (covgpu_hit *)malloc(sizeof(covgpu_hit) * (cap > 0 ? cap : 1));
-    st = covgpu_evalue_full(g->ctx, mi->COV->mx[0], data->ranklist_null->ha, data->ranklist_null->survfit,
-                            (double)ranklist->ht->Nc, (thresh > MAX_EVAL) ? 2.0 * MAX_EVAL : thresh, mi->Eval->mx[0],
-                            hits, cap, &nhit);
+    {
+      const double *src = cov_src(mi);
+      /* device-resident: neither COV nor Eval comes to the host */
+      st = covgpu_evalue_full(g->ctx, src, data->ranklist_null->ha, data->ranklist_null->survfit,
+                              (double)ranklist->ht->Nc, (thresh > MAX_EVAL) ? 2.0 * MAX_EVAL : thresh,
+                              src ? mi->Eval->mx[0] : NULL, hits, cap, &nhit);
+    }
     if (st) { free(hits); free(hl); XFAIL(eslFAIL, data->errbuf, "%s", covgpu_errmsg(g->ctx)); }
     if (nhit > cap) nhit = cap;
     hl->hit = (HIT *)calloc(nhit > 0 ? nhit : 1, sizeof(HIT));

@@ -6,8 +6,10 @@
 //                    multiple of TP, padding columns hold the gap code.
 //   column tiles     TP x TP blocks of column pairs (i in tile I, j in tile J,
 //                    I <= J), enumerated row by row of the upper triangle.
-//   counts           float [slot][tile][16][TP*TP]: the 4x4 weighted joint
-//                    counts of every pair of the tile, cell-major.
+//   counts           float [slot][tile][16][2][TP*TP]: the 4x4 weighted joint
+//                    counts of every pair of the tile, cell-major, each a
+//                    double-float (hi plane, then lo plane); unit-weight
+//                    counts (RAF) float [slot][tile][16][TP*TP], exact.
 //   scores           float2 [slot][stat][tile][TP*TP], double-float (hi, lo)
 //                    values of the tile-packed COV.
 //   column partials  double [slot][nT][nT][TP][...]: per-tile row sums
@@ -87,23 +89,6 @@ __host__ __device__ __forceinline__ uint32_t feistel_hbits(uint32_t L) {
 }
 
 constexpr uint32_t TAG_FLEAF = 0x11u, TAG_FCHOOSE = 0x12u, TAG_COLPERM = 0x13u, TAG_SUBST = 0x14u;
-
-// g(d) = (1+d) ln(1+d) - d, the non-negative per-cell term of the G-test
-// written as o ln(o/e) - (o - e) = e g((o-e)/e).  For |d| < 1/4,
-// g(d) = d^2 h(d) with h(d) = sum_m (-d)^m / ((m+1)(m+2)) replaced by its
-// degree-7 Chebyshev fit on [-1/4, 1/4] (fit error 3e-9 relative, below the
-// FP32 rounding of the Horner evaluation, 7e-8, as with the full series).
-__device__ __forceinline__ float gfun_poly(float d) {
-  float s = -1.525888499e-02f;
-  s = fmaf(s, d, 1.933413558e-02f);
-  s = fmaf(s, d, -2.374382876e-02f);
-  s = fmaf(s, d, 3.327445686e-02f);
-  s = fmaf(s, d, -5.000115186e-02f);
-  s = fmaf(s, d, 8.333407342e-02f);
-  s = fmaf(s, d, -1.666666567e-01f);
-  s = fmaf(s, d, 0.5f);
-  return d * d * s;
-}
 
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "cov_dev.cuh"
+#include "cov_df.cuh"
 #include "cov_kernels.h"
 #include "cov_fit.h"
 #include "cov_learn.h"
@@ -35,9 +36,12 @@ struct covgpu_ctx {
   TileRC* d_tiles = nullptr;
   int* d_tile_index = nullptr;
   uint8_t* d_ax = nullptr;
-  float* d_wf = nullptr;
   double* d_wd = nullptr;
   std::vector<double> h_w;
+  CountWeights cw;                  // quantised weights of the SIMT counting kernel
+  float* d_limbf = nullptr;         // their limbs as floats [3][N]
+  double wtot_q = 0.0;              // total of the quantised weights
+  float4* d_logtab = nullptr;       // df_log's table
   // host staging of covgpu_rscape (null histograms, survival tables, tail
   // tables), kept across calls so same-sized calls neither allocate nor clear
   std::vector<uint64_t> h_obs;
@@ -48,6 +52,7 @@ struct covgpu_ctx {
   float* d_ucnt = nullptr;
   double *d_part4 = nullptr, *d_partR = nullptr, *d_pm = nullptr, *d_meanp = nullptr, *d_ps = nullptr;
   float2* d_pmdf = nullptr;
+  float4* d_lpi = nullptr;          // {ln pm, 1/pm} as double-floats
   float2 *d_cov = nullptr, *d_cov2 = nullptr;   // score planes as double-float pairs
   float2* d_colxf = nullptr;
   float4* d_apcf = nullptr;
@@ -155,13 +160,20 @@ extern "C" int covgpu_create(covgpu_ctx** ret, int device, int N, int L, int max
   CK(cudaMemcpy(ctx->d_tile_index, tindex.data(), nT2 * sizeof(int), cudaMemcpyHostToDevice));
   CK(dalloc(&ctx->d_ax, S * N * ctx->Lp));
   CK(cudaMemset(ctx->d_ax, 4, S * N * ctx->Lp));
-  CK(dalloc(&ctx->d_wf, N));
+  CK(dalloc(&ctx->d_limbf, (size_t)3 * N));
   CK(dalloc(&ctx->d_wd, N));
-  CK(dalloc(&ctx->d_cnt, S * ntl * 16 * TPP));
+  CK(dalloc(&ctx->d_cnt, S * ntl * 32 * TPP));
+  CK(dalloc(&ctx->d_logtab, LOGTAB_N));
+  {
+    float4 tab[LOGTAB_N];
+    logtab_host(tab);
+    CK(cudaMemcpy(ctx->d_logtab, tab, sizeof(tab), cudaMemcpyHostToDevice));
+  }
   CK(dalloc(&ctx->d_part4, S * nT2 * TP * 4));
   CK(dalloc(&ctx->d_partR, S * nT2 * TP));
   CK(dalloc(&ctx->d_pm, S * ctx->Lp * 4));
   CK(dalloc(&ctx->d_pmdf, S * ctx->Lp * 4));
+  CK(dalloc(&ctx->d_lpi, S * ctx->Lp * 4));
   CK(dalloc(&ctx->d_meanp, S * 4));
   CK(dalloc(&ctx->d_ps, S * ctx->Lp * 5));
   CK(dalloc(&ctx->d_cov, S * MAXOUT * ntl * TPP));
@@ -188,7 +200,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->dev);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
-  void* ptrs[] = {ctx->d_tiles, ctx->d_tile_index, ctx->d_ax, ctx->d_wf, ctx->d_wd, ctx->d_cnt, ctx->d_ucnt,
+  void* ptrs[] = {ctx->d_tiles, ctx->d_tile_index, ctx->d_ax, ctx->d_limbf, ctx->d_logtab, ctx->d_lpi, ctx->d_wd, ctx->d_cnt, ctx->d_ucnt,
                   ctx->d_part4, ctx->d_partR, ctx->d_pm, ctx->d_meanp, ctx->d_ps, ctx->d_cov, ctx->d_cov2,
                   ctx->d_part1, ctx->d_colx, ctx->d_avg, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status,
                   ctx->d_left, ctx->d_right, ctx->d_lnodes, ctx->d_fitch, ctx->d_scratch, ctx->d_obs, ctx->d_sf,
@@ -245,19 +257,24 @@ extern "C" int covgpu_resize(covgpu_ctx* ctx, int N, int L) {
 
 extern "C" int covgpu_set_weights(covgpu_ctx* ctx, const double* wgt) {
   CK(cudaSetDevice(ctx->dev));
-  ctx->h_w.assign(wgt, wgt + ctx->N);
-  std::vector<float> wf(ctx->N);
+  const int N = ctx->N;
   double s = 0.0;
-  for (int i = 0; i < ctx->N; i++) {
+  for (int i = 0; i < N; i++) {
     if (!(wgt[i] >= 0.0) || !std::isfinite(wgt[i])) return fail(ctx, 11, "weight %d is negative or not finite", i);
-    wf[i] = (float)wgt[i];
     s += wgt[i];
   }
+  ctx->h_w.assign(wgt, wgt + N);
   ctx->wtot = s;
-  CK(cudaMemcpyAsync(ctx->d_wd, wgt, ctx->N * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-  CK(cudaMemcpyAsync(ctx->d_wf, wf.data(), ctx->N * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
+  // the counting kernels count quantised weights (make_limbs); the SIMT path
+  // takes the limbs as floats, the tensor path as FP16 operands
+  std::vector<uint16_t> lim((size_t)3 * N);
+  make_limbs(wgt, N, N, lim.data(), &ctx->cw, &ctx->wtot_q);
+  std::vector<float> lf(lim.begin(), lim.end());
+  CK(cudaMemcpyAsync(ctx->d_wd, wgt, N * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+  CK(cudaMemcpyAsync(ctx->d_limbf, lf.data(), lf.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
-  if (ctx->umma) umma_set_weights(ctx->umma, wgt, ctx->N, ctx->st);
+  ctx->cw.d_limbf = ctx->d_limbf;
+  if (ctx->umma) umma_set_weights(ctx->umma, wgt, N, ctx->st);
   ctx->have_w = true;
   return 0;
 }
@@ -652,12 +669,12 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
       CK(umma_count(ctx->umma, ax, sstride, nslots, false, ctx->d_cnt, ctx->st, ctx->ev[4], ctx->ev[5]));
     } else {
       cudaEventRecord(ctx->ev[4], ctx->st);
-      CK(launch_count_simt(ax, sstride, ctx->d_wf, false, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_cnt, ctx->st));
+      CK(launch_count_simt(ax, sstride, ctx->cw, false, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_cnt, ctx->st));
       cudaEventRecord(ctx->ev[5], ctx->st);
     }
     ctx->counted = true;
     CK(launch_pair_marg(ctx->d_cnt, L, ctx->d_tiles, ntiles, nT, nslots, ctx->d_part4, ctx->d_partR, ctx->st));
-    CK(launch_pm_final(ctx->d_part4, ctx->d_partR, L, Lp, nT, nslots, ctx->d_pm, ctx->d_pmdf, ctx->d_ps,
+    CK(launch_pm_final(ctx->d_part4, ctx->d_partR, L, Lp, nT, nslots, ctx->d_pm, ctx->d_pmdf, ctx->d_lpi, ctx->d_ps,
                        ctx->d_meanp, ctx->d_status, ctx->st));
     // operand preparation + count (tensor) or count; marginals, pm, mean p
     ctx->nlaunch += (counter == COVGPU_COUNT_TENSOR ? 2 : 1) + 3;
@@ -670,7 +687,7 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
       for (int k = 0; k < 16; k++) if (allow[k] > 0.0) mask |= 1u << k;
       CK(umma_count(ctx->umma, ax, sstride, nslots, true, ctx->d_ucnt, ctx->st, nullptr, nullptr, mask));
     } else {
-      CK(launch_count_simt(ax, sstride, ctx->d_wf, true, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_ucnt, ctx->st));
+      CK(launch_count_simt(ax, sstride, ctx->cw, true, N, Lp, ctx->d_tiles, ntiles, nslots, ctx->d_ucnt, ctx->st));
     }
     ctx->nlaunch += (counter == COVGPU_COUNT_TENSOR && ctx->umma) ? 2 : 1;   // FP8 preparation + count
   }
@@ -678,14 +695,16 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   A.ucnt = need_u ? ctx->d_ucnt : nullptr;
   A.pm = ctx->d_pm;
   A.pmdf = ctx->d_pmdf;
+  A.lpi = ctx->d_lpi;
+  A.logtab = ctx->d_logtab;
   A.meanp = ctx->d_meanp;
   A.cov = ctx->d_cov;
   A.part1 = ctx->d_part1;
   A.tiles = ctx->d_tiles;
   A.ntiles = ntiles; A.nT = nT; A.L = L; A.Lp = Lp; A.N = N;
   {
-    const float hi = (float)ctx->wtot;
-    A.wtot = make_float2(hi, (float)(ctx->wtot - (double)hi));
+    const float hi = (float)ctx->wtot_q;
+    A.wtot = make_float2(hi, (float)(ctx->wtot_q - (double)hi));
   }
   A.stats = mask;
   A.cls = cls;
@@ -700,6 +719,7 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
     // RAF only: pm is never read, but keep the pointers valid
     CK(cudaMemsetAsync(ctx->d_pm, 0, (size_t)nslots * Lp * 4 * sizeof(double), ctx->st));
     CK(cudaMemsetAsync(ctx->d_pmdf, 0, (size_t)nslots * Lp * 4 * sizeof(float2), ctx->st));
+    CK(cudaMemsetAsync(ctx->d_lpi, 0, (size_t)nslots * Lp * 4 * sizeof(float4), ctx->st));
   }
   CK(launch_stats(A, nslots, ctx->st));
   ctx->nlaunch += 1;
@@ -788,12 +808,14 @@ extern "C" int covgpu_get_probs(covgpu_ctx* ctx, int slot, const double* wgt, do
   }
   if (pp || nseff || ngap) {
     const size_t ntl = ctx->ntiles;
-    std::vector<float> c(ntl * 16 * TPP);
-    CK(cudaMemcpyAsync(c.data(), ctx->d_cnt + (size_t)rel * ntl * 16 * TPP, c.size() * sizeof(float),
+    std::vector<float> c(ntl * 32 * TPP);
+    CK(cudaMemcpyAsync(c.data(), ctx->d_cnt + (size_t)rel * ntl * 32 * TPP, c.size() * sizeof(float),
                        cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
-    double wt = 0.0;
-    for (int s = 0; s < N; s++) wt += wgt ? wgt[s] : ctx->h_w[s];
+    // ngap = (sum of the weights) - nseff, both of the quantised weights the
+    // counts were made from (wgt, when given, for the exact total)
+    double wt = ctx->wtot_q;
+    if (wgt) { wt = 0.0; for (int s = 0; s < N; s++) wt += wgt[s]; }
     std::vector<TileRC> tiles(ntl);
     CK(cudaMemcpy(tiles.data(), ctx->d_tiles, ntl * sizeof(TileRC), cudaMemcpyDeviceToHost));
     if (nseff) for (int64_t k = 0; k < (int64_t)L * L; k++) nseff[k] = 0.0;
@@ -804,7 +826,10 @@ extern "C" int covgpu_get_probs(covgpu_ctx* ctx, int slot, const double* wgt, do
         const int i = tiles[t].I * TP + p / TP, j = tiles[t].J * TP + p % TP;
         if (!(i < j && j < L)) continue;
         double C[16], ne = 0.0, sum = 0.0;
-        for (int q = 0; q < 16; q++) { C[q] = c[(t * 16 + q) * TPP + p]; ne += C[q]; }
+        for (int q = 0; q < 16; q++) {
+          C[q] = (double)c[(t * 32 + 2 * q) * TPP + p] + (double)c[(t * 32 + 2 * q + 1) * TPP + p];
+          ne += C[q];
+        }
         if (nseff) nseff[(int64_t)i * L + j] = nseff[(int64_t)j * L + i] = ne;
         if (ngap) ngap[(int64_t)i * L + j] = wt - ne;
         if (pp) {
@@ -1431,6 +1456,18 @@ extern "C" int covgpu_flush_l2(covgpu_ctx* ctx) {
   if (!ctx->d_flush) CK(dalloc(&ctx->d_flush, n));
   CK(cudaMemsetAsync(ctx->d_flush, ctx->nlaunch & 0xff, n, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
+  return 0;
+}
+
+extern "C" int covgpu_validate_probs(covgpu_ctx* ctx, double tol) {
+  CK(cudaSetDevice(ctx->dev));
+  if (!ctx->counted || ctx->last_first != 0) return fail(ctx, 11, "no weighted counts of slot 0 on the device");
+  CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
+  CK(launch_validate_pp(ctx->d_cnt, ctx->d_tiles, ctx->ntiles, ctx->L, tol, ctx->d_nhits, ctx->st));
+  int bad = 0;
+  CK(cudaMemcpyAsync(&bad, ctx->d_nhits, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  if (bad) return fail(ctx, 20, "pair probabilities failed validation");
   return 0;
 }
 

@@ -20,6 +20,7 @@
 // FP64 is kept for the row/column means, a bin next to a bin boundary, and
 // the E-value tables.
 #include "cov_dev.cuh"
+#include "cov_df.cuh"
 #include "cov_kernels.h"
 
 #include <algorithm>
@@ -48,114 +49,119 @@ __host__ __device__ __forceinline__ int exact_bin(double x, double bmin, double 
 // Counting (plain SIMT path): one CTA per (tile, alignment); 256 threads,
 // each owning a 2x2 block of pairs and 4x16 fp32 accumulators.  Sequences
 // are staged 32 at a time in shared memory as float4 one-hot (i side) and
-// weight-scaled one-hot (j side) vectors; every pair then takes 16 FMAs per
-// sequence.  With unit weights the counts are exact integers (< 2^24).
+// value-scaled one-hot (j side) vectors; every pair then takes 16 FMAs per
+// sequence.  The j-side values are integers (1, or one weight limb of at
+// most 2^b - 1 with N (2^b - 1) < 2^24), so every accumulator holds an exact
+// integer.
+//   MODE_UNIT   unit weights (RAF): FP32 counts, one plane
+//   MODE_EQUAL  all weights equal to w: the unit count times w as a
+//               double-float (unit_count)
+//   MODE_LIMBS  three weight limbs, counted one after the other (limb 2,
+//               then 1, then 0) and combined exactly as limb_count does: the
+//               partial result of the previous limb is kept in the output
+//               planes, which only this thread touches
+// Double-float counts go to two planes per cell, [slot][tile][16][hi|lo][TPP].
 // ------------------------------------------------------------------------
-template <bool UNIT>
+enum CountMode { MODE_UNIT = 0, MODE_EQUAL = 1, MODE_LIMBS = 3 };
+
+template <int MODE>
 __global__ void __launch_bounds__(256, 2)
-k_count_simt(const uint8_t* __restrict__ ax, int64_t slot_stride, const float* __restrict__ w,
-             int N, int Lp, const TileRC* __restrict__ tiles, int ntiles, float* __restrict__ cnt) {
+k_count_simt(const uint8_t* __restrict__ ax, int64_t slot_stride, const float* __restrict__ limbs, int N, int Lp,
+             const TileRC* __restrict__ tiles, int ntiles, float* __restrict__ cnt, float B, float s_hi, float s_lo) {
   __shared__ float4 ohi[32][TP];
   __shared__ float4 whj[32][TP];
   const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   const uint8_t* A = ax + (int64_t)slot * slot_stride;
   const int ty = tid >> 4, tx = tid & 15;
-  float acc[4][16];
+  constexpr int NPASS = (MODE == MODE_LIMBS) ? 3 : 1;
+  const int64_t tbase = (int64_t)slot * ntiles + t;
+#pragma unroll 1
+  for (int pass = 0; pass < NPASS; pass++) {
+    const int limb = NPASS - 1 - pass;     // limbs 2, 1, 0
+    float acc[4][16];
 #pragma unroll
-  for (int p = 0; p < 4; p++)
+    for (int p = 0; p < 4; p++)
 #pragma unroll
-    for (int c = 0; c < 16; c++) acc[p][c] = 0.f;
-
-  for (int s0 = 0; s0 < N; s0 += 32) {
+      for (int c = 0; c < 16; c++) acc[p][c] = 0.f;
+    for (int s0 = 0; s0 < N; s0 += 32) {
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-      const int e = tid + 256 * k;          // 0..2047
-      const int half = e >> 10, s = (e >> 5) & 31, c = e & 31;
-      const int seq = s0 + s;
-      int code = 4;
-      float val = 0.f;
-      if (seq < N) {
-        code = A[(int64_t)seq * Lp + (half ? tr.J : tr.I) * TP + c];
-        val = half ? (UNIT ? 1.f : w[seq]) : 1.f;
+      for (int k = 0; k < 8; k++) {
+        const int e = tid + 256 * k;          // 0..2047
+        const int half = e >> 10, s = (e >> 5) & 31, c = e & 31;
+        const int seq = s0 + s;
+        int code = 4;
+        float val = 0.f;
+        if (seq < N) {
+          code = A[(int64_t)seq * Lp + (half ? tr.J : tr.I) * TP + c];
+          val = (half && MODE == MODE_LIMBS) ? limbs[(int64_t)limb * N + seq] : 1.f;
+        }
+        float4 v;
+        v.x = (code == 0) ? val : 0.f;
+        v.y = (code == 1) ? val : 0.f;
+        v.z = (code == 2) ? val : 0.f;
+        v.w = (code == 3) ? val : 0.f;
+        if (half) whj[s][c] = v; else ohi[s][c] = v;
       }
-      float4 v;
-      v.x = (code == 0) ? val : 0.f;
-      v.y = (code == 1) ? val : 0.f;
-      v.z = (code == 2) ? val : 0.f;
-      v.w = (code == 3) ? val : 0.f;
-      if (half) whj[s][c] = v; else ohi[s][c] = v;
+      __syncthreads();
+      const int smax = min(32, N - s0);
+      for (int s = 0; s < smax; s++) {
+        const float4 i0 = ohi[s][2 * ty], i1 = ohi[s][2 * ty + 1];
+        const float4 j0 = whj[s][2 * tx], j1 = whj[s][2 * tx + 1];
+        const float iv[2][4] = {{i0.x, i0.y, i0.z, i0.w}, {i1.x, i1.y, i1.z, i1.w}};
+        const float jv[2][4] = {{j0.x, j0.y, j0.z, j0.w}, {j1.x, j1.y, j1.z, j1.w}};
+#pragma unroll
+        for (int a = 0; a < 2; a++)
+#pragma unroll
+          for (int b = 0; b < 2; b++)
+#pragma unroll
+            for (int x = 0; x < 4; x++)
+#pragma unroll
+              for (int y = 0; y < 4; y++)
+                acc[a * 2 + b][x * 4 + y] = fmaf(iv[a][x], jv[b][y], acc[a * 2 + b][x * 4 + y]);
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    const int smax = min(32, N - s0);
-    for (int s = 0; s < smax; s++) {
-      const float4 i0 = ohi[s][2 * ty], i1 = ohi[s][2 * ty + 1];
-      const float4 j0 = whj[s][2 * tx], j1 = whj[s][2 * tx + 1];
-      const float iv[2][4] = {{i0.x, i0.y, i0.z, i0.w}, {i1.x, i1.y, i1.z, i1.w}};
-      const float jv[2][4] = {{j0.x, j0.y, j0.z, j0.w}, {j1.x, j1.y, j1.z, j1.w}};
+    if (MODE == MODE_UNIT) {
+      float* out = cnt + tbase * 16 * TPP;
 #pragma unroll
       for (int a = 0; a < 2; a++)
 #pragma unroll
-        for (int b = 0; b < 2; b++)
-#pragma unroll
-          for (int x = 0; x < 4; x++)
-#pragma unroll
-            for (int y = 0; y < 4; y++) acc[a * 2 + b][x * 4 + y] = fmaf(iv[a][x], jv[b][y], acc[a * 2 + b][x * 4 + y]);
+        for (int c = 0; c < 16; c++)
+          *reinterpret_cast<float2*>(out + c * TPP + (2 * ty + a) * TP + 2 * tx) =
+              make_float2(acc[a * 2 + 0][c], acc[a * 2 + 1][c]);
+      continue;
     }
-    __syncthreads();
+    float* out = cnt + tbase * 32 * TPP;
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+      for (int c = 0; c < 16; c++) {
+        float2* hp = reinterpret_cast<float2*>(out + (2 * c) * TPP + (2 * ty + a) * TP + 2 * tx);
+        float2* lp = reinterpret_cast<float2*>(out + (2 * c + 1) * TPP + (2 * ty + a) * TP + 2 * tx);
+        df r[2];
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+          const float d = acc[a * 2 + b][c];
+          if (MODE == MODE_EQUAL) {
+            r[b] = unit_count(d, s_hi, s_lo);
+          } else if (limb == 2) {
+            r[b] = {d * (B * B), 0.f};                       // c2
+          } else if (limb == 1) {
+            const float2 h = *hp;
+            r[b] = two_sum(b ? h.y : h.x, d * B);           // s1 = c2 + c1
+          } else {
+            const float2 h = *hp, l = *lp;
+            const df s2 = two_sum(b ? h.y : h.x, d);        // s1.hi + c0
+            const df q = fast_two_sum(s2.hi, (b ? l.y : l.x) + s2.lo);
+            r[b] = {q.hi * s_hi, q.lo * s_hi};               // times 2^-E
+          }
+        }
+        *hp = make_float2(r[0].hi, r[1].hi);
+        *lp = make_float2(r[0].lo, r[1].lo);
+      }
   }
-  float* out = cnt + ((int64_t)slot * ntiles + t) * 16 * TPP;
-#pragma unroll
-  for (int a = 0; a < 2; a++)
-#pragma unroll
-    for (int c = 0; c < 16; c++) {
-      float2 v = make_float2(acc[a * 2 + 0][c], acc[a * 2 + 1][c]);
-      *reinterpret_cast<float2*>(out + c * TPP + (2 * ty + a) * TP + 2 * tx) = v;
-    }
 }
-
-// double-float arithmetic (pairs of fp32 values, ~48-bit significand)
-struct df { float hi, lo; };
-
-__device__ __forceinline__ df two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  return {s, (a - (s - bb)) + (b - bb)};
-}
-__device__ __forceinline__ df fast_two_sum(float a, float b) {   // |a| >= |b|
-  const float s = a + b;
-  return {s, b - (s - a)};
-}
-__device__ __forceinline__ df df_add_f(df a, float b) {
-  const df s = two_sum(a.hi, b);
-  return fast_two_sum(s.hi, s.lo + a.lo);
-}
-__device__ __forceinline__ df df_add(df a, df b) {
-  const df s = two_sum(a.hi, b.hi);
-  return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
-}
-__device__ __forceinline__ df df_mul(df a, df b) {
-  const float p = a.hi * b.hi;
-  const float e = fmaf(a.hi, b.hi, -p);
-  return fast_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
-}
-__device__ __forceinline__ df df_of(double x) {
-  const float hi = (float)x;
-  return {hi, (float)(x - (double)hi)};
-}
-__device__ __forceinline__ double df_to_d(df a) { return (double)a.hi + (double)a.lo; }
-__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
-// a * b exactly as a double-float (FMA residual)
-__device__ __forceinline__ df two_prod(float a, float b) {
-  const float p = a * b;
-  return {p, fmaf(a, b, -p)};
-}
-__device__ __forceinline__ df ld_df(const float2* p) { const float2 v = *p; return {v.x, v.y}; }
-__device__ __forceinline__ void st_df(float2* p, df v) { *p = make_float2(v.hi, v.lo); }
-// order of normalised double-float values (|lo| <= ulp(hi)/2)
-__device__ __forceinline__ bool df_lt(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
-__device__ __forceinline__ df df_min(df a, df b) { return df_lt(b, a) ? b : a; }
-__device__ __forceinline__ df df_max(df a, df b) { return df_lt(a, b) ? b : a; }
 
 // constants of the bin function, split on the host
 struct BinC {
@@ -290,87 +296,99 @@ __device__ __forceinline__ void tile_rowcol_store(const df (&v)[4][NV], double* 
 }
 
 // Pair-normalised marginal contributions: for every pair with nseff > 0,
-// row i gains (4e-10 + sum_y C(x,y)) / S and column j gains
-// (4e-10 + sum_x C(x,y)) / S, S = 16e-10 + nseff (the prior of
-// src/correlators.c:1713 and the normalisation of :1758).  Each pair's
-// contribution is formed in fp32 (relative error ~1e-7, independent from pair
-// to pair) and summed over partners in FP64, so the marginals keep ~1e-9.
-// Also the upper-triangle row sums of nseff for the CCF column means.
+// row i gains (4e-10 + sum_y C(x,y)) / Z and column j gains
+// (4e-10 + sum_x C(x,y)) / Z, Z = 16e-10 + nseff (the prior of
+// src/correlators.c:1713 and the normalisation of :1758).  The counts are
+// double-float; each contribution is a double-float quotient and the sums
+// over partners are double-float (stored as FP64), so pm keeps ~1e-13.  Also
+// the upper-triangle row sums of nseff for the CCF column means.
+__device__ __forceinline__ df cnt_df(const float* __restrict__ C, int q, int p) {
+  return {C[(2 * q) * TPP + p], C[(2 * q + 1) * TPP + p]};
+}
+
 __global__ void __launch_bounds__(256)
 k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ tiles, int ntiles, int nT,
             double* __restrict__ part4, double* __restrict__ partR) {
   const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
-  const float* C = cnt + ((int64_t)slot * ntiles + t) * 16 * TPP;
-  // every pair's row contributions, column contributions and nseff go to
-  // shared tiles as they are formed (FP32: the double-float sums below take
-  // them with a zero low part), so nothing is held in registers across pairs
-  __shared__ float sr[4][TP][TP + 1];
-  __shared__ float sc[4][TP][TP + 1];
-  __shared__ float sn[TP][TP + 1];
-  __shared__ float2 srow[4][TP];   // diagonal tiles: row sums, added to the column sums
+  const float* C = cnt + ((int64_t)slot * ntiles + t) * 32 * TPP;
+  // one buffer for the row contributions, then for the column ones
+  __shared__ float2 sb[4][TP][TP + 1];
+  __shared__ float2 sn[TP][TP + 1];
+  df colc[4][4];
 #pragma unroll
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
-    float c[16];
+    df row[4], col[4];
 #pragma unroll
-    for (int q = 0; q < 16; q++) c[q] = C[q * TPP + p];
-    float row[4], col[4];
+    for (int x = 0; x < 4; x++) { row[x] = {0.f, 0.f}; col[x] = {0.f, 0.f}; }
 #pragma unroll
-    for (int x = 0; x < 4; x++) {
-      row[x] = (c[x * 4 + 0] + c[x * 4 + 1]) + (c[x * 4 + 2] + c[x * 4 + 3]);
-      col[x] = (c[0 * 4 + x] + c[1 * 4 + x]) + (c[2 * 4 + x] + c[3 * 4 + x]);
+    for (int q = 0; q < 16; q++) {
+      const df c = cnt_df(C, q, p);
+      df_acc(row[q >> 2], c);
+      df_acc(col[q & 3], c);
     }
-    const float ne = (row[0] + row[1]) + (row[2] + row[3]);
+    df ne = {0.f, 0.f};
+#pragma unroll
+    for (int x = 0; x < 4; x++) { row[x] = df_norm(row[x]); col[x] = df_norm(col[x]); df_acc(ne, row[x]); }
+    ne = df_norm(ne);
     const bool pair = (i < j) && (j < L);
-    const bool ok = pair && (ne > 0.f);
-    const float invS = ok ? 1.0f / (16e-10f + ne) : 0.f;
+    const bool ok = pair && (ne.hi > 0.f);
+    const df iZ = df_recip(df_add_f(ne, 1.6e-9f));
 #pragma unroll
     for (int x = 0; x < 4; x++) {
-      sr[x][a][b] = ok ? (4e-10f + row[x]) * invS : 0.f;
-      sc[x][a][b] = ok ? (4e-10f + col[x]) * invS : 0.f;
+      const df r = ok ? df_mul(df_add_f(row[x], 4e-10f), iZ) : df{0.f, 0.f};
+      colc[k][x] = ok ? df_mul(df_add_f(col[x], 4e-10f), iZ) : df{0.f, 0.f};
+      sb[x][a][b] = make_float2(r.hi, r.lo);
     }
-    sn[a][b] = pair ? ne : 0.f;
+    sn[a][b] = pair ? make_float2(ne.hi, ne.lo) : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  // row sums over b (threads 0-127) and column sums over a (128-255), one
-  // thread per (value, line) adding its 32 entries in order; rows into
-  // part[I][J], columns into part[J][I], both into part[I][I] on a diagonal
-  // tile
+  // threads 0-127: row sums over b, then column sums over a, one thread per
+  // (state, line) adding its 32 entries in order; rows go to part[I][J],
+  // columns to part[J][I], both to part[I][I] on a diagonal tile.
+  // threads 128-159: the nseff row sums.
   double* P4 = part4 + (int64_t)slot * nT * nT * TP * 4;
   double* PR = partR + (int64_t)slot * nT * nT * TP;
   const bool diag = (tr.I == tr.J);
   const int c4 = (tid >> 5) & 3, line = tid & 31;
-  df sum = {0.f, 0.f};
+  df rsum = {0.f, 0.f};
   if (tid < 128) {
-    for (int b = 0; b < TP; b++) sum = df_add_f(sum, sr[c4][line][b]);
-    if (!diag) P4[(((int64_t)tr.I * nT + tr.J) * TP + line) * 4 + c4] = df_to_d(sum);
-    else       srow[c4][line] = make_float2(sum.hi, sum.lo);
-  } else {
-    for (int a = 0; a < TP; a++) sum = df_add_f(sum, sc[c4][a][line]);
-    if (!diag) P4[(((int64_t)tr.J * nT + tr.I) * TP + line) * 4 + c4] = df_to_d(sum);
-  }
-  if (diag) {
-    __syncthreads();
-    if (tid >= 128)
-      P4[(((int64_t)tr.I * nT + tr.I) * TP + line) * 4 + c4] =
-          df_to_d(df_add({srow[c4][line].x, srow[c4][line].y}, sum));
-  }
-  if (tid < TP) {
+    for (int b = 0; b < TP; b++) df_acc(rsum, {sb[c4][line][b].x, sb[c4][line][b].y});
+    rsum = df_norm(rsum);
+    if (!diag) P4[(((int64_t)tr.I * nT + tr.J) * TP + line) * 4 + c4] = df_to_d(rsum);
+  } else if (tid < 128 + TP) {
     df ns = {0.f, 0.f};
-    for (int b = 0; b < TP; b++) ns = df_add_f(ns, sn[tid][b]);
-    PR[((int64_t)tr.I * nT + tr.J) * TP + tid] = df_to_d(ns);
-    if (!diag) PR[((int64_t)tr.J * nT + tr.I) * TP + tid] = 0.0;   // the column sums of nseff are not used
+    for (int b = 0; b < TP; b++) df_acc(ns, {sn[line][b].x, sn[line][b].y});
+    PR[((int64_t)tr.I * nT + tr.J) * TP + line] = df_to_d(df_norm(ns));
+    if (!diag) PR[((int64_t)tr.J * nT + tr.I) * TP + line] = 0.0;   // the column sums of nseff are not used
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+#pragma unroll
+    for (int x = 0; x < 4; x++) sb[x][a][b] = make_float2(colc[k][x].hi, colc[k][x].lo);
+  }
+  __syncthreads();
+  if (tid < 128) {
+    df csum = {0.f, 0.f};
+    for (int a = 0; a < TP; a++) df_acc(csum, {sb[c4][a][line].x, sb[c4][a][line].y});
+    csum = df_norm(csum);
+    if (!diag) P4[(((int64_t)tr.J * nT + tr.I) * TP + line) * 4 + c4] = df_to_d(csum);
+    else       P4[(((int64_t)tr.I * nT + tr.I) * TP + line) * 4 + c4] = df_to_d(df_add(rsum, csum));
   }
 }
 
 // pm[c][x] = normalise(sum over every tile touching column c); one thread
-// per column.  mpc[c][x] = pm[c][x] * (sum_{j>c} nseff[c][j]) feeds the CCF
+// per column.  pmdf is pm as a double-float; lpi[c][x] = {ln pm, 1/pm} as
+// double-floats (FP64 log and division, 0 where pm = 0) for the pair
+// statistics.  mpc[c][x] = pm[c][x] * (sum_{j>c} nseff[c][j]) feeds the CCF
 // column means (src/correlators.c:1030-1036).
 __global__ void k_pm_final(const double* __restrict__ part4, const double* __restrict__ partR, int L, int Lp, int nT,
-                           double* __restrict__ pm, float2* __restrict__ pmdf, double* __restrict__ mpc,
-                           int* __restrict__ status) {
+                           double* __restrict__ pm, float2* __restrict__ pmdf, float4* __restrict__ lpi,
+                           double* __restrict__ mpc, int* __restrict__ status) {
   const int slot = blockIdx.y;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= L) return;
@@ -389,10 +407,12 @@ __global__ void k_pm_final(const double* __restrict__ part4, const double* __res
   if (fabs(m[0] + m[1] + m[2] + m[3] - 1.0) > 1e-6) atomicExch(status, 2);
 #pragma unroll
   for (int x = 0; x < 4; x++) {
-    pm[((int64_t)slot * Lp + c) * 4 + x] = m[x];
-    const float hi = (float)m[x];
-    pmdf[((int64_t)slot * Lp + c) * 4 + x] = make_float2(hi, (float)(m[x] - (double)hi));
-    mpc[((int64_t)slot * Lp + c) * 4 + x] = rs * m[x];
+    const int64_t o = ((int64_t)slot * Lp + c) * 4 + x;
+    pm[o] = m[x];
+    st_df(pmdf + o, df_of(m[x]));
+    const df l = df_of(m[x] > 0.0 ? log(m[x]) : 0.0), r = df_of(m[x] > 0.0 ? 1.0 / m[x] : 0.0);
+    lpi[o] = make_float4(l.hi, l.lo, r.hi, r.lo);
+    mpc[o] = rs * m[x];
   }
 }
 
@@ -435,70 +455,59 @@ __global__ void k_ps(const uint8_t* __restrict__ ax, int64_t slot_stride, const 
 }
 
 // ------------------------------------------------------------------------
-// Statistics.  Per cell, o = nseff*pp and e = nseff*pm_i(x)*pm_j(y) are
-// formed in double-float arithmetic (pairs of fp32 values, ~48-bit
-// significand; GB300 runs fp32 at 64x its FP64 rate) and their difference
-// u = o - e is rounded once to fp32; the rest is fp32.  The G-test is summed
-// as 2*sum_e e*g(u/e) (each term >= 0), which equals the reference's
-// 2*sum o*ln(o/e) because sum u = 0 to rounding when every cell enters (pp
-// and pm are normalised); the CWC form, which sums a subset of cells, adds
-// its sum u explicitly.
-//
-// o = (1e-10 + C) ne / (16e-10 + ne) is written as C + do with
-// do = 1e-10 - 16e-10 C / ne (to 1e-18 absolute), the prior of
-// src/correlators.c:1713 and the normalisation of :1758.
+// Statistics, all per-pair arithmetic in double-float.  With c' = 1e-10 + C
+// (the prior of src/correlators.c:1713), Z = sum c' = nseff + 16e-10 and
+// pp = c'/Z (:1758), S = sum c' ln c', R_x = sum_y c'_xy, K_y = sum_x c'_xy:
+//   MI   = sum pp (ln pp - ln pm_i - ln pm_j)
+//        = (S - Z ln Z - sum_x R_x ln pm_i(x) - sum_y K_y ln pm_j(y)) / Z
+//   GT   = 2 sum o ln(o/e), o = nseff pp, e = nseff pm_i pm_j  =  2 nseff MI
+//   H    = -sum pp ln pp = ln Z - S/Z                       (MIr = MI / H)
+//   MIg  = MI - ngap / nseff
+//   CHI  = sum (o - e)^2 / e = (nseff / Z^2) sum_x T_x / pm_i(x) - nseff,
+//          T_x = sum_y c'_xy^2 / pm_j(y)       (sum o = sum e = nseff)
+//   OMES = sum (o - e)^2 / nseff
+//        = nseff (sum c'^2 / Z^2 - (2/Z) sum_x pm_i(x) V_x + |pm_i|^2 |pm_j|^2),
+//          V_x = sum_y c'_xy pm_j(y)
+// These are the reference's C16 sums (src/correlators.c:92-122, 224-252,
+// 359-390, 536-561, 659-690, 792-822) regrouped so that a cell costs one
+// double-float logarithm and a few products.  Every cell enters: nseff > 0
+// makes every pm of both columns positive (the partner contributes at least
+// the prior).  The regrouped sums cancel at most log2(Z ln Z / |Z MI|) of
+// the 48 bits, which leaves the scores within ~1e-11 relative of FP64 for
+// the alignments of this path.  The C2 class (merged allowed / other cells,
+// :137-168, 269-301, 426-463, 575-605, 705-736, 838-866) and the GT CWC
+// class (:393-423) are formed from the same pieces on their cells; pairs
+// with nseff = 0 (prior only, pp = 1/16) are FP64.
 // ------------------------------------------------------------------------
-// u = o - e with o = c + dc (c >= 0 exact fp32, |dc| tiny), e in double-float
-__device__ __forceinline__ float diff_oe(float c, float dc, df e) {
-  const df s = two_sum(c, -e.hi);
-  return s.hi + (s.lo + (dc - e.lo));
-}
-
-// G-test term e*g(d), d = u/e, o = c + dc: for |d| < 1/4 the polynomial
-// gfun_poly, elsewhere r ln r - (r - 1) with r = 1 + d, as
-// r log1p(d) - d.  Below zero r is the quotient o/e (relative error 2^-22,
-// so r ln r is off by at most 2.4e-7 r |ln r| <= 9e-8), not 1 + d: for
-// empty cells (r ~ 1e-10) 1 + d rounds to a multiple of 2^-24 and, times
-// log1p(d) ~ -20, would add ~1e-6 e per cell.  Both forms are evaluated and
-// one is selected: a warp holds pairs whose cells fall on both sides, and a
-// branch would make every warp run every path.  ie = 1/e (approximate
-// reciprocal, shared with the caller's CHI term).
-__device__ __forceinline__ float gterm_f(float u, float e, float ie, float o) {
-  const float d = u * ie;
-  const float dn = fminf(fmaxf(d, -0.25f), 0.25f);     // the polynomial only where it is used
-  const float near = gfun_poly(dn);
-  const float dp = fmaxf(d, -1.f);
-  const float r = (d < 0.f) ? o * ie : 1.f + dp;
-  const float l = log1pf(fmaxf(dp, -0.99999994f));     // finite where 1 + d rounds to 0
-  const float far = r * l - dp;
-  return e * ((fabsf(d) < 0.25f) ? near : far);
-}
-
-struct PairOut { float chi, gt, mi, mir, mig, omes; df raf, ccf; };
+struct PairOut { df chi, gt, mi, mir, mig, omes, raf, ccf; };
 
 __device__ __forceinline__ df pick_df(const PairOut& o, int k) {
   switch (k) {
-    case 0: return {o.chi, 0.f};
-    case 1: return {o.gt, 0.f};
-    case 2: return {o.mi, 0.f};
-    case 3: return {o.mir, 0.f};
-    case 4: return {o.mig, 0.f};
-    case 5: return {o.omes, 0.f};
+    case 0: return o.chi;
+    case 1: return o.gt;
+    case 2: return o.mi;
+    case 3: return o.mir;
+    case 4: return o.mig;
+    case 5: return o.omes;
     case 6: return o.raf;
     case 8: return o.ccf;
   }
   return {0.f, 0.f};
 }
 
-// per-cell terms a k_stats variant computes (the C16/CWC cell loop is the
-// hot part; a variant carries only what its statistics read)
-enum CellF : unsigned { CF_G = 1u, CF_CHI = 2u, CF_OMES = 4u, CF_H = 8u, CF_ALL = 15u };
+// per-cell terms a k_stats variant computes: the logarithm family (GT, MI,
+// MIr, MIg), CHI, OMES
+enum CellF : unsigned { CF_G = 1u, CF_CHI = 2u, CF_OMES = 4u, CF_ALL = 7u };
 
+__device__ __forceinline__ bool above_h(df H) {   // H > 1e-2 as the FP64 value would compare
+  return (H.hi > 0.0100001f) || (H.hi > 0.0099999f && df_to_d(H) > 1e-2);
+}
 
 template <unsigned CF>
-__device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[16], const float (&uc)[16],
-                                           bool have_uc, const float2* pmi, const float2* pmj, const double* pmid,
-                                           const double* pmjd, const double* meanp, df ne, PairOut& out) {
+__device__ __forceinline__ void pair_stats(const StatsArgs& A, const df (&c)[16], const float (&uc)[16],
+                                           bool have_uc, const float2* pmi, const float2* pmj, const float4* lpi,
+                                           const float4* lpj, const double* pmid, const double* pmjd,
+                                           const double* meanp, const float4* tab, PairOut& out) {
   const unsigned S = A.stats;
   // ---- RAF from unit-weight counts (src/correlators.c:897-925 reduced):
   // the sums are exact integers in fp32 (< 2^24); c_ij = nA^2 - (sum r_x^2
@@ -533,6 +542,13 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
     out.raf = df_add({2.f * q1.hi, 2.f * q1.lo}, df_neg(q2));
   }
   // ---- CCF (src/correlators.c:1038-1053), FP64 ----
+  df ne;
+  {
+    df z = {0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < 16; q++) df_acc(z, c[q]);
+    ne = df_norm(z);
+  }
   if (S & S_CCF) {
     const double ned = df_to_d(ne);
     double ccf = 0.0;
@@ -568,87 +584,119 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
       if (pw > 0.0) { mi += pw * (log(pw) - log(qw)); hh -= pw * log(pw); }
       if (pn > 0.0) { mi += pn * (log(pn) - log(qn)); hh -= pn * log(pn); }
     }
-    out.chi = 0.f; out.gt = 0.f; out.omes = 0.f;
-    out.mi = (float)mi; out.mir = (float)((hh > 1e-2) ? mi / hh : 0.0); out.mig = (float)mi;
+    out.chi = out.gt = out.omes = df{0.f, 0.f};
+    out.mi = df_of(mi); out.mir = df_of((hh > 1e-2) ? mi / hh : 0.0); out.mig = df_of(mi);
     return;
   }
 
-  const float inv_ne = 1.0f / ne.hi;
-  const df ng = df_add({A.wtot.x, A.wtot.y}, {-ne.hi, -ne.lo});   // ngap = sum w - nseff
-  if (A.cls == 0 || A.cls == 2) {
-    float gsum = 0.f, chi = 0.f, omes = 0.f, hh = 0.f, usum = 0.f;
+  const df Z = df_add_f(ne, 16.f * 1e-10f);
+  const df iZ = df_recip(Z);
+  const df wt = {A.wtot.x, A.wtot.y};
+  if (A.cls == 0) {
+    // ---- C16: one pass over the cells ----
+    df R[4], K[4], T[4], V[4], Sx = {0.f, 0.f}, W = {0.f, 0.f};
 #pragma unroll
-    for (int x = 0; x < 4; x++) {
-      const df ax = df_mul(ne, {pmi[x].x, pmi[x].y});
-#pragma unroll
-      for (int y = 0; y < 4; y++) {
-        if (A.cls == 2 && !(A.allow[x * 4 + y] > 0.f)) continue;
-        const float C = c[x * 4 + y];
-        const float dc = 1e-10f - 16e-10f * C * inv_ne;
-        const float o = C + dc;
-        if (CF & (CF_G | CF_CHI | CF_OMES)) {
-          const df e = df_mul(ax, {pmj[y].x, pmj[y].y});
-          const float u = diff_oe(C, dc, e);
-          if (e.hi > 0.f) {
-            const float ie = __fdividef(1.f, e.hi);
-            if (CF & CF_G) { gsum += gterm_f(u, e.hi, ie, o); usum += u; }
-            if (CF & CF_CHI) chi += u * u * ie;
-            if (CF & CF_OMES) omes += u * u;
-          }
-        }
-        if (CF & CF_H) {
-          const float p = o * inv_ne;
-          hh -= (p > 0.f) ? p * __logf(p) : 0.f;
-        }
-      }
-    }
-    const float gt = (A.cls == 2) ? 2.f * (gsum + usum) : 2.f * gsum;
-    const float mi = gsum * inv_ne;
-    out.chi = chi;
-    out.gt = gt;
-    out.mi = mi;
-    out.mir = (hh > 1e-2f) ? mi / hh : 0.f;
-    out.mig = mi - (ng.hi + ng.lo) * inv_ne;
-    out.omes = omes * inv_ne;
-  } else {
-    // C2: allowed / not-allowed merged cells (e.g. src/correlators.c:426-458)
-    df Cw = {0.f, 0.f}, Cn = {0.f, 0.f}, qw = {0.f, 0.f}, qn = {0.f, 0.f};
-    int nal = 0;
+    for (int x = 0; x < 4; x++) R[x] = K[x] = T[x] = V[x] = df{0.f, 0.f};
 #pragma unroll
     for (int x = 0; x < 4; x++)
 #pragma unroll
       for (int y = 0; y < 4; y++) {
-        const df pq = df_mul({pmi[x].x, pmi[x].y}, {pmj[y].x, pmj[y].y});
-        if (A.allow[x * 4 + y] > 0.f) { Cw = df_add_f(Cw, c[x * 4 + y]); qw = df_add(qw, pq); nal++; }
-        else                          { Cn = df_add_f(Cn, c[x * 4 + y]); qn = df_add(qn, pq); }
+        const df cp = df_add_f(c[x * 4 + y], 1e-10f);
+        df_acc(R[x], cp);
+        df_acc(K[y], cp);
+        if (CF & CF_G) df_acc(Sx, df_mul_u(cp, df_log(cp, tab)));
+        if (CF & (CF_CHI | CF_OMES)) {
+          const df sq = df_sqr_u(cp);
+          if (CF & CF_CHI) df_acc(T[x], df_mul_u(sq, {lpj[y].z, lpj[y].w}));
+          if (CF & CF_OMES) { df_acc(W, sq); df_acc(V[x], df_mul_u(cp, {pmj[y].x, pmj[y].y})); }
+        }
       }
-    const float dw = nal * 1e-10f - 16e-10f * Cw.hi * inv_ne;
-    const float dn = (16 - nal) * 1e-10f - 16e-10f * Cn.hi * inv_ne;
-    const df ew = df_mul(ne, qw), en = df_mul(ne, qn);
-    // u = (Cw.hi + Cw.lo + dw) - ew
-    const float uw = diff_oe(Cw.hi, Cw.lo + dw, ew);
-    const float un = diff_oe(Cn.hi, Cn.lo + dn, en);
-    const float ow = Cw.hi + (Cw.lo + dw), on = Cn.hi + (Cn.lo + dn);
-    float g = 0.f, chi = 0.f, om = 0.f;
-    if (ew.hi > 0.f) {
-      const float ie = __fdividef(1.f, ew.hi);
-      g += gterm_f(uw, ew.hi, ie, ow); chi += uw * uw * ie; om += uw * uw;
+    if (CF & CF_G) {
+      const df Sn = df_norm(Sx);
+      const df lnZ = df_log(Z, tab);
+      df P = {0.f, 0.f};
+#pragma unroll
+      for (int x = 0; x < 4; x++) {
+        df_acc(P, df_mul_u(df_norm(R[x]), {lpi[x].x, lpi[x].y}));
+        df_acc(P, df_mul_u(df_norm(K[x]), {lpj[x].x, lpj[x].y}));
+      }
+      const df Mn = df_sub(df_sub(Sn, df_mul(Z, lnZ)), df_norm(P));
+      const df mi = df_mul(Mn, iZ);
+      out.mi = mi;
+      out.gt = df_scale(df_mul(ne, mi), 2.f);
+      const df H = df_sub(lnZ, df_mul(Sn, iZ));
+      out.mir = above_h(H) ? df_div(mi, H) : df{0.f, 0.f};
+      out.mig = df_sub(mi, df_div(df_sub(wt, ne), ne));
     }
-    if (en.hi > 0.f) {
-      const float ie = __fdividef(1.f, en.hi);
-      g += gterm_f(un, en.hi, ie, on); chi += un * un * ie; om += un * un;
+    if (CF & CF_CHI) {
+      df Q = {0.f, 0.f};
+#pragma unroll
+      for (int x = 0; x < 4; x++) df_acc(Q, df_mul_u(df_norm(T[x]), {lpi[x].z, lpi[x].w}));
+      out.chi = df_sub(df_mul(df_mul(ne, df_mul(iZ, iZ)), df_norm(Q)), ne);
     }
-    const float pw = ow * inv_ne, pn = on * inv_ne;
-    float hh = 0.f;
-    hh -= (pw > 0.f) ? pw * __logf(pw) : 0.f;
-    hh -= (pn > 0.f) ? pn * __logf(pn) : 0.f;
-    const float mi = g * inv_ne;
-    out.chi = chi;
-    out.gt = 2.f * g;
+    if (CF & CF_OMES) {
+      df U = {0.f, 0.f}, Ai = {0.f, 0.f}, Aj = {0.f, 0.f};
+#pragma unroll
+      for (int x = 0; x < 4; x++) {
+        df_acc(U, df_mul_u({pmi[x].x, pmi[x].y}, df_norm(V[x])));
+        df_acc(Ai, df_sqr_u({pmi[x].x, pmi[x].y}));
+        df_acc(Aj, df_sqr_u({pmj[x].x, pmj[x].y}));
+      }
+      const df t1 = df_mul(df_norm(W), df_mul(iZ, iZ));
+      const df t2 = df_scale(df_mul(df_norm(U), iZ), 2.f);
+      const df t3 = df_mul(df_norm(Ai), df_norm(Aj));
+      out.omes = df_mul(ne, df_add(df_sub(t1, t2), t3));
+    }
+  } else if (A.cls == 2) {
+    // ---- GT, CWC: the allowed cells only ----
+    df SA = {0.f, 0.f}, CA = {0.f, 0.f}, PA = {0.f, 0.f};
+#pragma unroll
+    for (int x = 0; x < 4; x++)
+#pragma unroll
+      for (int y = 0; y < 4; y++) {
+        if (!(A.allow[x * 4 + y] > 0.f)) continue;
+        const df cp = df_add_f(c[x * 4 + y], 1e-10f);
+        df_acc(SA, df_mul_u(cp, df_log(cp, tab)));
+        df_acc(CA, cp);
+        df_acc(PA, df_mul_u(cp, df_add({lpi[x].x, lpi[x].y}, {lpj[y].x, lpj[y].y})));
+      }
+    const df lnZ = df_log(Z, tab);
+    const df M = df_sub(df_sub(df_norm(SA), df_mul(lnZ, df_norm(CA))), df_norm(PA));
+    out.gt = df_scale(df_mul(df_mul(ne, iZ), M), 2.f);
+  } else {
+    // ---- C2: allowed / not-allowed merged cells (e.g. src/correlators.c:426-458) ----
+    df Cw = {0.f, 0.f}, Cn = {0.f, 0.f}, qw = {0.f, 0.f}, qn = {0.f, 0.f};
+#pragma unroll
+    for (int x = 0; x < 4; x++)
+#pragma unroll
+      for (int y = 0; y < 4; y++) {
+        const df cp = df_add_f(c[x * 4 + y], 1e-10f);
+        const df pq = df_mul_u({pmi[x].x, pmi[x].y}, {pmj[y].x, pmj[y].y});
+        if (A.allow[x * 4 + y] > 0.f) { df_acc(Cw, cp); df_acc(qw, pq); }
+        else                          { df_acc(Cn, cp); df_acc(qn, pq); }
+      }
+    Cw = df_norm(Cw); Cn = df_norm(Cn); qw = df_norm(qw); qn = df_norm(qn);
+    const df pw = df_mul(Cw, iZ), pn = df_mul(Cn, iZ);
+    const df lnZ = df_log(Z, tab);
+    const bool hw = Cw.hi > 0.f, hn = Cn.hi > 0.f;   // the prior makes both positive
+    const df lCw = hw ? df_sub(df_log(Cw, tab), lnZ) : df{0.f, 0.f};   // ln pw
+    const df lCn = hn ? df_sub(df_log(Cn, tab), lnZ) : df{0.f, 0.f};   // ln pn
+    const df lqw = (qw.hi > 0.f) ? df_log(qw, tab) : df{0.f, 0.f};
+    const df lqn = (qn.hi > 0.f) ? df_log(qn, tab) : df{0.f, 0.f};
+    df mi = {0.f, 0.f}, hh = {0.f, 0.f};
+    if (hw && qw.hi > 0.f) mi = df_add(mi, df_mul(pw, df_sub(lCw, lqw)));
+    if (hn && qn.hi > 0.f) mi = df_add(mi, df_mul(pn, df_sub(lCn, lqn)));
+    if (hw) hh = df_sub(hh, df_mul(pw, lCw));
+    if (hn) hh = df_sub(hh, df_mul(pn, lCn));
+    df chi = {0.f, 0.f}, om = {0.f, 0.f};
+    if (qw.hi > 0.f) { const df d = df_sub(pw, qw); const df d2 = df_mul(d, d); chi = df_add(chi, df_div(d2, qw)); om = df_add(om, d2); }
+    if (qn.hi > 0.f) { const df d = df_sub(pn, qn); const df d2 = df_mul(d, d); chi = df_add(chi, df_div(d2, qn)); om = df_add(om, d2); }
+    out.chi = df_mul(ne, chi);
+    out.gt = df_scale(df_mul(ne, mi), 2.f);
     out.mi = mi;
-    out.mir = (hh > 1e-2f) ? mi / hh : 0.f;
-    out.mig = mi - (ng.hi + ng.lo) * inv_ne;
-    out.omes = om * inv_ne;
+    out.mir = above_h(hh) ? df_div(mi, hh) : df{0.f, 0.f};
+    out.mig = df_sub(mi, df_div(df_sub(wt, ne), ne));
+    out.omes = df_mul(ne, om);
   }
 }
 
@@ -659,36 +707,38 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const float (&c)[
 // per (column, output) its column in double-float, in a fixed order, for the
 // APC/ASC partials.
 template <unsigned CF>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 k_stats(StatsArgs A) {
   const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
   const TileRC tr = A.tiles[t];
-  const float* C = A.cnt ? A.cnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
+  const float* C = A.cnt ? A.cnt + ((int64_t)slot * A.ntiles + t) * 32 * TPP : nullptr;
   const float* U = A.ucnt ? A.ucnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
   const double* pm = A.pm + (int64_t)slot * A.Lp * 4;
   const float2* pmdf = A.pmdf + (int64_t)slot * A.Lp * 4;
+  const float4* lpi = A.lpi + (int64_t)slot * A.Lp * 4;
   const double* meanp = A.meanp + slot * 4;
   __shared__ float2 vs[MAXOUT][TP][TP + 1];   // the tile's scores, [q][a][b]
+  __shared__ float4 tab[LOGTAB_N];
+  if (tid < LOGTAB_N) tab[tid] = A.logtab[tid];
+  __syncthreads();
 #pragma unroll 1
   for (int k = 0; k < 4; k++) {
     const int p = tid + 256 * k, a = p >> 5, b = p & 31;
     const int i = tr.I * TP + a, j = tr.J * TP + b;
     const bool valid = (i < j) && (j < A.L);
-    float c[16], uc[16];
+    df c[16];
+    float uc[16];
 #pragma unroll
     for (int q = 0; q < 16; q++) {
-      c[q] = C ? C[q * TPP + p] : 0.f;
+      c[q] = C ? df{C[(2 * q) * TPP + p], C[(2 * q + 1) * TPP + p]} : df{0.f, 0.f};
       uc[q] = (U && A.allow[q] > 0.f) ? U[q * TPP + p] : 0.f;   // RAF reads the allowed cells only
     }
-    df ne = {0.f, 0.f};
-#pragma unroll
-    for (int q = 0; q < 16; q++) ne = df_add_f(ne, c[q]);
     PairOut o;
-    o.chi = o.gt = o.mi = o.mir = o.mig = o.omes = 0.f;
-    o.raf = o.ccf = df{0.f, 0.f};
+    o.chi = o.gt = o.mi = o.mir = o.mig = o.omes = o.raf = o.ccf = df{0.f, 0.f};
     if (valid) {
       const int ii = i < A.L ? i : 0, jj = j < A.L ? j : 0;
-      pair_stats<CF>(A, c, uc, U != nullptr, pmdf + ii * 4, pmdf + jj * 4, pm + ii * 4, pm + jj * 4, meanp, ne, o);
+      pair_stats<CF>(A, c, uc, U != nullptr, pmdf + ii * 4, pmdf + jj * 4, lpi + ii * 4, lpi + jj * 4, pm + ii * 4,
+                     pm + jj * 4, meanp, tab, o);
     }
 #pragma unroll
     for (int q = 0; q < MAXOUT; q++) {
@@ -720,6 +770,38 @@ k_stats(StatsArgs A) {
     for (int b = 0; b < TP; b++) r = df_add(r, {vs[q][line][b].x, vs[q][line][b].y});
     for (int a = 0; a < TP; a++) c = df_add(c, {vs[q][a][line].x, vs[q][a][line].y});
     base[q * qstride + ((int64_t)tr.I * A.nT + tr.I) * TP + line] = df_to_d(df_add(r, c));
+  }
+}
+
+// corr_ValidateProbs (src/correlators.c:1499-1545) for the pair
+// probabilities pp = (1e-10 + C) / (16e-10 + nseff) of one alignment, from
+// its double-float counts: each in [0, 1 + tol], summing to 1 within tol;
+// a failing pair sets *bad
+__global__ void __launch_bounds__(256)
+k_validate_pp(const float* __restrict__ cnt, const TileRC* __restrict__ tiles, int L, double tol,
+              int* __restrict__ bad) {
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  const float* C = cnt + (int64_t)t * 32 * TPP;
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    if (!(i < j && j < L)) continue;
+    double c[16], Z = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      c[q] = 1e-10 + ((double)C[(2 * q) * TPP + p] + (double)C[(2 * q + 1) * TPP + p]);
+      Z += c[q];
+    }
+    double sum = 0.0;
+    bool ok = (Z > 0.0);
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      const double v = c[q] / Z;
+      ok = ok && (v >= 0.0) && (v <= 1.0 + tol);
+      sum += v;
+    }
+    if (!ok || !(fabs(sum - 1.0) <= tol)) atomicExch(bad, 1);
   }
 }
 
@@ -1065,11 +1147,17 @@ k_tile_rowsums(const float2* __restrict__ tilev, const TileRC* __restrict__ tile
 // ------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------
-cudaError_t launch_count_simt(const uint8_t* ax, int64_t slot_stride, const float* w, bool unit, int N, int Lp,
+cudaError_t launch_count_simt(const uint8_t* ax, int64_t slot_stride, const CountWeights& W, bool unit, int N, int Lp,
                               const TileRC* tiles, int ntiles, int nslots, float* cnt, cudaStream_t st) {
   dim3 grid(ntiles, nslots);
-  if (unit) k_count_simt<true><<<grid, 256, 0, st>>>(ax, slot_stride, w, N, Lp, tiles, ntiles, cnt);
-  else      k_count_simt<false><<<grid, 256, 0, st>>>(ax, slot_stride, w, N, Lp, tiles, ntiles, cnt);
+  if (unit)
+    k_count_simt<MODE_UNIT><<<grid, 256, 0, st>>>(ax, slot_stride, nullptr, N, Lp, tiles, ntiles, cnt, 1.f, 1.f, 0.f);
+  else if (W.nl == 1)
+    k_count_simt<MODE_EQUAL><<<grid, 256, 0, st>>>(ax, slot_stride, nullptr, N, Lp, tiles, ntiles, cnt, 1.f, W.s_hi,
+                                                    W.s_lo);
+  else
+    k_count_simt<MODE_LIMBS><<<grid, 256, 0, st>>>(ax, slot_stride, W.d_limbf, N, Lp, tiles, ntiles, cnt, W.B, W.s_hi,
+                                                    0.f);
   return cudaGetLastError();
 }
 
@@ -1080,8 +1168,8 @@ cudaError_t launch_pair_marg(const float* cnt, int L, const TileRC* tiles, int n
 }
 
 cudaError_t launch_pm_final(const double* part4, const double* partR, int L, int Lp, int nT, int nslots, double* pm,
-                            float2* pmdf, double* mpc, double* meanp, int* status, cudaStream_t st) {
-  k_pm_final<<<dim3((L + 127) / 128, nslots), 128, 0, st>>>(part4, partR, L, Lp, nT, pm, pmdf, mpc, status);
+                            float2* pmdf, float4* lpi, double* mpc, double* meanp, int* status, cudaStream_t st) {
+  k_pm_final<<<dim3((L + 127) / 128, nslots), 128, 0, st>>>(part4, partR, L, Lp, nT, pm, pmdf, lpi, mpc, status);
   k_meanp<<<nslots, 256, 0, st>>>(mpc, L, Lp, meanp);
   return cudaGetLastError();
 }
@@ -1098,12 +1186,17 @@ cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st) {
   if (A.stats & (S_GT | S_MI | S_MIr | S_MIg)) cf |= CF_G;
   if (A.stats & S_CHI) cf |= CF_CHI;
   if (A.stats & S_OMES) cf |= CF_OMES;
-  if (A.stats & S_MIr) cf |= CF_H;
   const dim3 grid(A.ntiles, nslots);
   if (cf == 0 || cf == CF_G)          k_stats<CF_G><<<grid, 256, 0, st>>>(A);
   else if (cf == CF_CHI)              k_stats<CF_CHI><<<grid, 256, 0, st>>>(A);
   else if (cf == (CF_G | CF_CHI))     k_stats<CF_G | CF_CHI><<<grid, 256, 0, st>>>(A);
   else                                k_stats<CF_ALL><<<grid, 256, 0, st>>>(A);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_validate_pp(const float* cnt, const TileRC* tiles, int ntiles, int L, double tol, int* bad,
+                               cudaStream_t st) {
+  k_validate_pp<<<ntiles, 256, 0, st>>>(cnt, tiles, L, tol, bad);
   return cudaGetLastError();
 }
 
@@ -1205,6 +1298,60 @@ cudaError_t launch_untile(const double* tilev, const TileRC* tiles, int ntiles, 
                           cudaStream_t st) {
   k_untile<double><<<ntiles, 256, 0, st>>>(tilev, tiles, L, diag, full);
   return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// host helpers
+// ------------------------------------------------------------------------
+void logtab_host(float4* tab) {
+  for (int j = 0; j < LOGTAB_N; j++) {
+    const double cj = 1.0 + (j + 0.5) / LOGTAB_N;
+    const float r = (float)(1.0 / cj);
+    const double nl = -std::log((double)r);
+    const float hi = (float)nl;
+    tab[j] = make_float4(r, hi, (float)(nl - (double)hi), 0.f);
+  }
+}
+
+void make_limbs(const double* w, int N, int stride, uint16_t* lim, CountWeights* W, double* wtot_q) {
+  double wmax = 0.0;
+  bool equal = true;
+  for (int s = 0; s < N; s++) { wmax = std::max(wmax, w[s]); if (w[s] != w[0]) equal = false; }
+  std::memset(lim, 0, sizeof(uint16_t) * 3 * (size_t)stride);
+  W->d_limbf = nullptr;
+  if (equal || wmax <= 0.0) {
+    const double s0 = (N > 0) ? w[0] : 1.0;
+    W->nl = 1; W->bits = 0; W->B = 1.f;
+    W->s_hi = (float)s0; W->s_lo = (float)(s0 - (double)W->s_hi);
+    for (int s = 0; s < N; s++) lim[s] = 1;
+    *wtot_q = (double)N * s0;
+    return;
+  }
+  // b-bit limbs with N (2^b - 1) < 2^24: every limb sum is an exact FP32
+  // integer, and b <= 11 keeps a limb exact in FP16
+  int b = 11;
+  while (b > 1 && (double)N * (double)((1 << b) - 1) >= 16777216.0) b--;
+  const int bits = 3 * b;
+  int e2;
+  std::frexp(wmax, &e2);                     // wmax = f 2^e2, f in [0.5, 1)
+  const int E = bits - e2;                   // wmax 2^E < 2^bits
+  const double qmax = std::ldexp(1.0, bits) - 1.0;
+  const uint64_t mask = (1ull << b) - 1ull;
+  uint64_t tot = 0;
+  for (int s = 0; s < N; s++) {
+    double qd = std::nearbyint(std::ldexp(w[s], E));
+    if (qd > qmax) qd = qmax;
+    const uint64_t q = (uint64_t)qd;
+    lim[s] = (uint16_t)(q & mask);
+    lim[stride + s] = (uint16_t)((q >> b) & mask);
+    lim[2 * (size_t)stride + s] = (uint16_t)(q >> (2 * b));
+    tot += q;
+  }
+  W->nl = 3; W->bits = b;
+  W->B = (float)(1 << b);
+  W->s_hi = (float)std::ldexp(1.0, -E);
+  W->s_lo = 0.f;
+  *wtot_q = std::ldexp((double)tot, -E);
 }
 
 }  // namespace covgpu

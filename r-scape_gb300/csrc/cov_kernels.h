@@ -10,16 +10,18 @@ namespace covgpu {
 constexpr int MAXOUT = 4;   // score matrices produced by one k_stats launch
 
 struct StatsArgs {
-  const float*  cnt;        // weighted counts  [slot][tile][16][TPP]
-  const float*  ucnt;       // unit-weight counts (RAF) or nullptr
+  const float*  cnt;        // weighted counts [slot][tile][16][2][TPP] (double-float planes)
+  const float*  ucnt;       // unit-weight counts (RAF) [slot][tile][16][TPP] or nullptr
   const double* pm;         // [slot][Lp][4]
   const float2* pmdf;       // [slot][Lp][4] pm as double-float (hi, lo)
+  const float4* lpi;        // [slot][Lp][4] {ln pm, 1/pm} as double-floats
+  const float4* logtab;     // df_log's table (LOGTAB_N entries)
   const double* meanp;      // [slot][4]
   float2*       cov;        // [slot][nout][tile][TPP] scores as double-float (hi, lo)
   double*       part1;      // [slot][nout][nT][nT][TP]
   const TileRC* tiles;
   int           ntiles, nT, L, Lp, N;
-  float2        wtot;       // sum of the weights as double-float (ngap = wtot - nseff)
+  float2        wtot;       // sum of the quantised weights as double-float (ngap = wtot - nseff)
   float2        invD, invN; // 1/(N(N-1)) and 1/N for RAF, as double-float
   unsigned      stats;      // StatBit mask of what pair_stats must compute
   int           cls;        // 0 = C16, 1 = C2, 2 = CWC (GT)
@@ -37,15 +39,30 @@ struct EvalTables {
   int           nb, imin, imax;
 };
 
-cudaError_t launch_count_simt(const uint8_t* ax, int64_t slot_stride, const float* w, bool unit, int N, int Lp,
+// weights of the counting kernels: nl = 1 (all weights equal: count times
+// s_hi + s_lo) or 3 limbs of b bits (count = limb_count(d0, d1, d2, B = 2^b,
+// s_hi = 2^-E)); d_limbf = the limbs as floats, [3][N], for the SIMT path
+struct CountWeights {
+  int          nl = 1, bits = 0;
+  float        B = 1.f, s_hi = 1.f, s_lo = 0.f;
+  const float* d_limbf = nullptr;
+};
+// quantises the weights (host): limbs lim[3][stride] (uint16, zero-padded),
+// the scale 2^-E, and the total of the quantised weights
+void make_limbs(const double* w, int N, int stride, uint16_t* lim, CountWeights* W, double* wtot_q);
+
+cudaError_t launch_count_simt(const uint8_t* ax, int64_t slot_stride, const CountWeights& W, bool unit, int N, int Lp,
                               const TileRC* tiles, int ntiles, int nslots, float* cnt, cudaStream_t st);
 cudaError_t launch_pair_marg(const float* cnt, int L, const TileRC* tiles, int ntiles, int nT, int nslots,
                              double* part4, double* partR, cudaStream_t st);
 cudaError_t launch_pm_final(const double* part4, const double* partR, int L, int Lp, int nT, int nslots, double* pm,
-                            float2* pmdf, double* mpc, double* meanp, int* status, cudaStream_t st);
+                            float2* pmdf, float4* lpi, double* mpc, double* meanp, int* status, cudaStream_t st);
 cudaError_t launch_ps(const uint8_t* ax, int64_t slot_stride, const double* w, int N, int L, int Lp, int nslots,
                       double* ps, cudaStream_t st);
 cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st);
+// pair-probability validation of one alignment's double-float counts; *bad set on failure
+cudaError_t launch_validate_pp(const float* cnt, const TileRC* tiles, int ntiles, int L, double tol, int* bad,
+                               cudaStream_t st);
 cudaError_t launch_rafs(const float2* raf, float2* out, int64_t sin, int64_t sout, const TileRC* tiles,
                         const int* tile_index, int ntiles, int nT, int L, int nslots, double* part1, int64_t pstride,
                         cudaStream_t st);

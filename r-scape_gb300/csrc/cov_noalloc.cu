@@ -12,11 +12,17 @@
 // The array is shared by every call: calls that run at the same time on the
 // GPU (different streams, or different host threads) race on it and must be
 // serialised by the caller.  Each call clears the parts it accumulates into.
+//
+// A NaN among the corrected scores is an error in the reference
+// (src/correlators.c:1124, "bad covariation").  The call is asynchronous, so
+// it reports this in the result: d_minmax becomes {NaN, NaN}.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 
 #include "covgpu.h"
 
@@ -30,6 +36,7 @@ struct Scratch {
   double avg;
   double tmin[MMBLK];
   double tmax[MMBLK];
+  int nan;            // set when a corrected score is NaN
 };
 static __device__ __align__(256) Scratch g_scratch;
 
@@ -46,7 +53,10 @@ __global__ void k_na_colx(const double* __restrict__ cov, int L, Scratch* sc) {
     if ((int)threadIdx.x < o) buf[threadIdx.x] += buf[threadIdx.x + o];
     __syncthreads();
   }
-  if (threadIdx.x == 0) sc->colx[i] = (L > 1) ? buf[0] / ((double)L - 1.0) : buf[0];
+  if (threadIdx.x == 0) {
+    sc->colx[i] = (L > 1) ? buf[0] / ((double)L - 1.0) : buf[0];
+    if (i == 0) sc->nan = 0;   // this call's NaN flag (read after k_na_apply)
+  }
 }
 
 // avg = 2/(L(L-1)) sum_{i<j} COV = sum_i COVx[i] / L
@@ -63,9 +73,9 @@ __global__ void k_na_avg(int L, Scratch* sc) {
   if (threadIdx.x == 0) sc->avg = (L > 1) ? buf[0] * ((double)L - 1.0) / ((double)L * ((double)L - 1.0)) : 0.0;
 }
 
-// out[i][j] = corrected score (i != j), diagonal -inf; per-block min/max
-__global__ void k_na_apply(const double* __restrict__ cov, double* __restrict__ out, int L, int actype,
-                           Scratch* sc) {
+// out[i][j] = corrected score (i != j), diagonal -inf; per-block min/max.
+// Each element is read and written by the same thread, so out may be cov.
+__global__ void k_na_apply(const double* cov, double* out, int L, int actype, Scratch* sc) {
   __shared__ double smin[256], smax[256];
   const double A = sc->avg;
   double lo = DBL_MAX, hi = -DBL_MAX;
@@ -78,6 +88,7 @@ __global__ void k_na_apply(const double* __restrict__ cov, double* __restrict__ 
     if (actype == 0) r = (A != 0.0) ? v - sc->colx[i] * sc->colx[j] / A : 0.0;
     else             r = v - (sc->colx[i] + sc->colx[j] - A);
     out[k] = r;
+    if (isnan(r)) sc->nan = 1;
     lo = fmin(lo, r); hi = fmax(hi, r);
   }
   smin[threadIdx.x] = lo; smax[threadIdx.x] = hi;
@@ -98,13 +109,43 @@ __global__ void k_na_minmax(Scratch* sc, int nblk, double* __restrict__ minmax) 
     for (int b = 0; b < nblk; b++) { lo = fmin(lo, sc->tmin[b]); hi = fmax(hi, sc->tmax[b]); }
     minmax[0] = (lo == DBL_MAX) ? INFINITY : lo;
     minmax[1] = (hi == -DBL_MAX) ? -INFINITY : hi;
+    if (sc->nan) minmax[0] = minmax[1] = NAN;
   }
 }
 
-// device address of g_scratch, looked up once per device (the host-side
-// symbol is only a stand-in and must never be handed to a kernel)
+// device address of g_scratch, looked up once per device and context (the
+// host-side symbol is only a stand-in and must never be handed to a kernel).
+// The context id is part of the key: after a device reset the module is
+// loaded again into a new context, possibly at another address.
 constexpr int MAXDEV = 64;
-Scratch* g_addr[MAXDEV] = {nullptr};
+struct AddrCache { unsigned long long ctx_id = 0; Scratch* addr = nullptr; };
+AddrCache g_addr[MAXDEV];
+std::mutex g_addr_mu;
+
+// id of the current context, through the driver entry points the runtime
+// exposes (no link against the driver library); 0 if unavailable
+unsigned long long current_ctx_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)p;
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)p;
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 }  // namespace
 
@@ -115,12 +156,18 @@ extern "C" int covgpu_correct_noalloc(const double* d_cov, double* d_out, int L,
   if (!d_cov || !d_out || !d_minmax) return 11;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAXDEV) return 90;
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return 90;
-    g_addr[dev] = (Scratch*)p;
+  Scratch* sc = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_addr_mu);
+    const unsigned long long id = current_ctx_id();
+    if (!g_addr[dev].addr || id != g_addr[dev].ctx_id) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return 90;
+      g_addr[dev].addr = (Scratch*)p;
+      g_addr[dev].ctx_id = id;
+    }
+    sc = g_addr[dev].addr;
   }
-  Scratch* sc = g_addr[dev];
   cudaStream_t st = (cudaStream_t)stream;
   k_na_colx<<<L, 256, 0, st>>>(d_cov, L, sc);
   k_na_avg<<<1, 256, 0, st>>>(L, sc);

@@ -6,21 +6,21 @@
 // of mutual_naive_ppij (src/correlators.c:1695-1780) for all pairs at once.
 // Operands, K-major (sequences contiguous):
 //   A      = X^T                         (0/1, exact)
-//   B_l    = l_l(s) X^T,  l = 0..nl-1     weight limbs: each weight is
-//            quantised to q_s = round(w_s 2^E) and split into limbs
-//   * N <= 8196: q < 2^22, two 11-bit limbs q = l0 + 2^11 l1 (integers
-//     <= 2047, exact in FP16), FP16 operands;
-//   * larger N: q < 2^24, three 8-bit limbs q = l0 + 2^8 l1 + 2^16 l2
-//     (integers <= 255, exact in BF16), BF16 operands.
+//   B_l    = l_l(s) X^T,  l = 0..2        weight limbs: each weight is
+//            quantised to q_s = round(w_s 2^E) < 2^(3b) and split into three
+//            b-bit limbs q = l0 + 2^b l1 + 2^2b l2, b = min(11,
+//            floor(log2((2^24 - 1)/N))): integers exact in FP16, FP16
+//            operands (33-bit weights up to N = 8196, 27 bits at N = 20000).
 // Each limb accumulates in its own FP32 TMEM accumulator, where the sum
-// (<= 2047 N or 255 N, below 2^24 in both cases) is an exact integer; the
-// epilogue adds the limbs with error-free FP32 sums (two_sum) and one final
-// rounding, so each count is within one FP32 rounding of the exact count of
-// the quantised weights, times the power of two 2^-E, with no FP64 and no
-// integer conversion on the path (exact integers under unit weights).  Two
-// FP16 limbs carry a third less MMA work and operand traffic than three
-// BF16 ones, and their two accumulators (256 TMEM columns) leave room for a
-// second set, so the epilogue of one tile overlaps the MMAs of the next.
+// (<= (2^b - 1) N < 2^24) is an exact integer; the epilogue combines the
+// three with error-free FP32 sums into a double-float count (limb_count),
+// exact to 2^-46 relative, times the power of two 2^-E, with no FP64 and no
+// integer conversion on the path (exact integers under unit weights).  The
+// double-float counts go out as two planes (hi, lo).  Equal weights take one
+// limb (the unit count times the weight, unit_count).  Three limbs need 384
+// TMEM columns, one accumulator set: the epilogue reads a cell row of all
+// three limbs, hands the set back after the last row, and stores while the
+// next task's MMAs run.
 //
 // Operand rows are state-major inside each 32-column tile
 // (row = 128 tile + 32 x + column), so accumulator row m = 32 x + a and
@@ -54,6 +54,8 @@
 #include <cstring>
 #include <vector>
 
+#include "cov_df.cuh"
+#include "cov_kernels.h"
 #include "cov_umma.h"
 
 namespace covgpu {
@@ -72,13 +74,12 @@ struct UmmaPlan {
   int* d_order = nullptr;           // launch order of the tiles (blocked raster)
   int4* d_jpairs = nullptr;         // unit-weight tasks: {I, J0, tile (I, J0), tile (I, J0 + 1)}, same raster
   int njpairs = 0;
-  __nv_bfloat16* d_ops = nullptr;   // [(1 + 3) * maxslots * 4Lp][Npad] (FP16 bits with two limbs)
+  __nv_bfloat16* d_ops = nullptr;   // [(1 + 3) * maxslots * 4Lp][Npad] FP16 bits: one-hot, then 3 limb buffers
   uint8_t* d_ops8 = nullptr;        // [maxslots * 4Lp][Npad8] FP8 E4M3 one-hot (unit weights)
   int Npad8 = 0;                    // sequences padded to UK8
   CUtensorMap tmap8;
   uint16_t* d_limbs = nullptr;      // [3][Npad] weight limbs
-  int nl = 3;                       // limbs in use (1 when all weights are equal; 2: FP16 operands)
-  double scale = 1.0;               // count = limb sum * scale
+  CountWeights cw;                  // limbs in use (1 when all weights are equal, else 3) and the scale
   CUtensorMap tmap;
   int* d_err = nullptr;
   int nsm = 152;
@@ -150,11 +151,6 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
   return d;
 }
 
-// instruction descriptor, kind::f16: BF16 x BF16 -> F32, both K-major
-__host__ __device__ constexpr uint32_t make_idesc(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
 // instruction descriptor, kind::f16: F16 x F16 -> F32, both K-major (A and
 // B formats 0 = F16)
 __host__ __device__ constexpr uint32_t make_idesc_fp16(int M, int N) {
@@ -217,16 +213,11 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 
 // ---------------------------------------------------------------------------
 // operand preparation: codes [slot][N][Lp] -> one-hot rows [4Lp][Npad] (A)
-// and limb-scaled rows (B_l), FP16 (HALF) or BF16, row 128 t + 32 x + c for
-// column 32 t + c and state x; one CTA per (64 sequences, 32 columns, slot)
+// and limb-scaled rows (B_l), FP16, row 128 t + 32 x + c for column 32 t + c
+// and state x; one CTA per (64 sequences, 32 columns, slot)
 // ---------------------------------------------------------------------------
-template <bool HALF>
-__device__ __forceinline__ uint16_t op_bits(float v) {
-  if (HALF) return __half_as_ushort(__float2half_rn(v));
-  return __bfloat16_as_ushort(__float2bfloat16(v));
-}
+__device__ __forceinline__ uint16_t op_bits(float v) { return __half_as_ushort(__float2half_rn(v)); }
 
-template <bool HALF>
 __global__ void __launch_bounds__(256)
 k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, int Npad, int nslots, int nl,
             const uint16_t* __restrict__ limbs, bool unit, uint16_t* __restrict__ ops) {
@@ -244,7 +235,7 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
   // 128 rows (4 states x 32 columns, state-major) x 64 sequences; each
   // thread writes 8 consecutive sequences (16 bytes) of one row
   const int64_t rows_per_buf = (int64_t)nslots * 4 * Lp;
-  const uint16_t one = op_bits<HALF>(1.f), zero = op_bits<HALF>(0.f);
+  const uint16_t one = op_bits(1.f), zero = op_bits(0.f);
   for (int e = tid; e < 128 * 8; e += 256) {
     const int r = e / 8, chunk = e % 8;
     const int x = r / 32, c = r % 32;
@@ -257,7 +248,7 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
       const bool on = (cs[s][c] == x);
       va[k] = on ? one : zero;
 #pragma unroll
-      for (int l = 0; l < 3; l++) vb[l][k] = (on && l < nl) ? op_bits<HALF>((float)lb[l][s]) : zero;
+      for (int l = 0; l < 3; l++) vb[l][k] = (on && l < nl) ? op_bits((float)lb[l][s]) : zero;
     }
     *reinterpret_cast<uint4*>(ops + row * Npad + s0 + chunk * 8) = *reinterpret_cast<uint4*>(va);
 #pragma unroll
@@ -320,7 +311,7 @@ __global__ void __launch_bounds__(192, 1)
 k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
              const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles,
              const int4* __restrict__ jpairs, int npairs, int nslots_buf,
-             int nslots, int Lp, int nkb, int bbuf, float s_hi, float s_lo, unsigned cellmask,
+             int nslots, int Lp, int nkb, int bbuf, float B, float s_hi, float s_lo, unsigned cellmask,
              int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   constexpr int NB = F8 ? 2 : NL;          // B tiles per stage (limbs, or the column tiles J0, J0 + 1)
@@ -401,15 +392,14 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
   } else if (warp == 1) {
     if (lane == 0) {
       // ---- MMA issuer ----
-      constexpr uint32_t idesc = F8 ? make_idesc_e4m3(UM, UN) : (NL == 2 ? make_idesc_fp16(UM, UN) : make_idesc(UM, UN));
+      constexpr uint32_t idesc = F8 ? make_idesc_e4m3(UM, UN) : make_idesc_fp16(UM, UN);
       // limbs 0 and 1 as one M = 128, N = 256 MMA: their B tiles are
       // consecutive in the stage (256 rows, 1024-byte 8-row groups throughout)
       // and their accumulators consecutive in TMEM, so A is read from shared
       // memory once for both (the ring's shared-memory bandwidth, A read per
       // limb, bounded the two-MMA form)
       constexpr bool PAIR = !F8 && NL >= 2;
-      constexpr uint32_t idesc2 = F8 ? make_idesc_e4m3(UM, 2 * UN)
-                                     : (NL == 2 ? make_idesc_fp16(UM, 2 * UN) : make_idesc(UM, 2 * UN));
+      constexpr uint32_t idesc2 = F8 ? make_idesc_e4m3(UM, 2 * UN) : make_idesc_fp16(UM, 2 * UN);
       uint32_t g = 0;
       int i = 0;
       for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x, i++) {
@@ -481,54 +471,52 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
           if (lane == 0)
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty_bar[a])) : "memory");
         }
-        float v[32];
+        // F8 (unit weights): exact FP32 integers, one plane; weighted:
+        // double-float counts, a hi and a lo plane
+        float vh[32], vl[32];
 #pragma unroll
         for (int k = 0; k < 32; k++) {
-          if (NL == 1) {
-            // exact integer times the scale, rounded once (s_lo carries the
-            // part of the scale below FP32 precision)
-            const float c = __uint_as_float(d[0][k]);
-            const float p = c * s_hi;
-            v[k] = p + (fmaf(c, s_hi, -p) + c * s_lo);
+          if (F8) {
+            vh[k] = __uint_as_float(d[0][k]);
+            vl[k] = 0.f;
+          } else if (NL == 1) {
+            const df c = unit_count(__uint_as_float(d[0][k]), s_hi, s_lo);
+            vh[k] = c.hi; vl[k] = c.lo;
           } else {
-            // D0 + B D1 + B^2 D2 (B = 2^11 for two FP16 limbs, 2^8 for three
-            // BF16 ones) with two error-free sums (each limb sum is an
-            // exact integer, the scalings are exact): within one rounding
-            // of the exact count, all on the FP32 pipe
-            constexpr float LB = (NL == 2) ? 2048.f : 256.f;
-            const float c0 = __uint_as_float(d[0][k]);
-            const float c1 = __uint_as_float(d[1][k]) * LB;
-            const float c2 = (NL > 2) ? __uint_as_float(d[NL > 2 ? 2 : 0][k]) * (LB * LB) : 0.f;
-            const float s1 = c2 + c1;
-            const float b1 = s1 - c2;
-            const float e1 = (c2 - (s1 - b1)) + (c1 - b1);
-            const float s2 = s1 + c0;
-            const float b2 = s2 - s1;
-            const float e2 = (s1 - (s2 - b2)) + (c0 - b2);
-            v[k] = (s2 + (e1 + e2)) * s_hi;   // s_hi = 2^-E, exact
+            const df c = limb_count(__uint_as_float(d[0][k]), __uint_as_float(d[NL > 1 ? 1 : 0][k]),
+                                    __uint_as_float(d[NL > 2 ? 2 : 0][k]), B, s_hi);
+            vh[k] = c.hi; vl[k] = c.lo;
           }
         }
         const int t = h ? t1 : t0;
         if (t < 0) continue;                                // outside I <= J < nT
         if (!((cellmask >> (x * 4 + y)) & 1u)) continue;   // a cell nobody reads is not stored
-        const int orow0 = ((slot * ntiles + t) * 16 + x * 4) * 32;   // cell (x, y = 0), a = 0
-        uint8_t* buf = wbuf + (nst & 1u) * 4096;
-        if (nst >= 2) {
-          if (lane == 0) bulk_wait_read<1>();   // the store two back has read this buffer
-          __syncwarp();
-        }
-        // row a = lane, 16-byte chunk c at position c ^ (a & 7) (128B swizzle)
+        constexpr int NPL = F8 ? 1 : 2;
+        // F8: row block of cell (x, y) in [slot][tile][16][32]; weighted: of
+        // plane h2 of cell (x, y) in [slot][tile][16][2][32]
+        const int orow0 = F8 ? ((slot * ntiles + t) * 16 + x * 4 + y) * 32
+                             : ((slot * ntiles + t) * 32 + 2 * (x * 4 + y)) * 32;
 #pragma unroll
-        for (int c = 0; c < 8; c++)
-          *reinterpret_cast<float4*>(buf + lane * 128 + ((c ^ (lane & 7)) << 4)) =
-              make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
-        fence_proxy_async();
-        __syncwarp();
-        if (lane == 0) {
-          tma_store_2d(&omap, buf, 0, orow0 + y * 32);
-          bulk_commit();
+        for (int h2 = 0; h2 < NPL; h2++) {
+          uint8_t* buf = wbuf + (nst & 1u) * 4096;
+          if (nst >= 2) {
+            if (lane == 0) bulk_wait_read<1>();   // the store two back has read this buffer
+            __syncwarp();
+          }
+          const float* v = h2 ? vl : vh;
+          // row a = lane, 16-byte chunk c at position c ^ (a & 7) (128B swizzle)
+#pragma unroll
+          for (int c = 0; c < 8; c++)
+            *reinterpret_cast<float4*>(buf + lane * 128 + ((c ^ (lane & 7)) << 4)) =
+                make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+          fence_proxy_async();
+          __syncwarp();
+          if (lane == 0) {
+            tma_store_2d(&omap, buf, 0, orow0 + h2 * 32);
+            bulk_commit();
+          }
+          nst++;
         }
-        nst++;
       }
     }
     if (lane == 0) bulk_wait_all();
@@ -566,17 +554,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
 }
 
 constexpr int STAGES3 = 3;   // 3 limbs: 64 KB per stage
-constexpr int STAGES2 = 4;   // 2 limbs: 48 KB per stage
 constexpr int STAGES1 = 4;   // 1 limb : 32 KB per stage (FP8, two column tiles: 48 KB)
-static_assert(STAGES1 == STAGES2, "the FP8 kernel's ring is sized as the two-limb one");
 
 constexpr int ACC3 = 1;      // 3 limbs: 384 TMEM columns, one accumulator set
-constexpr int ACC2 = 2;      // 2 limbs: two 256-column sets, epilogue overlapped
 constexpr int ACC1 = 2;      // 1 limb : two 128-column sets, epilogue overlapped
 
-static size_t smem_bytes(int nl) {
-  const int stages = (nl == 1) ? STAGES1 : (nl == 2 ? STAGES2 : STAGES3);
-  const size_t ring = (size_t)stages * TILE_BYTES * (1 + nl);
+// nb = B tiles per stage (limbs, or the FP8 kernel's two column tiles)
+static size_t smem_bytes(int nb, int stages) {
+  const size_t ring = (size_t)stages * TILE_BYTES * (1 + nb);
   const size_t stage_out = (size_t)4 * 8192;   // two 4 KB buffers per epilogue warp
   return ring + stage_out + 1024;
 }
@@ -665,13 +650,11 @@ UmmaPlan* umma_plan_create(int N, int L, int Lp, int nT, const TileRC* d_tiles, 
   cudaMemset(p->d_err, 0, sizeof(int));
   if (!plan_dims(p, N, L, Lp, nT, ntiles)) { umma_plan_destroy(p); return nullptr; }
   cudaFuncSetAttribute(k_count_umma<3, STAGES3, ACC3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem_bytes(3));
-  cudaFuncSetAttribute(k_count_umma<2, STAGES2, ACC2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem_bytes(2));
+                       (int)smem_bytes(3, STAGES3));
   cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem_bytes(1));
+                       (int)smem_bytes(1, STAGES1));
   cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem_bytes(2));   // two B tiles per stage
+                       (int)smem_bytes(2, STAGES1));   // two B tiles per stage
   cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev);
   return p;
 }
@@ -692,47 +675,18 @@ void umma_plan_destroy(UmmaPlan* p) {
 }
 
 void umma_set_weights(UmmaPlan* p, const double* wgt, int N, cudaStream_t st) {
-  double wmax = 0.0;
-  bool equal = true;
-  for (int s = 0; s < N; s++) { wmax = std::max(wmax, wgt[s]); if (wgt[s] != wgt[0]) equal = false; }
   std::vector<uint16_t> lim((size_t)3 * p->Npad, 0);
-  if (equal || wmax <= 0.0) {
-    p->nl = 1;
-    p->scale = (N > 0) ? wgt[0] : 1.0;
-    for (int s = 0; s < N; s++) lim[s] = 1;
-  } else {
-    // q = round(w 2^E) < 2^bits: two 11-bit limbs while 2047 N < 2^24 (the
-    // FP32 limb sums stay exact), else three 8-bit limbs
-    const bool two = (N <= 8196);
-    const int bits = two ? 22 : 24;
-    int e2;
-    std::frexp(wmax, &e2);                 // wmax = f 2^e2, f in [0.5,1)
-    const int E = bits - e2;               // wmax 2^E < 2^bits
-    p->nl = two ? 2 : 3;
-    p->scale = std::ldexp(1.0, -E);
-    const double qmax = std::ldexp(1.0, bits) - 1.0;
-    for (int s = 0; s < N; s++) {
-      double qd = std::nearbyint(std::ldexp(wgt[s], E));
-      if (qd > qmax) qd = qmax;
-      const uint32_t q = (uint32_t)qd;
-      if (two) {
-        lim[s] = (uint16_t)(q & 2047u);
-        lim[p->Npad + s] = (uint16_t)(q >> 11);
-      } else {
-        lim[s] = (uint16_t)(q & 255u);
-        lim[p->Npad + s] = (uint16_t)((q >> 8) & 255u);
-        lim[2 * (size_t)p->Npad + s] = (uint16_t)(q >> 16);
-      }
-    }
-  }
+  double wtot_q = 0.0;
+  make_limbs(wgt, N, p->Npad, lim.data(), &p->cw, &wtot_q);
   cudaMemcpyAsync(p->d_limbs, lim.data(), lim.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, st);
   cudaStreamSynchronize(st);
 }
 
-// TMA store map over the count buffer [maxslots][ntiles][16][32][32] FP32,
-// viewed as rows of 32 counts, box 32 x 32, 128-byte swizzle
-static bool encode_out_map(UmmaPlan* p, float* cnt, CUtensorMap* m) {
-  const uint64_t rows = (uint64_t)p->maxslots * p->ntiles * 16 * 32;
+// TMA store map over a count buffer viewed as rows of 32 FP32 counts, box
+// 32 x 32, 128-byte swizzle: [maxslots][ntiles][16][planes][32][32] (planes
+// = 2 for double-float counts, 1 for the FP8 unit counts)
+static bool encode_out_map(UmmaPlan* p, float* cnt, int planes, CUtensorMap* m) {
+  const uint64_t rows = (uint64_t)p->maxslots * p->ntiles * 16 * planes * 32;
   if (rows >= ((uint64_t)1 << 31)) return false;
   cuuint64_t gdim[2] = {32, (cuuint64_t)rows};
   cuuint64_t gstride[1] = {32 * sizeof(float)};
@@ -776,7 +730,7 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
   if (nslots > p->maxslots) return cudaErrorInvalidValue;
   if (((uintptr_t)cnt & 15u) != 0) return cudaErrorInvalidValue;
   CUtensorMap omap;
-  if (!encode_out_map(p, cnt, &omap)) return cudaErrorInvalidValue;
+  if (!encode_out_map(p, cnt, unit ? 1 : 2, &omap)) return cudaErrorInvalidValue;
   // persistent: one CTA per SM, tasks (alignment, tile in raster order)
   const int64_t ntask = (int64_t)p->ntiles * nslots;
   const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntask, p->nsm));
@@ -788,36 +742,25 @@ cudaError_t umma_count(UmmaPlan* p, const uint8_t* ax, int64_t slot_stride, int 
                                                                             nslots, p->d_ops8);
     const int64_t ntask8 = (int64_t)p->njpairs * nslots;
     const int grid8 = (int)std::max<int64_t>(1, std::min<int64_t>(ntask8, p->nsm));
-    k_count_umma<1, STAGES1, ACC1, true><<<grid8, 192, smem_bytes(2), st>>>(
+    k_count_umma<1, STAGES1, ACC1, true><<<grid8, 192, smem_bytes(2, STAGES1), st>>>(
         p->tmap8, omap, p->d_tiles, p->d_order, p->ntiles, p->d_jpairs, p->njpairs, p->maxslots, nslots, p->Lp,
-        p->Npad8 / UK8, 0, 1.0f, 0.0f, cellmask, p->d_err);
+        p->Npad8 / UK8, 0, 1.0f, 1.0f, 0.0f, cellmask, p->d_err);
     return cudaGetLastError();
   }
-  const int nl = p->nl;
+  const CountWeights& W = p->cw;
   dim3 pg(p->Npad / 64, p->Lp / 32, nslots);
-  if (nl == 2)
-    k_umma_prep<true><<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, nl, p->d_limbs, false,
-                                          reinterpret_cast<uint16_t*>(p->d_ops));
-  else
-    k_umma_prep<false><<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, nl, p->d_limbs, false,
-                                           reinterpret_cast<uint16_t*>(p->d_ops));
+  k_umma_prep<<<pg, 256, 0, st>>>(ax, slot_stride, p->N, p->Lp, p->Npad, p->maxslots, W.nl, p->d_limbs, false,
+                                  reinterpret_cast<uint16_t*>(p->d_ops));
   const int nkb = p->Npad / UK;
-  // the scale as an unevaluated FP32 pair (a power of two with limbs)
-  const double scale = p->scale;
-  const float s_hi = (float)scale, s_lo = (float)(scale - (double)s_hi);
   if (ev0) cudaEventRecord(ev0, st);
-  if (nl == 1)
-    k_count_umma<1, STAGES1, ACC1, false><<<grid, 192, smem_bytes(1), st>>>(
-        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, nullptr, 0, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo,
-        0xFFFFu, p->d_err);
-  else if (nl == 2)
-    k_count_umma<2, STAGES2, ACC2, false><<<grid, 192, smem_bytes(2), st>>>(
-        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, nullptr, 0, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo,
-        0xFFFFu, p->d_err);
+  if (W.nl == 1)
+    k_count_umma<1, STAGES1, ACC1, false><<<grid, 192, smem_bytes(1, STAGES1), st>>>(
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, nullptr, 0, p->maxslots, nslots, p->Lp, nkb, 1, 1.0f,
+        W.s_hi, W.s_lo, 0xFFFFu, p->d_err);
   else
-    k_count_umma<3, STAGES3, ACC3, false><<<grid, 192, smem_bytes(3), st>>>(
-        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, nullptr, 0, p->maxslots, nslots, p->Lp, nkb, 1, s_hi, s_lo,
-        0xFFFFu, p->d_err);
+    k_count_umma<3, STAGES3, ACC3, false><<<grid, 192, smem_bytes(3, STAGES3), st>>>(
+        p->tmap, omap, p->d_tiles, p->d_order, p->ntiles, nullptr, 0, p->maxslots, nslots, p->Lp, nkb, 1, W.B,
+        W.s_hi, W.s_lo, 0xFFFFu, p->d_err);
   if (ev1) cudaEventRecord(ev1, st);
   return cudaGetLastError();
 }

@@ -1,8 +1,8 @@
 """Generates the golden fixtures under tests/golden/ from the reference tree.
 
-Run once in a container that has the reference checked out (the path is the
-first argument, default /root/reference); the outputs are committed, and no
-test reads the reference at run time.
+Run once where the reference source tree is checked out, with its path as
+the only argument; the outputs are committed, and no test reads the
+reference at run time.
 
 Outputs
   arisong.npz   the Arisong alignment of tutorial/updated_Arisong.sto in Easel
@@ -76,7 +76,9 @@ def read_tutorial_table(path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <R-scape source tree>")
+    ref = sys.argv[1]
     here = os.path.dirname(os.path.abspath(__file__))
     names, seqs, ss = read_stockholm(os.path.join(ref, "tutorial", "updated_Arisong.sto"))
     ax = np.stack([digitize(s) for s in seqs])

@@ -1,33 +1,19 @@
 """GPU library vs the CPU oracle on the same inputs (needs a GB300).
 
 Tolerances: pair counts and nseff are compared bit-exactly under unit
-weights; probabilities within 1e-12; every statistic within 1e-5 relative,
-|gpu - ref| <= 1e-5 |ref| + a * S with S the largest magnitude of the
-statistic before APC/ASC and a = 2e-7 (unit weights) or 1e-6 (float weights,
-where the SIMT path accumulates in fp32); null alignments byte for byte; the
-E < 0.05 pair set exactly, E-values within 1e-5 (deep-tail E-values amplify
-the fp32-level differences of the fitted tail parameters).
+weights (float weights are quantised to 33 bits, so their counts are within
+1e-9 relative); probabilities within 1e-12; every statistic, raw or
+APC/ASC-corrected, within 1e-5 relative on each pair of at least 1e-3 of the
+largest magnitude and within 1e-8 of that magnitude below it (parity_tol);
+null alignments byte for byte; the E < 0.05 pair set exactly, E-values
+within 1e-5 relative.
 """
 import numpy as np
 import pytest
 
+from parity_tol import stat_close
+
 pytestmark = pytest.mark.gpu
-
-RTOL = 1e-5
-ATOL_SCALE = 2e-7      # unit weights: counts are exact
-ATOL_SCALE_FP32 = 1e-6  # float weights on the SIMT path: fp32 accumulation
-
-
-def close(gpu, ref, scale=None, atol_scale=ATOL_SCALE):
-    """|gpu - ref| <= RTOL |ref| + ATOL_SCALE * scale, where scale is the
-    largest magnitude of the statistic before any APC/ASC correction (the
-    correction subtracts terms of that size, so rounding scales with it)."""
-    gpu = np.asarray(gpu)
-    ref = np.asarray(ref)
-    if scale is None:
-        scale = np.max(np.abs(ref)) if ref.size else 0.0
-    err = np.abs(gpu - ref)
-    return bool(np.all(err <= RTOL * np.abs(ref) + atol_scale * scale + 1e-300)), float(err.max(initial=0.0))
 
 
 def make(covgpu, N, L, seed, unit=False, tree_kind=1, nbp=None):
@@ -55,8 +41,8 @@ def test_counts_unit_weights_bit_exact(covgpu, oracle, N, L):
     assert np.array_equal(ne[iu], one[iu])
     assert np.array_equal(ng[iu], ong[iu])
     assert np.allclose(pp[iu], opp[iu], rtol=1e-14, atol=0)
-    # pm sums one fp32-rounded contribution per partner in FP64
-    assert np.allclose(pm, opm, rtol=1e-7, atol=1e-15)
+    # pm sums one double-float contribution per partner
+    assert np.allclose(pm, opm, rtol=1e-12, atol=1e-15)
     assert np.allclose(ps, ops, rtol=1e-12, atol=1e-15)
     e.close()
 
@@ -77,15 +63,13 @@ def test_statistics(covgpu, oracle, N, L, unit, corr):
         mm = e.score(types)
         for q, t in enumerate(types):
             ref, (rmin, rmax) = oracle.cov_calculate(t, s.ax, w)
-            raw, _ = oracle.cov_calculate(t.rstrip("pa") if corr else t, s.ax, w)
             got = e.get_cov(0, q)
             iu = np.triu_indices(L, 1)
-            tol = ATOL_SCALE if unit else ATOL_SCALE_FP32
-            ok, err = close(got[iu], ref[iu], np.max(np.abs(raw[iu])), tol)
-            assert ok, "%s N=%d L=%d unit=%s max err %g" % (t, N, L, unit, err)
+            ok, rel, small = stat_close(got[iu], ref[iu])
+            assert ok, "%s N=%d L=%d unit=%s rel %g small %g" % (t, N, L, unit, rel, small)
             assert np.allclose(got.T[iu], got[iu])
-            ok, _ = close(mm[0, q], [rmin, rmax], np.max(np.abs(raw[iu])), tol)
-            assert ok, (t, mm[0, q], rmin, rmax)
+            assert np.allclose(mm[0, q], [rmin, rmax], rtol=1e-5, atol=1e-8 * np.max(np.abs(ref[iu]))), \
+                (t, mm[0, q], rmin, rmax)
     e.close()
 
 
@@ -100,11 +84,10 @@ def test_classes(covgpu, oracle, cls):
     e.score(types, covclass=cls)
     for q, t in enumerate(types):
         ref, _ = oracle.cov_calculate(t, s.ax, w, covclass=cls)
-        raw, _ = oracle.cov_calculate(t.rstrip("p"), s.ax, w, covclass=cls)
         got = e.get_cov(0, q)
         iu = np.triu_indices(L, 1)
-        ok, err = close(got[iu], ref[iu], np.max(np.abs(raw[iu])), ATOL_SCALE_FP32)
-        assert ok, (t, cls, err)
+        ok, rel, small = stat_close(got[iu], ref[iu])
+        assert ok, (t, cls, rel, small)
     e.close()
 
 
@@ -132,16 +115,16 @@ def test_null_alignments_identical(covgpu, oracle, N, L):
     (60, 45, ["MIa"]),
 ])
 def test_rscape_pipeline(covgpu, oracle, N, L, types, counter):
-    """The whole path against the oracle.  The histogram width w follows the
-    first null's score range, so the fp32-level error of the plain path's
-    float-weight counts moves w, phi and the fit by ~1e-6 relative; the
-    tensor path's counts are exact for the quantised weights."""
+    """The whole path against the oracle: the width w (from the first null's
+    score range), the null histogram, the tail fit, the hits and their
+    E-values.  Both counting paths count the same 33-bit quantised weights
+    exactly, so they give the same scores."""
     s, w = make(covgpu, N, L, 42, nbp=L // 5)
     ns = 8
     e = covgpu.Engine(N, L, maxslots=ns + 1, maxnull=ns)
     e.set_tree(s.parent, s.left, s.right)
     cnt = covgpu.SIMT if counter == "simt" else covgpu.TENSOR
-    rtol = 1e-5 if counter == "simt" else 1e-6
+    rtol = 1e-6
     res = e.rscape(s.ax, w, types, nshuffle=ns, counter=cnt)
     T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
     for q, t in enumerate(types):
@@ -159,6 +142,37 @@ def test_rscape_pipeline(covgpu, oracle, N, L, types, counter):
         assert set(gh) == set(rh), (t, sorted(set(gh) ^ set(rh))[:10])
         for k in rh:
             assert abs(gh[k][1] - rh[k][1]) <= 100 * rtol * rh[k][1] + 1e-300, (t, k, gh[k], rh[k])
+    e.close()
+
+
+@pytest.mark.parametrize("counter", ["simt", "tensor"])
+@pytest.mark.parametrize("types", [["GTp"], ["MIp", "CHIp"]])
+def test_rscape_pipeline_exponential_tail(covgpu, oracle, counter, types):
+    """R-scape's --expo path (cov_NullFitExponential, src/covariation.c:1914-1941):
+    the null tail fitted by the binned exponential ML fit instead of the
+    gamma; the width, histogram, fit, hits and E-values against the
+    oracle's fit_exp."""
+    N, L, ns = 180, 110, 8
+    s, w = make(covgpu, N, L, 31, nbp=L // 5)
+    e = covgpu.Engine(N, L, maxslots=ns + 1, maxnull=ns)
+    e.set_tree(s.parent, s.left, s.right)
+    cnt = covgpu.SIMT if counter == "simt" else covgpu.TENSOR
+    res = e.rscape(s.ax, w, types, nshuffle=ns, counter=cnt, doexpfit=1, thresh=10.0)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    for q, t in enumerate(types):
+        ref = oracle.rscape(s.ax, w, T, covtype=t, nshuffle=ns, doexpfit=1, thresh=10.0)
+        g = res[q]
+        assert g["status"] == 0
+        assert abs(g["w"] - ref["w"]) <= 1e-6 * abs(ref["w"])
+        for k in ("h_nb", "h_imin", "h_imax", "h_cmin", "h_n", "h_Nc", "h_No"):
+            assert g[k] == ref[k], (t, k, g[k], ref[k])
+        assert abs(g["mu"] - ref["mu"]) <= 1e-6 * (abs(ref["mu"]) + 10.0)
+        assert abs(g["lambda_"] - ref["lambda_"]) <= 1e-6 * abs(ref["lambda_"]), (t, g["lambda_"], ref["lambda_"])
+        gh = {(i, j): E for (i, j, sc, E, p) in g["hits"]}
+        rh = {(i, j): E for (i, j, sc, E, p) in ref["hits"]}
+        assert set(gh) == set(rh) and len(rh) > 0, (t, sorted(set(gh) ^ set(rh))[:10])
+        for k in rh:
+            assert abs(gh[k] - rh[k]) <= 1e-5 * rh[k] + 1e-300, (t, k, gh[k], rh[k])
     e.close()
 
 
@@ -243,10 +257,10 @@ def test_tensor_counts(covgpu, oracle, N, L, unit):
         assert np.array_equal(ne[iu], one[iu])
         assert np.allclose(pp[iu], opp[iu], rtol=1e-14, atol=0)
     else:
-        # weights quantised to 24 bits, counts then rounded once to fp32
-        assert np.allclose(ne[iu], one[iu], rtol=5e-7, atol=0)
-        assert np.allclose(pp[iu], opp[iu], rtol=1e-6, atol=1e-12)
-    assert np.allclose(pm, opm, rtol=1e-6, atol=1e-12)
+        # weights quantised to 33 bits, counts exact for them (double-float)
+        assert np.allclose(ne[iu], one[iu], rtol=1e-9, atol=0)
+        assert np.allclose(pp[iu], opp[iu], rtol=1e-9, atol=1e-15)
+    assert np.allclose(pm, opm, rtol=1e-9, atol=1e-15)
     e.close()
 
 
@@ -261,10 +275,9 @@ def test_tensor_statistics(covgpu, oracle, N, L):
     iu = np.triu_indices(L, 1)
     for q, t in enumerate(types):
         ref, _ = oracle.cov_calculate(t, s.ax, w)
-        raw, _ = oracle.cov_calculate(t[:-1], s.ax, w)
         got = e.get_cov(0, q)
-        ok, err = close(got[iu], ref[iu], np.max(np.abs(raw[iu])), 5e-7)
-        assert ok, (t, err)
+        ok, rel, small = stat_close(got[iu], ref[iu])
+        assert ok, (t, rel, small)
     e.close()
 
 

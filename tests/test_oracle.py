@@ -218,3 +218,21 @@ def test_c2_and_cwc_statistics_match_definitions(oracle):
         assert np.allclose(got[iu], ref[t][iu], rtol=1e-12, atol=1e-12), t
     got, _ = oracle.cov_calculate("GT", ax, w, covclass=oracle.CWC)
     assert np.allclose(got[iu], ref["CWC"][iu], rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("N,L,seed", [(40, 30, 1), (97, 50, 2), (7, 25, 3)])
+def test_raf_count_form_equals_the_loop(oracle, N, L, seed):
+    """The deep-alignment RAF of the oracle (unit counts of the allowed
+    cells) against its restatement of corr_CalculateRAF's O(N^2) loop
+    (src/correlators.c:876-933), including gaps and unknown residues."""
+    rng = np.random.default_rng(seed)
+    ax = rng.integers(0, 5, size=(N, L)).astype(np.uint8)
+    ax[rng.random((N, L)) < 0.05] = 15
+    allow = oracle.default_allow()
+    a, b = np.zeros(L * L), np.zeros(L * L)
+    mma, mmb = np.zeros(2), np.zeros(2)
+    assert oracle.lib().orc_raf(ax, N, L, allow, a, mma) == 0
+    assert oracle.lib().orc_raf_counts(ax, N, L, allow, b, mmb) == 0
+    iu = np.triu_indices(L, 1)
+    assert np.allclose(a.reshape(L, L)[iu], b.reshape(L, L)[iu], rtol=0, atol=1e-15)
+    assert np.allclose(mma, mmb, rtol=0, atol=1e-15)
