@@ -145,6 +145,13 @@ int  covgpu_sim_tables(covgpu_ctx *ctx, double *P4, double *P16);
  * ... CCFa=26), at most 4 per call; minmax[slot][type][2] on return */
 int  covgpu_score(covgpu_ctx *ctx, int first_slot, int nslots, int ntypes, const int *covtypes, int covclass,
                   int nseqthresh, int alenthresh, const double *allow, int counter, double *minmax);
+/* covgpu_score that reuses the weighted counts a previous score of the same
+ * slots (same counter) left on the device, when no call since has changed
+ * those alignments, the weights or the count buffer; otherwise it counts as
+ * covgpu_score does.  (corr_Probs then corr_Calculate* on one alignment
+ * count once.) */
+int  covgpu_score_reuse(covgpu_ctx *ctx, int first_slot, int nslots, int ntypes, const int *covtypes, int covclass,
+                        int nseqthresh, int alenthresh, const double *allow, int counter, double *minmax);
 /* full L x L score matrix of one (slot, type index of the last covgpu_score),
  * diagonal -inf, both triangles (the layout of mi->COV) */
 int  covgpu_get_cov(covgpu_ctx *ctx, int slot, int which, double *COV);

@@ -112,6 +112,9 @@ def lib():
         L.orc_mlp_grad.argtypes = [f32p, f32p, f32p, f32p, C.c_int, f64p]
         L.orc_mlp_grad.restype = C.c_double
         L.orc_raf_counts.argtypes = [u8p, C.c_int, C.c_int, f64p, f64p, f64p]
+        L.orc_rscape_multi.argtypes = [C.POINTER(Params), C.c_int, C.c_void_p, u8p, f64p, C.c_int, C.c_int,
+                                       C.POINTER(Tree), C.c_void_p, C.c_void_p, u64p, C.c_int, i32p, i32p, f64p, f64p,
+                                       f64p, C.c_int, C.c_void_p]
         for f in ("orc_agg_fisher", "orc_agg_sidak"):
             getattr(L, f).argtypes = [C.c_int, f64p]
             getattr(L, f).restype = C.c_double
@@ -333,6 +336,41 @@ def rscape(ax, wgt, tree, want_matrices=False, hit_cap=1 << 20, **kw):
     if want_matrices:
         out["COV"] = COV.reshape(L, L)
         out["Eval"] = Ev.reshape(L, L)
+    return out
+
+
+def rscape_multi(ax, wgt, tree, covtypes, hit_cap=1 << 20, **kw):
+    """rscape() for several statistics that share the null alignments (each
+    alignment's probabilities formed once); a list of dicts, one per
+    statistic, as rscape() returns."""
+    p = params(**kw)
+    ax = np.ascontiguousarray(ax, dtype=np.uint8)
+    wgt = np.ascontiguousarray(wgt, dtype=np.float64)
+    N, L = ax.shape
+    nt = len(covtypes)
+    codes = np.array([covtype_code(t) for t in covtypes], dtype=np.int32)
+    cap = 1 << 16
+    obs = np.zeros(nt * cap, dtype=np.uint64)
+    hi = np.zeros(nt * hit_cap, dtype=np.int32)
+    hj = np.zeros(nt * hit_cap, dtype=np.int32)
+    hs = np.zeros(nt * hit_cap)
+    he = np.zeros(nt * hit_cap)
+    hp = np.zeros(nt * hit_cap)
+    res = (Result * nt)()
+    st = lib().orc_rscape_multi(C.byref(p), nt, codes.ctypes.data, ax, wgt, N, L, C.byref(tree.ct), None, None,
+                                obs, cap, hi, hj, hs, he, hp, hit_cap, res)
+    if st:
+        raise RuntimeError("orc_rscape_multi failed %d" % st)
+    out = []
+    for t in range(nt):
+        r = res[t]
+        n = min(r.nhit, hit_cap)
+        o = t * hit_cap
+        d = {f[0]: getattr(r, f[0]) for f in Result._fields_}
+        d["null_obs"] = obs[t * cap:t * cap + r.h_nb].copy()
+        d["hits"] = list(zip(hi[o:o + n].tolist(), hj[o:o + n].tolist(), hs[o:o + n].tolist(),
+                             he[o:o + n].tolist(), hp[o:o + n].tolist()))
+        out.append(d)
     return out
 
 

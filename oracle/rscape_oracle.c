@@ -342,24 +342,31 @@ orc_probs(const uint8_t *ax, const double *wgt, int N, int L, double tol,
   } else {
     /* deep alignments: the same sums (sequence order per pair) from a
      * column-major copy, pairs spread over the host threads */
+    /* column-major codes folded to 0..3 (canonical) and 4 (anything
+     * else); each pair's weights then go to a 5x5 table without branches,
+     * every cell summing its sequences' weights in sequence order */
     uint8_t *axT = malloc((size_t)N * L);
     if (!axT) return 5;
     for (s = 0; s < N; s++)
-      for (i = 0; i < L; i++) axT[(size_t)i * N + s] = ax[(size_t)s * L + i];
+      for (i = 0; i < L; i++) {
+        const int r = ax[(size_t)s * L + i];
+        axT[(size_t)i * N + s] = (uint8_t)(IS_CANON(r) ? r : K4);
+      }
 #pragma omp parallel for schedule(dynamic, 1) private(j, x, y, s)
     for (i = 0; i < L - 1; i++) {
       const uint8_t *ci = axT + (size_t)i * N;
       for (j = i + 1; j < L; j++) {
         const uint8_t *cj = axT + (size_t)j * N;
         double *p = pp + ((int64_t)i * L + j) * K16;
-        double  ne = 0.0, ng = 0.0, c[K16];
-        for (x = 0; x < K16; x++) c[x] = 1e-10;
-        for (s = 0; s < N; s++) {
-          const int ri = ci[s], rj = cj[s];
-          if (IS_CANON(ri) && IS_CANON(rj)) { ne += wgt[s]; c[ri * K4 + rj] += wgt[s]; }
-          else                              { ng += wgt[s]; }
+        double  ne = 0.0, ng = 0.0, c[25];
+        for (x = 0; x < 25; x++) c[x] = 0.0;
+        for (s = 0; s < N; s++) c[ci[s] * 5 + cj[s]] += wgt[s];
+        for (x = 0; x < 25; x++) {
+          if (x % 5 < K4 && x / 5 < K4) ne += c[x];
+          else                          ng += c[x];
         }
-        for (x = 0; x < K16; x++) p[x] = c[x];
+        for (x = 0; x < K4; x++)
+          for (y = 0; y < K4; y++) p[x * K4 + y] = 1e-10 + c[x * 5 + y];
         vec_norm(p, K16);
         for (x = 0; x < K4; x++)
           for (y = 0; y < K4; y++)
@@ -551,8 +558,11 @@ orc_raf_counts(const uint8_t *ax, int N, int L, const double *allow, double *COV
   uint8_t *axT = malloc((size_t)N * L);
   int      i, s;
   if (!axT) return 5;
-  for (s = 0; s < N; s++)
-    for (i = 0; i < L; i++) axT[(size_t)i * N + s] = ax[(size_t)s * L + i];
+  for (s = 0; s < N; s++)   /* codes folded to 0..3 and 4 (not canonical) */
+    for (i = 0; i < L; i++) {
+      const int r = ax[(size_t)s * L + i];
+      axT[(size_t)i * N + s] = (uint8_t)(r < K4 ? r : K4);
+    }
   cov_reset(L, COV, minmax);
 #pragma omp parallel for schedule(dynamic, 1)
   for (i = 0; i < L - 1; i++) {
@@ -560,15 +570,13 @@ orc_raf_counts(const uint8_t *ax, int N, int L, const double *allow, double *COV
     int j;
     for (j = i + 1; j < L; j++) {
       const uint8_t *cj = axT + (size_t)j * N;
-      long long n[K16] = {0}, r[K4] = {0}, c[K4] = {0}, nA = 0, sq = 0;
+      int n[25] = {0};
+      long long r[K4] = {0}, c[K4] = {0}, nA = 0, sq = 0;
       int x, y, t;
-      for (t = 0; t < N; t++) {
-        const int a = ci[t], b = cj[t];
-        if (a < K4 && b < K4) n[a * K4 + b]++;
-      }
+      for (t = 0; t < N; t++) n[ci[t] * 5 + cj[t]]++;
       for (x = 0; x < K4; x++)
         for (y = 0; y < K4; y++)
-          if (is_allowed(x, y, allow)) { nA += n[x * K4 + y]; r[x] += n[x * K4 + y]; c[y] += n[x * K4 + y]; }
+          if (is_allowed(x, y, allow)) { nA += n[x * 5 + y]; r[x] += n[x * 5 + y]; c[y] += n[x * 5 + y]; }
       for (x = 0; x < K4; x++) sq += r[x] * r[x] + c[x] * c[x];
       {
         double cij = (double)(nA * nA - sq / 2), qij = (double)(N - nA);
@@ -1295,15 +1303,40 @@ orc_rscape(const orc_params_t *p, const uint8_t *ax, const double *wgt, int N, i
            int *hit_i, int *hit_j, double *hit_sc, double *hit_E, double *hit_p, int hit_cap,
            orc_result_t *res)
 {
-  double  *COV = malloc(sizeof(double) * (size_t)L * L), mm[2];
-  uint8_t *shax = malloc((size_t)N * L);
-  orc_hist_t *cum = NULL, *h = NULL;
-  double  w = p->w0, fracfit = p->fracfit, pmass = p->pmass;
-  double *sf = NULL;
-  int     ns = p->nshuffle, s, i, j, status = 0, nhit = 0;
+  return orc_rscape_multi(p, 1, &p->covtype, ax, wgt, N, L, T, COV_out, Eval_out, null_obs, null_obs_cap, hit_i,
+                          hit_j, hit_sc, hit_E, hit_p, hit_cap, res);
+}
 
-  memset(res, 0, sizeof(*res));
-  if (!COV || !shax) return 1;
+/* orc_rscape for nt statistics that share the null alignments: each
+ * alignment's probabilities are formed once and every statistic is scored
+ * from them (as R-scape would with one run per statistic on the same nulls).
+ * Per-statistic outputs are nt consecutive blocks: COV_out / Eval_out of
+ * L*L, null_obs of null_obs_cap, the hit arrays of hit_cap, res[nt]. */
+int
+orc_rscape_multi(const orc_params_t *p, int nt, const int *covtypes, const uint8_t *ax, const double *wgt, int N,
+                 int L, const orc_tree_t *T, double *COV_out, double *Eval_out, uint64_t *null_obs,
+                 int null_obs_cap, int *hit_i, int *hit_j, double *hit_sc, double *hit_E, double *hit_p,
+                 int hit_cap, orc_result_t *res)
+{
+  const size_t LL = (size_t)L * L;
+  double  *COV = malloc(sizeof(double) * LL * (nt > 0 ? nt : 1)), (*mm)[2] = malloc(sizeof(double[2]) * nt);
+  uint8_t *shax = malloc((size_t)N * L);
+  double  *pp = NULL, *nseff = NULL, *ngap = NULL, *pm = NULL, *ps = NULL;
+  orc_hist_t **cum = calloc(nt, sizeof(orc_hist_t *));
+  double  *w = malloc(sizeof(double) * nt);
+  double   fracfit = p->fracfit;
+  int      ns = p->nshuffle, s, t, i, j, status = 0, probs = 0;
+
+  if (!COV || !mm || !shax || !cum || !w) { status = 1; goto DONE; }
+  for (t = 0; t < nt; t++) { memset(&res[t], 0, sizeof(res[t])); w[t] = p->w0; probs |= needs_probs(covtypes[t]); }
+  if (probs) {
+    pp    = malloc(sizeof(double) * LL * K16);
+    nseff = malloc(sizeof(double) * LL);
+    ngap  = malloc(sizeof(double) * LL);
+    pm    = malloc(sizeof(double) * (size_t)L * K4);
+    ps    = malloc(sizeof(double) * (size_t)L * 5);
+    if (!pp || !nseff || !ngap || !pm || !ps) { status = 1; goto DONE; }
+  }
   if (ns < 0) {
     ns = 20;
     if ((double)N * L < 1e3) ns = 200;
@@ -1312,78 +1345,99 @@ orc_rscape(const orc_params_t *p, const uint8_t *ax, const double *wgt, int N, i
     if (N < 4)  ns = 300;
   }
   if ((double)N * L < 1e3) fracfit = 0.3;
-  res->nshuffle = ns;
+  for (t = 0; t < nt; t++) res[t].nshuffle = ns;
+
+  /* the scores of one alignment for every statistic, into COV + t*LL */
+#define SCORE_ALL(AX)                                                                                         \
+  do {                                                                                                       \
+    if (probs && (status = orc_probs((AX), wgt, N, L, p->tol, pp, nseff, ngap, pm, ps))) goto DONE;          \
+    for (t = 0; t < nt; t++)                                                                                 \
+      if ((status = cov_from_probs(covtypes[t], p->covclass, (AX), N, L, p->nseqthresh, p->alenthresh,       \
+                                   p->allow, pp, nseff, ngap, pm, COV + t * LL, mm[t])))                     \
+        goto DONE;                                                                                           \
+  } while (0)
 
   for (s = 0; s < ns && N > 1; s++) {
-    orc_hist_t *hs = NULL;
     if ((status = orc_null_msa(ax, N, L, T, p->seed, (uint32_t)s, shax))) goto DONE;
-    status = orc_cov_calculate(p->covtype, p->covclass, shax, wgt, N, L, p->nseqthresh, p->alenthresh,
-                               p->allow, p->tol, COV, mm);
-    if (status) goto DONE;
-    if (s == 0) {
-      double lo = (p->bmin > mm[0]) ? p->bmin : mm[0], wn;
-      if (mm[1] <= p->bmin) { status = 5; goto DONE; }
-      wn = (mm[1] - lo) / (double)p->hpts;
-      w  = (w < wn) ? w : wn;
-      if (w < p->tol) w = 0.0;
-      res->null_minCOV = mm[0]; res->null_maxCOV = mm[1];
-    }
-    if (w < 1e-20) continue;       /* covariation.c:348-374: no ranklist */
-    hs  = rank_scores(L, COV, mm[1], p->bmin, w, p->tol);
-    cum = null_add(cum, hs);
-    orc_hist_free(hs);
-  }
-  res->w = w;
-
-  status = orc_cov_calculate(p->covtype, p->covclass, ax, wgt, N, L, p->nseqthresh, p->alenthresh,
-                             p->allow, p->tol, COV, mm);
-  if (status) goto DONE;
-  res->minCOV = mm[0]; res->maxCOV = mm[1];
-  if (COV_out) memcpy(COV_out, COV, sizeof(double) * (size_t)L * L);
-  if (Eval_out) for (i = 0; i < L * L; i++) Eval_out[i] = INFINITY;
-
-  if (N > 1 && w >= 1e-20 && cum) {
-    double Nt;
-    h = rank_scores(L, COV, mm[1], p->bmin, w, p->tol);
-    Nt = (double)h->Nc;
-    res->Nt = h->Nc;
-    hist_extend(cum, h->nb);
-    res->pmass_used = hist_pmass(cum, pmass, fracfit);
-    if (isnan(res->pmass_used)) { status = 6; goto DONE; }
-    res->newmass = hist_set_tail(cum, res->pmass_used);
-    if (p->doexpfit) {
-      if (fit_exp(cum, &res->mu, &res->lambda)) { status = 7; goto DONE; }
-      res->tau = 0.0;
-    } else {
-      if (fit_gamma(cum, &res->mu, &res->lambda, &res->tau)) { status = 7; goto DONE; }
-    }
-    res->fit_ok = 1;
-    if (!isinf(res->lambda)) sf = surv_tail(cum, res->newmass, p->doexpfit, res->mu, res->lambda, res->tau);
-    res->sc_thresh = evalue2cov(p->thresh, Nt, cum, sf);
-    for (i = 0; i < L - 1; i++)
-      for (j = i + 1; j < L; j++) {
-        double cov = COV[(int64_t)i * L + j];
-        double pv  = cov2evalue(cov, 1.0, cum, sf);
-        double ev  = pv * Nt;
-        if (Eval_out) Eval_out[(int64_t)i * L + j] = Eval_out[(int64_t)j * L + i] = ev;
-        if (ev < p->thresh || p->thresh > 1000) {
-          if (nhit < hit_cap) {
-            hit_i[nhit] = i; hit_j[nhit] = j; hit_sc[nhit] = cov; hit_E[nhit] = ev; hit_p[nhit] = pv;
-          }
-          nhit++;
-        }
+    SCORE_ALL(shax);
+    for (t = 0; t < nt; t++) {
+      orc_hist_t *hs;
+      if (s == 0) {
+        double lo = (p->bmin > mm[t][0]) ? p->bmin : mm[t][0], wn;
+        if (mm[t][1] <= p->bmin) { status = 5; goto DONE; }
+        wn = (mm[t][1] - lo) / (double)p->hpts;
+        w[t] = (w[t] < wn) ? w[t] : wn;
+        if (w[t] < p->tol) w[t] = 0.0;
+        res[t].null_minCOV = mm[t][0]; res[t].null_maxCOV = mm[t][1];
       }
+      if (w[t] < 1e-20) continue;       /* covariation.c:348-374: no ranklist */
+      hs     = rank_scores(L, COV + t * LL, mm[t][1], p->bmin, w[t], p->tol);
+      cum[t] = null_add(cum[t], hs);
+      orc_hist_free(hs);
+    }
   }
-  res->nhit = nhit;
-  if (cum) {
-    res->h_bmin = cum->bmin; res->h_w = cum->w; res->h_nb = cum->nb;
-    res->h_imin = cum->imin; res->h_imax = cum->imax; res->h_cmin = cum->cmin;
-    res->h_n = cum->n; res->h_Nc = cum->Nc; res->h_No = cum->No;
-    res->h_xmin = cum->xmin; res->h_xmax = cum->xmax; res->h_phi = cum->phi;
-    if (null_obs) for (i = 0; i < cum->nb && i < null_obs_cap; i++) null_obs[i] = cum->obs[i];
+
+  SCORE_ALL(ax);
+#undef SCORE_ALL
+  for (t = 0; t < nt; t++) {
+    const double *C = COV + t * LL;
+    orc_result_t *r = &res[t];
+    orc_hist_t   *h = NULL, *cm = cum[t];
+    double       *sf = NULL;
+    int           nhit = 0;
+    r->w = w[t];
+    r->minCOV = mm[t][0]; r->maxCOV = mm[t][1];
+    if (COV_out) memcpy(COV_out + t * LL, C, sizeof(double) * LL);
+    if (Eval_out) for (i = 0; i < (int)LL; i++) Eval_out[t * LL + i] = INFINITY;
+    if (N > 1 && w[t] >= 1e-20 && cm) {
+      double Nt;
+      h = rank_scores(L, C, mm[t][1], p->bmin, w[t], p->tol);
+      Nt = (double)h->Nc;
+      r->Nt = h->Nc;
+      hist_extend(cm, h->nb);
+      r->pmass_used = hist_pmass(cm, p->pmass, fracfit);
+      if (isnan(r->pmass_used)) { orc_hist_free(h); status = 6; goto DONE; }
+      r->newmass = hist_set_tail(cm, r->pmass_used);
+      if (p->doexpfit) {
+        if (fit_exp(cm, &r->mu, &r->lambda)) { orc_hist_free(h); status = 7; goto DONE; }
+        r->tau = 0.0;
+      } else {
+        if (fit_gamma(cm, &r->mu, &r->lambda, &r->tau)) { orc_hist_free(h); status = 7; goto DONE; }
+      }
+      r->fit_ok = 1;
+      if (!isinf(r->lambda)) sf = surv_tail(cm, r->newmass, p->doexpfit, r->mu, r->lambda, r->tau);
+      r->sc_thresh = evalue2cov(p->thresh, Nt, cm, sf);
+      for (i = 0; i < L - 1; i++)
+        for (j = i + 1; j < L; j++) {
+          double cov = C[(int64_t)i * L + j];
+          double pv  = cov2evalue(cov, 1.0, cm, sf);
+          double ev  = pv * Nt;
+          if (Eval_out) Eval_out[t * LL + (int64_t)i * L + j] = Eval_out[t * LL + (int64_t)j * L + i] = ev;
+          if (ev < p->thresh || p->thresh > 1000) {
+            if (nhit < hit_cap) {
+              const size_t o = (size_t)t * hit_cap + nhit;
+              hit_i[o] = i; hit_j[o] = j; hit_sc[o] = cov; hit_E[o] = ev; hit_p[o] = pv;
+            }
+            nhit++;
+          }
+        }
+    }
+    r->nhit = nhit;
+    if (cm) {
+      r->h_bmin = cm->bmin; r->h_w = cm->w; r->h_nb = cm->nb;
+      r->h_imin = cm->imin; r->h_imax = cm->imax; r->h_cmin = cm->cmin;
+      r->h_n = cm->n; r->h_Nc = cm->Nc; r->h_No = cm->No;
+      r->h_xmin = cm->xmin; r->h_xmax = cm->xmax; r->h_phi = cm->phi;
+      if (null_obs)
+        for (i = 0; i < cm->nb && i < null_obs_cap; i++) null_obs[(size_t)t * null_obs_cap + i] = cm->obs[i];
+    }
+    free(sf);
+    orc_hist_free(h);
   }
 DONE:
-  free(sf); orc_hist_free(h); orc_hist_free(cum); free(COV); free(shax);
+  if (cum) for (t = 0; t < nt; t++) orc_hist_free(cum[t]);
+  free(cum); free(w); free(COV); free(mm); free(shax);
+  free(pp); free(nseff); free(ngap); free(pm); free(ps);
   return status;
 }
 

@@ -165,6 +165,12 @@ int  orc_rscape(const orc_params_t *p, const uint8_t *ax, const double *wgt, int
                 uint64_t *null_obs, int null_obs_cap,      /* cumulative null histogram */
                 int *hit_i, int *hit_j, double *hit_sc, double *hit_E, double *hit_p, int hit_cap,
                 orc_result_t *res);
+/* orc_rscape for nt statistics sharing the nulls; per-statistic outputs in nt
+ * consecutive blocks (COV/Eval L*L, null_obs null_obs_cap, hits hit_cap) */
+int  orc_rscape_multi(const orc_params_t *p, int nt, const int *covtypes, const uint8_t *ax, const double *wgt,
+                      int N, int L, const orc_tree_t *T, double *COV_out, double *Eval_out, uint64_t *null_obs,
+                      int null_obs_cap, int *hit_i, int *hit_j, double *hit_sc, double *hit_E, double *hit_p,
+                      int hit_cap, orc_result_t *res);
 
 /* ---- reference-faithful timing mode (per-pair column gathers, FP64) ---- */
 double orc_faithful_rows(const uint8_t *ax, const double *wgt, int N, int L, int i0, int i1,

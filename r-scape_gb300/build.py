@@ -18,7 +18,8 @@ LIB = os.path.join(HERE, "libcovgpu.so")
 SYNTHLIB = os.path.join(HERE, "libcovsynth.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC]
+NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-I", INC,
+                  "-I", CSRC]
 CFLAGS = ["-O2", "-fPIC", "-std=c11", "-fopenmp", "-D_DEFAULT_SOURCE", "-Wall", "-I", INC]
 
 

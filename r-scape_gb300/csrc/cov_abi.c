@@ -143,8 +143,9 @@ corr_ReuseCOV(struct mutual_s *mi, COVTYPE mitype, COVCLASS miclass)
 {
   mi->type = mitype;
   mi->class_ = miclass;
-  if (mi->COV)  dmx_set(mi->COV, -INFINITY);
-  if (mi->Eval) dmx_set(mi->Eval, INFINITY);
+  /* device-resident: the host matrices are written only by corr_SyncHost */
+  if (mi->COV && !mi->device_resident)  dmx_set(mi->COV, -INFINITY);
+  if (mi->Eval && !mi->device_resident) dmx_set(mi->Eval, INFINITY);
   mi->besthreshCOV = -INFINITY;
   mi->minCOV = INFINITY;
   mi->maxCOV = -INFINITY;
@@ -156,9 +157,11 @@ corr_Reuse(struct mutual_s *mi, int ishuffled, COVTYPE mitype, COVCLASS miclass)
 {
   const size_t L = (size_t)mi->alen;
   mi->ishuffled = ishuffled;
-  memset(mi->pp[0][0], 0, sizeof(double) * L * L * 16);
-  memset(mi->nseff[0], 0, sizeof(double) * L * L);
-  memset(mi->ngap[0], 0, sizeof(double) * L * L);
+  if (!mi->device_resident) {   /* device-resident: pp, nseff, ngap live on the device */
+    memset(mi->pp[0][0], 0, sizeof(double) * L * L * 16);
+    memset(mi->nseff[0], 0, sizeof(double) * L * L);
+    memset(mi->ngap[0], 0, sizeof(double) * L * L);
+  }
   memset(mi->pm[0], 0, sizeof(double) * L * 4);
   memset(mi->ps[0], 0, sizeof(double) * L * 5);
   return corr_ReuseCOV(mi, mitype, miclass);
@@ -225,10 +228,12 @@ allow16(const ESL_DMATRIX *allowpair, double *a)
 static int
 score_dev(gpu_state *g, struct mutual_s *mi, int covtype, int cls, const double *allow, double *mm)
 {
-  int st = covgpu_score(g->ctx, 0, 1, 1, &covtype, cls, mi->nseqthresh, mi->alenthresh, allow, COVGPU_COUNT_TENSOR,
-                        mm);
+  /* the counts of corr_Probs on the same alignment are reused */
+  int st = covgpu_score_reuse(g->ctx, 0, 1, 1, &covtype, cls, mi->nseqthresh, mi->alenthresh, allow,
+                              COVGPU_COUNT_TENSOR, mm);
   if (st == 12)
-    st = covgpu_score(g->ctx, 0, 1, 1, &covtype, cls, mi->nseqthresh, mi->alenthresh, allow, COVGPU_COUNT_SIMT, mm);
+    st = covgpu_score_reuse(g->ctx, 0, 1, 1, &covtype, cls, mi->nseqthresh, mi->alenthresh, allow,
+                            COVGPU_COUNT_SIMT, mm);
   return st;
 }
 

@@ -99,6 +99,12 @@ struct covgpu_ctx {
   bool have_qsum = false;
   unsigned char* d_flush = nullptr;
   bool counted = false;
+  // the weighted counts in d_cnt are those of slots [cnt_first, cnt_first +
+  // cnt_nslots) as they are now (invalidated by anything that changes those
+  // alignments or the weights), so a later covgpu_score of the same slots
+  // reuses them
+  bool cnt_valid = false;
+  int cnt_first = 0, cnt_nslots = 0, cnt_counter = -1;
   cudaEvent_t ev[6] = {};
   double tms[5] = {0, 0, 0, 0, 0};
   double fit_ms = 0.0;
@@ -232,6 +238,7 @@ static int build_tiles(covgpu_ctx* ctx) {
 
 extern "C" int covgpu_resize(covgpu_ctx* ctx, int N, int L) {
   CK(cudaSetDevice(ctx->dev));
+  ctx->cnt_valid = false;
   if (N < 1 || L < 1 || N > ctx->capN || L > ctx->capL)
     return fail(ctx, 11, "%d x %d is outside the context's %d x %d", N, L, ctx->capN, ctx->capL);
   CK(cudaStreamSynchronize(ctx->st));
@@ -246,6 +253,7 @@ extern "C" int covgpu_resize(covgpu_ctx* ctx, int N, int L) {
   ctx->have_w = false;
   ctx->have_tree = false;
   ctx->counted = false;
+  ctx->cnt_valid = false;
   ctx->last_nout = ctx->last_first = ctx->last_nslots = 0;
   ctx->sim_key.clear();
   if (ctx->umma && !umma_plan_resize(ctx->umma, N, L, ctx->Lp, ctx->nT, ctx->ntiles)) {
@@ -258,6 +266,7 @@ extern "C" int covgpu_resize(covgpu_ctx* ctx, int N, int L) {
 extern "C" int covgpu_set_weights(covgpu_ctx* ctx, const double* wgt) {
   CK(cudaSetDevice(ctx->dev));
   const int N = ctx->N;
+  ctx->cnt_valid = false;
   double s = 0.0;
   for (int i = 0; i < N; i++) {
     if (!(wgt[i] >= 0.0) || !std::isfinite(wgt[i])) return fail(ctx, 11, "weight %d is negative or not finite", i);
@@ -282,6 +291,7 @@ extern "C" int covgpu_set_weights(covgpu_ctx* ctx, const double* wgt) {
 extern "C" int covgpu_set_alignment(covgpu_ctx* ctx, int slot, const uint8_t* ax) {
   if (slot < 0 || slot >= ctx->maxslots) return fail(ctx, 11, "slot %d out of range", slot);
   CK(cudaSetDevice(ctx->dev));
+  ctx->cnt_valid = false;
   // the largest code first (a reduction the compiler vectorises); the
   // position of a bad code is looked up only when there is one
   const int64_t n = (int64_t)ctx->N * ctx->L;
@@ -347,6 +357,7 @@ extern "C" int covgpu_set_tree(covgpu_ctx* ctx, const int* parent, const int* le
 
 static int make_nulls_async(covgpu_ctx* ctx, uint64_t seed, int first_null, int nnull, int first_slot) {
   if (nnull <= 0) return 0;
+  ctx->cnt_valid = false;
   if (!ctx->have_tree) return fail(ctx, 11, "no tree set");
   if (nnull > ctx->maxnull) return fail(ctx, 11, "%d nulls > capacity %d", nnull, ctx->maxnull);
   if (first_slot < 1 || first_slot + nnull > ctx->maxslots) return fail(ctx, 11, "null slots out of range");
@@ -364,6 +375,7 @@ static int check_status(covgpu_ctx* ctx);
 
 extern "C" int covgpu_weights_pb_dev(covgpu_ctx* ctx, int slot, int set, double* wgt) {
   CK(cudaSetDevice(ctx->dev));
+  ctx->cnt_valid = false;
   const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
   if (slot < 0 || slot >= ctx->maxslots || !wgt) return fail(ctx, 11, "bad slot or output");
   // scratch kept across calls (a cudaFree per call would synchronise the device)
@@ -383,6 +395,7 @@ extern "C" int covgpu_weights_pb_dev(covgpu_ctx* ctx, int slot, int set, double*
 
 extern "C" int covgpu_weights_gsc_dev(covgpu_ctx* ctx, int slot, int set, double* wgt) {
   CK(cudaSetDevice(ctx->dev));
+  ctx->cnt_valid = false;
   const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
   if (slot < 0 || slot >= ctx->maxslots || !wgt) return fail(ctx, 11, "bad slot or output");
   if (N > 16384) return fail(ctx, 11, "GSC weights are for up to 16384 sequences (N^2 distances)");
@@ -512,6 +525,7 @@ extern "C" int covgpu_simulate(covgpu_ctx* ctx, const double* ld, const double* 
                                const uint8_t* root, double gap_rate, double gap_mean, uint64_t seed, uint32_t rep0,
                                int first_slot, int nrep) {
   CK(cudaSetDevice(ctx->dev));
+  ctx->cnt_valid = false;
   const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
   if (!ctx->have_tree) return fail(ctx, 11, "no tree set");
   if (N < 2) return fail(ctx, 11, "the simulator needs a tree of at least two leaves");
@@ -627,7 +641,7 @@ static int stat_index(int base) {
 }
 
 static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const int* types, int covclass,
-                       int nseqthresh, int alenthresh, const double* allow, int counter) {
+                       int nseqthresh, int alenthresh, const double* allow, int counter, bool reuse = false) {
   if (ntypes < 1 || ntypes > MAXOUT) return fail(ctx, 11, "1..%d covariation types per call", MAXOUT);
   if (first < 0 || nslots < 1 || first + nslots > ctx->maxslots) return fail(ctx, 11, "slots out of range");
   if (!ctx->have_w) return fail(ctx, 11, "weights not set");
@@ -658,7 +672,9 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
   const int64_t sstride = (int64_t)N * Lp;
   const uint8_t* ax = ctx->d_ax + first * sstride;
   const int64_t cstride = (int64_t)ntiles * 16 * TPP;
-  if (need_w) {
+  const bool have = reuse && ctx->cnt_valid && ctx->cnt_first == first && ctx->cnt_nslots == nslots &&
+                    ctx->cnt_counter == counter;
+  if (need_w && !have) {
     if (counter == COVGPU_COUNT_TENSOR) {
       if (!ctx->umma) {
         ctx->umma = umma_plan_create(N, L, Lp, ctx->nT, ctx->d_tiles, ntiles, ctx->maxslots, ctx->capN, ctx->capLp,
@@ -678,6 +694,8 @@ static int score_async(covgpu_ctx* ctx, int first, int nslots, int ntypes, const
                        ctx->d_meanp, ctx->d_status, ctx->st));
     // operand preparation + count (tensor) or count; marginals, pm, mean p
     ctx->nlaunch += (counter == COVGPU_COUNT_TENSOR ? 2 : 1) + 3;
+    ctx->cnt_valid = true;
+    ctx->cnt_first = first; ctx->cnt_nslots = nslots; ctx->cnt_counter = counter;
   }
   if (need_u) {
     if (!ctx->d_ucnt) CK(dalloc(&ctx->d_ucnt, (size_t)ctx->maxslots * ctx->capntiles * 16 * TPP));
@@ -759,17 +777,31 @@ static int check_status(covgpu_ctx* ctx) {
   return 0;
 }
 
-extern "C" int covgpu_score(covgpu_ctx* ctx, int first_slot, int nslots, int ntypes, const int* covtypes,
-                            int covclass, int nseqthresh, int alenthresh, const double* allow, int counter,
-                            double* minmax) {
+static int score_sync(covgpu_ctx* ctx, int first_slot, int nslots, int ntypes, const int* covtypes, int covclass,
+                      int nseqthresh, int alenthresh, const double* allow, int counter, double* minmax, bool reuse) {
   CK(cudaSetDevice(ctx->dev));
-  int s = score_async(ctx, first_slot, nslots, ntypes, covtypes, covclass, nseqthresh, alenthresh, allow, counter);
+  int s = score_async(ctx, first_slot, nslots, ntypes, covtypes, covclass, nseqthresh, alenthresh, allow, counter,
+                      reuse);
   if (s) return s;
   if (minmax)
     CK(cudaMemcpyAsync(minmax, ctx->d_mm, (size_t)nslots * ntypes * 2 * sizeof(double), cudaMemcpyDeviceToHost,
                        ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   return check_status(ctx);
+}
+
+extern "C" int covgpu_score(covgpu_ctx* ctx, int first_slot, int nslots, int ntypes, const int* covtypes,
+                            int covclass, int nseqthresh, int alenthresh, const double* allow, int counter,
+                            double* minmax) {
+  return score_sync(ctx, first_slot, nslots, ntypes, covtypes, covclass, nseqthresh, alenthresh, allow, counter,
+                    minmax, false);
+}
+
+extern "C" int covgpu_score_reuse(covgpu_ctx* ctx, int first_slot, int nslots, int ntypes, const int* covtypes,
+                                  int covclass, int nseqthresh, int alenthresh, const double* allow, int counter,
+                                  double* minmax) {
+  return score_sync(ctx, first_slot, nslots, ntypes, covtypes, covclass, nseqthresh, alenthresh, allow, counter,
+                    minmax, true);
 }
 
 extern "C" int covgpu_get_cov(covgpu_ctx* ctx, int slot, int which, double* COV) {
@@ -818,10 +850,17 @@ extern "C" int covgpu_get_probs(covgpu_ctx* ctx, int slot, const double* wgt, do
     if (wgt) { wt = 0.0; for (int s = 0; s < N; s++) wt += wgt[s]; }
     std::vector<TileRC> tiles(ntl);
     CK(cudaMemcpy(tiles.data(), ctx->d_tiles, ntl * sizeof(TileRC), cudaMemcpyDeviceToHost));
-    if (nseff) for (int64_t k = 0; k < (int64_t)L * L; k++) nseff[k] = 0.0;
-    if (ngap) for (int64_t k = 0; k < (int64_t)L * L; k++) ngap[k] = 0.0;
-    if (pp) for (int64_t k = 0; k < (int64_t)L * L * 16; k++) pp[k] = 0.0;
-    for (size_t t = 0; t < ntl; t++)
+    // the reference's host layout, filled over the host threads (every pair
+    // belongs to one tile, so the tiles' writes are disjoint)
+    const int64_t LL = (int64_t)L * L;
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < LL; k++) {
+      if (nseff) nseff[k] = 0.0;
+      if (ngap) ngap[k] = 0.0;
+      if (pp) for (int q = 0; q < 16; q++) pp[k * 16 + q] = 0.0;
+    }
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t t = 0; t < (int64_t)ntl; t++)
       for (int p = 0; p < TPP; p++) {
         const int i = tiles[t].I * TP + p / TP, j = tiles[t].J * TP + p % TP;
         if (!(i < j && j < L)) continue;
@@ -923,6 +962,7 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   }
   ctx->nlaunch = 0;
   ctx->counted = false;
+  ctx->cnt_valid = false;
   ctx->fit_ms = 0.0;
   int s;
   // ax / wgt == NULL: use the alignment and weights already on the device
@@ -1420,6 +1460,7 @@ extern "C" int covgpu_aggregate(covgpu_ctx* ctx, int method, int nh, const int* 
 extern "C" int covgpu_autotune(covgpu_ctx* ctx, int first_slot, int nslots, int ncand, const int* cand, float* ms,
                                int* best) {
   CK(cudaSetDevice(ctx->dev));
+  ctx->cnt_valid = false;
   static const int defaults[] = {4, 6, 8, 10, 12, 16, 24};
   if (!cand || ncand <= 0) { cand = defaults; ncand = (int)(sizeof(defaults) / sizeof(defaults[0])); }
   if (first_slot < 0 || nslots < 1 || first_slot + nslots > ctx->maxslots) return fail(ctx, 11, "slots out of range");
@@ -1439,6 +1480,7 @@ extern "C" int covgpu_autotune(covgpu_ctx* ctx, int first_slot, int nslots, int 
   if (ms) for (int k = 0; k < ncand; k++) ms[k] = t[k];
   if (best) *best = b;
   ctx->counted = false;
+  ctx->cnt_valid = false;
   return check_status(ctx);
 }
 

@@ -200,3 +200,31 @@ def test_shipped_network_on_held_out_families(covgpu):
     assert s["used_net"] >= 14 and s["null_reduction"] >= 5
     assert s["net_finite_frac"] == 1.0
     assert s["net_median_rel_E_error"] < 0.35
+
+
+def test_network_beats_its_quick_nulls_own_fit(covgpu):
+    """What the trained network gains over the method without it: on 40
+    held-out families (seeds outside the training and evaluation ranges),
+    the E-values from the quick nulls plus the network against those from
+    the same quick nulls' own tail fit, both judged by the 200-null fit.
+    The network must have the lower median relative E-value error and win
+    in most of the families with a tail."""
+    import importlib.util
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("learned_null", os.path.join(root, "r-scape_gb300",
+                                                                                "learned_null.py"))
+    ln = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(ln)
+    path = os.path.join(root, "r-scape_gb300", "learned_null_gtp.npz")
+    net = ln.load(path)
+    nq = int(np.load(path)["nquick"])
+    rows = ln.evaluate(net, 310001, 40, 200, nquick=nq, few=0)
+    s = ln.summarize(rows, 200)
+    net.close()
+    print("\nheld-out families: %s" % {k: s[k] for k in ("families_with_tail", "net_median_rel_E_error",
+                                                            "quick_median_rel_E_error", "net_better_than_quick",
+                                                            "null_reduction")})
+    assert s["families_with_tail"] >= 15
+    assert s["net_median_rel_E_error"] < s["quick_median_rel_E_error"]
+    assert s["net_better_than_quick"] > s["families_with_tail"] / 2
