@@ -359,6 +359,18 @@ def cpu_reference(ax, w, budget_s, threads):
                                     "count_gt_pairs_per_s": 1.0 / t_count}
 
 
+def max_over_ranks(values, world):
+    """Each value's largest over the ranks (the slowest rank's times), by an
+    all-reduce on the process group; the values themselves with one rank."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -485,11 +497,7 @@ def main():
             e2e_hits = sum(len(x["hits"]) for x in r)
         e2e_s = (time.perf_counter() - t0) / args.steps
     step_s = sum(dev_ms) / len(dev_ms) / 1000.0
-    if world > 1:
-        import torch
-        t = torch.tensor([step_s, e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_s, e2e_s = float(t[0]), float(t[1])
+    step_s, e2e_s = max_over_ranks([step_s, e2e_s], world)
     if rank != 0:
         return
     value = world * pairs_step / step_s
@@ -540,6 +548,8 @@ def main():
         "gpu_launches": nl,
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic, "kernel": kname,
+                     # three FP16 weight limbs: the tensor cores execute 3 x the algorithmic FLOP
+                     "executed_frac": (3.0 * achieved / peak) if kind == "tensor" else None,
                      "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback 1.9 PFLOP/s"},
         "cpu_baseline": {"value": cpu_v, "unit": "column-pairs/s", "cores": threads, "kind": "port",
                          "sample": cpu_sample,

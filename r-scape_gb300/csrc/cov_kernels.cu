@@ -397,8 +397,9 @@ __global__ void k_pm_final(const double* __restrict__ part4, const double* __res
   const int I = c / TP, a = c % TP;
   double m[4] = {0, 0, 0, 0}, rs = 0.0;
   for (int K = 0; K < nT; K++) {
-    const double4 v = *reinterpret_cast<const double4*>(P + (((int64_t)I * nT + K) * TP + a) * 4);
-    m[0] += v.x; m[1] += v.y; m[2] += v.z; m[3] += v.w;
+    const double2* v = reinterpret_cast<const double2*>(P + (((int64_t)I * nT + K) * TP + a) * 4);
+    const double2 v0 = v[0], v1 = v[1];
+    m[0] += v0.x; m[1] += v0.y; m[2] += v1.x; m[3] += v1.y;
     rs += R[((int64_t)I * nT + K) * TP + a];
   }
   const double sum = m[0] + m[1] + m[2] + m[3];
