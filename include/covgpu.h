@@ -167,6 +167,41 @@ int  covgpu_get_probs(covgpu_ctx *ctx, int slot, const double *wgt, double *pp, 
 int  covgpu_rscape(covgpu_ctx *ctx, const covgpu_params *p, const uint8_t *ax, const double *wgt,
                    int ntypes, const int *covtypes, covgpu_result *results, covgpu_hit *hits, int hitcap);
 
+/* ---- the E-valued path over a batch of alignment families ----
+ * A family is one input alignment with its tree; families differ in N, L and
+ * null count.  covgpu_rscape_families does for every family what
+ * covgpu_rscape does for one (the same nulls for the same seed, the same
+ * statistics, histograms, tail fits and E-values), with every device pass
+ * one grouped launch over the families: GSC or position-based weights
+ * (R-scape's rule, src/R-scape.c:1545-1562, where wgt is NULL), the nulls
+ * (one launch per tree depth over every family), the counts (one persistent
+ * tensor-core launch over every family's tiles), the statistics and APC/ASC,
+ * the null histograms, the tail fits (one block per fit), the survival
+ * tables and the E-values; the host steps run once per phase for all
+ * families.  Families are processed in chunks that fit the batch's device
+ * budget (mem_gb; 0: a quarter of the free memory); the device passes of a
+ * chunk run as a CUDA graph, replayed while the chunk's layout repeats. */
+typedef struct covgpu_batch covgpu_batch;
+typedef struct {
+  int            N, L;
+  const uint8_t *ax;       /* N x L codes, row-major */
+  const double  *wgt;      /* N weights, or NULL: R-scape's rule on the device */
+  const int     *parent;   /* the tree (covgpu_set_tree convention), N-1 entries each; */
+  const int     *left;     /* parent may be NULL */
+  const int     *right;
+} covgpu_family;
+int  covgpu_batch_create(covgpu_batch **ret, int device, double mem_gb);
+void covgpu_batch_destroy(covgpu_batch *b);
+const char *covgpu_batch_errmsg(const covgpu_batch *b);
+/* results[nfam * ntypes] (family-major); hits[nfam * ntypes * hitcap];
+ * returns 0 or the first error (its message names the family) */
+int  covgpu_rscape_families(covgpu_batch *b, const covgpu_params *p, int nfam, const covgpu_family *fams,
+                            int ntypes, const int *covtypes, covgpu_result *results, covgpu_hit *hits, int hitcap);
+/* the last call: device milliseconds of [0] the passes from the nulls to the
+ * corrected scores, [1] the histograms, fits and E-values (with their host
+ * steps), [2] host wall clock of the whole call; kernel launches; chunks */
+int  covgpu_batch_timing(const covgpu_batch *b, double *ms3, int *nlaunch, int *nchunks);
+
 /* device timing of the last covgpu_rscape phases, milliseconds:
  * [0] nulls [1] counts [2] statistics+correction [3] histograms+fit+E-values
  * [4] total; also the number of kernel launches */

@@ -56,6 +56,11 @@ class Hit(C.Structure):
     _fields_ = [("i", C.c_int), ("j", C.c_int), ("sc", C.c_double), ("E", C.c_double), ("pval", C.c_double)]
 
 
+class Family(C.Structure):
+    _fields_ = [("N", C.c_int), ("L", C.c_int), ("ax", C.c_void_p), ("wgt", C.c_void_p), ("parent", C.c_void_p),
+                ("left", C.c_void_p), ("right", C.c_void_p)]
+
+
 def lib():
     global _LIB
     if _LIB is None:
@@ -119,6 +124,13 @@ def lib():
         L.covgpu_learned_features.argtypes = [vp, C.POINTER(Params), C.c_double, C.c_int, C.c_int, f32p]
         L.covgpu_rscape_learned.argtypes = [vp, C.POINTER(Params), vp, vp, vp, C.c_double, C.c_int, C.c_int,
                                             C.POINTER(Result), C.POINTER(Hit), C.c_int, C.POINTER(C.c_int)]
+        L.covgpu_batch_create.argtypes = [C.POINTER(vp), C.c_int, C.c_double]
+        L.covgpu_batch_destroy.argtypes = [vp]
+        L.covgpu_batch_errmsg.argtypes = [vp]
+        L.covgpu_batch_errmsg.restype = C.c_char_p
+        L.covgpu_rscape_families.argtypes = [vp, C.POINTER(Params), C.c_int, C.POINTER(Family), C.c_int, i32p,
+                                             C.POINTER(Result), C.POINTER(Hit), C.c_int]
+        L.covgpu_batch_timing.argtypes = [vp, f64p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _LIB = L
     return _LIB
 
@@ -503,3 +515,77 @@ class MLP:
         hist = np.zeros(epochs, dtype=np.float32)
         self._ck(lib().covgpu_mlp_train(self.h, X, T, X.shape[0], epochs, batch, lr, wd, seed, hist))
         return hist
+
+
+class Batch:
+    """The E-valued path over a batch of alignment families on one device
+    (include/covgpu.h, covgpu_rscape_families)."""
+
+    def __init__(self, device=0, mem_gb=0.0):
+        self.h = C.c_void_p()
+        st = lib().covgpu_batch_create(C.byref(self.h), device, float(mem_gb))
+        if st:
+            msg = lib().covgpu_batch_errmsg(self.h).decode() if self.h else ""
+            self.close()
+            raise RuntimeError("covgpu_batch_create failed (%d): %s" % (st, msg))
+
+    def close(self):
+        if self.h:
+            lib().covgpu_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def rscape(self, families, types, hitcap=1 << 12, **kw):
+        """families: dicts with ax [N][L] (uint8), parent/left/right (int32,
+        N-1 each; parent optional) and optionally wgt [N] (None: R-scape's rule
+        on the device).  Returns, per family, the list of result dicts of
+        covgpu_rscape (one per type)."""
+        p = params(**kw)
+        codes = np.array([covtype_code(t) for t in types], dtype=np.int32)
+        nf, nt = len(families), len(codes)
+        keep = []
+        fam = (Family * max(nf, 1))()
+        for k, f in enumerate(families):
+            ax = np.ascontiguousarray(f["ax"], dtype=np.uint8)
+            keep.append(ax)
+            fam[k].N, fam[k].L = ax.shape
+            fam[k].ax = ax.ctypes.data
+            for name in ("wgt", "parent", "left", "right"):
+                v = f.get(name)
+                if v is None:
+                    setattr(fam[k], name, None)
+                    continue
+                a = np.ascontiguousarray(v, dtype=np.float64 if name == "wgt" else np.int32)
+                keep.append(a)
+                setattr(fam[k], name, a.ctypes.data)
+        res = (Result * max(nf * nt, 1))()
+        hits = (Hit * max(nf * nt * hitcap, 1))()
+        st = lib().covgpu_rscape_families(self.h, C.byref(p), nf, fam, nt, codes, res, hits, hitcap)
+        if st:
+            raise RuntimeError("covgpu batch error %d: %s" % (st, lib().covgpu_batch_errmsg(self.h).decode()))
+        out = []
+        for k in range(nf):
+            rows = []
+            for q in range(nt):
+                e = k * nt + q
+                r = {f[0]: getattr(res[e], f[0]) for f in Result._fields_}
+                n = min(r["nhit"], hitcap)
+                b = e * hitcap
+                r["hits"] = [(hits[b + i].i, hits[b + i].j, hits[b + i].sc, hits[b + i].E, hits[b + i].pval)
+                             for i in range(n)]
+                rows.append(r)
+            out.append(rows)
+        return out
+
+    def timing(self):
+        """(ms of the passes to the corrected scores, ms of the rest, host ms
+        of the call, kernel launches, chunks) of the last call."""
+        ms = np.zeros(3)
+        n, c = C.c_int(), C.c_int()
+        lib().covgpu_batch_timing(self.h, ms, C.byref(n), C.byref(c))
+        return ms[0], ms[1], ms[2], n.value, c.value

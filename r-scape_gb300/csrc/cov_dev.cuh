@@ -32,6 +32,24 @@ constexpr int NSTAT = 9;
 
 struct TileRC { int I, J; };
 
+// the block a kernel body works on: the launch's own blockIdx.x, blockIdx.y
+// and gridDim.x, or the coordinates inside one alignment family of a grouped
+// launch (one launch over the blocks of many families)
+struct GridIdx { int x, y, gx; };
+__device__ __forceinline__ GridIdx native_grid() {
+  return GridIdx{(int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x};
+}
+// the entry f of the ascending prefix pre[0..nf] with pre[f] <= b < pre[f + 1]
+// (entries of empty families are skipped: their prefix does not advance)
+__device__ __forceinline__ int grp_find(const int* __restrict__ pre, int nf, int b) {
+  int lo = 0, hi = nf;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(pre + mid) <= b) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // ---- Philox4x32-10 (Salmon et al., SC'11) ----
 __host__ __device__ __forceinline__ void philox4x32(uint32_t k0, uint32_t k1, uint32_t c[4]) {
 #pragma unroll

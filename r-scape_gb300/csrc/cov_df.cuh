@@ -4,7 +4,12 @@
 // scores are carried in double-float on the FP32 pipes.
 //
 // Error-free transformations: two_sum (Knuth), fast_two_sum (Dekker,
-// |a| >= |b|), two_prod via FMA.  df_log is a table-driven natural
+// |a| >= |b|), two_prod via FMA.  Their sums and the products that feed them
+// are written with the round-to-nearest intrinsics (__fadd_rn, __fsub_rn,
+// __fmul_rn), which the compiler never contracts into an FMA: a product
+// fused into the sum of a transformation would leave its low word wrong by
+// up to an FP32 rounding, and would do so differently in every kernel that
+// inlines it.  df_log is a table-driven natural
 // logarithm (argument reduction by a 128-entry reciprocal table, then the
 // series of ln(1 + t) for |t| < 2^-7.9); its absolute error is below
 // 2e-13 over the range the statistics use (1e-10 .. 2^40), against the
@@ -18,56 +23,58 @@ namespace covgpu {
 struct df { float hi, lo; };
 
 __device__ __forceinline__ df two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  return {s, (a - (s - bb)) + (b - bb)};
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
 }
 __device__ __forceinline__ df fast_two_sum(float a, float b) {   // |a| >= |b| or a == 0
-  const float s = a + b;
-  return {s, b - (s - a)};
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 __device__ __forceinline__ df df_norm(df a) { return fast_two_sum(a.hi, a.lo); }
 __device__ __forceinline__ df df_add_f(df a, float b) {
   const df s = two_sum(a.hi, b);
-  return fast_two_sum(s.hi, s.lo + a.lo);
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
 }
 __device__ __forceinline__ df df_add(df a, df b) {
   const df s = two_sum(a.hi, b.hi);
-  return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 // accumulation without renormalising: the low part gathers the rounding
 // errors (each below ulp(hi)), renormalised once by the caller (df_norm)
 __device__ __forceinline__ void df_acc(df& s, df b) {
   const df t = two_sum(s.hi, b.hi);
   s.hi = t.hi;
-  s.lo += t.lo + b.lo;
+  s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, b.lo));
 }
 __device__ __forceinline__ df df_mul(df a, df b) {
-  const float p = a.hi * b.hi;
+  const float p = __fmul_rn(a.hi, b.hi);
   const float e = fmaf(a.hi, b.hi, -p);
   return fast_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
 }
 // product left unnormalised (for df_acc)
 __device__ __forceinline__ df df_mul_u(df a, df b) {
-  const float p = a.hi * b.hi;
+  const float p = __fmul_rn(a.hi, b.hi);
   return {p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)))};
 }
 // a^2, unnormalised
 __device__ __forceinline__ df df_sqr_u(df a) {
-  const float p = a.hi * a.hi;
+  const float p = __fmul_rn(a.hi, a.hi);
   return {p, fmaf(2.f * a.hi, a.lo, fmaf(a.hi, a.hi, -p))};
 }
-__device__ __forceinline__ df df_scale(df a, float s) { return {a.hi * s, a.lo * s}; }   // s a power of two
+__device__ __forceinline__ df df_scale(df a, float s) {   // s a power of two
+  return {__fmul_rn(a.hi, s), __fmul_rn(a.lo, s)};
+}
 __device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
 // 1/b and a/b: an FP32 estimate corrected by one residual step (relative
 // error ~2^-46)
 __device__ __forceinline__ df df_div(df a, df b) {
   const float r = 1.0f / b.hi;
-  const float q1 = a.hi * r;
+  const float q1 = __fmul_rn(a.hi, r);
   const df pr = df_mul_u(b, {q1, 0.f});
   const df res = df_add(a, df_neg(df_norm(pr)));
-  return fast_two_sum(q1, res.hi * r);
+  return fast_two_sum(q1, __fmul_rn(res.hi, r));
 }
 __device__ __forceinline__ df df_recip(df b) { return df_div({1.f, 0.f}, b); }
 __device__ __forceinline__ df df_of(double x) {
@@ -76,7 +83,7 @@ __device__ __forceinline__ df df_of(double x) {
 }
 __device__ __forceinline__ double df_to_d(df a) { return (double)a.hi + (double)a.lo; }
 __device__ __forceinline__ df two_prod(float a, float b) {
-  const float p = a * b;
+  const float p = __fmul_rn(a, b);
   return {p, fmaf(a, b, -p)};
 }
 __device__ __forceinline__ df ld_df(const float2* p) { const float2 v = *p; return {v.x, v.y}; }
@@ -109,20 +116,20 @@ __device__ __forceinline__ df df_log(df a, const float4* __restrict__ tab) {
   const int j = (bits >> 16) & (LOGTAB_N - 1);
   const float m = __int_as_float((bits & 0x007FFFFF) | 0x3F800000);
   const float4 T = tab[j];
-  const float p = m * T.x;
+  const float p = __fmul_rn(m, T.x);
   const float pe = fmaf(m, T.x, -p);
-  const df t = fast_two_sum(p - 1.0f, pe);   // p - 1 is exact (p within 2^-7 of 1)
-  const float s2 = t.hi * t.hi;
+  const df t = fast_two_sum(__fsub_rn(p, 1.0f), pe);   // p - 1 is exact (p within 2^-7 of 1)
+  const float s2 = __fmul_rn(t.hi, t.hi);
   const float s2e = fmaf(t.hi, t.hi, -s2);  // t.hi^2 = s2 + s2e exactly
-  const float poly = (t.hi * s2) * fmaf(t.hi, fmaf(t.hi, 0.2f, -0.25f), 0.333333343f);
+  const float poly = __fmul_rn(__fmul_rn(t.hi, s2), fmaf(t.hi, fmaf(t.hi, 0.2f, -0.25f), 0.333333343f));
   const float corr = __fdividef(a.lo, a.hi);
-  const float low = ((t.lo - t.hi * t.lo) - 0.5f * s2e) + (poly + corr);
-  const df l1p = fast_two_sum(t.hi, -0.5f * s2);
+  const float low = __fadd_rn(__fsub_rn(fmaf(-t.hi, t.lo, t.lo), __fmul_rn(0.5f, s2e)), __fadd_rn(poly, corr));
+  const df l1p = fast_two_sum(t.hi, __fmul_rn(-0.5f, s2));
   const float kf = (float)k;
-  df kl = two_sum(kf * LN2_A, kf * LN2_B);
+  df kl = two_sum(__fmul_rn(kf, LN2_A), __fmul_rn(kf, LN2_B));
   kl.lo = fmaf(kf, LN2_C, kl.lo);
   df r = df_add(kl, {T.y, T.z});
-  return df_add(r, {l1p.hi, l1p.lo + low});
+  return df_add(r, {l1p.hi, __fadd_rn(l1p.lo, low)});
 }
 
 // the table of df_log (LOGTAB_N entries), made on the host in FP64; each
@@ -142,16 +149,16 @@ void logtab_host(float4* tab);
 // scale 2^-E is a power of two.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ df limb_count(float d0, float d1, float d2, float B, float scale) {
-  const float c2 = d2 * (B * B), c1 = d1 * B;
+  const float c2 = __fmul_rn(d2, __fmul_rn(B, B)), c1 = __fmul_rn(d1, B);
   const df s1 = two_sum(c2, c1);
   const df s2 = two_sum(s1.hi, d0);
-  const df r = fast_two_sum(s2.hi, s1.lo + s2.lo);
-  return {r.hi * scale, r.lo * scale};
+  const df r = fast_two_sum(s2.hi, __fadd_rn(s1.lo, s2.lo));
+  return {__fmul_rn(r.hi, scale), __fmul_rn(r.lo, scale)};
 }
 // equal weights w (one limb: the unit count c times w as hi + lo)
 __device__ __forceinline__ df unit_count(float c, float w_hi, float w_lo) {
-  const float p = c * w_hi;
-  return fast_two_sum(p, fmaf(c, w_hi, -p) + c * w_lo);
+  const float p = __fmul_rn(c, w_hi);
+  return fast_two_sum(p, fmaf(c, w_lo, fmaf(c, w_hi, -p)));
 }
 
 }  // namespace covgpu

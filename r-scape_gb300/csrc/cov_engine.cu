@@ -22,6 +22,7 @@
 #include "cov_subst.h"
 #include "cov_umma.h"
 #include "covgpu.h"
+#include "cov_rscape_host.h"
 #include "rscape_cov.h"
 
 using namespace covgpu;
@@ -950,6 +951,126 @@ static void null_summary(const ESL_HISTOGRAM* h, double xmax, double mu, double 
   out[16] = (out[16] - out[13]) / m;
 }
 
+// ------------------------------------------------------------------------
+// the host steps of the E-valued path per statistic, shared by
+// covgpu_rscape and the family batch (cov_rscape_host.h)
+// ------------------------------------------------------------------------
+int rs_nshuffle(const covgpu_params* p, int N, int L, double* fracfit) {
+  int ns = p->nshuffle;
+  *fracfit = p->fracfit;
+  if (ns < 0) {   // src/R-scape.c:2449-2456
+    ns = 20;
+    if ((double)N * L < 1e3) ns = 200;
+    if (L < 50) ns = 200;
+    if (L < 40) ns = 300;
+    if (N < 4) ns = 300;
+  }
+  if ((double)N * L < 1e3) *fracfit = 0.3;   // :2458-2459
+  if (N == 1) ns = 0;
+  return ns;
+}
+
+int rs_width(const covgpu_params* p, int N, int ns, const double* mm, int ntypes, int q, covgpu_result& R,
+             RsStat& X, char* err, size_t errlen) {
+  auto MMn = [&](int slot, int k) { return mm[((size_t)slot * ntypes + q) * 2 + k]; };
+  R.nshuffle = ns;
+  R.minCOV = MMn(0, 0); R.maxCOV = MMn(0, 1);
+  if (N == 1) { R.status = 2; return 0; }
+  // calculate_width_histo (src/R-scape.c:1353-1360) on the first null
+  double w = p->w0;
+  const double nmin = MMn(1, 0), nmax = MMn(1, 1);
+  R.null_minCOV = nmin; R.null_maxCOV = nmax;
+  if (nmax <= p->bmin) {
+    snprintf(err, errlen, "bmin %f should be larger than maxCOV %f", p->bmin, nmax);
+    return 30;
+  }
+  const double wn = (nmax - std::max(p->bmin, nmin)) / (double)p->hpts;
+  w = std::min(w, wn);
+  if (w < p->tol) w = 0.0;
+  R.w = w;
+  if (w < 1e-20) { R.status = 1; return 0; }   // src/covariation.c:348-374
+  // null histograms share bmin and w: their sum is the cumulative null
+  int nbcum = 0;
+  double xmin = INFINITY, xmax = -INFINITY;
+  for (int k = 1; k <= ns; k++) {
+    double bmax = MMn(k, 1) + 5 * w;
+    while (fabs(bmax - p->bmin) < p->tol) bmax += w;
+    nbcum = std::max(nbcum, bins_for(p->bmin, bmax, w));
+    xmin = std::min(xmin, std::max(MMn(k, 0), p->bmin + w));
+    xmax = std::max(xmax, std::max(MMn(k, 1), p->bmin + w));
+  }
+  double bmax_r = R.maxCOV + 5 * w;
+  while (fabs(bmax_r - p->bmin) < p->tol) bmax_r += w;
+  X.active = true;
+  X.w = w; X.xmin = xmin; X.xmax = xmax; X.nbcum = nbcum;
+  X.nb_real = bins_for(p->bmin, bmax_r, w);
+  // the window starts one bin below the smallest null score's bin
+  X.wbase = std::isfinite(xmin) ? std::max(0, (int)std::floor((xmin - p->bmin) / w) - 2) : 0;
+  return 0;
+}
+
+int rs_histogram(const covgpu_params* p, double fracfit, int ns, int64_t P, const uint64_t* ob, RsStat& X, char* err,
+                 size_t errlen) {
+  const int nbcum = X.nbcum;
+  double bmax_c = p->bmin + nbcum * X.w;
+  ESL_HISTOGRAM* h = covh_Create(p->bmin, bmax_c, X.w);
+  if (!h) { snprintf(err, errlen, "out of host memory"); return 5; }
+  X.h = h;
+  if (h->nb != nbcum) {   // guard the rounding of (bmax - bmin)/w
+    free(h->obs); h->nb = nbcum; h->obs = (uint64_t*)calloc(nbcum, sizeof(uint64_t));
+  }
+  uint64_t tot = 0;
+  int imin = nbcum, imax = -1;
+  for (int b = 0; b < nbcum; b++) {
+    h->obs[b] = ob[b]; tot += ob[b];
+    if (ob[b]) { imin = std::min(imin, b); imax = std::max(imax, b); }
+  }
+  h->n = (uint64_t)ns * (uint64_t)P; h->Nc = tot; h->No = tot;
+  h->xmin = X.xmin; h->xmax = X.xmax; h->imin = imin; h->imax = imax; h->cmin = imin;
+  if (h->nb < X.nb_real) {   // src/covariation.c:462-466
+    h->obs = (uint64_t*)realloc(h->obs, sizeof(uint64_t) * X.nb_real);
+    for (int b = h->nb; b < X.nb_real; b++) h->obs[b] = 0;
+    h->nb = X.nb_real;
+  }
+  X.pmass = covh_pmass(h, p->pmass, fracfit);
+  if (std::isnan(X.pmass)) { snprintf(err, errlen, "bad null histogram fit, pmass is nan"); return 31; }
+  // tail by mass, then the tail fit and the survival table on the device
+  // (src/covariation.c:1914-1973)
+  X.newmass = covh_SetTailByMass(h, X.pmass);
+  X.mu = h->phi;
+  if (p->doexpfit) {
+    double n = 0.0, sk = 0.0;
+    for (int b = h->cmin; b <= h->imax; b++) { n += (double)h->obs[b]; sk += (double)(b - h->cmin) * (double)h->obs[b]; }
+    if (n <= 0) { snprintf(err, errlen, "could not do exponential fit"); return 32; }
+    X.lambda = (sk > 0.0) ? log(1.0 + n / sk) / h->w : INFINITY;
+  }
+  return 0;
+}
+
+void rs_tables(const covgpu_params* p, int64_t P, RsStat& X, const double* sf, covgpu_result& R, double* tq) {
+  const ESL_HISTOGRAM* h = X.h;
+  R.pmass = X.pmass; R.newmass = X.newmass; R.mu = X.mu; R.lambda = X.lambda; R.tau = X.tau;
+  R.Nt = (uint64_t)P;
+  R.sc_thresh = covh_evalue2cov(p->thresh, (double)P, X.h, X.have_sf ? sf : nullptr);
+  R.h_bmin = h->bmin; R.h_w = h->w; R.h_nb = h->nb; R.h_imin = h->imin; R.h_imax = h->imax; R.h_cmin = h->cmin;
+  R.h_n = h->n; R.h_Nc = h->Nc; R.h_No = h->No; R.h_xmin = h->xmin; R.h_xmax = h->xmax; R.h_phi = h->phi;
+  // cov2evalue tables: the tail branch's p-values tail[b] / Nc
+  double c = 0.0;
+  for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tq[b] = c; }
+  for (int b = 0; b < h->nb; b++) tq[b] /= (double)h->Nc;
+}
+
+EvalTables rs_evaltables(const covgpu_params* p, int64_t P, const RsStat& X, const double* d_sf, const double* d_tail) {
+  const ESL_HISTOGRAM* h = X.h;
+  EvalTables T;
+  T.sf = X.have_sf ? d_sf : nullptr;
+  T.ptail = d_tail;
+  T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = (double)P;
+  T.pNc = 1.0 / T.Nc;
+  T.thresh = p->thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
+  return T;
+}
+
 extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint8_t* ax, const double* wgt,
                              int ntypes, const int* covtypes, covgpu_result* results, covgpu_hit* hits, int hitcap) {
   CK(cudaSetDevice(ctx->dev));
@@ -969,17 +1090,8 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   if (wgt && (s = covgpu_set_weights(ctx, wgt))) return s;
   if (ax && (s = covgpu_set_alignment(ctx, 0, ax))) return s;
   if (!ctx->have_w) return fail(ctx, 11, "weights not set");
-  int ns = p->nshuffle;
   double fracfit = p->fracfit;
-  if (ns < 0) {   // src/R-scape.c:2449-2456
-    ns = 20;
-    if ((double)N * L < 1e3) ns = 200;
-    if (L < 50) ns = 200;
-    if (L < 40) ns = 300;
-    if (N < 4) ns = 300;
-  }
-  if ((double)N * L < 1e3) fracfit = 0.3;   // :2458-2459
-  if (N == 1) ns = 0;
+  const int ns = rs_nshuffle(p, N, L, &fracfit);
   if (ns > ctx->maxnull || ns + 1 > ctx->maxslots)
     return fail(ctx, 11, "%d null alignments need maxnull >= %d and maxslots >= %d", ns, ns, ns + 1);
   CK(cudaEventRecord(ctx->ev[0], ctx->st));
@@ -993,8 +1105,6 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   CK(cudaMemcpyAsync(mm.data(), ctx->d_mm, mm.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   if ((s = check_status(ctx))) return s;
-  auto MMn = [&](int slot, int q, int k) { return mm[((size_t)slot * ntypes + q) * 2 + k]; };
-
   const int64_t plane = (int64_t)ctx->ntiles * TPP;
   // hit buffers: hitcap per statistic
   if (hitcap > 0 && ctx->hitcap < hitcap * ntypes) {
@@ -1008,58 +1118,19 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   // survival table and the E-values phase by phase, all statistics in each
   // phase, so each phase costs one host round trip instead of one per
   // statistic.
-  struct Stat {
-    bool active = false;
-    double w = 0.0, xmin = INFINITY, xmax = -INFINITY;
-    int nbcum = 0, nb_real = 0, wbase = 0;
-    int64_t obs_off = 0, sf_off = 0, tail_off = 0;
-    ESL_HISTOGRAM* h = nullptr;
-    double pmass = 0.0, newmass = 0.0, mu = 0.0, lambda = 0.0, tau = 0.0;
-    int evals = 0;
-    bool have_sf = false;
-  };
   struct Stats {
-    Stat q[MAXOUT];
+    RsStat q[MAXOUT];
     ~Stats() { for (auto& x : q) if (x.h) covh_Destroy(x.h); }
   } S;
 
   // phase 1: width and bins from the nulls' ranges, the histograms
   int64_t obs_tot = 0;
   for (int q = 0; q < ntypes; q++) {
-    covgpu_result& R = results[q];
-    Stat& X = S.q[q];
-    R.nshuffle = ns;
-    R.minCOV = MMn(0, q, 0); R.maxCOV = MMn(0, q, 1);
-    if (N == 1) { R.status = 2; continue; }
-    // calculate_width_histo (src/R-scape.c:1353-1360) on the first null
-    double w = p->w0;
-    const double nmin = MMn(1, q, 0), nmax = MMn(1, q, 1);
-    R.null_minCOV = nmin; R.null_maxCOV = nmax;
-    if (nmax <= p->bmin) return fail(ctx, 30, "bmin %f should be larger than maxCOV %f", p->bmin, nmax);
-    const double wn = (nmax - std::max(p->bmin, nmin)) / (double)p->hpts;
-    w = std::min(w, wn);
-    if (w < p->tol) w = 0.0;
-    R.w = w;
-    if (w < 1e-20) { R.status = 1; continue; }   // src/covariation.c:348-374
-    // null histograms share bmin and w: their sum is the cumulative null
-    int nbcum = 0;
-    double xmin = INFINITY, xmax = -INFINITY;
-    for (int k = 1; k <= ns; k++) {
-      double bmax = MMn(k, q, 1) + 5 * w;
-      while (fabs(bmax - p->bmin) < p->tol) bmax += w;
-      nbcum = std::max(nbcum, bins_for(p->bmin, bmax, w));
-      xmin = std::min(xmin, std::max(MMn(k, q, 0), p->bmin + w));
-      xmax = std::max(xmax, std::max(MMn(k, q, 1), p->bmin + w));
-    }
-    double bmax_r = R.maxCOV + 5 * w;
-    while (fabs(bmax_r - p->bmin) < p->tol) bmax_r += w;
-    X.active = true;
-    X.w = w; X.xmin = xmin; X.xmax = xmax; X.nbcum = nbcum;
-    X.nb_real = bins_for(p->bmin, bmax_r, w);
-    // the window starts one bin below the smallest null score's bin
-    X.wbase = std::isfinite(xmin) ? std::max(0, (int)std::floor((xmin - p->bmin) / w) - 2) : 0;
+    RsStat& X = S.q[q];
+    if ((s = rs_width(p, N, ns, mm.data(), ntypes, q, results[q], X, ctx->err, sizeof(ctx->err)))) return s;
+    if (!X.active) continue;
     X.obs_off = obs_tot;
-    obs_tot += nbcum;
+    obs_tot += X.nbcum;
   }
   if (ctx->nbcap < obs_tot) {
     if (ctx->d_obs) cudaFree(ctx->d_obs);
@@ -1072,7 +1143,7 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   if (obs_tot > 0) {
     CK(cudaMemsetAsync(ctx->d_obs, 0, (size_t)obs_tot * sizeof(unsigned long long), ctx->st));
     for (int q = 0; q < ntypes; q++) {
-      const Stat& X = S.q[q];
+      const RsStat& X = S.q[q];
       if (!X.active) continue;
       CK(launch_hist(ctx->d_cov + ((int64_t)1 * ntypes + q) * plane, ntypes * plane, ctx->d_tiles, ctx->ntiles, L, ns,
                      p->bmin, X.w, X.nbcum, X.wbase, ctx->d_obs + X.obs_off, ctx->d_status, ctx->st));
@@ -1088,54 +1159,22 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   auto tf0 = std::chrono::steady_clock::now();
   bool any_fit = false;
   for (int q = 0; q < ntypes; q++) {
-    Stat& X = S.q[q];
+    RsStat& X = S.q[q];
     if (!X.active) continue;
-    const int nbcum = X.nbcum;
-    const uint64_t* ob = obs.data() + X.obs_off;
-    double bmax_c = p->bmin + nbcum * X.w;
-    ESL_HISTOGRAM* h = covh_Create(p->bmin, bmax_c, X.w);
-    if (!h) return fail(ctx, 5, "out of host memory");
-    X.h = h;
-    if (h->nb != nbcum) {   // guard the rounding of (bmax - bmin)/w
-      free(h->obs); h->nb = nbcum; h->obs = (uint64_t*)calloc(nbcum, sizeof(uint64_t));
-    }
-    uint64_t tot = 0;
-    int imin = nbcum, imax = -1;
-    for (int b = 0; b < nbcum; b++) {
-      h->obs[b] = ob[b]; tot += ob[b];
-      if (ob[b]) { imin = std::min(imin, b); imax = std::max(imax, b); }
-    }
-    h->n = (uint64_t)ns * (uint64_t)P; h->Nc = tot; h->No = tot;
-    h->xmin = X.xmin; h->xmax = X.xmax; h->imin = imin; h->imax = imax; h->cmin = imin;
-    if (h->nb < X.nb_real) {   // src/covariation.c:462-466
-      h->obs = (uint64_t*)realloc(h->obs, sizeof(uint64_t) * X.nb_real);
-      for (int b = h->nb; b < X.nb_real; b++) h->obs[b] = 0;
-      h->nb = X.nb_real;
-    }
-    X.pmass = covh_pmass(h, p->pmass, fracfit);
-    if (std::isnan(X.pmass)) return fail(ctx, 31, "bad null histogram fit, pmass is nan");
-    // tail by mass, then the tail fit and the survival table on the device
-    // (src/covariation.c:1914-1973)
-    X.newmass = covh_SetTailByMass(h, X.pmass);
-    if (p->doexpfit) {
-      double n = 0.0, sk = 0.0;
-      for (int b = h->cmin; b <= h->imax; b++) { n += (double)h->obs[b]; sk += (double)(b - h->cmin) * (double)h->obs[b]; }
-      if (n <= 0) return fail(ctx, 32, "could not do exponential fit");
-      X.mu = h->phi;
-      X.lambda = (sk > 0.0) ? log(1.0 + n / sk) / h->w : INFINITY;
-    } else {
+    if ((s = rs_histogram(p, fracfit, ns, P, obs.data() + X.obs_off, X, ctx->err, sizeof(ctx->err)))) return s;
+    if (!p->doexpfit) {
+      const ESL_HISTOGRAM* h = X.h;
       if (!ctx->fitw[q]) ctx->fitw[q] = fitwork_create();
       const int fs = gamma_fit_launch(ctx->fitw[q], h->obs, h->cmin, h->imax, h->bmin, h->w, h->phi, ctx->st);
       if (fs) return fail(ctx, 32, "could not do a Gamma fit (%d)", fs);
       ctx->nlaunch += 1;
-      X.mu = h->phi;
       any_fit = true;
     }
   }
   if (any_fit) {
     CK(cudaStreamSynchronize(ctx->st));
     for (int q = 0; q < ntypes; q++) {
-      Stat& X = S.q[q];
+      RsStat& X = S.q[q];
       if (!X.active || p->doexpfit) continue;
       const int fs = gamma_fit_collect(ctx->fitw[q], &X.lambda, &X.tau, &X.evals);
       if (fs) return fail(ctx, 32, "could not do a Gamma fit (%d)", fs);
@@ -1145,7 +1184,7 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   // phase 3: the survival tables on the device
   int64_t sf_tot = 0, tail_tot = 0;
   for (int q = 0; q < ntypes; q++) {
-    Stat& X = S.q[q];
+    RsStat& X = S.q[q];
     if (!X.active) continue;
     X.tail_off = tail_tot;
     tail_tot += X.h->nb;
@@ -1164,7 +1203,7 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   sfh.resize(std::max<int64_t>(sf_tot, 1));
   if (sf_tot > 0) {
     for (int q = 0; q < ntypes; q++) {
-      const Stat& X = S.q[q];
+      const RsStat& X = S.q[q];
       if (!X.have_sf) continue;
       CK(launch_survfit(X.h->cmin, X.h->nb, X.h->bmin, X.h->w, X.newmass, p->doexpfit, X.mu, X.lambda, X.tau,
                         ctx->d_sf + X.sf_off, ctx->st));
@@ -1180,38 +1219,21 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   std::vector<double>& tail = ctx->h_tail;   // every entry of each statistic is written below
   tail.resize(std::max<int64_t>(tail_tot, 1));
   for (int q = 0; q < ntypes; q++) {
-    covgpu_result& R = results[q];
-    const Stat& X = S.q[q];
+    RsStat& X = S.q[q];
     if (!X.active) continue;
-    const ESL_HISTOGRAM* h = X.h;
     if (getenv("COVGPU_DEBUG"))
       fprintf(stderr, "covgpu: type %d nb %d tail bins %d fit %.2f ms (%d evaluations) mu %g lambda %g tau %g\n",
-              covtypes[q], h->nb, h->imax - h->cmin + 1, ctx->fit_ms, X.evals, X.mu, X.lambda, X.tau);
-    R.pmass = X.pmass; R.newmass = X.newmass; R.mu = X.mu; R.lambda = X.lambda; R.tau = X.tau;
-    R.Nt = (uint64_t)P;
-    R.sc_thresh = covh_evalue2cov(p->thresh, (double)P, X.h, X.have_sf ? sfh.data() + X.sf_off : nullptr);
-    R.h_bmin = h->bmin; R.h_w = h->w; R.h_nb = h->nb; R.h_imin = h->imin; R.h_imax = h->imax; R.h_cmin = h->cmin;
-    R.h_n = h->n; R.h_Nc = h->Nc; R.h_No = h->No; R.h_xmin = h->xmin; R.h_xmax = h->xmax; R.h_phi = h->phi;
-    // cov2evalue tables: the tail branch's p-values tail[b] / Nc
-    double* tq = tail.data() + X.tail_off;
-    double c = 0.0;
-    for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tq[b] = c; }
-    for (int b = 0; b < h->nb; b++) tq[b] /= (double)h->Nc;
+              covtypes[q], X.h->nb, X.h->imax - X.h->cmin + 1, ctx->fit_ms, X.evals, X.mu, X.lambda, X.tau);
+    rs_tables(p, P, X, sfh.data() + X.sf_off, results[q], tail.data() + X.tail_off);
   }
   int nhit[MAXOUT] = {0, 0, 0, 0};
   if (tail_tot > 0) {
     CK(cudaMemcpyAsync(ctx->d_tail, tail.data(), (size_t)tail_tot * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemsetAsync(ctx->d_nhits, 0, MAXOUT * sizeof(int), ctx->st));
     for (int q = 0; q < ntypes; q++) {
-      const Stat& X = S.q[q];
+      const RsStat& X = S.q[q];
       if (!X.active) continue;
-      const ESL_HISTOGRAM* h = X.h;
-      EvalTables T;
-      T.sf = X.have_sf ? ctx->d_sf + X.sf_off : nullptr;
-      T.ptail = ctx->d_tail + X.tail_off;
-      T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = (double)P;
-      T.pNc = 1.0 / T.Nc;
-      T.thresh = p->thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
+      const EvalTables T = rs_evaltables(p, P, X, ctx->d_sf + X.sf_off, ctx->d_tail + X.tail_off);
       const size_t ho = (size_t)q * hitcap;
       CK(launch_evalue(ctx->d_cov + (int64_t)q * plane, ctx->d_tiles, ctx->ntiles, L, T, nullptr, ctx->d_nhits + q,
                        hitcap, ctx->d_hi + ho, ctx->d_hj + ho, ctx->d_hsc + ho, ctx->d_hE + ho, ctx->d_hp + ho,
@@ -1246,7 +1268,7 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   }
   if (nall > 0) CK(cudaStreamSynchronize(ctx->st));
   for (int q = 0; q < ntypes; q++) {
-    const Stat& X = S.q[q];
+    const RsStat& X = S.q[q];
     if (!X.active) continue;
     const size_t n = hoff[q + 1] - hoff[q], o = hoff[q];
     if (n > 0) {

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <vector>
 
+#include "cov_dev.cuh"
 #include "cov_fit.h"
 
 namespace covgpu {
@@ -117,14 +118,14 @@ struct FitGrid {
 // arrives at the grid barrier, then adds all block sums in block order into
 // F (shared).  False when the barrier timed out.
 __device__ bool fit_eval(const FitGrid& g, const FitPoint* pts, int npts, unsigned& phase, double* F, double* red,
-                         int* flag) {
-  const int G = gridDim.x, T = G * blockDim.x, nw = blockDim.x >> 5;
+                         int* flag, int G, int bid) {
+  const int T = G * blockDim.x, nw = blockDim.x >> 5;
   const int nitems = npts * g.nnz;
   double* part = g.part + (size_t)(phase & 1u) * kFitMaxPts * G;
   double acc[kFitMaxPts];
 #pragma unroll
   for (int q = 0; q < kFitMaxPts; q++) acc[q] = 0.0;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitems; it += T) {
+  for (int it = bid * blockDim.x + threadIdx.x; it < nitems; it += T) {
     const int q = it / g.nnz, k = it - q * g.nnz;
     const int b = g.bins[k];
     const double lo = g.w * b + g.bmin, hi = g.w * (b + 1) + g.bmin;
@@ -144,7 +145,7 @@ __device__ bool fit_eval(const FitGrid& g, const FitPoint* pts, int npts, unsign
   if (threadIdx.x < npts) {
     double t = 0.0;
     for (int i = 0; i < nw; i++) t += red[i * kFitMaxPts + threadIdx.x];
-    part[threadIdx.x * G + blockIdx.x] = t;
+    part[threadIdx.x * G + bid] = t;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -199,14 +200,15 @@ __device__ __forceinline__ void fit_set_points(FitPoint* pts, const double (*pc)
 // Phase 2, only when phase 1 did not converge in 40 rounds: Nelder-Mead from
 // the best point of phase 1, the same points a sequential Nelder-Mead
 // visits, to 1e-12 in F and 1e-9 in theta.
-__global__ void __launch_bounds__(256)
-k_gam_fit(FitGrid g, double s00, double s01) {
+// (G, bid): the blocks of the search and this block's index; a grouped
+// launch runs one search per block (G = 1)
+__device__ __forceinline__ void gam_fit_body(const FitGrid& g, double s00, double s01, int G, int bid) {
   __shared__ FitPoint pts[kFitMaxPts];
   __shared__ double F[kFitMaxPts], red[8 * kFitMaxPts], pc[kFitMaxPts][2];
   __shared__ int flag, ctl;
   {
-    const int T = gridDim.x * blockDim.x;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.nnz; k += T) {
+    const int T = G * blockDim.x;
+    for (int k = bid * blockDim.x + threadIdx.x; k < g.nnz; k += T) {
       const double x = (g.w * g.bins[k] + g.bmin) - g.mu;
       g.logx[k] = (x > 0.0) ? log(x) : 0.0;
     }
@@ -215,7 +217,7 @@ k_gam_fit(FitGrid g, double s00, double s01) {
   // no points publishes them grid-wide
   unsigned phase = 0;
   int evals = 0, status = 0;
-  if (!fit_eval(g, pts, 0, phase, F, red, &flag)) status = 2;
+  if (!fit_eval(g, pts, 0, phase, F, red, &flag, G, bid)) status = 2;
 
   // ---- phase 1: Newton ----
   // Steps below kNewtonTol in (log lambda, log tau) end the search: the
@@ -237,7 +239,7 @@ k_gam_fit(FitGrid g, double s00, double s01) {
       pc[5][0] = th0 + H; pc[5][1] = th1 + H;
     }
     fit_set_points(pts, pc, 6);
-    if (!fit_eval(g, pts, 6, phase, F, red, &flag)) { status = 2; break; }
+    if (!fit_eval(g, pts, 6, phase, F, red, &flag, G, bid)) { status = 2; break; }
     evals += 6;
     if (threadIdx.x == 0) {
       ctl = 1;
@@ -286,7 +288,7 @@ k_gam_fit(FitGrid g, double s00, double s01) {
   __syncthreads();
   if (need_nm && !status) {
     fit_set_points(pts, pc, 3);
-    if (!fit_eval(g, pts, 3, phase, F, red, &flag)) status = 2;
+    if (!fit_eval(g, pts, 3, phase, F, red, &flag, G, bid)) status = 2;
     evals += 3;
     if (threadIdx.x == 0) for (int k = 0; k < 3; k++) SF[k] = F[k];
     for (int it = 0; it < 4000 && !status; it++) {
@@ -310,7 +312,7 @@ k_gam_fit(FitGrid g, double s00, double s01) {
       __syncthreads();
       if (!ctl) break;
       fit_set_points(pts, pc, 3);
-      if (!fit_eval(g, pts, 3, phase, F, red, &flag)) { status = 2; break; }
+      if (!fit_eval(g, pts, 3, phase, F, red, &flag, G, bid)) { status = 2; break; }
       evals += 3;
       if (threadIdx.x == 0) {
         const double fr = F[0];
@@ -336,7 +338,7 @@ k_gam_fit(FitGrid g, double s00, double s01) {
       __syncthreads();
       if (ctl == 2) {
         fit_set_points(pts, pc, 2);
-        if (!fit_eval(g, pts, 2, phase, F, red, &flag)) { status = 2; break; }
+        if (!fit_eval(g, pts, 2, phase, F, red, &flag, G, bid)) { status = 2; break; }
         evals += 2;
         if (threadIdx.x == 0) {
           int nq = 0;
@@ -347,7 +349,7 @@ k_gam_fit(FitGrid g, double s00, double s01) {
       __syncthreads();
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (bid == 0 && threadIdx.x == 0) {
     double l0 = bth0, l1 = bth1;
     if (need_nm) {
       int lo = 0;
@@ -359,6 +361,19 @@ k_gam_fit(FitGrid g, double s00, double s01) {
     g.out->evals = evals;
     g.out->status = status;
   }
+}
+
+__global__ void __launch_bounds__(256)
+k_gam_fit(FitGrid g, double s00, double s01) {
+  gam_fit_body(g, s00, s01, (int)gridDim.x, (int)blockIdx.x);
+}
+
+// one search per block: fit e of the batch's fits
+__global__ void __launch_bounds__(256)
+k_gam_fit_grp(const FitGrid* __restrict__ gs, const double2* __restrict__ start) {
+  const FitGrid g = gs[blockIdx.x];
+  const double2 s0 = start[blockIdx.x];
+  gam_fit_body(g, s0.x, s0.y, 1, 0);
 }
 
 struct FitWork {
@@ -412,16 +427,13 @@ cudaError_t launch_survfit(int cmin, int nb, double bmin, double w, double mass,
   return cudaGetLastError();
 }
 
-// 0 ok, 1 empty tail, 90 CUDA error; the result is read by gamma_fit_collect
-// once the stream has passed the launch
-int gamma_fit_launch(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, double bmin, double w, double phi,
-                     cudaStream_t st) {
-  FitWork& fw = *fwp;
-  const double mu = phi;
-  // moment estimates of the start, and the non-empty tail bins
+// the start of a gamma fit (moment estimates, log lambda and log tau) and
+// the non-empty tail bins; 1 when the tail is empty
+static int fit_prepare(const uint64_t* h_obs, int cmin, int imax, double bmin, double w, double mu,
+                       std::vector<int>& bins, std::vector<double>& cnts, double* s00, double* s01) {
   double m = 0.0, v = 0.0, n = 0.0;
-  std::vector<int> bins;
-  std::vector<double> cnts;
+  bins.clear();
+  cnts.clear();
   for (int b = cmin; b <= imax; b++) {
     const double mid = (w * b + bmin) + 0.5 * w - mu;
     n += (double)h_obs[b]; m += (double)h_obs[b] * mid;
@@ -435,6 +447,21 @@ int gamma_fit_launch(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, do
   }
   v /= n;
   if (!(v > 0.0) || !(m > 0.0)) { v = w * w; if (!(m > 0.0)) m = w; }
+  *s00 = std::log(m / v);
+  *s01 = std::log(m * m / v);
+  return 0;
+}
+
+// 0 ok, 1 empty tail, 90 CUDA error; the result is read by gamma_fit_collect
+// once the stream has passed the launch
+int gamma_fit_launch(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, double bmin, double w, double phi,
+                     cudaStream_t st) {
+  FitWork& fw = *fwp;
+  const double mu = phi;
+  std::vector<int> bins;
+  std::vector<double> cnts;
+  double s00 = 0.0, s01 = 0.0;
+  if (fit_prepare(h_obs, cmin, imax, bmin, w, mu, bins, cnts, &s00, &s01)) return 1;
 
   if (!fw.max_grid) {
     int dev = 0, nsm = 0, occ = 0, coop = 0;
@@ -471,7 +498,6 @@ int gamma_fit_launch(FitWork* fwp, const uint64_t* h_obs, int cmin, int imax, do
   g.bins = fw.d_bins; g.cnts = fw.d_cnts; g.logx = fw.d_logx; g.nnz = nnz;
   g.bmin = bmin; g.w = w; g.mu = mu;
   g.part = fw.d_part; g.bar = fw.d_bar; g.out = fw.d_out;
-  double s00 = std::log(m / v), s01 = std::log(m * m / v);
   void* args[] = {&g, &s00, &s01};
   // one warp per SM until every SM has one, then up to 8 warps per block
   const int nitems = kFitMaxPts * nnz;
@@ -495,6 +521,149 @@ int gamma_fit_collect(FitWork* fwp, double* ret_lambda, double* ret_tau, int* re
 
 
 
+
+// ------------------------------------------------------------------------
+// a batch of gamma fits (one block per fit, every search launched at once)
+// and the survival tables of a batch of tails
+// ------------------------------------------------------------------------
+struct FitBatch {
+  int cap_fit = 0, cap_bins = 0;
+  FitGrid* d_grid = nullptr;
+  double2* d_start = nullptr;
+  int* d_bins = nullptr;
+  double* d_cnts = nullptr;
+  double* d_logx = nullptr;
+  double* d_part = nullptr;
+  unsigned* d_bar = nullptr;
+  FitOut* d_out = nullptr;
+  FitOut* h_out = nullptr;   // pinned
+  std::vector<int> status;   // per fit: 1 empty tail (not launched)
+  std::vector<int> slot;     // per fit: its block, or -1
+  bool inv_set = false;
+};
+
+FitBatch* fitbatch_create() { return new FitBatch(); }
+void fitbatch_destroy(FitBatch* fb) {
+  if (!fb) return;
+  void* p[] = {fb->d_grid, fb->d_start, fb->d_bins, fb->d_cnts, fb->d_logx, fb->d_part, fb->d_bar, fb->d_out};
+  for (void* x : p) if (x) cudaFree(x);
+  if (fb->h_out) cudaFreeHost(fb->h_out);
+  delete fb;
+}
+
+int gamma_fit_batch_launch(FitBatch* fb, int nfit, const FitReq* req, cudaStream_t st) {
+  fb->status.assign(nfit, 0);
+  fb->slot.assign(nfit, -1);
+  if (!fb->inv_set) {
+    double inv[64];
+    for (int k = 0; k < 64; k++) inv[k] = 1.0 / (k + 1);
+    if (cudaMemcpyToSymbol(c_inv, inv, sizeof(inv)) != cudaSuccess) return 90;
+    fb->inv_set = true;
+  }
+  std::vector<int> bins_all, bins;
+  std::vector<double> cnts_all, cnts;
+  std::vector<int> boff;
+  std::vector<double2> start;
+  int nl = 0;
+  for (int k = 0; k < nfit; k++) {
+    double s00, s01;
+    if (fit_prepare(req[k].obs, req[k].cmin, req[k].imax, req[k].bmin, req[k].w, req[k].phi, bins, cnts, &s00,
+                    &s01)) {
+      fb->status[k] = 1;
+      continue;
+    }
+    fb->slot[k] = nl++;
+    boff.push_back((int)bins_all.size());
+    bins_all.insert(bins_all.end(), bins.begin(), bins.end());
+    cnts_all.insert(cnts_all.end(), cnts.begin(), cnts.end());
+    start.push_back(make_double2(s00, s01));
+  }
+  boff.push_back((int)bins_all.size());
+  if (nl == 0) return 0;
+  const int nb = (int)bins_all.size();
+  if (fb->cap_fit < nl) {
+    void* p[] = {fb->d_grid, fb->d_start, fb->d_part, fb->d_bar, fb->d_out};
+    for (void* x : p) if (x) cudaFree(x);
+    if (fb->h_out) cudaFreeHost(fb->h_out);
+    fb->d_grid = nullptr; fb->d_start = nullptr; fb->d_part = nullptr; fb->d_bar = nullptr; fb->d_out = nullptr;
+    fb->h_out = nullptr; fb->cap_fit = 0;
+    const int cap = std::max(nl, 64);
+    if (cudaMalloc(&fb->d_grid, sizeof(FitGrid) * cap) != cudaSuccess ||
+        cudaMalloc(&fb->d_start, sizeof(double2) * cap) != cudaSuccess ||
+        cudaMalloc(&fb->d_part, sizeof(double) * 2 * kFitMaxPts * cap) != cudaSuccess ||
+        cudaMalloc(&fb->d_bar, sizeof(unsigned) * cap) != cudaSuccess ||
+        cudaMalloc(&fb->d_out, sizeof(FitOut) * cap) != cudaSuccess ||
+        cudaMallocHost(&fb->h_out, sizeof(FitOut) * cap) != cudaSuccess)
+      return 90;
+    fb->cap_fit = cap;
+  }
+  if (fb->cap_bins < nb) {
+    if (fb->d_bins) cudaFree(fb->d_bins);
+    if (fb->d_cnts) cudaFree(fb->d_cnts);
+    if (fb->d_logx) cudaFree(fb->d_logx);
+    fb->d_bins = nullptr; fb->d_cnts = nullptr; fb->d_logx = nullptr; fb->cap_bins = 0;
+    const int cap = std::max(nb, 4096);
+    if (cudaMalloc(&fb->d_bins, sizeof(int) * cap) != cudaSuccess ||
+        cudaMalloc(&fb->d_cnts, sizeof(double) * cap) != cudaSuccess ||
+        cudaMalloc(&fb->d_logx, sizeof(double) * cap) != cudaSuccess)
+      return 90;
+    fb->cap_bins = cap;
+  }
+  std::vector<FitGrid> grid(nl);
+  for (int k = 0; k < nfit; k++) {
+    const int e = fb->slot[k];
+    if (e < 0) continue;
+    FitGrid& g = grid[e];
+    g.bins = fb->d_bins + boff[e]; g.cnts = fb->d_cnts + boff[e]; g.logx = fb->d_logx + boff[e];
+    g.nnz = boff[e + 1] - boff[e];
+    g.bmin = req[k].bmin; g.w = req[k].w; g.mu = req[k].phi;
+    g.part = fb->d_part + (size_t)e * 2 * kFitMaxPts;
+    g.bar = fb->d_bar + e;
+    g.out = fb->d_out + e;
+  }
+  if (cudaMemcpyAsync(fb->d_bins, bins_all.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(fb->d_cnts, cnts_all.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(fb->d_grid, grid.data(), sizeof(FitGrid) * nl, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(fb->d_start, start.data(), sizeof(double2) * nl, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemsetAsync(fb->d_bar, 0, sizeof(unsigned) * nl, st) != cudaSuccess)
+    return 90;
+  k_gam_fit_grp<<<nl, 256, 0, st>>>(fb->d_grid, fb->d_start);
+  if (cudaGetLastError() != cudaSuccess) return 90;
+  if (cudaMemcpyAsync(fb->h_out, fb->d_out, sizeof(FitOut) * nl, cudaMemcpyDeviceToHost, st) != cudaSuccess) return 90;
+  return 0;
+}
+
+int gamma_fit_batch_collect(FitBatch* fb, int k, double* ret_lambda, double* ret_tau, int* ret_evals) {
+  if (fb->status[k]) return fb->status[k];
+  const FitOut& o = fb->h_out[fb->slot[k]];
+  if (o.status) return o.status;
+  *ret_lambda = o.lambda;
+  *ret_tau = o.tau;
+  if (ret_evals) *ret_evals = o.evals;
+  return 0;
+}
+
+__global__ void k_survfit_grp(const SurvReq* __restrict__ r, const int* __restrict__ pre, int nr) {
+  const int e = grp_find(pre, nr, (int)blockIdx.x);
+  const SurvReq& q = r[e];
+  const int b = ((int)blockIdx.x - __ldg(pre + e)) * blockDim.x + threadIdx.x;
+  if (b >= 2 * q.nb) return;
+  double v = 0.0;
+  if (b >= q.cmin) {
+    const double x = q.w * (b + 1) + q.bmin;
+    double S;
+    if (x <= q.mu) S = 1.0;
+    else if (q.doexp) S = exp(-q.lambda * (x - q.mu));
+    else S = gamma_q_dev(q.tau, q.lambda * (x - q.mu), q.lga);
+    v = q.mass * S;
+  }
+  q.sf[b] = v;
+}
+
+cudaError_t grp_survfit(const SurvReq* d_req, const int* pre, int nr, int nb, cudaStream_t st) {
+  if (nb > 0) k_survfit_grp<<<nb, 256, 0, st>>>(d_req, pre, nr);
+  return cudaGetLastError();
+}
 
 // ------------------------------------------------------------------------
 // helix aggregation of pair p-values (agg_FISHER, agg_LANCASTER,

@@ -22,6 +22,7 @@
 #include "cov_dev.cuh"
 #include "cov_df.cuh"
 #include "cov_kernels.h"
+#include "cov_batch.h"
 
 #include <algorithm>
 #include <cfloat>
@@ -65,12 +66,13 @@ __host__ __device__ __forceinline__ int exact_bin(double x, double bmin, double 
 enum CountMode { MODE_UNIT = 0, MODE_EQUAL = 1, MODE_LIMBS = 3 };
 
 template <int MODE>
-__global__ void __launch_bounds__(256, 2)
-k_count_simt(const uint8_t* __restrict__ ax, int64_t slot_stride, const float* __restrict__ limbs, int N, int Lp,
+__device__ __forceinline__ void count_simt_body(
+    const GridIdx g, const uint8_t* __restrict__ ax, int64_t slot_stride, const float* __restrict__ limbs, int N,
+    int Lp,
              const TileRC* __restrict__ tiles, int ntiles, float* __restrict__ cnt, float B, float s_hi, float s_lo) {
   __shared__ float4 ohi[32][TP];
   __shared__ float4 whj[32][TP];
-  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+  const int t = g.x, slot = g.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   const uint8_t* A = ax + (int64_t)slot * slot_stride;
   const int ty = tid >> 4, tx = tid & 15;
@@ -162,19 +164,14 @@ k_count_simt(const uint8_t* __restrict__ ax, int64_t slot_stride, const float* _
       }
   }
 }
+template <int MODE>
+__global__ void __launch_bounds__(256, 2)
+k_count_simt(const uint8_t* __restrict__ ax, int64_t slot_stride, const float* __restrict__ limbs, int N, int Lp,
+             const TileRC* __restrict__ tiles, int ntiles, float* __restrict__ cnt, float B, float s_hi, float s_lo) {
+  count_simt_body<MODE>(native_grid(), ax, slot_stride, limbs, N, Lp, tiles, ntiles, cnt, B, s_hi, s_lo);
+}
 
 // constants of the bin function, split on the host
-struct BinC {
-  float2 nbmin;    // -bmin
-  float2 invw;     // 1/w
-  float2 lo;       // bmin + w (scores are clamped up to it)
-  float  mconst;   // absolute part of the fast-path margin
-  float  absb;     // |bmin|
-  float  mscale;   // 4e-7 / w: the FP32 estimate's error per unit of |x| + |bmin|
-  int    bin_lo;   // bin of the clamp value bmin + w, from its FP64 value
-  double bmin, w;
-};
-
 static BinC make_binc(double bmin, double w) {
   auto split = [](double x) { const float h = (float)x; return make_float2(h, (float)(x - (double)h)); };
   BinC B;
@@ -306,10 +303,10 @@ __device__ __forceinline__ df cnt_df(const float* __restrict__ C, int q, int p) 
   return {C[(2 * q) * TPP + p], C[(2 * q + 1) * TPP + p]};
 }
 
-__global__ void __launch_bounds__(256)
-k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ tiles, int ntiles, int nT,
+__device__ __forceinline__ void pair_marg_body(
+    const GridIdx g, const float* __restrict__ cnt, int L, const TileRC* __restrict__ tiles, int ntiles, int nT,
             double* __restrict__ part4, double* __restrict__ partR) {
-  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+  const int t = g.x, slot = g.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   const float* C = cnt + ((int64_t)slot * ntiles + t) * 32 * TPP;
   // one buffer for the row contributions, then for the column ones
@@ -380,17 +377,23 @@ k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ til
     else       P4[(((int64_t)tr.I * nT + tr.I) * TP + line) * 4 + c4] = df_to_d(df_add(rsum, csum));
   }
 }
+__global__ void __launch_bounds__(256)
+k_pair_marg(const float* __restrict__ cnt, int L, const TileRC* __restrict__ tiles, int ntiles, int nT,
+            double* __restrict__ part4, double* __restrict__ partR) {
+  pair_marg_body(native_grid(), cnt, L, tiles, ntiles, nT, part4, partR);
+}
 
 // pm[c][x] = normalise(sum over every tile touching column c); one thread
 // per column.  pmdf is pm as a double-float; lpi[c][x] = {ln pm, 1/pm} as
 // double-floats (FP64 log and division, 0 where pm = 0) for the pair
 // statistics.  mpc[c][x] = pm[c][x] * (sum_{j>c} nseff[c][j]) feeds the CCF
 // column means (src/correlators.c:1030-1036).
-__global__ void k_pm_final(const double* __restrict__ part4, const double* __restrict__ partR, int L, int Lp, int nT,
+__device__ __forceinline__ void pm_final_body(
+    const GridIdx g, const double* __restrict__ part4, const double* __restrict__ partR, int L, int Lp, int nT,
                            double* __restrict__ pm, float2* __restrict__ pmdf, float4* __restrict__ lpi,
                            double* __restrict__ mpc, int* __restrict__ status) {
-  const int slot = blockIdx.y;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int slot = g.y;
+  const int c = g.x * blockDim.x + threadIdx.x;
   if (c >= L) return;
   const double* P = part4 + (int64_t)slot * nT * nT * TP * 4;
   const double* R = partR + (int64_t)slot * nT * nT * TP;
@@ -416,9 +419,15 @@ __global__ void k_pm_final(const double* __restrict__ part4, const double* __res
     mpc[o] = rs * m[x];
   }
 }
+__global__ void k_pm_final(const double* __restrict__ part4, const double* __restrict__ partR, int L, int Lp, int nT,
+                           double* __restrict__ pm, float2* __restrict__ pmdf, float4* __restrict__ lpi,
+                           double* __restrict__ mpc, int* __restrict__ status) {
+  pm_final_body(native_grid(), part4, partR, L, Lp, nT, pm, pmdf, lpi, mpc, status);
+}
 
-__global__ void k_meanp(const double* __restrict__ mpc, int L, int Lp, double* __restrict__ meanp) {
-  const int slot = blockIdx.x;
+__device__ __forceinline__ void meanp_body(
+    const GridIdx g, const double* __restrict__ mpc, int L, int Lp, double* __restrict__ meanp) {
+  const int slot = g.x;
   __shared__ double buf[4][256];
   double acc[4] = {0, 0, 0, 0};
   for (int c = threadIdx.x; c < L; c += blockDim.x)
@@ -437,6 +446,9 @@ __global__ void k_meanp(const double* __restrict__ mpc, int L, int Lp, double* _
     const double s = buf[0][0] + buf[1][0] + buf[2][0] + buf[3][0];
     for (int x = 0; x < 4; x++) meanp[slot * 4 + x] = (s != 0.0) ? buf[x][0] / s : 0.25;
   }
+}
+__global__ void k_meanp(const double* __restrict__ mpc, int L, int Lp, double* __restrict__ meanp) {
+  meanp_body(native_grid(), mpc, L, Lp, meanp);
 }
 
 // ps[c][x], x over the five codes 0..4 (gap included), prior 1e-5.
@@ -708,9 +720,9 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const df (&c)[16]
 // per (column, output) its column in double-float, in a fixed order, for the
 // APC/ASC partials.
 template <unsigned CF>
-__global__ void __launch_bounds__(256, 2)
-k_stats(StatsArgs A) {
-  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+__device__ __forceinline__ void stats_body(
+    const GridIdx g, StatsArgs A) {
+  const int t = g.x, slot = g.y, tid = threadIdx.x;
   const TileRC tr = A.tiles[t];
   const float* C = A.cnt ? A.cnt + ((int64_t)slot * A.ntiles + t) * 32 * TPP : nullptr;
   const float* U = A.ucnt ? A.ucnt + ((int64_t)slot * A.ntiles + t) * 16 * TPP : nullptr;
@@ -773,6 +785,11 @@ k_stats(StatsArgs A) {
     base[q * qstride + ((int64_t)tr.I * A.nT + tr.I) * TP + line] = df_to_d(df_add(r, c));
   }
 }
+template <unsigned CF>
+__global__ void __launch_bounds__(256, 2)
+k_stats(StatsArgs A) {
+  stats_body<CF>(native_grid(), A);
+}
 
 // corr_ValidateProbs (src/correlators.c:1499-1545) for the pair
 // probabilities pp = (1e-10 + C) / (16e-10 + nseff) of one alignment, from
@@ -813,11 +830,12 @@ __device__ __forceinline__ df tile_get(const float2* cov, const int* tile_index,
   return ld_df(cov + (int64_t)t * TPP + (i % TP) * TP + (j % TP));
 }
 
-__global__ void __launch_bounds__(256)
-k_rafs(const float2* __restrict__ raf, float2* __restrict__ out, int64_t slot_stride_in, int64_t slot_stride_out,
+__device__ __forceinline__ void rafs_body(
+    const GridIdx g, const float2* __restrict__ raf, float2* __restrict__ out, int64_t slot_stride_in,
+    int64_t slot_stride_out,
        const TileRC* __restrict__ tiles, const int* __restrict__ tile_index, int ntiles, int nT, int L,
        double* __restrict__ part1, int64_t part_stride) {
-  const int t = blockIdx.x, slot = blockIdx.y, tid = threadIdx.x;
+  const int t = g.x, slot = g.y, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   const float2* B = raf + slot * slot_stride_in;
   df v[4][1];
@@ -838,13 +856,21 @@ k_rafs(const float2* __restrict__ raf, float2* __restrict__ out, int64_t slot_st
   }
   tile_rowcol_store<1>(v, part1 + slot * part_stride, nT, tr.I, tr.J);
 }
+__global__ void __launch_bounds__(256)
+k_rafs(const float2* __restrict__ raf, float2* __restrict__ out, int64_t slot_stride_in, int64_t slot_stride_out,
+       const TileRC* __restrict__ tiles, const int* __restrict__ tile_index, int ntiles, int nT, int L,
+       double* __restrict__ part1, int64_t part_stride) {
+  rafs_body(native_grid(), raf, out, slot_stride_in, slot_stride_out, tiles, tile_index, ntiles, nT, L, part1,
+                           part_stride);
+}
 
 // COVx[c] = sum_{j != c} COV[c][j] / (L-1), from the tile partials
-__global__ void k_apc_colx(const double* __restrict__ part1, int nT, int L, int Lp, double* __restrict__ colx,
+__device__ __forceinline__ void apc_colx_body(
+    const GridIdx g, const double* __restrict__ part1, int nT, int L, int Lp, double* __restrict__ colx,
                            float2* __restrict__ colxf) {
-  const int sq = blockIdx.y;   // (slot, stat) flattened
+  const int sq = g.y;   // (slot, stat) flattened
   const double* P = part1 + (int64_t)sq * nT * nT * TP;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < L; c += gridDim.x * blockDim.x) {
+  for (int c = g.x * blockDim.x + threadIdx.x; c < L; c += g.gx * blockDim.x) {
     const int I = c / TP, a = c % TP;
     double s = 0.0;
     for (int K = 0; K < nT; K++) s += P[((int64_t)I * nT + K) * TP + a];
@@ -853,11 +879,16 @@ __global__ void k_apc_colx(const double* __restrict__ part1, int nT, int L, int 
     st_df(colxf + (int64_t)sq * Lp + c, df_of(x));
   }
 }
+__global__ void k_apc_colx(const double* __restrict__ part1, int nT, int L, int Lp, double* __restrict__ colx,
+                           float2* __restrict__ colxf) {
+  apc_colx_body(native_grid(), part1, nT, L, Lp, colx, colxf);
+}
 
 // avg = 2/(L(L-1)) * sum_{i<j} COV = sum_c COVx[c] / L
-__global__ void k_apc_avg(const double* __restrict__ colx, int L, int Lp, double* __restrict__ avg,
+__device__ __forceinline__ void apc_avg_body(
+    const GridIdx g, const double* __restrict__ colx, int L, int Lp, double* __restrict__ avg,
                           float4* __restrict__ apcf) {
-  const int sq = blockIdx.x;
+  const int sq = g.x;
   __shared__ double buf[256];
   double s = 0.0;
   for (int c = threadIdx.x; c < L; c += blockDim.x) s += colx[(int64_t)sq * Lp + c];
@@ -874,6 +905,10 @@ __global__ void k_apc_avg(const double* __restrict__ colx, int L, int Lp, double
     apcf[sq] = make_float4(a.hi, a.lo, ia.hi, ia.lo);
   }
 }
+__global__ void k_apc_avg(const double* __restrict__ colx, int L, int Lp, double* __restrict__ avg,
+                          float4* __restrict__ apcf) {
+  apc_avg_body(native_grid(), colx, L, Lp, avg, apcf);
+}
 
 // COV <- COV - COVx_i COVx_j / avg (APC) or COV - (COVx_i + COVx_j - avg) (ASC);
 // per-tile min/max of the corrected scores.  Double-float arithmetic.
@@ -881,11 +916,11 @@ __global__ void k_apc_avg(const double* __restrict__ colx, int L, int Lp, double
 // reduction amortised over them), two pairs per 16-byte access
 constexpr int APC_TILES = 4;
 
-__global__ void __launch_bounds__(256)
-k_apc_apply(float2* __restrict__ cov, const float2* __restrict__ colxf, const double* __restrict__ avg,
+__device__ __forceinline__ void apc_apply_body(
+    const GridIdx g, float2* __restrict__ cov, const float2* __restrict__ colxf, const double* __restrict__ avg,
             const float4* __restrict__ apcf, CorrTypes ct, const TileRC* __restrict__ tiles, int ntiles, int L, int Lp,
             double* __restrict__ tmin, double* __restrict__ tmax, int* __restrict__ status) {
-  const int sq = blockIdx.y, tid = threadIdx.x;
+  const int sq = g.y, tid = threadIdx.x;
   const int actype = ct.act[sq % ct.nout];
   const bool Anz = (avg[sq] != 0.0);
   const float4 af = apcf[sq];
@@ -898,7 +933,7 @@ k_apc_apply(float2* __restrict__ cov, const float2* __restrict__ colxf, const do
     return v;
   };
   for (int tt = 0; tt < APC_TILES; tt++) {
-    const int t = blockIdx.x * APC_TILES + tt;
+    const int t = g.x * APC_TILES + tt;
     if (t >= ntiles) break;
     const TileRC tr = tiles[t];
     float4* V = reinterpret_cast<float4*>(cov + ((int64_t)sq * ntiles + t) * TPP);
@@ -923,8 +958,14 @@ k_apc_apply(float2* __restrict__ cov, const float2* __restrict__ colxf, const do
       if (actype >= 0 && (ok0 || ok1)) V[q] = make_float4(v0.hi, v0.lo, v1.hi, v1.lo);
     }
   }
-  const int nblk = gridDim.x;
-  block_minmax_store(lo, hi, tmin + (int64_t)sq * nblk + blockIdx.x, tmax + (int64_t)sq * nblk + blockIdx.x);
+  const int nblk = g.gx;
+  block_minmax_store(lo, hi, tmin + (int64_t)sq * nblk + g.x, tmax + (int64_t)sq * nblk + g.x);
+}
+__global__ void __launch_bounds__(256)
+k_apc_apply(float2* __restrict__ cov, const float2* __restrict__ colxf, const double* __restrict__ avg,
+            const float4* __restrict__ apcf, CorrTypes ct, const TileRC* __restrict__ tiles, int ntiles, int L, int Lp,
+            double* __restrict__ tmin, double* __restrict__ tmax, int* __restrict__ status) {
+  apc_apply_body(native_grid(), cov, colxf, avg, apcf, ct, tiles, ntiles, L, Lp, tmin, tmax, status);
 }
 
 // min/max of the scores of every valid pair (before any correction)
@@ -943,9 +984,10 @@ k_tile_minmax(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, 
   block_minmax_store(lo, hi, tmin + (int64_t)sq * ntiles + t, tmax + (int64_t)sq * ntiles + t);
 }
 
-__global__ void k_reduce_minmax(const double* __restrict__ tmin, const double* __restrict__ tmax, int ntiles,
+__device__ __forceinline__ void reduce_minmax_body(
+    const GridIdx g, const double* __restrict__ tmin, const double* __restrict__ tmax, int ntiles,
                                 double* __restrict__ mm) {
-  const int sq = blockIdx.x;
+  const int sq = g.x;
   __shared__ double smin[256], smax[256];
   double lo = DBL_MAX, hi = -DBL_MAX;
   for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
@@ -962,6 +1004,10 @@ __global__ void k_reduce_minmax(const double* __restrict__ tmin, const double* _
     __syncthreads();
   }
   if (threadIdx.x == 0) { mm[sq * 2 + 0] = (smin[0] == DBL_MAX) ? INFINITY : smin[0]; mm[sq * 2 + 1] = (smax[0] == -DBL_MAX) ? -INFINITY : smax[0]; }
+}
+__global__ void k_reduce_minmax(const double* __restrict__ tmin, const double* __restrict__ tmax, int ntiles,
+                                double* __restrict__ mm) {
+  reduce_minmax_body(native_grid(), tmin, tmax, ntiles, mm);
 }
 
 // Histogram of max(COV, bmin + w) over the valid pairs of several alignments
@@ -987,17 +1033,18 @@ __device__ __forceinline__ void hist_add(df x, int i, int j, int L, const BinC& 
   else                        atomicAdd(obs + bin, 1ull);
 }
 
-__global__ void __launch_bounds__(1024)
-k_hist(const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __restrict__ tiles, int ntiles, int nslots,
+__device__ __forceinline__ void hist_body(
+    const GridIdx g, const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __restrict__ tiles,
+    int ntiles, int nslots,
        int L, BinC B, int nbcap, int wbase, int nwin, unsigned long long* __restrict__ obs, int* __restrict__ status) {
   extern __shared__ unsigned int sh[];
   for (int k = threadIdx.x; k < nwin; k += blockDim.x) sh[k] = 0u;
   __syncthreads();
-  // group vb of G = gridDim.x * R groups; its item (slot, t) advances by
+  // group vb of G = g.gx * R groups; its item (slot, t) advances by
   // G = gs ntiles + gt
   const int R = blockDim.x >> 8, tid = threadIdx.x & 255;
-  const int vb = blockIdx.x * R + (threadIdx.x >> 8);
-  const int G = gridDim.x * R, gs = G / ntiles, gt = G - gs * ntiles;
+  const int vb = g.x * R + (threadIdx.x >> 8);
+  const int G = g.gx * R, gs = G / ntiles, gt = G - gs * ntiles;
   int slot = vb / ntiles, t = vb - slot * ntiles;
   auto advance = [&](int& sl, int& tt) { tt += gt; sl += gs; if (tt >= ntiles) { tt -= ntiles; sl++; } };
   // this thread's scores of a tile: p = 2 (tid + 256 k) + h, k, h in {0, 1}
@@ -1033,6 +1080,11 @@ k_hist(const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __rest
   for (int k = threadIdx.x; k < nwin; k += blockDim.x)
     if (sh[k]) atomicAdd(obs + wbase + k, (unsigned long long)sh[k]);
 }
+__global__ void __launch_bounds__(1024)
+k_hist(const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __restrict__ tiles, int ntiles, int nslots,
+       int L, BinC B, int nbcap, int wbase, int nwin, unsigned long long* __restrict__ obs, int* __restrict__ status) {
+  hist_body(native_grid(), cov, slot_stride, tiles, ntiles, nslots, L, B, nbcap, wbase, nwin, obs, status);
+}
 
 // E-value of every pair (cov2evalue at src/covariation.c:2369-2400 with
 // Nc = 1, times the number of tests) and the compacted hit list.  The FP64
@@ -1041,11 +1093,6 @@ k_hist(const float2* __restrict__ cov, int64_t slot_stride, const TileRC* __rest
 // phi and xmax are decided on x.hi against float brackets two ulps either
 // side (FP64 only inside them), and E < thresh is compared on the bit
 // patterns (non-negative doubles order as their bits).
-struct EvalCmp {
-  float phi_dn, phi_up, xmax_dn, xmax_up;   // x.hi < dn: x < y; x.hi > up: x > y
-  long long thresh_bits;
-  int all;                                   // thresh > 1000: every pair is listed
-};
 
 __device__ __forceinline__ bool ge_df(df x, float dn, float up, double y) {
   if (x.hi > up) return true;
@@ -1053,11 +1100,12 @@ __device__ __forceinline__ bool ge_df(df x, float dn, float up, double y) {
   return df_to_d(x) >= y;
 }
 
-__global__ void __launch_bounds__(256)
-k_evalue(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L, EvalTables T, BinC B,
+__device__ __forceinline__ void evalue_body(
+    const GridIdx g, const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L,
+    EvalTables T, BinC B,
          EvalCmp K, double* __restrict__ evt, int* __restrict__ nhits, int hitcap, int* __restrict__ hi,
          int* __restrict__ hj, double* __restrict__ hsc, double* __restrict__ hE, double* __restrict__ hp) {
-  const int t = blockIdx.x, tid = threadIdx.x;
+  const int t = g.x, tid = threadIdx.x;
   const TileRC tr = tiles[t];
   const float2* V = cov + (int64_t)t * TPP;
   for (int k = 0; k < 4; k++) {
@@ -1085,6 +1133,12 @@ k_evalue(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int n
     }
     if (evt) evt[(int64_t)t * TPP + p] = E;
   }
+}
+__global__ void __launch_bounds__(256)
+k_evalue(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int ntiles, int L, EvalTables T, BinC B,
+         EvalCmp K, double* __restrict__ evt, int* __restrict__ nhits, int hitcap, int* __restrict__ hi,
+         int* __restrict__ hj, double* __restrict__ hsc, double* __restrict__ hE, double* __restrict__ hp) {
+  evalue_body(native_grid(), cov, tiles, ntiles, L, T, B, K, evt, nhits, hitcap, hi, hj, hsc, hE, hp);
 }
 
 // tile-packed -> full symmetric L x L (diagonal = diag)
@@ -1258,9 +1312,7 @@ cudaError_t launch_hist(const float2* cov, int64_t slot_stride, const TileRC* ti
   return cudaGetLastError();
 }
 
-cudaError_t launch_evalue(const float2* cov, const TileRC* tiles, int ntiles, int L, const EvalTables& T, double* evt,
-                          int* nhits, int hitcap, int* hi, int* hj, double* hsc, double* hE, double* hp,
-                          cudaStream_t st) {
+EvalCmp evalcmp_host(const EvalTables& T) {
   auto bracket = [](double y, float& dn, float& up) {
     const float f = (float)y;
     up = std::nextafter(std::nextafter(f, INFINITY), INFINITY);
@@ -1273,8 +1325,14 @@ cudaError_t launch_evalue(const float2* cov, const TileRC* tiles, int ntiles, in
   K.thresh_bits = 0;
   if (T.thresh > 0.0) std::memcpy(&K.thresh_bits, &T.thresh, sizeof(double));
   K.all = (T.thresh > 1000.0) ? 1 : 0;
-  k_evalue<<<ntiles, 256, 0, st>>>(cov, tiles, ntiles, L, T, make_binc(T.bmin, T.w), K, evt, nhits, hitcap, hi, hj,
-                                   hsc, hE, hp);
+  return K;
+}
+
+cudaError_t launch_evalue(const float2* cov, const TileRC* tiles, int ntiles, int L, const EvalTables& T, double* evt,
+                          int* nhits, int hitcap, int* hi, int* hj, double* hsc, double* hE, double* hp,
+                          cudaStream_t st) {
+  k_evalue<<<ntiles, 256, 0, st>>>(cov, tiles, ntiles, L, T, make_binc(T.bmin, T.w), evalcmp_host(T), evt, nhits,
+                                   hitcap, hi, hj, hsc, hE, hp);
   return cudaGetLastError();
 }
 
@@ -1353,6 +1411,188 @@ void make_limbs(const double* w, int N, int stride, uint16_t* lim, CountWeights*
   W->s_hi = (float)std::ldexp(1.0, -E);
   W->s_lo = 0.f;
   *wtot_q = std::ldexp((double)tot, -E);
+}
+
+// ------------------------------------------------------------------------
+// grouped launches over a batch of families (cov_batch.h): block b of a
+// grouped launch is block b - pre[f] of family f's own grid, x-major
+// ------------------------------------------------------------------------
+struct GrpLoc { int f; GridIdx g; };
+__device__ __forceinline__ GrpLoc grp_loc(const int* __restrict__ pre, int nf, int gx_of_f(const FamDev&),
+                                          const FamDev* __restrict__ F) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const int loc = (int)blockIdx.x - __ldg(pre + f), gx = gx_of_f(F[f]);
+  return GrpLoc{f, GridIdx{loc % gx, loc / gx, gx}};
+}
+__device__ __forceinline__ int gx_tiles(const FamDev& d) { return d.ntiles; }
+__device__ __forceinline__ int gx_cols128(const FamDev& d) { return (d.L + 127) / 128; }
+__device__ __forceinline__ int gx_cols256(const FamDev& d) { return (d.L + 255) / 256; }
+__device__ __forceinline__ int gx_one(const FamDev&) { return 1; }
+__device__ __forceinline__ int gx_apc(const FamDev& d) { return (d.ntiles + APC_TILES - 1) / APC_TILES; }
+
+template <bool UNIT>
+__global__ void __launch_bounds__(256, 2)
+k_count_simt_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf) {
+  const GrpLoc l = grp_loc(pre, nf, gx_tiles, F);
+  const FamDev& d = F[l.f];
+  const int64_t ss = (int64_t)d.N * d.Lp;
+  if (UNIT)
+    count_simt_body<MODE_UNIT>(l.g, d.ax, ss, nullptr, d.N, d.Lp, d.tiles, d.ntiles, d.ucnt, 1.f, 1.f, 0.f);
+  else if (d.nl == 1)
+    count_simt_body<MODE_EQUAL>(l.g, d.ax, ss, nullptr, d.N, d.Lp, d.tiles, d.ntiles, d.cnt, 1.f, d.s_hi, d.s_lo);
+  else
+    count_simt_body<MODE_LIMBS>(l.g, d.ax, ss, d.limbf, d.N, d.Lp, d.tiles, d.ntiles, d.cnt, d.B, d.s_hi, 0.f);
+}
+
+__global__ void __launch_bounds__(256)
+k_pair_marg_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf) {
+  const GrpLoc l = grp_loc(pre, nf, gx_tiles, F);
+  const FamDev& d = F[l.f];
+  pair_marg_body(l.g, d.cnt, d.L, d.tiles, d.ntiles, d.nT, d.part4, d.partR);
+}
+
+__global__ void k_pm_final_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf) {
+  const GrpLoc l = grp_loc(pre, nf, gx_cols128, F);
+  const FamDev& d = F[l.f];
+  pm_final_body(l.g, d.part4, d.partR, d.L, d.Lp, d.nT, d.pm, d.pmdf, d.lpi, d.mpc, d.status);
+}
+
+__global__ void k_meanp_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf) {
+  const GrpLoc l = grp_loc(pre, nf, gx_one, F);
+  const FamDev& d = F[l.f];
+  meanp_body(GridIdx{l.g.y, 0, 1}, d.mpc, d.L, d.Lp, d.meanp);
+}
+
+template <unsigned CF>
+__global__ void __launch_bounds__(256, 2)
+k_stats_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf) {
+  const GrpLoc l = grp_loc(pre, nf, gx_tiles, F);
+  stats_body<CF>(l.g, F[l.f].sa);
+}
+
+__global__ void __launch_bounds__(256)
+k_rafs_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf, int q) {
+  const GrpLoc l = grp_loc(pre, nf, gx_tiles, F);
+  const FamDev& d = F[l.f];
+  const int nout = d.sa.nout;
+  const int64_t plane = (int64_t)d.ntiles * TPP, pplane = (int64_t)d.nT * d.nT * TP;
+  rafs_body(l.g, d.cov2, d.cov + q * plane, plane, nout * plane, d.tiles, d.tile_index, d.ntiles, d.nT, d.L,
+            d.part1 + q * pplane, nout * pplane);
+}
+
+__global__ void k_apc_colx_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf) {
+  const GrpLoc l = grp_loc(pre, nf, gx_cols256, F);
+  const FamDev& d = F[l.f];
+  apc_colx_body(l.g, d.part1, d.nT, d.L, d.Lp, d.colx, d.colxf);
+}
+
+__global__ void k_apc_avg_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf) {
+  const GrpLoc l = grp_loc(pre, nf, gx_one, F);
+  const FamDev& d = F[l.f];
+  apc_avg_body(GridIdx{l.g.y, 0, 1}, d.colx, d.L, d.Lp, d.avg, d.apcf);
+}
+
+__global__ void __launch_bounds__(256)
+k_apc_apply_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf, CorrTypes ct) {
+  const GrpLoc l = grp_loc(pre, nf, gx_apc, F);
+  const FamDev& d = F[l.f];
+  apc_apply_body(l.g, d.cov, d.colxf, d.avg, d.apcf, ct, d.tiles, d.ntiles, d.L, d.Lp, d.tmin, d.tmax, d.status);
+}
+
+__global__ void k_reduce_minmax_grp(const FamDev* __restrict__ F, const int* __restrict__ pre, int nf) {
+  const GrpLoc l = grp_loc(pre, nf, gx_one, F);
+  const FamDev& d = F[l.f];
+  reduce_minmax_body(GridIdx{l.g.y, 0, 1}, d.tmin, d.tmax, (d.ntiles + APC_TILES - 1) / APC_TILES, d.mm);
+}
+
+// one (family, statistic) per entry of S: the nulls' scores of that
+// statistic into its histogram
+__global__ void __launch_bounds__(1024)
+k_hist_grp(const FamDev* __restrict__ F, const StatDev* __restrict__ S, const int* __restrict__ pre, int ns) {
+  const int e = grp_find(pre, ns, (int)blockIdx.x);
+  const StatDev& x = S[e];
+  const FamDev& d = F[x.fam];
+  const int gx = __ldg(pre + e + 1) - __ldg(pre + e);
+  const int64_t plane = (int64_t)d.ntiles * TPP;
+  const int nout = d.sa.nout;
+  hist_body(GridIdx{(int)blockIdx.x - __ldg(pre + e), 0, gx}, d.cov + (int64_t)(nout + x.q) * plane, nout * plane,
+            d.tiles, d.ntiles, d.nslots - 1, d.L, x.hb, x.nbcap, x.wbase, x.nwin, x.obs, d.status);
+}
+
+__global__ void __launch_bounds__(256)
+k_evalue_grp(const FamDev* __restrict__ F, const StatDev* __restrict__ S, const int* __restrict__ pre, int ns) {
+  const int e = grp_find(pre, ns, (int)blockIdx.x);
+  const StatDev& x = S[e];
+  const FamDev& d = F[x.fam];
+  const int64_t plane = (int64_t)d.ntiles * TPP;
+  evalue_body(GridIdx{(int)blockIdx.x - __ldg(pre + e), 0, d.ntiles}, d.cov + (int64_t)x.q * plane, d.tiles,
+              d.ntiles, d.L, x.T, x.hb, x.K, nullptr, x.nhits, x.hitcap, x.hi, x.hj, x.hsc, x.hE, x.hp);
+}
+
+unsigned stats_cf(unsigned mask) {
+  unsigned cf = 0;
+  if (mask & (S_GT | S_MI | S_MIr | S_MIg)) cf |= CF_G;
+  if (mask & S_CHI) cf |= CF_CHI;
+  if (mask & S_OMES) cf |= CF_OMES;
+  return cf;
+}
+int apc_blocks(int ntiles) { return (ntiles + APC_TILES - 1) / APC_TILES; }
+int hist_threads() { return 1024; }
+BinC binc_host(double bmin, double w) { return make_binc(bmin, w); }
+
+cudaError_t grp_count_simt(const FamDev* F, int nf, const int* pre, int nb, bool unit, bool limbs, cudaStream_t st) {
+  (void)limbs;
+  if (nb <= 0) return cudaSuccess;
+  if (unit) k_count_simt_grp<true><<<nb, 256, 0, st>>>(F, pre, nf);
+  else      k_count_simt_grp<false><<<nb, 256, 0, st>>>(F, pre, nf);
+  return cudaGetLastError();
+}
+
+cudaError_t grp_marginals(const FamDev* F, int nf, const int* pre_marg, int nb_marg, const int* pre_pm, int nb_pm,
+                          const int* pre_mp, int nb_mp, cudaStream_t st) {
+  if (nb_marg > 0) k_pair_marg_grp<<<nb_marg, 256, 0, st>>>(F, pre_marg, nf);
+  if (nb_pm > 0) k_pm_final_grp<<<nb_pm, 128, 0, st>>>(F, pre_pm, nf);
+  if (nb_mp > 0) k_meanp_grp<<<nb_mp, 256, 0, st>>>(F, pre_mp, nf);
+  return cudaGetLastError();
+}
+
+cudaError_t grp_stats(const FamDev* F, int nf, const int* pre, int nb, unsigned cf, cudaStream_t st) {
+  if (nb <= 0) return cudaSuccess;
+  if (cf == 0 || cf == CF_G)          k_stats_grp<CF_G><<<nb, 256, 0, st>>>(F, pre, nf);
+  else if (cf == CF_CHI)              k_stats_grp<CF_CHI><<<nb, 256, 0, st>>>(F, pre, nf);
+  else if (cf == (CF_G | CF_CHI))     k_stats_grp<CF_G | CF_CHI><<<nb, 256, 0, st>>>(F, pre, nf);
+  else                                k_stats_grp<CF_ALL><<<nb, 256, 0, st>>>(F, pre, nf);
+  return cudaGetLastError();
+}
+
+cudaError_t grp_rafs(const FamDev* F, int nf, const int* pre, int nb, int q, cudaStream_t st) {
+  if (nb > 0) k_rafs_grp<<<nb, 256, 0, st>>>(F, pre, nf, q);
+  return cudaGetLastError();
+}
+
+cudaError_t grp_apc(const FamDev* F, int nf, const int* pre_colx, int nb_colx, const int* pre_sq, int nb_sq,
+                    const int* pre_apply, int nb_apply, CorrTypes ct, cudaStream_t st) {
+  if (nb_colx > 0) k_apc_colx_grp<<<nb_colx, 256, 0, st>>>(F, pre_colx, nf);
+  if (nb_sq > 0) k_apc_avg_grp<<<nb_sq, 256, 0, st>>>(F, pre_sq, nf);
+  if (nb_apply > 0) k_apc_apply_grp<<<nb_apply, 256, 0, st>>>(F, pre_apply, nf, ct);
+  if (nb_sq > 0) k_reduce_minmax_grp<<<nb_sq, 256, 0, st>>>(F, pre_sq, nf);
+  return cudaGetLastError();
+}
+
+cudaError_t grp_hist(const FamDev* F, const StatDev* S, int ns, const int* pre, int nb, int maxwin, cudaStream_t st) {
+  if (nb <= 0) return cudaSuccess;
+  static const bool attr = [] {
+    cudaFuncSetAttribute(k_hist_grp, cudaFuncAttributeMaxDynamicSharedMemorySize, HIST_WIN * 4);
+    return true;
+  }();
+  (void)attr;
+  k_hist_grp<<<nb, 1024, (size_t)std::max(1, maxwin) * 4, st>>>(F, S, pre, ns);
+  return cudaGetLastError();
+}
+
+cudaError_t grp_evalue(const FamDev* F, const StatDev* S, int ns, const int* pre, int nb, cudaStream_t st) {
+  if (nb > 0) k_evalue_grp<<<nb, 256, 0, st>>>(F, S, pre, ns);
+  return cudaGetLastError();
 }
 
 }  // namespace covgpu

@@ -30,6 +30,18 @@ struct StatsArgs {
   float         allow[16];
 };
 
+// constants of the histogram's bin function, split on the host
+struct BinC {
+  float2 nbmin;    // -bmin
+  float2 invw;     // 1/w
+  float2 lo;       // bmin + w (scores are clamped up to it)
+  float  mconst;   // absolute part of the fast-path margin
+  float  absb;     // |bmin|
+  float  mscale;   // 4e-7 / w: the FP32 estimate's error per unit of |x| + |bmin|
+  int    bin_lo;   // bin of the clamp value bmin + w, from its FP64 value
+  double bmin, w;
+};
+
 // tables of cov2evalue for one null histogram
 struct EvalTables {
   const double* sf;         // survival fit [2*nb] or nullptr
@@ -37,6 +49,13 @@ struct EvalTables {
   double        bmin, w, phi, xmax, Nc, Nt, thresh;
   double        pNc;        // 1 / Nc
   int           nb, imin, imax;
+};
+
+// the E-value pass's comparison bounds (made on the host from EvalTables)
+struct EvalCmp {
+  float phi_dn, phi_up, xmax_dn, xmax_up;   // x.hi < dn: x < y; x.hi > up: x > y
+  long long thresh_bits;
+  int all;                                   // thresh > 1000: every pair is listed
 };
 
 // weights of the counting kernels: nl = 1 (all weights equal: count times

@@ -32,6 +32,7 @@
 // the null alignment; leaf rows go straight to the output alignment slot.
 #include "cov_dev.cuh"
 #include "cov_kernels.h"
+#include "cov_batch.h"
 
 namespace covgpu {
 
@@ -75,13 +76,14 @@ __device__ __forceinline__ uint32_t fitch_word(uint32_t a, uint32_t b) {
 }
 
 // up pass for the internal nodes of one depth
-__global__ void __launch_bounds__(256)
-k_fitch_up(const uint8_t* __restrict__ ax, int N, int Lp, const int* __restrict__ left, const int* __restrict__ right,
-           const int* __restrict__ nodes, int nn, uint64_t seed, uint32_t first_null, uint8_t* __restrict__ SR) {
+__device__ __forceinline__ void fitch_up_body(
+    const GridIdx g, const uint8_t* __restrict__ ax, int N, int Lp, const int* __restrict__ left,
+    const int* __restrict__ right, const int* __restrict__ nodes, int nn, uint64_t seed, uint32_t first_null,
+    uint8_t* __restrict__ SR) {
   const int chunks = Lp >> 4;
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int idx = g.x * blockDim.x + threadIdx.x;
   if (idx >= nn * chunks) return;
-  const int q = blockIdx.y, v = nodes[idx / chunks], c0 = (idx % chunks) << 4;
+  const int q = g.y, v = nodes[idx / chunks], c0 = (idx % chunks) << 4;
   const uint32_t nid = first_null + q;
   uint8_t* S = SR + (int64_t)q * (N - 1) * Lp;
   const uint4 a = child_sets(left[v], ax, S, Lp, c0, seed, nid);
@@ -89,27 +91,42 @@ k_fitch_up(const uint8_t* __restrict__ ax, int N, int Lp, const int* __restrict_
   *reinterpret_cast<uint4*>(S + (int64_t)v * Lp + c0) =
       make_uint4(fitch_word(a.x, b.x), fitch_word(a.y, b.y), fitch_word(a.z, b.z), fitch_word(a.w, b.w));
 }
+__global__ void __launch_bounds__(256)
+k_fitch_up(const uint8_t* __restrict__ ax, int N, int Lp, const int* __restrict__ left, const int* __restrict__ right,
+           const int* __restrict__ nodes, int nn, uint64_t seed, uint32_t first_null, uint8_t* __restrict__ SR) {
+  fitch_up_body(native_grid(), ax, N, Lp, left, right, nodes, nn, seed, first_null, SR);
+}
 
 // the root's states F[q][0][c] from its sets
-__global__ void __launch_bounds__(256)
-k_root_state(int N, int L, int Lp, uint64_t seed, uint32_t first_null, const uint8_t* __restrict__ SR,
+__device__ __forceinline__ void root_state_body(
+    const GridIdx g, int N, int L, int Lp, uint64_t seed, uint32_t first_null, const uint8_t* __restrict__ SR,
              uint8_t* __restrict__ F) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
+  const int c = g.x * blockDim.x + threadIdx.x, q = g.y;
   if (c >= L) return;
   const int64_t off = (int64_t)q * (N - 1) * Lp;
   F[off + c] = (uint8_t)choose_member(SR[off + c], seed, first_null + q, 0u, (uint32_t)c);
 }
+__global__ void __launch_bounds__(256)
+k_root_state(int N, int L, int Lp, uint64_t seed, uint32_t first_null, const uint8_t* __restrict__ SR,
+             uint8_t* __restrict__ F) {
+  root_state_body(native_grid(), N, L, Lp, seed, first_null, SR, F);
+}
 
 // the root's row of the null: its states with the columns shuffled
-__global__ void __launch_bounds__(256)
-k_root_row(int N, int L, int Lp, uint64_t seed, uint32_t first_null, const uint8_t* __restrict__ F,
+__device__ __forceinline__ void root_row_body(
+    const GridIdx g, int N, int L, int Lp, uint64_t seed, uint32_t first_null, const uint8_t* __restrict__ F,
            uint8_t* __restrict__ SR) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x, q = blockIdx.y;
+  const int c = g.x * blockDim.x + threadIdx.x, q = g.y;
   if (c >= Lp) return;
   uint32_t rk[6];
   round_keys(seed, TAG_COLPERM, first_null + q, 0, rk);
   const int64_t off = (int64_t)q * (N - 1) * Lp;
   SR[off + c] = (c < L) ? F[off + feistel_perm((uint32_t)c, feistel_hbits((uint32_t)L), (uint32_t)L, rk)] : (uint8_t)4;
+}
+__global__ void __launch_bounds__(256)
+k_root_row(int N, int L, int Lp, uint64_t seed, uint32_t first_null, const uint8_t* __restrict__ F,
+           uint8_t* __restrict__ SR) {
+  root_row_body(native_grid(), N, L, Lp, seed, first_null, F, SR);
 }
 
 // The replay of one (branch, null) item: phase 1, the child's Fitch states
@@ -206,8 +223,8 @@ __device__ __forceinline__ unsigned pick5(const unsigned (&m)[5], int k) {
 
 // one warp per item, eight items per CTA (SROW: Lp bytes of row per warp)
 template <bool SROW>
-__global__ void __launch_bounds__(256)
-k_replay_warp(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
+__device__ __forceinline__ void replay_warp_body(
+    const GridIdx g, const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
               const int* __restrict__ right, const int* __restrict__ nodes, int nn, uint64_t seed,
               uint32_t first_null, uint8_t* __restrict__ F, uint8_t* __restrict__ SR, uint8_t* __restrict__ out_ax,
               int64_t out_slot_stride) {
@@ -215,9 +232,9 @@ k_replay_warp(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* _
   __shared__ int nsub_s[8][25];
   __shared__ int cum_s[8][5][6];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int item = blockIdx.x * 8 + warp;
+  const int item = g.x * 8 + warp;
   if (item >= 2 * nn) return;
-  const ReplayItem it = replay_item(ax, N, Lp, left, right, nodes, item, blockIdx.y, first_null, F, SR, out_ax,
+  const ReplayItem it = replay_item(ax, N, Lp, left, right, nodes, item, g.y, first_null, F, SR, out_ax,
                                     out_slot_stride);
   int* nsub = nsub_s[warp];
   if (lane < 25) nsub[lane] = 0;
@@ -266,11 +283,20 @@ k_replay_warp(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* _
     if (done) break;
   }
 }
+template <bool SROW>
+__global__ void __launch_bounds__(256)
+k_replay_warp(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
+              const int* __restrict__ right, const int* __restrict__ nodes, int nn, uint64_t seed,
+              uint32_t first_null, uint8_t* __restrict__ F, uint8_t* __restrict__ SR, uint8_t* __restrict__ out_ax,
+              int64_t out_slot_stride) {
+  replay_warp_body<SROW>(native_grid(), ax, N, L, Lp, left, right, nodes, nn, seed, first_null, F, SR, out_ax,
+                                        out_slot_stride);
+}
 
 // one CTA per item (SROW: Lp bytes of row)
 template <bool SROW>
-__global__ void __launch_bounds__(256)
-k_replay_cta(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
+__device__ __forceinline__ void replay_cta_body(
+    const GridIdx g, const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
              const int* __restrict__ right, const int* __restrict__ nodes, int nn, uint64_t seed,
              uint32_t first_null, uint8_t* __restrict__ F, uint8_t* __restrict__ SR, uint8_t* __restrict__ out_ax,
              int64_t out_slot_stride) {
@@ -280,9 +306,9 @@ k_replay_cta(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __
   __shared__ int gcnt[8][5];   // slots per class in each warp's group of the chunk
   __shared__ int base[5];      // slots per class before the chunk
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int item = blockIdx.x;
+  const int item = g.x;
   if (item >= 2 * nn) return;
-  const ReplayItem it = replay_item(ax, N, Lp, left, right, nodes, item, blockIdx.y, first_null, F, SR, out_ax,
+  const ReplayItem it = replay_item(ax, N, Lp, left, right, nodes, item, g.y, first_null, F, SR, out_ax,
                                     out_slot_stride);
   if (tid < 25) nsub[tid] = 0;
   __syncthreads();
@@ -337,6 +363,15 @@ k_replay_cta(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __
     for (int oc = 0; oc < 5; oc++) all = all && (base[oc] >= need[oc]);
     if (all) break;   // the same in every thread
   }
+}
+template <bool SROW>
+__global__ void __launch_bounds__(256)
+k_replay_cta(const uint8_t* __restrict__ ax, int N, int L, int Lp, const int* __restrict__ left,
+             const int* __restrict__ right, const int* __restrict__ nodes, int nn, uint64_t seed,
+             uint32_t first_null, uint8_t* __restrict__ F, uint8_t* __restrict__ SR, uint8_t* __restrict__ out_ax,
+             int64_t out_slot_stride) {
+  replay_cta_body<SROW>(native_grid(), ax, N, L, Lp, left, right, nodes, nn, seed, first_null, F, SR, out_ax,
+                                       out_slot_stride);
 }
 
 // items per level up to which the replay goes one CTA per item: measured on
@@ -450,6 +485,105 @@ cudaError_t launch_nullgen(const uint8_t* ax, int N, int L, int Lp, const NullTr
         k_replay_warp<false><<<g, 256, 0, st>>>(ax, N, L, Lp, T.left, T.right, lv, nn, seed, first_null, fitch,
                                                 scratch, out_ax, out_slot_stride);
     }
+  }
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// grouped launches over a batch of families: one tree depth of every
+// family per launch (lv[f] = {offset of the depth in lnodes, nodes at it});
+// every family's nulls use the single-family streams (null ids 0..ns-1)
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_fitch_up_grp(const FamDev* __restrict__ F, int nf, const int2* __restrict__ lv, const int* __restrict__ pre,
+               uint64_t seed) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  const int2 v = lv[f];
+  const int gx = (v.y * (d.Lp >> 4) + 255) / 256, loc = (int)blockIdx.x - __ldg(pre + f);
+  fitch_up_body(GridIdx{loc % gx, loc / gx, gx}, d.ax, d.N, d.Lp, d.left, d.right, d.lnodes + v.x, v.y, seed, 0u,
+                d.scratch);
+}
+
+__global__ void __launch_bounds__(256)
+k_root_state_grp(const FamDev* __restrict__ F, int nf, const int* __restrict__ pre, uint64_t seed) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  const int gx = (d.L + 255) / 256, loc = (int)blockIdx.x - __ldg(pre + f);
+  root_state_body(GridIdx{loc % gx, loc / gx, gx}, d.N, d.L, d.Lp, seed, 0u, d.scratch, d.fitch);
+}
+
+__global__ void __launch_bounds__(256)
+k_root_row_grp(const FamDev* __restrict__ F, int nf, const int* __restrict__ pre, uint64_t seed) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  const int gx = (d.Lp + 255) / 256, loc = (int)blockIdx.x - __ldg(pre + f);
+  root_row_body(GridIdx{loc % gx, loc / gx, gx}, d.N, d.L, d.Lp, seed, 0u, d.fitch, d.scratch);
+}
+
+template <bool SROW>
+__global__ void __launch_bounds__(256)
+k_replay_warp_grp(const FamDev* __restrict__ F, int nf, const int2* __restrict__ lv, const int* __restrict__ pre,
+                  uint64_t seed) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  const int2 v = lv[f];
+  const int gx = (2 * v.y + 7) / 8, loc = (int)blockIdx.x - __ldg(pre + f);
+  const int64_t ss = (int64_t)d.N * d.Lp;
+  replay_warp_body<SROW>(GridIdx{loc % gx, loc / gx, gx}, d.ax, d.N, d.L, d.Lp, d.left, d.right, d.lnodes + v.x, v.y,
+                         seed, 0u, d.fitch, d.scratch, d.ax + ss, ss);
+}
+
+template <bool SROW>
+__global__ void __launch_bounds__(256)
+k_replay_cta_grp(const FamDev* __restrict__ F, int nf, const int2* __restrict__ lv, const int* __restrict__ pre,
+                 uint64_t seed) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  const int2 v = lv[f];
+  const int gx = 2 * v.y, loc = (int)blockIdx.x - __ldg(pre + f);
+  const int64_t ss = (int64_t)d.N * d.Lp;
+  replay_cta_body<SROW>(GridIdx{loc % gx, loc / gx, gx}, d.ax, d.N, d.L, d.Lp, d.left, d.right, d.lnodes + v.x, v.y,
+                        seed, 0u, d.fitch, d.scratch, d.ax + ss, ss);
+}
+
+bool replay_uses_cta(int nn, int nnull) { return (int64_t)2 * nn * nnull <= kReplayCtaItems; }
+int replay_smem_max() {
+  static const int lim = [] {
+    const int l = replay_smem_limit();
+    if (l > 48 * 1024 &&
+        (cudaFuncSetAttribute(k_replay_warp_grp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, l) != cudaSuccess ||
+         cudaFuncSetAttribute(k_replay_cta_grp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, l) != cudaSuccess))
+      return 48 * 1024;
+    return l;
+  }();
+  return lim;
+}
+
+cudaError_t grp_fitch_up(const FamDev* F, int nf, const int2* lv, const int* pre, int nb, uint64_t seed,
+                         cudaStream_t st) {
+  if (nb > 0) k_fitch_up_grp<<<nb, 256, 0, st>>>(F, nf, lv, pre, seed);
+  return cudaGetLastError();
+}
+
+cudaError_t grp_root(const FamDev* F, int nf, const int* pre_state, int nb_state, const int* pre_row, int nb_row,
+                     uint64_t seed, cudaStream_t st) {
+  if (nb_state > 0) k_root_state_grp<<<nb_state, 256, 0, st>>>(F, nf, pre_state, seed);
+  if (nb_row > 0) k_root_row_grp<<<nb_row, 256, 0, st>>>(F, nf, pre_row, seed);
+  return cudaGetLastError();
+}
+
+// srow: every family of the launch has its rows staged in shared memory
+// (maxLp bytes per item)
+cudaError_t grp_replay(const FamDev* F, int nf, const int2* lv, const int* pre, int nb, bool cta, bool srow,
+                       int maxLp, uint64_t seed, cudaStream_t st) {
+  if (nb <= 0) return cudaSuccess;
+  if (cta) {
+    if (srow) k_replay_cta_grp<true><<<nb, 256, (size_t)maxLp, st>>>(F, nf, lv, pre, seed);
+    else      k_replay_cta_grp<false><<<nb, 256, 0, st>>>(F, nf, lv, pre, seed);
+  } else {
+    if (srow) k_replay_warp_grp<true><<<nb, 256, (size_t)8 * maxLp, st>>>(F, nf, lv, pre, seed);
+    else      k_replay_warp_grp<false><<<nb, 256, 0, st>>>(F, nf, lv, pre, seed);
   }
   return cudaGetLastError();
 }

@@ -38,13 +38,15 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "cov_dev.cuh"
 #include "cov_prep.h"
+#include "cov_batch.h"
 
 namespace covgpu {
 
-__global__ void __launch_bounds__(256)
-k_pb_colinv(const uint8_t* __restrict__ ax, int N, int L, int Lp, double* __restrict__ inv) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void pb_colinv_body(
+    const GridIdx g, const uint8_t* __restrict__ ax, int N, int L, int Lp, double* __restrict__ inv) {
+  const int c = g.x * blockDim.x + threadIdx.x;
   if (c >= L) return;
   int cnt[4] = {0, 0, 0, 0};
   for (int s = 0; s < N; s++) {
@@ -56,11 +58,16 @@ k_pb_colinv(const uint8_t* __restrict__ ax, int N, int L, int Lp, double* __rest
   for (int x = 0; x < 4; x++)
     inv[(int64_t)c * 4 + x] = (types > 0 && cnt[x] > 0) ? 1.0 / ((double)types * (double)cnt[x]) : 0.0;
 }
-
 __global__ void __launch_bounds__(256)
-k_pb_rows(const uint8_t* __restrict__ ax, int L, int Lp, const double* __restrict__ inv, double* __restrict__ w) {
+k_pb_colinv(const uint8_t* __restrict__ ax, int N, int L, int Lp, double* __restrict__ inv) {
+  pb_colinv_body(native_grid(), ax, N, L, Lp, inv);
+}
+
+__device__ __forceinline__ void pb_rows_body(
+    const GridIdx g, const uint8_t* __restrict__ ax, int L, int Lp, const double* __restrict__ inv,
+    double* __restrict__ w) {
   __shared__ double red[8];
-  const int s = blockIdx.x;
+  const int s = g.x;
   const uint8_t* row = ax + (int64_t)s * Lp;
   double acc = 0.0;
   for (int c = threadIdx.x; c < L; c += blockDim.x) {
@@ -75,6 +82,10 @@ k_pb_rows(const uint8_t* __restrict__ ax, int L, int Lp, const double* __restric
     for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += red[i];
     w[s] = t;
   }
+}
+__global__ void __launch_bounds__(256)
+k_pb_rows(const uint8_t* __restrict__ ax, int L, int Lp, const double* __restrict__ inv, double* __restrict__ w) {
+  pb_rows_body(native_grid(), ax, L, Lp, inv, w);
 }
 
 __global__ void __launch_bounds__(256)
@@ -92,11 +103,11 @@ k_gapfilter(const uint8_t* __restrict__ ax, const double* __restrict__ wgt, int 
   useme[c] = (r > 0.0 && r / tot >= idthresh) ? 1 : 0;
 }
 
-__global__ void __launch_bounds__(256)
-k_gsc_codes(const uint8_t* __restrict__ ax, int N, int L, int Lp, int Lw, uint32_t* __restrict__ ra,
+__device__ __forceinline__ void gsc_codes_body(
+    const GridIdx g, const uint8_t* __restrict__ ax, int N, int L, int Lp, int Lw, uint32_t* __restrict__ ra,
             uint32_t* __restrict__ rb, int* __restrict__ len) {
   __shared__ int red[8];
-  const int s = blockIdx.x;
+  const int s = g.x;
   int n = 0;
   for (int w = threadIdx.x; w < Lw; w += blockDim.x) {
     uint32_t va = 0, vb = 0;
@@ -121,13 +132,18 @@ k_gsc_codes(const uint8_t* __restrict__ ax, int N, int L, int Lp, int Lw, uint32
     len[s] = t;
   }
 }
-
-// D[a][b] for the 32 x 32 tile (blockIdx.y, blockIdx.x), a < b
 __global__ void __launch_bounds__(256)
-k_gsc_ident(const uint32_t* __restrict__ ra, const uint32_t* __restrict__ rb, const int* __restrict__ len, int N,
-            int Lw, double* __restrict__ D) {
+k_gsc_codes(const uint8_t* __restrict__ ax, int N, int L, int Lp, int Lw, uint32_t* __restrict__ ra,
+            uint32_t* __restrict__ rb, int* __restrict__ len) {
+  gsc_codes_body(native_grid(), ax, N, L, Lp, Lw, ra, rb, len);
+}
+
+// D[a][b] for the 32 x 32 tile (g.y, g.x), a < b
+__device__ __forceinline__ void gsc_ident_body(
+    const GridIdx g, const uint32_t* __restrict__ ra, const uint32_t* __restrict__ rb, const int* __restrict__ len,
+    int N, int Lw, double* __restrict__ D) {
   __shared__ uint32_t sa[32][33], sb[32][33];
-  const int A0 = blockIdx.y * 32, B0 = blockIdx.x * 32;
+  const int A0 = g.y * 32, B0 = g.x * 32;
   if (B0 + 31 < A0) return;   // tile entirely below the diagonal
   const int tid = threadIdx.x, ty = tid >> 5, tx = tid & 31;
   int cnt[4] = {0, 0, 0, 0};
@@ -157,6 +173,11 @@ k_gsc_ident(const uint32_t* __restrict__ ra, const uint32_t* __restrict__ rb, co
       D[(int64_t)b * N + a] = d;
     }
   }
+}
+__global__ void __launch_bounds__(256)
+k_gsc_ident(const uint32_t* __restrict__ ra, const uint32_t* __restrict__ rb, const int* __restrict__ len, int N,
+            int Lw, double* __restrict__ D) {
+  gsc_ident_body(native_grid(), ra, rb, len, N, Lw, D);
 }
 
 struct GscBest { double d; int a, b; };
@@ -274,36 +295,35 @@ __device__ __forceinline__ bool key_better(unsigned long long k, int a, int b, u
 }
 
 // all N-1 UPGMA merges in one CTA of 1024 threads.  The clusters' state
-// (liveness, sizes, heights, leaf labels, weights) sits in shared memory,
+// (liveness, sizes, heights, weight sums, leaf labels, weights) sits in
+// shared memory,
 // the distances in global memory (L2-resident).  Each live row a keeps its
 // closest live column b > a (ties to the smaller b), so the closest pair is
 // the best row minimum in (d, a, b) order -- the same pair as a full scan.
 // A merge of (ba, bb) changes row ba, column ba of the rows above it and
 // kills column bb; only rows whose cached minimum pointed at ba or bb, and
 // row ba, are rescanned (one warp per row).  The weight split and the
-// distance update are the FP64 operations of k_gsc_merge, in the same order.
-__global__ void __launch_bounds__(1024)
-k_gsc_upgma(double* __restrict__ D, int N, double* __restrict__ w_out) {
+// distance update are the FP64 operations of k_gsc_upgma_grid, and each
+// cluster's weight sum is kept as that kernel keeps it ((ta + bla) + (tb +
+// blb) at a merge), so both kernels give the same weights.
+__device__ __forceinline__ void gsc_upgma_body(double* __restrict__ D, int N, double* __restrict__ w_out) {
   extern __shared__ __align__(16) unsigned char gsm[];
   unsigned long long* rkey = reinterpret_cast<unsigned long long*>(gsm);
   double* height = reinterpret_cast<double*>(rkey + N);
   double* w = height + N;
-  int* rarg = reinterpret_cast<int*>(w + N);
+  double* cw = w + N;
+  int* rarg = reinterpret_cast<int*>(cw + N);
   int* size = rarg + N;
   int* cl = size + N;
   int* resc = cl + N;
   unsigned char* alive = reinterpret_cast<unsigned char*>(resc + N);
   __shared__ GscKey wb[32];
   __shared__ GscKey best;
-  __shared__ double rtot[2][32];
-  __shared__ int rcnt[2][32];
-  __shared__ double tot[2];
-  __shared__ int cnt[2];
   __shared__ int nresc;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const unsigned long long NONE = ~0ull;
   for (int s = tid; s < N; s += blockDim.x) {
-    alive[s] = 1; size[s] = 1; height[s] = 0.0; cl[s] = s; w[s] = 0.0;
+    alive[s] = 1; size[s] = 1; height[s] = 0.0; cl[s] = s; w[s] = 0.0; cw[s] = 0.0;
   }
   __syncthreads();
   // the best live column b > a of row a (warp-wide; 8 loads in flight per
@@ -357,33 +377,16 @@ k_gsc_upgma(double* __restrict__ D, int N, double* __restrict__ w_out) {
     const int ba = best.a, bb = best.b;
     if (best.k == NONE || ba >= N || bb >= N) break;   // no pair left with a distance
     const double h = __longlong_as_double((long long)best.k) / 2.0;
-    // the leaves of each side: their weight sums and counts
-    double ta = 0.0, tb = 0.0;
-    int ca = 0, cb = 0;
-    for (int l = tid; l < N; l += blockDim.x) {
-      if (cl[l] == ba) { ta += w[l]; ca++; }
-      else if (cl[l] == bb) { tb += w[l]; cb++; }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      ta += __shfl_xor_sync(0xffffffffu, ta, o); tb += __shfl_xor_sync(0xffffffffu, tb, o);
-      ca += __shfl_xor_sync(0xffffffffu, ca, o); cb += __shfl_xor_sync(0xffffffffu, cb, o);
-    }
-    if (lane == 0) { rtot[0][warp] = ta; rtot[1][warp] = tb; rcnt[0][warp] = ca; rcnt[1][warp] = cb; }
-    __syncthreads();
-    if (tid == 0) {
-      double x = 0.0, y = 0.0;
-      int mm = 0, n = 0;
-      for (int i = 0; i < nwarps; i++) { x += rtot[0][i]; y += rtot[1][i]; mm += rcnt[0][i]; n += rcnt[1][i]; }
-      tot[0] = x; tot[1] = y; cnt[0] = mm; cnt[1] = n;
-    }
-    __syncthreads();
+    // the leaves of each side share the side's new branch in proportion to
+    // their weights (equally while the side's weight sum is 0)
+    const double ta = cw[ba], tb = cw[bb];
     double bla = h - height[ba], blb = h - height[bb];
     if (bla < 0.0) bla = 0.0;
     if (blb < 0.0) blb = 0.0;
     const int sa = size[ba], sb = size[bb];
     for (int l = tid; l < N; l += blockDim.x) {
-      if (cl[l] == ba) w[l] += (tot[0] > 0.0) ? __ddiv_rn(__dmul_rn(bla, w[l]), tot[0]) : bla / (double)cnt[0];
-      else if (cl[l] == bb) w[l] += (tot[1] > 0.0) ? __ddiv_rn(__dmul_rn(blb, w[l]), tot[1]) : blb / (double)cnt[1];
+      if (cl[l] == ba) w[l] += (ta > 0.0) ? __ddiv_rn(__dmul_rn(bla, w[l]), ta) : bla / (double)sa;
+      else if (cl[l] == bb) w[l] += (tb > 0.0) ? __ddiv_rn(__dmul_rn(blb, w[l]), tb) : blb / (double)sb;
     }
     for (int c = tid; c < N; c += blockDim.x) {
       if (alive[c] && c != ba && c != bb) {
@@ -405,7 +408,7 @@ k_gsc_upgma(double* __restrict__ D, int N, double* __restrict__ w_out) {
     for (int l = tid; l < N; l += blockDim.x)
       if (cl[l] == bb) cl[l] = ba;
     if (tid == 0) {
-      size[ba] = sa + sb; height[ba] = h; alive[bb] = 0;
+      size[ba] = sa + sb; height[ba] = h; cw[ba] = (ta + bla) + (tb + blb); alive[bb] = 0;
       resc[atomicAdd(&nresc, 1)] = ba;
     }
     __syncthreads();
@@ -413,6 +416,10 @@ k_gsc_upgma(double* __restrict__ D, int N, double* __restrict__ w_out) {
     __syncthreads();
   }
   for (int s = tid; s < N; s += blockDim.x) w_out[s] = w[s];
+}
+__global__ void __launch_bounds__(1024)
+k_gsc_upgma(double* __restrict__ D, int N, double* __restrict__ w_out) {
+  gsc_upgma_body(D, N, w_out);
 }
 
 // ------------------------------------------------------------------------
@@ -640,7 +647,7 @@ static size_t gsc_grid_smem(int N, int G) {
 }
 
 // shared memory of k_gsc_upgma for N sequences
-static size_t gsc_upgma_smem(int N) { return (size_t)N * (3 * sizeof(double) + 4 * sizeof(int) + 1) + 16; }
+static size_t gsc_upgma_smem(int N) { return (size_t)N * (4 * sizeof(double) + 4 * sizeof(int) + 1) + 16; }
 
 __global__ void k_gsc_init(int N, int* __restrict__ alive, int* __restrict__ size, double* __restrict__ height,
                            int* __restrict__ cl, double* __restrict__ w) {
@@ -735,6 +742,69 @@ cudaError_t launch_weights_pb(const uint8_t* ax, int N, int L, int Lp, double* i
 cudaError_t launch_gapfilter(const uint8_t* ax, const double* wgt, int N, int L, int Lp, double gapthresh, int* useme,
                              cudaStream_t st) {
   k_gapfilter<<<(L + 255) / 256, 256, 0, st>>>(ax, wgt, N, L, Lp, 1.0 - gapthresh, useme);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// grouped launches over a batch of families: position-based weights of the
+// families with pb set, GSC weights (one CTA per family for the merges) of
+// those with gsc set
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_pb_colinv_grp(const FamDev* __restrict__ F, int nf, const int* __restrict__ pre) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  pb_colinv_body(GridIdx{(int)blockIdx.x - __ldg(pre + f), 0, (d.L + 255) / 256}, d.ax, d.N, d.L, d.Lp, d.pbinv);
+}
+
+__global__ void __launch_bounds__(256)
+k_pb_rows_grp(const FamDev* __restrict__ F, int nf, const int* __restrict__ pre) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  pb_rows_body(GridIdx{(int)blockIdx.x - __ldg(pre + f), 0, d.N}, d.ax, d.L, d.Lp, d.pbinv, d.w);
+}
+
+__global__ void __launch_bounds__(256)
+k_gsc_codes_grp(const FamDev* __restrict__ F, int nf, const int* __restrict__ pre) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  gsc_codes_body(GridIdx{(int)blockIdx.x - __ldg(pre + f), 0, d.N}, d.ax, d.N, d.L, d.Lp, d.Lw, d.gra, d.grb, d.glen);
+}
+
+__global__ void __launch_bounds__(256)
+k_gsc_ident_grp(const FamDev* __restrict__ F, int nf, const int* __restrict__ pre) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  const int nt = (d.N + 31) / 32, loc = (int)blockIdx.x - __ldg(pre + f);
+  gsc_ident_body(GridIdx{loc % nt, loc / nt, nt}, d.gra, d.grb, d.glen, d.N, d.Lw, d.gD);
+}
+
+__global__ void __launch_bounds__(1024)
+k_gsc_upgma_grp(const FamDev* __restrict__ F, int nf, const int* __restrict__ pre) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  gsc_upgma_body(d.gD, d.N, d.w);
+}
+
+cudaError_t grp_weights_pb(const FamDev* F, int nf, const int* pre_col, int nb_col, const int* pre_row, int nb_row,
+                           cudaStream_t st) {
+  if (nb_col > 0) k_pb_colinv_grp<<<nb_col, 256, 0, st>>>(F, nf, pre_col);
+  if (nb_row > 0) k_pb_rows_grp<<<nb_row, 256, 0, st>>>(F, nf, pre_row);
+  return cudaGetLastError();
+}
+
+// maxN: the largest N among the GSC families (the merges' shared memory)
+cudaError_t grp_weights_gsc(const FamDev* F, int nf, const int* pre_codes, int nb_codes, const int* pre_ident,
+                            int nb_ident, const int* pre_upgma, int nb_upgma, int maxN, cudaStream_t st) {
+  if (nb_upgma <= 0) return cudaSuccess;
+  const size_t sm = gsc_upgma_smem(maxN);
+  if (sm > 200 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(k_gsc_upgma_grp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
+    return e;
+  if (nb_codes > 0) k_gsc_codes_grp<<<nb_codes, 256, 0, st>>>(F, nf, pre_codes);
+  if (nb_ident > 0) k_gsc_ident_grp<<<nb_ident, 256, 0, st>>>(F, nf, pre_ident);
+  k_gsc_upgma_grp<<<nb_upgma, 1024, sm, st>>>(F, nf, pre_upgma);
   return cudaGetLastError();
 }
 

@@ -57,6 +57,7 @@
 #include "cov_df.cuh"
 #include "cov_kernels.h"
 #include "cov_umma.h"
+#include "cov_batch.h"
 
 namespace covgpu {
 
@@ -218,19 +219,22 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint16_t op_bits(float v) { return __half_as_ushort(__float2half_rn(v)); }
 
-__global__ void __launch_bounds__(256)
-k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, int Npad, int nslots, int nl,
-            const uint16_t* __restrict__ limbs, bool unit, uint16_t* __restrict__ ops) {
+// (sb, cb, slot): the block of 64 sequences, of 32 columns, the alignment;
+// pitch: sequences per operand row; limbs: [3][lstride]
+__device__ __forceinline__ void umma_prep_body(int sb, int cb, int slot, const uint8_t* __restrict__ ax,
+                                               int64_t slot_stride, int N, int Lp, int pitch, int nslots, int nl,
+                                               const uint16_t* __restrict__ limbs, int lstride, bool unit,
+                                               uint16_t* __restrict__ ops) {
   __shared__ uint8_t cs[64][33];
   __shared__ uint16_t lb[3][64];
-  const int s0 = blockIdx.x * 64, c0 = blockIdx.y * 32, slot = blockIdx.z, tid = threadIdx.x;
+  const int s0 = sb * 64, c0 = cb * 32, tid = threadIdx.x;
   const uint8_t* A = ax + (int64_t)slot * slot_stride;
   for (int e = tid; e < 64 * 32; e += 256) {
     const int s = e / 32, c = e % 32;
     cs[s][c] = (s0 + s < N) ? A[(int64_t)(s0 + s) * Lp + c0 + c] : (uint8_t)4;
   }
   if (tid < 64)
-    for (int l = 0; l < nl; l++) lb[l][tid] = (s0 + tid < N) ? (unit ? 1 : limbs[l * Npad + s0 + tid]) : 0;
+    for (int l = 0; l < nl; l++) lb[l][tid] = (s0 + tid < N) ? (unit ? 1 : limbs[l * lstride + s0 + tid]) : 0;
   __syncthreads();
   // 128 rows (4 states x 32 columns, state-major) x 64 sequences; each
   // thread writes 8 consecutive sequences (16 bytes) of one row
@@ -250,13 +254,20 @@ k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, 
 #pragma unroll
       for (int l = 0; l < 3; l++) vb[l][k] = (on && l < nl) ? op_bits((float)lb[l][s]) : zero;
     }
-    *reinterpret_cast<uint4*>(ops + row * Npad + s0 + chunk * 8) = *reinterpret_cast<uint4*>(va);
+    *reinterpret_cast<uint4*>(ops + row * pitch + s0 + chunk * 8) = *reinterpret_cast<uint4*>(va);
 #pragma unroll
     for (int l = 0; l < 3; l++)   // compile-time limb index: the arrays stay in registers
       if (l < nl)
-        *reinterpret_cast<uint4*>(ops + ((1 + l) * rows_per_buf + row) * Npad + s0 + chunk * 8) =
+        *reinterpret_cast<uint4*>(ops + ((1 + l) * rows_per_buf + row) * pitch + s0 + chunk * 8) =
             *reinterpret_cast<uint4*>(vb[l]);
   }
+}
+
+__global__ void __launch_bounds__(256)
+k_umma_prep(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp, int Npad, int nslots, int nl,
+            const uint16_t* __restrict__ limbs, bool unit, uint16_t* __restrict__ ops) {
+  umma_prep_body(blockIdx.x, blockIdx.y, blockIdx.z, ax, slot_stride, N, Lp, Npad, nslots, nl, limbs, Npad, unit,
+                 ops);
 }
 
 // FP8 E4M3 one-hot rows [4Lp][Npad8] (1.0 = 0x38), state-major as above;
@@ -306,13 +317,19 @@ k_umma_prep8(const uint8_t* __restrict__ ax, int64_t slot_stride, int N, int Lp,
 // reads the A tile once for both, where the shared-memory bandwidth, A and B
 // read per MMA and written by TMA, bounded the one-tile form.
 // ---------------------------------------------------------------------------
-template <int NL, int STAGES, int ACC, bool F8>
+// GRP: a grouped launch over the families of a batch (fams, tpre, nfam):
+// task k is task k - tpre[f] of family f, (slot, tile in fams[f].order); the
+// operand rows, K blocks, weight scale and output rows are family f's;
+// ntiles is then the number of tasks and nslots 1
+template <int NL, int STAGES, int ACC, bool F8, bool GRP = false>
 __global__ void __launch_bounds__(192, 1)
 k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ CUtensorMap omap,
              const TileRC* __restrict__ tiles, const int* __restrict__ order, int ntiles,
              const int4* __restrict__ jpairs, int npairs, int nslots_buf,
              int nslots, int Lp, int nkb, int bbuf, float B, float s_hi, float s_lo, unsigned cellmask,
-             int* __restrict__ err) {
+             int* __restrict__ err, const UmmaFam* __restrict__ fams = nullptr, const int* __restrict__ tpre = nullptr,
+             int nfam = 0) {
+  static_assert(!(GRP && F8), "grouped launches count weighted alignments");
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   constexpr int NB = F8 ? 2 : NL;          // B tiles per stage (limbs, or the column tiles J0, J0 + 1)
   constexpr int STAGE_BYTES = TILE_BYTES * (1 + NB);
@@ -362,13 +379,26 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
       // ---- TMA producer ----
       uint32_t g = 0;
       for (int64_t task = blockIdx.x; task < ntask; task += gridDim.x) {
-        const int slot = (int)(task / nunits);
-        int I, J0;
-        if (F8) { const int4 q = jpairs[task % nunits]; I = q.x; J0 = q.y; }
-        else    { const TileRC tr = tiles[order[task % nunits]]; I = tr.I; J0 = tr.J; }
-        const int rowA = (int)((int64_t)slot * 4 * Lp + (int64_t)I * UM);
-        const int rowB = (int)((int64_t)slot * 4 * Lp + (int64_t)J0 * UN);
-        for (int kb = 0; kb < nkb; kb++, g++) {
+        int rowA, rowB, tnkb = nkb;
+        int64_t rpb = rows_per_buf;
+        if (GRP) {
+          const int f = grp_find(tpre, nfam, (int)task);
+          const UmmaFam& fm = fams[f];
+          const int loc = (int)task - tpre[f], slot = loc / fm.ntiles;
+          const TileRC tr = fm.tiles[fm.order[loc - slot * fm.ntiles]];
+          rowA = fm.row0 + slot * 4 * fm.Lp + tr.I * UM;
+          rowB = fm.row0 + slot * 4 * fm.Lp + tr.J * UN;
+          tnkb = fm.nkb;
+          rpb = fm.rows_per_buf;
+        } else {
+          const int slot = (int)(task / nunits);
+          int I, J0;
+          if (F8) { const int4 q = jpairs[task % nunits]; I = q.x; J0 = q.y; }
+          else    { const TileRC tr = tiles[order[task % nunits]]; I = tr.I; J0 = tr.J; }
+          rowA = (int)((int64_t)slot * 4 * Lp + (int64_t)I * UM);
+          rowB = (int)((int64_t)slot * 4 * Lp + (int64_t)J0 * UN);
+        }
+        for (int kb = 0; kb < tnkb; kb++, g++) {
           const int s = (int)(g % STAGES);
           const uint32_t ph = (g / STAGES) & 1u;
           if (g >= STAGES) {
@@ -383,7 +413,7 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
 #pragma unroll
           for (int l = 0; l < NB; l++)
             tma_load_2d(st + (size_t)(1 + l) * TILE_BYTES, &tmap, kb * KE,
-                        F8 ? rowB + l * UN : (int)((bbuf + l) * rows_per_buf) + rowB, &full_bar[s]);
+                        F8 ? rowB + l * UN : (int)((bbuf + l) * rpb) + rowB, &full_bar[s]);
           issued = g + 1;
         }
         if (*(volatile int*)&abort_flag) break;
@@ -409,7 +439,9 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
         if (*(volatile int*)&abort_flag) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t dacc = tmem + (uint32_t)a * ACC_COLS;
-        for (int kb = 0; kb < nkb; kb++, g++) {
+        int tnkb = nkb;
+        if (GRP) tnkb = fams[grp_find(tpre, nfam, (int)task)].nkb;
+        for (int kb = 0; kb < tnkb; kb++, g++) {
           const int s = (int)(g % STAGES);
           const uint32_t ph = (g / STAGES) & 1u;
           if (!mbar_wait(&full_bar[s], ph)) { atomicExch(err, 102); abort_flag = 1; }
@@ -450,10 +482,23 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
       __syncwarp();
       if (*(volatile int*)&abort_flag) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int slot = (int)(task / nunits);
-      int t0, t1 = -1;
-      if (F8) { const int4 q = jpairs[task % nunits]; t0 = q.z; t1 = q.w; }
-      else    { t0 = order[task % nunits]; }
+      int slot, t0, t1 = -1, tnt = ntiles;
+      float tB = B, ts_hi = s_hi, ts_lo = s_lo;
+      int64_t orow_f = 0;
+      if (GRP) {
+        const int f = grp_find(tpre, nfam, (int)task);
+        const UmmaFam& fm = fams[f];
+        const int loc = (int)task - tpre[f];
+        slot = loc / fm.ntiles;
+        t0 = fm.order[loc - slot * fm.ntiles];
+        tnt = fm.ntiles;
+        tB = fm.B; ts_hi = fm.s_hi; ts_lo = fm.s_lo;
+        orow_f = fm.orow0;
+      } else {
+        slot = (int)(task / nunits);
+        if (F8) { const int4 q = jpairs[task % nunits]; t0 = q.z; t1 = q.w; }
+        else    { t0 = order[task % nunits]; }
+      }
       const uint32_t taddr = tmem + ((uint32_t)(x * 32) << 16) + (uint32_t)a * ACC_COLS;
       // F8: cells of tile J0 (h = 0), then of J0 + 1 (h = 1)
       constexpr int NCHUNK = F8 ? 8 : 4;
@@ -480,11 +525,11 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
             vh[k] = __uint_as_float(d[0][k]);
             vl[k] = 0.f;
           } else if (NL == 1) {
-            const df c = unit_count(__uint_as_float(d[0][k]), s_hi, s_lo);
+            const df c = unit_count(__uint_as_float(d[0][k]), ts_hi, ts_lo);
             vh[k] = c.hi; vl[k] = c.lo;
           } else {
             const df c = limb_count(__uint_as_float(d[0][k]), __uint_as_float(d[NL > 1 ? 1 : 0][k]),
-                                    __uint_as_float(d[NL > 2 ? 2 : 0][k]), B, s_hi);
+                                    __uint_as_float(d[NL > 2 ? 2 : 0][k]), tB, ts_hi);
             vh[k] = c.hi; vl[k] = c.lo;
           }
         }
@@ -495,7 +540,7 @@ k_count_umma(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ C
         // F8: row block of cell (x, y) in [slot][tile][16][32]; weighted: of
         // plane h2 of cell (x, y) in [slot][tile][16][2][32]
         const int orow0 = F8 ? ((slot * ntiles + t) * 16 + x * 4 + y) * 32
-                             : ((slot * ntiles + t) * 32 + 2 * (x * 4 + y)) * 32;
+                             : (int)(orow_f + ((int64_t)(slot * tnt + t) * 32 + 2 * (x * 4 + y)) * 32);
 #pragma unroll
         for (int h2 = 0; h2 < NPL; h2++) {
           uint8_t* buf = wbuf + (nst & 1u) * 4096;
@@ -804,6 +849,76 @@ int umma_error(UmmaPlan* p) {
   cudaMemcpy(&e, p->d_err, sizeof(int), cudaMemcpyDeviceToHost);
   if (e) cudaMemset(p->d_err, 0, sizeof(int));
   return e;
+}
+
+// ------------------------------------------------------------------------
+// grouped launches over a batch of families (cov_batch.h)
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+k_umma_prep_grp(const FamDev* __restrict__ F, int nf, const int* __restrict__ pre, int pitch,
+                uint16_t* __restrict__ ops) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  const FamDev& d = F[f];
+  const int nsb = d.Npad / 64, ncb = d.Lp / 32;
+  const int loc = (int)blockIdx.x - __ldg(pre + f), sb = loc % nsb, rest = loc / nsb;
+  umma_prep_body(sb, rest % ncb, rest / ncb, d.ax, (int64_t)d.N * d.Lp, d.N, d.Lp, pitch, d.nslots, d.nl, d.limbs,
+                 d.Npad, false, ops + (int64_t)d.oprow0 * pitch);
+}
+
+cudaError_t grp_umma_prep(const FamDev* F, int nf, const int* pre, int nb, int pitch, uint16_t* ops,
+                          cudaStream_t st) {
+  if (nb > 0) k_umma_prep_grp<<<nb, 256, 0, st>>>(F, nf, pre, pitch, ops);
+  return cudaGetLastError();
+}
+
+// 0 ok, 11 the buffers exceed a tensor map's 32-bit row coordinates or the
+// device has no tensor path, 90 CUDA error
+int grp_umma_count(const UmmaFam* fams, int nf, const int* tpre, int64_t ntask, int nl, const uint16_t* ops,
+                   int pitch, int64_t rows, float* cnt_base, int64_t cnt_rows, int* err, cudaStream_t st) {
+  if (ntask <= 0) return 0;
+  if (ntask >= ((int64_t)1 << 31) || rows >= ((int64_t)1 << 31) || cnt_rows >= ((int64_t)1 << 31)) return 11;
+  if (!get_encode() || (pitch % UK) != 0 || ((uintptr_t)ops & 15u) || ((uintptr_t)cnt_base & 15u)) return 11;
+  CUtensorMap tmap, omap;
+  {
+    cuuint64_t gdim[2] = {(cuuint64_t)pitch, (cuuint64_t)rows};
+    cuuint64_t gstride[1] = {(cuuint64_t)pitch * sizeof(uint16_t)};
+    cuuint32_t box[2] = {UK, UM};
+    cuuint32_t estride[2] = {1, 1};
+    if (get_encode()(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)ops, gdim, gstride, box, estride,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return 11;
+  }
+  {
+    cuuint64_t gdim[2] = {32, (cuuint64_t)cnt_rows};
+    cuuint64_t gstride[1] = {32 * sizeof(float)};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t estride[2] = {1, 1};
+    if (get_encode()(&omap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, cnt_base, gdim, gstride, box, estride,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return 11;
+  }
+  static const int nsm = [] {
+    int dev = 0, n = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(k_count_umma<3, STAGES3, ACC3, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem_bytes(3, STAGES3));
+    cudaFuncSetAttribute(k_count_umma<1, STAGES1, ACC1, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem_bytes(1, STAGES1));
+    return n;
+  }();
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntask, nsm));
+  if (nl == 1)
+    k_count_umma<1, STAGES1, ACC1, false, true><<<grid, 192, smem_bytes(1, STAGES1), st>>>(
+        tmap, omap, nullptr, nullptr, (int)ntask, nullptr, 0, 1, 1, 0, 0, 1, 1.f, 1.f, 0.f, 0xFFFFu, err, fams,
+        tpre, nf);
+  else
+    k_count_umma<3, STAGES3, ACC3, false, true><<<grid, 192, smem_bytes(3, STAGES3), st>>>(
+        tmap, omap, nullptr, nullptr, (int)ntask, nullptr, 0, 1, 1, 0, 0, 1, 1.f, 1.f, 0.f, 0xFFFFu, err, fams,
+        tpre, nf);
+  return cudaGetLastError() == cudaSuccess ? 0 : 90;
 }
 
 }  // namespace covgpu
