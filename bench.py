@@ -205,29 +205,23 @@ def load_learned_null():
     return g._load("learned_null", os.path.join(ROOT, "r-scape_gb300", "learned_null.py"))
 
 
-def ragged_families(cg, nfam, counter, device, workers=4):
-    """E-valued MSAs/s over a stream of families drawn as the ragged-family
-    workload draws them (N ~ U[20,2000], L ~ logU[50,1500], tree length
-    ~ U[0.5,3], base-pair fraction ~ U[0.1,0.35]; seeds 1..nfam).  `workers`
-    host threads each drive one context (its own CUDA stream), made for the
-    largest size and resized per family, so small families' kernels overlap
-    on the GPU.  Per family the alignment and tree go in, R-scape's weights
-    (GSC up to 1000 sequences, else position-based) and its null count rule
-    run on the device, GTp with APC, and the hit list comes out.  Families
-    are synthesised before the timed region."""
+def ragged_per_family(cg, fams, data, counter, device, workers=4):
+    """The families run one call each (covgpu_rscape): `workers` host
+    threads each drive one context (its own CUDA stream), made for the
+    largest size and resized per family.  Per family the alignment and tree
+    go in, R-scape's weights (GSC up to 1000 sequences, else position-based)
+    and its null count rule run on the device, GTp with APC, and the hit list
+    comes out."""
     import threading
-    ln = load_learned_null()
-    fams = [ln.draw_family(k) for k in range(1, nfam + 1)]
-    data = [ln.make_family(f) for f in fams]
+    nfam = len(fams)
     engines = [cg.Engine(2000, 1500, maxslots=21, maxnull=20, device=device) for _ in range(workers)]
-    pairs = [0] * workers
     errors = []
 
     def work(k):
         e = engines[k]
         try:
             for i in range(k, nfam, workers):
-                f, (s, _) = fams[i], data[i]
+                f, s = fams[i], data[i]
                 e.resize(f["N"], f["L"])
                 e.set_alignment(0, s.ax)
                 if f["N"] <= 1000:
@@ -235,8 +229,7 @@ def ragged_families(cg, nfam, counter, device, workers=4):
                 else:
                     e.weights_pb(0, set=True)
                 e.set_tree(s.parent, s.left, s.right)
-                r = e.rscape(None, None, ["GTp"], counter=counter)[0]
-                pairs[k] += (r["nshuffle"] + 1) * f["L"] * (f["L"] - 1) // 2
+                e.rscape(None, None, ["GTp"], counter=counter)
         except Exception as err:   # reported after the join
             errors.append(err)
 
@@ -251,9 +244,46 @@ def ragged_families(cg, nfam, counter, device, workers=4):
         e.close()
     if errors:
         raise errors[0]
-    return {"families": nfam, "workers": workers, "seconds": dt, "msas_per_s": nfam / dt,
-            "column_pairs_per_s": sum(pairs) / dt, "statistic": "GTp", "nulls": "R-scape rule (20 here)",
-            "timing": "host wall clock, host buffers in/out"}
+    return {"families": nfam, "workers": workers, "seconds": dt, "msas_per_s": nfam / dt}
+
+
+def ragged_families(cg, nfam, counter, device, compare=200):
+    """E-valued MSAs/s over families drawn as the ragged-family workload
+    draws them (N ~ U[20,2000], L ~ logU[50,1500], tree length ~ U[0.5,3],
+    base-pair fraction ~ U[0.1,0.35]; seeds 1..nfam), all in one call of
+    covgpu_rscape_families: every device pass one grouped launch over the
+    families, the passes from the nulls to the corrected scores a CUDA graph.
+    Per family the alignment and tree go in, R-scape's weights (GSC up to
+    1000 sequences, else position-based) and its null count rule run on the
+    device, GTp with APC, and the hit list comes out.  Families are
+    synthesised before the timed region; one warm-up call (allocation, graph
+    capture), then the best of two timed calls.  For comparison the first
+    `compare` families also run one call each on four host threads."""
+    ln = load_learned_null()
+    fams = [ln.draw_family(k) for k in range(1, nfam + 1)]
+    data = [ln.make_family(f)[0] for f in fams]
+    fl = [dict(ax=s.ax, parent=s.parent, left=s.left, right=s.right) for s in data]
+    b = cg.Batch(device=device)
+    b.rscape(fl, ["GTp"], counter=counter)
+    ts = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        r = b.rscape(fl, ["GTp"], counter=counter)
+        ts.append(time.perf_counter() - t0)
+    dev_ms, rest_ms, host_ms, nl, nch = b.timing()
+    b.close()
+    dt = min(ts)
+    pairs = sum((x[0]["nshuffle"] + 1) * f["L"] * (f["L"] - 1) // 2 for x, f in zip(r, fams))
+    out = {"families": nfam, "seconds": dt, "msas_per_s": nfam / dt, "column_pairs_per_s": pairs / dt,
+           "statistic": "GTp", "nulls": "R-scape rule (20 here)", "counter": "tensor" if counter else "simt",
+           "mode": "grouped: one launch per pass over all families, device passes as a CUDA graph",
+           "launches": nl, "chunks": nch,
+           "device_ms": {"nulls_to_corrected_scores": dev_ms, "histograms_fits_evalues": rest_ms},
+           "timing": "host wall clock of one call, host buffers in, hit lists out; best of 2 after a warm-up call"}
+    if compare > 0:
+        k = min(compare, nfam)
+        out["per_family_calls"] = ragged_per_family(cg, fams[:k], data[:k], counter, device)
+    return out
 
 
 def batched_nulls(cg, counter, device, steps=3):
@@ -387,10 +417,12 @@ def main():
     ap.add_argument("--L", type=int, default=None, help="override L (profiling a smaller case)")
     ap.add_argument("--nshuffle", type=int, default=None, help="override the number of nulls")
     ap.add_argument("--types", default=None, help="comma-separated statistics (default GTp,MIp,CHIp,RAFp)")
-    ap.add_argument("--families", type=int, default=200,
-                    help="families of the ragged-family stream timed after the main workload (0: skip)")
-    ap.add_argument("--family-workers", type=int, default=4,
-                    help="host threads (one context and stream each) for the ragged-family stream")
+    ap.add_argument("--families", type=int, default=1000,
+                    help="families of the ragged-family batch timed after the main workload (0: skip)")
+    ap.add_argument("--once-families", type=int, default=0,
+                    help="only one call of the family batch on this many ragged families (profiler launch lists)")
+    ap.add_argument("--family-compare", type=int, default=200,
+                    help="families also run one call each on four host threads, for comparison (0: skip)")
     ap.add_argument("--no-extras", action="store_true",
                     help="only the main workload: no CPU baseline, simulator, families or batched nulls "
                          "(for profiler launch lists)")
@@ -441,6 +473,23 @@ def main():
         return
 
     cg = load_covgpu()
+    if args.once_families > 0:
+        # one call of the family batch, nothing else (for profiler launch lists)
+        ln = load_learned_null()
+        fams = [ln.draw_family(k) for k in range(1, args.once_families + 1)]
+        fl = []
+        for f in fams:
+            sf = ln.make_family(f)[0]
+            fl.append(dict(ax=sf.ax, parent=sf.parent, left=sf.left, right=sf.right))
+        b = cg.Batch()
+        t0 = time.perf_counter()
+        b.rscape(fl, ["GTp"], counter=cg.TENSOR)
+        dt = time.perf_counter() - t0
+        dev_ms, rest_ms, host_ms, nl, nch = b.timing()
+        b.close()
+        print(json.dumps({"once_families": args.once_families, "seconds": dt, "device_ms": [dev_ms, rest_ms],
+                          "launches": nl, "chunks": nch}))
+        return
     s, ax, w = workload(cg)
     N, L = ax.shape
     P = L * (L - 1) // 2
@@ -527,7 +576,7 @@ def main():
                      "pairs_e_lt_thresh": [len(x["hits"]) for x in rs]}
         cpu_v, cpu_sample, cpu_parts = cpu_reference(ax, w, args.cpu_budget, threads)
         sim = simulator_rate(cg, e, s, N, L, ns)
-        fam = ragged_families(cg, args.families, counter, local, args.family_workers) if args.families > 0 else None
+        fam = ragged_families(cg, args.families, counter, local, args.family_compare) if args.families > 0 else None
         bnull = batched_nulls(cg, counter, local)
         dflow = dropin_flow(cg, e, ax, w, ns)
     out = {

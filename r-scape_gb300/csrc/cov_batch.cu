@@ -77,6 +77,8 @@ struct Bump {
 struct covgpu_batch {
   int dev = 0;
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;  // the weights, alongside the nulls
+  cudaEvent_t fork = nullptr, join = nullptr;
   char err[512] = {0};
   size_t budget = 0;
   uint8_t* arena = nullptr;
@@ -128,6 +130,9 @@ extern "C" int covgpu_batch_create(covgpu_batch** ret, int device, double mem_gb
   *ret = b;
   BK(cudaSetDevice(device));
   BK(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+  BK(cudaStreamCreateWithFlags(&b->st2, cudaStreamNonBlocking));
+  BK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  BK(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
   for (auto& e : b->ev) BK(cudaEventCreate(&e));
   size_t fr = 0, tot = 0;
   BK(cudaMemGetInfo(&fr, &tot));
@@ -154,6 +159,9 @@ extern "C" void covgpu_batch_destroy(covgpu_batch* b) {
   for (void* x : p) if (x) cudaFree(x);
   if (b->fits) fitbatch_destroy(b->fits);
   for (auto& e : b->ev) if (e) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->st2) cudaStreamDestroy(b->st2);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }
@@ -473,45 +481,22 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
   BK(cudaMemcpyAsync(Lo.tiles, tiles_h.data(), Lo.tiles_bytes, cudaMemcpyHostToDevice, b->st));
   BK(cudaMemcpyAsync(Lo.tree, tree_h.data(), tree_h.size() * sizeof(int), cudaMemcpyHostToDevice, b->st));
 
-  // ---- weights: R-scape's rule on the device where the caller gave none ----
+  // ---- weights: the caller's, normalised and quantised here; R-scape's
+  // rule (GSC or position-based), normalised and quantised on the device
+  // inside the graph below, alongside the nulls ----
   std::vector<uint8_t> wreg(Lo.wreg_bytes, 0);
-  bool any_dev = false;
-  for (int k = 0; k < nf; k++) any_dev |= (fams[k].gsc || fams[k].pb);
-  Tab tb;
-  const size_t F_off = tb.put(Lo.F.data(), nf * sizeof(FamDev));
-  if (any_dev) {
-    Pre pcol = prefix(nf, [&](int k) { return fams[k].pb ? (fams[k].L + 255) / 256 : 0; });
-    Pre prow = prefix(nf, [&](int k) { return fams[k].pb ? fams[k].N : 0; });
-    Pre pcod = prefix(nf, [&](int k) { return fams[k].gsc ? fams[k].N : 0; });
-    Pre pid = prefix(nf, [&](int k) { const int nt = (fams[k].N + 31) / 32; return fams[k].gsc ? nt * nt : 0; });
-    Pre pup = prefix(nf, [&](int k) { return fams[k].gsc ? 1 : 0; });
-    int maxN = 1;
-    for (auto& f : fams) if (f.gsc) maxN = std::max(maxN, f.N);
-    const size_t o_col = tb.put(pcol.v.data(), pcol.v.size() * 4), o_row = tb.put(prow.v.data(), prow.v.size() * 4);
-    const size_t o_cod = tb.put(pcod.v.data(), pcod.v.size() * 4), o_id = tb.put(pid.v.data(), pid.v.size() * 4);
-    const size_t o_up = tb.put(pup.v.data(), pup.v.size() * 4);
-    if ((s = grow(b, &b->tab, &b->tab_cap, tb.h.size()))) return s;
-    BK(cudaMemcpyAsync(b->tab, tb.h.data(), tb.h.size(), cudaMemcpyHostToDevice, b->st));
-    const FamDev* dF = reinterpret_cast<const FamDev*>(b->tab + F_off);
-    auto P = [&](size_t o) { return reinterpret_cast<const int*>(b->tab + o); };
-    BK(grp_weights_pb(dF, nf, P(o_col), pcol.total(), P(o_row), prow.total(), b->st));
-    BK(grp_weights_gsc(dF, nf, P(o_cod), pcod.total(), P(o_id), pid.total(), P(o_up), pup.total(), maxN, b->st));
-    b->nlaunch += (pcol.total() ? 2 : 0) + (pup.total() ? 3 : 0);
-    BK(cudaMemcpyAsync(wreg.data(), Lo.w, Lo.wreg_bytes, cudaMemcpyDeviceToHost, b->st));
-    BK(cudaStreamSynchronize(b->st));
-  }
-  // the weights counted: normalised (R-scape's rule) or the caller's, limbs
   std::vector<double> wtot_q(nf, 0.0);
   for (int k = 0; k < nf; k++) {
     const FamHost& f = fams[k];
+    FamDev& d = Lo.F[k];
+    if (f.gsc || f.pb) {   // made on the device: three limbs
+      d.nl = 3; d.B = 0.f; d.s_hi = 0.f; d.s_lo = 0.f;
+      continue;
+    }
     double* w = reinterpret_cast<double*>(wreg.data() + Lo.w_off[k]);
     const double* src = fam_in[f.idx].wgt;
-    if (!src && f.N == 1) {
-      w[0] = 1.0;
-    } else if (f.gsc || f.pb) {
-      double sum = 0.0;
-      for (int i = 0; i < f.N; i++) sum += w[i];
-      for (int i = 0; i < f.N; i++) w[i] = (sum > 0.0) ? w[i] * (double)f.N / sum : 1.0;
+    if (!src) {   // one sequence
+      for (int i = 0; i < f.N; i++) w[i] = 1.0;
     } else {
       for (int i = 0; i < f.N; i++) {
         if (!(src[i] >= 0.0) || !std::isfinite(src[i]))
@@ -526,7 +511,6 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
     float* lf = reinterpret_cast<float*>(wreg.data() + Lo.lf_off[k]);
     for (int l = 0; l < 3; l++)
       for (int i = 0; i < f.N; i++) lf[(size_t)l * f.N + i] = (float)lim[(size_t)l * f.Npad + i];
-    FamDev& d = Lo.F[k];
     d.nl = cw.nl; d.B = cw.B; d.s_hi = cw.s_hi; d.s_lo = cw.s_lo;
   }
   BK(cudaMemcpyAsync(Lo.w, wreg.data(), Lo.wreg_bytes, cudaMemcpyHostToDevice, b->st));
@@ -541,7 +525,7 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
     A.pm = d.pm; A.pmdf = d.pmdf; A.lpi = d.lpi; A.logtab = b->d_logtab; A.meanp = d.meanp;
     A.cov = d.cov; A.part1 = d.part1; A.tiles = d.tiles;
     A.ntiles = f.ntiles; A.nT = f.nT; A.L = f.L; A.Lp = f.Lp; A.N = f.N;
-    const float hi = (float)wtot_q[k];
+    const float hi = (float)wtot_q[k];   // made on the device for R-scape's weights
     A.wtot = make_float2(hi, (float)(wtot_q[k] - (double)hi));
     A.stats = T.mask;
     int cls = p->covclass;
@@ -556,7 +540,7 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
   }
 
   // ---- the device passes from the nulls to the corrected scores ----
-  tb.h.clear();
+  Tab tb;
   const size_t oF = tb.put(Lo.F.data(), nf * sizeof(FamDev));
   int maxdepth = 0, maxLp = 32;
   for (auto& f : fams) { maxdepth = std::max(maxdepth, f.depth()); maxLp = std::max(maxLp, f.Lp); }
@@ -582,6 +566,17 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
     lvl[dd].cta = tb.put(pc.v.data(), pc.v.size() * 4); lvl[dd].ncta = pc.total();
     lvl[dd].warp = tb.put(pw.v.data(), pw.v.size() * 4); lvl[dd].nwarp = pw.total();
   }
+  Pre pcol = prefix(nf, [&](int k) { return fams[k].pb ? (fams[k].L + 255) / 256 : 0; });
+  Pre prow = prefix(nf, [&](int k) { return fams[k].pb ? fams[k].N : 0; });
+  Pre pcod = prefix(nf, [&](int k) { return fams[k].gsc ? fams[k].N : 0; });
+  Pre pid = prefix(nf, [&](int k) { const int nt = (fams[k].N + 31) / 32; return fams[k].gsc ? nt * nt : 0; });
+  Pre pup = prefix(nf, [&](int k) { return fams[k].gsc ? 1 : 0; });
+  Pre plb = prefix(nf, [&](int k) { return (fams[k].gsc || fams[k].pb) ? 1 : 0; });
+  int maxN = 1;
+  for (auto& f : fams) if (f.gsc) maxN = std::max(maxN, f.N);
+  const size_t o_col = tb.put(pcol.v.data(), pcol.v.size() * 4), o_row = tb.put(prow.v.data(), prow.v.size() * 4);
+  const size_t o_cod = tb.put(pcod.v.data(), pcod.v.size() * 4), o_id = tb.put(pid.v.data(), pid.v.size() * 4);
+  const size_t o_up = tb.put(pup.v.data(), pup.v.size() * 4), o_lb = tb.put(plb.v.data(), plb.v.size() * 4);
   Pre prs = prefix(nf, [&](int k) { return fams[k].ns > 0 ? (fams[k].L + 255) / 256 * fams[k].ns : 0; });
   Pre prr = prefix(nf, [&](int k) { return fams[k].ns > 0 ? (fams[k].Lp + 255) / 256 * fams[k].ns : 0; });
   Pre pprep = prefix(nf, [&](int k) { return fams[k].Npad / 64 * (fams[k].Lp / 32) * fams[k].nslots; });
@@ -616,6 +611,7 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
   BK(cudaMemcpyAsync(b->tab, tb.h.data(), tb.h.size(), cudaMemcpyHostToDevice, b->st));
   const FamDev* dF = reinterpret_cast<const FamDev*>(b->tab + oF);
   auto P = [&](size_t o) { return reinterpret_cast<const int*>(b->tab + o); };
+  if (pup.total() && !grp_weights_gsc_prepare()) return bfail(b, 90, "GSC kernel attributes");
 
   // the key of this chunk's device passes: the descriptor tables (they hold
   // every pointer and size the launches read) and the launch parameters
@@ -629,6 +625,19 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
   }
   int launches = 0;
   auto passes = [&]() -> int {
+    // R-scape's weights on the second stream, alongside the nulls
+    const bool wdev = plb.total() > 0;
+    if (wdev) {
+      BK(cudaEventRecord(b->fork, b->st));
+      BK(cudaStreamWaitEvent(b->st2, b->fork, 0));
+      FamDev* dFw = reinterpret_cast<FamDev*>(b->tab + oF);
+      UmmaFam* dUw = reinterpret_cast<UmmaFam*>(b->tab + o_uf);
+      BK(grp_weights_pb(dF, nf, P(o_col), pcol.total(), P(o_row), prow.total(), b->st2));
+      BK(grp_weights_gsc(dF, nf, P(o_cod), pcod.total(), P(o_id), pid.total(), P(o_up), pup.total(), maxN, b->st2));
+      BK(grp_weights_limbs(dFw, nf, P(o_lb), plb.total(), dUw, b->st2));
+      BK(cudaEventRecord(b->join, b->st2));
+      launches += (pcol.total() ? 2 : 0) + (pup.total() ? 3 : 0) + 1;
+    }
     // nulls: Fitch up the tree, the roots, the replay down it
     for (int dd = maxdepth - 1; dd >= 0; dd--)
       if (lvl[dd].nup) {
@@ -651,6 +660,7 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
         launches++;
       }
     }
+    if (wdev) BK(cudaStreamWaitEvent(b->st, b->join, 0));
     // counts and marginals
     if (T.need_w) {
       if (counter == COVGPU_COUNT_TENSOR) {

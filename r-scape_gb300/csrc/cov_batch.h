@@ -99,6 +99,9 @@ cudaError_t grp_weights_pb(const FamDev* F, int nf, const int* pre_col, int nb_c
                            cudaStream_t st);
 cudaError_t grp_weights_gsc(const FamDev* F, int nf, const int* pre_codes, int nb_codes, const int* pre_ident,
                             int nb_ident, const int* pre_upgma, int nb_upgma, int maxN, cudaStream_t st);
+// normalisation and limbs of the device weights (one block per family of pre)
+cudaError_t grp_weights_limbs(FamDev* F, int nf, const int* pre, int nb, UmmaFam* U, cudaStream_t st);
+int         grp_weights_gsc_prepare();
 // nulls (cov_null.cu): one depth d of every family; lv[f] = {offset of depth d
 // in lnodes, nodes at depth d} (nn = 0: nothing at this depth)
 cudaError_t grp_fitch_up(const FamDev* F, int nf, const int2* lv, const int* pre, int nb, uint64_t seed,

@@ -798,14 +798,103 @@ cudaError_t grp_weights_gsc(const FamDev* F, int nf, const int* pre_codes, int n
                             int nb_ident, const int* pre_upgma, int nb_upgma, int maxN, cudaStream_t st) {
   if (nb_upgma <= 0) return cudaSuccess;
   const size_t sm = gsc_upgma_smem(maxN);
-  if (sm > 200 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e;
-  if ((e = cudaFuncSetAttribute(k_gsc_upgma_grp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
-    return e;
+  if (sm > 200 * 1024 || !grp_weights_gsc_prepare()) return cudaErrorInvalidValue;
   if (nb_codes > 0) k_gsc_codes_grp<<<nb_codes, 256, 0, st>>>(F, nf, pre_codes);
   if (nb_ident > 0) k_gsc_ident_grp<<<nb_ident, 256, 0, st>>>(F, nf, pre_ident);
   k_gsc_upgma_grp<<<nb_upgma, 1024, sm, st>>>(F, nf, pre_upgma);
   return cudaGetLastError();
+}
+
+// the device weights of each family of pre (one block each), made as the
+// host makes a caller's weights: normalised to sum to N (the sum in sequence
+// order), then quantised to three b-bit limbs as make_limbs does
+// (cov_kernels.cu) in its general form -- normalised weights that are all
+// equal are all 1.0, whose limbs give the same counts as the one-limb form.
+// Writes the limbs (uint16 [3][Npad], zero-padded, and as floats [3][N]) and
+// the family's limb base, scale and quantised total into F and U.
+__global__ void __launch_bounds__(256)
+k_weights_limbs_grp(FamDev* __restrict__ F, int nf, const int* __restrict__ pre, UmmaFam* __restrict__ U) {
+  const int f = grp_find(pre, nf, (int)blockIdx.x);
+  FamDev& d = F[f];
+  const int N = d.N, tid = threadIdx.x;
+  __shared__ double ssum, red[256];
+  __shared__ unsigned long long tot;
+  __shared__ int sE, sb;
+  if (tid == 0) {
+    double sum = 0.0;
+    for (int i = 0; i < N; i++) sum = __dadd_rn(sum, d.w[i]);
+    ssum = sum;
+    tot = 0ull;
+  }
+  __syncthreads();
+  const double sum = ssum;
+  double wmax = 0.0;
+  for (int i = tid; i < N; i += blockDim.x) {
+    const double w = (sum > 0.0) ? __ddiv_rn(__dmul_rn(d.w[i], (double)N), sum) : 1.0;
+    d.w[i] = w;
+    wmax = fmax(wmax, w);
+  }
+  red[tid] = wmax;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (tid < o) red[tid] = fmax(red[tid], red[tid + o]);
+    __syncthreads();
+  }
+  if (tid == 0) {
+    int b = 11;
+    while (b > 1 && (double)N * (double)((1 << b) - 1) >= 16777216.0) b--;
+    int e2;
+    frexp(red[0], &e2);
+    sb = b;
+    sE = 3 * b - e2;
+  }
+  __syncthreads();
+  const int b = sb, E = sE;
+  const double qmax = ldexp(1.0, 3 * b) - 1.0;
+  const unsigned long long mask = (1ull << b) - 1ull;
+  unsigned long long t = 0;
+  for (int i = tid; i < d.Npad; i += blockDim.x) {
+    unsigned long long q = 0;
+    if (i < N) {
+      double qd = rint(ldexp(d.w[i], E));
+      if (qd > qmax) qd = qmax;
+      q = (unsigned long long)qd;
+    }
+    const uint16_t l0 = (uint16_t)(q & mask), l1 = (uint16_t)((q >> b) & mask), l2 = (uint16_t)(q >> (2 * b));
+    d.limbs[i] = l0;
+    d.limbs[d.Npad + i] = l1;
+    d.limbs[2 * d.Npad + i] = l2;
+    if (i < N) {
+      d.limbf[i] = (float)l0;
+      d.limbf[N + i] = (float)l1;
+      d.limbf[2 * N + i] = (float)l2;
+    }
+    t += q;
+  }
+  atomicAdd(&tot, t);
+  __syncthreads();
+  if (tid == 0) {
+    const float B = (float)(1 << b), s_hi = (float)ldexp(1.0, -E);
+    const double wq = ldexp((double)tot, -E);
+    const float whi = (float)wq;
+    d.nl = 3; d.B = B; d.s_hi = s_hi; d.s_lo = 0.f;
+    d.sa.wtot = make_float2(whi, (float)(wq - (double)whi));
+    U[f].B = B; U[f].s_hi = s_hi; U[f].s_lo = 0.f;
+  }
+}
+
+cudaError_t grp_weights_limbs(FamDev* F, int nf, const int* pre, int nb, UmmaFam* U, cudaStream_t st) {
+  if (nb > 0) k_weights_limbs_grp<<<nb, 256, 0, st>>>(F, nf, pre, U);
+  return cudaGetLastError();
+}
+
+// the merges' shared-memory limit, raised once, outside any stream capture
+int grp_weights_gsc_prepare() {
+  static const int ok = [] {
+    return cudaFuncSetAttribute(k_gsc_upgma_grp, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) ==
+                   cudaSuccess ? 1 : 0;
+  }();
+  return ok;
 }
 
 }  // namespace covgpu
