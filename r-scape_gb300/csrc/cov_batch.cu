@@ -72,30 +72,63 @@ struct Bump {
   }
 };
 
+// the chunk's device buffers, every kind over all of its families
+struct Layout {
+  std::vector<FamDev> F;
+  uint8_t* ax = nullptr; size_t ax_bytes = 0;
+  double* w = nullptr;                       // weights region start (w, limbf, limbs)
+  size_t wreg_bytes = 0;
+  std::vector<size_t> w_off, lf_off, lb_off; // byte offsets inside the weights region
+  int* tree = nullptr; size_t tree_n = 0;    // left, right, lnodes of every family
+  uint8_t* tiles = nullptr; size_t tiles_bytes = 0;
+  uint16_t* ops = nullptr; int pitch = 0; int64_t op_rows = 0;
+  float* cnt = nullptr; int64_t cnt_floats = 0;
+  double* pm = nullptr; size_t pm_bytes = 0; // pm, pmdf, lpi regions (RAF only: zeroed)
+  double* mm = nullptr; size_t mm_n = 0;
+  int* status = nullptr;
+  size_t total = 0;
+};
+
+// the state of one chunk between its device passes and its host phases
+struct Pending {
+  std::vector<FamHost> fams;
+  Layout Lo;
+  size_t tab_used = 0, oF = 0;
+};
+
+// one of the batch's two pipeline slots: while the host phases of one chunk
+// run on one slot, the device passes of the next run on the other
+struct Slot {
+  cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;  // the weights, alongside the nulls
+  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaEvent_t ev[3] = {};
+  uint8_t* arena = nullptr;
+  size_t arena_cap = 0;
+  uint8_t* tab = nullptr;      // descriptor tables
+  size_t tab_cap = 0;
+  int* d_uerr = nullptr;       // the tensor count kernel's error word
+  // the captured device passes of the slot's recent chunk layouts, keyed by
+  // the descriptor tables and launch parameters (least recently used first out)
+  struct Graph { std::vector<uint8_t> key; cudaGraphExec_t exec = nullptr; int launches = 0; uint64_t used = 0; };
+  std::vector<Graph> graphs;
+  uint64_t tick = 0;
+  Pending pc;
+};
+
 }  // namespace
 
 struct covgpu_batch {
   int dev = 0;
-  cudaStream_t st = nullptr;
-  cudaStream_t st2 = nullptr;  // the weights, alongside the nulls
-  cudaEvent_t fork = nullptr, join = nullptr;
   char err[512] = {0};
-  size_t budget = 0;
-  uint8_t* arena = nullptr;
-  size_t arena_cap = 0;
-  uint8_t* stat = nullptr;     // per (family, statistic) buffers
+  size_t budget = 0;           // device bytes of one chunk (half of the batch's budget)
+  uint8_t* stat = nullptr;     // per (family, statistic) buffers of the chunk in its host phases
   size_t stat_cap = 0;
-  uint8_t* tab = nullptr;      // descriptor tables
-  size_t tab_cap = 0;
   float4* d_logtab = nullptr;
-  int* d_uerr = nullptr;
   FitBatch* fits = nullptr;
-  cudaEvent_t ev[3] = {};
   double ms[3] = {0, 0, 0};
-  int nlaunch = 0, nchunks = 0, graph_replays = 0, glaunch = 0;
-  // the captured device passes of the last chunk layout
-  cudaGraphExec_t gexec = nullptr;
-  std::vector<uint8_t> gkey;
+  int nlaunch = 0, nchunks = 0, graph_replays = 0;
+  Slot slot[2];
 };
 
 static int bfail(covgpu_batch* b, int code, const char* fmt, ...) {
@@ -129,23 +162,25 @@ extern "C" int covgpu_batch_create(covgpu_batch** ret, int device, double mem_gb
   b->dev = device;
   *ret = b;
   BK(cudaSetDevice(device));
-  BK(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
-  BK(cudaStreamCreateWithFlags(&b->st2, cudaStreamNonBlocking));
-  BK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
-  BK(cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming));
-  for (auto& e : b->ev) BK(cudaEventCreate(&e));
+  for (Slot& S : b->slot) {
+    BK(cudaStreamCreateWithFlags(&S.st, cudaStreamNonBlocking));
+    BK(cudaStreamCreateWithFlags(&S.st2, cudaStreamNonBlocking));
+    BK(cudaEventCreateWithFlags(&S.fork, cudaEventDisableTiming));
+    BK(cudaEventCreateWithFlags(&S.join, cudaEventDisableTiming));
+    for (auto& e : S.ev) BK(cudaEventCreate(&e));
+    BK(cudaMalloc(&S.d_uerr, sizeof(int)));
+    BK(cudaMemset(S.d_uerr, 0, sizeof(int)));
+  }
   size_t fr = 0, tot = 0;
   BK(cudaMemGetInfo(&fr, &tot));
   const double want = mem_gb > 0.0 ? mem_gb * 1e9 : 0.25 * (double)fr;
-  b->budget = (size_t)std::max(1.6e7, std::min(want, 0.8 * (double)fr));
+  b->budget = (size_t)std::max(1.6e7, std::min(want, 0.8 * (double)fr)) / 2;
   BK(cudaMalloc(&b->d_logtab, LOGTAB_N * sizeof(float4)));
   {
     float4 tab[LOGTAB_N];
     logtab_host(tab);
     BK(cudaMemcpy(b->d_logtab, tab, sizeof(tab), cudaMemcpyHostToDevice));
   }
-  BK(cudaMalloc(&b->d_uerr, sizeof(int)));
-  BK(cudaMemset(b->d_uerr, 0, sizeof(int)));
   b->fits = fitbatch_create();
   return 0;
 }
@@ -153,16 +188,23 @@ extern "C" int covgpu_batch_create(covgpu_batch** ret, int device, double mem_gb
 extern "C" void covgpu_batch_destroy(covgpu_batch* b) {
   if (!b) return;
   cudaSetDevice(b->dev);
-  if (b->st) cudaStreamSynchronize(b->st);
-  if (b->gexec) cudaGraphExecDestroy(b->gexec);
-  void* p[] = {b->arena, b->stat, b->tab, b->d_logtab, b->d_uerr};
+  for (Slot& S : b->slot) {
+    if (S.st) cudaStreamSynchronize(S.st);
+    if (S.st2) cudaStreamSynchronize(S.st2);
+  }
+  for (Slot& S : b->slot) {
+    for (auto& g : S.graphs) if (g.exec) cudaGraphExecDestroy(g.exec);
+    void* q[] = {S.arena, S.tab, S.d_uerr};
+    for (void* x : q) if (x) cudaFree(x);
+    for (auto& e : S.ev) if (e) cudaEventDestroy(e);
+    if (S.fork) cudaEventDestroy(S.fork);
+    if (S.join) cudaEventDestroy(S.join);
+    if (S.st2) cudaStreamDestroy(S.st2);
+    if (S.st) cudaStreamDestroy(S.st);
+  }
+  void* p[] = {b->stat, b->d_logtab};
   for (void* x : p) if (x) cudaFree(x);
   if (b->fits) fitbatch_destroy(b->fits);
-  for (auto& e : b->ev) if (e) cudaEventDestroy(e);
-  if (b->fork) cudaEventDestroy(b->fork);
-  if (b->join) cudaEventDestroy(b->join);
-  if (b->st2) cudaStreamDestroy(b->st2);
-  if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }
 
@@ -241,22 +283,6 @@ void tile_order(int nT, int SB, std::vector<int>& order) {
         for (int J = std::max(I, bJ); J < std::min(nT, bJ + SB); J++) order.push_back(tindex(I, J));
 }
 
-// the chunk's device buffers, every kind over all of its families
-struct Layout {
-  std::vector<FamDev> F;
-  uint8_t* ax = nullptr; size_t ax_bytes = 0;
-  double* w = nullptr;                       // weights region start (w, limbf, limbs)
-  size_t wreg_bytes = 0;
-  std::vector<size_t> w_off, lf_off, lb_off; // byte offsets inside the weights region
-  int* tree = nullptr; size_t tree_n = 0;    // left, right, lnodes of every family
-  uint8_t* tiles = nullptr; size_t tiles_bytes = 0;
-  uint16_t* ops = nullptr; int pitch = 0; int64_t op_rows = 0;
-  float* cnt = nullptr; int64_t cnt_floats = 0;
-  double* pm = nullptr; size_t pm_bytes = 0; // pm, pmdf, lpi regions (RAF only: zeroed)
-  double* mm = nullptr; size_t mm_n = 0;
-  int* status = nullptr;
-  size_t total = 0;
-};
 
 size_t fam_bytes_hint(const FamHost& f, int nout, bool need_u, bool rafs, int pitch) {
   const size_t S = f.nslots, nT2 = (size_t)f.nT * f.nT, ntl = f.ntiles;
@@ -421,9 +447,11 @@ Pre prefix(int n, F blocks) {
 
 }  // namespace
 
-// one chunk of families: results and hits written at each family's position
-static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_family* fam_in, std::vector<FamHost>& fams,
-                     const Types& T, const int* covtypes, covgpu_result* results, covgpu_hit* hits, int hitcap) {
+// the device passes of one chunk on slot S, from the uploads to the
+// corrected scores, launched and left running; the chunk's state is kept in
+// S.pc for chunk_finish
+static int chunk_launch(covgpu_batch* b, Slot& S, const covgpu_params* p, const covgpu_family* fam_in,
+                        std::vector<FamHost>& fams, const Types& T) {
   const int nf = (int)fams.size(), nout = T.ntypes;
   const int counter = p->counter;
   const bool rafs = !T.rafs_q.empty();
@@ -431,8 +459,8 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
   Layout Lo;
   place(Lo, fams, T, counter, nullptr, rafs);
   int s;
-  if ((s = grow(b, &b->arena, &b->arena_cap, Lo.total))) return s;
-  place(Lo, fams, T, counter, b->arena, rafs);
+  if ((s = grow(b, &S.arena, &S.arena_cap, Lo.total))) return s;
+  place(Lo, fams, T, counter, S.arena, rafs);
   // ---- host tables: tiles, trees, weights given by the caller ----
   std::vector<uint8_t> tiles_h(Lo.tiles_bytes, 0);
   for (int k = 0; k < nf; k++) {
@@ -472,14 +500,14 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
     d.sa.nout = nout;
   }
   // ---- uploads ----
-  BK(cudaMemsetAsync(Lo.ax, 4, Lo.ax_bytes, b->st));
-  BK(cudaMemsetAsync(Lo.status, 0, nf * sizeof(int), b->st));
+  BK(cudaMemsetAsync(Lo.ax, 4, Lo.ax_bytes, S.st));
+  BK(cudaMemsetAsync(Lo.status, 0, nf * sizeof(int), S.st));
   for (int k = 0; k < nf; k++) {
     const FamHost& f = fams[k];
-    BK(cudaMemcpy2DAsync(Lo.F[k].ax, f.Lp, fam_in[f.idx].ax, f.L, f.L, f.N, cudaMemcpyHostToDevice, b->st));
+    BK(cudaMemcpy2DAsync(Lo.F[k].ax, f.Lp, fam_in[f.idx].ax, f.L, f.L, f.N, cudaMemcpyHostToDevice, S.st));
   }
-  BK(cudaMemcpyAsync(Lo.tiles, tiles_h.data(), Lo.tiles_bytes, cudaMemcpyHostToDevice, b->st));
-  BK(cudaMemcpyAsync(Lo.tree, tree_h.data(), tree_h.size() * sizeof(int), cudaMemcpyHostToDevice, b->st));
+  BK(cudaMemcpyAsync(Lo.tiles, tiles_h.data(), Lo.tiles_bytes, cudaMemcpyHostToDevice, S.st));
+  BK(cudaMemcpyAsync(Lo.tree, tree_h.data(), tree_h.size() * sizeof(int), cudaMemcpyHostToDevice, S.st));
 
   // ---- weights: the caller's, normalised and quantised here; R-scape's
   // rule (GSC or position-based), normalised and quantised on the device
@@ -513,7 +541,7 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
       for (int i = 0; i < f.N; i++) lf[(size_t)l * f.N + i] = (float)lim[(size_t)l * f.Npad + i];
     d.nl = cw.nl; d.B = cw.B; d.s_hi = cw.s_hi; d.s_lo = cw.s_lo;
   }
-  BK(cudaMemcpyAsync(Lo.w, wreg.data(), Lo.wreg_bytes, cudaMemcpyHostToDevice, b->st));
+  BK(cudaMemcpyAsync(Lo.w, wreg.data(), Lo.wreg_bytes, cudaMemcpyHostToDevice, S.st));
   // the statistics pass's arguments
   for (int k = 0; k < nf; k++) {
     const FamHost& f = fams[k];
@@ -607,18 +635,21 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
     u.B = d.B; u.s_hi = d.s_hi; u.s_lo = d.s_lo;
   }
   const size_t o_uf = tb.put(uf.data(), nf * sizeof(UmmaFam));
-  if ((s = grow(b, &b->tab, &b->tab_cap, tb.h.size()))) return s;
-  BK(cudaMemcpyAsync(b->tab, tb.h.data(), tb.h.size(), cudaMemcpyHostToDevice, b->st));
-  const FamDev* dF = reinterpret_cast<const FamDev*>(b->tab + oF);
-  auto P = [&](size_t o) { return reinterpret_cast<const int*>(b->tab + o); };
+  // with room after the tables for the histogram pass's tables (chunk_finish)
+  const size_t stat_room = align_up((size_t)nf * nout * sizeof(StatDev)) + align_up(((size_t)nf * nout + 1) * 4) +
+                           2 * kAlign;
+  if ((s = grow(b, &S.tab, &S.tab_cap, align_up(tb.h.size()) + stat_room))) return s;
+  BK(cudaMemcpyAsync(S.tab, tb.h.data(), tb.h.size(), cudaMemcpyHostToDevice, S.st));
+  const FamDev* dF = reinterpret_cast<const FamDev*>(S.tab + oF);
+  auto P = [&](size_t o) { return reinterpret_cast<const int*>(S.tab + o); };
   if (pup.total() && !grp_weights_gsc_prepare()) return bfail(b, 90, "GSC kernel attributes");
 
   // the key of this chunk's device passes: the descriptor tables (they hold
   // every pointer and size the launches read) and the launch parameters
   std::vector<uint8_t> key(tb.h);
   {
-    const int64_t extra[] = {nf, counter, (int64_t)T.mask, T.need_w, T.need_u, (int64_t)(uintptr_t)b->arena,
-                             (int64_t)(uintptr_t)b->tab, maxLp, (int64_t)p->seed};
+    const int64_t extra[] = {nf, counter, (int64_t)T.mask, T.need_w, T.need_u, (int64_t)(uintptr_t)S.arena,
+                             (int64_t)(uintptr_t)S.tab, maxLp, (int64_t)p->seed};
     key.insert(key.end(), (const uint8_t*)extra, (const uint8_t*)extra + sizeof(extra));
     for (int q : T.rafs_q) key.push_back((uint8_t)q);
     key.insert(key.end(), (const uint8_t*)&T.ct, (const uint8_t*)&T.ct + sizeof(T.ct));
@@ -628,114 +659,140 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
     // R-scape's weights on the second stream, alongside the nulls
     const bool wdev = plb.total() > 0;
     if (wdev) {
-      BK(cudaEventRecord(b->fork, b->st));
-      BK(cudaStreamWaitEvent(b->st2, b->fork, 0));
-      FamDev* dFw = reinterpret_cast<FamDev*>(b->tab + oF);
-      UmmaFam* dUw = reinterpret_cast<UmmaFam*>(b->tab + o_uf);
-      BK(grp_weights_pb(dF, nf, P(o_col), pcol.total(), P(o_row), prow.total(), b->st2));
-      BK(grp_weights_gsc(dF, nf, P(o_cod), pcod.total(), P(o_id), pid.total(), P(o_up), pup.total(), maxN, b->st2));
-      BK(grp_weights_limbs(dFw, nf, P(o_lb), plb.total(), dUw, b->st2));
-      BK(cudaEventRecord(b->join, b->st2));
+      BK(cudaEventRecord(S.fork, S.st));
+      BK(cudaStreamWaitEvent(S.st2, S.fork, 0));
+      FamDev* dFw = reinterpret_cast<FamDev*>(S.tab + oF);
+      UmmaFam* dUw = reinterpret_cast<UmmaFam*>(S.tab + o_uf);
+      BK(grp_weights_pb(dF, nf, P(o_col), pcol.total(), P(o_row), prow.total(), S.st2));
+      BK(grp_weights_gsc(dF, nf, P(o_cod), pcod.total(), P(o_id), pid.total(), P(o_up), pup.total(), maxN, S.st2));
+      BK(grp_weights_limbs(dFw, nf, P(o_lb), plb.total(), dUw, S.st2));
+      BK(cudaEventRecord(S.join, S.st2));
       launches += (pcol.total() ? 2 : 0) + (pup.total() ? 3 : 0) + 1;
     }
     // nulls: Fitch up the tree, the roots, the replay down it
     for (int dd = maxdepth - 1; dd >= 0; dd--)
       if (lvl[dd].nup) {
-        BK(grp_fitch_up(dF, nf, reinterpret_cast<const int2*>(b->tab + lvl[dd].lv), P(lvl[dd].up), lvl[dd].nup,
-                        p->seed, b->st));
+        BK(grp_fitch_up(dF, nf, reinterpret_cast<const int2*>(S.tab + lvl[dd].lv), P(lvl[dd].up), lvl[dd].nup,
+                        p->seed, S.st));
         launches++;
       }
     if (prs.total()) {
-      BK(grp_root(dF, nf, P(o_rs), prs.total(), P(o_rr), prr.total(), p->seed, b->st));
+      BK(grp_root(dF, nf, P(o_rs), prs.total(), P(o_rr), prr.total(), p->seed, S.st));
       launches += 2;
     }
     for (int dd = 0; dd < maxdepth; dd++) {
-      const int2* lv = reinterpret_cast<const int2*>(b->tab + lvl[dd].lv);
+      const int2* lv = reinterpret_cast<const int2*>(S.tab + lvl[dd].lv);
       if (lvl[dd].ncta) {
-        BK(grp_replay(dF, nf, lv, P(lvl[dd].cta), lvl[dd].ncta, true, srow_cta, maxLp, p->seed, b->st));
+        BK(grp_replay(dF, nf, lv, P(lvl[dd].cta), lvl[dd].ncta, true, srow_cta, maxLp, p->seed, S.st));
         launches++;
       }
       if (lvl[dd].nwarp) {
-        BK(grp_replay(dF, nf, lv, P(lvl[dd].warp), lvl[dd].nwarp, false, srow_warp, maxLp, p->seed, b->st));
+        BK(grp_replay(dF, nf, lv, P(lvl[dd].warp), lvl[dd].nwarp, false, srow_warp, maxLp, p->seed, S.st));
         launches++;
       }
     }
-    if (wdev) BK(cudaStreamWaitEvent(b->st, b->join, 0));
+    if (wdev) BK(cudaStreamWaitEvent(S.st, S.join, 0));
     // counts and marginals
     if (T.need_w) {
       if (counter == COVGPU_COUNT_TENSOR) {
-        BK(grp_umma_prep(dF, nf, P(o_prep), pprep.total(), Lo.pitch, Lo.ops, b->st));
-        const UmmaFam* dU = reinterpret_cast<const UmmaFam*>(b->tab + o_uf);
+        BK(grp_umma_prep(dF, nf, P(o_prep), pprep.total(), Lo.pitch, Lo.ops, S.st));
+        const UmmaFam* dU = reinterpret_cast<const UmmaFam*>(S.tab + o_uf);
         for (int nl : {3, 1}) {
           const Pre& pt = (nl == 3) ? pt3 : pt1;
           if (!pt.total()) continue;
           const int us = grp_umma_count(dU, nf, P(nl == 3 ? o_t3 : o_t1), pt.total(), nl, Lo.ops, Lo.pitch,
-                                        Lo.op_rows, Lo.cnt, Lo.cnt_floats / 32, b->d_uerr, b->st);
+                                        Lo.op_rows, Lo.cnt, Lo.cnt_floats / 32, S.d_uerr, S.st);
           if (us) return bfail(b, us == 11 ? 12 : 90, "tensor counting not available for this batch (%d)", us);
           launches++;
         }
         launches++;
       } else {
-        BK(grp_count_simt(dF, nf, P(o_tile), ptile.total(), false, true, b->st));
+        BK(grp_count_simt(dF, nf, P(o_tile), ptile.total(), false, true, S.st));
         launches++;
       }
-      BK(grp_marginals(dF, nf, P(o_tile), ptile.total(), P(o_pm), ppm.total(), P(o_mp), pmp.total(), b->st));
+      BK(grp_marginals(dF, nf, P(o_tile), ptile.total(), P(o_pm), ppm.total(), P(o_mp), pmp.total(), S.st));
       launches += 3;
     } else {
-      BK(cudaMemsetAsync(Lo.pm, 0, Lo.pm_bytes, b->st));
+      BK(cudaMemsetAsync(Lo.pm, 0, Lo.pm_bytes, S.st));
     }
     if (T.need_u) {
-      BK(grp_count_simt(dF, nf, P(o_tile), ptile.total(), true, false, b->st));
+      BK(grp_count_simt(dF, nf, P(o_tile), ptile.total(), true, false, S.st));
       launches++;
     }
-    BK(grp_stats(dF, nf, P(o_tile), ptile.total(), stats_cf(T.mask), b->st));
+    BK(grp_stats(dF, nf, P(o_tile), ptile.total(), stats_cf(T.mask), S.st));
     launches++;
     for (int q : T.rafs_q) {
       for (int k = 0; k < nf; k++) {
         const FamDev& d = Lo.F[k];
         const int64_t plane = (int64_t)d.ntiles * TPP;
         BK(cudaMemcpy2DAsync(d.cov2, plane * sizeof(float2), d.cov + q * plane, nout * plane * sizeof(float2),
-                             plane * sizeof(float2), d.nslots, cudaMemcpyDeviceToDevice, b->st));
+                             plane * sizeof(float2), d.nslots, cudaMemcpyDeviceToDevice, S.st));
       }
-      BK(grp_rafs(dF, nf, P(o_tile), ptile.total(), q, b->st));
+      BK(grp_rafs(dF, nf, P(o_tile), ptile.total(), q, S.st));
       launches++;
     }
-    BK(grp_apc(dF, nf, P(o_cx), pcx.total(), P(o_sq), psq.total(), P(o_ap), pap.total(), T.ct, b->st));
+    BK(grp_apc(dF, nf, P(o_cx), pcx.total(), P(o_sq), psq.total(), P(o_ap), pap.total(), T.ct, S.st));
     launches += 4;
     return 0;
   };
-  BK(cudaEventRecord(b->ev[0], b->st));
-  if (b->gexec && key == b->gkey) {
-    BK(cudaGraphLaunch(b->gexec, b->st));
+  BK(cudaEventRecord(S.ev[0], S.st));
+  Slot::Graph* hit = nullptr;
+  for (auto& g : S.graphs)
+    if (g.key == key) { hit = &g; break; }
+  if (hit) {
+    BK(cudaGraphLaunch(hit->exec, S.st));
     b->graph_replays++;
-    launches = b->glaunch;
+    launches = hit->launches;
+    hit->used = ++S.tick;
   } else {
-    if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
-    b->gkey.clear();
     cudaGraph_t g = nullptr;
-    BK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    BK(cudaStreamBeginCapture(S.st, cudaStreamCaptureModeThreadLocal));
     const int ps = passes();
-    cudaError_t ce = cudaStreamEndCapture(b->st, &g);
+    cudaError_t ce = cudaStreamEndCapture(S.st, &g);
     if (ps) { if (g) cudaGraphDestroy(g); return ps; }
     if (ce != cudaSuccess) return bfail(b, 90, "graph capture: %s", cudaGetErrorString(ce));
-    ce = cudaGraphInstantiate(&b->gexec, g, 0);
+    cudaGraphExec_t exec = nullptr;
+    ce = cudaGraphInstantiate(&exec, g, 0);
     cudaGraphDestroy(g);
-    if (ce != cudaSuccess) { b->gexec = nullptr; return bfail(b, 90, "graph instantiate: %s", cudaGetErrorString(ce)); }
-    b->gkey = key;
-    b->glaunch = launches;
-    BK(cudaGraphLaunch(b->gexec, b->st));
+    if (ce != cudaSuccess) return bfail(b, 90, "graph instantiate: %s", cudaGetErrorString(ce));
+    constexpr size_t kGraphs = 24;
+    if (S.graphs.size() >= kGraphs) {   // out goes the least recently used
+      auto old = std::min_element(S.graphs.begin(), S.graphs.end(),
+                                  [](const Slot::Graph& x, const Slot::Graph& y) { return x.used < y.used; });
+      cudaGraphExecDestroy(old->exec);
+      S.graphs.erase(old);
+    }
+    S.graphs.push_back(Slot::Graph{std::move(key), exec, launches, ++S.tick});
+    BK(cudaGraphLaunch(exec, S.st));
   }
   b->nlaunch += launches;
-  BK(cudaEventRecord(b->ev[1], b->st));
+  BK(cudaEventRecord(S.ev[1], S.st));
+  S.pc.fams = std::move(fams);
+  S.pc.Lo = std::move(Lo);
+  S.pc.tab_used = tb.h.size();
+  S.pc.oF = oF;
+  return 0;
+}
+
+// the host phases of the chunk whose device passes chunk_launch started on
+// slot S: ranges, histograms, fits, survival tables, E-values and hits,
+// written at each family's position
+static int chunk_finish(covgpu_batch* b, Slot& S, const covgpu_params* p, const Types& T, const int* covtypes,
+                        covgpu_result* results, covgpu_hit* hits, int hitcap) {
+  std::vector<FamHost>& fams = S.pc.fams;
+  Layout& Lo = S.pc.Lo;
+  const int nf = (int)fams.size(), nout = T.ntypes;
+  const FamDev* dF = reinterpret_cast<const FamDev*>(S.tab + S.pc.oF);
+  int s;
   std::vector<double> mm(Lo.mm_n);
   std::vector<int> stat(nf);
-  BK(cudaMemcpyAsync(mm.data(), Lo.mm, mm.size() * sizeof(double), cudaMemcpyDeviceToHost, b->st));
-  BK(cudaMemcpyAsync(stat.data(), Lo.status, nf * sizeof(int), cudaMemcpyDeviceToHost, b->st));
+  BK(cudaMemcpyAsync(mm.data(), Lo.mm, mm.size() * sizeof(double), cudaMemcpyDeviceToHost, S.st));
+  BK(cudaMemcpyAsync(stat.data(), Lo.status, nf * sizeof(int), cudaMemcpyDeviceToHost, S.st));
   int uerr = 0;
-  BK(cudaMemcpyAsync(&uerr, b->d_uerr, sizeof(int), cudaMemcpyDeviceToHost, b->st));
-  BK(cudaStreamSynchronize(b->st));
+  BK(cudaMemcpyAsync(&uerr, S.d_uerr, sizeof(int), cudaMemcpyDeviceToHost, S.st));
+  BK(cudaStreamSynchronize(S.st));
   if (uerr) {
-    cudaMemset(b->d_uerr, 0, sizeof(int));
+    cudaMemset(S.d_uerr, 0, sizeof(int));
     return bfail(b, 24, "tensor counting kernel: barrier wait timed out (code %d)", uerr);
   }
   auto status_fail = [&](int k, int st) {
@@ -816,22 +873,17 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
     Pre ph = prefix(na, [&](int e) { return hb[e]; });
     Tab t2;
     const size_t o_sd = t2.put(SD.data(), na * sizeof(StatDev)), o_ph = t2.put(ph.v.data(), ph.v.size() * 4);
-    uint8_t* tab2 = b->tab + align_up(tb.h.size());
-    if ((s = grow(b, &b->tab, &b->tab_cap, align_up(tb.h.size()) + t2.h.size()))) return s;
-    if (b->tab + align_up(tb.h.size()) != tab2) {   // the table moved: the descriptor tables go again
-      BK(cudaMemcpyAsync(b->tab, tb.h.data(), tb.h.size(), cudaMemcpyHostToDevice, b->st));
-      if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; b->gkey.clear(); }
-      tab2 = b->tab + align_up(tb.h.size());
-      dF = reinterpret_cast<const FamDev*>(b->tab + oF);
-    }
-    BK(cudaMemcpyAsync(tab2, t2.h.data(), t2.h.size(), cudaMemcpyHostToDevice, b->st));
-    BK(cudaMemsetAsync(d_obs, 0, std::max<int64_t>(obs_tot, 1) * 8, b->st));
+    // the room after the descriptor tables was reserved by chunk_launch
+    uint8_t* tab2 = S.tab + align_up(S.pc.tab_used);
+    if (align_up(S.pc.tab_used) + t2.h.size() > S.tab_cap) return bfail(b, 90, "batch table area overflow");
+    BK(cudaMemcpyAsync(tab2, t2.h.data(), t2.h.size(), cudaMemcpyHostToDevice, S.st));
+    BK(cudaMemsetAsync(d_obs, 0, std::max<int64_t>(obs_tot, 1) * 8, S.st));
     BK(grp_hist(dF, reinterpret_cast<const StatDev*>(tab2 + o_sd), na, reinterpret_cast<const int*>(tab2 + o_ph),
-                ph.total(), maxwin, b->st));
+                ph.total(), maxwin, S.st));
     b->nlaunch += 1;
-    BK(cudaMemcpyAsync(obs.data(), d_obs, obs_tot * 8, cudaMemcpyDeviceToHost, b->st));
-    BK(cudaMemcpyAsync(stat.data(), Lo.status, nf * sizeof(int), cudaMemcpyDeviceToHost, b->st));
-    BK(cudaStreamSynchronize(b->st));
+    BK(cudaMemcpyAsync(obs.data(), d_obs, obs_tot * 8, cudaMemcpyDeviceToHost, S.st));
+    BK(cudaMemcpyAsync(stat.data(), Lo.status, nf * sizeof(int), cudaMemcpyDeviceToHost, S.st));
+    BK(cudaStreamSynchronize(S.st));
     for (int k = 0; k < nf; k++)
       if (stat[k]) return status_fail(k, stat[k]);
 
@@ -853,10 +905,10 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
       }
     }
     if (!fr.empty()) {
-      const int fs = gamma_fit_batch_launch(b->fits, (int)fr.size(), fr.data(), b->st);
+      const int fs = gamma_fit_batch_launch(b->fits, (int)fr.size(), fr.data(), S.st);
       if (fs) return bfail(b, 32, "could not do the Gamma fits (%d)", fs);
       b->nlaunch += 1;
-      BK(cudaStreamSynchronize(b->st));
+      BK(cudaStreamSynchronize(S.st));
       for (size_t k = 0; k < fr.size(); k++) {
         const int e = fe[k];
         RsStat& X = XS[act[e].first][act[e].second];
@@ -896,12 +948,12 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
       Tab t3;
       const size_t o_sr = t3.put(sr.data(), sr.size() * sizeof(SurvReq)), o_ps = t3.put(psf.v.data(), psf.v.size() * 4);
       uint8_t* tab3 = sm.take<uint8_t>(t3.h.size());
-      BK(cudaMemcpyAsync(tab3, t3.h.data(), t3.h.size(), cudaMemcpyHostToDevice, b->st));
+      BK(cudaMemcpyAsync(tab3, t3.h.data(), t3.h.size(), cudaMemcpyHostToDevice, S.st));
       BK(grp_survfit(reinterpret_cast<const SurvReq*>(tab3 + o_sr), reinterpret_cast<const int*>(tab3 + o_ps),
-                     (int)sr.size(), psf.total(), b->st));
+                     (int)sr.size(), psf.total(), S.st));
       b->nlaunch += 1;
-      BK(cudaMemcpyAsync(sfh.data(), d_sf, sf_tot * 8, cudaMemcpyDeviceToHost, b->st));
-      BK(cudaStreamSynchronize(b->st));
+      BK(cudaMemcpyAsync(sfh.data(), d_sf, sf_tot * 8, cudaMemcpyDeviceToHost, S.st));
+      BK(cudaStreamSynchronize(S.st));
     }
 
     // ---- phase 4: thresholds, tail tables, E-values and hits ----
@@ -933,15 +985,15 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
     const size_t o_sd4 = t4.put(SD.data(), na * sizeof(StatDev)), o_pe = t4.put(pe.v.data(), pe.v.size() * 4);
     uint8_t* tab4 = sm.take<uint8_t>(t4.h.size());
     if (sm.off > b->stat_cap) return bfail(b, 90, "batch statistics area overflow");
-    BK(cudaMemcpyAsync(d_tail, tail.data(), std::max<int64_t>(tail_tot, 1) * 8, cudaMemcpyHostToDevice, b->st));
-    BK(cudaMemcpyAsync(tab4, t4.h.data(), t4.h.size(), cudaMemcpyHostToDevice, b->st));
-    BK(cudaMemsetAsync(d_nh, 0, na * sizeof(int), b->st));
+    BK(cudaMemcpyAsync(d_tail, tail.data(), std::max<int64_t>(tail_tot, 1) * 8, cudaMemcpyHostToDevice, S.st));
+    BK(cudaMemcpyAsync(tab4, t4.h.data(), t4.h.size(), cudaMemcpyHostToDevice, S.st));
+    BK(cudaMemsetAsync(d_nh, 0, na * sizeof(int), S.st));
     BK(grp_evalue(dF, reinterpret_cast<const StatDev*>(tab4 + o_sd4), na, reinterpret_cast<const int*>(tab4 + o_pe),
-                  pe.total(), b->st));
+                  pe.total(), S.st));
     b->nlaunch += 1;
     std::vector<int> nh(na);
-    BK(cudaMemcpyAsync(nh.data(), d_nh, na * sizeof(int), cudaMemcpyDeviceToHost, b->st));
-    BK(cudaStreamSynchronize(b->st));
+    BK(cudaMemcpyAsync(nh.data(), d_nh, na * sizeof(int), cudaMemcpyDeviceToHost, S.st));
+    BK(cudaStreamSynchronize(S.st));
     // the hit lists, read back together
     std::vector<size_t> ho(na + 1, 0);
     for (int e = 0; e < na; e++) ho[e + 1] = ho[e] + (hits ? (size_t)std::max(0, std::min(nh[e], dcap[e])) : 0);
@@ -951,13 +1003,13 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
     for (int e = 0; e < na; e++) {
       const size_t n = ho[e + 1] - ho[e], o = ho[e];
       if (!n) continue;
-      BK(cudaMemcpyAsync(hi_.data() + o, SD[e].hi, n * sizeof(int), cudaMemcpyDeviceToHost, b->st));
-      BK(cudaMemcpyAsync(hj_.data() + o, SD[e].hj, n * sizeof(int), cudaMemcpyDeviceToHost, b->st));
-      BK(cudaMemcpyAsync(hs_.data() + o, SD[e].hsc, n * sizeof(double), cudaMemcpyDeviceToHost, b->st));
-      BK(cudaMemcpyAsync(hE_.data() + o, SD[e].hE, n * sizeof(double), cudaMemcpyDeviceToHost, b->st));
-      BK(cudaMemcpyAsync(hp_.data() + o, SD[e].hp, n * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+      BK(cudaMemcpyAsync(hi_.data() + o, SD[e].hi, n * sizeof(int), cudaMemcpyDeviceToHost, S.st));
+      BK(cudaMemcpyAsync(hj_.data() + o, SD[e].hj, n * sizeof(int), cudaMemcpyDeviceToHost, S.st));
+      BK(cudaMemcpyAsync(hs_.data() + o, SD[e].hsc, n * sizeof(double), cudaMemcpyDeviceToHost, S.st));
+      BK(cudaMemcpyAsync(hE_.data() + o, SD[e].hE, n * sizeof(double), cudaMemcpyDeviceToHost, S.st));
+      BK(cudaMemcpyAsync(hp_.data() + o, SD[e].hp, n * sizeof(double), cudaMemcpyDeviceToHost, S.st));
     }
-    if (nall) BK(cudaStreamSynchronize(b->st));
+    if (nall) BK(cudaStreamSynchronize(S.st));
     for (int e = 0; e < na; e++) {
       const int k = act[e].first, q = act[e].second;
       covgpu_result& R = results[(size_t)fams[k].idx * nout + q];
@@ -970,11 +1022,11 @@ static int run_chunk(covgpu_batch* b, const covgpu_params* p, const covgpu_famil
       std::sort(H, H + n, [](const covgpu_hit& a, const covgpu_hit& c) { return (a.i != c.i) ? a.i < c.i : a.j < c.j; });
     }
   }
-  BK(cudaEventRecord(b->ev[2], b->st));
-  BK(cudaEventSynchronize(b->ev[2]));
+  BK(cudaEventRecord(S.ev[2], S.st));
+  BK(cudaEventSynchronize(S.ev[2]));
   float a = 0.f, c = 0.f;
-  cudaEventElapsedTime(&a, b->ev[0], b->ev[1]);
-  cudaEventElapsedTime(&c, b->ev[1], b->ev[2]);
+  cudaEventElapsedTime(&a, S.ev[0], S.ev[1]);
+  cudaEventElapsedTime(&c, S.ev[1], S.ev[2]);
   b->ms[0] += a; b->ms[1] += c;
   return 0;
 }
@@ -1036,11 +1088,17 @@ extern "C" int covgpu_rscape_families(covgpu_batch* b, const covgpu_params* p, i
     int s;
     if ((s = plan_tree(b, f, h))) return s;
   }
-  // chunks: families sorted by padded N, cut at the device budget
+  // chunks: families sorted by padded N, cut at the device budget; chunk
+  // k + 1's device passes are launched on the other slot before chunk k's
+  // host phases run
   std::vector<int> ord(nfam);
   std::iota(ord.begin(), ord.end(), 0);
   std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return all[a].Npad < all[c].Npad; });
   const bool rafs = !T.rafs_q.empty();
+  int cur = 0, prev = -1;
+  auto drain = [&]() {
+    for (Slot& S : b->slot) { cudaStreamSynchronize(S.st); cudaStreamSynchronize(S.st2); }
+  };
   size_t k = 0;
   while (k < ord.size()) {
     std::vector<FamHost> chunk;
@@ -1060,9 +1118,16 @@ extern "C" int covgpu_rscape_families(covgpu_batch* b, const covgpu_params* p, i
       pitch = pn;
       k++;
     }
-    int s = run_chunk(b, p, fams_in, chunk, T, covtypes, results, hits, hitcap);
-    if (s) return s;
+    int s = chunk_launch(b, b->slot[cur], p, fams_in, chunk, T);
+    if (!s && prev >= 0) s = chunk_finish(b, b->slot[prev], p, T, covtypes, results, hits, hitcap);
+    if (s) { drain(); return s; }
     b->nchunks++;
+    prev = cur;
+    cur ^= 1;
+  }
+  if (prev >= 0) {
+    const int s = chunk_finish(b, b->slot[prev], p, T, covtypes, results, hits, hitcap);
+    if (s) { drain(); return s; }
   }
   b->ms[2] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return 0;

@@ -637,9 +637,12 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const df (&c)[16]
       const df mi = df_mul(Mn, iZ);
       out.mi = mi;
       out.gt = df_scale(df_mul(ne, mi), 2.f);
-      const df H = df_sub(lnZ, df_mul(Sn, iZ));
-      out.mir = above_h(H) ? df_div(mi, H) : df{0.f, 0.f};
-      out.mig = df_sub(mi, df_div(df_sub(wt, ne), ne));
+      // the mask is the same for every thread: no divergence
+      if (S & S_MIr) {
+        const df H = df_sub(lnZ, df_mul(Sn, iZ));
+        out.mir = above_h(H) ? df_div(mi, H) : df{0.f, 0.f};
+      }
+      if (S & S_MIg) out.mig = df_sub(mi, df_div(df_sub(wt, ne), ne));
     }
     if (CF & CF_CHI) {
       df Q = {0.f, 0.f};
@@ -699,17 +702,27 @@ __device__ __forceinline__ void pair_stats(const StatsArgs& A, const df (&c)[16]
     df mi = {0.f, 0.f}, hh = {0.f, 0.f};
     if (hw && qw.hi > 0.f) mi = df_add(mi, df_mul(pw, df_sub(lCw, lqw)));
     if (hn && qn.hi > 0.f) mi = df_add(mi, df_mul(pn, df_sub(lCn, lqn)));
-    if (hw) hh = df_sub(hh, df_mul(pw, lCw));
-    if (hn) hh = df_sub(hh, df_mul(pn, lCn));
-    df chi = {0.f, 0.f}, om = {0.f, 0.f};
-    if (qw.hi > 0.f) { const df d = df_sub(pw, qw); const df d2 = df_mul(d, d); chi = df_add(chi, df_div(d2, qw)); om = df_add(om, d2); }
-    if (qn.hi > 0.f) { const df d = df_sub(pn, qn); const df d2 = df_mul(d, d); chi = df_add(chi, df_div(d2, qn)); om = df_add(om, d2); }
-    out.chi = df_mul(ne, chi);
     out.gt = df_scale(df_mul(ne, mi), 2.f);
     out.mi = mi;
-    out.mir = above_h(hh) ? df_div(mi, hh) : df{0.f, 0.f};
-    out.mig = df_sub(mi, df_div(df_sub(wt, ne), ne));
-    out.omes = df_mul(ne, om);
+    if (S & S_MIr) {
+      if (hw) hh = df_sub(hh, df_mul(pw, lCw));
+      if (hn) hh = df_sub(hh, df_mul(pn, lCn));
+      out.mir = above_h(hh) ? df_div(mi, hh) : df{0.f, 0.f};
+    }
+    if (S & S_MIg) out.mig = df_sub(mi, df_div(df_sub(wt, ne), ne));
+    if (S & (S_CHI | S_OMES)) {
+      df chi = {0.f, 0.f}, om = {0.f, 0.f};
+      if (qw.hi > 0.f) {
+        const df d = df_sub(pw, qw), d2 = df_mul(d, d);
+        chi = df_add(chi, df_div(d2, qw)); om = df_add(om, d2);
+      }
+      if (qn.hi > 0.f) {
+        const df d = df_sub(pn, qn), d2 = df_mul(d, d);
+        chi = df_add(chi, df_div(d2, qn)); om = df_add(om, d2);
+      }
+      out.chi = df_mul(ne, chi);
+      out.omes = df_mul(ne, om);
+    }
   }
 }
 
