@@ -215,10 +215,10 @@ def val_loss(net, X, T):
     return float(np.mean(((net.forward(X) - T) / ys) ** 2))
 
 
-def train_selected(X, T, grid_epochs=(5, 10, 20, 40, 80, 160), grid_wd=(1e-4, 1e-2, 1e-1), val_frac=0.15, batch=256,
-                   lr=2e-3, seed=1, log=None):
+def train_selected(X, T, grid_epochs=(5, 10, 20, 40, 80, 160), grid_wd=(1e-4, 1e-2, 1e-1, 0.3, 1.0), val_frac=0.15,
+                   batch=256, lr=2e-3, seed=1, log=None):
     """Epochs and weight decay chosen on a held-out split of the families;
-    the network kept is the one trained with the chosen setting on the rest."""
+    the network kept is trained with the chosen setting on every family."""
     rng = np.random.default_rng(seed)
     idx = rng.permutation(len(X))
     nv = max(1, int(val_frac * len(X)))
@@ -237,8 +237,10 @@ def train_selected(X, T, grid_epochs=(5, 10, 20, 40, 80, 160), grid_wd=(1e-4, 1e
             else:
                 net.close()
     zero = float(np.mean(((T[va] - T[tr].mean(0)) / T[tr].std(0)) ** 2))
-    return best[1], dict(val_loss=best[0], epochs=best[2], wd=best[3], val_loss_mean_predictor=zero,
-                         train_rows=len(tr), val_rows=len(va))
+    best[1].close()
+    net, _ = train(X, T, epochs=best[2], batch=batch, lr=lr, wd=best[3], seed=seed, log=log)
+    return net, dict(val_loss=best[0], epochs=best[2], wd=best[3], val_loss_mean_predictor=zero,
+                     train_rows=len(X), val_rows=len(va))
 
 
 def save(net, path, nquick):
