@@ -264,6 +264,13 @@ def ragged_families(cg, nfam, counter, device, compare=200):
     data = [ln.make_family(f)[0] for f in fams]
     fl = [dict(ax=s.ax, parent=s.parent, left=s.left, right=s.right) for s in data]
     b = cg.Batch(device=device)
+    # the count schedule, tuned on the first families
+    tuned = None
+    if counter == cg.TENSOR:
+        bt, bs, times = b.autotune(fl[:min(200, nfam)], ["GTp"], counter=counter)
+        tuned = {"simt_below": bt, "raster_superblock": bs,
+                 "seconds": {"%d,%d" % k: v for k, v in sorted(times.items())},
+                 "families": min(200, nfam)}
     b.rscape(fl, ["GTp"], counter=counter)
     ts = []
     for _ in range(2):
@@ -277,7 +284,7 @@ def ragged_families(cg, nfam, counter, device, compare=200):
     out = {"families": nfam, "seconds": dt, "msas_per_s": nfam / dt, "column_pairs_per_s": pairs / dt,
            "statistic": "GTp", "nulls": "R-scape rule (20 here)", "counter": "tensor" if counter else "simt",
            "mode": "grouped: one launch per pass over all families, device passes as a CUDA graph",
-           "launches": nl, "chunks": nch,
+           "launches": nl, "chunks": nch, "schedule": tuned,
            "device_ms": {"nulls_to_corrected_scores": dev_ms, "histograms_fits_evalues": rest_ms},
            "timing": "host wall clock of one call, host buffers in, hit lists out; best of 2 after a warm-up call"}
     if compare > 0:

@@ -197,6 +197,16 @@ const char *covgpu_batch_errmsg(const covgpu_batch *b);
  * returns 0 or the first error (its message names the family) */
 int  covgpu_rscape_families(covgpu_batch *b, const covgpu_params *p, int nfam, const covgpu_family *fams,
                             int ntypes, const int *covtypes, covgpu_result *results, covgpu_hit *hits, int hitcap);
+/* the count schedule: families of fewer than simt_below sequences are
+ * counted on the SIMT kernel when the tensor counter is asked for (the counts
+ * are the same), sb the raster super-block of the tensor count's tile order
+ * (defaults 64 and 10); covgpu_batch_autotune times the caller's families
+ * under every (thr[i], sbs[j]) pair (host wall clock, best of two calls
+ * after a warm-up; ms[i * nsb + j]) and keeps the fastest */
+int  covgpu_batch_set_schedule(covgpu_batch *b, int simt_below, int sb);
+int  covgpu_batch_autotune(covgpu_batch *b, const covgpu_params *p, int nfam, const covgpu_family *fams,
+                           int ntypes, const int *covtypes, int nthr, const int *thr, int nsb, const int *sbs,
+                           double *ms, int *best_thr, int *best_sb);
 /* the last call: device milliseconds of [0] the passes from the nulls to the
  * corrected scores, [1] the histograms, fits and E-values (with their host
  * steps), [2] host wall clock of the whole call; kernel launches; chunks */

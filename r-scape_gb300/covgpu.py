@@ -131,6 +131,9 @@ def lib():
         L.covgpu_rscape_families.argtypes = [vp, C.POINTER(Params), C.c_int, C.POINTER(Family), C.c_int, i32p,
                                              C.POINTER(Result), C.POINTER(Hit), C.c_int]
         L.covgpu_batch_timing.argtypes = [vp, f64p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.covgpu_batch_set_schedule.argtypes = [vp, C.c_int, C.c_int]
+        L.covgpu_batch_autotune.argtypes = [vp, C.POINTER(Params), C.c_int, C.POINTER(Family), C.c_int, i32p, C.c_int,
+                                            i32p, C.c_int, i32p, f64p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _LIB = L
     return _LIB
 
@@ -540,16 +543,10 @@ class Batch:
         except Exception:
             pass
 
-    def rscape(self, families, types, hitcap=1 << 12, **kw):
-        """families: dicts with ax [N][L] (uint8), parent/left/right (int32,
-        N-1 each; parent optional) and optionally wgt [N] (None: R-scape's rule
-        on the device).  Returns, per family, the list of result dicts of
-        covgpu_rscape (one per type)."""
-        p = params(**kw)
-        codes = np.array([covtype_code(t) for t in types], dtype=np.int32)
-        nf, nt = len(families), len(codes)
+    @staticmethod
+    def _families(families):
         keep = []
-        fam = (Family * max(nf, 1))()
+        fam = (Family * max(len(families), 1))()
         for k, f in enumerate(families):
             ax = np.ascontiguousarray(f["ax"], dtype=np.uint8)
             keep.append(ax)
@@ -563,6 +560,40 @@ class Batch:
                 a = np.ascontiguousarray(v, dtype=np.float64 if name == "wgt" else np.int32)
                 keep.append(a)
                 setattr(fam[k], name, a.ctypes.data)
+        return fam, keep
+
+    def set_schedule(self, simt_below, sb):
+        """Families of fewer than simt_below sequences count on the SIMT kernel; sb the raster super-block."""
+        if lib().covgpu_batch_set_schedule(self.h, int(simt_below), int(sb)):
+            raise ValueError("bad schedule")
+
+    def autotune(self, families, types, thr=(0, 64, 128, 256), sb=(6, 10, 16), **kw):
+        """Time the families under every (threshold, super-block) pair and keep the
+        fastest: (best threshold, best super-block, {(thr, sb): seconds})."""
+        p = params(**kw)
+        codes = np.array([covtype_code(t) for t in types], dtype=np.int32)
+        fam, keep = self._families(families)
+        th = np.ascontiguousarray(thr, dtype=np.int32)
+        sbs = np.ascontiguousarray(sb, dtype=np.int32)
+        ms = np.zeros(len(th) * len(sbs))
+        bt, bs = C.c_int(), C.c_int()
+        st = lib().covgpu_batch_autotune(self.h, C.byref(p), len(families), fam, len(codes), codes, len(th), th,
+                                         len(sbs), sbs, ms, C.byref(bt), C.byref(bs))
+        if st:
+            raise RuntimeError("covgpu batch error %d: %s" % (st, lib().covgpu_batch_errmsg(self.h).decode()))
+        times = {(int(a), int(c)): float(ms[i * len(sbs) + j]) / 1000.0 for i, a in enumerate(th)
+                 for j, c in enumerate(sbs)}
+        return bt.value, bs.value, times
+
+    def rscape(self, families, types, hitcap=1 << 12, **kw):
+        """families: dicts with ax [N][L] (uint8), parent/left/right (int32,
+        N-1 each; parent optional) and optionally wgt [N] (None: R-scape's rule
+        on the device).  Returns, per family, the list of result dicts of
+        covgpu_rscape (one per type)."""
+        p = params(**kw)
+        codes = np.array([covtype_code(t) for t in types], dtype=np.int32)
+        nf, nt = len(families), len(codes)
+        fam, keep = self._families(families)
         res = (Result * max(nf * nt, 1))()
         hits = (Hit * max(nf * nt * hitcap, 1))()
         st = lib().covgpu_rscape_families(self.h, C.byref(p), nf, fam, nt, codes, res, hits, hitcap)

@@ -54,6 +54,7 @@ struct FamHost {
   int N = 0, L = 0, Lp = 0, nT = 0, ntiles = 0, ns = 0, nslots = 0, Npad = 0, Lw = 0;
   double fracfit = 1.0;
   bool gsc = false, pb = false;
+  bool tens = false;           // weighted counts on the tensor cores (else on the SIMT kernel)
   std::vector<int> order;      // internal nodes by depth (lnodes)
   std::vector<int> loff;       // depth offsets into order
   int depth() const { return (int)loff.size() - 1; }
@@ -128,6 +129,8 @@ struct covgpu_batch {
   FitBatch* fits = nullptr;
   double ms[3] = {0, 0, 0};
   int nlaunch = 0, nchunks = 0, graph_replays = 0;
+  int simt_below = 64;         // families of fewer sequences count on the SIMT kernel (tensor counter)
+  int sb = 10;                 // raster super-block of the tensor count's tile order
   Slot slot[2];
 };
 
@@ -363,15 +366,17 @@ void place(Layout& Lo, std::vector<FamHost>& fams, const Types& T, int counter, 
     Lo.F[k].fitch = rows ? m.take<uint8_t>(rows) : nullptr;
     Lo.F[k].scratch = rows ? m.take<uint8_t>(rows) : nullptr;
   }
-  // tensor operands: [family][4 buffers][nslots][4 Lp] rows of pitch
-  Lo.pitch = 0;
-  for (auto& f : fams) Lo.pitch = std::max(Lo.pitch, f.Npad);
+  // tensor operands of the families counted on the tensor cores:
+  // [family][4 buffers][nslots][4 Lp] rows of pitch
+  Lo.pitch = 64;
+  for (auto& f : fams) if (f.tens) Lo.pitch = std::max(Lo.pitch, f.Npad);
   Lo.op_rows = 0;
   for (int k = 0; k < nf; k++) {
     Lo.F[k].oprow0 = (int)Lo.op_rows;
-    Lo.op_rows += (int64_t)4 * fams[k].nslots * 4 * fams[k].Lp;
+    if (fams[k].tens) Lo.op_rows += (int64_t)4 * fams[k].nslots * 4 * fams[k].Lp;
   }
-  Lo.ops = (counter == COVGPU_COUNT_TENSOR && T.need_w) ? m.take<uint16_t>((size_t)Lo.op_rows * Lo.pitch) : nullptr;
+  Lo.ops = (Lo.op_rows > 0 && T.need_w) ? m.take<uint16_t>((size_t)Lo.op_rows * Lo.pitch) : nullptr;
+  (void)counter;
   // counts
   const size_t c0 = m.off;
   for (int k = 0; k < nf; k++)
@@ -475,7 +480,7 @@ static int chunk_launch(covgpu_batch* b, Slot& S, const covgpu_params* p, const 
     for (int I = 0; I < f.nT; I++)
       for (int J = I; J < f.nT; J++) { ti[I * f.nT + J] = n; tl[n++] = TileRC{I, J}; }
     std::vector<int> order;
-    tile_order(f.nT, 10, order);
+    tile_order(f.nT, b->sb, order);
     memcpy(od, order.data(), order.size() * sizeof(int));
   }
   std::vector<int> tree_h(Lo.tree_n, 0);
@@ -607,10 +612,13 @@ static int chunk_launch(covgpu_batch* b, Slot& S, const covgpu_params* p, const 
   const size_t o_up = tb.put(pup.v.data(), pup.v.size() * 4), o_lb = tb.put(plb.v.data(), plb.v.size() * 4);
   Pre prs = prefix(nf, [&](int k) { return fams[k].ns > 0 ? (fams[k].L + 255) / 256 * fams[k].ns : 0; });
   Pre prr = prefix(nf, [&](int k) { return fams[k].ns > 0 ? (fams[k].Lp + 255) / 256 * fams[k].ns : 0; });
-  Pre pprep = prefix(nf, [&](int k) { return fams[k].Npad / 64 * (fams[k].Lp / 32) * fams[k].nslots; });
+  Pre pprep = prefix(nf, [&](int k) {
+    return fams[k].tens ? fams[k].Npad / 64 * (fams[k].Lp / 32) * fams[k].nslots : 0;
+  });
   Pre ptile = prefix(nf, [&](int k) { return fams[k].ntiles * fams[k].nslots; });
-  Pre pt3 = prefix(nf, [&](int k) { return Lo.F[k].nl == 3 ? fams[k].ntiles * fams[k].nslots : 0; });
-  Pre pt1 = prefix(nf, [&](int k) { return Lo.F[k].nl == 1 ? fams[k].ntiles * fams[k].nslots : 0; });
+  Pre pt3 = prefix(nf, [&](int k) { return (fams[k].tens && Lo.F[k].nl == 3) ? fams[k].ntiles * fams[k].nslots : 0; });
+  Pre pt1 = prefix(nf, [&](int k) { return (fams[k].tens && Lo.F[k].nl == 1) ? fams[k].ntiles * fams[k].nslots : 0; });
+  Pre psimt = prefix(nf, [&](int k) { return fams[k].tens ? 0 : fams[k].ntiles * fams[k].nslots; });
   Pre ppm = prefix(nf, [&](int k) { return (fams[k].L + 127) / 128 * fams[k].nslots; });
   Pre pmp = prefix(nf, [&](int k) { return fams[k].nslots; });
   Pre pcx = prefix(nf, [&](int k) { return (fams[k].L + 255) / 256 * fams[k].nslots * nout; });
@@ -619,6 +627,7 @@ static int chunk_launch(covgpu_batch* b, Slot& S, const covgpu_params* p, const 
   const size_t o_rs = tb.put(prs.v.data(), prs.v.size() * 4), o_rr = tb.put(prr.v.data(), prr.v.size() * 4);
   const size_t o_prep = tb.put(pprep.v.data(), pprep.v.size() * 4), o_tile = tb.put(ptile.v.data(), ptile.v.size() * 4);
   const size_t o_t3 = tb.put(pt3.v.data(), pt3.v.size() * 4), o_t1 = tb.put(pt1.v.data(), pt1.v.size() * 4);
+  const size_t o_simt = tb.put(psimt.v.data(), psimt.v.size() * 4);
   const size_t o_pm = tb.put(ppm.v.data(), ppm.v.size() * 4), o_mp = tb.put(pmp.v.data(), pmp.v.size() * 4);
   const size_t o_cx = tb.put(pcx.v.data(), pcx.v.size() * 4), o_sq = tb.put(psq.v.data(), psq.v.size() * 4);
   const size_t o_ap = tb.put(pap.v.data(), pap.v.size() * 4);
@@ -694,7 +703,9 @@ static int chunk_launch(covgpu_batch* b, Slot& S, const covgpu_params* p, const 
     if (wdev) BK(cudaStreamWaitEvent(S.st, S.join, 0));
     // counts and marginals
     if (T.need_w) {
-      if (counter == COVGPU_COUNT_TENSOR) {
+      // the tensor cores count the families at or above the batch's SIMT
+      // threshold, the SIMT kernel the others: the two give the same counts
+      if (pprep.total()) {
         BK(grp_umma_prep(dF, nf, P(o_prep), pprep.total(), Lo.pitch, Lo.ops, S.st));
         const UmmaFam* dU = reinterpret_cast<const UmmaFam*>(S.tab + o_uf);
         for (int nl : {3, 1}) {
@@ -706,8 +717,9 @@ static int chunk_launch(covgpu_batch* b, Slot& S, const covgpu_params* p, const 
           launches++;
         }
         launches++;
-      } else {
-        BK(grp_count_simt(dF, nf, P(o_tile), ptile.total(), false, true, S.st));
+      }
+      if (psimt.total()) {
+        BK(grp_count_simt(dF, nf, P(o_simt), psimt.total(), false, true, S.st));
         launches++;
       }
       BK(grp_marginals(dF, nf, P(o_tile), ptile.total(), P(o_pm), ppm.total(), P(o_mp), pmp.total(), S.st));
@@ -1082,6 +1094,7 @@ extern "C" int covgpu_rscape_families(covgpu_batch* b, const covgpu_params* p, i
     h.nslots = h.ns + 1;
     h.Npad = (f.N + 63) / 64 * 64;
     h.Lw = (f.L + 3) / 4;
+    h.tens = p->counter == COVGPU_COUNT_TENSOR && f.N >= b->simt_below;
     h.gsc = !f.wgt && f.N <= 1000 && f.N > 1;
     h.pb = !f.wgt && f.N > 1000;
     if (h.gsc && f.N > 4096) return bfail(b, 11, "family %d: GSC weights in a batch are for up to 4096 sequences", k);
@@ -1109,13 +1122,14 @@ extern "C" int covgpu_rscape_families(covgpu_batch* b, const covgpu_params* p, i
       const int pn = std::max(pitch, f.Npad);
       // operands of the families already in the chunk grow with the pitch
       size_t grown = bytes;
-      if (pn != pitch && p->counter == COVGPU_COUNT_TENSOR)
-        for (const auto& c : chunk) grown += (size_t)4 * c.nslots * 4 * c.Lp * (pn - pitch) * 2;
-      const size_t add = fam_bytes_hint(f, ntypes, T.need_u, rafs, p->counter == COVGPU_COUNT_TENSOR ? pn : 0);
+      const int pn2 = f.tens ? pn : pitch;
+      if (pn2 != pitch)
+        for (const auto& c : chunk) if (c.tens) grown += (size_t)4 * c.nslots * 4 * c.Lp * (pn2 - pitch) * 2;
+      const size_t add = fam_bytes_hint(f, ntypes, T.need_u, rafs, f.tens ? pn2 : 0);
       if (!chunk.empty() && grown + add > b->budget) break;
       chunk.push_back(f);
       bytes = grown + add;
-      pitch = pn;
+      pitch = pn2;
       k++;
     }
     int s = chunk_launch(b, b->slot[cur], p, fams_in, chunk, T);
@@ -1130,5 +1144,53 @@ extern "C" int covgpu_rscape_families(covgpu_batch* b, const covgpu_params* p, i
     if (s) { drain(); return s; }
   }
   b->ms[2] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return 0;
+}
+
+// the batch's count schedule: families of fewer than simt_below sequences
+// are counted on the SIMT kernel when the tensor counter is asked for (the
+// two give the same counts), and sb is the raster super-block of the tensor
+// count's tile order
+extern "C" int covgpu_batch_set_schedule(covgpu_batch* b, int simt_below, int sb) {
+  if (!b || simt_below < 0 || sb < 1) return 11;
+  b->simt_below = simt_below;
+  b->sb = sb;
+  return 0;
+}
+
+// Schedule autotuner of the batch: runs the caller's families once per
+// (threshold, super-block) pair, each timed as the best of two calls after a
+// warm-up call (host wall clock of the whole call), and keeps the fastest.
+// ms[i * nsb + j] gets each time.
+extern "C" int covgpu_batch_autotune(covgpu_batch* b, const covgpu_params* p, int nfam, const covgpu_family* fams,
+                                     int ntypes, const int* covtypes, int nthr, const int* thr, int nsb,
+                                     const int* sbs, double* ms, int* best_thr, int* best_sb) {
+  if (!b) return 11;
+  if (nthr < 1 || nsb < 1 || !thr || !sbs || nfam < 1) return bfail(b, 11, "bad autotune candidates");
+  std::vector<covgpu_result> res((size_t)nfam * std::max(ntypes, 1));
+  const int keep_thr = b->simt_below, keep_sb = b->sb;
+  double best = INFINITY;
+  int bt = keep_thr, bs = keep_sb;
+  for (int i = 0; i < nthr; i++)
+    for (int j = 0; j < nsb; j++) {
+      if (thr[i] < 0 || sbs[j] < 1) {
+        b->simt_below = keep_thr; b->sb = keep_sb;
+        return bfail(b, 11, "bad autotune candidate (%d, %d)", thr[i], sbs[j]);
+      }
+      b->simt_below = thr[i];
+      b->sb = sbs[j];
+      double t = INFINITY;
+      for (int r = 0; r < 3; r++) {
+        const int s = covgpu_rscape_families(b, p, nfam, fams, ntypes, covtypes, res.data(), nullptr, 0);
+        if (s) { b->simt_below = keep_thr; b->sb = keep_sb; return s; }
+        if (r) t = std::min(t, b->ms[2]);
+      }
+      if (ms) ms[(size_t)i * nsb + j] = t;
+      if (t < best) { best = t; bt = thr[i]; bs = sbs[j]; }
+    }
+  b->simt_below = bt;
+  b->sb = bs;
+  if (best_thr) *best_thr = bt;
+  if (best_sb) *best_sb = bs;
   return 0;
 }

@@ -173,3 +173,24 @@ def test_batch_reports_the_bad_family(covgpu):
     r = b.rscape(fl, ["GTp"], counter=covgpu.TENSOR)
     assert len(r) == 3
     b.close()
+
+
+def test_batch_schedules_give_the_same_results(covgpu):
+    """The count schedule (which families the SIMT kernel counts, the tensor
+    count's raster order) changes no result: the two counters give the same
+    counts.  The autotuner returns one of its candidates."""
+    fams = [family(covgpu, N, L, seed) for N, L, seed in SIZES]
+    fl = [dict(ax=s.ax, parent=s.parent, left=s.left, right=s.right) for s in fams]
+    b = covgpu.Batch()
+    ref = b.rscape(fl, ["GTp", "CHIp"], counter=covgpu.TENSOR, thresh=10.0)
+    for thr, sb in ((0, 4), (1 << 20, 10), (300, 16)):   # all tensor, all SIMT, mixed
+        b.set_schedule(thr, sb)
+        got = b.rscape(fl, ["GTp", "CHIp"], counter=covgpu.TENSOR, thresh=10.0)
+        for k in range(len(fams)):
+            for q in range(2):
+                for key in ref[k][q]:
+                    assert got[k][q][key] == ref[k][q][key], (thr, sb, k, q, key)
+    bt, bs, times = b.autotune(fl[:5], ["GTp"], thr=(0, 200), sb=(6, 10), counter=covgpu.TENSOR)
+    assert len(times) == 4 and (bt, bs) in times
+    assert times[(bt, bs)] == min(times.values())
+    b.close()
