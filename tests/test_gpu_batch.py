@@ -194,3 +194,34 @@ def test_batch_schedules_give_the_same_results(covgpu):
     assert len(times) == 4 and (bt, bs) in times
     assert times[(bt, bs)] == min(times.values())
     b.close()
+
+
+def test_batch_edge_families_and_raf_only(covgpu):
+    """Families of one, two and three sequences in a batch with ordinary
+    ones, against per-family calls; and a batch asked for RAF alone (no
+    weighted counts at all)."""
+    rng = np.random.default_rng(3)
+    fams = [family(covgpu, 40, 90, 31), family(covgpu, 3, 60, 32), family(covgpu, 2, 55, 33),
+            family(covgpu, 150, 70, 34)]
+    one = rng.integers(0, 4, size=(1, 80)).astype(np.uint8)
+    fl = [dict(ax=s.ax, parent=s.parent, left=s.left, right=s.right) for s in fams]
+    fl.insert(1, dict(ax=one))
+    b = covgpu.Batch()
+    got = b.rscape(fl, ["GTp"], counter=covgpu.TENSOR, thresh=10.0)
+    assert got[1][0]["status"] == 2 and got[1][0]["nshuffle"] == 0
+    for k, s in ((0, fams[0]), (2, fams[1]), (3, fams[2]), (4, fams[3])):
+        N, L = s.ax.shape
+        ns = 300 if (N < 4 or L < 40) else (200 if (L < 50 or N * L < 1000) else 20)
+        e = covgpu.Engine(N, L, maxslots=ns + 1, maxnull=ns)
+        e.set_tree(s.parent, s.left, s.right)
+        e.set_alignment(0, s.ax)
+        e.weights_gsc(0, set=True)
+        ref = e.rscape(None, None, ["GTp"], hitcap=1 << 12, counter=covgpu.TENSOR, thresh=10.0)[0]
+        e.close()
+        same(got[k][0], ref, (k, N, L))
+    raf = b.rscape(fl, ["RAFp", "RAF"], counter=covgpu.TENSOR, thresh=10.0)
+    both = b.rscape(fl, ["RAFp", "GTp"], counter=covgpu.TENSOR, thresh=10.0)
+    for k in (0, 2, 3, 4):
+        for key in raf[k][0]:
+            assert raf[k][0][key] == both[k][0][key], (k, key)
+    b.close()
