@@ -137,6 +137,13 @@ int  covgpu_substitutions(covgpu_ctx *ctx, int slot, uint64_t seed, int includeg
 int  covgpu_power(covgpu_ctx *ctx, int ns, const double *subs, const double *prob, const double *subs_join,
                   const double *prob_join, const double *subs_double, const double *prob_double, double *power,
                   double *power_join, double *power_double);
+/* the pair classes of power_SPAIR_AddMI (src/power.c:201-218) from the
+ * weighted counts of the last covgpu_score/covgpu_rscape of slot, without
+ * the pair probabilities on the host: per pair i < j (row-major over the
+ * upper triangle, L(L-1)/2 each) the Watson-Crick fraction pp(AU) + pp(UA) +
+ * pp(CG) + pp(GC), the wobble fraction pp(GU) + pp(UG) and the rest, with
+ * pp = (1e-10 + C)/sum as covgpu_get_probs gives it; any pointer may be NULL */
+int  covgpu_pair_classes(covgpu_ctx *ctx, int slot, double *wcf, double *wobble, double *noncan);
 /* the per-branch conditionals of the last covgpu_simulate: P4 [2(N-1)][4][4]
  * and P16 [2(N-1)][16][16], branch 2v (left child of v) and 2v+1 (right) */
 int  covgpu_sim_tables(covgpu_ctx *ctx, double *P4, double *P16);

@@ -124,6 +124,7 @@ def lib():
         L.covgpu_learned_features.argtypes = [vp, C.POINTER(Params), C.c_double, C.c_int, C.c_int, f32p]
         L.covgpu_rscape_learned.argtypes = [vp, C.POINTER(Params), vp, vp, vp, C.c_double, C.c_int, C.c_int,
                                             C.POINTER(Result), C.POINTER(Hit), C.c_int, C.POINTER(C.c_int)]
+        L.covgpu_pair_classes.argtypes = [vp, C.c_int, vp, vp, vp]
         L.covgpu_batch_create.argtypes = [C.POINTER(vp), C.c_int, C.c_double]
         L.covgpu_batch_destroy.argtypes = [vp]
         L.covgpu_batch_errmsg.argtypes = [vp]
@@ -311,6 +312,14 @@ class Engine:
         outs = [np.zeros(P) for _ in range(3)]
         self._ck(lib().covgpu_power(self.h, ns, *args, *[o.ctypes.data for o in outs]))
         return outs
+
+    def pair_classes(self, slot=0):
+        """(Watson-Crick, wobble, non-canonical) pair fractions of power_SPAIR_AddMI for
+        every pair i < j (row-major), from the last scoring's counts of slot."""
+        P = self.L * (self.L - 1) // 2
+        out = [np.zeros(P) for _ in range(3)]
+        self._ck(lib().covgpu_pair_classes(self.h, slot, *[o.ctypes.data for o in out]))
+        return out
 
     def weights_gsc(self, slot=0, set=True):
         """GSC tree weights of the alignment in slot, computed on the device."""

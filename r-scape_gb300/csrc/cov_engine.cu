@@ -77,6 +77,7 @@ struct covgpu_ctx {
   double *d_hsc = nullptr, *d_hE = nullptr, *d_hp = nullptr;
   int hitcap = 0;
   double* d_full = nullptr;
+  double* d_pcls = nullptr;         // covgpu_pair_classes outputs [3][capL(capL-1)/2]
   UmmaPlan* umma = nullptr;
   FitWork* fitw[MAXOUT] = {};
   // simulator
@@ -212,7 +213,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
                   ctx->d_part1, ctx->d_colx, ctx->d_avg, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status,
                   ctx->d_left, ctx->d_right, ctx->d_lnodes, ctx->d_fitch, ctx->d_scratch, ctx->d_obs, ctx->d_sf,
                   ctx->d_tail, ctx->d_nhits, ctx->d_hi, ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->d_full,
-                  ctx->d_flush, ctx->d_pmdf, ctx->d_colxf, ctx->d_apcf, ctx->d_evt};
+                  ctx->d_flush, ctx->d_pmdf, ctx->d_colxf, ctx->d_apcf, ctx->d_evt, ctx->d_pcls};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (ctx->umma) umma_plan_destroy(ctx->umma);
   for (FitWork* f : ctx->fitw) if (f) fitwork_destroy(f);
@@ -1532,6 +1533,25 @@ extern "C" int covgpu_validate_probs(covgpu_ctx* ctx, double tol) {
   CK(cudaMemcpyAsync(&bad, ctx->d_nhits, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
   CK(cudaStreamSynchronize(ctx->st));
   if (bad) return fail(ctx, 20, "pair probabilities failed validation");
+  return 0;
+}
+
+extern "C" int covgpu_pair_classes(covgpu_ctx* ctx, int slot, double* wcf, double* wobble, double* noncan) {
+  CK(cudaSetDevice(ctx->dev));
+  if (!ctx->cnt_valid || slot < ctx->cnt_first || slot >= ctx->cnt_first + ctx->cnt_nslots)
+    return fail(ctx, 11, "no weighted counts of slot %d on the device", slot);
+  const int L = ctx->L;
+  const int64_t P = (int64_t)L * (L - 1) / 2;
+  if (P < 1) return 0;
+  // three outputs of P values each, for the largest L of the context
+  if (!ctx->d_pcls) CK(dalloc(&ctx->d_pcls, 3 * ((size_t)ctx->capL * (ctx->capL - 1) / 2)));
+  double* d = ctx->d_pcls;
+  const float* cnt = ctx->d_cnt + (size_t)(slot - ctx->cnt_first) * ctx->ntiles * 32 * TPP;
+  CK(launch_pair_classes(cnt, ctx->d_tiles, ctx->ntiles, L, d, d + P, d + 2 * P, ctx->st));
+  if (wcf) CK(cudaMemcpyAsync(wcf, d, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  if (wobble) CK(cudaMemcpyAsync(wobble, d + P, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  if (noncan) CK(cudaMemcpyAsync(noncan, d + 2 * P, P * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
   return 0;
 }
 

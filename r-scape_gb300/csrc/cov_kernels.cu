@@ -804,6 +804,38 @@ k_stats(StatsArgs A) {
   stats_body<CF>(native_grid(), A);
 }
 
+// power_SPAIR_AddMI (src/power.c:201-218) for every pair i < j of one
+// alignment, from its double-float counts: the pair probabilities pp =
+// (1e-10 + C) / sum (the FP64 operations the host fill of mi->pp makes), then
+// the Watson-Crick fraction pp(AU) + pp(UA) + pp(CG) + pp(GC), the wobble
+// fraction pp(GU) + pp(UG) and the rest; written at the row-major index of
+// (i, j) in the upper triangle
+__global__ void __launch_bounds__(256)
+k_pair_classes(const float* __restrict__ cnt, const TileRC* __restrict__ tiles, int L, double* __restrict__ wcf,
+               double* __restrict__ wob, double* __restrict__ non) {
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  const float* C = cnt + (int64_t)t * 32 * TPP;
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k, a = p >> 5, b = p & 31;
+    const int i = tr.I * TP + a, j = tr.J * TP + b;
+    if (!(i < j && j < L)) continue;
+    double c[16], sum = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      c[q] = __dadd_rn(1e-10, __dadd_rn((double)C[(2 * q) * TPP + p], (double)C[(2 * q + 1) * TPP + p]));
+      sum = __dadd_rn(sum, c[q]);
+    }
+    auto pp = [&](int q) { return __ddiv_rn(c[q], sum); };
+    const double w = __dadd_rn(__dadd_rn(__dadd_rn(pp(0 * 4 + 3), pp(3 * 4 + 0)), pp(1 * 4 + 2)), pp(2 * 4 + 1));
+    const double g = __dadd_rn(pp(2 * 4 + 3), pp(3 * 4 + 2));
+    const int64_t n = (int64_t)i * (2 * (int64_t)L - i - 1) / 2 + (j - i - 1);
+    wcf[n] = w;
+    wob[n] = g;
+    non[n] = __dsub_rn(__dsub_rn(1.0, w), g);
+  }
+}
+
 // corr_ValidateProbs (src/correlators.c:1499-1545) for the pair
 // probabilities pp = (1e-10 + C) / (16e-10 + nseff) of one alignment, from
 // its double-float counts: each in [0, 1 + tol], summing to 1 within tol;
@@ -1259,6 +1291,12 @@ cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st) {
   else if (cf == CF_CHI)              k_stats<CF_CHI><<<grid, 256, 0, st>>>(A);
   else if (cf == (CF_G | CF_CHI))     k_stats<CF_G | CF_CHI><<<grid, 256, 0, st>>>(A);
   else                                k_stats<CF_ALL><<<grid, 256, 0, st>>>(A);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_classes(const float* cnt, const TileRC* tiles, int ntiles, int L, double* wcf, double* wob,
+                                double* non, cudaStream_t st) {
+  k_pair_classes<<<ntiles, 256, 0, st>>>(cnt, tiles, L, wcf, wob, non);
   return cudaGetLastError();
 }
 

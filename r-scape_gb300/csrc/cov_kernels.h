@@ -79,6 +79,10 @@ cudaError_t launch_pm_final(const double* part4, const double* partR, int L, int
 cudaError_t launch_ps(const uint8_t* ax, int64_t slot_stride, const double* w, int N, int L, int Lp, int nslots,
                       double* ps, cudaStream_t st);
 cudaError_t launch_stats(const StatsArgs& A, int nslots, cudaStream_t st);
+// power_SPAIR_AddMI's pair classes of one alignment's double-float counts:
+// [L(L-1)/2] each, row-major over i < j
+cudaError_t launch_pair_classes(const float* cnt, const TileRC* tiles, int ntiles, int L, double* wcf, double* wob,
+                                double* non, cudaStream_t st);
 // pair-probability validation of one alignment's double-float counts; *bad set on failure
 cudaError_t launch_validate_pp(const float* cnt, const TileRC* tiles, int ntiles, int L, double tol, int* bad,
                                cudaStream_t st);

@@ -54,3 +54,35 @@ def test_power_matches_oracle(covgpu, oracle):
     q1, qj, qd = e.power(single=curves[0])
     assert np.array_equal(q1, ref1) and np.all(qj == -1.0) and np.all(qd == -1.0)
     e.close()
+
+
+def classes_of(pp, L):
+    """power_SPAIR_AddMI (src/power.c:201-218) on pair probabilities pp[L][L][16]."""
+    iu = np.triu_indices(L, 1)
+    p = pp[iu]
+    w = ((p[:, 3] + p[:, 12]) + p[:, 6]) + p[:, 9]
+    g = p[:, 11] + p[:, 14]
+    return w, g, (1.0 - w) - g
+
+
+@pytest.mark.parametrize("N,L", [(60, 70), (400, 130)])
+def test_pair_classes_match_host_pp_and_oracle(covgpu, oracle, N, L):
+    """The device pair classes equal those computed from the host pair
+    probabilities the drop-in fills (same FP64 operations), and those of the
+    oracle's pair probabilities within 2e-9 (the counts are of 33-bit
+    quantised weights)."""
+    s = covgpu.Synth(N, L, 1.5, L // 6, 2, 5, 12, 0.1, seed=N + L)
+    w = covgpu.weights_pb(s.ax) * np.random.default_rng(3).uniform(0.7, 1.3, N)
+    e = covgpu.Engine(N, L)
+    e.set_weights(w)
+    e.set_alignment(0, s.ax)
+    for counter in (covgpu.SIMT, covgpu.TENSOR):
+        e.score(["GT"], counter=counter)
+        got = e.pair_classes(0)
+        pp = e.get_probs(0, w)[0]
+        for g, h in zip(got, classes_of(pp, L)):
+            assert np.array_equal(g, h)
+        ref = classes_of(oracle.probs(s.ax, w)[0], L)
+        for g, h in zip(got, ref):
+            assert np.max(np.abs(g - h)) <= 2e-9
+    e.close()
