@@ -178,9 +178,9 @@ extern "C" int covgpu_batch_create(covgpu_batch** ret, int device, double mem_gb
   BK(cudaMemGetInfo(&fr, &tot));
   const double want = mem_gb > 0.0 ? mem_gb * 1e9 : 0.25 * (double)fr;
   b->budget = (size_t)std::max(1.6e7, std::min(want, 0.8 * (double)fr)) / 2;
-  BK(cudaMalloc(&b->d_logtab, LOGTAB_N * sizeof(float4)));
+  BK(cudaMalloc(&b->d_logtab, LOGTAB_TOT * sizeof(float4)));
   {
-    float4 tab[LOGTAB_N];
+    float4 tab[LOGTAB_TOT];
     logtab_host(tab);
     BK(cudaMemcpy(b->d_logtab, tab, sizeof(tab), cudaMemcpyHostToDevice));
   }

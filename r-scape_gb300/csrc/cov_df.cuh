@@ -102,20 +102,19 @@ __device__ __forceinline__ df df_max(df a, df b) { return df_lt(a, b) ? b : a; }
 //   ln a = k ln 2 - ln r_j + ln(1 + t) + ln(1 + lo/hi),
 //   ln(1 + t) = t - t^2/2 + t^3/3 - t^4/4 + t^5/5 (next term < 1e-15),
 //   ln(1 + lo/hi) = lo/hi (next term < 2e-15).
-//   k ln 2 is formed from three pieces of ln 2, the first two with 16-bit
-//   significands, so k times each is exact for |k| < 256.
+//   k ln 2 comes from a second table indexed by hi's biased exponent
+//   (256 entries of k ln 2 as hi + lo, two to a float4), so it costs one
+//   shared load instead of a three-piece product.
 // ---------------------------------------------------------------------------
-constexpr int LOGTAB_N = 128;
-constexpr float LN2_A = 0.693145751953125f;        // 16 significant bits
-constexpr float LN2_B = 1.4285906217992306e-06f;   // 16 significant bits
-constexpr float LN2_C = 1.619851018665656e-11f;
+constexpr int LOGTAB_N = 128;                    // the 1/c_j entries
+constexpr int LOGTAB_TOT = LOGTAB_N + 256 / 2;   // + the k ln 2 entries
 
 __device__ __forceinline__ df df_log(df a, const float4* __restrict__ tab) {
   const int bits = __float_as_int(a.hi);
-  const int k = (bits >> 23) - 127;
   const int j = (bits >> 16) & (LOGTAB_N - 1);
   const float m = __int_as_float((bits & 0x007FFFFF) | 0x3F800000);
   const float4 T = tab[j];
+  const float2 K = reinterpret_cast<const float2*>(tab + LOGTAB_N)[((unsigned)bits >> 23) & 255u];   // k ln 2
   const float p = __fmul_rn(m, T.x);
   const float pe = fmaf(m, T.x, -p);
   const df t = fast_two_sum(__fsub_rn(p, 1.0f), pe);   // p - 1 is exact (p within 2^-7 of 1)
@@ -125,14 +124,11 @@ __device__ __forceinline__ df df_log(df a, const float4* __restrict__ tab) {
   const float corr = __fdividef(a.lo, a.hi);
   const float low = __fadd_rn(__fsub_rn(fmaf(-t.hi, t.lo, t.lo), __fmul_rn(0.5f, s2e)), __fadd_rn(poly, corr));
   const df l1p = fast_two_sum(t.hi, __fmul_rn(-0.5f, s2));
-  const float kf = (float)k;
-  df kl = two_sum(__fmul_rn(kf, LN2_A), __fmul_rn(kf, LN2_B));
-  kl.lo = fmaf(kf, LN2_C, kl.lo);
-  df r = df_add(kl, {T.y, T.z});
+  const df r = df_add({K.x, K.y}, {T.y, T.z});
   return df_add(r, {l1p.hi, __fadd_rn(l1p.lo, low)});
 }
 
-// the table of df_log (LOGTAB_N entries), made on the host in FP64; each
+// the table of df_log (LOGTAB_TOT float4), made on the host in FP64; each
 // context keeps a copy in global memory and kernels stage it in shared
 // memory (the index differs from lane to lane)
 void logtab_host(float4* tab);

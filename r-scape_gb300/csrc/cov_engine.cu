@@ -171,9 +171,9 @@ extern "C" int covgpu_create(covgpu_ctx** ret, int device, int N, int L, int max
   CK(dalloc(&ctx->d_limbf, (size_t)3 * N));
   CK(dalloc(&ctx->d_wd, N));
   CK(dalloc(&ctx->d_cnt, S * ntl * 32 * TPP));
-  CK(dalloc(&ctx->d_logtab, LOGTAB_N));
+  CK(dalloc(&ctx->d_logtab, LOGTAB_TOT));
   {
-    float4 tab[LOGTAB_N];
+    float4 tab[LOGTAB_TOT];
     logtab_host(tab);
     CK(cudaMemcpy(ctx->d_logtab, tab, sizeof(tab), cudaMemcpyHostToDevice));
   }

@@ -744,8 +744,9 @@ __device__ __forceinline__ void stats_body(
   const float4* lpi = A.lpi + (int64_t)slot * A.Lp * 4;
   const double* meanp = A.meanp + slot * 4;
   __shared__ float2 vs[MAXOUT][TP][TP + 1];   // the tile's scores, [q][a][b]
-  __shared__ float4 tab[LOGTAB_N];
-  if (tid < LOGTAB_N) tab[tid] = A.logtab[tid];
+  __shared__ float4 tab[LOGTAB_TOT];
+  static_assert(LOGTAB_TOT <= 256, "one table entry per thread");
+  if (tid < LOGTAB_TOT) tab[tid] = A.logtab[tid];
   __syncthreads();
 #pragma unroll 1
   for (int k = 0; k < 4; k++) {
@@ -1420,6 +1421,16 @@ void logtab_host(float4* tab) {
     const double nl = -std::log((double)r);
     const float hi = (float)nl;
     tab[j] = make_float4(r, hi, (float)(nl - (double)hi), 0.f);
+  }
+  // k ln 2 for the biased exponent e = k + 127, ln 2 as a double pair
+  const double ln2_hi = 0.6931471805599453, ln2_lo = 2.3190468138462996e-17;
+  float* kl = reinterpret_cast<float*>(tab + LOGTAB_N);
+  for (int e = 0; e < 256; e++) {
+    const double k = (double)(e - 127);
+    const double v = k * ln2_hi;   // |k| < 2^8: error below 2^-52 |v|
+    const float hi = (float)v;
+    kl[2 * e] = hi;
+    kl[2 * e + 1] = (float)((v - (double)hi) + k * ln2_lo);
   }
 }
 

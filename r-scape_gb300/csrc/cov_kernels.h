@@ -15,7 +15,7 @@ struct StatsArgs {
   const double* pm;         // [slot][Lp][4]
   const float2* pmdf;       // [slot][Lp][4] pm as double-float (hi, lo)
   const float4* lpi;        // [slot][Lp][4] {ln pm, 1/pm} as double-floats
-  const float4* logtab;     // df_log's table (LOGTAB_N entries)
+  const float4* logtab;     // df_log's table (LOGTAB_TOT entries)
   const double* meanp;      // [slot][4]
   float2*       cov;        // [slot][nout][tile][TPP] scores as double-float (hi, lo)
   double*       part1;      // [slot][nout][nT][nT][TP]
