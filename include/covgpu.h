@@ -288,6 +288,7 @@ int  covgpu_flush_l2(covgpu_ctx *ctx);
 #define COVGPU_NFEAT 64
 #define COVGPU_NOUT 3
 #define COVGPU_MLP_NPARAM 148995
+#define COVGPU_MLP_MAXMEM 16   /* members of an ensemble */
 typedef struct covgpu_mlp covgpu_mlp;
 
 /* the alignment part (features 0-46; 47-63 are set to 0) of the learned
@@ -319,6 +320,12 @@ int  covgpu_mlp_set_norm(covgpu_mlp *net, const float *xmean, const float *xstd,
                          const float *ystd, const float *xlo, const float *xhi);
 int  covgpu_mlp_get_norm(const covgpu_mlp *net, float *xmean, float *xstd, float *ymean, float *ystd, float *xlo,
                          float *xhi);
+/* an ensemble: nmem parameter sets params[nmem][COVGPU_MLP_NPARAM] (nmem
+ * 0..COVGPU_MLP_MAXMEM, 0 = none) sharing this network's standardisation;
+ * covgpu_mlp_forward (and so covgpu_rscape_learned) then averages the
+ * members' standardised outputs in member order.  Training and gradients
+ * keep using the network's own parameters. */
+int  covgpu_mlp_set_members(covgpu_mlp *net, const float *params, int nmem);
 /* 1 if every feature lies inside the training range */
 int  covgpu_mlp_in_range(const covgpu_mlp *net, const float *feat);
 /* Y[n][3] = network(X[n][64]) */

@@ -110,6 +110,7 @@ def lib():
         L.covgpu_mlp_errmsg.restype = C.c_char_p
         L.covgpu_mlp_set_params.argtypes = [vp, f32p]
         L.covgpu_mlp_get_params.argtypes = [vp, f32p]
+        L.covgpu_mlp_set_members.argtypes = [vp, vp, C.c_int]
         L.covgpu_mlp_set_norm.argtypes = [vp, f32p, f32p, f32p, f32p, vp, vp]
         L.covgpu_mlp_get_norm.argtypes = [vp, f32p, f32p, f32p, f32p, f32p, f32p]
         L.covgpu_mlp_in_range.argtypes = [vp, f32p]
@@ -485,6 +486,13 @@ class MLP:
 
     def set_params(self, p):
         self._ck(lib().covgpu_mlp_set_params(self.h, np.ascontiguousarray(p, dtype=np.float32)))
+
+    def set_members(self, params):
+        """An ensemble: params[k] (k < 16) are the members' parameters; forward
+        averages their standardised outputs.  An empty list restores the
+        single network."""
+        P = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(-1, NPARAM))
+        self._ck(lib().covgpu_mlp_set_members(self.h, P.ctypes.data if len(P) else None, len(P)))
 
     def set_norm(self, xmean, xstd, ymean, ystd, xlo=None, xhi=None):
         f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32)

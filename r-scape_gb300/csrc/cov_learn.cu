@@ -357,10 +357,18 @@ __global__ void k_gather(const float* __restrict__ X, const float* __restrict__ 
   }
 }
 
-__global__ void k_denorm(const float* __restrict__ Yp, int n, const float* __restrict__ nrm, float* __restrict__ Y) {
+// Y = (Yp scale) ystd + ymean; scale = 1 / members for an ensemble's sum
+__global__ void k_denorm(const float* __restrict__ Yp, int n, const float* __restrict__ nrm, float scale,
+                         float* __restrict__ Y) {
   const float *ym = nrm + 2 * kNFeat, *ys = ym + kOut;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < n * kOut) Y[e] = Yp[e] * ys[e % kOut] + ym[e % kOut];
+  if (e < n * kOut) Y[e] = (Yp[e] * scale) * ys[e % kOut] + ym[e % kOut];
+}
+
+// the members' standardised outputs summed in member order
+__global__ void k_accum(const float* __restrict__ Yp, int n, bool first, float* __restrict__ Yacc) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) Yacc[e] = first ? Yp[e] : Yacc[e] + Yp[e];
 }
 
 // dY = 2 (Y - T) / (B * 3); loss = mean squared error.  With a counter:
@@ -438,6 +446,12 @@ struct covgpu_mlp {
   float *Xin = nullptr, *Xb = nullptr, *Tb = nullptr, *Yp = nullptr, *dY = nullptr, *Yout = nullptr;
   float *Z[3] = {}, *H[3] = {}, *D[3] = {};
   int* counter = nullptr;
+  // an ensemble: nmem parameter sets (FP32 and BF16) whose outputs the
+  // forward pass averages; the primary parameters p stay the trained ones
+  int nmem = 0;
+  float* mp = nullptr;
+  __nv_bfloat16* mpb = nullptr;
+  float* Yacc = nullptr;
 };
 
 static int mfail(covgpu_mlp* net, int code, const char* fmt, ...) {
@@ -459,17 +473,19 @@ static cudaError_t malloc_n(T** p, size_t n) {
   return cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T));
 }
 
-static void enqueue_forward(covgpu_mlp* net, int B) {
+// the network with parameters p (FP32 biases) and pb (BF16 weights)
+static void enqueue_forward(covgpu_mlp* net, int B, const float* p, const __nv_bfloat16* pb) {
   cudaStream_t st = net->st;
-  gemm<float, __nv_bfloat16, EPI_SILU>(st, net->Xb, kNFeat, 1, net->pb + oW1, 1, kNFeat, B, kHid, kNFeat,
-                                       net->p + ob1, nullptr, net->H[0], net->Z[0]);
-  gemm<float, __nv_bfloat16, EPI_SILU>(st, net->H[0], kHid, 1, net->pb + oW2, 1, kHid, B, kHid, kHid, net->p + ob2,
-                                       nullptr, net->H[1], net->Z[1]);
-  gemm<float, __nv_bfloat16, EPI_SILU>(st, net->H[1], kHid, 1, net->pb + oW3, 1, kHid, B, kHid, kHid, net->p + ob3,
-                                       nullptr, net->H[2], net->Z[2]);
-  gemm<float, __nv_bfloat16, EPI_PLAIN>(st, net->H[2], kHid, 1, net->pb + oW4, 1, kHid, B, kOut, kHid,
-                                        net->p + ob4, nullptr, net->Yp);
+  gemm<float, __nv_bfloat16, EPI_SILU>(st, net->Xb, kNFeat, 1, pb + oW1, 1, kNFeat, B, kHid, kNFeat, p + ob1,
+                                       nullptr, net->H[0], net->Z[0]);
+  gemm<float, __nv_bfloat16, EPI_SILU>(st, net->H[0], kHid, 1, pb + oW2, 1, kHid, B, kHid, kHid, p + ob2, nullptr,
+                                       net->H[1], net->Z[1]);
+  gemm<float, __nv_bfloat16, EPI_SILU>(st, net->H[1], kHid, 1, pb + oW3, 1, kHid, B, kHid, kHid, p + ob3, nullptr,
+                                       net->H[2], net->Z[2]);
+  gemm<float, __nv_bfloat16, EPI_PLAIN>(st, net->H[2], kHid, 1, pb + oW4, 1, kHid, B, kOut, kHid, p + ob4, nullptr,
+                                        net->Yp);
 }
+static void enqueue_forward(covgpu_mlp* net, int B) { enqueue_forward(net, B, net->p, net->pb); }
 
 // gradients into net->g, from dY
 static void enqueue_backward(covgpu_mlp* net, int B) {
@@ -503,7 +519,7 @@ extern "C" void covgpu_mlp_destroy(covgpu_mlp* net) {
   cudaSetDevice(net->dev);
   void* bufs[] = {net->p, net->m, net->v, net->g, net->pb, net->nrm, net->hyper, net->Xin, net->Xb, net->Tb,
                   net->Yp, net->dY, net->Yout, net->Z[0], net->Z[1], net->Z[2], net->H[0], net->H[1], net->H[2],
-                  net->D[0], net->D[1], net->D[2], net->counter};
+                  net->D[0], net->D[1], net->D[2], net->counter, net->mp, net->mpb, net->Yacc};
   for (void* b : bufs) if (b) cudaFree(b);
   if (net->st) cudaStreamDestroy(net->st);
   delete net;
@@ -555,6 +571,29 @@ extern "C" int covgpu_mlp_set_params(covgpu_mlp* net, const float* params) {
   k_to_bf16<<<(kNParam + 255) / 256, 256, 0, net->st>>>(net->p, net->pb, kNParam);
   MCK(cudaGetLastError());
   MCK(cudaStreamSynchronize(net->st));
+  return 0;
+}
+
+extern "C" int covgpu_mlp_set_members(covgpu_mlp* net, const float* params, int nmem) {
+  MCK(cudaSetDevice(net->dev));
+  if (nmem < 0 || nmem > COVGPU_MLP_MAXMEM) return mfail(net, 11, "%d members outside 0..%d", nmem, COVGPU_MLP_MAXMEM);
+  if (nmem > 0 && !params) return mfail(net, 11, "no member parameters");
+  for (size_t k = 0; k < (size_t)nmem * kNParam; k++)
+    if (!std::isfinite(params[k])) return mfail(net, 11, "member %d parameter %d is not finite", (int)(k / kNParam),
+                                                (int)(k % kNParam));
+  MCK(cudaStreamSynchronize(net->st));
+  if (net->mp) cudaFree(net->mp);
+  if (net->mpb) cudaFree(net->mpb);
+  if (net->Yacc) cudaFree(net->Yacc);
+  net->mp = nullptr; net->mpb = nullptr; net->Yacc = nullptr; net->nmem = 0;
+  if (nmem == 0) return 0;
+  const size_t n = (size_t)nmem * kNParam;
+  MCK(malloc_n(&net->mp, n)); MCK(malloc_n(&net->mpb, n)); MCK(malloc_n(&net->Yacc, (size_t)net->cap * kOut));
+  MCK(cudaMemcpyAsync(net->mp, params, n * sizeof(float), cudaMemcpyHostToDevice, net->st));
+  k_to_bf16<<<(int)((n + 255) / 256), 256, 0, net->st>>>(net->mp, net->mpb, (int)n);
+  MCK(cudaGetLastError());
+  MCK(cudaStreamSynchronize(net->st));
+  net->nmem = nmem;
   return 0;
 }
 
@@ -614,8 +653,17 @@ extern "C" int covgpu_mlp_forward(covgpu_mlp* net, const float* X, int n, float*
                         cudaMemcpyHostToDevice, net->st));
     k_gather<<<std::min(1024, (B * kNFeat + 255) / 256), 256, 0, net->st>>>(net->Xin, nullptr, nullptr, nullptr, 1,
                                                                             B, net->nrm, net->Xb, nullptr);
-    enqueue_forward(net, B);
-    k_denorm<<<(B * kOut + 255) / 256, 256, 0, net->st>>>(net->Yp, B, net->nrm, net->Yout);
+    if (net->nmem == 0) {
+      enqueue_forward(net, B);
+      k_denorm<<<(B * kOut + 255) / 256, 256, 0, net->st>>>(net->Yp, B, net->nrm, 1.f, net->Yout);
+    } else {
+      for (int k = 0; k < net->nmem; k++) {
+        enqueue_forward(net, B, net->mp + (size_t)k * kNParam, net->mpb + (size_t)k * kNParam);
+        k_accum<<<(B * kOut + 255) / 256, 256, 0, net->st>>>(net->Yp, B * kOut, k == 0, net->Yacc);
+      }
+      k_denorm<<<(B * kOut + 255) / 256, 256, 0, net->st>>>(net->Yacc, B, net->nrm, 1.f / (float)net->nmem,
+                                                            net->Yout);
+    }
     MCK(cudaGetLastError());
     MCK(cudaMemcpyAsync(Y + (size_t)r0 * kOut, net->Yout, (size_t)B * kOut * sizeof(float), cudaMemcpyDeviceToHost,
                         net->st));

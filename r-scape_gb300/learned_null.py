@@ -243,18 +243,32 @@ def train_selected(X, T, grid_epochs=(5, 10, 20, 40, 80, 160), grid_wd=(1e-4, 1e
                      train_rows=len(X), val_rows=len(va))
 
 
-def save(net, path, nquick):
+def train_members(X, T, n, epochs, wd, batch=256, lr=2e-3, seed=1, log=None):
+    """n networks with the same setting on every family, seeds seed..seed+n-1
+    (one standardisation, that of the data)"""
+    return [train(X, T, epochs=epochs, batch=batch, lr=lr, wd=wd, seed=seed + k, log=log)[0] for k in range(n)]
+
+
+def save(net, path, nquick, members=None):
+    """The network's standardisation and parameters; with members (networks
+    trained on the same standardisation) params holds one row per member."""
     xm, xs, ym, ys, lo, hi = net.norm()
-    np.savez_compressed(path, params=net.params(), xmean=xm, xstd=xs, ymean=ym, ystd=ys, xlo=lo, xhi=hi,
+    params = np.stack([m.params() for m in members]) if members else net.params()
+    np.savez_compressed(path, params=params, xmean=xm, xstd=xs, ymean=ym, ystd=ys, xlo=lo, xhi=hi,
                         nquick=np.int32(nquick))
 
 
 def load(path, batch_cap=512):
+    """A saved network; a file with several parameter rows is an ensemble
+    (covgpu_mlp_set_members), its first row the primary parameters."""
     cg = _covgpu()
     z = np.load(path)
     net = cg.MLP(batch_cap=batch_cap)
-    net.set_params(z["params"])
+    P = np.asarray(z["params"], dtype=np.float32)
+    net.set_params(P[0] if P.ndim == 2 else P)
     net.set_norm(z["xmean"], z["xstd"], z["ymean"], z["ystd"], z["xlo"], z["xhi"])
+    if P.ndim == 2 and len(P) > 1:
+        net.set_members(P)
     return net
 
 
@@ -360,6 +374,8 @@ def main(argv=None):
     t.add_argument("--absolute-summary", action="store_true",
                    help="treat every data file as holding the quick-null summary as absolute scores")
     t.add_argument("--lr", type=float, default=2e-3)
+    t.add_argument("--members", type=int, default=1,
+                   help="train this many networks (seeds 1..) with the selected setting and save them as an ensemble")
     t.add_argument("--out", required=True)
     e = sub.add_parser("eval")
     e.add_argument("--net", required=True)
@@ -380,8 +396,12 @@ def main(argv=None):
         except ValueError as e:
             raise SystemExit(str(e))
         net, info = train_selected(X, T, batch=a.batch, lr=a.lr, log=sys.stderr)
-        save(net, a.out, nquick)
-        print(json.dumps(dict(rows=len(X), **info)))
+        members = None
+        if a.members > 1:
+            members = [net] + train_members(X, T, a.members - 1, info["epochs"], info["wd"], batch=a.batch,
+                                            lr=a.lr, seed=2, log=sys.stderr)
+        save(net, a.out, nquick, members)
+        print(json.dumps(dict(rows=len(X), members=a.members, **info)))
     else:
         net = load(a.net)
         rows = evaluate(net, a.first, a.count, a.nnull, nquick=a.nquick, few=a.few, log=sys.stderr)

@@ -91,6 +91,38 @@ def test_network_forward_and_gradient_match_oracle(covgpu, oracle):
     net.close()
 
 
+def test_ensemble_forward_is_the_members_mean(covgpu, oracle):
+    """covgpu_mlp_set_members: the forward pass averages the members'
+    outputs (the oracle's FP64 network per member, then the mean); training
+    parameters are untouched, and clearing the members restores them."""
+    rng = np.random.default_rng(12)
+    net = covgpu.MLP(batch_cap=64, seed=5)
+    xm = rng.standard_normal(64).astype(np.float32)
+    xs = (0.5 + rng.random(64)).astype(np.float32)
+    ym = np.array([3.0, -0.5, 0.2], np.float32)
+    ys = np.array([1.5, 0.6, 0.3], np.float32)
+    net.set_norm(xm, xs, ym, ys)
+    nrm = np.concatenate([xm, xs, ym, ys]).astype(np.float32)
+    X = (xm + xs * rng.standard_normal((150, 64))).astype(np.float32)   # 150 rows: three batches of 64
+    single = net.forward(X)
+    p0 = net.params()
+    members = []
+    for k in range(3):
+        m = covgpu.MLP(batch_cap=8, seed=20 + k)
+        members.append(m.params())
+        m.close()
+    net.set_members(members)
+    Y = net.forward(X)
+    Yr = np.mean([oracle.mlp_forward(p, nrm, X) for p in members], axis=0)
+    assert np.allclose(Y, Yr, rtol=1e-4, atol=1e-4 * np.abs(Yr).max()), np.abs(Y - Yr).max()
+    assert np.array_equal(net.params(), p0)
+    with pytest.raises(RuntimeError):
+        net.set_members(np.zeros((17, covgpu.NPARAM), np.float32))
+    net.set_members([])
+    assert np.array_equal(net.forward(X), single)
+    net.close()
+
+
 def test_training_is_reproducible_and_fits(covgpu):
     rng = np.random.default_rng(4)
     X = rng.standard_normal((2048, 64)).astype(np.float32)
