@@ -159,16 +159,20 @@ def test_evalue_errors():
 
 
 def test_shipped_network_file(oracle):
-    """The trained network shipped with the package: complete, finite, and
-    its training range contains its own mean features."""
-    z = np.load(os.path.join(ROOT, "r-scape_gb300", "learned_null_gtp.npz"))
-    assert z["params"].shape == (148995,) and np.all(np.isfinite(z["params"]))
-    assert int(z["nquick"]) >= 1
-    assert np.all(z["xstd"] > 0) and np.all(z["ystd"] > 0)
-    assert np.all(z["xlo"] <= z["xmean"]) and np.all(z["xmean"] <= z["xhi"])
-    nrm = np.concatenate([z["xmean"], z["xstd"], z["ymean"], z["ystd"]]).astype(np.float32)
-    y = oracle.mlp_forward(z["params"], nrm, z["xmean"][None, :])
-    assert np.all(np.isfinite(y)) and np.all(np.abs(y) < 5)
+    """The trained networks shipped with the package: complete, finite, and
+    their training range contains their own mean features; an ensemble file
+    holds one parameter row per member (at most 16), each a working network."""
+    for name in ("learned_null_gtp.npz", "learned_null_gtp_q10.npz"):
+        z = np.load(os.path.join(ROOT, "r-scape_gb300", name))
+        P = np.atleast_2d(z["params"])
+        assert P.shape[1:] == (148995,) and 1 <= len(P) <= 16 and np.all(np.isfinite(P))
+        assert int(z["nquick"]) >= 1
+        assert np.all(z["xstd"] > 0) and np.all(z["ystd"] > 0)
+        assert np.all(z["xlo"] <= z["xmean"]) and np.all(z["xmean"] <= z["xhi"])
+        nrm = np.concatenate([z["xmean"], z["xstd"], z["ymean"], z["ystd"]]).astype(np.float32)
+        for p in P:
+            y = oracle.mlp_forward(p, nrm, z["xmean"][None, :])
+            assert np.all(np.isfinite(y)) and np.all(np.abs(y) < 5)
 
 
 def test_training_data_conversion(tmp_path):
