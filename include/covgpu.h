@@ -241,6 +241,15 @@ int  covgpu_hist_full(covgpu_ctx *ctx, const double *COV, double bmin, double w,
  * times Nt tests; Eval full L x L (may be NULL); pairs with E < thresh */
 int  covgpu_evalue_full(covgpu_ctx *ctx, const double *COV, const void *h, const double *survfit, double Nt,
                         double thresh, double *Eval, covgpu_hit *hits, int hitcap, int *nhit);
+/* covgpu_evalue_full with the two-set test and --structured
+ * (cov_CreateHitList, src/covariation.c:828-870): pair n = i (2L - i - 1)/2
+ * + j - i - 1 takes Nb tests when bit n of bpmask (may be NULL) is set; any
+ * other pair takes expBP tests while fewer than expBP pairs before it in
+ * scan order are hits (expBP <= 0: never), else Nt.  Hits come in scan
+ * order. */
+int  covgpu_evalue_sets(covgpu_ctx *ctx, const double *COV, const void *h, const double *survfit, double Nt,
+                        double Nb, double expBP, const uint32_t *bpmask, double thresh, double *Eval,
+                        covgpu_hit *hits, int hitcap, int *nhit);
 
 /* APC (actype 0) or ASC (1) of a device-resident L x L score matrix (both
  * triangles; the diagonal is ignored) into the device buffer d_out (diagonal

@@ -92,6 +92,21 @@ typedef enum { NAIVE = 0, NULLPHYLO = 1, GIVENNULL = 2 } STATSMETHOD;
 typedef enum { GIVSS = 0, FOLDSS = 1, RANSS = 2 } MODE;
 typedef enum { SAMPLE_CONTACTS = 0, SAMPLE_BP = 1, SAMPLE_WC = 2, SAMPLE_ALL = 3 } SAMPLESIZE;
 typedef enum { Eval = 0 } THRESHTYPE;
+/* contact types (BPTYPE, lib/R-view/src/rview_contacts.h:22-62): the 32
+ * base-pair families 0..31 (WWc = 0), then these three */
+typedef enum { WWc = 0, STACKED = 32, CONTACT = 33, BPNONE = 34 } BPTYPE;
+
+/* the fields of CNT and CLIST (rview_contacts.h:65-110) read on this path:
+ * contact h joins alignment positions cnt[h].i < cnt[h].j (1-based) */
+typedef struct cnt_s {
+  int64_t i, j;
+  BPTYPE  bptype;
+} CNT;
+typedef struct clist_s {
+  int   ncnt;
+  int   mind;     /* with msa2pdb: pairs closer than mind in the PDB are not ranked */
+  CNT  *cnt;
+} CLIST;
 
 struct mutual_s {
   int64_t       alen;
@@ -181,6 +196,8 @@ struct data_s {
   double           tol;
   int              verbose;
   char            *errbuf;       /* caller-provided, >= 256 bytes */
+  CLIST           *clist;        /* the given structure's contacts (may be NULL: none) */
+  int             *msa2pdb;      /* [alen] PDB position of each column, -1 for none (may be NULL) */
 };
 
 #define MAX_EVAL 1000

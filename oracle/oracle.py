@@ -42,7 +42,9 @@ class Params(C.Structure):
     _fields_ = [("covtype", C.c_int), ("covclass", C.c_int), ("nseqthresh", C.c_int), ("alenthresh", C.c_int),
                 ("nshuffle", C.c_int), ("thresh", C.c_double), ("bmin", C.c_double), ("w0", C.c_double),
                 ("hpts", C.c_int), ("pmass", C.c_double), ("fracfit", C.c_double), ("doexpfit", C.c_int),
-                ("tol", C.c_double), ("seed", C.c_uint64), ("allow", C.c_double * 16)]
+                ("tol", C.c_double), ("seed", C.c_uint64), ("allow", C.c_double * 16),
+                ("samplesize", C.c_int), ("ncnt", C.c_int), ("cnt_i", C.c_void_p), ("cnt_j", C.c_void_p),
+                ("cnt_type", C.c_void_p), ("mind", C.c_int), ("msa2pdb", C.c_void_p), ("expBP", C.c_double)]
 
 
 class Result(C.Structure):
@@ -52,7 +54,8 @@ class Result(C.Structure):
                 ("sc_thresh", C.c_double), ("Nt", C.c_uint64), ("nhit", C.c_int),
                 ("h_bmin", C.c_double), ("h_w", C.c_double), ("h_nb", C.c_int), ("h_imin", C.c_int),
                 ("h_imax", C.c_int), ("h_cmin", C.c_int), ("h_n", C.c_uint64), ("h_Nc", C.c_uint64),
-                ("h_No", C.c_uint64), ("h_xmin", C.c_double), ("h_xmax", C.c_double), ("h_phi", C.c_double)]
+                ("h_No", C.c_uint64), ("h_xmin", C.c_double), ("h_xmax", C.c_double), ("h_phi", C.c_double),
+                ("sc_nbp", C.c_double), ("Nb", C.c_uint64)]
 
 
 def build(force=False):
@@ -293,9 +296,18 @@ def simulate(tree, L, ct, P4, P16, pi4, pi16, root, gap_rate, gap_mean, seed, re
     return out.reshape(N, L)
 
 
+SAMPLE_CONTACTS, SAMPLE_BP, SAMPLE_WC, SAMPLE_ALL = 0, 1, 2, 3
+WWc, STACKED, CONTACT, BPNONE = 0, 32, 33, 34
+
+
 def params(**kw):
+    """orc_params_t with R-scape's defaults, overridden by kw.  contacts =
+    [(i, j, bptype), ...] (1-based alignment positions) and msa2pdb (an
+    int array over the columns, -1 where a column has no PDB position) are
+    kept alive on the returned object."""
     p = Params()
     lib().orc_params_default(C.byref(p))
+    keep = []
     for k, v in kw.items():
         if k == "covtype" and isinstance(v, str):
             v = covtype_code(v)
@@ -303,7 +315,21 @@ def params(**kw):
             for i in range(16):
                 p.allow[i] = float(v[i])
             continue
+        if k == "contacts":
+            c = np.asarray(v, dtype=np.int64).reshape(-1, 3)
+            ci, cj = np.ascontiguousarray(c[:, 0]), np.ascontiguousarray(c[:, 1])
+            ct = np.ascontiguousarray(c[:, 2].astype(np.int32))
+            keep += [ci, cj, ct]
+            p.ncnt = len(c)
+            p.cnt_i, p.cnt_j, p.cnt_type = ci.ctypes.data, cj.ctypes.data, ct.ctypes.data
+            continue
+        if k == "msa2pdb":
+            m = np.ascontiguousarray(v, dtype=np.int32)
+            keep.append(m)
+            p.msa2pdb = m.ctypes.data
+            continue
         setattr(p, k, v)
+    p._keep = keep
     return p
 
 

@@ -915,21 +915,72 @@ null_add(orc_hist_t *cum, const orc_hist_t *h)
   return cum;
 }
 
-/* cov_SignificantPairs_Ranking histogram part, src/covariation.c:414-457
- * (no PDB, one-set test: every pair goes to ha and ht). */
+/* the contact predicates of the two-set test (CMAP_IsContactLocal,
+ * CMAP_IsBPLocal, CMAP_IsWCLocal, lib/R-view/src/rview_contacts.c:537-574):
+ * does any contact (i, j) (1-based, either order) satisfy the sample's rule */
+static int
+cnt_select(const orc_params_t *p, int64_t i, int64_t j)
+{
+  int64_t ii = (i < j) ? i : j, jj = (i < j) ? j : i;
+  int h;
+  for (h = 0; h < p->ncnt; h++) {
+    if (p->cnt_i[h] != ii || p->cnt_j[h] != jj) continue;
+    switch (p->samplesize) {
+      case ORC_SAMPLE_CONTACTS: return 1;
+      case ORC_SAMPLE_BP:       if (p->cnt_type[h] < ORC_STACKED) return 1; break;
+      case ORC_SAMPLE_WC:       if (p->cnt_type[h] == ORC_WWc) return 1; break;
+      default:                  return 0;
+    }
+  }
+  return 0;
+}
+
+/* CMAP_GetBPTYPE (rview_contacts.c:523-535): the type of the first contact
+ * (i, j), BPNONE if none */
+static int
+cnt_type(const orc_params_t *p, int64_t i, int64_t j)
+{
+  int64_t ii = (i < j) ? i : j, jj = (i < j) ? j : i;
+  int h;
+  for (h = 0; h < p->ncnt; h++)
+    if (p->cnt_i[h] == ii && p->cnt_j[h] == jj) return p->cnt_type[h];
+  return ORC_BPNONE;
+}
+
+/* cov_CreateHitList's isbp (src/covariation.c:836-841) */
+static int
+cnt_isbp(const orc_params_t *p, int bptype)
+{
+  switch (p->samplesize) {
+    case ORC_SAMPLE_CONTACTS: return bptype < ORC_BPNONE;
+    case ORC_SAMPLE_BP:       return bptype < ORC_STACKED;
+    case ORC_SAMPLE_WC:       return bptype == ORC_WWc;
+    default:                  return 0;
+  }
+}
+
+/* cov_SignificantPairs_Ranking histogram part, src/covariation.c:414-457:
+ * every pair not excluded by the PDB distance rule goes to ha; with
+ * classes (the GIVSS run) the selected pairs go to hb, the others to ht. */
 static orc_hist_t *
-rank_scores(int L, const double *COV, double maxCOV, double bmin, double w, double tol)
+rank_scores(const orc_params_t *p, int L, const double *COV, double maxCOV, double bmin, double w, double tol,
+            orc_hist_t **ret_hb, orc_hist_t **ret_ht)
 {
   double bmax = maxCOV + 5 * w;
-  orc_hist_t *h;
+  orc_hist_t *h, *hb = NULL, *ht = NULL;
   int i, j;
   while (fabs(bmax - bmin) < tol) bmax += w;
   h = orc_hist_create(bmin, bmax, w);
+  if (ret_hb) { hb = orc_hist_create(bmin, bmax, w); ht = orc_hist_create(bmin, bmax, w); }
   for (i = 0; i < L - 1; i++)
     for (j = i + 1; j < L; j++) {
       double v = COV[(int64_t)i * L + j], add = (v > bmin + w) ? v : bmin + w;
+      if (p->msa2pdb && p->msa2pdb[i] >= 0 && p->msa2pdb[j] >= 0 && p->msa2pdb[j] - p->msa2pdb[i] < p->mind)
+        continue;
       orc_hist_add(h, add);
+      if (hb) orc_hist_add(cnt_select(p, i + 1, j + 1) ? hb : ht, add);
     }
+  if (ret_hb) { *ret_hb = hb; *ret_ht = ht; }
   return h;
 }
 
@@ -1290,12 +1341,16 @@ orc_params_default(orc_params_t *p)
   p->allow[0 * 4 + 3] = p->allow[3 * 4 + 0] = 1.0;   /* src/R-scape.c:883-887 */
   p->allow[1 * 4 + 2] = p->allow[2 * 4 + 1] = 1.0;
   p->allow[2 * 4 + 3] = p->allow[3 * 4 + 2] = 1.0;
+  p->samplesize = ORC_SAMPLE_ALL;
+  p->expBP = -1.0;
 }
 
 /* null_rscape (src/R-scape.c:1614-1724) with calculate_width_histo
  * (:1281-1371) and the nshuffle rule (:2449-2459), then the GIVSS run
  * (:2502, cov_SignificantPairs_Ranking and cov_CreateHitList,
- * src/covariation.c:325-530, 778-1006), one-set test. */
+ * src/covariation.c:325-530, 778-1006): the one-set test, or with
+ * p->samplesize and a structure's contacts the two-set test; p->expBP as
+ * --structured sets it. */
 int
 orc_rscape(const orc_params_t *p, const uint8_t *ax, const double *wgt, int N, int L,
            const orc_tree_t *T, double *COV_out, double *Eval_out,
@@ -1371,7 +1426,7 @@ orc_rscape_multi(const orc_params_t *p, int nt, const int *covtypes, const uint8
         res[t].null_minCOV = mm[t][0]; res[t].null_maxCOV = mm[t][1];
       }
       if (w[t] < 1e-20) continue;       /* covariation.c:348-374: no ranklist */
-      hs     = rank_scores(L, COV + t * LL, mm[t][1], p->bmin, w[t], p->tol);
+      hs     = rank_scores(p, L, COV + t * LL, mm[t][1], p->bmin, w[t], p->tol, NULL, NULL);
       cum[t] = null_add(cum[t], hs);
       orc_hist_free(hs);
     }
@@ -1390,10 +1445,14 @@ orc_rscape_multi(const orc_params_t *p, int nt, const int *covtypes, const uint8
     if (COV_out) memcpy(COV_out + t * LL, C, sizeof(double) * LL);
     if (Eval_out) for (i = 0; i < (int)LL; i++) Eval_out[t * LL + i] = INFINITY;
     if (N > 1 && w[t] >= 1e-20 && cm) {
-      double Nt;
-      h = rank_scores(L, C, mm[t][1], p->bmin, w[t], p->tol);
-      Nt = (double)h->Nc;
-      r->Nt = h->Nc;
+      orc_hist_t *hb = NULL, *ht = NULL;
+      double Nt, Nb;
+      int64_t nh = 0;   /* hits so far (h of src/covariation.c:852) */
+      h = rank_scores(p, L, C, mm[t][1], p->bmin, w[t], p->tol, &hb, &ht);
+      Nt = (double)ht->Nc;
+      Nb = (double)hb->Nc;
+      r->Nt = ht->Nc;
+      r->Nb = hb->Nc;
       hist_extend(cm, h->nb);
       r->pmass_used = hist_pmass(cm, p->pmass, fracfit);
       if (isnan(r->pmass_used)) { orc_hist_free(h); status = 6; goto DONE; }
@@ -1406,12 +1465,18 @@ orc_rscape_multi(const orc_params_t *p, int nt, const int *covtypes, const uint8
       }
       r->fit_ok = 1;
       if (!isinf(r->lambda)) sf = surv_tail(cm, r->newmass, p->doexpfit, r->mu, r->lambda, r->tau);
-      r->sc_thresh = evalue2cov(p->thresh, Nt, cm, sf);
+      /* the thresholds of base pairs and of the other pairs (:490-500) */
+      r->sc_thresh = evalue2cov(p->thresh, (hb->Nc > 0) ? (double)hb->Nc : (double)h->Nc, cm, sf);
+      r->sc_nbp    = evalue2cov(p->thresh, (hb->Nc > 0) ? (double)ht->Nc : (double)h->Nc, cm, sf);
+      /* cov_CreateHitList (src/covariation.c:828-870): base pairs take Nb
+       * tests, the others expBP while fewer than expBP hits were listed,
+       * then Nt */
       for (i = 0; i < L - 1; i++)
         for (j = i + 1; j < L; j++) {
-          double cov = C[(int64_t)i * L + j];
-          double pv  = cov2evalue(cov, 1.0, cm, sf);
-          double ev  = pv * Nt;
+          double cov  = C[(int64_t)i * L + j];
+          double pv   = cov2evalue(cov, 1.0, cm, sf);
+          int    isbp = cnt_isbp(p, cnt_type(p, i + 1, j + 1));
+          double ev   = isbp ? pv * Nb : ((double)nh < p->expBP ? pv * p->expBP : pv * Nt);
           if (Eval_out) Eval_out[t * LL + (int64_t)i * L + j] = Eval_out[t * LL + (int64_t)j * L + i] = ev;
           if (ev < p->thresh || p->thresh > 1000) {
             if (nhit < hit_cap) {
@@ -1419,8 +1484,11 @@ orc_rscape_multi(const orc_params_t *p, int nt, const int *covtypes, const uint8
               hit_i[o] = i; hit_j[o] = j; hit_sc[o] = cov; hit_E[o] = ev; hit_p[o] = pv;
             }
             nhit++;
+            nh++;
           }
         }
+      orc_hist_free(hb);
+      orc_hist_free(ht);
     }
     r->nhit = nhit;
     if (cm) {

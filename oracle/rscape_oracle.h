@@ -76,7 +76,20 @@ typedef struct {
   double tol;            /* 1e-6 */
   uint64_t seed;         /* 42 */
   double allow[16];      /* allowed pairs, row-major 4x4 */
+  /* the two-set test (R-scape -s, src/R-scape.c:1139-1160) and
+   * --structured (:1911-1918) */
+  int            samplesize;  /* ORC_SAMPLE_ALL (one-set test) by default */
+  int            ncnt;        /* contacts of the given structure */
+  const int64_t *cnt_i;       /* [ncnt] 1-based alignment positions */
+  const int64_t *cnt_j;
+  const int     *cnt_type;    /* [ncnt] BPTYPE */
+  int            mind;        /* with msa2pdb: pairs closer than mind in the PDB are not ranked */
+  const int     *msa2pdb;     /* [L] or NULL */
+  double         expBP;       /* -1 by default */
 } orc_params_t;
+
+enum { ORC_SAMPLE_CONTACTS = 0, ORC_SAMPLE_BP = 1, ORC_SAMPLE_WC = 2, ORC_SAMPLE_ALL = 3 };
+enum { ORC_WWc = 0, ORC_STACKED = 32, ORC_CONTACT = 33, ORC_BPNONE = 34 };
 
 typedef struct {
   int      nshuffle;
@@ -85,14 +98,16 @@ typedef struct {
   double   minCOV, maxCOV; /* of the real alignment after correction */
   double   pmass_used, newmass, mu, lambda, tau;
   int      fit_ok;
-  double   sc_thresh;     /* evalue2cov threshold (one-set test) */
-  uint64_t Nt;            /* number of tests */
+  double   sc_thresh;     /* evalue2cov threshold (of base pairs in the two-set test: sc_bp) */
+  uint64_t Nt;            /* number of tests (of the pairs outside the structure in the two-set test) */
   int      nhit;
   /* null histogram metadata */
   double   h_bmin, h_w;
   int      h_nb, h_imin, h_imax, h_cmin;
   uint64_t h_n, h_Nc, h_No;
   double   h_xmin, h_xmax, h_phi;
+  double   sc_nbp;        /* threshold of the pairs outside the structure */
+  uint64_t Nb;            /* number of tests of the base pairs (0 in the one-set test) */
 } orc_result_t;
 
 /* ---- RNG: Philox4x32-10 (Salmon et al., SC'11) ---- */

@@ -15,7 +15,9 @@
  * corr_Calculate* and cov_CreateHitList, and corr_SyncHost copies COV back on
  * request.
  *
- * Scope: the one-set test (SAMPLE_ALL; every pair tested alike).  Files the
+ * Scope: the one-set test (SAMPLE_ALL; every pair tested alike) and the
+ * two-set test (R-scape -s: the given structure's contacts against the other
+ * pairs), --structured (expBP) and the PDB distance rule (msa2pdb).  Files the
  * reference writes from cov_CreateHitList (.cov, .sorted.cov, .power) and
  * helix aggregation belong to its output layer and are not produced here.
  */
@@ -616,7 +618,92 @@ rank_into(struct mutual_s *mi, ESL_HISTOGRAM *h, char *errbuf)
   return eslOK;
 }
 
-/* cov_SignificantPairs_Ranking, src/covariation.c:325-530 (one-set test) */
+/* pair (i, j), i < j (0-based), in the scan order of the reference's loops */
+static int64_t
+scan_index(int64_t i, int64_t j, int64_t L)
+{
+  return i * (2 * L - i - 1) / 2 + (j - i - 1);
+}
+
+/* does contact type t count as a base pair for the sample (the predicates
+ * of lib/R-view/src/rview_contacts.c:537-574 and cov_CreateHitList's isbp,
+ * src/covariation.c:836-841) */
+static int
+sample_takes(SAMPLESIZE ss, int t)
+{
+  switch (ss) {
+    case SAMPLE_CONTACTS: return t < BPNONE;
+    case SAMPLE_BP:       return t < STACKED;
+    case SAMPLE_WC:       return t == WWc;
+    default:              return 0;
+  }
+}
+
+/* the structure's contacts over the L(L-1)/2 pairs (either output may be
+ * NULL): sel, bit n set when any contact of pair n satisfies the sample's
+ * rule (CMAP_Is*Local, the ranking's classes); first[n], the type of the
+ * first contact of pair n, BPNONE for none (CMAP_GetBPTYPE,
+ * rview_contacts.c:523-535).  A contact matches pair (i, j) only as
+ * cnt.i = i + 1 < cnt.j = j + 1, as the reference compares them. */
+static int
+contact_maps(const CLIST *cl, SAMPLESIZE ss, int64_t L, uint32_t **ret_sel, uint8_t **ret_first)
+{
+  int64_t P = L * (L - 1) / 2, n;
+  uint32_t *sel = NULL;
+  uint8_t *first = NULL, *seen = NULL;
+  int h;
+  if (ret_sel) {
+    sel = (uint32_t *)calloc((size_t)((P + 31) / 32) + 1, sizeof(uint32_t));
+    if (!sel) return eslEMEM;
+  }
+  first = (uint8_t *)malloc((size_t)(P > 0 ? P : 1));
+  seen  = (uint8_t *)calloc((size_t)(P > 0 ? P : 1), 1);
+  if (!first || !seen) { free(sel); free(first); free(seen); return eslEMEM; }
+  memset(first, BPNONE, (size_t)(P > 0 ? P : 1));
+  for (h = 0; cl && h < cl->ncnt; h++) {
+    const CNT *c = &cl->cnt[h];
+    if (c->i < 1 || c->j > L || c->i >= c->j) continue;
+    n = scan_index(c->i - 1, c->j - 1, L);
+    if (!seen[n]) { seen[n] = 1; first[n] = (uint8_t)c->bptype; }
+    if (sel && sample_takes(ss, (int)c->bptype)) sel[n >> 5] |= 1u << (n & 31);
+  }
+  free(seen);
+  if (ret_sel) *ret_sel = sel;
+  if (ret_first) *ret_first = first; else free(first);
+  return eslOK;
+}
+
+/* the ranking on the host (src/covariation.c:420-457), for the two-set
+ * classes or the PDB distance rule: every pair not excluded goes to ha and,
+ * with classes, to hb (sel) or ht */
+static int
+rank_host(struct data_s *data, RANKLIST *rl, int classes)
+{
+  struct mutual_s *mi = data->mi;
+  const int64_t L = mi->alen;
+  const int mind = data->clist ? data->clist->mind : 0;
+  uint32_t *sel = NULL;
+  int64_t i, j, n = 0;
+  if (mi->device_resident && corr_SyncHost(mi, data->errbuf)) return eslFAIL;
+  if (classes && contact_maps(data->clist, data->samplesize, L, &sel, NULL)) XFAIL(eslEMEM, data->errbuf, "out of memory");
+  for (i = 0; i < L - 1; i++)
+    for (j = i + 1; j < L; j++, n++) {
+      double add;
+      if (data->msa2pdb && data->msa2pdb[i] >= 0 && data->msa2pdb[j] >= 0 && data->msa2pdb[j] - data->msa2pdb[i] < mind)
+        continue;
+      add = mi->COV->mx[i][j];
+      if (add < data->bmin + data->w) add = data->bmin + data->w;
+      if (covh_Add(rl->ha, add) != eslOK ||
+          (classes && covh_Add(((sel[n >> 5] >> (n & 31)) & 1u) ? rl->hb : rl->ht, add) != eslOK)) {
+        free(sel);
+        XFAIL(eslFAIL, data->errbuf, "histogram add failed");
+      }
+    }
+  free(sel);
+  return eslOK;
+}
+
+/* cov_SignificantPairs_Ranking, src/covariation.c:325-530 */
 int
 cov_SignificantPairs_Ranking(struct data_s *data, RANKLIST **ret_ranklist, HITLIST **ret_hitlist,
                              RMLIST **ret_rmlist)
@@ -625,7 +712,7 @@ cov_SignificantPairs_Ranking(struct data_s *data, RANKLIST **ret_ranklist, HITLI
   RANKLIST *ranklist;
   HITLIST  *hitlist = NULL;
   double    bmax, pmass, newmass;
-  int       st;
+  int       st, classes;
   if (ret_rmlist) *ret_rmlist = NULL;
   if (ret_ranklist) *ret_ranklist = NULL;
   if (ret_hitlist) *ret_hitlist = NULL;
@@ -637,10 +724,23 @@ cov_SignificantPairs_Ranking(struct data_s *data, RANKLIST **ret_ranklist, HITLI
   while (fabs(bmax - data->bmin) < data->tol) bmax += data->w;
   ranklist = cov_CreateRankList(bmax, data->bmin, data->w);
   if (!ranklist) XFAIL(eslEMEM, data->errbuf, "out of memory");
-  if ((st = rank_into(mi, ranklist->ha, data->errbuf))) { cov_FreeRankList(ranklist); return st; }
-  if (data->mode == GIVSS || data->mode == FOLDSS) {   /* SAMPLE_ALL: every pair goes to ht */
+  classes = (data->mode == GIVSS || data->mode == FOLDSS) && data->samplesize != SAMPLE_ALL;
+  if (classes || data->msa2pdb) {
+    /* the two-set classes or the PDB rule: ha (and hb, ht) on the host */
+    if ((st = rank_host(data, ranklist, classes))) { cov_FreeRankList(ranklist); return st; }
+  } else if ((st = rank_into(mi, ranklist->ha, data->errbuf))) {
+    cov_FreeRankList(ranklist);
+    return st;
+  }
+  if ((data->mode == GIVSS || data->mode == FOLDSS) && !classes) {   /* SAMPLE_ALL: every pair goes to ht */
     ESL_HISTOGRAM *ht = ranklist->ht, *ha = ranklist->ha;
+    if (ht->nb < ha->nb) {
+      uint64_t *o = (uint64_t *)realloc(ht->obs, sizeof(uint64_t) * ha->nb);
+      if (!o) { cov_FreeRankList(ranklist); XFAIL(eslEMEM, data->errbuf, "out of memory"); }
+      ht->obs = o;
+    }
     memcpy(ht->obs, ha->obs, sizeof(uint64_t) * ha->nb);
+    ht->nb = ha->nb; ht->bmin = ha->bmin; ht->bmax = ha->bmax;
     ht->n = ha->n; ht->Nc = ha->Nc; ht->No = ha->No; ht->xmin = ha->xmin; ht->xmax = ha->xmax;
     ht->imin = ha->imin; ht->imax = ha->imax; ht->cmin = ha->cmin;
   }
@@ -665,11 +765,15 @@ cov_SignificantPairs_Ranking(struct data_s *data, RANKLIST **ret_ranklist, HITLI
     if (st) { cov_FreeRankList(ranklist); return st; }
   }
   if (data->mode == GIVSS && data->thresh) {   /* :490-500 */
-    double Nc = (double)((ranklist->hb->Nc > 0) ? ranklist->hb->Nc : ranklist->ha->Nc);
+    const int two = ranklist->hb->Nc > 0;
+    const double Nb = (double)(two ? ranklist->hb->Nc : ranklist->ha->Nc);
+    const double Nn = (double)(two ? ranklist->ht->Nc : ranklist->ha->Nc);
     data->thresh->sc_bp = data->ranklist_null
-                              ? covh_evalue2cov(data->thresh->val, Nc, data->ranklist_null->ha, data->ranklist_null->survfit)
+                              ? covh_evalue2cov(data->thresh->val, Nb, data->ranklist_null->ha, data->ranklist_null->survfit)
                               : INFINITY;
-    data->thresh->sc_nbp = data->thresh->sc_bp;
+    data->thresh->sc_nbp = data->ranklist_null
+                               ? covh_evalue2cov(data->thresh->val, Nn, data->ranklist_null->ha, data->ranklist_null->survfit)
+                               : INFINITY;
   }
   if (data->mode == GIVSS) {
     if ((st = cov_CreateHitList(data, mi, ranklist, &hitlist, NULL, NULL, NULL))) {
@@ -682,7 +786,9 @@ cov_SignificantPairs_Ranking(struct data_s *data, RANKLIST **ret_ranklist, HITLI
   return eslOK;
 }
 
-/* cov_CreateHitList, src/covariation.c:778-1006 (one-set test: E = p * Nt) */
+/* cov_CreateHitList, src/covariation.c:778-1006: E = p Nb for the pairs the
+ * structure's first contact makes base pairs (two-set test), else p expBP
+ * while fewer than expBP hits were listed (--structured), else p Nt */
 int
 cov_CreateHitList(struct data_s *data, struct mutual_s *mi, RANKLIST *ranklist, HITLIST **ret_hitlist,
                   RMLIST **ret_rmlist, char *covtype, char *threshtype)
@@ -693,14 +799,28 @@ cov_CreateHitList(struct data_s *data, struct mutual_s *mi, RANKLIST *ranklist, 
   int64_t     P = mi->alen * (mi->alen - 1) / 2;
   int         nhit = 0, cap, k, st;
   double      thresh = data->thresh ? data->thresh->val : 0.05;
+  uint32_t   *bpmask = NULL;
+  uint8_t    *first = NULL;
   (void)covtype; (void)threshtype;
   if (ret_rmlist) *ret_rmlist = NULL;
+  /* the first contact's type of every pair (the hits' bptype) and, in the
+   * two-set test, the base pairs */
+  if (data->clist && data->clist->ncnt > 0) {
+    if (contact_maps(data->clist, data->samplesize, mi->alen, NULL, &first)) XFAIL(eslEMEM, data->errbuf, "out of memory");
+    if (data->samplesize != SAMPLE_ALL) {
+      int64_t n;
+      bpmask = (uint32_t *)calloc((size_t)((P + 31) / 32) + 1, sizeof(uint32_t));
+      if (!bpmask) { free(first); XFAIL(eslEMEM, data->errbuf, "out of memory"); }
+      for (n = 0; n < P; n++)
+        if (sample_takes(data->samplesize, first[n])) bpmask[n >> 5] |= 1u << (n & 31);
+    }
+  }
   hl = (HITLIST *)calloc(1, sizeof(HITLIST));
-  if (!hl) XFAIL(eslEMEM, data->errbuf, "out of memory");
+  if (!hl) { free(first); free(bpmask); XFAIL(eslEMEM, data->errbuf, "out of memory"); }
   hl->Nt = (int64_t)ranklist->ht->Nc;
   hl->Nb = (int64_t)ranklist->hb->Nc;
   if (!data->ranklist_null) {   /* naive: every pair with E = 0 */
-    if (corr_SyncHost(mi, data->errbuf)) { free(hl); return eslFAIL; }
+    if (corr_SyncHost(mi, data->errbuf)) { free(hl); free(first); free(bpmask); return eslFAIL; }
     dmx_set(mi->Eval, INFINITY);
     cap = (thresh > 0.0) ? (int)P : 0;
     hl->hit = (HIT *)calloc(cap > 0 ? cap : 1, sizeof(HIT));
@@ -709,29 +829,34 @@ cov_CreateHitList(struct data_s *data, struct mutual_s *mi, RANKLIST *ranklist, 
       while (rem >= mi->alen - 1 - i) { rem -= mi->alen - 1 - i; i++; }
       hl->hit[k].i = i; hl->hit[k].j = i + 1 + rem;
       hl->hit[k].sc = mi->COV->mx[i][i + 1 + rem];
+      hl->hit[k].bptype = first ? first[k] : BPNONE;
     }
     hl->nhit = cap;
   } else {
-    if (!g) { free(hl); XFAIL(eslFAIL, data->errbuf, "no device context"); }
+    if (!g) { free(hl); free(first); free(bpmask); XFAIL(eslFAIL, data->errbuf, "no device context"); }
     cap = (int)((P < (1 << 22)) ? P : (1 << 22));
     hits = (covgpu_hit *)malloc(sizeof(covgpu_hit) * (cap > 0 ? cap : 1));
     {
       const double *src = cov_src(mi);
       /* device-resident: neither COV nor Eval comes to the host */
-      st = covgpu_evalue_full(g->ctx, src, data->ranklist_null->ha, data->ranklist_null->survfit,
-                              (double)ranklist->ht->Nc, (thresh > MAX_EVAL) ? 2.0 * MAX_EVAL : thresh,
-                              src ? mi->Eval->mx[0] : NULL, hits, cap, &nhit);
+      st = covgpu_evalue_sets(g->ctx, src, data->ranklist_null->ha, data->ranklist_null->survfit,
+                              (double)ranklist->ht->Nc, (double)ranklist->hb->Nc, data->expBP, bpmask,
+                              (thresh > MAX_EVAL) ? 2.0 * MAX_EVAL : thresh, src ? mi->Eval->mx[0] : NULL, hits,
+                              cap, &nhit);
     }
-    if (st) { free(hits); free(hl); XFAIL(eslFAIL, data->errbuf, "%s", covgpu_errmsg(g->ctx)); }
+    if (st) { free(hits); free(hl); free(first); free(bpmask); XFAIL(eslFAIL, data->errbuf, "%s", covgpu_errmsg(g->ctx)); }
     if (nhit > cap) nhit = cap;
     hl->hit = (HIT *)calloc(nhit > 0 ? nhit : 1, sizeof(HIT));
     for (k = 0; k < nhit; k++) {
       hl->hit[k].i = hits[k].i; hl->hit[k].j = hits[k].j;
       hl->hit[k].sc = hits[k].sc; hl->hit[k].Eval = hits[k].E; hl->hit[k].pval = hits[k].pval;
+      hl->hit[k].bptype = first ? first[scan_index(hits[k].i, hits[k].j, mi->alen)] : BPNONE;
     }
     hl->nhit = nhit;
     free(hits);
   }
+  free(first);
+  free(bpmask);
   hl->srthit = (HIT **)malloc(sizeof(HIT *) * (hl->nhit > 0 ? hl->nhit : 1));
   for (k = 0; k < hl->nhit; k++) hl->srthit[k] = &hl->hit[k];
   *ret_hitlist = hl;

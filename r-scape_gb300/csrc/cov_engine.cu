@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -78,6 +79,7 @@ struct covgpu_ctx {
   int hitcap = 0;
   double* d_full = nullptr;
   double* d_pcls = nullptr;         // covgpu_pair_classes outputs [3][capL(capL-1)/2]
+  uint32_t* d_bpmask = nullptr;     // covgpu_evalue_sets: the base-pair bitmap [capL(capL-1)/2 bits]
   UmmaPlan* umma = nullptr;
   FitWork* fitw[MAXOUT] = {};
   // simulator
@@ -213,7 +215,8 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
                   ctx->d_part1, ctx->d_colx, ctx->d_avg, ctx->d_tmin, ctx->d_tmax, ctx->d_mm, ctx->d_status,
                   ctx->d_left, ctx->d_right, ctx->d_lnodes, ctx->d_fitch, ctx->d_scratch, ctx->d_obs, ctx->d_sf,
                   ctx->d_tail, ctx->d_nhits, ctx->d_hi, ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->d_full,
-                  ctx->d_flush, ctx->d_pmdf, ctx->d_colxf, ctx->d_apcf, ctx->d_evt, ctx->d_pcls};
+                  ctx->d_flush, ctx->d_pmdf, ctx->d_colxf, ctx->d_apcf, ctx->d_evt, ctx->d_pcls,
+                  ctx->d_bpmask};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (ctx->umma) umma_plan_destroy(ctx->umma);
   for (FitWork* f : ctx->fitw) if (f) fitwork_destroy(f);
@@ -1612,12 +1615,59 @@ extern "C" int covgpu_hist_full(covgpu_ctx* ctx, const double* COV, double bmin,
   return check_status(ctx);
 }
 
-extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void* hv, const double* survfit,
-                                  double Nt, double thresh, double* Eval, covgpu_hit* hits, int hitcap, int* nhit) {
+// the hit buffers hold at least cap hits
+static int hits_reserve(covgpu_ctx* ctx, int cap) {
+  if (cap > 0 && ctx->hitcap < cap) {
+    cudaFree(ctx->d_hi); cudaFree(ctx->d_hj); cudaFree(ctx->d_hsc); cudaFree(ctx->d_hE); cudaFree(ctx->d_hp);
+    ctx->d_hi = ctx->d_hj = nullptr;
+    ctx->d_hsc = ctx->d_hE = ctx->d_hp = nullptr;
+    ctx->hitcap = 0;
+    CK(dalloc(&ctx->d_hi, cap)); CK(dalloc(&ctx->d_hj, cap));
+    CK(dalloc(&ctx->d_hsc, cap)); CK(dalloc(&ctx->d_hE, cap)); CK(dalloc(&ctx->d_hp, cap));
+    ctx->hitcap = cap;
+  }
+  return 0;
+}
+
+// one E-value pass over the uploaded scores: the number of pairs with
+// E < thresh into *nh (the first hitcap of them in the hit buffers), the
+// tile-packed E-values into evt when given
+static int evalue_pass(covgpu_ctx* ctx, const EvalTables& T, double* evt, int* nh) {
+  CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
+  CK(launch_evalue(ctx->d_cov, ctx->d_tiles, ctx->ntiles, ctx->L, T, evt, ctx->d_nhits, ctx->hitcap, ctx->d_hi,
+                   ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->st));
+  CK(cudaMemcpyAsync(nh, ctx->d_nhits, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  CK(cudaStreamSynchronize(ctx->st));
+  return 0;
+}
+
+// the first n hits of the hit buffers, in scan order (i, then j)
+static int hits_fetch(covgpu_ctx* ctx, int n, std::vector<covgpu_hit>& out) {
+  out.resize(n);
+  if (n == 0) return 0;
+  std::vector<int> hi(n), hj(n);
+  std::vector<double> hs(n), hE(n), hp(n);
+  CK(cudaMemcpy(hi.data(), ctx->d_hi, n * sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hj.data(), ctx->d_hj, n * sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hs.data(), ctx->d_hsc, n * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hE.data(), ctx->d_hE, n * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hp.data(), ctx->d_hp, n * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < n; k++) out[k] = covgpu_hit{hi[k], hj[k], hs[k], hE[k], hp[k]};
+  std::sort(out.begin(), out.end(), [](const covgpu_hit& a, const covgpu_hit& b) {
+    return (a.i != b.i) ? a.i < b.i : a.j < b.j;
+  });
+  return 0;
+}
+
+extern "C" int covgpu_evalue_sets(covgpu_ctx* ctx, const double* COV, const void* hv, const double* survfit,
+                                  double Nt, double Nb, double expBP, const uint32_t* bpmask, double thresh,
+                                  double* Eval, covgpu_hit* hits, int hitcap, int* nhit) {
   CK(cudaSetDevice(ctx->dev));
   const ESL_HISTOGRAM* h = (const ESL_HISTOGRAM*)hv;
   int s = upload_full(ctx, COV);
   if (s) return s;
+  const int L = ctx->L;
+  const int64_t P = (int64_t)L * (L - 1) / 2;
   std::vector<double> tail(h->nb, 0.0);
   double c = 0.0;
   for (int b = h->nb - 1; b >= 0; b--) { if (b <= h->imax) c += (double)h->obs[b]; tail[b] = c; }
@@ -1631,49 +1681,77 @@ extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void
   }
   CK(cudaMemcpyAsync(ctx->d_tail, tail.data(), h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
   if (survfit) CK(cudaMemcpyAsync(ctx->d_sf, survfit, 2 * h->nb * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-  if (hitcap > 0 && ctx->hitcap < hitcap) {
-    cudaFree(ctx->d_hi); cudaFree(ctx->d_hj); cudaFree(ctx->d_hsc); cudaFree(ctx->d_hE); cudaFree(ctx->d_hp);
-    CK(dalloc(&ctx->d_hi, hitcap)); CK(dalloc(&ctx->d_hj, hitcap));
-    CK(dalloc(&ctx->d_hsc, hitcap)); CK(dalloc(&ctx->d_hE, hitcap)); CK(dalloc(&ctx->d_hp, hitcap));
-    ctx->hitcap = hitcap;
-  }
+  if ((s = hits_reserve(ctx, hitcap))) return s;
   EvalTables T;
   T.sf = survfit ? ctx->d_sf : nullptr;
   T.ptail = ctx->d_tail;
   T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = Nt;
   T.pNc = 1.0 / T.Nc;
   T.thresh = thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
-  const int64_t plane = (int64_t)ctx->ntiles * TPP;
+  if (bpmask) {
+    const size_t nw = (size_t)((P + 31) / 32), capw = (size_t)(((int64_t)ctx->capL * (ctx->capL - 1) / 2 + 31) / 32);
+    if (!ctx->d_bpmask) CK(dalloc(&ctx->d_bpmask, std::max<size_t>(capw, 1)));
+    CK(cudaMemcpyAsync(ctx->d_bpmask, bpmask, nw * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->st));
+    T.bpmask = ctx->d_bpmask;
+    T.Nb = Nb;
+  }
+  // --structured (src/covariation.c:850-854): a pair outside the structure
+  // takes expBP tests while fewer than expBP hits precede it in scan order.
+  // kstar is the scan index of the hit that brings the count to expBP: a
+  // first pass lists every pair that is a hit under the smaller of expBP and
+  // Nt (a superset of the hits), the host replays the rule over them in scan
+  // order, and the second pass applies it to every pair.
+  if (expBP > 0.0) {
+    T.Nx = expBP;
+    if (thresh > 1000.0) {
+      T.kstar = (long long)std::ceil(expBP) - 1;   // every pair is a hit: h = n
+    } else {
+      EvalTables T1 = T;
+      T1.Nx = std::min(expBP, Nt);
+      T1.kstar = LLONG_MAX;
+      int nc = 0;
+      if ((s = evalue_pass(ctx, T1, nullptr, &nc))) return s;
+      if (nc > ctx->hitcap) {
+        if ((s = hits_reserve(ctx, nc))) return s;
+        if ((s = evalue_pass(ctx, T1, nullptr, &nc))) return s;
+      }
+      std::vector<covgpu_hit> cand;
+      if ((s = hits_fetch(ctx, nc, cand))) return s;
+      long long kstar = LLONG_MAX;
+      int64_t nh = 0;
+      for (const covgpu_hit& x : cand) {
+        const long long n = (long long)x.i * (2LL * L - x.i - 1) / 2 + (x.j - x.i - 1);
+        const bool isbp = bpmask && ((bpmask[n >> 5] >> (n & 31)) & 1u);
+        const double E = isbp ? x.pval * Nb : ((double)nh < expBP ? x.pval * expBP : x.pval * Nt);
+        if (E < thresh && ++nh >= expBP) { kstar = n; break; }
+      }
+      T.kstar = kstar;
+    }
+  }
   double* evt = nullptr;
   if (Eval) {
     if (!ctx->d_evt) CK(dalloc(&ctx->d_evt, (size_t)ctx->capntiles * TPP));
     evt = ctx->d_evt;
   }
-  CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
-  CK(launch_evalue(ctx->d_cov, ctx->d_tiles, ctx->ntiles, ctx->L, T, evt, ctx->d_nhits, ctx->hitcap, ctx->d_hi,
-                   ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->st));
   int nh = 0;
-  CK(cudaMemcpyAsync(&nh, ctx->d_nhits, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  if ((s = evalue_pass(ctx, T, evt, &nh))) return s;
   if (Eval) {
     if (!ctx->d_full) CK(dalloc(&ctx->d_full, (size_t)ctx->capL * ctx->capL));
-    CK(launch_untile(evt, ctx->d_tiles, ctx->ntiles, ctx->L, INFINITY, ctx->d_full, ctx->st));
-    CK(cudaMemcpyAsync(Eval, ctx->d_full, (size_t)ctx->L * ctx->L * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(launch_untile(evt, ctx->d_tiles, ctx->ntiles, L, INFINITY, ctx->d_full, ctx->st));
+    CK(cudaMemcpyAsync(Eval, ctx->d_full, (size_t)L * L * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
   }
-  CK(cudaStreamSynchronize(ctx->st));
   *nhit = nh;
   const int nget = std::min(nh, hitcap);
   if (nget > 0 && hits) {
-    std::vector<int> hi(nget), hj(nget);
-    std::vector<double> hs(nget), hE(nget), hp(nget);
-    CK(cudaMemcpy(hi.data(), ctx->d_hi, nget * sizeof(int), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(hj.data(), ctx->d_hj, nget * sizeof(int), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(hs.data(), ctx->d_hsc, nget * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(hE.data(), ctx->d_hE, nget * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(hp.data(), ctx->d_hp, nget * sizeof(double), cudaMemcpyDeviceToHost));
-    for (int k = 0; k < nget; k++) hits[k] = covgpu_hit{hi[k], hj[k], hs[k], hE[k], hp[k]};
-    std::sort(hits, hits + nget, [](const covgpu_hit& a, const covgpu_hit& b) {
-      return (a.i != b.i) ? a.i < b.i : a.j < b.j;
-    });
+    std::vector<covgpu_hit> got;
+    if ((s = hits_fetch(ctx, std::min(nh, ctx->hitcap), got))) return s;
+    std::copy(got.begin(), got.begin() + nget, hits);
   }
   return 0;
+}
+
+extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void* hv, const double* survfit,
+                                  double Nt, double thresh, double* Eval, covgpu_hit* hits, int hitcap, int* nhit) {
+  return covgpu_evalue_sets(ctx, COV, hv, survfit, Nt, 0.0, -1.0, nullptr, thresh, Eval, hits, hitcap, nhit);
 }

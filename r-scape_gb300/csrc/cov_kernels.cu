@@ -1169,7 +1169,13 @@ __device__ __forceinline__ void evalue_body(
         const int ic = (icov < T.imin) ? T.imin : icov;
         pv = (ic >= T.imax - 1) ? T.pNc : T.ptail[ic];
       } else pv = INFINITY;
-      E = pv * T.Nt;
+      double mult = T.Nt;
+      if (T.bpmask || T.kstar >= 0) {
+        const long long n = (long long)i * (2LL * L - i - 1) / 2 + (j - i - 1);
+        if (T.bpmask && ((__ldg(T.bpmask + (n >> 5)) >> (n & 31)) & 1u)) mult = T.Nb;
+        else if (n <= T.kstar)                                             mult = T.Nx;
+      }
+      E = pv * mult;
       const long long eb = __double_as_longlong(E);
       const bool below = (eb >= 0) ? (eb < K.thresh_bits) : (E < T.thresh);
       if (below || K.all) {

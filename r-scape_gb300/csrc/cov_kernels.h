@@ -49,6 +49,12 @@ struct EvalTables {
   double        bmin, w, phi, xmax, Nc, Nt, thresh;
   double        pNc;        // 1 / Nc
   int           nb, imin, imax;
+  // the two-set test and --structured (src/covariation.c:846-854): pair
+  // n = i (2L - i - 1)/2 + j - i - 1 takes Nb tests when bit n of bpmask is
+  // set, else Nx tests when n <= kstar, else Nt
+  const uint32_t* bpmask = nullptr;
+  double        Nb = 0.0, Nx = 0.0;
+  long long     kstar = -1;
 };
 
 // the E-value pass's comparison bounds (made on the host from EvalTables)

@@ -59,6 +59,23 @@ class Rand(C.Structure):
     _fields_ = [("seed", C.c_uint64)]
 
 
+class Cnt(C.Structure):
+    _fields_ = [("i", C.c_int64), ("j", C.c_int64), ("bptype", C.c_int)]
+
+
+class Clist(C.Structure):
+    _fields_ = [("ncnt", C.c_int), ("mind", C.c_int), ("cnt", C.POINTER(Cnt))]
+
+
+def make_clist(contacts, mind=0):
+    """A CLIST of contacts [(i, j, bptype), ...] (1-based alignment
+    positions, i < j), the contact array kept alive on the object."""
+    arr = (Cnt * max(1, len(contacts)))(*[Cnt(int(i), int(j), int(t)) for (i, j, t) in contacts])
+    cl = Clist(len(contacts), mind, arr)
+    cl._arr = arr
+    return cl
+
+
 class Data(C.Structure):
     _fields_ = [("r", C.POINTER(Rand)), ("samplesize", C.c_int), ("ranklist_null", C.POINTER(RankList)),
                 ("ranklist_aux", C.POINTER(RankList)), ("mi", C.POINTER(Mutual)), ("thresh", C.POINTER(Thresh)),
@@ -66,10 +83,13 @@ class Data(C.Structure):
                 ("nseq", C.c_int), ("expBP", C.c_double), ("bmin", C.c_double), ("w", C.c_double),
                 ("fracfit", C.c_double), ("pmass", C.c_double), ("doexpfit", C.c_int), ("tau", C.c_double),
                 ("mu", C.c_double), ("lambda_", C.c_double), ("allowpair", C.POINTER(DMatrix)), ("tol", C.c_double),
-                ("verbose", C.c_int), ("errbuf", C.c_char_p)]
+                ("verbose", C.c_int), ("errbuf", C.c_char_p), ("clist", C.POINTER(Clist)),
+                ("msa2pdb", C.POINTER(C.c_int))]
 
 
 GIVSS, RANSS = 0, 2
+SAMPLE_CONTACTS, SAMPLE_BP, SAMPLE_WC, SAMPLE_ALL = 0, 1, 2, 3
+WWc, STACKED, CONTACT, BPNONE = 0, 32, 33, 34
 
 
 def setup_lib(path):

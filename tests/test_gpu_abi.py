@@ -109,3 +109,72 @@ def test_dropin_probs_and_statistic(covgpu, oracle, abi, device_resident):
     assert mi.contents.type == 4
     assert abs(mi.contents.maxCOV - rmax) <= 1e-5 * abs(rmax)
     lib.corr_Destroy(mi)
+
+
+@pytest.mark.parametrize("variant", ["two_set", "structured", "two_set_structured", "pdb_two_set", "wc_two_set"])
+def test_dropin_two_set_and_structured(covgpu, oracle, abi, variant):
+    """R-scape -s (the two-set test: the structure's base pairs against the
+    other pairs), --structured (expBP) and a PDB map with its distance rule
+    through the drop-in flow: the same hits, E-values, numbers of tests,
+    thresholds and contact types as the oracle."""
+    lib = abi.setup_lib(covgpu.LIBPATH)
+    N, L, ns = 160, 90, 6
+    s = covgpu.Synth(N, L, 1.5, 18, 2, 9, 9, 0.08, seed=21, tree_kind=1)
+    w = covgpu.weights_pb(s.ax)
+    code = covgpu.covtype_code("GTp")
+    bps = [(i, int(s.ct[i])) for i in range(L) if s.ct[i] > i]
+    # the planted pairs, one of them listed first as a non-canonical type;
+    # one pair listed first as STACKED and then as WWc; a contact with i > j,
+    # which the reference never matches
+    contacts = [(bps[0][0] + 1, bps[0][1] + 1, 5)]
+    contacts += [(i + 1, j + 1, abi.WWc) for i, j in bps]
+    extra = (2, 9) if (1, 8) not in bps else (3, 11)
+    contacts += [(extra[0], extra[1], abi.STACKED), (extra[0], extra[1], abi.WWc), (40, 12, abi.WWc)]
+    sample = {"two_set": abi.SAMPLE_BP, "structured": abi.SAMPLE_ALL, "two_set_structured": abi.SAMPLE_BP,
+              "pdb_two_set": abi.SAMPLE_CONTACTS, "wc_two_set": abi.SAMPLE_WC}[variant]
+    expBP = 6.5 if "structured" in variant else -1.0
+    mind = 4 if variant.startswith("pdb") else 0
+    m2p = np.arange(L, dtype=np.int32) if mind else None
+    abc = abi.Alphabet(1, 4, 18)
+    mi = lib.corr_Create(L, N, 0, 8, 50, C.byref(abc), 3)
+    errbuf = C.create_string_buffer(256)
+    th = abi.Thresh(0, 0.05, 0.0, 0.0)
+    rnd = abi.Rand(42)
+    cl = abi.make_clist(contacts, mind)
+    data = abi.Data(C.pointer(rnd), sample, None, None, mi, C.pointer(th), 1, 0, abi.RANSS, code, N, expBP, -10.0,
+                    0.05, 1.0, 0.0005, 0, 0.0, 0.0, 0.0, None, 1e-6, 0, C.cast(errbuf, C.c_char_p), C.pointer(cl),
+                    m2p.ctypes.data_as(C.POINTER(C.c_int)) if m2p is not None else None)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    nulls = [abi.MsaHolder(oracle.null_msa(s.ax, T, 42, k), w, abc) for k in range(ns)]
+    real = abi.MsaHolder(s.ax, w, abc)
+    rl, hl, cum = abi.rscape_flow(lib, mi, nulls, real, data, code)
+    kw = dict(covtype="GTp", nshuffle=ns, want_matrices=True, samplesize=sample, contacts=contacts, expBP=expBP)
+    if mind:
+        kw.update(msa2pdb=m2p, mind=mind)
+    ref = oracle.rscape(s.ax, w, T, **kw)
+    H = hl.contents
+    assert H.Nt == ref["Nt"] and H.Nb == ref["Nb"]
+    if sample != abi.SAMPLE_ALL:
+        assert H.Nb > 0
+    got = {(H.hit[k].i, H.hit[k].j): H.hit[k] for k in range(H.nhit)}
+    exp = {(i, j): E for (i, j, sc, E, p) in ref["hits"]}
+    assert sorted(got) == sorted(exp)
+    for k, E in exp.items():
+        assert abs(got[k].Eval - E) <= 1e-5 * E
+    first = {}
+    for (i, j, t) in contacts:
+        if 1 <= i < j <= L:
+            first.setdefault((i - 1, j - 1), t)
+    for k, h in got.items():
+        assert h.bptype == first.get(k, abi.BPNONE)
+    assert abs(th.sc_bp - ref["sc_thresh"]) <= 1e-5 * abs(ref["sc_thresh"]) + 1e-9
+    assert abs(th.sc_nbp - ref["sc_nbp"]) <= 1e-5 * abs(ref["sc_nbp"]) + 1e-9
+    # mi->Eval: every pair's E-value with its own number of tests
+    Ev = np.ctypeslib.as_array(mi.contents.Eval.contents.mx[0], shape=(L * L,)).reshape(L, L)
+    iu = np.triu_indices(L, 1)
+    fin = np.isfinite(ref["Eval"][iu]) & (ref["Eval"][iu] > 0)
+    assert np.allclose(Ev[iu][fin], ref["Eval"][iu][fin], rtol=1e-5, atol=0)
+    lib.cov_FreeHitList(hl)
+    lib.cov_FreeRankList(rl)
+    lib.cov_FreeRankList(cum)
+    lib.corr_Destroy(mi)

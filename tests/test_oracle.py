@@ -236,3 +236,66 @@ def test_raf_count_form_equals_the_loop(oracle, N, L, seed):
     iu = np.triu_indices(L, 1)
     assert np.allclose(a.reshape(L, L)[iu], b.reshape(L, L)[iu], rtol=0, atol=1e-15)
     assert np.allclose(mma, mmb, rtol=0, atol=1e-15)
+
+
+def _replay_structured(E_one, P, expBP, thresh):
+    """cov_CreateHitList's --structured rule (src/covariation.c:850-854) by
+    hand, from the one-set E-values (E = p * P): pairs in scan order take
+    expBP tests while fewer than expBP hits were listed, then P."""
+    L = E_one.shape[0]
+    out = np.full_like(E_one, np.inf)
+    h = 0
+    for i in range(L - 1):
+        for j in range(i + 1, L):
+            pv = E_one[i, j] / P
+            e = pv * expBP if h < expBP else pv * P
+            out[i, j] = e
+            if e < thresh:
+                h += 1
+    return out
+
+
+def test_two_set_test_and_structured(oracle, covgpu):
+    """The two-set test (R-scape -s; src/covariation.c:414-457, 490-500,
+    828-870): the structure's base pairs form their own set of Nb tests,
+    the other pairs Nt = P - Nb; the null histogram does not change.  With
+    --structured (expBP) the first hits take expBP tests.  With a PDB map,
+    pairs closer than mind are left out of the ranking and of Nt."""
+    L, P = 120, 120 * 119 // 2
+    s = covgpu.Synth(200, L, 1.5, 30, 3, 10, 10, 0.08, seed=42, tree_kind=1)
+    w = oracle.weights_pb(s.ax)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    bps = [(i, int(s.ct[i])) for i in range(L) if s.ct[i] > i]
+    # planted pairs as WWc; one extra pair listed first as STACKED, then as
+    # WWc: the ranking's any-match rule counts it as a base pair, the hit
+    # list's first-match type does not
+    extra = (1, 7) if (0, 6) not in bps else (2, 9)
+    contacts = [(extra[0], extra[1], oracle.STACKED), (extra[0], extra[1], oracle.WWc)]
+    contacts += [(i + 1, j + 1, oracle.WWc) for i, j in bps]
+    kw = dict(covtype="GTp", nshuffle=5, want_matrices=True, contacts=contacts)
+    one = oracle.rscape(s.ax, w, T, **kw)
+    two = oracle.rscape(s.ax, w, T, samplesize=oracle.SAMPLE_BP, **kw)
+    assert one["Nt"] == P and one["Nb"] == 0 and one["sc_nbp"] == one["sc_thresh"]
+    assert two["Nb"] == len(bps) + 1 and two["Nt"] == P - len(bps) - 1
+    assert np.array_equal(one["null_obs"], two["null_obs"])
+    assert two["sc_thresh"] < two["sc_nbp"]
+    iu = np.triu_indices(L, 1)
+    bp = np.zeros((L, L), bool)
+    for i, j in bps:
+        bp[i, j] = True
+    pv = one["Eval"][iu] / P
+    mult = np.where(bp[iu], two["Nb"], two["Nt"]).astype(np.float64)
+    assert np.allclose(two["Eval"][iu], pv * mult, rtol=1e-14, atol=0)
+    nbp = lambda r: sum(1 for (i, j, sc, E, p) in r["hits"] if bp[i, j])
+    assert nbp(two) >= nbp(one) and nbp(two) >= 1
+    # --structured: expBP tests for the first hits
+    for expBP in (3.5, 1e9):
+        st = oracle.rscape(s.ax, w, T, expBP=expBP, **kw)
+        ref = _replay_structured(one["Eval"], P, expBP, 0.05)
+        assert np.allclose(st["Eval"][iu], ref[iu], rtol=1e-14, atol=0)
+        assert len(st["hits"]) == int(np.sum(ref[iu] < 0.05))
+    # the PDB distance rule: pairs with j - i < 4 are not ranked
+    m2p = np.arange(L, dtype=np.int32)
+    pdb = oracle.rscape(s.ax, w, T, msa2pdb=m2p, mind=4, **kw)
+    assert pdb["Nt"] == P - (3 * L - 6)
+    assert pdb["h_n"] == 5 * (P - (3 * L - 6))
