@@ -19,6 +19,7 @@
  */
 #ifndef COVGPU_H
 #define COVGPU_H
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -241,6 +242,11 @@ int  covgpu_hist_full(covgpu_ctx *ctx, const double *COV, double bmin, double w,
  * times Nt tests; Eval full L x L (may be NULL); pairs with E < thresh */
 int  covgpu_evalue_full(covgpu_ctx *ctx, const double *COV, const void *h, const double *survfit, double Nt,
                         double thresh, double *Eval, covgpu_hit *hits, int hitcap, int *nhit);
+/* page-lock (pin) a host array the caller copies to and from the device,
+ * and undo it before the array is freed; 0, or 90 when the driver refuses
+ * (the copies then run unpinned) */
+int  covgpu_host_pin(void *p, size_t bytes);
+void covgpu_host_unpin(void *p);
 /* covgpu_evalue_full with the two-set test and --structured
  * (cov_CreateHitList, src/covariation.c:828-870): pair n = i (2L - i - 1)/2
  * + j - i - 1 takes Nb tests when bit n of bpmask (may be NULL) is set; any

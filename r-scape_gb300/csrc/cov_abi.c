@@ -41,7 +41,31 @@ typedef struct {
   int         have_counts;
   int         cov_on_dev;  /* device-resident mode: the device holds mi's current scores */
   double     *wgt;        /* weights of the uploaded alignment */
+  void       *pinned[5];  /* host arrays page-locked for the copies (pp, nseff, ngap, COV, Eval) */
 } gpu_state;
+
+/* host-array mode copies pp (L^2 16 doubles), nseff, ngap, COV and Eval
+ * between host and device for every alignment: page-locked once per
+ * mutual_s, those copies run at the link's DMA rate */
+static void
+pin_host(struct mutual_s *mi, gpu_state *g)
+{
+  const size_t LL = (size_t)mi->alen * (size_t)mi->alen;
+  void  *p[5] = {mi->pp[0][0], mi->nseff[0], mi->ngap[0], mi->COV->mx[0], mi->Eval->mx[0]};
+  size_t n[5] = {LL * 16 * sizeof(double), LL * sizeof(double), LL * sizeof(double), LL * sizeof(double),
+                 LL * sizeof(double)};
+  int k;
+  if (mi->device_resident) return;
+  for (k = 0; k < 5; k++)
+    if (!g->pinned[k] && covgpu_host_pin(p[k], n[k]) == 0) g->pinned[k] = p[k];
+}
+
+static void
+unpin_host(gpu_state *g)
+{
+  int k;
+  for (k = 0; k < 5; k++) { covgpu_host_unpin(g->pinned[k]); g->pinned[k] = NULL; }
+}
 
 /* the score matrix to hand to the engine: NULL = the device's own copy */
 static const double *
@@ -69,6 +93,7 @@ gpu(struct mutual_s *mi, char *errbuf)
       return NULL;
     }
   }
+  pin_host(mi, g);
   return g;
 }
 
@@ -94,8 +119,23 @@ dmx_destroy(ESL_DMATRIX *D)
 static void
 dmx_set(ESL_DMATRIX *D, double v)
 {
-  size_t k, n = (size_t)D->n * D->m;
+  const int64_t n = (int64_t)D->n * D->m;
+  int64_t k;
+#pragma omp parallel for schedule(static)
   for (k = 0; k < n; k++) D->mx[0][k] = v;
+}
+
+/* zero n doubles with the host's threads (corr_Reuse clears L^2 16 of them) */
+static void
+zero_doubles(double *p, size_t n)
+{
+  const int64_t nc = (int64_t)((n + 65535) / 65536);
+  int64_t c;
+#pragma omp parallel for schedule(static)
+  for (c = 0; c < nc; c++) {
+    const size_t a = (size_t)c * 65536, b = (a + 65536 < n) ? a + 65536 : n;
+    memset(p + a, 0, sizeof(double) * (b - a));
+  }
 }
 
 /* ---------------------------------------------------------------------- */
@@ -160,9 +200,9 @@ corr_Reuse(struct mutual_s *mi, int ishuffled, COVTYPE mitype, COVCLASS miclass)
   const size_t L = (size_t)mi->alen;
   mi->ishuffled = ishuffled;
   if (!mi->device_resident) {   /* device-resident: pp, nseff, ngap live on the device */
-    memset(mi->pp[0][0], 0, sizeof(double) * L * L * 16);
-    memset(mi->nseff[0], 0, sizeof(double) * L * L);
-    memset(mi->ngap[0], 0, sizeof(double) * L * L);
+    zero_doubles(mi->pp[0][0], L * L * 16);
+    zero_doubles(mi->nseff[0], L * L);
+    zero_doubles(mi->ngap[0], L * L);
   }
   memset(mi->pm[0], 0, sizeof(double) * L * 4);
   memset(mi->ps[0], 0, sizeof(double) * L * 5);
@@ -175,7 +215,7 @@ corr_Destroy(struct mutual_s *mi)
   gpu_state *g;
   if (!mi) return;
   g = (gpu_state *)mi->gpu;
-  if (g) { covgpu_destroy(g->ctx); free(g->wgt); free(g); }
+  if (g) { unpin_host(g); covgpu_destroy(g->ctx); free(g->wgt); free(g); }
   if (mi->pp)    { if (mi->pp[0]) free(mi->pp[0][0]); free(mi->pp[0]); free(mi->pp); }
   if (mi->nseff) { free(mi->nseff[0]); free(mi->nseff); }
   if (mi->ngap)  { free(mi->ngap[0]); free(mi->ngap); }
@@ -322,9 +362,12 @@ corr_ValidateProbs(struct mutual_s *mi, double tol, int verbose, char *errbuf)
   if (mi->device_resident && g && g->have_counts) {
     if (covgpu_validate_probs(g->ctx, tol)) XFAIL(eslFAIL, errbuf, "pp validation failed");
   } else {
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 8) reduction(| : bad) private(j)
     for (i = 0; i < mi->alen - 1; i++)
-      for (j = i + 1; j < mi->alen; j++)
-        if (validate_vec(mi->pp[i][j], 16, tol)) XFAIL(eslFAIL, errbuf, "pp validation failed");
+      for (j = i + 1; j < mi->alen && !bad; j++)
+        if (validate_vec(mi->pp[i][j], 16, tol)) bad = 1;
+    if (bad) XFAIL(eslFAIL, errbuf, "pp validation failed");
   }
   for (i = 0; i < mi->alen; i++) {
     if (validate_vec(mi->pm[i], 4, tol)) XFAIL(eslFAIL, errbuf, "pm validation failed");

@@ -80,6 +80,7 @@ struct covgpu_ctx {
   double* d_full = nullptr;
   double* d_pcls = nullptr;         // covgpu_pair_classes outputs [3][capL(capL-1)/2]
   uint32_t* d_bpmask = nullptr;     // covgpu_evalue_sets: the base-pair bitmap [capL(capL-1)/2 bits]
+  double* d_pphost = nullptr;       // covgpu_get_probs: pp, nseff, ngap in the host layout [capL^2 (16 + 2)]
   UmmaPlan* umma = nullptr;
   FitWork* fitw[MAXOUT] = {};
   // simulator
@@ -110,6 +111,10 @@ struct covgpu_ctx {
   bool cnt_valid = false;
   int cnt_first = 0, cnt_nslots = 0, cnt_counter = -1;
   cudaEvent_t ev[6] = {};
+  // the statistics' tail fits run side by side, one stream each (a fit is a
+  // cooperative launch of a few dozen small blocks)
+  cudaStream_t fst[MAXOUT] = {};
+  cudaEvent_t fev[MAXOUT + 1] = {};
   double tms[5] = {0, 0, 0, 0, 0};
   double fit_ms = 0.0;
   int nlaunch = 0;
@@ -159,6 +164,8 @@ extern "C" int covgpu_create(covgpu_ctx** ret, int device, int N, int L, int max
   CK(cudaSetDevice(device));
   CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
   for (auto& e : ctx->ev) CK(cudaEventCreate(&e));
+  for (auto& f : ctx->fst) CK(cudaStreamCreateWithFlags(&f, cudaStreamNonBlocking));
+  for (auto& e : ctx->fev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   std::vector<TileRC> tiles;
   std::vector<int> tindex((size_t)ctx->nT * ctx->nT, -1);
   for (int I = 0; I < ctx->nT; I++)
@@ -216,7 +223,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
                   ctx->d_left, ctx->d_right, ctx->d_lnodes, ctx->d_fitch, ctx->d_scratch, ctx->d_obs, ctx->d_sf,
                   ctx->d_tail, ctx->d_nhits, ctx->d_hi, ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->d_full,
                   ctx->d_flush, ctx->d_pmdf, ctx->d_colxf, ctx->d_apcf, ctx->d_evt, ctx->d_pcls,
-                  ctx->d_bpmask};
+                  ctx->d_bpmask, ctx->d_pphost};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (ctx->umma) umma_plan_destroy(ctx->umma);
   for (FitWork* f : ctx->fitw) if (f) fitwork_destroy(f);
@@ -225,6 +232,8 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
                   ctx->d_feat, ctx->d_gsc, ctx->d_pbscr};
   for (void* p : sims) if (p) cudaFree(p);
   for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
+  for (auto& e : ctx->fev) if (e) cudaEventDestroy(e);
+  for (auto& f : ctx->fst) if (f) { cudaStreamSynchronize(f); cudaStreamDestroy(f); }
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
 }
@@ -844,48 +853,24 @@ extern "C" int covgpu_get_probs(covgpu_ctx* ctx, int slot, const double* wgt, do
     memcpy(ps, t.data(), (size_t)L * 5 * sizeof(double));
   }
   if (pp || nseff || ngap) {
-    const size_t ntl = ctx->ntiles;
-    std::vector<float> c(ntl * 32 * TPP);
-    CK(cudaMemcpyAsync(c.data(), ctx->d_cnt + (size_t)rel * ntl * 32 * TPP, c.size() * sizeof(float),
-                       cudaMemcpyDeviceToHost, ctx->st));
-    CK(cudaStreamSynchronize(ctx->st));
     // ngap = (sum of the weights) - nseff, both of the quantised weights the
     // counts were made from (wgt, when given, for the exact total)
     double wt = ctx->wtot_q;
     if (wgt) { wt = 0.0; for (int s = 0; s < N; s++) wt += wgt[s]; }
-    std::vector<TileRC> tiles(ntl);
-    CK(cudaMemcpy(tiles.data(), ctx->d_tiles, ntl * sizeof(TileRC), cudaMemcpyDeviceToHost));
-    // the reference's host layout, filled over the host threads (every pair
-    // belongs to one tile, so the tiles' writes are disjoint)
-    const int64_t LL = (int64_t)L * L;
-#pragma omp parallel for schedule(static)
-    for (int64_t k = 0; k < LL; k++) {
-      if (nseff) nseff[k] = 0.0;
-      if (ngap) ngap[k] = 0.0;
-      if (pp) for (int q = 0; q < 16; q++) pp[k * 16 + q] = 0.0;
-    }
-#pragma omp parallel for schedule(dynamic, 8)
-    for (int64_t t = 0; t < (int64_t)ntl; t++)
-      for (int p = 0; p < TPP; p++) {
-        const int i = tiles[t].I * TP + p / TP, j = tiles[t].J * TP + p % TP;
-        if (!(i < j && j < L)) continue;
-        double C[16], ne = 0.0, sum = 0.0;
-        for (int q = 0; q < 16; q++) {
-          C[q] = (double)c[(t * 32 + 2 * q) * TPP + p] + (double)c[(t * 32 + 2 * q + 1) * TPP + p];
-          ne += C[q];
-        }
-        if (nseff) nseff[(int64_t)i * L + j] = nseff[(int64_t)j * L + i] = ne;
-        if (ngap) ngap[(int64_t)i * L + j] = wt - ne;
-        if (pp) {
-          for (int q = 0; q < 16; q++) sum += 1e-10 + C[q];
-          for (int x = 0; x < 4; x++)
-            for (int y = 0; y < 4; y++) {
-              const double v = (1e-10 + C[x * 4 + y]) / sum;
-              pp[((int64_t)i * L + j) * 16 + x * 4 + y] = v;
-              pp[((int64_t)j * L + i) * 16 + y * 4 + x] = v;
-            }
-        }
-      }
+    // the reference's host layout, made on the device and copied in one
+    // transfer per array (the diagonal and ngap's lower triangle stay zero)
+    const size_t LL = (size_t)L * L;
+    if (!ctx->d_pphost) CK(dalloc(&ctx->d_pphost, (size_t)ctx->capL * ctx->capL * 18));
+    double* dpp = ctx->d_pphost;
+    double* dns = dpp + LL * 16;
+    double* dng = dns + LL;
+    CK(cudaMemsetAsync(dpp, 0, LL * 18 * sizeof(double), ctx->st));
+    CK(launch_probs_host_layout(ctx->d_cnt + (size_t)rel * ctx->ntiles * 32 * TPP, ctx->d_tiles, ctx->ntiles, L, wt,
+                                pp ? dpp : nullptr, nseff ? dns : nullptr, ngap ? dng : nullptr, ctx->st));
+    if (pp) CK(cudaMemcpyAsync(pp, dpp, LL * 16 * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    if (nseff) CK(cudaMemcpyAsync(nseff, dns, LL * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    if (ngap) CK(cudaMemcpyAsync(ngap, dng, LL * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
   }
   return 0;
 }
@@ -1159,9 +1144,11 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   }
 
   // phase 2: the histograms on the host, tail by mass, the tail fits
-  // (gamma: likelihood on the device, one search per statistic back to back)
+  // (gamma: likelihood on the device, the statistics' searches side by side
+  // on their own streams, forked from and joined back into the main one)
   auto tf0 = std::chrono::steady_clock::now();
   bool any_fit = false;
+  CK(cudaEventRecord(ctx->fev[MAXOUT], ctx->st));
   for (int q = 0; q < ntypes; q++) {
     RsStat& X = S.q[q];
     if (!X.active) continue;
@@ -1169,8 +1156,14 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
     if (!p->doexpfit) {
       const ESL_HISTOGRAM* h = X.h;
       if (!ctx->fitw[q]) ctx->fitw[q] = fitwork_create();
-      const int fs = gamma_fit_launch(ctx->fitw[q], h->obs, h->cmin, h->imax, h->bmin, h->w, h->phi, ctx->st);
-      if (fs) return fail(ctx, 32, "could not do a Gamma fit (%d)", fs);
+      CK(cudaStreamWaitEvent(ctx->fst[q], ctx->fev[MAXOUT], 0));
+      const int fs = gamma_fit_launch(ctx->fitw[q], h->obs, h->cmin, h->imax, h->bmin, h->w, h->phi, ctx->fst[q]);
+      if (fs) {
+        cudaStreamSynchronize(ctx->fst[q]);
+        return fail(ctx, 32, "could not do a Gamma fit (%d)", fs);
+      }
+      CK(cudaEventRecord(ctx->fev[q], ctx->fst[q]));
+      CK(cudaStreamWaitEvent(ctx->st, ctx->fev[q], 0));
       ctx->nlaunch += 1;
       any_fit = true;
     }
@@ -1206,11 +1199,16 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   std::vector<double>& sfh = ctx->h_sf;      // every entry is written by the copy below
   sfh.resize(std::max<int64_t>(sf_tot, 1));
   if (sf_tot > 0) {
+    // the survival tables side by side, as the fits
+    CK(cudaEventRecord(ctx->fev[MAXOUT], ctx->st));
     for (int q = 0; q < ntypes; q++) {
       const RsStat& X = S.q[q];
       if (!X.have_sf) continue;
+      CK(cudaStreamWaitEvent(ctx->fst[q], ctx->fev[MAXOUT], 0));
       CK(launch_survfit(X.h->cmin, X.h->nb, X.h->bmin, X.h->w, X.newmass, p->doexpfit, X.mu, X.lambda, X.tau,
-                        ctx->d_sf + X.sf_off, ctx->st));
+                        ctx->d_sf + X.sf_off, ctx->fst[q]));
+      CK(cudaEventRecord(ctx->fev[q], ctx->fst[q]));
+      CK(cudaStreamWaitEvent(ctx->st, ctx->fev[q], 0));
       ctx->nlaunch += 1;
     }
     CK(cudaMemcpyAsync(sfh.data(), ctx->d_sf, (size_t)sf_tot * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
@@ -1749,6 +1747,17 @@ extern "C" int covgpu_evalue_sets(covgpu_ctx* ctx, const double* COV, const void
     std::copy(got.begin(), got.begin() + nget, hits);
   }
   return 0;
+}
+
+// page-locks a host array for the copies to and from the device (the
+// drop-in's pp, nseff, ngap, COV and Eval); 0, or 90 when the driver refuses
+extern "C" int covgpu_host_pin(void* p, size_t bytes) {
+  if (!p || bytes == 0) return 0;
+  return cudaHostRegister(p, bytes, cudaHostRegisterDefault) == cudaSuccess ? 0 : (cudaGetLastError(), 90);
+}
+
+extern "C" void covgpu_host_unpin(void* p) {
+  if (p) cudaHostUnregister(p);
 }
 
 extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void* hv, const double* survfit,

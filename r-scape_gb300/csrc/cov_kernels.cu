@@ -1193,6 +1193,51 @@ k_evalue(const float2* __restrict__ cov, const TileRC* __restrict__ tiles, int n
   evalue_body(native_grid(), cov, tiles, ntiles, L, T, B, K, evt, nhits, hitcap, hi, hj, hsc, hE, hp);
 }
 
+// pp, nseff and ngap of every pair in the reference's host layout
+// (mi->pp[i][j][16], nseff[i][j], ngap[i][j]) from the double-float counts:
+// C_q = hi + lo, nseff = sum_q C_q, pp = (1e-10 + C_xy) / sum_q (1e-10 + C_q)
+// at [i][j][4x + y] and [j][i][4y + x] (src/correlators.c:1300-1317,
+// 1695-1780), ngap[i][j] = wt - nseff, all in FP64 in that order
+__global__ void __launch_bounds__(256)
+k_probs_host_layout(const float* __restrict__ cnt, const TileRC* __restrict__ tiles, int L, double wt,
+                    double* __restrict__ pp, double* __restrict__ nseff, double* __restrict__ ngap) {
+  const int t = blockIdx.x, tid = threadIdx.x;
+  const TileRC tr = tiles[t];
+  const float* Cb = cnt + (int64_t)t * 32 * TPP;
+  for (int k = 0; k < 4; k++) {
+    const int p = tid + 256 * k;
+    const int i = tr.I * TP + (p >> 5), j = tr.J * TP + (p & 31);
+    if (!(i < j && j < L)) continue;
+    double C[16], ne = 0.0, sum = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      C[q] = __dadd_rn((double)Cb[(2 * q) * TPP + p], (double)Cb[(2 * q + 1) * TPP + p]);
+      ne = __dadd_rn(ne, C[q]);
+    }
+    const int64_t ij = (int64_t)i * L + j, ji = (int64_t)j * L + i;
+    if (nseff) { nseff[ij] = ne; nseff[ji] = ne; }
+    if (ngap) ngap[ij] = __dsub_rn(wt, ne);
+    if (pp) {
+#pragma unroll
+      for (int q = 0; q < 16; q++) sum = __dadd_rn(sum, __dadd_rn(1e-10, C[q]));
+#pragma unroll
+      for (int x = 0; x < 4; x++)
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+          const double v = __ddiv_rn(__dadd_rn(1e-10, C[x * 4 + y]), sum);
+          pp[ij * 16 + x * 4 + y] = v;
+          pp[ji * 16 + y * 4 + x] = v;
+        }
+    }
+  }
+}
+
+cudaError_t launch_probs_host_layout(const float* cnt, const TileRC* tiles, int ntiles, int L, double wt, double* pp,
+                                     double* nseff, double* ngap, cudaStream_t st) {
+  if (ntiles > 0) k_probs_host_layout<<<ntiles, 256, 0, st>>>(cnt, tiles, L, wt, pp, nseff, ngap);
+  return cudaGetLastError();
+}
+
 // tile-packed -> full symmetric L x L (diagonal = diag)
 __device__ __forceinline__ double to_d(double v) { return v; }
 __device__ __forceinline__ double to_d(float2 v) { return (double)v.x + (double)v.y; }

@@ -78,6 +78,10 @@ void make_limbs(const double* w, int N, int stride, uint16_t* lim, CountWeights*
 
 cudaError_t launch_count_simt(const uint8_t* ax, int64_t slot_stride, const CountWeights& W, bool unit, int N, int Lp,
                               const TileRC* tiles, int ntiles, int nslots, float* cnt, cudaStream_t st);
+// pp [L][L][16], nseff [L][L], ngap [L][L] (each may be null) of the tiles'
+// double-float counts in the reference's host layout
+cudaError_t launch_probs_host_layout(const float* cnt, const TileRC* tiles, int ntiles, int L, double wt, double* pp,
+                                     double* nseff, double* ngap, cudaStream_t st);
 cudaError_t launch_pair_marg(const float* cnt, int L, const TileRC* tiles, int ntiles, int nT, int nslots,
                              double* part4, double* partR, cudaStream_t st);
 cudaError_t launch_pm_final(const double* part4, const double* partR, int L, int Lp, int nT, int nslots, double* pm,

@@ -8,6 +8,7 @@ import ctypes as C
 
 import numpy as np
 
+
 class Alphabet(C.Structure):
     _fields_ = [("type", C.c_int), ("K", C.c_int), ("Kp", C.c_int)]
 
@@ -123,6 +124,18 @@ class MsaHolder:
         self.msa = Msa(self.ptrs, self.w.ctypes.data_as(C.POINTER(C.c_double)), N, L, C.pointer(abc))
 
 
+def bin2bin(h, c, b):
+    """cov_ranklist_Bin2Bin (src/covariation.c:2334-2362) for the bins b of
+    histogram h into histogram c, in FP64 as the library computes it: the
+    bins and whether each lies in [0, c.nb)."""
+    x = h.w * np.asarray(b, dtype=np.float64) + h.bmin
+    v = (x - c.bmin) / c.w
+    t = np.trunc(v)
+    r = t + np.where(np.abs(v - t) >= 0.5, np.sign(v), 0.0)   # C's round(): halves away from zero
+    ok = np.isfinite(r) & (r >= 0) & (r < c.nb)
+    return np.where(ok, r, -1).astype(np.int64), ok
+
+
 def null_add(lib, rl, cum):
     """null_add2cumranklist, src/R-scape.c:1564-1612."""
     h = rl.contents.ha.contents
@@ -137,13 +150,21 @@ def null_add(lib, rl, cum):
         c.xmin, c.xmax = min(c.xmin, h.xmin), max(c.xmax, h.xmax)
         c.imin, c.imax = min(c.imin, h.imin), max(c.imax, h.imax)
     c = cum.contents.ha.contents
-    for b in range(h.imin, h.imax + 1):
-        cb = C.c_int()
-        lib.cov_ranklist_Bin2Bin(b, rl.contents.ha, cum.contents.ha, C.byref(cb))
-        if cb.value < c.nb:
-            c.obs[cb.value] += h.obs[b]
-            c.Nc += h.obs[b]
-            c.No += h.obs[b]
+    if h.imax < h.imin:
+        return cum
+    # the reference's loop over bins imin..imax, where only the non-empty
+    # bins change the sum, mapped as cov_ranklist_Bin2Bin maps them
+    # (src/covariation.c:2334-2362): x = w b + bmin, then C's round() of
+    # (x - bmin') / w' (halves away from zero), all in FP64
+    obs = np.ctypeslib.as_array(h.obs, shape=(h.nb,))
+    cobs = np.ctypeslib.as_array(c.obs, shape=(c.nb,))
+    b = np.flatnonzero(obs[h.imin:h.imax + 1]) + h.imin
+    r, ok = bin2bin(h, c, b)
+    add = obs[b[ok]]
+    np.add.at(cobs, r[ok], add)
+    n = int(add.sum())
+    c.Nc += n
+    c.No += n
     return cum
 
 

@@ -109,6 +109,34 @@ def test_histogram_io_roundtrip(covgpu, tmp_path):
     lib.cov_FreeRankList(r2)
 
 
+def test_null_merge_bin_mapping_matches_the_library(covgpu):
+    """rscape_abi.bin2bin (the vectorised mapping of the callers' null
+    merge, null_add2cumranklist at src/R-scape.c:1564-1612) gives the
+    library's cov_ranklist_Bin2Bin for every bin, including halves and bins
+    outside the target."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("rscape_abi", os.path.join(os.path.dirname(covgpu.LIBPATH),
+                                                                               "rscape_abi.py"))
+    abi = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(abi)
+    lib = abi.setup_lib(covgpu.LIBPATH)
+    rng = np.random.default_rng(3)
+    cb = ctypes.c_int()
+    for trial in range(60):
+        w = float(rng.choice([0.05, 0.013, 0.0071, 1e-3, 0.25, 0.1]))
+        bmin = float(rng.choice([-10.0, rng.uniform(-20, -5)]))
+        rl = lib.cov_CreateRankList(float(rng.uniform(5, 60)), bmin, w)
+        cum = lib.cov_CreateRankList(float(rng.uniform(5, 60)),
+                                     float(rng.choice([bmin, bmin - 20 * w, rng.uniform(-30, bmin)])), w)
+        h, c = rl.contents.ha.contents, cum.contents.ha.contents
+        r, ok = abi.bin2bin(h, c, np.arange(h.nb))
+        for k in range(h.nb):
+            lib.cov_ranklist_Bin2Bin(k, rl.contents.ha, cum.contents.ha, ctypes.byref(cb))
+            assert r[k] == (cb.value if 0 <= cb.value < c.nb else -1), (trial, k)
+        lib.cov_FreeRankList(rl)
+        lib.cov_FreeRankList(cum)
+
+
 def test_default_parameters_are_the_reference_defaults(covgpu):
     """covgpu_params_default against R-scape's defaults: -E 0.05
     (src/R-scape.c:258), CSELECT with nseqthresh 8 and alenthresh 50 (:345-347),
