@@ -349,8 +349,9 @@ def dropin_flow(cg, e, ax, w, ns):
         for rep in range(2):
             data = abi.Data(C.pointer(rnd), 3, None, None, mi, C.pointer(th), 1, 0, abi.RANSS, code, N, -1.0, -10.0,
                             0.05, 1.0, 0.0005, 0, 0.0, 0.0, 0.0, None, 1e-6, 0, C.cast(errbuf, C.c_char_p))
+            steps = {}
             t0 = time.perf_counter()
-            rl, hl, cum = abi.rscape_flow(lib, mi, nulls, real, data, code)
+            rl, hl, cum = abi.rscape_flow(lib, mi, nulls, real, data, code, timing=steps)
             dt = time.perf_counter() - t0
             first = dt if first is None else first
             nhit = hl.contents.nhit
@@ -359,7 +360,8 @@ def dropin_flow(cg, e, ax, w, ns):
             lib.cov_FreeRankList(cum)
         lib.corr_Destroy(mi)
         out[name] = {"seconds": dt, "msas_per_s": 1.0 / dt, "column_pairs_per_s": (ns + 2) * L * (L - 1) / 2 / dt,
-                     "hits": nhit, "first_flow_seconds": first}
+                     "hits": nhit, "first_flow_seconds": first,
+                     "step_seconds": {k: round(v, 4) for k, v in steps.items()}}
     return out
 
 

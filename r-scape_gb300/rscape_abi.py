@@ -168,35 +168,48 @@ def null_add(lib, rl, cum):
     return cum
 
 
-def rscape_flow(lib, mi, nulls, real, data, code):
+def rscape_flow(lib, mi, nulls, real, data, code, timing=None):
     """R-scape's per-alignment path through the reference-named entry points
     (src/R-scape.c:1614-1724, 2502): calculate_width_histo on the first null
     (:1281-1371), cov_Calculate in RANSS mode on every null merged into the
     cumulative null histogram, then cov_Calculate in GIVSS mode on the
     alignment.  nulls and real are MsaHolder objects; data is the caller's
-    struct data_s.  Returns (ranklist, hitlist, cumulative null ranklist)."""
+    struct data_s.  With a dict for timing, the wall seconds of each step
+    (corr_Reuse, the nulls' cov_Calculate, the merge, the alignment's
+    cov_Calculate) are added to it.  Returns (ranklist, hitlist, cumulative
+    null ranklist)."""
+    import time
+
+    def step(name, f, *a):
+        t0 = time.perf_counter()
+        r = f(*a)
+        if timing is not None:
+            timing[name] = timing.get(name, 0.0) + time.perf_counter() - t0
+        return r
+
     data.mode = RANSS
     data.ranklist_null = None
     cum = None
     errbuf = data.errbuf
     for k, nm in enumerate(nulls):
         if k == 0:
-            lib.corr_Reuse(mi, 1, code, 3)
-            if lib.cov_Calculate(C.byref(data), C.byref(nm.msa), None, None, None, 0):
+            step("corr_Reuse", lib.corr_Reuse, mi, 1, code, 3)
+            if step("cov_Calculate_nulls", lib.cov_Calculate, C.byref(data), C.byref(nm.msa), None, None, None, 0):
                 raise RuntimeError(errbuf)
             m = mi.contents
             data.w = min(0.05, (m.maxCOV - max(-10.0, m.minCOV)) / 400)
-        lib.corr_Reuse(mi, 1, code, 3)
+        step("corr_Reuse", lib.corr_Reuse, mi, 1, code, 3)
         rl = C.POINTER(RankList)()
-        if lib.cov_Calculate(C.byref(data), C.byref(nm.msa), C.byref(rl), None, None, 1):
+        if step("cov_Calculate_nulls", lib.cov_Calculate, C.byref(data), C.byref(nm.msa), C.byref(rl), None, None, 1):
             raise RuntimeError(errbuf)
-        cum = null_add(lib, rl, cum)
+        cum = step("null_merge", null_add, lib, rl, cum)
         lib.cov_FreeRankList(rl)
     data.mode = GIVSS
     data.ranklist_null = cum
-    lib.corr_Reuse(mi, 0, code, 3)
+    step("corr_Reuse", lib.corr_Reuse, mi, 0, code, 3)
     rl = C.POINTER(RankList)()
     hl = C.POINTER(HitList)()
-    if lib.cov_Calculate(C.byref(data), C.byref(real.msa), C.byref(rl), C.byref(hl), None, 1):
+    if step("cov_Calculate_alignment", lib.cov_Calculate, C.byref(data), C.byref(real.msa), C.byref(rl), C.byref(hl),
+            None, 1):
         raise RuntimeError(errbuf)
     return rl, hl, cum
