@@ -306,10 +306,11 @@ extern "C" int covgpu_set_alignment(covgpu_ctx* ctx, int slot, const uint8_t* ax
   if (slot < 0 || slot >= ctx->maxslots) return fail(ctx, 11, "slot %d out of range", slot);
   CK(cudaSetDevice(ctx->dev));
   ctx->cnt_valid = false;
-  // the largest code first (a reduction the compiler vectorises); the
+  // the largest code first (a reduction over the host threads); the
   // position of a bad code is looked up only when there is one
   const int64_t n = (int64_t)ctx->N * ctx->L;
   uint8_t mx = 0;
+#pragma omp parallel for reduction(max : mx) schedule(static) if (n > (1 << 20))
   for (int64_t k = 0; k < n; k++) mx = std::max(mx, ax[k]);
   if (mx > 17)
     for (int64_t k = 0; k < n; k++)
