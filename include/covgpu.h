@@ -47,6 +47,15 @@ typedef struct {
   uint64_t seed;         /* 42 */
   double   allow[16];    /* allowed pairs (AU UA CG GC GU UG) */
   int      counter;      /* COVGPU_COUNT_SIMT or COVGPU_COUNT_TENSOR */
+  /* the two-set test (R-scape -s) and --structured, covgpu_rscape only:
+   * the given structure's contacts, 1-based alignment positions
+   * cnt_i[h] < cnt_j[h] with their BPTYPE (WWc = 0 ... 31, STACKED 32,
+   * CONTACT 33, BPNONE 34), as R-scape's CLIST holds them */
+  int             samplesize;  /* 3 (default): one-set test; 0 contacts, 1 base pairs, 2 WC pairs */
+  int             ncnt;        /* 0 (default): no structure */
+  const int64_t  *cnt_i, *cnt_j;
+  const int      *cnt_type;
+  double          expBP;       /* --structured: expected base pairs; <= 0 (default -1) off */
 } covgpu_params;
 
 typedef struct {
@@ -57,13 +66,15 @@ typedef struct {
   double   minCOV, maxCOV;          /* input alignment, after correction */
   double   null_minCOV, null_maxCOV; /* first null */
   double   pmass, newmass, mu, lambda, tau;
-  double   sc_thresh;     /* score at the E-value threshold */
-  uint64_t Nt;            /* number of tests */
+  double   sc_thresh;     /* score at the E-value threshold (of base pairs in the two-set test: sc_bp) */
+  uint64_t Nt;            /* number of tests (of the pairs outside the structure in the two-set test) */
   int      nhit;          /* pairs with E < thresh (may exceed hitcap) */
   /* cumulative null histogram */
   double   h_bmin, h_w, h_xmin, h_xmax, h_phi;
   int      h_nb, h_imin, h_imax, h_cmin;
   uint64_t h_n, h_Nc, h_No;
+  double   sc_nbp;        /* score at the E-value threshold of the pairs outside the structure */
+  uint64_t Nb;            /* number of tests of the base pairs (0 in the one-set test) */
 } covgpu_result;
 
 typedef struct {

@@ -38,7 +38,9 @@ class Params(C.Structure):
     _fields_ = [("covclass", C.c_int), ("nseqthresh", C.c_int), ("alenthresh", C.c_int), ("nshuffle", C.c_int),
                 ("thresh", C.c_double), ("bmin", C.c_double), ("w0", C.c_double), ("hpts", C.c_int),
                 ("pmass", C.c_double), ("fracfit", C.c_double), ("doexpfit", C.c_int), ("tol", C.c_double),
-                ("seed", C.c_uint64), ("allow", C.c_double * 16), ("counter", C.c_int)]
+                ("seed", C.c_uint64), ("allow", C.c_double * 16), ("counter", C.c_int),
+                ("samplesize", C.c_int), ("ncnt", C.c_int), ("cnt_i", C.c_void_p), ("cnt_j", C.c_void_p),
+                ("cnt_type", C.c_void_p), ("expBP", C.c_double)]
 
 
 class Result(C.Structure):
@@ -49,7 +51,7 @@ class Result(C.Structure):
                 ("nhit", C.c_int), ("h_bmin", C.c_double), ("h_w", C.c_double), ("h_xmin", C.c_double),
                 ("h_xmax", C.c_double), ("h_phi", C.c_double), ("h_nb", C.c_int), ("h_imin", C.c_int),
                 ("h_imax", C.c_int), ("h_cmin", C.c_int), ("h_n", C.c_uint64), ("h_Nc", C.c_uint64),
-                ("h_No", C.c_uint64)]
+                ("h_No", C.c_uint64), ("sc_nbp", C.c_double), ("Nb", C.c_uint64)]
 
 
 class Hit(C.Structure):
@@ -147,17 +149,33 @@ def default_allow():
     return a
 
 
+SAMPLE_CONTACTS, SAMPLE_BP, SAMPLE_WC, SAMPLE_ALL = 0, 1, 2, 3
+
+
 def params(**kw):
+    """covgpu_params with the defaults of covgpu_params_default, overridden
+    by kw.  contacts = [(i, j, bptype), ...] (1-based columns, i < j) gives
+    the structure of the two-set test (with samplesize); the arrays are kept
+    alive on the returned object."""
     p = Params()
     lib().covgpu_params_default(C.byref(p))
+    keep = []
     for k, v in kw.items():
         if k == "allow":
             for i in range(16):
                 p.allow[i] = float(v[i])
             continue
+        if k == "contacts":
+            c = np.asarray(v, dtype=np.int64).reshape(-1, 3)
+            ci, cj = np.ascontiguousarray(c[:, 0]), np.ascontiguousarray(c[:, 1])
+            ct = np.ascontiguousarray(c[:, 2].astype(np.int32))
+            keep += [ci, cj, ct]
+            p.ncnt, p.cnt_i, p.cnt_j, p.cnt_type = len(c), ci.ctypes.data, cj.ctypes.data, ct.ctypes.data
+            continue
         if not hasattr(p, k):
             raise KeyError(k)
         setattr(p, k, v)
+    p._keep = keep
     return p
 
 

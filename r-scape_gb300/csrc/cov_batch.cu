@@ -977,7 +977,7 @@ static int chunk_finish(covgpu_batch* b, Slot& S, const covgpu_params* p, const 
       RsStat& X = XS[k][q];
       const int64_t P = (int64_t)f.L * (f.L - 1) / 2;
       covgpu_result& R = results[(size_t)f.idx * nout + q];
-      rs_tables(p, P, X, sfh.data() + X.sf_off, R, tail.data() + X.tail_off);
+      rs_tables(p, P, 0, X, sfh.data() + X.sf_off, R, tail.data() + X.tail_off);
       StatDev& x = SD[e];
       x.T = rs_evaltables(p, P, X, d_sf + X.sf_off, d_tail + X.tail_off);
       x.K = evalcmp_host(x.T);
@@ -1056,6 +1056,8 @@ extern "C" int covgpu_rscape_families(covgpu_batch* b, const covgpu_params* p, i
     return bfail(b, 11, "bad arguments");
   if (ntypes < 1 || ntypes > MAXOUT) return bfail(b, 11, "1..%d covariation types per call", MAXOUT);
   if (p->counter != COVGPU_COUNT_SIMT && p->counter != COVGPU_COUNT_TENSOR) return bfail(b, 11, "bad counter");
+  if ((p->ncnt > 0 && p->samplesize != 3) || p->expBP > 0.0)
+    return bfail(b, 11, "a structure belongs to one alignment: the two-set test and --structured run in covgpu_rscape");
   // the statistics, as score_async reads them
   Types T;
   T.ntypes = ntypes;

@@ -79,7 +79,10 @@ struct covgpu_ctx {
   int hitcap = 0;
   double* d_full = nullptr;
   double* d_pcls = nullptr;         // covgpu_pair_classes outputs [3][capL(capL-1)/2]
-  uint32_t* d_bpmask = nullptr;     // covgpu_evalue_sets: the base-pair bitmap [capL(capL-1)/2 bits]
+  uint32_t* d_bpmask = nullptr;     // the two-set test's base-pair bitmap [capL(capL-1)/2 bits]
+  int *d_ci = nullptr, *d_cj = nullptr;   // --structured: the hits under the first hits' rule
+  double* d_cd = nullptr;                 // their scores, E-values and p-values [3][ccap]
+  int ccap = 0;
   double* d_pphost = nullptr;       // covgpu_get_probs: pp, nseff, ngap in the host layout [capL^2 (16 + 2)]
   UmmaPlan* umma = nullptr;
   FitWork* fitw[MAXOUT] = {};
@@ -144,6 +147,7 @@ extern "C" void covgpu_params_default(covgpu_params* p) {
   p->covclass = 3; p->nseqthresh = 8; p->alenthresh = 50; p->nshuffle = -1;
   p->thresh = 0.05; p->bmin = -10.0; p->w0 = 0.05; p->hpts = 400; p->pmass = 0.0005; p->fracfit = 1.0;
   p->doexpfit = 0; p->tol = 1e-6; p->seed = 42; p->counter = COVGPU_COUNT_SIMT;
+  p->samplesize = 3; p->expBP = -1.0;
   p->allow[0 * 4 + 3] = p->allow[3 * 4 + 0] = 1.0;   // src/R-scape.c:883-887
   p->allow[1 * 4 + 2] = p->allow[2 * 4 + 1] = 1.0;
   p->allow[2 * 4 + 3] = p->allow[3 * 4 + 2] = 1.0;
@@ -204,7 +208,7 @@ extern "C" int covgpu_create(covgpu_ctx** ret, int device, int N, int L, int max
   CK(dalloc(&ctx->d_mm, S * MAXOUT * 2));
   CK(dalloc(&ctx->d_status, 1));
   CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
-  CK(dalloc(&ctx->d_nhits, MAXOUT));
+  CK(dalloc(&ctx->d_nhits, MAXOUT + 1));   // per statistic, and the --structured pass's
   if (maxnull > 0 && N > 1) {
     CK(dalloc(&ctx->d_fitch, (size_t)maxnull * (N - 1) * ctx->Lp));
     CK(dalloc(&ctx->d_scratch, (size_t)maxnull * (N - 1) * ctx->Lp));
@@ -223,7 +227,7 @@ extern "C" void covgpu_destroy(covgpu_ctx* ctx) {
                   ctx->d_left, ctx->d_right, ctx->d_lnodes, ctx->d_fitch, ctx->d_scratch, ctx->d_obs, ctx->d_sf,
                   ctx->d_tail, ctx->d_nhits, ctx->d_hi, ctx->d_hj, ctx->d_hsc, ctx->d_hE, ctx->d_hp, ctx->d_full,
                   ctx->d_flush, ctx->d_pmdf, ctx->d_colxf, ctx->d_apcf, ctx->d_evt, ctx->d_pcls,
-                  ctx->d_bpmask, ctx->d_pphost};
+                  ctx->d_bpmask, ctx->d_pphost, ctx->d_ci, ctx->d_cj, ctx->d_cd};
   for (void* p : ptrs) if (p) cudaFree(p);
   if (ctx->umma) umma_plan_destroy(ctx->umma);
   for (FitWork* f : ctx->fitw) if (f) fitwork_destroy(f);
@@ -1037,11 +1041,16 @@ int rs_histogram(const covgpu_params* p, double fracfit, int ns, int64_t P, cons
   return 0;
 }
 
-void rs_tables(const covgpu_params* p, int64_t P, RsStat& X, const double* sf, covgpu_result& R, double* tq) {
+void rs_tables(const covgpu_params* p, int64_t P, int64_t Nb, RsStat& X, const double* sf, covgpu_result& R,
+               double* tq) {
   const ESL_HISTOGRAM* h = X.h;
   R.pmass = X.pmass; R.newmass = X.newmass; R.mu = X.mu; R.lambda = X.lambda; R.tau = X.tau;
-  R.Nt = (uint64_t)P;
-  R.sc_thresh = covh_evalue2cov(p->thresh, (double)P, X.h, X.have_sf ? sf : nullptr);
+  // the pairs outside the structure are Nt = P - Nb tests; the thresholds of
+  // base pairs and of the others (src/covariation.c:490-500)
+  R.Nt = (uint64_t)(P - Nb);
+  R.Nb = (uint64_t)Nb;
+  R.sc_thresh = covh_evalue2cov(p->thresh, (double)(Nb > 0 ? Nb : P), X.h, X.have_sf ? sf : nullptr);
+  R.sc_nbp = covh_evalue2cov(p->thresh, (double)(Nb > 0 ? P - Nb : P), X.h, X.have_sf ? sf : nullptr);
   R.h_bmin = h->bmin; R.h_w = h->w; R.h_nb = h->nb; R.h_imin = h->imin; R.h_imax = h->imax; R.h_cmin = h->cmin;
   R.h_n = h->n; R.h_Nc = h->Nc; R.h_No = h->No; R.h_xmin = h->xmin; R.h_xmax = h->xmax; R.h_phi = h->phi;
   // cov2evalue tables: the tail branch's p-values tail[b] / Nc
@@ -1050,15 +1059,93 @@ void rs_tables(const covgpu_params* p, int64_t P, RsStat& X, const double* sf, c
   for (int b = 0; b < h->nb; b++) tq[b] /= (double)h->Nc;
 }
 
-EvalTables rs_evaltables(const covgpu_params* p, int64_t P, const RsStat& X, const double* d_sf, const double* d_tail) {
+EvalTables rs_evaltables(const covgpu_params* p, int64_t Nt, const RsStat& X, const double* d_sf,
+                         const double* d_tail) {
   const ESL_HISTOGRAM* h = X.h;
   EvalTables T;
   T.sf = X.have_sf ? d_sf : nullptr;
   T.ptail = d_tail;
-  T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = (double)P;
+  T.bmin = h->bmin; T.w = h->w; T.phi = h->phi; T.xmax = h->xmax; T.Nc = (double)h->Nc; T.Nt = (double)Nt;
   T.pNc = 1.0 / T.Nc;
   T.thresh = p->thresh; T.nb = h->nb; T.imin = h->imin; T.imax = h->imax;
   return T;
+}
+
+int rs_pair_sets(const covgpu_params* p, int L, std::vector<uint32_t>& bpmask, int64_t* nsel, char* err,
+                 size_t errlen) {
+  const int64_t P = (int64_t)L * (L - 1) / 2;
+  bpmask.clear();
+  *nsel = 0;
+  if (p->ncnt <= 0 || p->samplesize == 3) return 0;
+  if (p->samplesize < 0 || p->samplesize > 3) { snprintf(err, errlen, "samplesize %d", p->samplesize); return 11; }
+  if (!p->cnt_i || !p->cnt_j || !p->cnt_type) { snprintf(err, errlen, "%d contacts without arrays", p->ncnt); return 11; }
+  auto takes = [&](int t) {
+    return p->samplesize == 0 ? t < 34 : (p->samplesize == 1 ? t < 32 : t == 0);
+  };
+  std::vector<uint32_t> sel((size_t)(P + 31) / 32 + 1, 0u), seen((size_t)(P + 31) / 32 + 1, 0u);
+  bpmask.assign((size_t)(P + 31) / 32 + 1, 0u);
+  for (int h = 0; h < p->ncnt; h++) {
+    const int64_t i = p->cnt_i[h], j = p->cnt_j[h];
+    if (i < 1 || j > L || i >= j) continue;   // the reference matches cnt.i == i + 1 < cnt.j == j + 1 only
+    const int64_t n = (i - 1) * (2LL * L - (i - 1) - 1) / 2 + (j - i - 1);
+    const uint32_t bit = 1u << (n & 31);
+    if (!(seen[n >> 5] & bit)) {   // the first contact's type (CMAP_GetBPTYPE)
+      seen[n >> 5] |= bit;
+      if (takes(p->cnt_type[h])) bpmask[n >> 5] |= bit;
+    }
+    if (takes(p->cnt_type[h])) sel[n >> 5] |= bit;   // any contact (CMAP_Is*Local)
+  }
+  for (uint32_t w : sel) *nsel += __builtin_popcount(w);
+  return 0;
+}
+
+// --structured (src/covariation.c:850-854): a pair outside the structure
+// takes expBP tests while fewer than expBP hits precede it in scan order.
+// Up to the hit that brings the count to m = ceil(expBP) every pair follows
+// that rule (Nb tests for the structure's base pairs), so that hit is the
+// m-th of the pairs that are hits under it: one compaction pass of the
+// statistic's scores with the rule, its scan index into *kstar (LLONG_MAX
+// when fewer than m pairs are such hits).
+static int structured_kstar(covgpu_ctx* ctx, const float2* cov, EvalTables T, double expBP, long long* kstar) {
+  const int L = ctx->L;
+  T.Nx = expBP;
+  T.kstar = LLONG_MAX;
+  const long long m = (long long)std::ceil(expBP);
+  for (int round = 0; round < 2; round++) {
+    if (ctx->ccap < 1024) {
+      cudaFree(ctx->d_ci); cudaFree(ctx->d_cj); cudaFree(ctx->d_cd);
+      ctx->d_ci = ctx->d_cj = nullptr; ctx->d_cd = nullptr; ctx->ccap = 0;
+      CK(dalloc(&ctx->d_ci, 1024)); CK(dalloc(&ctx->d_cj, 1024)); CK(dalloc(&ctx->d_cd, 3 * 1024));
+      ctx->ccap = 1024;
+    }
+    const int cap = ctx->ccap;
+    CK(cudaMemsetAsync(ctx->d_nhits + MAXOUT, 0, sizeof(int), ctx->st));
+    CK(launch_evalue(cov, ctx->d_tiles, ctx->ntiles, L, T, nullptr, ctx->d_nhits + MAXOUT, cap, ctx->d_ci, ctx->d_cj,
+                     ctx->d_cd, ctx->d_cd + cap, ctx->d_cd + 2 * cap, ctx->st));
+    int nc = 0;
+    CK(cudaMemcpyAsync(&nc, ctx->d_nhits + MAXOUT, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->nlaunch += 1;
+    if (nc > cap) {   // room for all of them, then once more
+      cudaFree(ctx->d_ci); cudaFree(ctx->d_cj); cudaFree(ctx->d_cd);
+      ctx->d_ci = ctx->d_cj = nullptr; ctx->d_cd = nullptr; ctx->ccap = 0;
+      CK(dalloc(&ctx->d_ci, nc)); CK(dalloc(&ctx->d_cj, nc)); CK(dalloc(&ctx->d_cd, 3 * (size_t)nc));
+      ctx->ccap = nc;
+      continue;
+    }
+    std::vector<int> ci(nc), cj(nc);
+    if (nc > 0) {
+      CK(cudaMemcpy(ci.data(), ctx->d_ci, nc * sizeof(int), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(cj.data(), ctx->d_cj, nc * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    std::vector<long long> n(nc);
+    for (int k = 0; k < nc; k++) n[k] = (long long)ci[k] * (2LL * L - ci[k] - 1) / 2 + (cj[k] - ci[k] - 1);
+    if ((long long)nc < m) { *kstar = LLONG_MAX; return 0; }
+    std::nth_element(n.begin(), n.begin() + (m - 1), n.end());
+    *kstar = n[m - 1];
+    return 0;
+  }
+  return fail(ctx, 90, "--structured: the hit count changed between two passes");
 }
 
 extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint8_t* ax, const double* wgt,
@@ -1080,6 +1167,10 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
   if (wgt && (s = covgpu_set_weights(ctx, wgt))) return s;
   if (ax && (s = covgpu_set_alignment(ctx, 0, ax))) return s;
   if (!ctx->have_w) return fail(ctx, 11, "weights not set");
+  // the two-set test's pairs (none in the one-set test)
+  std::vector<uint32_t> bpmask;
+  int64_t Nb = 0;
+  if ((s = rs_pair_sets(p, L, bpmask, &Nb, ctx->err, sizeof(ctx->err)))) return s;
   double fracfit = p->fracfit;
   const int ns = rs_nshuffle(p, N, L, &fracfit);
   if (ns > ctx->maxnull || ns + 1 > ctx->maxslots)
@@ -1227,16 +1318,34 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
     if (getenv("COVGPU_DEBUG"))
       fprintf(stderr, "covgpu: type %d nb %d tail bins %d fit %.2f ms (%d evaluations) mu %g lambda %g tau %g\n",
               covtypes[q], X.h->nb, X.h->imax - X.h->cmin + 1, ctx->fit_ms, X.evals, X.mu, X.lambda, X.tau);
-    rs_tables(p, P, X, sfh.data() + X.sf_off, results[q], tail.data() + X.tail_off);
+    rs_tables(p, P, Nb, X, sfh.data() + X.sf_off, results[q], tail.data() + X.tail_off);
   }
   int nhit[MAXOUT] = {0, 0, 0, 0};
   if (tail_tot > 0) {
     CK(cudaMemcpyAsync(ctx->d_tail, tail.data(), (size_t)tail_tot * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    if (!bpmask.empty()) {
+      const size_t capw = (size_t)(((int64_t)ctx->capL * (ctx->capL - 1) / 2 + 31) / 32) + 1;
+      if (!ctx->d_bpmask) CK(dalloc(&ctx->d_bpmask, capw));
+      CK(cudaMemcpyAsync(ctx->d_bpmask, bpmask.data(), (size_t)((P + 31) / 32) * sizeof(uint32_t),
+                         cudaMemcpyHostToDevice, ctx->st));
+    }
+    // --structured: where the first hits' rule ends, per statistic
+    long long kstar[MAXOUT] = {-1, -1, -1, -1};
+    for (int q = 0; q < ntypes && p->expBP > 0.0; q++) {
+      const RsStat& X = S.q[q];
+      if (!X.active) continue;
+      if (p->thresh > 1000.0) { kstar[q] = (long long)std::ceil(p->expBP) - 1; continue; }   // every pair a hit
+      EvalTables T = rs_evaltables(p, P - Nb, X, ctx->d_sf + X.sf_off, ctx->d_tail + X.tail_off);
+      if (!bpmask.empty()) { T.bpmask = ctx->d_bpmask; T.Nb = (double)Nb; }
+      if ((s = structured_kstar(ctx, ctx->d_cov + (int64_t)q * plane, T, p->expBP, &kstar[q]))) return s;
+    }
     CK(cudaMemsetAsync(ctx->d_nhits, 0, MAXOUT * sizeof(int), ctx->st));
     for (int q = 0; q < ntypes; q++) {
       const RsStat& X = S.q[q];
       if (!X.active) continue;
-      const EvalTables T = rs_evaltables(p, P, X, ctx->d_sf + X.sf_off, ctx->d_tail + X.tail_off);
+      EvalTables T = rs_evaltables(p, P - Nb, X, ctx->d_sf + X.sf_off, ctx->d_tail + X.tail_off);
+      if (!bpmask.empty()) { T.bpmask = ctx->d_bpmask; T.Nb = (double)Nb; }
+      if (p->expBP > 0.0) { T.Nx = p->expBP; T.kstar = kstar[q]; }
       const size_t ho = (size_t)q * hitcap;
       CK(launch_evalue(ctx->d_cov + (int64_t)q * plane, ctx->d_tiles, ctx->ntiles, L, T, nullptr, ctx->d_nhits + q,
                        hitcap, ctx->d_hi + ho, ctx->d_hj + ho, ctx->d_hsc + ho, ctx->d_hE + ho, ctx->d_hp + ho,
@@ -1347,6 +1456,8 @@ extern "C" int covgpu_rscape_learned(covgpu_ctx* ctx, const covgpu_params* p, co
   const int L = ctx->L;
   const int64_t P = (int64_t)L * (L - 1) / 2;
   if (!net) return fail(ctx, 11, "no network");
+  if ((p->ncnt > 0 && p->samplesize != 3) || p->expBP > 0.0)
+    return fail(ctx, 11, "the learned null computes one-set E-values (no two-set test, no --structured)");
   *used_net = 0;
   int s;
   if (wgt && (s = covgpu_set_weights(ctx, wgt))) return s;

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 #include "cov_kernels.h"
 #include "covgpu.h"
@@ -39,7 +40,16 @@ int rs_width(const covgpu_params* p, int N, int ns, const double* mm, int ntypes
 int rs_histogram(const covgpu_params* p, double fracfit, int ns, int64_t P, const uint64_t* ob, RsStat& X, char* err,
                  size_t errlen);
 // sf: the host copy of the survival table (read when X.have_sf); tq: nb
-// entries of the tail table
-void rs_tables(const covgpu_params* p, int64_t P, RsStat& X, const double* sf, covgpu_result& R, double* tq);
-covgpu::EvalTables rs_evaltables(const covgpu_params* p, int64_t P, const RsStat& X, const double* d_sf,
+// entries of the tail table; Nb of the P pairs are the structure's (the
+// two-set test), the other P - Nb the tests of the remaining pairs
+void rs_tables(const covgpu_params* p, int64_t P, int64_t Nb, RsStat& X, const double* sf, covgpu_result& R,
+               double* tq);
+covgpu::EvalTables rs_evaltables(const covgpu_params* p, int64_t Nt, const RsStat& X, const double* d_sf,
                                  const double* d_tail);
+// the two-set test's pairs from p's contacts over the L(L-1)/2 pairs in
+// scan order: bpmask, pairs whose first contact is a base pair for the
+// sample (the hit list's rule); *nsel, pairs with any such contact (the
+// ranking's classes, Nb).  Empty without contacts or with samplesize 3.
+// 0, or 11 (err set).
+int rs_pair_sets(const covgpu_params* p, int L, std::vector<uint32_t>& bpmask, int64_t* nsel, char* err,
+                 size_t errlen);

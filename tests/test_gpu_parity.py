@@ -321,3 +321,61 @@ def test_small_rna_workload(covgpu, oracle, counter, seed):
     for k in rh:
         assert abs(gh[k] - rh[k]) <= 1e-3 * rh[k]
     assert {k for k in gh if gh[k] < 0.05} == {k for k in rh if rh[k] < 0.05}
+
+
+@pytest.mark.parametrize("variant", ["two_set", "structured", "two_set_structured", "wc_two_set", "all_hits"])
+def test_rscape_two_set_and_structured(covgpu, oracle, variant):
+    """covgpu_rscape with a structure: the two-set test (R-scape -s: Nb tests
+    for the structure's base pairs, P - Nb for the others) and --structured
+    (expBP tests for the first hits) against the oracle: numbers of tests,
+    both thresholds, the hits and their E-values.  Contacts listed twice
+    with different types, and one with i > j, follow the reference's
+    matching rules."""
+    N, L, ns = 200, 120, 8
+    s, w = make(covgpu, N, L, 42, nbp=L // 5)
+    bps = [(i, int(s.ct[i])) for i in range(L) if s.ct[i] > i]
+    contacts = [(bps[0][0] + 1, bps[0][1] + 1, 5)] + [(i + 1, j + 1, oracle.WWc) for i, j in bps]
+    extra = (2, 9) if (1, 8) not in bps else (3, 11)
+    contacts += [(extra[0], extra[1], oracle.STACKED), (extra[0], extra[1], oracle.WWc), (40, 12, oracle.WWc)]
+    sample = {"two_set": 1, "structured": 3, "two_set_structured": 1, "wc_two_set": 2, "all_hits": 1}[variant]
+    expBP = 4.5 if "structured" in variant else (3.0 if variant == "all_hits" else -1.0)
+    thresh = 2000.0 if variant == "all_hits" else 0.05
+    e = covgpu.Engine(N, L, maxslots=ns + 1, maxnull=ns)
+    e.set_tree(s.parent, s.left, s.right)
+    kw = dict(nshuffle=ns, samplesize=sample, contacts=contacts, expBP=expBP, thresh=thresh)
+    g = e.rscape(s.ax, w, ["GTp"], counter=covgpu.TENSOR, hitcap=1 << 16, **kw)[0]
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    ref = oracle.rscape(s.ax, w, T, covtype="GTp", **kw)
+    assert g["Nt"] == ref["Nt"] and g["Nb"] == ref["Nb"]
+    if sample != 3:
+        assert g["Nb"] > 0
+    for k in ("sc_thresh", "sc_nbp"):
+        assert abs(g[k] - ref[k]) <= 1e-5 * abs(ref[k]) + 1e-9, (k, g[k], ref[k])
+    gh = {(i, j): E for (i, j, sc, E, p) in g["hits"]}
+    rh = {(i, j): E for (i, j, sc, E, p) in ref["hits"]}
+    assert g["nhit"] == ref["nhit"]
+    assert set(gh) == set(rh), sorted(set(gh) ^ set(rh))[:10]
+    for k, E in rh.items():
+        assert abs(gh[k] - E) <= 1e-4 * E + 1e-300, (k, gh[k], E)
+    e.close()
+
+
+def test_structure_only_in_the_single_alignment_path(covgpu):
+    """A structure belongs to one alignment: the family batch and the learned
+    null refuse the two-set test and --structured."""
+    N, L = 60, 50
+    s, w = make(covgpu, N, L, 3)
+    fam = dict(ax=s.ax, wgt=w, parent=s.parent, left=s.left, right=s.right)
+    b = covgpu.Batch(mem_gb=1.0)
+    with pytest.raises(RuntimeError):
+        b.rscape([fam], ["GTp"], samplesize=1, contacts=[(1, 10, 0)])
+    with pytest.raises(RuntimeError):
+        b.rscape([fam], ["GTp"], expBP=5.0)
+    b.close()
+    e = covgpu.Engine(N, L, maxslots=5, maxnull=4)
+    e.set_tree(s.parent, s.left, s.right)
+    net = covgpu.MLP(batch_cap=8)
+    with pytest.raises(RuntimeError):
+        e.rscape_learned(s.ax, w, net, 1.0, "GTp", nquick=4, expBP=5.0)
+    net.close()
+    e.close()
