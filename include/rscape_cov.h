@@ -243,6 +243,9 @@ extern int  corr_COVTYPEString(char **ret_covtype, COVTYPE type, char *errbuf);
  * device's current score matrix into mi->COV (both triangles, diagonal -inf); a no-op otherwise. */
 extern int  corr_SyncHost(struct mutual_s *mi, char *errbuf);
 extern int  corr_String2COVTYPE(char *covtype, COVTYPE *ret_type, char *errbuf);
+/* the Akmaev pair probabilities are not provided: returns eslFAIL (errbuf set) */
+extern int  corr_PostOrderPP(ESL_MSA *msa, ESL_TREE *T, void *ribosum, struct mutual_s *mi, double tol, int verbose,
+                             char *errbuf);
 
 /* ---------------- covariation.h (src/covariation.h:27-60) ---------------- */
 #define BMIN  -10.0
@@ -268,6 +271,23 @@ extern int       cov_NullFitExponential(ESL_HISTOGRAM *h, double **ret_survfit, 
 extern int       cov_histogram_SetSurvFitTail(ESL_HISTOGRAM *h, double **ret_survfit, double pmass,
                                               double (*surv)(double x, void *params), void *params);
 extern int       cov_ranklist_Bin2Bin(int b, ESL_HISTOGRAM *h, ESL_HISTOGRAM *new_, int *ret_newb);
+extern int       cov_THRESHTYPEString(char **ret_threshtype, THRESHTYPE type, char *errbuf);
+extern int       cov_Add2SubsHistogram(ESL_HISTOGRAM *hsubs, HITLIST *hitlist, int verbose);
+/* as the reference, both print to stdout whatever fp is */
+extern int       cov_DumpRankList(FILE *fp, RANKLIST *ranklist);
+extern int       cov_DumpHistogram(FILE *fp, ESL_HISTOGRAM *h);
+extern int       cov_SignificantPairs_ZScore(struct mutual_s *mi, int *msamap, int firstpos, int *ct, int verbose,
+                                             char *errbuf);
+extern int       cov_FisherExactTest(double *ret_pval, int cBP, int cNBP, int BP, int alen);
+extern int       cov_histogram_PlotSurvival(FILE *fp, ESL_HISTOGRAM *h, double *survfit);
+/* writes covhisfile's survival curves; the gnuplot figures are not drawn
+ * (gnuplot, covqqfile and title are not read) */
+extern int       cov_WriteHistogram(struct data_s *data, char *gnuplot, char *covhisfile, char *covqqfile,
+                                    SAMPLESIZE samplesize, RANKLIST *ranklist, char *title);
+/* CaCoFold's hit list is not provided: returns eslFAIL (errbuf set) */
+extern int       cov_CreateFOLDHitList(struct data_s *data, void *foldctlist, RANKLIST *ranklist, HITLIST *hitlist,
+                                       void *r3d, HITLIST **ret_foldhitlist, RMLIST **ret_foldrmlist, char *covtype,
+                                       char *threshtype);
 
 /* ---------------- histogram helpers (Easel esl_histogram restated) ---------------- */
 extern ESL_HISTOGRAM *covh_Create(double bmin, double bmax, double w);

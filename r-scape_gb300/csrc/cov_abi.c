@@ -559,6 +559,16 @@ corr_SyncHost(struct mutual_s *mi, char *errbuf)
   return eslOK;
 }
 
+/* corr_PostOrderPP (src/correlators.c, the Akmaev pair probabilities on a
+ * tree) is outside this library */
+int
+corr_PostOrderPP(ESL_MSA *msa, ESL_TREE *T, void *ribosum, struct mutual_s *mi, double tol, int verbose,
+                 char *errbuf)
+{
+  (void)msa; (void)T; (void)ribosum; (void)mi; (void)tol; (void)verbose;
+  XFAIL(eslFAIL, errbuf, "corr_PostOrderPP: the AKMAEV pair probabilities are not provided by this library");
+}
+
 /* corr_COVTYPEString / corr_String2COVTYPE, src/correlators.c:1562-1662 */
 static const char *COVNAMES[] = {"CHI", "CHIp", "CHIa", "GT", "GTp", "GTa", "MI", "MIp", "MIa", "MIr",
                                  "MIrp", "MIra", "MIg", "MIgp", "MIga", "OMES", "OMESp", "OMESa", "RAF", "RAFp",
@@ -904,4 +914,92 @@ cov_CreateHitList(struct data_s *data, struct mutual_s *mi, RANKLIST *ranklist, 
   for (k = 0; k < hl->nhit; k++) hl->srthit[k] = &hl->hit[k];
   *ret_hitlist = hl;
   return eslOK;
+}
+
+/* cov_THRESHTYPEString, src/covariation.c:309-323 */
+int
+cov_THRESHTYPEString(char **ret_threshtype, THRESHTYPE type, char *errbuf)
+{
+  if (type != Eval) XFAIL(eslFAIL, errbuf, "wrong THRESHTYPE");
+  *ret_threshtype = (char *)malloc(5);
+  if (!*ret_threshtype) XFAIL(eslEMEM, errbuf, "out of memory");
+  memcpy(*ret_threshtype, "Eval", 5);
+  return eslOK;
+}
+
+/* cov_SignificantPairs_ZScore, src/covariation.c:1531-1582: for every base
+ * pair (i, ct[i+1]-1) of a 1-based ct, the mean and deviation of the other
+ * scores of rows i and ct[i+1]-1 and the pair's z-score against the
+ * partner row, printed as the reference prints them (its min of the two
+ * z-scores takes the partner's twice) */
+int
+cov_SignificantPairs_ZScore(struct mutual_s *mi, int *msamap, int firstpos, int *ct, int verbose, char *errbuf)
+{
+  const int64_t L = mi->alen;
+  int64_t i, j, k;
+  (void)verbose;
+  if (corr_SyncHost(mi, errbuf)) return eslFAIL;
+  for (i = 0; i < L; i++) {
+    if (ct[i + 1] > 0 && ct[i + 1] > i + 1) {
+      const int64_t ip = ct[i + 1] - 1;
+      double avgi = 0.0, stdi = 0.0, avgj = 0.0, stdj = 0.0, zi, zj;
+      for (j = 0; j < L; j++) {
+        if (j != ip) {
+          if (j != i) { avgi += mi->COV->mx[i][j]; stdi += mi->COV->mx[i][j] * mi->COV->mx[i][j]; }
+        } else {
+          avgj = 0.0; stdj = 0.0;
+          for (k = 0; k < L; k++)
+            if (k != j && k != i) { avgj += mi->COV->mx[j][k]; stdj += mi->COV->mx[j][k] * mi->COV->mx[j][k]; }
+          avgj /= (L - 2);
+          stdj /= (L - 2);
+          stdj -= avgj * avgj;
+          stdj = sqrt(stdj);
+        }
+      }
+      avgi /= (L - 2);
+      stdi /= (L - 2);
+      stdi -= avgi * avgi;
+      stdi = sqrt(stdi);
+      zi = (mi->COV->mx[i][ip] - avgi) / stdi;
+      zj = (mi->COV->mx[i][ip] - avgj) / stdj;
+      (void)zi;
+      printf("[%d][%d] %f | %f | %f %f | %f %f\n", msamap[i] + firstpos, msamap[ip] + firstpos, zj, mi->COV->mx[i][ip],
+             avgi, stdi, avgj, stdj);
+    }
+  }
+  return eslOK;
+}
+
+/* cov_WriteHistogram, src/covariation.c:1869-1915: the survival curves of
+ * the alignment's base pairs, its other pairs and the null (with its fit)
+ * into covhisfile; the gnuplot figures are not drawn */
+int
+cov_WriteHistogram(struct data_s *data, char *gnuplot, char *covhisfile, char *covqqfile, SAMPLESIZE samplesize,
+                   RANKLIST *ranklist, char *title)
+{
+  FILE *fp;
+  int st = eslOK;
+  (void)gnuplot; (void)covqqfile; (void)samplesize; (void)title;
+  if (ranklist == NULL || covhisfile == NULL) return eslOK;
+  if ((fp = fopen(covhisfile, "w")) == NULL) XFAIL(eslFAIL, data->errbuf, "could not open covhisfile %s\n", covhisfile);
+  if (cov_histogram_PlotSurvival(fp, ranklist->hb, NULL) ||
+      cov_histogram_PlotSurvival(fp, ranklist->ht, NULL) ||
+      (data->ranklist_null &&
+       cov_histogram_PlotSurvival(fp, data->ranklist_null->ha, data->ranklist_null->survfit)))
+    st = eslFAIL;
+  fclose(fp);
+  if (st) XFAIL(eslFAIL, data->errbuf, "histogram survival plot write failed");
+  return eslOK;
+}
+
+/* cov_CreateFOLDHitList (src/covariation.c:1009, the hit list of a
+ * CaCoFold structure) is outside this library */
+int
+cov_CreateFOLDHitList(struct data_s *data, void *foldctlist, RANKLIST *ranklist, HITLIST *hitlist, void *r3d,
+                      HITLIST **ret_foldhitlist, RMLIST **ret_foldrmlist, char *covtype, char *threshtype)
+{
+  (void)foldctlist; (void)ranklist; (void)hitlist; (void)r3d; (void)covtype; (void)threshtype;
+  if (ret_foldhitlist) *ret_foldhitlist = NULL;
+  if (ret_foldrmlist) *ret_foldrmlist = NULL;
+  XFAIL(eslFAIL, data->errbuf, "cov_CreateFOLDHitList: CaCoFold's hit list is not provided by this library");
 }

@@ -580,3 +580,94 @@ cov_ReadNullHistogram(char *nullhisfile, RANKLIST **ret_ranklist, char *errbuf, 
   *ret_ranklist = r;
   return eslOK;
 }
+
+/* cov_Add2SubsHistogram, src/covariation.c:667-679: nsubs + 1 of every WWc
+ * hit */
+int
+cov_Add2SubsHistogram(ESL_HISTOGRAM *hsubs, HITLIST *hitlist, int verbose)
+{
+  int h;
+  (void)verbose;
+  for (h = 0; h < hitlist->nhit; h++)
+    if (hitlist->hit[h].bptype == WWc) covh_Add(hsubs, (double)(hitlist->hit[h].nsubs + 1));
+  return eslOK;
+}
+
+/* cov_DumpRankList, src/covariation.c:738-754 (stdout, as the reference) */
+int
+cov_DumpRankList(FILE *fp, RANKLIST *ranklist)
+{
+  int b;
+  (void)fp;
+  if (ranklist == NULL) return eslOK;
+  printf("imin %d imax %d covmin %f covmax %f\n", ranklist->ha->imin, ranklist->ha->imax, ranklist->ha->xmin,
+         ranklist->ha->xmax);
+  for (b = ranklist->ha->imax; b >= ranklist->ha->imin; b--) {
+    double cov = covh_Bin2LBound(ranklist->ha, b);
+    printf("cov %f eval %g\n", cov, covh_cov2evalue(cov, (double)ranklist->ha->Nc, ranklist->ha, NULL));
+  }
+  return eslOK;
+}
+
+/* cov_DumpHistogram, src/covariation.c:756-776 (stdout; the histograms here
+ * carry no expected counts) */
+int
+cov_DumpHistogram(FILE *fp, ESL_HISTOGRAM *h)
+{
+  double nobs = 0.0, cum = 0.0;
+  int b;
+  (void)fp;
+  for (b = h->imax; b >= h->imin; b--) nobs += (double)h->obs[b];
+  printf("imin %d imax %d covmin %f covmax %f nobs %f\n", h->imin, h->imax, h->xmin, h->xmax, nobs);
+  for (b = h->imax; b >= h->imin; b--) {
+    cum += (double)h->obs[b];
+    printf("b %d val %f obs %f cum_obs %f\n", b, covh_Bin2LBound(h, b), (double)h->obs[b], cum);
+  }
+  return eslOK;
+}
+
+/* cov_FisherExactTest, src/covariation.c:1584-1633: the one-sided sum of
+ * hypergeometric probabilities from cNBP covarying pairs outside BP base
+ * pairs up, log-factorials from lgamma (the reference uses Easel's) */
+int
+cov_FisherExactTest(double *ret_pval, int cBP, int cNBP, int BP, int alen)
+{
+  const int NBP = alen * (alen - 1) / 2, total = BP + NBP, cov = cBP + cNBP, non = total - cov;
+  const double fixed = lgamma(BP + 1.0) + lgamma(NBP + 1.0) + lgamma(cov + 1.0) + lgamma(non + 1.0) - lgamma(total + 1.0);
+  double pval = 0.0;
+  int cnbp;
+  for (cnbp = cNBP; cnbp <= NBP; cnbp++) {
+    const int cbp = cov - cnbp, ncbp = BP - cbp, ncnbp = non - ncbp;
+    if (cbp < 0) break;
+    pval += exp(fixed - lgamma(cbp + 1.0) - lgamma(ncbp + 1.0) - lgamma(cnbp + 1.0) - lgamma(ncnbp + 1.0));
+  }
+  if (pval > 1.0 && pval < 1.0 + 1e-3) pval = 1.0;
+  *ret_pval = pval;
+  return eslOK;
+}
+
+/* cov_histogram_PlotSurvival, src/covariation.c:1636-1676: the observed
+ * survival (largest value first, then every non-empty bin's lower bound
+ * with the fraction at or above it), "&", and the fitted survival when
+ * given, "&" */
+int
+cov_histogram_PlotSurvival(FILE *fp, ESL_HISTOGRAM *h, double *survfit)
+{
+  uint64_t c = 0;
+  int i;
+  if (h->imax >= 0 && h->obs[h->imax] > 1)
+    if (fprintf(fp, "%f\t%g\n", h->xmax, 1.0 / (double)h->Nc) < 0) return eslFAIL;
+  for (i = h->imax; i >= h->imin; i--)
+    if (h->obs[i] > 0) {
+      c += h->obs[i];
+      if (fprintf(fp, "%f\t%g\n", covh_Bin2LBound(h, i), (double)c / (double)h->Nc) < 0) return eslFAIL;
+    }
+  if (fprintf(fp, "&\n") < 0) return eslFAIL;
+  if (survfit) {
+    for (i = 2 * h->nb - 1; i >= 0; i--)
+      if (survfit[i] > 0.)
+        if (fprintf(fp, "%f\t%g\n", covh_Bin2LBound(h, i), survfit[i]) < 0) return eslFAIL;
+    if (fprintf(fp, "&\n") < 0) return eslFAIL;
+  }
+  return eslOK;
+}

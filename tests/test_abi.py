@@ -186,3 +186,76 @@ def test_histogram_bins_and_tail_survival(covgpu):
     for x in (2.5, 4.0, 9.0, 30.0):
         assert lib.covh_gamma_surv(x, gp) == pytest.approx(sp.gammaincc(tau, lam * (x - mu)), rel=1e-10)
         assert lib.covh_exp_surv(x, ep) == pytest.approx(np.exp(-lam * (x - mu)), rel=1e-12)
+
+
+def _abi(covgpu):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("rscape_abi", os.path.join(os.path.dirname(covgpu.LIBPATH),
+                                                                               "rscape_abi.py"))
+    abi = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(abi)
+    return abi, abi.setup_lib(covgpu.LIBPATH)
+
+
+def test_fisher_exact_test_is_the_hypergeometric_tail(covgpu):
+    """cov_FisherExactTest (src/covariation.c:1584-1633): the probability of
+    at least cNBP covarying pairs outside the BP base pairs, a hypergeometric
+    upper tail over alen(alen-1)/2 + BP pairs."""
+    from scipy.stats import hypergeom
+    lib = ctypes.CDLL(covgpu.LIBPATH)
+    lib.cov_FisherExactTest.argtypes = [ctypes.POINTER(ctypes.c_double)] + [ctypes.c_int] * 4
+    for cBP, cNBP, BP, alen in ((3, 2, 20, 40), (10, 0, 30, 80), (0, 5, 12, 30), (7, 7, 25, 60)):
+        p = ctypes.c_double()
+        assert lib.cov_FisherExactTest(ctypes.byref(p), cBP, cNBP, BP, alen) == 0
+        NBP = alen * (alen - 1) // 2
+        ref = hypergeom.sf(cNBP - 1, BP + NBP, NBP, cBP + cNBP)
+        assert p.value == pytest.approx(min(ref, 1.0), rel=1e-9, abs=1e-300)
+
+
+def test_small_reference_entry_points(covgpu, tmp_path, capfd):
+    """cov_THRESHTYPEString, cov_Add2SubsHistogram, cov_WriteHistogram's
+    survival file (cov_histogram_PlotSurvival), cov_DumpRankList, and the
+    refusals of corr_PostOrderPP and cov_CreateFOLDHitList."""
+    abi, lib = _abi(covgpu)
+    s = ctypes.c_char_p()
+    lib.cov_THRESHTYPEString.argtypes = [ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.c_char_p]
+    eb = ctypes.create_string_buffer(256)
+    assert lib.cov_THRESHTYPEString(ctypes.byref(s), 0, eb) == 0 and s.value == b"Eval"
+    assert lib.cov_THRESHTYPEString(ctypes.byref(s), 1, eb) != 0
+    # WWc hits add nsubs + 1 to the substitution histogram
+    hits = (abi.Hit * 4)()
+    for k, (bpt, ns) in enumerate(((abi.WWc, 3), (abi.STACKED, 9), (abi.WWc, 0), (abi.BPNONE, 5))):
+        hits[k].bptype, hits[k].nsubs = bpt, ns
+    hl = abi.HitList(4, None, hits, 0, 0)
+    rl = lib.cov_CreateRankList(20.0, 0.0, 1.0)
+    h = rl.contents.ha
+    lib.cov_Add2SubsHistogram.argtypes = [ctypes.POINTER(abi.Hist), ctypes.POINTER(abi.HitList), ctypes.c_int]
+    assert lib.cov_Add2SubsHistogram(h, ctypes.byref(hl), 0) == 0
+    hh = h.contents
+    assert hh.Nc == 2 and hh.xmin == 1.0 and hh.xmax == 4.0
+    # the survival file: ht's observed curve, hb's (empty), the null's
+    lib.covh_Add.argtypes = [ctypes.POINTER(abi.Hist), ctypes.c_double]
+    for x in (2.5, 3.5, 3.7, 8.0):
+        lib.covh_Add(rl.contents.ht, x)
+    data = abi.Data()
+    data.errbuf = ctypes.cast(eb, ctypes.c_char_p)
+    lib.cov_WriteHistogram.argtypes = [ctypes.POINTER(abi.Data), ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                       ctypes.c_int, ctypes.POINTER(abi.RankList), ctypes.c_char_p]
+    f = tmp_path / "surv.txt"
+    assert lib.cov_WriteHistogram(ctypes.byref(data), None, str(f).encode(), None, 3, rl, None) == 0
+    lines = f.read_text().splitlines()
+    assert lines[0] == "&"                                  # hb: empty
+    body = lines[1:lines.index("&", 1)]
+    # bins with data from the top: [8, 9) 1 of 4, [3, 4) 3 of 4, [2, 3) all
+    assert [float(l.split("\t")[1]) for l in body] == [0.25, 0.75, 1.0]
+    lib.cov_DumpRankList.argtypes = [ctypes.c_void_p, ctypes.POINTER(abi.RankList)]
+    capfd.readouterr()
+    assert lib.cov_DumpRankList(None, rl) == 0
+    ctypes.CDLL(None).fflush(None)   # C's stdout buffer
+    out = capfd.readouterr().out
+    assert out.startswith("imin ") and "eval" in out
+    lib.cov_FreeRankList(rl)
+    lib.corr_PostOrderPP.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_double, ctypes.c_int, ctypes.c_char_p]
+    assert lib.corr_PostOrderPP(None, None, None, None, 1e-6, 0, eb) != 0 and b"AKMAEV" in eb.value
+    lib.cov_CreateFOLDHitList.argtypes = [ctypes.POINTER(abi.Data)] + [ctypes.c_void_p] * 8
+    assert lib.cov_CreateFOLDHitList(ctypes.byref(data), None, None, None, None, None, None, None, None) != 0
