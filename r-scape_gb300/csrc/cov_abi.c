@@ -42,6 +42,8 @@ typedef struct {
   int         cov_on_dev;  /* device-resident mode: the device holds mi's current scores */
   double     *wgt;        /* weights of the uploaded alignment */
   void       *pinned[5];  /* host arrays page-locked for the copies (pp, nseff, ngap, COV, Eval) */
+  uint8_t    *axbuf;      /* the alignment's codes, contiguous, page-locked once (axpinned) */
+  int         axpinned;
 } gpu_state;
 
 /* host-array mode copies pp (L^2 16 doubles), nseff, ngap, COV and Eval
@@ -215,7 +217,14 @@ corr_Destroy(struct mutual_s *mi)
   gpu_state *g;
   if (!mi) return;
   g = (gpu_state *)mi->gpu;
-  if (g) { unpin_host(g); covgpu_destroy(g->ctx); free(g->wgt); free(g); }
+  if (g) {
+    unpin_host(g);
+    if (g->axpinned) covgpu_host_unpin(g->axbuf);
+    covgpu_destroy(g->ctx);
+    free(g->axbuf);
+    free(g->wgt);
+    free(g);
+  }
   if (mi->pp)    { if (mi->pp[0]) free(mi->pp[0][0]); free(mi->pp[0]); free(mi->pp); }
   if (mi->nseff) { free(mi->nseff[0]); free(mi->nseff); }
   if (mi->ngap)  { free(mi->ngap[0]); free(mi->ngap); }
@@ -240,16 +249,30 @@ upload_msa(struct mutual_s *mi, ESL_MSA *msa, char *errbuf)
     XFAIL(eslEINVAL, errbuf, "alignment %d x %lld does not match mutual_s %lld x %lld", msa->nseq,
           (long long)msa->alen, (long long)mi->nseq, (long long)mi->alen);
   if (!(g = gpu(mi, errbuf))) return eslFAIL;
-  ax = (uint8_t *)malloc((size_t)msa->nseq * L);
-  if (!ax) XFAIL(eslEMEM, errbuf, "out of memory");
+  /* one staging buffer per mutual_s, page-locked, for every alignment it
+   * scores (R-scape's nulls and the alignment itself) */
+  if (!g->axbuf) {
+    g->axbuf = (uint8_t *)malloc((size_t)msa->nseq * L);
+    if (!g->axbuf) XFAIL(eslEMEM, errbuf, "out of memory");
+    g->axpinned = covgpu_host_pin(g->axbuf, (size_t)msa->nseq * L) == 0;
+  }
+  ax = g->axbuf;
   for (s = 0; s < msa->nseq; s++) memcpy(ax + s * L, msa->ax[s] + 1, (size_t)L);
   st = covgpu_set_alignment(g->ctx, 0, ax);
-  free(ax);
   if (st) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
-  free(g->wgt);
-  g->wgt = (double *)malloc(sizeof(double) * msa->nseq);
-  for (s = 0; s < msa->nseq; s++) g->wgt[s] = msa->wgt ? msa->wgt[s] : 1.0;
-  if ((st = covgpu_set_weights(g->ctx, g->wgt))) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+  /* the weights again only when they changed (R-scape's nulls carry the
+   * alignment's) */
+  {
+    int same = g->wgt != NULL;
+    for (s = 0; same && s < msa->nseq; s++) same = g->wgt[s] == (msa->wgt ? msa->wgt[s] : 1.0);
+    if (!same) {
+      free(g->wgt);
+      g->wgt = (double *)malloc(sizeof(double) * msa->nseq);
+      if (!g->wgt) XFAIL(eslEMEM, errbuf, "out of memory");
+      for (s = 0; s < msa->nseq; s++) g->wgt[s] = msa->wgt ? msa->wgt[s] : 1.0;
+      if ((st = covgpu_set_weights(g->ctx, g->wgt))) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+    }
+  }
   g->have_msa = 1;
   g->have_counts = 0;
   return eslOK;

@@ -857,11 +857,14 @@ k_validate_pp(const float* __restrict__ cnt, const TileRC* __restrict__ tiles, i
       c[q] = 1e-10 + ((double)C[(2 * q) * TPP + p] + (double)C[(2 * q + 1) * TPP + p]);
       Z += c[q];
     }
+    // one reciprocal per pair (FP64 division is slow on this part): each
+    // value within an ulp of c/Z, far inside the checks' tolerance
     double sum = 0.0;
     bool ok = (Z > 0.0);
+    const double iZ = 1.0 / Z;
 #pragma unroll
     for (int q = 0; q < 16; q++) {
-      const double v = c[q] / Z;
+      const double v = c[q] * iZ;
       ok = ok && (v >= 0.0) && (v <= 1.0 + tol);
       sum += v;
     }
