@@ -111,8 +111,9 @@ def test_dropin_probs_and_statistic(covgpu, oracle, abi, device_resident):
     lib.corr_Destroy(mi)
 
 
+@pytest.mark.parametrize("device_resident", [0, 1])
 @pytest.mark.parametrize("variant", ["two_set", "structured", "two_set_structured", "pdb_two_set", "wc_two_set"])
-def test_dropin_two_set_and_structured(covgpu, oracle, abi, variant):
+def test_dropin_two_set_and_structured(covgpu, oracle, abi, variant, device_resident):
     """R-scape -s (the two-set test: the structure's base pairs against the
     other pairs), --structured (expBP) and a PDB map with its distance rule
     through the drop-in flow: the same hits, E-values, numbers of tests,
@@ -137,6 +138,7 @@ def test_dropin_two_set_and_structured(covgpu, oracle, abi, variant):
     m2p = np.arange(L, dtype=np.int32) if mind else None
     abc = abi.Alphabet(1, 4, 18)
     mi = lib.corr_Create(L, N, 0, 8, 50, C.byref(abc), 3)
+    mi.contents.device_resident = device_resident
     errbuf = C.create_string_buffer(256)
     th = abi.Thresh(0, 0.05, 0.0, 0.0)
     rnd = abi.Rand(42)
@@ -169,11 +171,12 @@ def test_dropin_two_set_and_structured(covgpu, oracle, abi, variant):
         assert h.bptype == first.get(k, abi.BPNONE)
     assert abs(th.sc_bp - ref["sc_thresh"]) <= 1e-5 * abs(ref["sc_thresh"]) + 1e-9
     assert abs(th.sc_nbp - ref["sc_nbp"]) <= 1e-5 * abs(ref["sc_nbp"]) + 1e-9
-    # mi->Eval: every pair's E-value with its own number of tests
-    Ev = np.ctypeslib.as_array(mi.contents.Eval.contents.mx[0], shape=(L * L,)).reshape(L, L)
-    iu = np.triu_indices(L, 1)
-    fin = np.isfinite(ref["Eval"][iu]) & (ref["Eval"][iu] > 0)
-    assert np.allclose(Ev[iu][fin], ref["Eval"][iu][fin], rtol=1e-5, atol=0)
+    # mi->Eval (host-array mode): every pair's E-value with its own number of tests
+    if not device_resident:
+        Ev = np.ctypeslib.as_array(mi.contents.Eval.contents.mx[0], shape=(L * L,)).reshape(L, L)
+        iu = np.triu_indices(L, 1)
+        fin = np.isfinite(ref["Eval"][iu]) & (ref["Eval"][iu] > 0)
+        assert np.allclose(Ev[iu][fin], ref["Eval"][iu][fin], rtol=1e-5, atol=0)
     lib.cov_FreeHitList(hl)
     lib.cov_FreeRankList(rl)
     lib.cov_FreeRankList(cum)
