@@ -270,7 +270,12 @@ upload_msa(struct mutual_s *mi, ESL_MSA *msa, char *errbuf)
       g->wgt = (double *)malloc(sizeof(double) * msa->nseq);
       if (!g->wgt) XFAIL(eslEMEM, errbuf, "out of memory");
       for (s = 0; s < msa->nseq; s++) g->wgt[s] = msa->wgt ? msa->wgt[s] : 1.0;
-      if ((st = covgpu_set_weights(g->ctx, g->wgt))) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+      if ((st = covgpu_set_weights(g->ctx, g->wgt))) {
+        /* forget them, so the next alignment uploads its weights again */
+        free(g->wgt);
+        g->wgt = NULL;
+        XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
+      }
     }
   }
   g->have_msa = 1;
