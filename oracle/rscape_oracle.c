@@ -1196,6 +1196,41 @@ cov2evalue(double cov, double Nc, const orc_hist_t *h, const double *sf)
   return INFINITY;
 }
 
+/* the empirical branch's counts of cov2evalue for every bin at once:
+ * suf[k] = sum of obs[imin + k .. imax] (exact integer sums, so
+ * cov2evalue_suf returns exactly what cov2evalue's loop gives, in O(1) per
+ * pair instead of O(bins)); NULL when imax < imin or out of memory */
+static uint64_t *
+cov2evalue_suffix(const orc_hist_t *h)
+{
+  uint64_t *suf;
+  int i;
+  if (h->imax < h->imin) return NULL;
+  suf = malloc(sizeof(uint64_t) * (size_t)(h->imax - h->imin + 1));
+  if (!suf) return NULL;
+  suf[h->imax - h->imin] = h->obs[h->imax];
+  for (i = h->imax - 1; i >= h->imin; i--) suf[i - h->imin] = suf[i - h->imin + 1] + h->obs[i];
+  return suf;
+}
+
+/* cov2evalue with the suffix table (falls back to the loop without one) */
+static double
+cov2evalue_suf(double cov, double Nc, const orc_hist_t *h, const double *sf, const uint64_t *suf)
+{
+  int icov;
+  if (!suf) return cov2evalue(cov, Nc, h, sf);
+  icov = orc_hist_score2bin(h, cov);
+  if      (sf && icov >= 2 * h->nb - 1) return sf[2 * h->nb - 1] * Nc;
+  else if (sf && cov >= h->phi)         return sf[icov + 1] * Nc;
+  if (cov >= h->xmax) return Nc / (double)h->Nc;
+  if (icov <= h->imax) {
+    if (icov < h->imin) icov = h->imin;
+    if (icov >= h->imax - 1) return Nc / (double)h->Nc;
+    return (double)suf[icov - h->imin] * Nc / (double)h->Nc;
+  }
+  return INFINITY;
+}
+
 /* evalue2cov, src/covariation.c:2403-2435 */
 static double
 evalue2cov(double thr, double Nc, const orc_hist_t *h, const double *sf)
@@ -1446,6 +1481,7 @@ orc_rscape_multi(const orc_params_t *p, int nt, const int *covtypes, const uint8
     if (Eval_out) for (i = 0; i < (int)LL; i++) Eval_out[t * LL + i] = INFINITY;
     if (N > 1 && w[t] >= 1e-20 && cm) {
       orc_hist_t *hb = NULL, *ht = NULL;
+      uint64_t   *suf = NULL;
       double Nt, Nb;
       int64_t nh = 0;   /* hits so far (h of src/covariation.c:852) */
       h = rank_scores(p, L, C, mm[t][1], p->bmin, w[t], p->tol, &hb, &ht);
@@ -1471,10 +1507,11 @@ orc_rscape_multi(const orc_params_t *p, int nt, const int *covtypes, const uint8
       /* cov_CreateHitList (src/covariation.c:828-870): base pairs take Nb
        * tests, the others expBP while fewer than expBP hits were listed,
        * then Nt */
+      suf = cov2evalue_suffix(cm);
       for (i = 0; i < L - 1; i++)
         for (j = i + 1; j < L; j++) {
           double cov  = C[(int64_t)i * L + j];
-          double pv   = cov2evalue(cov, 1.0, cm, sf);
+          double pv   = cov2evalue_suf(cov, 1.0, cm, sf, suf);
           int    isbp = cnt_isbp(p, cnt_type(p, i + 1, j + 1));
           double ev   = isbp ? pv * Nb : ((double)nh < p->expBP ? pv * p->expBP : pv * Nt);
           if (Eval_out) Eval_out[t * LL + (int64_t)i * L + j] = Eval_out[t * LL + (int64_t)j * L + i] = ev;
@@ -1487,6 +1524,7 @@ orc_rscape_multi(const orc_params_t *p, int nt, const int *covtypes, const uint8
             nh++;
           }
         }
+      free(suf);
       orc_hist_free(hb);
       orc_hist_free(ht);
     }

@@ -154,6 +154,43 @@ def test_rscape_pipeline_small(oracle, covgpu):
     assert planted >= max(1, len(r["hits"]) // 2)
 
 
+def test_empirical_pvalues_follow_the_bin_walk(oracle, covgpu):
+    """Below the fitted tail a pair's p-value is the null mass in the score's
+    bin and above (cov2evalue, src/covariation.c:2369-2400: the loop over the
+    bins imax .. icov).  The oracle takes that mass from a table of suffix
+    sums; here every pair of a small alignment (thresh > 1000 lists them all)
+    is checked against the loop itself, bit for bit."""
+    import math
+    s = covgpu.Synth(150, 100, 1.5, 25, 3, 8, 9, 0.08, seed=11, tree_kind=1)
+    w = oracle.weights_pb(s.ax)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    r = oracle.rscape(s.ax, w, T, covtype="GTp", nshuffle=8, thresh=2000.0)
+    obs = [int(x) for x in r["null_obs"]]
+    Nc = float(r["h_Nc"])
+    have_sf = r["fit_ok"] == 1 and math.isfinite(r["lambda_"])
+    assert len(r["hits"]) == 100 * 99 // 2
+    walked = 0
+    for (i, j, sc, E, p) in r["hits"]:
+        if have_sf and sc >= r["h_phi"]:
+            continue
+        if sc >= r["h_xmax"]:
+            want = 1.0 / Nc
+        else:
+            icov = int(math.ceil((sc - r["h_bmin"]) / r["h_w"] - 1.0))
+            assert icov <= r["h_imax"]
+            icov = max(icov, r["h_imin"])
+            if icov >= r["h_imax"] - 1:
+                want = 1.0 / Nc
+            else:
+                c = 0
+                for b in range(r["h_imax"], icov - 1, -1):
+                    c += obs[b]
+                want = float(c) * 1.0 / Nc
+                walked += 1
+        assert p == want, (i, j, sc, p, want)
+    assert walked > 1000
+
+
 def test_c16_statistics_match_definitions(oracle):
     """CHI, OMES, GT, MI, MIr and MIg of the C16 class from the oracle's own
     pair probabilities, marginals and nseff, written out cell by cell
