@@ -320,8 +320,9 @@ def dropin_flow(cg, e, ax, w, ns):
     calculate_width_histo on the first null, cov_Calculate in RANSS mode on
     each of the ns nulls merged into the cumulative null histogram, then
     cov_Calculate in GIVSS mode on the alignment (src/R-scape.c:1281-1371,
-    1614-1724, 2502).  Timed once in the reference's host-array mode (pp,
-    nseff, ngap, COV and Eval filled on the host by every call) and once in
+    1614-1724, 2502).  Timed once in the reference's host-array mode (COV
+    filled on the host by every call, pp, nseff, ngap and Eval for the given
+    alignment; a null's pp stays on the device) and once in
     device-resident mode; host wall clock, host alignments in, hit list out.
     The null alignments come from the engine before the timed region."""
     import ctypes as C

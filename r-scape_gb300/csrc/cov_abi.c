@@ -13,7 +13,13 @@
  * With mi->device_resident set, pp/nseff/ngap and the score matrix stay on
  * the device instead: no L x L array crosses the bus between
  * corr_Calculate* and cov_CreateHitList, and corr_SyncHost copies COV back on
- * request.
+ * request.  For a shuffled alignment (mi->ishuffled, which R-scape sets
+ * through corr_Create / corr_Reuse for its null alignments,
+ * src/R-scape.c:2432,2574) pp/nseff/ngap stay on the device in both modes:
+ * R-scape reads them only for the given alignment (power_SPAIR_AddMI in
+ * GIVSS mode, src/covariation.c:260-263; CaCoFold outside RANSS mode,
+ * src/R-scape.c:2682), so the host arrays are neither cleared nor filled
+ * for a null and keep what the last given alignment left there.
  *
  * Scope: the one-set test (SAMPLE_ALL; every pair tested alike) and the
  * two-set test (R-scape -s: the given structure's contacts against the other
@@ -67,6 +73,15 @@ unpin_host(gpu_state *g)
 {
   int k;
   for (k = 0; k < 5; k++) { covgpu_host_unpin(g->pinned[k]); g->pinned[k] = NULL; }
+}
+
+/* whether pp, nseff and ngap of the current alignment go to the host
+ * arrays: not in device-resident mode, and not for a shuffled (null)
+ * alignment, whose pair probabilities R-scape never reads */
+static int
+probs_on_host(const struct mutual_s *mi)
+{
+  return !mi->device_resident && !mi->ishuffled;
 }
 
 /* the score matrix to hand to the engine: NULL = the device's own copy */
@@ -201,7 +216,7 @@ corr_Reuse(struct mutual_s *mi, int ishuffled, COVTYPE mitype, COVCLASS miclass)
 {
   const size_t L = (size_t)mi->alen;
   mi->ishuffled = ishuffled;
-  if (!mi->device_resident) {   /* device-resident: pp, nseff, ngap live on the device */
+  if (probs_on_host(mi)) {   /* else pp, nseff, ngap live on the device */
     zero_doubles(mi->pp[0][0], L * L * 16);
     zero_doubles(mi->nseff[0], L * L);
     zero_doubles(mi->ngap[0], L * L);
@@ -329,7 +344,7 @@ corr_NaivePP(ESL_RANDOMNESS *r, ESL_MSA *msa, struct mutual_s *mi, double tol, i
   if ((st = upload_msa(mi, msa, errbuf))) return st;
   if ((st = count_on_device(mi, errbuf))) return st;
   g = (gpu_state *)mi->gpu;
-  if (mi->device_resident) return eslOK;   /* pp, nseff, ngap stay on the device */
+  if (!probs_on_host(mi)) return eslOK;   /* pp, nseff, ngap stay on the device */
   if (covgpu_get_probs(g->ctx, 0, g->wgt, mi->pp[0][0], mi->nseff[0], mi->ngap[0], NULL, NULL))
     XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
   return eslOK;
@@ -380,14 +395,15 @@ validate_vec(const double *v, int n, double tol)
 }
 
 /* corr_ValidateProbs, src/correlators.c:1499-1545; the pair probabilities
- * are checked on the device in device-resident mode */
+ * are checked on the device when they stay there (device-resident mode, or
+ * a shuffled alignment) */
 int
 corr_ValidateProbs(struct mutual_s *mi, double tol, int verbose, char *errbuf)
 {
   int64_t i, j;
   gpu_state *g = (gpu_state *)mi->gpu;
   (void)verbose;
-  if (mi->device_resident && g && g->have_counts) {
+  if (!probs_on_host(mi) && g && g->have_counts) {
     if (covgpu_validate_probs(g->ctx, tol)) XFAIL(eslFAIL, errbuf, "pp validation failed");
   } else {
     int bad = 0;
@@ -682,6 +698,8 @@ rank_into(struct mutual_s *mi, ESL_HISTOGRAM *h, char *errbuf)
     xmin = (mi->minCOV > lo) ? mi->minCOV : lo;
     xmax = (mi->maxCOV > lo) ? mi->maxCOV : lo;
   } else {
+    /* over the host threads (a minimum and a maximum do not depend on the order) */
+#pragma omp parallel for schedule(dynamic, 16) reduction(min : xmin) reduction(max : xmax) private(j)
     for (i = 0; i < L - 1; i++)
       for (j = i + 1; j < L; j++) {
         double v = mi->COV->mx[i][j];

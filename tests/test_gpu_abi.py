@@ -60,6 +60,16 @@ def test_dropin_rscape_flow(covgpu, oracle, abi, covtype, device_resident):
         # mi->Eval holds every pair's E-value
         Ev = np.ctypeslib.as_array(mi.contents.Eval.contents.mx[0], shape=(L * L,)).reshape(L, L)
         assert np.all(Ev[np.triu_indices(L, 1)] > 0)
+        if covtype != "RAFp":
+            # pp and nseff on the host are the given alignment's (the nulls',
+            # shuffled, stayed on the device)
+            opp, one, ong, opm, ops = oracle.probs(s.ax, w)
+            iu = np.triu_indices(L, 1)
+            ne = np.ctypeslib.as_array(mi.contents.nseff[0], shape=(L * L,)).reshape(L, L)
+            ppp = C.cast(mi.contents.pp, C.POINTER(C.POINTER(C.POINTER(C.c_double))))
+            pp = np.ctypeslib.as_array(ppp[0][0], shape=(L * L * 16,)).reshape(L, L, 16)
+            assert np.allclose(ne[iu], one[iu], rtol=1e-9)
+            assert np.allclose(pp[iu], opp[iu], rtol=1e-6, atol=1e-15)
     # mi->COV: the corrected scores
     cov = np.ctypeslib.as_array(mi.contents.COV.contents.mx[0], shape=(L * L,)).reshape(L, L)
     iu = np.triu_indices(L, 1)
