@@ -136,7 +136,11 @@ struct mutual_s {
                                     * cov_CreateHitList (the hit list and minCOV/maxCOV come back);
                                     * corr_SyncHost copies COV to the host.  A caller sets it after
                                     * corr_Create when nothing reads those arrays (no power
-                                    * analysis, no CaCoFold), and must not write mi->COV meanwhile. */
+                                    * analysis, no CaCoFold), and must not write mi->COV meanwhile.
+                                    * With 0, a shuffled alignment (ishuffled, R-scape's nulls) is
+                                    * treated as with 1: R-scape reads only its ranklist and
+                                    * minCOV/maxCOV, and the host arrays keep the last given
+                                    * alignment's values. */
 };
 
 typedef struct ranklist_s {
@@ -239,8 +243,9 @@ extern int  corr_Probs(ESL_RANDOMNESS *r, ESL_MSA *msa, ESL_TREE *T, void *ribos
                        METHOD method, double tol, int verbose, char *errbuf);
 extern int  corr_ValidateProbs(struct mutual_s *mi, double tol, int verbose, char *errbuf);
 extern int  corr_COVTYPEString(char **ret_covtype, COVTYPE type, char *errbuf);
-/* No counterpart in the reference: in device-resident mode (mi->device_resident = 1), copies the
- * device's current score matrix into mi->COV (both triangles, diagonal -inf); a no-op otherwise. */
+/* No counterpart in the reference: when the device alone holds the current score matrix
+ * (device-resident mode, or a shuffled alignment's scores), copies it into mi->COV (both
+ * triangles, diagonal -inf); a no-op otherwise. */
 extern int  corr_SyncHost(struct mutual_s *mi, char *errbuf);
 extern int  corr_String2COVTYPE(char *covtype, COVTYPE *ret_type, char *errbuf);
 /* the Akmaev pair probabilities are not provided: returns eslFAIL (errbuf set) */

@@ -15,11 +15,13 @@
  * corr_Calculate* and cov_CreateHitList, and corr_SyncHost copies COV back on
  * request.  For a shuffled alignment (mi->ishuffled, which R-scape sets
  * through corr_Create / corr_Reuse for its null alignments,
- * src/R-scape.c:2432,2574) pp/nseff/ngap stay on the device in both modes:
- * R-scape reads them only for the given alignment (power_SPAIR_AddMI in
- * GIVSS mode, src/covariation.c:260-263; CaCoFold outside RANSS mode,
- * src/R-scape.c:2682), so the host arrays are neither cleared nor filled
- * for a null and keep what the last given alignment left there.
+ * src/R-scape.c:2432,2574) pp/nseff/ngap and the score matrix stay on the
+ * device in both modes: R-scape reads those arrays only for the given
+ * alignment (power_SPAIR_AddMI in GIVSS mode, src/covariation.c:260-263;
+ * CaCoFold outside RANSS mode, src/R-scape.c:2682) and takes from a null
+ * its ranklist and minCOV/maxCOV (src/R-scape.c:1353-1360,1685-1690), so
+ * the host arrays are neither cleared nor filled for a null and keep what
+ * the last given alignment left there.
  *
  * Scope: the one-set test (SAMPLE_ALL; every pair tested alike) and the
  * two-set test (R-scape -s: the given structure's contacts against the other
@@ -45,7 +47,8 @@ typedef struct {
   covgpu_ctx *ctx;
   int         have_msa;
   int         have_counts;
-  int         cov_on_dev;  /* device-resident mode: the device holds mi's current scores */
+  int         cov_on_dev;  /* the device alone holds mi's current scores (device-resident mode, or a
+                            * shuffled alignment) */
   double     *wgt;        /* weights of the uploaded alignment */
   void       *pinned[5];  /* host arrays page-locked for the copies (pp, nseff, ngap, COV, Eval) */
   uint8_t    *axbuf;      /* the alignment's codes, contiguous, page-locked once (axpinned) */
@@ -75,9 +78,10 @@ unpin_host(gpu_state *g)
   for (k = 0; k < 5; k++) { covgpu_host_unpin(g->pinned[k]); g->pinned[k] = NULL; }
 }
 
-/* whether pp, nseff and ngap of the current alignment go to the host
- * arrays: not in device-resident mode, and not for a shuffled (null)
- * alignment, whose pair probabilities R-scape never reads */
+/* whether pp, nseff, ngap and the scores of the current alignment go to the
+ * host arrays: not in device-resident mode, and not for a shuffled (null)
+ * alignment, whose pair probabilities and score matrix R-scape never reads
+ * (it takes the null's ranklist and minCOV / maxCOV) */
 static int
 probs_on_host(const struct mutual_s *mi)
 {
@@ -89,7 +93,7 @@ static const double *
 cov_src(struct mutual_s *mi)
 {
   gpu_state *g = (gpu_state *)mi->gpu;
-  return (mi->device_resident && g && g->cov_on_dev) ? NULL : mi->COV->mx[0];
+  return (g && g->cov_on_dev) ? NULL : mi->COV->mx[0];
 }
 
 static gpu_state *
@@ -122,7 +126,9 @@ dmx_create(int n, int m)
   if (!D) return NULL;
   D->n = n; D->m = m;
   D->mx = (double **)malloc(sizeof(double *) * (n > 0 ? n : 1));
+  if (!D->mx) { free(D); return NULL; }
   D->mx[0] = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1) * (m > 0 ? m : 1));
+  if (!D->mx[0]) { free(D->mx); free(D); return NULL; }
   for (i = 1; i < n; i++) D->mx[i] = D->mx[0] + (size_t)i * m;
   return D;
 }
@@ -193,6 +199,10 @@ corr_Create(int64_t alen, int64_t nseq, int ishuffled, int nseqthresh, int alent
   }
   mi->COV  = dmx_create((int)L, (int)L);
   mi->Eval = dmx_create((int)L, (int)L);
+  if (!mi->COV || !mi->Eval) { corr_Destroy(mi); return NULL; }
+  /* the reference's initial values, whatever the object is made for */
+  dmx_set(mi->COV, -INFINITY);
+  dmx_set(mi->Eval, INFINITY);
   corr_ReuseCOV(mi, COVNONE, covclass);
   return mi;
 }
@@ -202,9 +212,10 @@ corr_ReuseCOV(struct mutual_s *mi, COVTYPE mitype, COVCLASS miclass)
 {
   mi->type = mitype;
   mi->class_ = miclass;
-  /* device-resident: the host matrices are written only by corr_SyncHost */
-  if (mi->COV && !mi->device_resident)  dmx_set(mi->COV, -INFINITY);
-  if (mi->Eval && !mi->device_resident) dmx_set(mi->Eval, INFINITY);
+  /* device-resident mode or a shuffled alignment: the host matrices are
+   * written only by corr_SyncHost */
+  if (mi->COV && probs_on_host(mi))  dmx_set(mi->COV, -INFINITY);
+  if (mi->Eval && probs_on_host(mi)) dmx_set(mi->Eval, INFINITY);
   mi->besthreshCOV = -INFINITY;
   mi->minCOV = INFINITY;
   mi->maxCOV = -INFINITY;
@@ -447,8 +458,8 @@ score_into_cov(struct mutual_s *mi, int covtype, int cls, const ESL_DMATRIX *all
   allow16(allowpair, a);
   st = score_dev(g, mi, covtype, cls, a, mm);
   if (st) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
-  g->cov_on_dev = mi->device_resident;
-  if (!mi->device_resident && covgpu_get_cov(g->ctx, 0, 0, mi->COV->mx[0]))
+  g->cov_on_dev = !probs_on_host(mi);
+  if (probs_on_host(mi) && covgpu_get_cov(g->ctx, 0, 0, mi->COV->mx[0]))
     XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
   g->have_counts = 1;
   mi->type = (COVTYPE)covtype;
@@ -593,12 +604,13 @@ corr_CalculateCOVCorrected(ACTYPE actype, struct data_s *data, int shiftnonneg)
   return eslOK;
 }
 
-/* device-resident mode: the device's score matrix into mi->COV */
+/* the device's score matrix into mi->COV, when the device alone holds it
+ * (device-resident mode, or a shuffled alignment's scores) */
 int
 corr_SyncHost(struct mutual_s *mi, char *errbuf)
 {
   gpu_state *g = (gpu_state *)mi->gpu;
-  if (!mi->device_resident || !g || !g->cov_on_dev) return eslOK;
+  if (!g || !g->cov_on_dev) return eslOK;
   if (covgpu_get_cov(g->ctx, 0, 0, mi->COV->mx[0])) XFAIL(eslFAIL, errbuf, "%s", covgpu_errmsg(g->ctx));
   return eslOK;
 }
@@ -783,7 +795,7 @@ rank_host(struct data_s *data, RANKLIST *rl, int classes)
   const int mind = data->clist ? data->clist->mind : 0;
   uint32_t *sel = NULL;
   int64_t i, j, n = 0;
-  if (mi->device_resident && corr_SyncHost(mi, data->errbuf)) return eslFAIL;
+  if (corr_SyncHost(mi, data->errbuf)) return eslFAIL;
   if (classes && contact_maps(data->clist, data->samplesize, L, &sel, NULL)) XFAIL(eslEMEM, data->errbuf, "out of memory");
   for (i = 0; i < L - 1; i++)
     for (j = i + 1; j < L; j++, n++) {
