@@ -6,7 +6,7 @@
  * alignments.  All arguments are plain pointers and sizes; host buffers are
  * ordinary (or pinned) host memory.  Every call returns 0 on success or a
  * nonzero status with a message in the context's error buffer
- * (covgpu_errmsg).
+ * (covgpu_errmsg); a NULL context (or batch, or network) returns 11.
  *
  * This is the fast path behind the reference-named entry points of
  * rscape_cov.h: one call of covgpu_rscape() does what R-scape's

@@ -255,6 +255,7 @@ static int build_tiles(covgpu_ctx* ctx) {
 }
 
 extern "C" int covgpu_resize(covgpu_ctx* ctx, int N, int L) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   ctx->cnt_valid = false;
   if (N < 1 || L < 1 || N > ctx->capN || L > ctx->capL)
@@ -282,6 +283,7 @@ extern "C" int covgpu_resize(covgpu_ctx* ctx, int N, int L) {
 }
 
 extern "C" int covgpu_set_weights(covgpu_ctx* ctx, const double* wgt) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const int N = ctx->N;
   ctx->cnt_valid = false;
@@ -307,6 +309,7 @@ extern "C" int covgpu_set_weights(covgpu_ctx* ctx, const double* wgt) {
 }
 
 extern "C" int covgpu_set_alignment(covgpu_ctx* ctx, int slot, const uint8_t* ax) {
+  if (!ctx) return 11;
   if (slot < 0 || slot >= ctx->maxslots) return fail(ctx, 11, "slot %d out of range", slot);
   CK(cudaSetDevice(ctx->dev));
   ctx->cnt_valid = false;
@@ -326,6 +329,7 @@ extern "C" int covgpu_set_alignment(covgpu_ctx* ctx, int slot, const uint8_t* ax
 }
 
 extern "C" int covgpu_get_alignment(covgpu_ctx* ctx, int slot, uint8_t* ax) {
+  if (!ctx) return 11;
   if (slot < 0 || slot >= ctx->maxslots) return fail(ctx, 11, "slot %d out of range", slot);
   CK(cudaSetDevice(ctx->dev));
   const uint8_t* src = ctx->d_ax + (size_t)slot * ctx->N * ctx->Lp;
@@ -335,6 +339,7 @@ extern "C" int covgpu_get_alignment(covgpu_ctx* ctx, int slot, uint8_t* ax) {
 }
 
 extern "C" int covgpu_set_tree(covgpu_ctx* ctx, const int* parent, const int* left, const int* right) {
+  if (!ctx) return 11;
   const int N = ctx->N;
   CK(cudaSetDevice(ctx->dev));
   if (N < 2) { ctx->have_tree = false; return 0; }
@@ -393,6 +398,7 @@ static int make_nulls_async(covgpu_ctx* ctx, uint64_t seed, int first_null, int 
 static int check_status(covgpu_ctx* ctx);
 
 extern "C" int covgpu_weights_pb_dev(covgpu_ctx* ctx, int slot, int set, double* wgt) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   ctx->cnt_valid = false;
   const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
@@ -413,6 +419,7 @@ extern "C" int covgpu_weights_pb_dev(covgpu_ctx* ctx, int slot, int set, double*
 }
 
 extern "C" int covgpu_weights_gsc_dev(covgpu_ctx* ctx, int slot, int set, double* wgt) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   ctx->cnt_valid = false;
   const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
@@ -448,6 +455,7 @@ constexpr uint32_t kReconStream = 0xFFFFFFFFu;
 
 extern "C" int covgpu_substitutions(covgpu_ctx* ctx, int slot, uint64_t seed, int includegaps, int* nsubs,
                                     int* ndouble, int* njoin) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
   if (!ctx->have_tree) return fail(ctx, 11, "no tree set");
@@ -491,6 +499,7 @@ extern "C" int covgpu_substitutions(covgpu_ctx* ctx, int slot, uint64_t seed, in
 extern "C" int covgpu_power(covgpu_ctx* ctx, int ns, const double* subs, const double* prob, const double* subs_join,
                             const double* prob_join, const double* subs_double, const double* prob_double,
                             double* power, double* power_join, double* power_double) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const int L = ctx->L;
   if (!ctx->d_nsubs) return fail(ctx, 11, "no substitutions yet");
@@ -519,6 +528,7 @@ extern "C" int covgpu_power(covgpu_ctx* ctx, int ns, const double* subs, const d
 }
 
 extern "C" int covgpu_gapfilter_dev(covgpu_ctx* ctx, int slot, const double* wgt, double gapthresh, int* useme) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
   if (slot < 0 || slot >= ctx->maxslots || !useme) return fail(ctx, 11, "bad slot or output");
@@ -543,6 +553,7 @@ extern "C" int covgpu_simulate(covgpu_ctx* ctx, const double* ld, const double* 
                                const double* pi4, const double* Q16, const double* pi16, const int* ct,
                                const uint8_t* root, double gap_rate, double gap_mean, uint64_t seed, uint32_t rep0,
                                int first_slot, int nrep) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   ctx->cnt_valid = false;
   const int N = ctx->N, L = ctx->L, Lp = ctx->Lp;
@@ -626,6 +637,7 @@ extern "C" int covgpu_simulate(covgpu_ctx* ctx, const double* ld, const double* 
 }
 
 extern "C" int covgpu_sim_tables(covgpu_ctx* ctx, double* P4, double* P16) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   if (!ctx->sim_branches) return fail(ctx, 11, "no simulation yet");
   if (P4) CK(cudaMemcpy(P4, ctx->d_P4, (size_t)ctx->sim_branches * 16 * sizeof(double), cudaMemcpyDeviceToHost));
@@ -634,6 +646,7 @@ extern "C" int covgpu_sim_tables(covgpu_ctx* ctx, double* P4, double* P16) {
 }
 
 extern "C" int covgpu_make_nulls(covgpu_ctx* ctx, uint64_t seed, int first_null, int nnull, int first_slot) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   int s = make_nulls_async(ctx, seed, first_null, nnull, first_slot);
   if (s) return s;
@@ -812,6 +825,7 @@ static int score_sync(covgpu_ctx* ctx, int first_slot, int nslots, int ntypes, c
 extern "C" int covgpu_score(covgpu_ctx* ctx, int first_slot, int nslots, int ntypes, const int* covtypes,
                             int covclass, int nseqthresh, int alenthresh, const double* allow, int counter,
                             double* minmax) {
+  if (!ctx) return 11;
   return score_sync(ctx, first_slot, nslots, ntypes, covtypes, covclass, nseqthresh, alenthresh, allow, counter,
                     minmax, false);
 }
@@ -819,11 +833,13 @@ extern "C" int covgpu_score(covgpu_ctx* ctx, int first_slot, int nslots, int nty
 extern "C" int covgpu_score_reuse(covgpu_ctx* ctx, int first_slot, int nslots, int ntypes, const int* covtypes,
                                   int covclass, int nseqthresh, int alenthresh, const double* allow, int counter,
                                   double* minmax) {
+  if (!ctx) return 11;
   return score_sync(ctx, first_slot, nslots, ntypes, covtypes, covclass, nseqthresh, alenthresh, allow, counter,
                     minmax, true);
 }
 
 extern "C" int covgpu_get_cov(covgpu_ctx* ctx, int slot, int which, double* COV) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const int rel = slot - ctx->last_first;
   if (rel < 0 || rel >= ctx->last_nslots || which < 0 || which >= ctx->last_nout)
@@ -839,6 +855,7 @@ extern "C" int covgpu_get_cov(covgpu_ctx* ctx, int slot, int which, double* COV)
 
 extern "C" int covgpu_get_probs(covgpu_ctx* ctx, int slot, const double* wgt, double* pp, double* nseff,
                                 double* ngap, double* pm, double* ps) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const int rel = slot - ctx->last_first;
   if (rel < 0 || rel >= ctx->last_nslots) return fail(ctx, 11, "slot %d was not scored", slot);
@@ -1150,6 +1167,7 @@ static int structured_kstar(covgpu_ctx* ctx, const float2* cov, EvalTables T, do
 
 extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint8_t* ax, const double* wgt,
                              int ntypes, const int* covtypes, covgpu_result* results, covgpu_hit* hits, int hitcap) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const int N = ctx->N, L = ctx->L;
   const int64_t P = (int64_t)L * (L - 1) / 2;
@@ -1410,6 +1428,7 @@ extern "C" int covgpu_rscape(covgpu_ctx* ctx, const covgpu_params* p, const uint
 // learned null
 // ------------------------------------------------------------------------
 extern "C" int covgpu_features(covgpu_ctx* ctx, int slot, double tree_len, float* feat) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   if (slot < 0 || slot >= ctx->maxslots || !feat) return fail(ctx, 11, "bad slot or output");
   if (!ctx->have_w) return fail(ctx, 11, "weights not set");
@@ -1444,6 +1463,7 @@ static int learned_features(covgpu_ctx* ctx, const covgpu_params* p, double tree
 
 extern "C" int covgpu_learned_features(covgpu_ctx* ctx, const covgpu_params* p, double tree_len, int covtype,
                                        int nquick, float* feat) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   covgpu_result quick;
   return learned_features(ctx, p, tree_len, covtype, nquick, feat, &quick);
@@ -1452,6 +1472,7 @@ extern "C" int covgpu_learned_features(covgpu_ctx* ctx, const covgpu_params* p, 
 extern "C" int covgpu_rscape_learned(covgpu_ctx* ctx, const covgpu_params* p, const uint8_t* ax, const double* wgt,
                                      covgpu_mlp* net, double tree_len, int covtype, int nquick,
                                      covgpu_result* result, covgpu_hit* hits, int hitcap, int* used_net) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const int L = ctx->L;
   const int64_t P = (int64_t)L * (L - 1) / 2;
@@ -1553,6 +1574,7 @@ extern "C" int covgpu_rscape_learned(covgpu_ctx* ctx, const covgpu_params* p, co
 // ------------------------------------------------------------------------
 extern "C" int covgpu_aggregate(covgpu_ctx* ctx, int method, int nh, const int* helix_off, const double* pval,
                                 const double* aux, double* pagg, double* Eagg) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   if (method < COVGPU_AGG_FISHER || method > COVGPU_AGG_SIDAK) return fail(ctx, 11, "unknown aggregation method");
   if (nh < 0 || (nh > 0 && (!helix_off || !pval || !pagg))) return fail(ctx, 11, "bad helix arguments");
@@ -1595,6 +1617,7 @@ extern "C" int covgpu_aggregate(covgpu_ctx* ctx, int method, int nh, const int* 
 // ------------------------------------------------------------------------
 extern "C" int covgpu_autotune(covgpu_ctx* ctx, int first_slot, int nslots, int ncand, const int* cand, float* ms,
                                int* best) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   ctx->cnt_valid = false;
   static const int defaults[] = {4, 6, 8, 10, 12, 16, 24};
@@ -1621,6 +1644,7 @@ extern "C" int covgpu_autotune(covgpu_ctx* ctx, int first_slot, int nslots, int 
 }
 
 extern "C" int covgpu_last_timing(const covgpu_ctx* ctx, double* ms5, int* nlaunch) {
+  if (!ctx) return 11;
   for (int k = 0; k < 5; k++) ms5[k] = ctx->tms[k];
   if (nlaunch) *nlaunch = ctx->nlaunch;
   return 0;
@@ -1629,6 +1653,7 @@ extern "C" int covgpu_last_timing(const covgpu_ctx* ctx, double* ms5, int* nlaun
 // overwrite a buffer larger than L2 (129 MB) so that the next call starts
 // from a cold cache
 extern "C" int covgpu_flush_l2(covgpu_ctx* ctx) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const size_t n = (size_t)256 << 20;
   if (!ctx->d_flush) CK(dalloc(&ctx->d_flush, n));
@@ -1638,6 +1663,7 @@ extern "C" int covgpu_flush_l2(covgpu_ctx* ctx) {
 }
 
 extern "C" int covgpu_validate_probs(covgpu_ctx* ctx, double tol) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   if (!ctx->counted || ctx->last_first != 0) return fail(ctx, 11, "no weighted counts of slot 0 on the device");
   CK(cudaMemsetAsync(ctx->d_nhits, 0, sizeof(int), ctx->st));
@@ -1650,6 +1676,7 @@ extern "C" int covgpu_validate_probs(covgpu_ctx* ctx, double tol) {
 }
 
 extern "C" int covgpu_pair_classes(covgpu_ctx* ctx, int slot, double* wcf, double* wobble, double* noncan) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   if (!ctx->cnt_valid || slot < ctx->cnt_first || slot >= ctx->cnt_first + ctx->cnt_nslots)
     return fail(ctx, 11, "no weighted counts of slot %d on the device", slot);
@@ -1686,6 +1713,7 @@ static int upload_full(covgpu_ctx* ctx, const double* COV) {
 }
 
 extern "C" int covgpu_correct(covgpu_ctx* ctx, const double* COV, int actype, double* out, double* minmax) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   if (actype != 0 && actype != 1) return fail(ctx, 11, "wrong correction type");
   int s = upload_full(ctx, COV);
@@ -1708,6 +1736,7 @@ extern "C" int covgpu_correct(covgpu_ctx* ctx, const double* COV, int actype, do
 }
 
 extern "C" int covgpu_hist_full(covgpu_ctx* ctx, const double* COV, double bmin, double w, int nb, uint64_t* obs) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   int s = upload_full(ctx, COV);
   if (s) return s;
@@ -1772,6 +1801,7 @@ static int hits_fetch(covgpu_ctx* ctx, int n, std::vector<covgpu_hit>& out) {
 extern "C" int covgpu_evalue_sets(covgpu_ctx* ctx, const double* COV, const void* hv, const double* survfit,
                                   double Nt, double Nb, double expBP, const uint32_t* bpmask, double thresh,
                                   double* Eval, covgpu_hit* hits, int hitcap, int* nhit) {
+  if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   const ESL_HISTOGRAM* h = (const ESL_HISTOGRAM*)hv;
   int s = upload_full(ctx, COV);
@@ -1874,5 +1904,6 @@ extern "C" void covgpu_host_unpin(void* p) {
 
 extern "C" int covgpu_evalue_full(covgpu_ctx* ctx, const double* COV, const void* hv, const double* survfit,
                                   double Nt, double thresh, double* Eval, covgpu_hit* hits, int hitcap, int* nhit) {
+  if (!ctx) return 11;
   return covgpu_evalue_sets(ctx, COV, hv, survfit, Nt, 0.0, -1.0, nullptr, thresh, Eval, hits, hitcap, nhit);
 }

@@ -564,6 +564,7 @@ extern "C" int covgpu_mlp_create(covgpu_mlp** ret, int device, int batch_cap, ui
 }
 
 extern "C" int covgpu_mlp_set_params(covgpu_mlp* net, const float* params) {
+  if (!net) return 11;
   MCK(cudaSetDevice(net->dev));
   for (int k = 0; k < kNParam; k++)
     if (!std::isfinite(params[k])) return mfail(net, 11, "parameter %d is not finite", k);
@@ -575,6 +576,7 @@ extern "C" int covgpu_mlp_set_params(covgpu_mlp* net, const float* params) {
 }
 
 extern "C" int covgpu_mlp_set_members(covgpu_mlp* net, const float* params, int nmem) {
+  if (!net) return 11;
   MCK(cudaSetDevice(net->dev));
   if (nmem < 0 || nmem > COVGPU_MLP_MAXMEM) return mfail(net, 11, "%d members outside 0..%d", nmem, COVGPU_MLP_MAXMEM);
   if (nmem > 0 && !params) return mfail(net, 11, "no member parameters");
@@ -598,6 +600,7 @@ extern "C" int covgpu_mlp_set_members(covgpu_mlp* net, const float* params, int 
 }
 
 extern "C" int covgpu_mlp_get_params(covgpu_mlp* net, float* params) {
+  if (!net) return 11;
   MCK(cudaSetDevice(net->dev));
   MCK(cudaMemcpyAsync(params, net->p, kNParam * sizeof(float), cudaMemcpyDeviceToHost, net->st));
   MCK(cudaStreamSynchronize(net->st));
@@ -606,6 +609,7 @@ extern "C" int covgpu_mlp_get_params(covgpu_mlp* net, float* params) {
 
 extern "C" int covgpu_mlp_set_norm(covgpu_mlp* net, const float* xmean, const float* xstd, const float* ymean,
                                    const float* ystd, const float* xlo, const float* xhi) {
+  if (!net) return 11;
   MCK(cudaSetDevice(net->dev));
   for (int f = 0; f < kNFeat; f++) {
     if (!(xstd[f] > 0.f) || !std::isfinite(xmean[f])) return mfail(net, 11, "feature %d: bad standardisation", f);
@@ -625,6 +629,7 @@ extern "C" int covgpu_mlp_set_norm(covgpu_mlp* net, const float* xmean, const fl
 
 extern "C" int covgpu_mlp_get_norm(const covgpu_mlp* net, float* xmean, float* xstd, float* ymean, float* ystd,
                                    float* xlo, float* xhi) {
+  if (!net) return 11;
   for (int f = 0; f < kNFeat; f++) {
     if (xmean) xmean[f] = net->h_nrm[f];
     if (xstd) xstd[f] = net->h_nrm[kNFeat + f];
@@ -639,12 +644,14 @@ extern "C" int covgpu_mlp_get_norm(const covgpu_mlp* net, float* xmean, float* x
 }
 
 extern "C" int covgpu_mlp_in_range(const covgpu_mlp* net, const float* feat) {
+  if (!net || !feat) return 0;
   for (int f = 0; f < kNFeat; f++)
     if (!(feat[f] >= net->xlo[f] && feat[f] <= net->xhi[f])) return 0;
   return 1;
 }
 
 extern "C" int covgpu_mlp_forward(covgpu_mlp* net, const float* X, int n, float* Y) {
+  if (!net) return 11;
   MCK(cudaSetDevice(net->dev));
   if (n < 0) return mfail(net, 11, "negative row count");
   for (int r0 = 0; r0 < n; r0 += net->cap) {
@@ -673,6 +680,7 @@ extern "C" int covgpu_mlp_forward(covgpu_mlp* net, const float* X, int n, float*
 }
 
 extern "C" int covgpu_mlp_grad(covgpu_mlp* net, const float* X, const float* T, int n, float* grad, float* loss) {
+  if (!net) return 11;
   MCK(cudaSetDevice(net->dev));
   if (n < 1 || n > net->cap) return mfail(net, 11, "batch of %d rows outside 1..%d", n, net->cap);
   float* dT = nullptr;
@@ -697,6 +705,7 @@ extern "C" int covgpu_mlp_grad(covgpu_mlp* net, const float* X, const float* T, 
 
 extern "C" int covgpu_mlp_train(covgpu_mlp* net, const float* X, const float* T, int n, int epochs, int batch,
                                 float lr, float wd, uint64_t seed, float* epoch_loss) {
+  if (!net) return 11;
   MCK(cudaSetDevice(net->dev));
   if (batch < 1 || batch > net->cap || n < batch || epochs < 1)
     return mfail(net, 11, "need 1 <= batch <= %d, batch <= n and epochs >= 1", net->cap);

@@ -259,3 +259,29 @@ def test_small_reference_entry_points(covgpu, tmp_path, capfd):
     assert lib.corr_PostOrderPP(None, None, None, None, 1e-6, 0, eb) != 0 and b"AKMAEV" in eb.value
     lib.cov_CreateFOLDHitList.argtypes = [ctypes.POINTER(abi.Data)] + [ctypes.c_void_p] * 8
     assert lib.cov_CreateFOLDHitList(ctypes.byref(data), None, None, None, None, None, None, None, None) != 0
+
+
+def handle_entry_points(path):
+    """(name, parameter count) of every function in a header whose first
+    parameter is a context, batch or network handle."""
+    src = re.sub(r"/\*.*?\*/", "", open(path).read(), flags=re.S)
+    out = []
+    for m in re.finditer(r"\bint\s+(covgpu_\w+)\s*\(\s*(?:const\s+)?covgpu_(?:ctx|batch|mlp)\s*\*\s*\w+([^;]*?)\)\s*;",
+                         src, flags=re.S):
+        rest = m.group(2).strip()
+        out.append((m.group(1), 1 + (rest.count(",") if rest else 0)))
+    return out
+
+
+def test_null_handles_are_rejected(covgpu):
+    """Every entry point that takes a context, batch or network returns 11
+    for a NULL handle, before any device work (no GPU needed)."""
+    lib = ctypes.CDLL(covgpu.LIBPATH)
+    entries = handle_entry_points(os.path.join(ROOT, "include", "covgpu.h"))
+    assert len(entries) > 40, entries
+    for name, nargs in entries:
+        f = getattr(lib, name)
+        f.restype = ctypes.c_int
+        got = f(*([None] * nargs))
+        want = 0 if name == "covgpu_mlp_in_range" else 11   # a yes/no answer: not in range
+        assert got == want, (name, got)
