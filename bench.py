@@ -426,6 +426,9 @@ def main():
                     help="one call of the P(t) simulator on the workload's tree (for profiler captures)")
     ap.add_argument("--once", action="store_true",
                     help="one covgpu_rscape call of the workload and exit (for profiler captures)")
+    ap.add_argument("--schedule", type=int, default=0,
+                    help="with --once: count-kernel raster super-block to set before a second call "
+                         "(e.g. 32004; profiler captures of that schedule)")
     ap.add_argument("--N", type=int, default=None, help="override N (profiling a smaller case)")
     ap.add_argument("--L", type=int, default=None, help="override L (profiling a smaller case)")
     ap.add_argument("--nshuffle", type=int, default=None, help="override the number of nulls")
@@ -526,6 +529,10 @@ def main():
         print(json.dumps({"once_sim": True, **simulator_rate(cg, e, s, N, L, ns)}))
         return
     if args.once:
+        if args.schedule and counter == 1:
+            # the given raster (one autotune candidate: four count launches), then the call again
+            e.autotune(ns + 1, candidates=(args.schedule,))
+            r = e.rscape(None, None, TYPES, nshuffle=ns, counter=counter)
         ms, n = e.last_timing()
         print(json.dumps({"once": True, "N": N, "L": L, "nshuffle": ns, "types": TYPES, "counter": counter,
                           "device_ms": list(ms), "launches": n, "hits": [len(x["hits"]) for x in r]}))

@@ -290,11 +290,12 @@ int  covgpu_correct_noalloc(const double *d_cov, double *d_out, int L, int actyp
 
 /* schedule autotuner of the tensor count kernel: times the weighted count of
  * slots first_slot .. first_slot+nslots-1 (weights set) for each raster
- * super-block size in cand[ncand] (NULL: 4, 6, 8, 10, 12, 16, 24; the
- * resident CTAs sweep blocks of size x size tiles so they share operand rows
- * in L2), keeps the fastest for the context's later calls, and returns the
- * median milliseconds of each in ms (may be NULL) and the choice in *best.
- * The count buffer is overwritten. */
+ * super-block in cand[ncand] and keeps the fastest for the context's later
+ * calls.  The resident CTAs sweep super-blocks of tiles so they share operand
+ * rows in L2: a value v < 1000 is a square of v x v tiles, v = 1000 a + b a
+ * band a tile rows high and b columns wide (NULL: 4, 6, 8, 10, 12, 16, 24,
+ * 32004, 48004, 48008, 96004).  Returns the median milliseconds of each in ms
+ * (may be NULL) and the choice in *best.  The count buffer is overwritten. */
 int  covgpu_autotune(covgpu_ctx *ctx, int first_slot, int nslots, int ncand, const int *cand, float *ms, int *best);
 
 /* writes a 256 MB device buffer (larger than L2) on the context's stream */

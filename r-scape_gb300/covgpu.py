@@ -449,8 +449,9 @@ class Engine:
                                         ax.ctypes.data if ax is not None else None, pagg, Eagg))
         return pagg, Eagg
 
-    def autotune(self, nslots, first_slot=0, candidates=(4, 6, 8, 10, 12, 16, 24)):
-        """Pick the tensor count kernel's raster super-block on these alignments: (best, {size: ms})."""
+    def autotune(self, nslots, first_slot=0, candidates=(4, 6, 8, 10, 12, 16, 24, 32004, 48004, 48008, 96004)):
+        """Pick the tensor count kernel's raster super-block on these alignments: (best, {size: ms}).
+        A size below 1000 is a square super-block; 1000 a + b is a band a tile rows high, b wide."""
         cand = np.ascontiguousarray(candidates, dtype=np.int32)
         ms = np.zeros(len(cand), dtype=np.float32)
         best = C.c_int(0)

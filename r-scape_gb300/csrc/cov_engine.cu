@@ -1620,7 +1620,7 @@ extern "C" int covgpu_autotune(covgpu_ctx* ctx, int first_slot, int nslots, int 
   if (!ctx) return 11;
   CK(cudaSetDevice(ctx->dev));
   ctx->cnt_valid = false;
-  static const int defaults[] = {4, 6, 8, 10, 12, 16, 24};
+  static const int defaults[] = {4, 6, 8, 10, 12, 16, 24, 32004, 48004, 48008, 96004};
   if (!cand || ncand <= 0) { cand = defaults; ncand = (int)(sizeof(defaults) / sizeof(defaults[0])); }
   if (first_slot < 0 || nslots < 1 || first_slot + nslots > ctx->maxslots) return fail(ctx, 11, "slots out of range");
   if (!ctx->have_w) return fail(ctx, 11, "weights not set");

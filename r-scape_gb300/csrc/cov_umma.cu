@@ -611,27 +611,47 @@ static size_t smem_bytes(int nb, int stages) {
   return ring + stage_out + 1024;
 }
 
-// blocked raster: super-blocks of SB x SB tiles (I <= J) in turn, so the
-// CTAs resident at one time share a few operand row blocks in L2
+// blocked raster: super-blocks of SBI x SBJ tiles (I <= J) in turn, band of
+// SBI tile rows by band, so the CTAs resident at one time share a few operand
+// row blocks in L2.  A schedule value v below 1000 is a square SB = v; v =
+// 1000 SBI + SBJ is a band SBI rows high and SBJ columns wide (a tall band
+// reads each column block's operands once per band, so fewer bands mean
+// fewer re-reads of the B operands from DRAM).
+static bool decode_sb(int v, int* sbi, int* sbj) {
+  if (v < 1) return false;
+  if (v < 1000) { *sbi = *sbj = v; return true; }
+  *sbi = v / 1000; *sbj = v % 1000;
+  return *sbi >= 1 && *sbj >= 1;
+}
+
 static bool set_order(UmmaPlan* p, int SB) {
+  int SBI = 0, SBJ = 0;
+  if (!decode_sb(SB, &SBI, &SBJ)) return false;
   const int nT = p->nT;
   std::vector<int> order;
   order.reserve(p->ntiles);
   auto tindex = [nT](int I, int J) { return I * nT - I * (I - 1) / 2 + (J - I); };   // I-major tile list
-  for (int bI = 0; bI < nT; bI += SB)
-    for (int bJ = bI; bJ < nT; bJ += SB)
-      for (int I = bI; I < std::min(nT, bI + SB); I++)
-        for (int J = std::max(I, bJ); J < std::min(nT, bJ + SB); J++) order.push_back(tindex(I, J));
+  for (int bI = 0; bI < nT; bI += SBI)
+    for (int bJ = bI; bJ < nT; bJ += SBJ)
+      for (int I = bI; I < std::min(nT, bI + SBI); I++)
+        for (int J = std::max(I, bJ); J < std::min(nT, bJ + SBJ); J++) order.push_back(tindex(I, J));
   if ((int)order.size() != p->ntiles) return false;
+  {   // every tile exactly once
+    std::vector<char> seen(p->ntiles, 0);
+    for (int t : order) {
+      if (t < 0 || t >= p->ntiles || seen[t]) return false;
+      seen[t] = 1;
+    }
+  }
   // column-tile pairs (J0, J0 + 1), J0 even, for the unit-weight kernel:
-  // super-blocks of SB rows x SB/2 pairs; each tile I <= J lies in exactly
+  // super-blocks of SBI rows x SBJ/2 pairs; each tile I <= J lies in exactly
   // one pair, so there are at most ntiles of them
   std::vector<int4> jp;
   jp.reserve(p->ntiles);
-  const int nP = (nT + 1) / 2, SP = std::max(1, SB / 2);
-  for (int bI = 0; bI < nT; bI += SB)
+  const int nP = (nT + 1) / 2, SP = std::max(1, SBJ / 2);
+  for (int bI = 0; bI < nT; bI += SBI)
     for (int bP = bI / 2; bP < nP; bP += SP)
-      for (int I = bI; I < std::min(nT, bI + SB); I++)
+      for (int I = bI; I < std::min(nT, bI + SBI); I++)
         for (int q = std::max(I / 2, bP); q < std::min(nP, bP + SP); q++) {
           const int J0 = 2 * q;
           jp.push_back(make_int4(I, J0, J0 >= I ? tindex(I, J0) : -1, J0 + 1 < nT ? tindex(I, J0 + 1) : -1));

@@ -57,12 +57,17 @@ def test_autotuned_schedule_gives_identical_scores(covgpu):
     e.set_weights(covgpu.weights_pb(s.ax))
     e.set_alignment(0, s.ax)
     e.make_nulls(42, 0, 2, 1)
-    e.score(["GTp", "MIp"], nslots=3, counter=covgpu.TENSOR)
-    before = [e.get_cov(k, q) for k in range(3) for q in range(2)]
-    best, ms = e.autotune(3, candidates=(2, 5, 10, 23))
-    assert best in (2, 5, 10, 23) and all(v > 0 for v in ms.values())
-    e.score(["GTp", "MIp"], nslots=3, counter=covgpu.TENSOR)
-    after = [e.get_cov(k, q) for k in range(3) for q in range(2)]
-    for a, b in zip(before, after):
-        assert np.array_equal(a, b)
+    types = ["GTp", "MIp", "RAFp"]   # RAF: the unit-weight kernel's column-pair order
+    e.score(types, nslots=3, counter=covgpu.TENSOR)
+    before = [e.get_cov(k, q) for k in range(3) for q in range(3)]
+    best, ms = e.autotune(3, candidates=(2, 5, 10, 23, 32004, 6003))
+    assert best in (2, 5, 10, 23, 32004, 6003) and all(v > 0 for v in ms.values())
+    # the autotuner's choice, then every square and band schedule forced alone
+    for cand in (None, 2, 23, 32004, 6003, 96002, 1001):
+        if cand is not None:
+            assert e.autotune(3, candidates=(cand,))[0] == cand
+        e.score(types, nslots=3, counter=covgpu.TENSOR)
+        after = [e.get_cov(k, q) for k in range(3) for q in range(3)]
+        for a, b in zip(before, after):
+            assert np.array_equal(a, b), cand
     e.close()
