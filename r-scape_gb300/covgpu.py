@@ -219,6 +219,59 @@ def gapfilter(ax, wgt=None, gapthresh=0.75):
     return use.astype(bool)
 
 
+# Easel's digital RNA alphabet: codes 0-3 the residues, 4 the gap, 5-15 the
+# degeneracies, 16 the nonresidue, 17 the missing-data symbol
+RNA_SYMBOLS = "ACGU-RYMKSWHBVDN*~"
+
+
+def write_stockholm(path, ax, names=None, msa_name=None, append=False):
+    """An alignment of Easel digital RNA codes [N][L] as one Stockholm record
+    (header, #=GF ID when msa_name is given, one line per sequence, //): the
+    format R-scape's --outnull writes its null alignments in
+    (src/R-scape.c:1645-1672, one esl_msafile_Write record per null).  With
+    append=True the records of several alignments go to one file."""
+    ax = np.asarray(ax, dtype=np.uint8)
+    if ax.ndim != 2 or (ax.size and int(ax.max()) >= len(RNA_SYMBOLS)):
+        raise ValueError("codes must be a 2-D array of values below %d" % len(RNA_SYMBOLS))
+    N = ax.shape[0]
+    names = ["seq%d" % (k + 1) for k in range(N)] if names is None else [str(n) for n in names]
+    if len(names) != N or any((not n) or any(ch.isspace() for ch in n) for n in names):
+        raise ValueError("one non-empty name without spaces per sequence")
+    table = np.frombuffer(RNA_SYMBOLS.encode(), dtype=np.uint8)
+    width = max(len(n) for n in names) if N else 0
+    with open(path, "a" if append else "w") as fh:
+        fh.write("# STOCKHOLM 1.0\n")
+        if msa_name:
+            fh.write("#=GF ID %s\n" % msa_name)
+        fh.write("\n")
+        for n, row in zip(names, ax):
+            fh.write("%-*s %s\n" % (width, n, table[row].tobytes().decode()))
+        fh.write("//\n")
+
+
+def read_stockholm(path):
+    """The records of a Stockholm file as (ID or None, names, codes [N][L])
+    tuples, for records written one line per sequence (write_stockholm's
+    form); the residues are mapped to Easel digital RNA codes (T as U, '.'
+    as a gap, lower case as upper case)."""
+    look = {ch: k for k, ch in enumerate(RNA_SYMBOLS)}
+    look.update({"T": 3, ".": 4, "_": 4})
+    out, name, names, rows = [], None, [], []
+    for line in open(path):
+        line = line.rstrip("\n")
+        if line.startswith("//"):
+            ax = np.array([[look[ch] for ch in r.upper()] for r in rows], dtype=np.uint8)
+            out.append((name, names, ax.reshape(len(rows), -1)))
+            name, names, rows = None, [], []
+        elif line.startswith("#=GF ID"):
+            name = line.split(None, 2)[2].strip()
+        elif line.strip() and not line.startswith("#"):
+            n, r = line.split()
+            names.append(n)
+            rows.append(r)
+    return out
+
+
 AGG_FISHER, AGG_LANCASTER, AGG_WFISHER, AGG_SIDAK = 0, 1, 2, 3
 
 
@@ -279,6 +332,16 @@ class Engine:
         out = np.zeros((self.N, self.L), dtype=np.uint8)
         self._ck(lib().covgpu_get_alignment(self.h, slot, out))
         return out
+
+    def write_nulls(self, path, first_slot, nslots, names=None, msa_name="null"):
+        """The alignments in slots first_slot .. first_slot+nslots-1 (the null
+        alignments after make_nulls, or after rscape) into one Stockholm file,
+        one record per alignment named msa_name + index, as R-scape's --outnull
+        writes its nulls (src/R-scape.c:1645-1672)."""
+        open(path, "w").close()
+        for k in range(nslots):
+            write_stockholm(path, self.get_alignment(first_slot + k), names, "%s%d" % (msa_name, k + 1),
+                            append=True)
 
     def set_tree(self, parent, left, right):
         self._ck(lib().covgpu_set_tree(self.h, np.ascontiguousarray(parent, dtype=np.int32),

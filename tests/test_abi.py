@@ -285,3 +285,24 @@ def test_null_handles_are_rejected(covgpu):
         got = f(*([None] * nargs))
         want = 0 if name == "covgpu_mlp_in_range" else 11   # a yes/no answer: not in range
         assert got == want, (name, got)
+
+
+def test_stockholm_round_trip(covgpu, tmp_path):
+    """Alignments written in R-scape's --outnull form (Stockholm, one record
+    per alignment) read back code for code, every digital RNA code included."""
+    rng = np.random.default_rng(4)
+    a = rng.integers(0, 18, size=(7, 33)).astype(np.uint8)
+    b = covgpu.Synth(12, 40, 1.0, 6, 1, 6, 6, 0.1, seed=9).ax
+    path = str(tmp_path / "nulls.sto")
+    covgpu.write_stockholm(path, a, msa_name="null1")
+    covgpu.write_stockholm(path, b, names=["s%02d" % k for k in range(12)], msa_name="null2", append=True)
+    text = open(path).read()
+    assert text.startswith("# STOCKHOLM 1.0\n") and text.count("//\n") == 2
+    recs = covgpu.read_stockholm(path)
+    assert [r[0] for r in recs] == ["null1", "null2"]
+    assert np.array_equal(recs[0][2], a) and np.array_equal(recs[1][2], b)
+    assert recs[1][1][0] == "s00"
+    with pytest.raises(ValueError):
+        covgpu.write_stockholm(path, np.full((2, 3), 18, dtype=np.uint8))
+    with pytest.raises(ValueError):
+        covgpu.write_stockholm(path, a, names=["x y"] * 7)

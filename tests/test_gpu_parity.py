@@ -108,6 +108,24 @@ def test_null_alignments_identical(covgpu, oracle, N, L):
     e.close()
 
 
+def test_null_alignments_written_as_stockholm(covgpu, oracle, tmp_path):
+    """The null alignments of an E-valued call, written in R-scape's --outnull
+    form (one Stockholm record per null), read back as the oracle's nulls."""
+    N, L, ns = 90, 70, 4
+    s, w = make(covgpu, N, L, 17)
+    e = covgpu.Engine(N, L, maxslots=ns + 1, maxnull=ns)
+    e.set_tree(s.parent, s.left, s.right)
+    e.rscape(s.ax, w, ["GTp"], nshuffle=ns)
+    path = str(tmp_path / "nulls.sto")
+    e.write_nulls(path, 1, ns)
+    e.close()
+    recs = covgpu.read_stockholm(path)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    assert [r[0] for r in recs] == ["null%d" % (k + 1) for k in range(ns)]
+    for k, (name, names, ax) in enumerate(recs):
+        assert np.array_equal(ax, oracle.null_msa(s.ax, T, 42, k)), name
+
+
 @pytest.mark.parametrize("counter", ["simt", "tensor"])
 @pytest.mark.parametrize("N,L,types", [
     (200, 120, ["GTp"]),
