@@ -696,11 +696,18 @@ cudaError_t launch_weights_gsc(const uint8_t* ax, int N, int L, int Lp, void* sc
   // the barrier and the reduction of the partials stay short
   const int G = std::max(1, std::min(std::min(nsm, 32), (N + 63) / 64));
   const size_t smg = gsc_grid_smem(N, G);
+  // the launch limit of both merge kernels is raised once, to the 200 KB
+  // that either may take: a limit set per call to that call's size would
+  // race with other host threads' calls for other N (a launch above the
+  // limit another thread just set fails with an invalid argument)
+  static const cudaError_t attr = [] {
+    cudaError_t r = cudaFuncSetAttribute(k_gsc_upgma_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (r == cudaSuccess) r = cudaFuncSetAttribute(k_gsc_upgma, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    return r;
+  }();
+  if (attr != cudaSuccess) return attr;
   if (coop && N >= 2 && smg <= 200 * 1024) {
     int occ = 0;
-    if ((e = cudaFuncSetAttribute(k_gsc_upgma_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smg)) !=
-        cudaSuccess)
-      return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gsc_upgma_grid, 256, smg)) != cudaSuccess) return e;
     if (occ >= 1 && G <= occ * nsm) {
       int n = N;
@@ -711,8 +718,6 @@ cudaError_t launch_weights_gsc(const uint8_t* ax, int N, int L, int Lp, void* sc
   // one CTA while the cluster state fits in its shared memory
   const size_t sm = gsc_upgma_smem(N);
   if (sm <= 200 * 1024) {
-    if ((e = cudaFuncSetAttribute(k_gsc_upgma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess)
-      return e;
     k_gsc_upgma<<<1, 1024, sm, st>>>(D, N, w);
     return cudaGetLastError();
   }
