@@ -297,6 +297,14 @@ int  covgpu_correct_noalloc(const double *d_cov, double *d_out, int L, int actyp
  * 32004, 48004, 48008, 96004).  Returns the median milliseconds of each in ms
  * (may be NULL) and the choice in *best.  The count buffer is overwritten. */
 int  covgpu_autotune(covgpu_ctx *ctx, int first_slot, int nslots, int ncand, const int *cand, float *ms, int *best);
+/* host code (no device): the tensor count's task orders for a schedule value
+ * (as in covgpu_autotune) on nT column tiles of 32 columns.  order[nT(nT+1)/2]
+ * receives the weighted kernel's tiles (indices into the row-major list of
+ * tiles I <= J); jpairs[4 * jcap] (may be NULL) the unit-weight kernel's
+ * tasks {I, J0, tile (I, J0), tile (I, J0 + 1)} (-1 for a tile outside
+ * I <= J < nT) and *njpairs their number.  Returns 0, or 11 (bad schedule,
+ * nT < 1, jcap too small). */
+int  covgpu_tile_order(int nT, int schedule, int *order, int *jpairs, int jcap, int *njpairs);
 
 /* writes a 256 MB device buffer (larger than L2) on the context's stream */
 int  covgpu_flush_l2(covgpu_ctx *ctx);

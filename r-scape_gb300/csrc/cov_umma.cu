@@ -624,30 +624,31 @@ static bool decode_sb(int v, int* sbi, int* sbj) {
   return *sbi >= 1 && *sbj >= 1;
 }
 
-static bool set_order(UmmaPlan* p, int SB) {
+// the two task orders of a schedule value on nT x nT tiles (host code)
+static bool build_order(int nT, int SB, std::vector<int>& order, std::vector<int4>& jp) {
   int SBI = 0, SBJ = 0;
-  if (!decode_sb(SB, &SBI, &SBJ)) return false;
-  const int nT = p->nT;
-  std::vector<int> order;
-  order.reserve(p->ntiles);
+  if (nT < 1 || !decode_sb(SB, &SBI, &SBJ)) return false;
+  const int ntiles = nT * (nT + 1) / 2;
+  order.clear();
+  order.reserve(ntiles);
   auto tindex = [nT](int I, int J) { return I * nT - I * (I - 1) / 2 + (J - I); };   // I-major tile list
   for (int bI = 0; bI < nT; bI += SBI)
     for (int bJ = bI; bJ < nT; bJ += SBJ)
       for (int I = bI; I < std::min(nT, bI + SBI); I++)
         for (int J = std::max(I, bJ); J < std::min(nT, bJ + SBJ); J++) order.push_back(tindex(I, J));
-  if ((int)order.size() != p->ntiles) return false;
+  if ((int)order.size() != ntiles) return false;
   {   // every tile exactly once
-    std::vector<char> seen(p->ntiles, 0);
+    std::vector<char> seen(ntiles, 0);
     for (int t : order) {
-      if (t < 0 || t >= p->ntiles || seen[t]) return false;
+      if (t < 0 || t >= ntiles || seen[t]) return false;
       seen[t] = 1;
     }
   }
   // column-tile pairs (J0, J0 + 1), J0 even, for the unit-weight kernel:
   // super-blocks of SBI rows x SBJ/2 pairs; each tile I <= J lies in exactly
   // one pair, so there are at most ntiles of them
-  std::vector<int4> jp;
-  jp.reserve(p->ntiles);
+  jp.clear();
+  jp.reserve(ntiles);
   const int nP = (nT + 1) / 2, SP = std::max(1, SBJ / 2);
   for (int bI = 0; bI < nT; bI += SBI)
     for (int bP = bI / 2; bP < nP; bP += SP)
@@ -656,12 +657,38 @@ static bool set_order(UmmaPlan* p, int SB) {
           const int J0 = 2 * q;
           jp.push_back(make_int4(I, J0, J0 >= I ? tindex(I, J0) : -1, J0 + 1 < nT ? tindex(I, J0 + 1) : -1));
         }
-  if ((int)jp.size() > p->ntiles) return false;
+  return (int)jp.size() <= ntiles;
+}
+
+static bool set_order(UmmaPlan* p, int SB) {
+  std::vector<int> order;
+  std::vector<int4> jp;
+  if (!build_order(p->nT, SB, order, jp) || (int)order.size() != p->ntiles) return false;
   p->sb = SB;
   p->njpairs = (int)jp.size();
   return cudaMemcpy(p->d_order, order.data(), sizeof(int) * p->ntiles, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(p->d_jpairs, jp.data(), sizeof(int4) * jp.size(), cudaMemcpyHostToDevice) == cudaSuccess;
 }
+
+}  // namespace covgpu
+
+// host code, no device: the tensor count's task orders for a schedule value
+// (see covgpu_autotune) on nT column tiles; order[nT (nT + 1) / 2] gets the
+// weighted kernel's tiles (indices into the I-major list of tiles I <= J),
+// jpairs[4 * capacity] the unit-weight kernel's {I, J0, tile (I, J0), tile
+// (I, J0 + 1)} (-1 outside I <= J < nT), *njpairs their number
+extern "C" int covgpu_tile_order(int nT, int schedule, int* order, int* jpairs, int jcap, int* njpairs) {
+  std::vector<int> o;
+  std::vector<int4> jp;
+  if (!order || !njpairs || !covgpu::build_order(nT, schedule, o, jp)) return 11;
+  if (jpairs && (int)jp.size() > jcap) return 11;
+  std::memcpy(order, o.data(), sizeof(int) * o.size());
+  if (jpairs) std::memcpy(jpairs, jp.data(), sizeof(int4) * jp.size());
+  *njpairs = (int)jp.size();
+  return 0;
+}
+
+namespace covgpu {
 
 // dimensions of the current alignments within the plan's buffers: tile
 // order, operand tensor maps; false when they do not fit

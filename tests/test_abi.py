@@ -306,3 +306,39 @@ def test_stockholm_round_trip(covgpu, tmp_path):
         covgpu.write_stockholm(path, np.full((2, 3), 18, dtype=np.uint8))
     with pytest.raises(ValueError):
         covgpu.write_stockholm(path, a, names=["x y"] * 7)
+
+
+@pytest.mark.parametrize("schedule", [1, 4, 10, 12, 24, 1001, 3005, 32004, 48008, 96004, 7001])
+def test_count_schedules_cover_every_tile_once(covgpu, schedule):
+    """Every raster the autotuner may pick (squares and bands) is a
+    permutation of the upper-triangle tiles for the weighted count, and the
+    unit-weight count's column-pair tasks cover each tile exactly once."""
+    lib = ctypes.CDLL(covgpu.LIBPATH)
+    for nT in list(range(1, 24)) + [47, 94, 188]:
+        nt = nT * (nT + 1) // 2
+        order = np.zeros(nt, dtype=np.int32)
+        jp = np.zeros((nt, 4), dtype=np.int32)
+        nj = ctypes.c_int()
+        assert lib.covgpu_tile_order(nT, schedule, order.ctypes.data, jp.ctypes.data, nt, ctypes.byref(nj)) == 0
+        assert np.array_equal(np.sort(order), np.arange(nt)), (nT, schedule)
+        jp = jp[:nj.value]
+        tiles = jp[:, 2:].ravel()
+        tiles = tiles[tiles >= 0]
+        assert np.array_equal(np.sort(tiles), np.arange(nt)), (nT, schedule)
+        # the tiles of a task lie in its row I, at columns J0 and J0 + 1
+        I, J0 = jp[:, 0], jp[:, 1]
+        row0 = I * nT - I * (I - 1) // 2
+        ok0 = jp[:, 2] < 0
+        assert np.all(ok0 | (jp[:, 2] == row0 + J0 - I))
+        ok1 = jp[:, 3] < 0
+        assert np.all(ok1 | (jp[:, 3] == row0 + J0 + 1 - I))
+        assert np.all(J0 % 2 == 0) and np.all(J0 + 1 >= I)
+
+
+def test_count_schedule_rejects_bad_values(covgpu):
+    lib = ctypes.CDLL(covgpu.LIBPATH)
+    order = np.zeros(64, dtype=np.int32)
+    nj = ctypes.c_int()
+    for bad in (0, -3, 5000, 1000):
+        assert lib.covgpu_tile_order(10, bad, order.ctypes.data, None, 0, ctypes.byref(nj)) == 11
+    assert lib.covgpu_tile_order(0, 10, order.ctypes.data, None, 0, ctypes.byref(nj)) == 11
