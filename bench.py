@@ -402,6 +402,16 @@ def cpu_reference(ax, w, budget_s, threads):
                                     "count_gt_pairs_per_s": 1.0 / t_count}
 
 
+def guarded(fn, *args, **kw):
+    """One of the bench line's extra measurements (measured after the headline
+    numbers): its result, or its error as a string in the line, so that a
+    failing extra neither hides the headline nor fails silently."""
+    try:
+        return fn(*args, **kw)
+    except Exception as ex:   # reported in the line
+        return {"error": "%s: %s" % (type(ex).__name__, ex)}
+
+
 def max_over_ranks(values, world):
     """Each value's largest over the ranks (the slowest rank's times), by an
     all-reduce on the process group; the values themselves with one rank."""
@@ -595,10 +605,11 @@ def main():
                      "tensor_speedup": ms_s / (step_s * 1000.0), "same_pair_sets": same,
                      "pairs_e_lt_thresh": [len(x["hits"]) for x in rs]}
         cpu_v, cpu_sample, cpu_parts = cpu_reference(ax, w, args.cpu_budget, threads)
-        sim = simulator_rate(cg, e, s, N, L, ns)
-        fam = ragged_families(cg, args.families, counter, local, args.family_compare) if args.families > 0 else None
-        bnull = batched_nulls(cg, counter, local)
-        dflow = dropin_flow(cg, e, ax, w, ns)
+        sim = guarded(simulator_rate, cg, e, s, N, L, ns)
+        fam = guarded(ragged_families, cg, args.families, counter, local, args.family_compare) \
+            if args.families > 0 else None
+        bnull = guarded(batched_nulls, cg, counter, local)
+        dflow = guarded(dropin_flow, cg, e, ax, w, ns)
     out = {
         "metric": METRIC, "value": value, "unit": "column-pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * step_s, "higher_is_better": True, "scaling": "weak",

@@ -19,3 +19,18 @@ def test_reference_arm_prints_contract_line(covgpu, oracle):
         assert k in line, k
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_extra_measurements_report_their_errors():
+    """A failing extra measurement puts its error into the bench line instead
+    of ending the run (the headline numbers are measured before the extras)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+
+    def bad(x):
+        raise RuntimeError("covgpu error 90: %s" % x)
+
+    assert b.guarded(lambda x, y=1: x + y, 2, y=3) == 5
+    assert b.guarded(bad, "invalid argument") == {"error": "RuntimeError: covgpu error 90: invalid argument"}
