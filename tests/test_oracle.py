@@ -336,3 +336,43 @@ def test_two_set_test_and_structured(oracle, covgpu):
     pdb = oracle.rscape(s.ax, w, T, msa2pdb=m2p, mind=4, **kw)
     assert pdb["Nt"] == P - (3 * L - 6)
     assert pdb["h_n"] == 5 * (P - (3 * L - 6))
+
+
+@pytest.mark.parametrize("doexpfit", [0, 1])
+def test_tail_fit_maximises_the_binned_likelihood(oracle, covgpu, doexpfit):
+    """The oracle's tail fit (esl_gam_FitCompleteBinned / esl_exp_FitCompleteBinned
+    restated: location at phi, binned maximum likelihood over the tail bins
+    cmin .. imax) against scipy's optimiser of the same binned likelihood,
+    written here from its definition."""
+    sp = pytest.importorskip("scipy.special")
+    so = pytest.importorskip("scipy.optimize")
+    s = covgpu.Synth(160, 110, 1.5, 25, 3, 8, 9, 0.08, seed=23, tree_kind=1)
+    w = oracle.weights_pb(s.ax)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    r = oracle.rscape(s.ax, w, T, covtype="GTp", nshuffle=20, doexpfit=doexpfit)
+    assert r["fit_ok"] == 1
+    obs = r["null_obs"].astype(np.float64)
+    bmin, bw, mu = r["h_bmin"], r["h_w"], r["h_phi"]
+    bins = [b for b in range(r["h_cmin"], r["h_imax"] + 1) if obs[b] > 0]
+    assert len(bins) >= 5
+    lo = np.maximum(bmin + np.array(bins) * bw, mu) - mu
+    hi = bmin + (np.array(bins) + 1) * bw - mu
+    n = obs[bins]
+
+    def nll(lam, tau):
+        p = sp.gammaincc(tau, lam * lo) - sp.gammaincc(tau, lam * hi) if not doexpfit else \
+            np.exp(-lam * lo) - np.exp(-lam * hi)
+        return -np.sum(n * np.log(np.maximum(p, 1e-300)))
+
+    assert r["mu"] == mu
+    if doexpfit:
+        best = so.minimize_scalar(lambda t: nll(np.exp(t), 1.0), bracket=(np.log(r["lambda_"]) - 1,
+                                                                         np.log(r["lambda_"]) + 1), tol=1e-12)
+        assert abs(np.exp(best.x) - r["lambda_"]) <= 1e-5 * r["lambda_"]
+    else:
+        x0 = [np.log(r["lambda_"]) + 0.3, np.log(r["tau"]) - 0.3]
+        best = so.minimize(lambda x: nll(np.exp(x[0]), np.exp(x[1])), x0, method="Nelder-Mead",
+                           options={"xatol": 1e-10, "fatol": 1e-12, "maxiter": 20000})
+        assert abs(np.exp(best.x[0]) - r["lambda_"]) <= 1e-4 * r["lambda_"]
+        assert abs(np.exp(best.x[1]) - r["tau"]) <= 1e-4 * r["tau"]
+        assert nll(r["lambda_"], r["tau"]) <= best.fun + 1e-7 * abs(best.fun)
