@@ -376,3 +376,67 @@ def test_tail_fit_maximises_the_binned_likelihood(oracle, covgpu, doexpfit):
         assert abs(np.exp(best.x[0]) - r["lambda_"]) <= 1e-4 * r["lambda_"]
         assert abs(np.exp(best.x[1]) - r["tau"]) <= 1e-4 * r["tau"]
         assert nll(r["lambda_"], r["tau"]) <= best.fun + 1e-7 * abs(best.fun)
+
+
+def test_position_based_weights_match_the_definition(oracle):
+    """Henikoff & Henikoff 1994 position-based weights (R-scape's choice above
+    1,000 sequences, src/R-scape.c:1556): per column, a sequence with residue
+    x scores 1 / (number of residue types in the column x sequences with x);
+    gaps and non-canonical codes score nothing; weights summed over columns
+    and scaled to sum to N."""
+    rng = np.random.default_rng(8)
+    ax = rng.integers(0, 6, size=(37, 29)).astype(np.uint8)   # 4, 5: gap and a degenerate code
+    ax[:, 3] = 4                                               # a column of gaps only
+    N, L = ax.shape
+    ref = np.zeros(N)
+    for c in range(L):
+        col = ax[:, c]
+        types = [x for x in range(4) if np.any(col == x)]
+        for s in range(N):
+            if col[s] < 4:
+                ref[s] += 1.0 / (len(types) * np.sum(col == col[s]))
+    ref *= N / ref.sum()
+    assert np.allclose(oracle.weights_pb(ax), ref, rtol=1e-13, atol=0)
+
+
+def _gsc_by_scipy(ax):
+    """Gerstein, Sonnhammer & Chothia 1994 weights on scipy's UPGMA tree:
+    distance 1 - identities / min(residues) over the columns where both
+    sequences carry a residue; each leaf starts with its branch to its
+    parent, and the branch above an internal node is shared among the leaves
+    below it in proportion to their weights; scaled to sum to N."""
+    from scipy.cluster.hierarchy import linkage
+    N = ax.shape[0]
+    res = ax < 4
+    D = np.zeros((N, N))
+    for a in range(N):
+        for b in range(a + 1, N):
+            m = min(res[a].sum(), res[b].sum())
+            ident = np.sum((ax[a] == ax[b]) & res[a] & res[b])
+            D[a, b] = D[b, a] = 1.0 - ident / m if m > 0 else 1.0
+    Z = linkage(D[np.triu_indices(N, 1)], method="average")
+    leaves, height, w = {k: [k] for k in range(N)}, {k: 0.0 for k in range(N)}, np.zeros(N)
+    for t, (a, b, d, _) in enumerate(Z):
+        a, b, h = int(a), int(b), d / 2.0
+        for ch in (a, b):
+            bl, lv = h - height[ch], leaves[ch]
+            if ch < N:
+                w[ch] += bl
+            elif w[lv].sum() > 0:
+                w[lv] += bl * w[lv] / w[lv].sum()
+            else:
+                w[lv] += bl / len(lv)
+        leaves[N + t], height[N + t] = leaves[a] + leaves[b], h
+    return w * N / w.sum()
+
+
+@pytest.mark.parametrize("seed", [0, 7, 19])
+def test_gsc_weights_on_an_independent_upgma(oracle, seed):
+    """The oracle's GSC weights (R-scape's choice up to 1,000 sequences,
+    src/R-scape.c:1555) against the same rule on scipy's UPGMA."""
+    pytest.importorskip("scipy.cluster.hierarchy")
+    rng = np.random.default_rng(seed)
+    base = rng.integers(0, 4, size=300)
+    ax = np.array([np.where(rng.random(300) < rng.uniform(0.05, 0.5), rng.integers(0, 5, 300), base)
+                   for _ in range(25)]).astype(np.uint8)
+    assert np.allclose(oracle.weights_gsc(ax), _gsc_by_scipy(ax), rtol=1e-12, atol=0)
