@@ -342,3 +342,38 @@ def test_count_schedule_rejects_bad_values(covgpu):
     for bad in (0, -3, 5000, 1000):
         assert lib.covgpu_tile_order(10, bad, order.ctypes.data, None, 0, ctypes.byref(nj)) == 11
     assert lib.covgpu_tile_order(0, 10, order.ctypes.data, None, 0, ctypes.byref(nj)) == 11
+
+
+def test_headers_compile_as_c_and_link(covgpu, tmp_path):
+    """include/covgpu.h and include/rscape_cov.h compile as strict C11 with
+    every warning an error, and a C program links against libcovgpu and runs
+    its host-only calls (no GPU)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi_check.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include "covgpu.h"
+#include "rscape_cov.h"
+int main(void) {
+  covgpu_params p;
+  int order[6], jp[24], nj = 0;
+  covgpu_params_default(&p);
+  if (p.nshuffle != -1 || p.thresh != 0.05) return 2;
+  if (covgpu_tile_order(3, 10, order, jp, 6, &nj) != 0 || nj < 1) return 3;
+  if (covgpu_rscape(NULL, &p, NULL, NULL, 1, NULL, NULL, NULL, 0) != 11) return 4;
+  printf("ok %d\n", nj);
+  return 0;
+}
+""")
+    exe = tmp_path / "abi_check"
+    libdir = os.path.dirname(covgpu.LIBPATH)
+    r = subprocess.run([cc, "-std=c11", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-o", str(exe), "-L", libdir, "-lcovgpu", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), (r.returncode, r.stdout, r.stderr)
