@@ -219,7 +219,8 @@ int  covgpu_rscape_families(covgpu_batch *b, const covgpu_params *p, int nfam, c
 /* the count schedule: families of fewer than simt_below sequences are
  * counted on the SIMT kernel when the tensor counter is asked for (the counts
  * are the same), sb the raster super-block of the tensor count's tile order
- * (defaults 64 and 10); covgpu_batch_autotune times the caller's families
+ * (a square or a band, as in covgpu_autotune; defaults 64 and 10; 11 for a
+ * bad value); covgpu_batch_autotune times the caller's families
  * under every (thr[i], sbs[j]) pair (host wall clock, best of two calls
  * after a warm-up; ms[i * nsb + j]) and keeps the fastest */
 int  covgpu_batch_set_schedule(covgpu_batch *b, int simt_below, int sb);

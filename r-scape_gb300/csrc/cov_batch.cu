@@ -277,13 +277,14 @@ int plan_tree(covgpu_batch* b, const covgpu_family& fam, FamHost& f) {
 
 // the blocked raster order of the tensor count kernel's tiles (as
 // umma_plan's, super-blocks of SB x SB tiles)
+// the grouped count's task order of one family: the single-alignment
+// count's rasters (covgpu_tile_order: squares, or bands of a x b tiles for
+// a schedule value 1000 a + b); the schedule is checked when it is set
 void tile_order(int nT, int SB, std::vector<int>& order) {
-  order.clear();
-  auto tindex = [nT](int I, int J) { return I * nT - I * (I - 1) / 2 + (J - I); };
-  for (int bI = 0; bI < nT; bI += SB)
-    for (int bJ = bI; bJ < nT; bJ += SB)
-      for (int I = bI; I < std::min(nT, bI + SB); I++)
-        for (int J = std::max(I, bJ); J < std::min(nT, bJ + SB); J++) order.push_back(tindex(I, J));
+  order.assign((size_t)nT * (nT + 1) / 2, 0);
+  int nj = 0;
+  if (covgpu_tile_order(nT, SB, order.data(), nullptr, 0, &nj) != 0)
+    covgpu_tile_order(nT, 10, order.data(), nullptr, 0, &nj);
 }
 
 
@@ -1154,7 +1155,8 @@ extern "C" int covgpu_rscape_families(covgpu_batch* b, const covgpu_params* p, i
 // two give the same counts), and sb is the raster super-block of the tensor
 // count's tile order
 extern "C" int covgpu_batch_set_schedule(covgpu_batch* b, int simt_below, int sb) {
-  if (!b || simt_below < 0 || sb < 1) return 11;
+  int probe[1], nj = 0;
+  if (!b || simt_below < 0 || covgpu_tile_order(1, sb, probe, nullptr, 0, &nj) != 0) return 11;
   b->simt_below = simt_below;
   b->sb = sb;
   return 0;
@@ -1175,7 +1177,8 @@ extern "C" int covgpu_batch_autotune(covgpu_batch* b, const covgpu_params* p, in
   int bt = keep_thr, bs = keep_sb;
   for (int i = 0; i < nthr; i++)
     for (int j = 0; j < nsb; j++) {
-      if (thr[i] < 0 || sbs[j] < 1) {
+      int probe[1], nj = 0;
+      if (thr[i] < 0 || covgpu_tile_order(1, sbs[j], probe, nullptr, 0, &nj) != 0) {
         b->simt_below = keep_thr; b->sb = keep_sb;
         return bfail(b, 11, "bad autotune candidate (%d, %d)", thr[i], sbs[j]);
       }

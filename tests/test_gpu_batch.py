@@ -183,7 +183,8 @@ def test_batch_schedules_give_the_same_results(covgpu):
     fl = [dict(ax=s.ax, parent=s.parent, left=s.left, right=s.right) for s in fams]
     b = covgpu.Batch()
     ref = b.rscape(fl, ["GTp", "CHIp"], counter=covgpu.TENSOR, thresh=10.0)
-    for thr, sb in ((0, 4), (1 << 20, 10), (300, 16)):   # all tensor, all SIMT, mixed
+    # all tensor, all SIMT, mixed; square and band rasters
+    for thr, sb in ((0, 4), (1 << 20, 10), (300, 16), (0, 32004), (300, 6003)):
         b.set_schedule(thr, sb)
         got = b.rscape(fl, ["GTp", "CHIp"], counter=covgpu.TENSOR, thresh=10.0)
         for k in range(len(fams)):
