@@ -118,8 +118,8 @@ def test_apc_definition(oracle):
 
 def test_null_preserves_composition(oracle, covgpu):
     """A null alignment keeps the number of sequences and columns, holds only
-    canonical codes and gaps, and every branch replays exactly the
-    substitution counts of its Fitch reconstruction."""
+    canonical codes and gaps, is the same for the same (seed, null index) and
+    differs between null indices."""
     s = covgpu.Synth(40, 60, 1.0, 10, 1, 10, 10, 0.1, seed=7)
     T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
     nm = oracle.null_msa(s.ax, T, 42, 3)
