@@ -440,3 +440,38 @@ def test_gsc_weights_on_an_independent_upgma(oracle, seed):
     ax = np.array([np.where(rng.random(300) < rng.uniform(0.05, 0.5), rng.integers(0, 5, 300), base)
                    for _ in range(25)]).astype(np.uint8)
     assert np.allclose(oracle.weights_gsc(ax), _gsc_by_scipy(ax), rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("fracfit,pmass", [(1.0, 0.0005), (0.3, 0.0005), (1.0, 0.05)])
+def test_tail_mass_and_tail_bins_follow_the_rules(oracle, covgpu, fracfit, pmass):
+    """cov_histogram_pmass (src/covariation.c:2483-2505: walk the non-empty
+    bins down from the top until fracfit of them or pmass of the mass is
+    passed) and the tail by mass (the smallest top set of bins holding at
+    least that mass; its lowest bin is cmin, its lower bound phi), written
+    here from the rules, against the oracle's histogram fields."""
+    s = covgpu.Synth(150, 100, 1.5, 25, 3, 8, 9, 0.08, seed=29, tree_kind=1)
+    w = oracle.weights_pb(s.ax)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    r = oracle.rscape(s.ax, w, T, covtype="GTp", nshuffle=10, pmass=pmass, fracfit=fracfit)
+    obs = [int(x) for x in r["null_obs"]]
+    imin, imax, n = r["h_imin"], r["h_imax"], r["h_n"]
+    assert sum(obs) == n
+    tp = sum(1 for b in range(imin, imax + 1) if obs[b] > 0)
+    c, nfit, want = 0, 0, None
+    for b in range(imax, imin - 1, -1):
+        c += obs[b]
+        if obs[b] > 0:
+            nfit += 1
+            want = c / n
+            if nfit / tp >= fracfit or want >= pmass:
+                break
+    assert r["pmass_used"] == want
+    acc = 0
+    for b in range(imax, imin - 1, -1):
+        acc += obs[b]
+        if acc >= want * n:
+            break
+    assert r["h_cmin"] == max(b, imin)
+    assert r["newmass"] == acc / n
+    assert r["h_phi"] == r["h_bmin"] + r["h_cmin"] * r["h_w"] or \
+        abs(r["h_phi"] - (r["h_bmin"] + r["h_cmin"] * r["h_w"])) <= 1e-12 * abs(r["h_phi"])
