@@ -475,3 +475,17 @@ def test_tail_mass_and_tail_bins_follow_the_rules(oracle, covgpu, fracfit, pmass
     assert r["newmass"] == acc / n
     assert r["h_phi"] == r["h_bmin"] + r["h_cmin"] * r["h_w"] or \
         abs(r["h_phi"] - (r["h_bmin"] + r["h_cmin"] * r["h_w"])) <= 1e-12 * abs(r["h_phi"])
+
+
+def test_histogram_width_from_the_first_null(oracle, covgpu):
+    """calculate_width_histo (src/R-scape.c:1281-1371): the bin width is
+    min(w0, (maxCOV - max(bmin, minCOV)) / hpts) of the first null's scores,
+    0 below tol."""
+    s = covgpu.Synth(120, 90, 1.5, 20, 2, 8, 10, 0.08, seed=31, tree_kind=1)
+    w = oracle.weights_pb(s.ax)
+    T = oracle.TreeArrays(s.parent, s.left, s.right, s.ld, s.rd)
+    for hpts, w0 in ((400, 0.05), (40, 0.05), (400, 1e-4)):
+        r = oracle.rscape(s.ax, w, T, covtype="MIp", nshuffle=3, hpts=hpts, w0=w0)
+        want = min(w0, (r["null_maxCOV"] - max(-10.0, r["null_minCOV"])) / hpts)
+        want = 0.0 if want < 1e-6 else want
+        assert r["w"] == want, (hpts, w0, r["w"], want)
