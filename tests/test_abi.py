@@ -377,3 +377,63 @@ int main(void) {
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.startswith("ok"), (r.returncode, r.stdout, r.stderr)
+
+
+def _c_layouts_match(tmp_path, incdir, header, pairs, cfield=None):
+    """Compile a C program printing sizeof/offsetof of each C structure of
+    pairs [(C type, ctypes class)] and compare with the ctypes layout."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    cfield = cfield or {}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "%s"' % header, "int main(void) {"]
+    for cname, py in pairs:
+        lines.append('  printf("%%s size %%zu\\n", "%s", sizeof(%s));' % (cname, cname))
+        for f in py._fields_:
+            lines.append('  printf("%%s %s %%zu\\n", "%s", offsetof(%s, %s));'
+                         % (f[0], cname, cname, cfield.get((cname, f[0]), f[0])))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / ("layout_%s.c" % header.replace(".", "_"))
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / ("layout_%s" % header.replace(".", "_"))
+    r = subprocess.run([cc, "-std=c11", "-D_DEFAULT_SOURCE", "-I", incdir, str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, timeout=60).stdout.splitlines():
+        name, key, val = line.rsplit(" ", 2)
+        got[(name, key)] = int(val)
+    for cname, py in pairs:
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f in py._fields_:
+            assert got[(cname, f[0])] == getattr(py, f[0]).offset, (cname, f[0])
+
+
+def test_ctypes_mirrors_match_the_c_layouts(covgpu, tmp_path):
+    """The ctypes structures of rscape_abi.py (the drop-in's Python binding,
+    used by the tests and the benchmark) have the sizes and field offsets of
+    the C structures in include/rscape_cov.h, as gcc lays them out."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("rscape_abi_t", os.path.join(ROOT, "r-scape_gb300", "rscape_abi.py"))
+    abi = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(abi)
+    pairs = [("ESL_ALPHABET", abi.Alphabet), ("ESL_MSA", abi.Msa), ("ESL_DMATRIX", abi.DMatrix),
+             ("ESL_HISTOGRAM", abi.Hist), ("struct mutual_s", abi.Mutual), ("RANKLIST", abi.RankList),
+             ("HIT", abi.Hit), ("HITLIST", abi.HitList), ("THRESH", abi.Thresh), ("ESL_RANDOMNESS", abi.Rand),
+             ("CNT", abi.Cnt), ("CLIST", abi.Clist), ("struct data_s", abi.Data)]
+    _c_layouts_match(tmp_path, os.path.join(ROOT, "include"), "rscape_cov.h", pairs,
+                     {("struct data_s", "lambda_"): "lambda"})   # a Python keyword, renamed in the mirror
+
+
+def test_covgpu_and_oracle_ctypes_mirrors_match(covgpu, oracle, tmp_path):
+    """covgpu.py's mirrors of include/covgpu.h and oracle.py's mirrors of
+    oracle/rscape_oracle.h have the C layouts."""
+    _c_layouts_match(tmp_path, os.path.join(ROOT, "include"), "covgpu.h",
+                     [("covgpu_params", covgpu.Params), ("covgpu_result", covgpu.Result), ("covgpu_hit", covgpu.Hit),
+                      ("covgpu_family", covgpu.Family)],
+                     {("covgpu_result", "lambda_"): "lambda"})
+    _c_layouts_match(tmp_path, os.path.join(ROOT, "oracle"), "rscape_oracle.h",
+                     [("orc_tree_t", oracle.Tree), ("orc_params_t", oracle.Params), ("orc_result_t", oracle.Result)],
+                     {("orc_result_t", "lambda_"): "lambda"})
